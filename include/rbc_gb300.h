@@ -1,0 +1,164 @@
+/*
+ * rbc_gb300.h -- C ABI of the GB300 Random Ball Cover k-NN engine.
+ *
+ * Plain C types only (pointers, sizes, status codes) so any FFI can bind it.
+ * Every function returns RBC_OK (0) or an RBC_ERR_* code; the message of the
+ * last failure on the calling thread is rbc_last_error().  Device pointers
+ * (prefix d) must be 16-byte aligned; `stream` is a cudaStream_t passed as
+ * void* (NULL = legacy default stream).  Calls on one index handle must not
+ * overlap: use one handle per host thread or serialise the calls.
+ *
+ * The entry points replace the reference's interface as follows (reference
+ * file:line in brackets):
+ *   rbc_build / rbc_build_host     buildRBC + setupReps   [rbc.h:11, rbc.cu:126-229]
+ *   rbc_query / rbc_query_host     kqueryRBC / queryRBC   [rbc.h:12-13, rbc.cu:19-123]
+ *   rbc_destroy                    destroyRBC             [rbc.h:14, rbc.cu:363-368]
+ *   rbc_brute_knn                  bruteK / bruteSearch   [brute.h:11-13, brute.cu:43-88]
+ *   rbc_brute_range_count          bruteRangeCount        [brute.h:10, brute.cu:19-40]
+ *   rbc_read_matrix_bin/_text      readData / readDataText [driver.cu:201-245]
+ *   rbc_write_neighbors_bin/_text  writeNeighbs           [driver.cu:352-393]
+ * The reference's own C++ names and by-value struct signatures are exported
+ * too, from rbc.h / brute.h / utils.h in this directory.
+ */
+#ifndef RBC_GB300_H
+#define RBC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define RBC_OK 0
+#define RBC_ERR_INVALID 1     /* bad argument (sizes, k, pointers, reps)      */
+#define RBC_ERR_CUDA 2        /* a CUDA runtime call or kernel launch failed  */
+#define RBC_ERR_NOMEM 3       /* device or host allocation failed             */
+#define RBC_ERR_ITER_LIMIT 4  /* a bounded device wait ran out                */
+#define RBC_ERR_UNSUPPORTED 5 /* shape outside what this build handles        */
+#define RBC_ERR_IO 6          /* file open/read/write failure                 */
+
+/* ---- metrics: the per-coordinate term of defs.h:20-21, summed in order ---- */
+#define RBC_L2 0 /* sum of (q-x)^2: squared Euclidean, never square-rooted */
+#define RBC_L1 1 /* sum of |q-x|                                           */
+
+#define RBC_KMAX 32 /* neighbours per query held by the engine (defs.h:9) */
+
+/* ---- build flags ---- */
+#define RBC_BUILD_PARTITION 1u /* nearest-representative lists for exact search */
+#define RBC_BUILD_ONESHOT 2u   /* the reference's lists: s nearest points per rep */
+
+/* ---- query modes ---- */
+#define RBC_QUERY_EXACT 0u   /* exact k-NN: triangle-inequality pruning of lists */
+#define RBC_QUERY_ONESHOT 1u /* reference one-shot: only the nearest rep's list  */
+
+/* ---- synthetic data kinds (counter-based, identical bits on host and GPU) ---- */
+#define RBC_SYNTH_UNIFORM 0   /* i.i.d. U[0,1)                                     */
+#define RBC_SYNTH_MIXTURE 1   /* isotropic Gaussian mixture, means U[0,1)^d        */
+#define RBC_SYNTH_GEOMETRIC 2 /* integer geometric(p=1/21), mean 20, clipped 255   */
+
+typedef struct rbc_index rbc_index; /* opaque handle */
+
+typedef struct {
+  uint32_t num_reps;       /* representatives; 1 <= num_reps <= n            */
+  uint32_t s;              /* one-shot list length (RBC_BUILD_ONESHOT)        */
+  int metric;              /* RBC_L2 or RBC_L1                                */
+  uint32_t flags;          /* RBC_BUILD_*; 0 means RBC_BUILD_PARTITION        */
+  uint64_t seed;           /* representative sampling seed                    */
+  const uint32_t *rep_ids; /* optional host array of num_reps distinct ids    */
+} rbc_build_params;
+
+typedef struct {
+  uint64_t n;
+  uint32_t d, ld, num_reps, s;
+  int metric;
+  uint32_t flags;
+  uint64_t min_list, max_list; /* partition list sizes                  */
+  uint64_t device_bytes;       /* device memory held by the index        */
+} rbc_index_info;
+
+typedef struct {               /* work done by the last rbc_query on an index */
+  uint64_t queries;
+  uint64_t rep_pairs;          /* query-to-representative distances           */
+  uint64_t lists_probed;       /* (query, list) pairs searched                */
+  uint64_t point_pairs;        /* (query, point) distances computed in lists  */
+} rbc_query_stats;
+
+const char *rbc_status_string(int status);
+const char *rbc_last_error(void);
+int rbc_version(void);
+
+/* Build an index over n rows of d floats at dX (row stride ldx >= d floats).
+ * The index keeps its own reordered device copy; dX may be freed after. */
+int rbc_build(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *params,
+              void *stream, rbc_index **out);
+/* Same from host memory (the copy to the device is part of the call). */
+int rbc_build_host(const float *hX, uint64_t n, uint32_t d, uint32_t ldx,
+                   const rbc_build_params *params, rbc_index **out);
+int rbc_destroy(rbc_index *index);
+
+int rbc_get_info(const rbc_index *index, rbc_index_info *info);
+/* Copies of the index structure to host memory (for tests and tooling). */
+int rbc_get_reps(const rbc_index *index, uint32_t *h_rep_ids /* num_reps */);
+int rbc_get_partition(const rbc_index *index, uint64_t *h_offsets /* num_reps+1 */,
+                      uint32_t *h_members /* n */, float *h_radius /* num_reps */);
+int rbc_get_oneshot(const rbc_index *index, uint32_t *h_lists /* num_reps x s */,
+                    uint32_t *h_counts /* num_reps */);
+
+/* k-NN of m queries (rows of d floats, stride ldq).  Results are sorted by
+ * (distance, id); row i of dIds/dDists (stride ldo >= k) holds query i.
+ * Missing neighbours are (FLT_MAX, 0xFFFFFFFF).  1 <= k <= RBC_KMAX. */
+int rbc_query(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
+              uint32_t *dIds, float *dDists, uint32_t ldo, void *stream);
+int rbc_query_host(rbc_index *index, const float *hQ, uint64_t m, uint32_t ldq, uint32_t k,
+                   uint32_t mode, uint32_t *hIds, float *hDists, uint32_t ldo);
+int rbc_get_query_stats(const rbc_index *index, rbc_query_stats *stats);
+
+/* Benchmark instrumentation (no counterpart in the reference): with profiling
+ * on, every list-search kernel launch of a query call is bracketed by CUDA
+ * events on the call's stream and its duration is summed. */
+typedef struct {
+  uint64_t search_launches; /* list-search kernel launches in the last query call */
+  double search_ms;         /* their summed duration in milliseconds            */
+} rbc_profile;
+int rbc_set_profiling(rbc_index *index, int enable);
+int rbc_get_profile(const rbc_index *index, rbc_profile *profile);
+/* Number of kernels this library has launched in this process. */
+uint64_t rbc_kernel_launches(void);
+
+/* Brute-force exact k-NN of every query over every database row. */
+int rbc_brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m,
+                  uint32_t ldq, uint32_t d, uint32_t k, int metric, uint32_t *dIds, float *dDists,
+                  uint32_t ldo, void *stream);
+/* counts[i] = number of database rows with distance strictly below ranges[i]. */
+int rbc_brute_range_count(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m,
+                          uint32_t ldq, uint32_t d, int metric, const float *dRanges,
+                          uint32_t *dCounts, void *stream);
+
+/* Rows [r0, r0+rows) of a synthetic matrix into dOut (stride ld, padding
+ * columns zeroed).  stream_id separates independent draws (database 0,
+ * queries 1, ...).  ncomp/sigma_* apply to RBC_SYNTH_MIXTURE. */
+int rbc_synth(int kind, uint64_t seed, uint64_t stream_id, uint64_t r0, uint64_t rows, uint32_t d,
+              uint32_t ld, float *dOut, uint32_t ncomp, float sigma_lo, float sigma_hi,
+              void *stream);
+
+/* Headerless float32 row-major files (driver.cu:201-221): rows x cols values
+ * read into a buffer of stride ld; text files hold whitespace-separated
+ * numbers (driver.cu:224-245). */
+int rbc_read_matrix_bin(const char *path, float *hBuf, uint64_t rows, uint32_t cols, uint32_t ld);
+int rbc_read_matrix_text(const char *path, float *hBuf, uint64_t rows, uint32_t cols, uint32_t ld);
+int rbc_write_matrix_bin(const char *path, const float *hBuf, uint64_t rows, uint32_t cols,
+                         uint32_t ld);
+/* Neighbour output (driver.cu:352-393): all m rows of k ids (uint32), then
+ * all m rows of k distances (float32); text writes the same order. */
+int rbc_write_neighbors_bin(const char *path, const uint32_t *hIds, const float *hDists, uint64_t m,
+                            uint32_t k, uint32_t ld);
+int rbc_write_neighbors_text(const char *path, const uint32_t *hIds, const float *hDists,
+                             uint64_t m, uint32_t k, uint32_t ld);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RBC_GB300_H */

@@ -1,0 +1,667 @@
+// engine.cu -- host orchestration of build, query and brute force, and the
+// C ABI of include/rbc_gb300.h.
+//
+// Everything runs on the caller's stream with stream-ordered temporaries
+// (cudaMallocAsync), so a call adds no device-wide synchronisation; the
+// public calls wait for their stream once at the end to report the device
+// error word.  There is no CPU fallback: if a kernel cannot run, the call
+// fails with RBC_ERR_CUDA.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <unordered_map>
+
+#include "engine.cuh"
+#include "rbc_common.cuh"
+
+namespace rbc {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+int fail(int code, const std::string &msg) {
+  set_error(msg);
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? RBC_ERR_NOMEM : RBC_ERR_CUDA;
+}
+
+#define CK(expr)                                        \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #expr); \
+  } while (0)
+#define TRY(expr)                      \
+  do {                                 \
+    int rc_ = (expr);                  \
+    if (rc_ != RBC_OK) return rc_;     \
+  } while (0)
+
+namespace {
+
+constexpr uint32_t kDefaultProbes = 1;  // lists searched before planning (the one-shot plan)
+
+void pool_setup() {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done[dev] = true;
+}
+
+uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// nr distinct ids of [0, n): a partial Fisher-Yates shuffle over a virtual
+// identity array (O(nr) memory), driven by a seeded 64-bit counter hash.
+// Plays the role of setupReps/subRandPerm (rbc.cu:212-229, utils.cu:17-37),
+// whose seed is the wall clock; here the seed is an argument.
+void sample_reps(uint64_t n, uint32_t nr, uint64_t seed, std::vector<uint32_t> &out) {
+  std::unordered_map<uint64_t, uint32_t> moved;
+  moved.reserve(nr * 2);
+  auto get = [&](uint64_t i) {
+    auto it = moved.find(i);
+    return it == moved.end() ? (uint32_t)i : it->second;
+  };
+  const uint64_t key = mix64(seed ^ 0xA0761D6478BD642Full);
+  out.resize(nr);
+  for (uint32_t i = 0; i < nr; i++) {
+    uint64_t j = i + mix64(key + i) % (n - i);
+    uint32_t vi = get(i), vj = get(j);
+    moved[j] = vi;
+    out[i] = vj;
+  }
+}
+
+int check_dims(uint32_t d, uint32_t ld, const char *what) {
+  if (d == 0) return fail(RBC_ERR_INVALID, std::string(what) + ": d must be >= 1");
+  if (ld < d) return fail(RBC_ERR_INVALID, std::string(what) + ": leading dimension smaller than d");
+  if (pad4(d) > kMaxDim)
+    return fail(RBC_ERR_UNSUPPORTED, std::string(what) + ": d larger than " + std::to_string(kMaxDim));
+  return RBC_OK;
+}
+
+// Per-call buffers of one query batch.
+struct QueryBufs {
+  DevBuf Qp, Dqr, probe, probed, res_d, res_i, tau, lock, cnt, start, cursor, tcnt, tstart, pair_q,
+      pair_thr, items, ctl, scan_tmp;
+};
+
+// Build the list-major plan for one mode and run the search over it.
+int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
+                    const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
+                    int grid, unsigned long long *stats, cudaStream_t s) {
+  const uint32_t nr = idx->nr, qtile = (uint32_t)search_query_tile(idx->dp);
+  uint32_t *ctl = b.ctl.as<uint32_t>();  // [0] work, [1] nitems, [2] err
+  PlanArgs a{};
+  a.Dqr = b.Dqr.as<float>();
+  a.radius = radius;
+  a.offsets = offsets;
+  a.probe = b.probe.as<uint32_t>();
+  a.probed = b.probed.as<float>();
+  a.tau = b.tau.as<uint32_t>();
+  a.m = m;
+  a.nr = nr;
+  a.P = P;
+  a.metric = (uint32_t)idx->metric;
+  a.qtile = qtile;
+  a.gamma = (double)(idx->dp + 8) * 1.1920928955078125e-07;
+  a.list_cursor = b.cursor.as<uint32_t>();
+  a.pair_q = b.pair_q.as<uint32_t>();
+  a.pair_thr = b.pair_thr.as<float>();
+  uint32_t *cnt = b.cnt.as<uint32_t>(), *start = b.start.as<uint32_t>();
+  uint32_t *tcnt = b.tcnt.as<uint32_t>(), *tstart = b.tstart.as<uint32_t>();
+
+  CK(cudaMemsetAsync(cnt, 0, (nr + 1) * sizeof(uint32_t), s));
+  CK(cudaMemsetAsync(b.cursor.p, 0, (nr + 1) * sizeof(uint32_t), s));
+  a.list_cnt = cnt;
+  a.phase = 0;
+  CK(launch_plan_pass(a, mode, s));
+  CK(launch_exclusive_scan(cnt, start, nr + 1, b.scan_tmp.p, ctl + 2, s));
+  a.list_cnt = start;
+  a.phase = 1;
+  CK(launch_plan_pass(a, mode, s));
+  CK(launch_tiles_per_list(cnt, nr, qtile, tcnt, s));
+  CK(launch_exclusive_scan(tcnt, tstart, nr + 1, b.scan_tmp.p, ctl + 2, s));
+  CK(launch_plan_items(cnt, start, tstart, offsets, nr, qtile, b.items.as<SearchItem>(), ctl + 1, s));
+
+  SearchArgs sa{};
+  sa.X = X;
+  sa.pid = pid;
+  sa.Q = b.Qp.as<float>();
+  sa.qidx = b.pair_q.as<uint32_t>();
+  sa.qthr = mode == 0 ? nullptr : b.pair_thr.as<float>();
+  sa.items = b.items.as<SearchItem>();
+  sa.nitems = ctl + 1;
+  sa.work = ctl;
+  sa.res_d = b.res_d.as<float>();
+  sa.res_i = b.res_i.as<uint32_t>();
+  sa.tau = b.tau.as<uint32_t>();
+  sa.lock = b.lock.as<uint32_t>();
+  sa.err = ctl + 2;
+  sa.stats = stats;
+  sa.ld = idx->ld;
+  sa.dp = idx->dp;
+  sa.k = k;
+  CK(cudaMemsetAsync(ctl, 0, sizeof(uint32_t), s));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (idx->profile) {
+    while (idx->ev_pool.size() < idx->ev_used + 2) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      idx->ev_pool.push_back(e);
+    }
+    e0 = idx->ev_pool[idx->ev_used++];
+    e1 = idx->ev_pool[idx->ev_used++];
+    CK(cudaEventRecord(e0, s));
+  }
+  CK(launch_search(idx->metric, sa, grid, s));
+  if (e1) CK(cudaEventRecord(e1, s));
+  return RBC_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ build
+int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *p,
+                cudaStream_t s, rbc_index **out) {
+  if (!out) return fail(RBC_ERR_INVALID, "rbc_build: out is NULL");
+  *out = nullptr;
+  if (!p) return fail(RBC_ERR_INVALID, "rbc_build: params is NULL");
+  if (!dX) return fail(RBC_ERR_INVALID, "rbc_build: X is NULL");
+  TRY(check_dims(d, ldx, "rbc_build"));
+  if (n == 0 || n >= 0xFFFFFFFFull) return fail(RBC_ERR_INVALID, "rbc_build: n must be in [1, 2^32-1)");
+  if (p->metric != RBC_L2 && p->metric != RBC_L1) return fail(RBC_ERR_INVALID, "rbc_build: unknown metric");
+  if (p->num_reps == 0 || p->num_reps > n)
+    return fail(RBC_ERR_INVALID, "rbc_build: num_reps must be in [1, n]");
+  if (p->num_reps > 32768) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: num_reps above 32768");
+  uint32_t flags = p->flags ? p->flags : RBC_BUILD_PARTITION;
+  if ((flags & RBC_BUILD_ONESHOT) && p->s == 0) return fail(RBC_ERR_INVALID, "rbc_build: s must be >= 1");
+  pool_setup();
+
+  rbc_index *idx = new rbc_index();
+  struct Guard {
+    rbc_index *&i;
+    ~Guard() {
+      if (i) rbc_destroy(i);
+    }
+  } guard{idx};
+  CK(cudaGetDevice(&idx->device));
+  idx->n = n;
+  idx->d = d;
+  idx->ld = pad16(d);
+  idx->dp = pad4(d);
+  idx->metric = p->metric;
+  idx->flags = flags;
+  idx->nr = p->num_reps;
+  const uint32_t nr = idx->nr, ld = idx->ld;
+
+  // representatives
+  if (p->rep_ids) {
+    idx->rep_ids.assign(p->rep_ids, p->rep_ids + nr);
+    std::vector<uint32_t> sorted = idx->rep_ids;
+    std::sort(sorted.begin(), sorted.end());
+    if (sorted.back() >= n) return fail(RBC_ERR_INVALID, "rbc_build: rep id out of range");
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+      return fail(RBC_ERR_INVALID, "rbc_build: rep ids are not distinct");
+  } else {
+    sample_reps(n, nr, p->seed, idx->rep_ids);
+  }
+
+  // padded copy of the input (zero columns past d, zero rows up to pad16(n))
+  idx->xi_rows = pad16((uint32_t)std::min<uint64_t>(n, 0xFFFFFFF0ull));
+  if (idx->xi_rows < n) idx->xi_rows = n;
+  DevBuf xi_tmp;
+  float *Xi = nullptr;
+  size_t xi_bytes = (size_t)idx->xi_rows * ld * 4;
+  if (flags & kBuildKeepInput) {
+    CK(cudaMalloc(&idx->Xi, xi_bytes));
+    Xi = idx->Xi;
+    idx->device_bytes += xi_bytes;
+  } else {
+    CK(xi_tmp.alloc(xi_bytes, s));
+    Xi = xi_tmp.as<float>();
+  }
+  CK(cudaMemsetAsync(Xi + n * ld, 0, (idx->xi_rows - n) * ld * 4, s));
+  CK(launch_pad_rows(dX, ldx, Xi, ld, n, d, s));
+
+  DevBuf rid;
+  CK(rid.alloc(nr * 4, s));
+  CK(cudaMemcpyAsync(rid.p, idx->rep_ids.data(), nr * 4, cudaMemcpyHostToDevice, s));
+  size_t r_bytes = (size_t)pad16(nr) * ld * 4;
+  CK(cudaMalloc(&idx->R, r_bytes));
+  idx->device_bytes += r_bytes;
+  CK(cudaMemsetAsync(idx->R, 0, r_bytes, s));
+  CK(launch_gather_rows(Xi, ld, rid.as<uint32_t>(), nr, idx->R, s));
+
+  if (flags & RBC_BUILD_PARTITION) {
+    DevBuf owner, odist, hist, hscan, tmp;
+    const uint32_t ntiles = (uint32_t)((n + owner_tile_rows() - 1) / owner_tile_rows());
+    const uint64_t hn = (uint64_t)nr * ntiles;
+    CK(owner.alloc(n * 4, s));
+    CK(odist.alloc(n * 4, s));
+    CK(hist.alloc(hn * 4, s));
+    CK(hscan.alloc(hn * 4, s));
+    CK(tmp.alloc(scan_temp_bytes(hn), s));
+    CK(cudaMalloc(&idx->perm, n * 4));
+    CK(cudaMalloc(&idx->offsets, (nr + 1) * 8));
+    CK(cudaMalloc(&idx->radius, nr * 4));
+    CK(cudaMalloc(&idx->Xp, (size_t)n * ld * 4));
+    idx->device_bytes += n * 4 + (nr + 1) * 8 + nr * 4 + (size_t)n * ld * 4;
+    CK(launch_argmin(idx->metric, Xi, n, idx->R, nr, ld, idx->dp, owner.as<uint32_t>(), odist.as<float>(), s));
+    CK(launch_owner_hist(owner.as<uint32_t>(), n, nr, hist.as<uint32_t>(), ntiles, s));
+    CK(launch_exclusive_scan(hist.as<uint32_t>(), hscan.as<uint32_t>(), hn, tmp.p, nullptr, s));
+    CK(launch_owner_scatter(owner.as<uint32_t>(), n, nr, hscan.as<uint32_t>(), ntiles,
+                            idx->perm, s));
+    CK(launch_list_offsets(hscan.as<uint32_t>(), nr, ntiles, n, idx->offsets, s));
+    CK(launch_list_radius(idx->offsets, idx->perm, odist.as<float>(), nr, idx->radius, s));
+    CK(launch_gather_rows(Xi, ld, idx->perm, n, idx->Xp, s));
+    std::vector<uint64_t> off(nr + 1);
+    CK(cudaMemcpyAsync(off.data(), idx->offsets, (nr + 1) * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    idx->min_list = UINT64_MAX;
+    idx->max_list = 0;
+    for (uint32_t r = 0; r < nr; r++) {
+      uint64_t c = off[r + 1] - off[r];
+      idx->min_list = std::min(idx->min_list, c);
+      idx->max_list = std::max(idx->max_list, c);
+    }
+  }
+
+  if (flags & RBC_BUILD_ONESHOT) {
+    const uint32_t s_eff = (uint32_t)std::min<uint64_t>(p->s, n);
+    idx->s = s_eff;
+    idx->lds = pad16(p->s);
+    size_t lists_bytes = (size_t)pad16(nr) * idx->lds * 4;
+    const uint64_t total = (uint64_t)nr * s_eff;
+    CK(cudaMalloc(&idx->os_lists, lists_bytes));
+    CK(cudaMemsetAsync(idx->os_lists, 0, lists_bytes, s));
+    CK(cudaMalloc(&idx->os_counts, nr * 4));
+    CK(cudaMalloc(&idx->os_offsets, (nr + 1) * 8));
+    CK(cudaMalloc(&idx->os_ids, total * 4));
+    CK(cudaMalloc(&idx->Xo, total * ld * 4));
+    idx->device_bytes += lists_bytes + nr * 4 + (nr + 1) * 8 + total * 4 + total * ld * 4;
+    // distance block per group of representatives, bounded to ~4 GiB
+    const uint64_t ldD = (n + 3) / 4 * 4;
+    uint64_t rows_per = std::max<uint64_t>(1, (4ull << 30) / (ldD * 4));
+    rows_per = std::min<uint64_t>(rows_per, nr);
+    DevBuf Dbuf, thr, need;
+    CK(Dbuf.alloc(rows_per * ldD * 4, s));
+    CK(thr.alloc(nr * 4, s));
+    CK(need.alloc(nr * 4, s));
+    for (uint64_t r0 = 0; r0 < nr; r0 += rows_per) {
+      uint32_t rows = (uint32_t)std::min<uint64_t>(rows_per, nr - r0);
+      CK(launch_dense_dist(idx->metric, idx->R + r0 * ld, rows, Xi, n, ld, idx->dp, Dbuf.as<float>(), ldD, s));
+      CK(launch_row_select(Dbuf.as<float>(), ldD, rows, n, s_eff, thr.as<uint32_t>() + r0,
+                           need.as<uint32_t>() + r0, s));
+      CK(launch_row_compact(Dbuf.as<float>(), ldD, rows, n, thr.as<uint32_t>() + r0, need.as<uint32_t>() + r0,
+                            idx->os_lists + r0 * idx->lds, idx->lds, idx->os_counts + r0, s));
+    }
+    // every list holds exactly s_eff ids: list r is rows [r s_eff, (r+1) s_eff) of Xo
+    std::vector<uint64_t> off(nr + 1);
+    for (uint32_t r = 0; r <= nr; r++) off[r] = (uint64_t)r * s_eff;
+    CK(cudaMemcpyAsync(idx->os_offsets, off.data(), (nr + 1) * 8, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpy2DAsync(idx->os_ids, (size_t)s_eff * 4, idx->os_lists, (size_t)idx->lds * 4, (size_t)s_eff * 4,
+                         nr, cudaMemcpyDeviceToDevice, s));
+    CK(launch_gather_rows(Xi, ld, idx->os_ids, total, idx->Xo, s));
+    CK(cudaStreamSynchronize(s));  // off[] is a host array
+  }
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  *out = idx;
+  idx = nullptr;
+  return RBC_OK;
+}
+
+// ------------------------------------------------------------------ query
+// Exact mode: nearest-rep probe round, then the pruned round over every other
+// list (plan.cu).  One-shot mode: the probe round alone over the one-shot
+// lists, which is the reference's kqueryRBC algorithm (rbc.cu:72-123).
+int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
+                uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s) {
+  if (!idx) return fail(RBC_ERR_INVALID, "rbc_query: index is NULL");
+  if (k < 1 || k > (uint32_t)kListWidth) return fail(RBC_ERR_INVALID, "rbc_query: k must be in [1, 32]");
+  if (ldo < k) return fail(RBC_ERR_INVALID, "rbc_query: ldo < k");
+  if (ldq < idx->d) return fail(RBC_ERR_INVALID, "rbc_query: ldq < d");
+  if (m == 0) return RBC_OK;
+  if (!dQ || (!dIds && !dDists)) return fail(RBC_ERR_INVALID, "rbc_query: NULL buffer");
+  if (m >= 0xFFFFFFFFull) return fail(RBC_ERR_INVALID, "rbc_query: m must be below 2^32-1");
+  const bool nosync = (mode & kQueryNoSync) != 0;
+  const uint32_t base = mode & 0xFFu;
+  const float *X;
+  const uint32_t *pid;
+  const uint64_t *offsets;
+  if (base == RBC_QUERY_EXACT) {
+    if (!(idx->flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_INVALID, "rbc_query: index has no partition lists");
+    X = idx->Xp;
+    pid = idx->perm;
+    offsets = idx->offsets;
+  } else if (base == RBC_QUERY_ONESHOT) {
+    if (!(idx->flags & RBC_BUILD_ONESHOT)) return fail(RBC_ERR_INVALID, "rbc_query: index has no one-shot lists");
+    X = idx->Xo;
+    pid = idx->os_ids;
+    offsets = idx->os_offsets;
+  } else {
+    return fail(RBC_ERR_INVALID, "rbc_query: unknown mode");
+  }
+  pool_setup();
+  const uint32_t nr = idx->nr, ld = idx->ld;
+  const uint32_t P = std::min(kDefaultProbes, nr);
+  const uint32_t qtile = (uint32_t)search_query_tile(idx->dp);
+  const int grid = search_grid(idx->metric, idx->dp);
+  // batch so the m x nr plan arrays stay near 2^27 entries
+  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
+  QueryBufs b;
+  const uint64_t pair_cap = mb * nr;
+  const uint64_t item_cap = pair_cap / qtile + nr + 1;
+  CK(b.Qp.alloc(mb * ld * 4, s));
+  CK(b.Dqr.alloc(mb * nr * 4, s));
+  CK(b.probe.alloc(mb * P * 4, s));
+  CK(b.probed.alloc(mb * P * 4, s));
+  CK(b.res_d.alloc(mb * kListWidth * 4, s));
+  CK(b.res_i.alloc(mb * kListWidth * 4, s));
+  CK(b.tau.alloc(mb * 4, s));
+  CK(b.lock.alloc(mb * 4, s));
+  CK(b.cnt.alloc((nr + 1) * 4, s));
+  CK(b.start.alloc((nr + 1) * 4, s));
+  CK(b.cursor.alloc((nr + 1) * 4, s));
+  CK(b.tcnt.alloc((nr + 1) * 4, s));
+  CK(b.tstart.alloc((nr + 1) * 4, s));
+  CK(b.pair_q.alloc(pair_cap * 4, s));
+  CK(b.pair_thr.alloc(pair_cap * 4, s));
+  CK(b.items.alloc(item_cap * sizeof(SearchItem), s));
+  CK(b.ctl.alloc(64, s));
+  CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
+  DevBuf stats;
+  CK(stats.alloc(2 * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(stats.p, 0, 2 * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
+  idx->ev_used = 0;
+  for (uint64_t b0 = 0; b0 < m; b0 += mb) {
+    const uint64_t mq = std::min(mb, m - b0);
+    CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
+    CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
+    CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+    CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
+                           b.lock.as<uint32_t>(), mq, s));
+    TRY(plan_and_search(idx, b, mq, P, k, 0, X, pid, offsets, idx->radius, grid, stats.as<unsigned long long>(), s));
+    if (base == RBC_QUERY_EXACT)
+      TRY(plan_and_search(idx, b, mq, P, k, 1, X, pid, offsets, idx->radius, grid, stats.as<unsigned long long>(), s));
+    CK(launch_write_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), mq, k, dIds ? dIds + b0 * ldo : nullptr,
+                            dDists ? dDists + b0 * ldo : nullptr, ldo, s));
+  }
+  idx->stats.queries = m;
+  idx->stats.rep_pairs = m * nr;
+  if (!nosync) {
+    unsigned long long st[2] = {0, 0};
+    uint32_t ctl[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(st, stats.p, sizeof(st), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctl, b.ctl.p, sizeof(ctl), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    idx->stats.point_pairs = st[0];
+    idx->stats.lists_probed = st[1];
+    if (ctl[2]) return fail((int)ctl[2], "rbc_query: a bounded device wait ran out");
+    if (idx->profile) {
+      idx->prof.search_launches = idx->ev_used / 2;
+      idx->prof.search_ms = 0;
+      for (size_t i = 0; i + 1 < idx->ev_used; i += 2) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, idx->ev_pool[i], idx->ev_pool[i + 1]));
+        idx->prof.search_ms += ms;
+      }
+    }
+  }
+  return RBC_OK;
+}
+
+// ------------------------------------------------------------------ brute force
+// One search over the whole database split into chunks (bruteK / bruteSearch,
+// brute.cu:43-88): every (chunk, query tile) pair is a work item.
+int brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,
+              uint32_t k, int metric, uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s) {
+  TRY(check_dims(d, std::min(ldx, ldq), "rbc_brute_knn"));
+  if (k < 1 || k > (uint32_t)kListWidth) return fail(RBC_ERR_INVALID, "rbc_brute_knn: k must be in [1, 32]");
+  if (ldo < k) return fail(RBC_ERR_INVALID, "rbc_brute_knn: ldo < k");
+  if (metric != RBC_L2 && metric != RBC_L1) return fail(RBC_ERR_INVALID, "rbc_brute_knn: unknown metric");
+  if (m == 0) return RBC_OK;
+  if (!dQ || (!dIds && !dDists) || (n && !dX)) return fail(RBC_ERR_INVALID, "rbc_brute_knn: NULL buffer");
+  if (n >= 0xFFFFFFFFull || m >= 0xFFFFFFFFull) return fail(RBC_ERR_INVALID, "rbc_brute_knn: n, m must be below 2^32-1");
+  pool_setup();
+  const uint32_t ld = pad16(d), dp = pad4(d);
+  const uint32_t qtile = (uint32_t)search_query_tile(dp);
+  const int grid = search_grid(metric, dp);
+  DevBuf Xp, Qp, res_d, res_i, tau, lock, qidx, items, ctl;
+  CK(Xp.alloc(std::max<uint64_t>(n, 1) * ld * 4, s));
+  CK(Qp.alloc(m * ld * 4, s));
+  CK(res_d.alloc(m * kListWidth * 4, s));
+  CK(res_i.alloc(m * kListWidth * 4, s));
+  CK(tau.alloc(m * 4, s));
+  CK(lock.alloc(m * 4, s));
+  CK(qidx.alloc(m * 4, s));
+  CK(ctl.alloc(64, s));
+  CK(cudaMemsetAsync(ctl.p, 0, 64, s));
+  CK(launch_pad_rows(dX, ldx, Xp.as<float>(), ld, n, d, s));
+  CK(launch_pad_rows(dQ, ldq, Qp.as<float>(), ld, m, d, s));
+  CK(launch_init_results(res_d.as<float>(), res_i.as<uint32_t>(), tau.as<uint32_t>(), lock.as<uint32_t>(), m, s));
+  const uint64_t qtiles = (m + qtile - 1) / qtile;
+  uint64_t nchunks = std::max<uint64_t>(1, (4ull * grid + qtiles - 1) / qtiles);
+  nchunks = std::min<uint64_t>(nchunks, std::max<uint64_t>(1, n / 256));
+  uint32_t chunk = (uint32_t)(((n + nchunks - 1) / nchunks + 31) / 32 * 32);
+  if (chunk == 0) chunk = 32;
+  nchunks = (n + chunk - 1) / chunk;
+  const uint64_t nitems = nchunks * qtiles;
+  CK(items.alloc(std::max<uint64_t>(nitems, 1) * sizeof(SearchItem), s));
+  CK(launch_brute_items(items.as<SearchItem>(), ctl.as<uint32_t>() + 1, qidx.as<uint32_t>(), n, chunk, m, qtile, s));
+  SearchArgs sa{};
+  sa.X = Xp.as<float>();
+  sa.pid = nullptr;
+  sa.Q = Qp.as<float>();
+  sa.qidx = qidx.as<uint32_t>();
+  sa.qthr = nullptr;
+  sa.items = items.as<SearchItem>();
+  sa.nitems = ctl.as<uint32_t>() + 1;
+  sa.work = ctl.as<uint32_t>();
+  sa.res_d = res_d.as<float>();
+  sa.res_i = res_i.as<uint32_t>();
+  sa.tau = tau.as<uint32_t>();
+  sa.lock = lock.as<uint32_t>();
+  sa.err = ctl.as<uint32_t>() + 2;
+  sa.stats = nullptr;
+  sa.ld = ld;
+  sa.dp = dp;
+  sa.k = k;
+  if (n) CK(launch_search(metric, sa, grid, s));
+  CK(launch_write_results(res_d.as<float>(), res_i.as<uint32_t>(), m, k, dIds, dDists, ldo, s));
+  uint32_t hctl[3];
+  CK(cudaMemcpyAsync(hctl, ctl.p, sizeof(hctl), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (hctl[2]) return fail((int)hctl[2], "rbc_brute_knn: a bounded device wait ran out");
+  return RBC_OK;
+}
+
+int brute_range_count(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq,
+                      uint32_t d, int metric, const float *dRanges, uint32_t *dCounts, cudaStream_t s) {
+  TRY(check_dims(d, std::min(ldx, ldq), "rbc_brute_range_count"));
+  if (metric != RBC_L2 && metric != RBC_L1) return fail(RBC_ERR_INVALID, "rbc_brute_range_count: unknown metric");
+  if (m == 0) return RBC_OK;
+  if (!dQ || !dRanges || !dCounts || (n && !dX)) return fail(RBC_ERR_INVALID, "rbc_brute_range_count: NULL buffer");
+  pool_setup();
+  const uint32_t ld = pad16(d), dp = pad4(d);
+  DevBuf Xp, Qp;
+  CK(Xp.alloc(std::max<uint64_t>(n, 1) * ld * 4, s));
+  CK(Qp.alloc(m * ld * 4, s));
+  CK(launch_pad_rows(dX, ldx, Xp.as<float>(), ld, n, d, s));
+  CK(launch_pad_rows(dQ, ldq, Qp.as<float>(), ld, m, d, s));
+  CK(launch_range_count(metric, Qp.as<float>(), m, Xp.as<float>(), n, ld, dp, dRanges, dCounts, s));
+  CK(cudaStreamSynchronize(s));
+  return RBC_OK;
+}
+
+}  // namespace rbc
+
+// ====================================================================== C ABI
+using namespace rbc;
+
+extern "C" {
+
+const char *rbc_status_string(int status) {
+  switch (status) {
+    case RBC_OK: return "ok";
+    case RBC_ERR_INVALID: return "invalid argument";
+    case RBC_ERR_CUDA: return "CUDA error";
+    case RBC_ERR_NOMEM: return "out of memory";
+    case RBC_ERR_ITER_LIMIT: return "bounded device wait ran out";
+    case RBC_ERR_UNSUPPORTED: return "unsupported shape";
+    case RBC_ERR_IO: return "I/O error";
+    default: return "unknown status";
+  }
+}
+
+const char *rbc_last_error(void) { return g_last_error.c_str(); }
+
+int rbc_version(void) { return 10000; }
+
+int rbc_build(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *params, void *stream,
+              rbc_index **out) {
+  return build_index(dX, n, d, ldx, params, (cudaStream_t)stream, out);
+}
+
+int rbc_build_host(const float *hX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *params,
+                   rbc_index **out) {
+  if (!hX) return fail(RBC_ERR_INVALID, "rbc_build_host: X is NULL");
+  if (ldx < d || n == 0) return build_index(hX, n, d, ldx, params, nullptr, out);  // reports the error
+  void *dX = nullptr;
+  CK(cudaMalloc(&dX, (size_t)n * ldx * 4));
+  cudaError_t e = cudaMemcpy(dX, hX, (size_t)n * ldx * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(dX);
+    return cuda_fail(e, "rbc_build_host: copy of X");
+  }
+  int rc = build_index((const float *)dX, n, d, ldx, params, nullptr, out);
+  cudaFree(dX);
+  return rc;
+}
+
+int rbc_destroy(rbc_index *idx) {
+  if (!idx) return RBC_OK;
+  void *ptrs[] = {idx->Xp, idx->perm, idx->offsets, idx->radius, idx->R, idx->os_lists,
+                  idx->os_counts, idx->os_ids, idx->os_offsets, idx->Xo, idx->Xi};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  for (cudaEvent_t e : idx->ev_pool) cudaEventDestroy(e);
+  delete idx;
+  return RBC_OK;
+}
+
+int rbc_get_info(const rbc_index *idx, rbc_index_info *info) {
+  if (!idx || !info) return fail(RBC_ERR_INVALID, "rbc_get_info: NULL argument");
+  info->n = idx->n;
+  info->d = idx->d;
+  info->ld = idx->ld;
+  info->num_reps = idx->nr;
+  info->s = idx->s;
+  info->metric = idx->metric;
+  info->flags = idx->flags & 0xFFu;
+  info->min_list = idx->min_list;
+  info->max_list = idx->max_list;
+  info->device_bytes = idx->device_bytes;
+  return RBC_OK;
+}
+
+int rbc_get_reps(const rbc_index *idx, uint32_t *h) {
+  if (!idx || !h) return fail(RBC_ERR_INVALID, "rbc_get_reps: NULL argument");
+  std::memcpy(h, idx->rep_ids.data(), idx->nr * 4);
+  return RBC_OK;
+}
+
+int rbc_get_partition(const rbc_index *idx, uint64_t *h_offsets, uint32_t *h_members, float *h_radius) {
+  if (!idx) return fail(RBC_ERR_INVALID, "rbc_get_partition: NULL index");
+  if (!(idx->flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_INVALID, "rbc_get_partition: no partition lists");
+  if (h_offsets) CK(cudaMemcpy(h_offsets, idx->offsets, (idx->nr + 1) * 8, cudaMemcpyDeviceToHost));
+  if (h_members) CK(cudaMemcpy(h_members, idx->perm, idx->n * 4, cudaMemcpyDeviceToHost));
+  if (h_radius) CK(cudaMemcpy(h_radius, idx->radius, idx->nr * 4, cudaMemcpyDeviceToHost));
+  return RBC_OK;
+}
+
+int rbc_get_oneshot(const rbc_index *idx, uint32_t *h_lists, uint32_t *h_counts) {
+  if (!idx) return fail(RBC_ERR_INVALID, "rbc_get_oneshot: NULL index");
+  if (!(idx->flags & RBC_BUILD_ONESHOT)) return fail(RBC_ERR_INVALID, "rbc_get_oneshot: no one-shot lists");
+  if (h_lists) CK(cudaMemcpy(h_lists, idx->os_ids, (size_t)idx->nr * idx->s * 4, cudaMemcpyDeviceToHost));
+  if (h_counts) CK(cudaMemcpy(h_counts, idx->os_counts, idx->nr * 4, cudaMemcpyDeviceToHost));
+  return RBC_OK;
+}
+
+int rbc_query(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode, uint32_t *dIds,
+              float *dDists, uint32_t ldo, void *stream) {
+  return query_index(idx, dQ, m, ldq, k, mode, dIds, dDists, ldo, (cudaStream_t)stream);
+}
+
+int rbc_query_host(rbc_index *idx, const float *hQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
+                   uint32_t *hIds, float *hDists, uint32_t ldo) {
+  if (!idx) return fail(RBC_ERR_INVALID, "rbc_query_host: index is NULL");
+  if (m == 0) return RBC_OK;
+  if (!hQ || (!hIds && !hDists)) return fail(RBC_ERR_INVALID, "rbc_query_host: NULL buffer");
+  if (ldq < idx->d || ldo < k) return query_index(idx, hQ, m, ldq, k, mode, nullptr, nullptr, ldo, nullptr);
+  cudaStream_t s = nullptr;
+  DevBuf q, ids, dists;
+  CK(q.alloc(m * ldq * 4, s));
+  CK(ids.alloc(m * ldo * 4, s));
+  CK(dists.alloc(m * ldo * 4, s));
+  CK(cudaMemcpyAsync(q.p, hQ, m * ldq * 4, cudaMemcpyHostToDevice, s));
+  TRY(query_index(idx, q.as<float>(), m, ldq, k, mode | kQueryNoSync, ids.as<uint32_t>(), dists.as<float>(), ldo, s));
+  if (hIds) CK(cudaMemcpyAsync(hIds, ids.p, m * ldo * 4, cudaMemcpyDeviceToHost, s));
+  if (hDists) CK(cudaMemcpyAsync(hDists, dists.p, m * ldo * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return RBC_OK;
+}
+
+int rbc_get_query_stats(const rbc_index *idx, rbc_query_stats *st) {
+  if (!idx || !st) return fail(RBC_ERR_INVALID, "rbc_get_query_stats: NULL argument");
+  *st = idx->stats;
+  return RBC_OK;
+}
+
+int rbc_set_profiling(rbc_index *idx, int enable) {
+  if (!idx) return fail(RBC_ERR_INVALID, "rbc_set_profiling: NULL index");
+  idx->profile = enable != 0;
+  return RBC_OK;
+}
+
+int rbc_get_profile(const rbc_index *idx, rbc_profile *out) {
+  if (!idx || !out) return fail(RBC_ERR_INVALID, "rbc_get_profile: NULL argument");
+  *out = idx->prof;
+  return RBC_OK;
+}
+
+uint64_t rbc_kernel_launches(void) { return g_kernel_launches.load(); }
+
+int rbc_brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,
+                  uint32_t k, int metric, uint32_t *dIds, float *dDists, uint32_t ldo, void *stream) {
+  return brute_knn(dX, n, ldx, dQ, m, ldq, d, k, metric, dIds, dDists, ldo, (cudaStream_t)stream);
+}
+
+int rbc_brute_range_count(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq,
+                          uint32_t d, int metric, const float *dRanges, uint32_t *dCounts, void *stream) {
+  return brute_range_count(dX, n, ldx, dQ, m, ldq, d, metric, dRanges, dCounts, (cudaStream_t)stream);
+}
+
+int rbc_synth(int kind, uint64_t seed, uint64_t stream_id, uint64_t r0, uint64_t rows, uint32_t d, uint32_t ld,
+              float *dOut, uint32_t ncomp, float sigma_lo, float sigma_hi, void *stream) {
+  if (kind < RBC_SYNTH_UNIFORM || kind > RBC_SYNTH_GEOMETRIC) return fail(RBC_ERR_INVALID, "rbc_synth: unknown kind");
+  if (ld < d || (rows && !dOut)) return fail(RBC_ERR_INVALID, "rbc_synth: bad buffer");
+  CK(launch_synth(kind, seed, stream_id, r0, rows, d, ld, dOut, ncomp, sigma_lo, sigma_hi, (cudaStream_t)stream));
+  return RBC_OK;
+}
+
+}  // extern "C"

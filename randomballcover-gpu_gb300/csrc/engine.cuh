@@ -1,0 +1,79 @@
+// engine.cuh -- host-side state of the RBC engine (internal).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/rbc_gb300.h"
+#include "kernels.cuh"
+
+namespace rbc {
+
+// Internal build flag: keep the padded copy of the input in original row
+// order (the legacy rbcStruct exposes it as rbcS.dx).
+constexpr uint32_t kBuildKeepInput = 0x100u;
+// Internal query flag: do not wait for the stream at the end of the call.
+constexpr uint32_t kQueryNoSync = 0x100u;
+
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+// Stream-ordered device buffer released on scope exit.
+struct DevBuf {
+  void *p = nullptr;
+  cudaStream_t s = nullptr;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  cudaError_t alloc(size_t bytes, cudaStream_t st) {
+    s = st;
+    return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+  }
+  template <typename T>
+  T *as() const {
+    return reinterpret_cast<T *>(p);
+  }
+};
+
+}  // namespace rbc
+
+struct rbc_index {
+  int device = 0;
+  uint64_t n = 0;
+  uint32_t d = 0, ld = 0, dp = 0;
+  int metric = RBC_L2;
+  uint32_t flags = 0;
+  uint32_t nr = 0, s = 0, lds = 0;
+  std::vector<uint32_t> rep_ids;
+  // partition (exact search)
+  float *Xp = nullptr;          // n x ld rows, list-major
+  uint32_t *perm = nullptr;     // list-major row -> original id
+  uint64_t *offsets = nullptr;  // nr + 1
+  float *radius = nullptr;      // nr
+  // representatives
+  float *R = nullptr;           // pad16(nr) x ld
+  // one-shot lists (the reference's structure)
+  uint32_t *os_lists = nullptr;   // pad16(nr) x lds original ids, increasing (rbcStruct.dxMap)
+  uint32_t *os_counts = nullptr;  // nr
+  uint32_t *os_ids = nullptr;     // nr x s packed ids: row -> id map of Xo
+  uint64_t *os_offsets = nullptr; // nr + 1 rows of Xo per list
+  float *Xo = nullptr;            // list-major copy of the one-shot lists' rows
+  // padded copy of the input in original order (legacy rbcStruct.dx)
+  float *Xi = nullptr;
+  uint64_t xi_rows = 0;
+  uint64_t min_list = 0, max_list = 0;
+  uint64_t device_bytes = 0;
+  rbc_query_stats stats{};
+  // benchmark instrumentation (rbc_set_profiling)
+  bool profile = false;
+  std::vector<cudaEvent_t> ev_pool;  // pairs of events around search launches
+  size_t ev_used = 0;
+  rbc_profile prof{};
+};

@@ -1,0 +1,143 @@
+// kernels.cuh -- launch interface between the host engine and the kernels.
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rbc {
+
+// Kernels launched by this library in this process (benchmark evidence).
+inline std::atomic<unsigned long long> g_kernel_launches{0};
+
+// Every launch wrapper ends with this: counts the launch, reports its error.
+inline cudaError_t launched() {
+  g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
+// One unit of list-search work: a contiguous run of database rows searched
+// for up to one tile of queries.
+struct SearchItem {
+  uint64_t p0;    // first row in the (reordered) database
+  uint32_t np;    // number of rows
+  uint32_t list;  // list (representative) index, or RBC_DUMMY for brute chunks
+  uint32_t q0;    // offset of the tile's first query slot in the slot arrays
+  uint32_t nq;    // query slots in the tile
+};
+
+struct SearchArgs {
+  const float *X;         // database rows, stride ld, zero-padded to dp
+  const uint32_t *pid;    // row -> original id (nullptr: the row itself)
+  const float *Q;         // query rows, stride ld, zero-padded to dp
+  const uint32_t *qidx;   // query index of every slot
+  const float *qthr;      // per-slot pruning threshold or nullptr
+  const SearchItem *items;
+  const uint32_t *nitems; // device-side item count
+  uint32_t *work;         // work counter, zero at launch
+  float *res_d;           // per-query lists [m][32], sorted by (dist, id)
+  uint32_t *res_i;
+  uint32_t *tau;          // per-query k-th distance (float bits)
+  uint32_t *lock;         // per-query lock words, zero at rest
+  uint32_t *err;          // error word
+  unsigned long long *stats;  // [0] (query, point) pairs, [1] (query, list) pairs
+  uint32_t ld, dp, k;
+};
+
+// Tile geometry of the list-search kernel for a dimensionality.
+int search_tq_for(uint32_t dp);
+int search_query_tile(uint32_t dp);  // 16 * TQ
+size_t search_smem_bytes(uint32_t dp);
+cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_t s);
+int search_grid(int metric, uint32_t dp);
+
+cudaError_t launch_init_results(float *res_d, uint32_t *res_i, uint32_t *tau, uint32_t *lock,
+                                uint64_t m, cudaStream_t s);
+cudaError_t launch_write_results(const float *res_d, const uint32_t *res_i, uint64_t m, uint32_t k,
+                                 uint32_t *ids, float *dists, uint32_t ldo, cudaStream_t s);
+cudaError_t launch_brute_items(SearchItem *items, uint32_t *nitems, uint32_t *qidx, uint64_t n,
+                               uint32_t chunk, uint64_t m, uint32_t qtile, cudaStream_t s);
+
+// Row-matrix utilities.
+cudaError_t launch_pad_rows(const float *src, uint64_t ld_src, float *dst, uint32_t ld_dst,
+                            uint64_t rows, uint32_t d, cudaStream_t s);
+cudaError_t launch_gather_rows(const float *src, uint32_t ld, const uint32_t *rows, uint64_t n,
+                               float *dst, cudaStream_t s);
+
+// Dense distances: D[i][j] = dist(A row i, B row j) for i < na, j < nb.
+cudaError_t launch_dense_dist(int metric, const float *A, uint64_t na, const float *B, uint64_t nb,
+                              uint32_t ld, uint32_t dp, float *D, uint64_t ldD, cudaStream_t s);
+// Nearest row of B for every row of A under (dist, index).
+cudaError_t launch_argmin(int metric, const float *A, uint64_t na, const float *B, uint32_t nb,
+                          uint32_t ld, uint32_t dp, uint32_t *best, float *bestd, cudaStream_t s);
+// Range counts: counts[i] = #{j : dist(Q_i, X_j) < ranges[i]}.
+cudaError_t launch_range_count(int metric, const float *Q, uint64_t m, const float *X, uint64_t n,
+                               uint32_t ld, uint32_t dp, const float *ranges, uint32_t *counts,
+                               cudaStream_t s);
+
+// Partition build: stable counting sort of row ids by owner.
+uint32_t owner_tile_rows();
+cudaError_t launch_owner_hist(const uint32_t *owner, uint64_t n, uint32_t nr, uint32_t *hist,
+                              uint32_t ntiles, cudaStream_t s);
+cudaError_t launch_owner_scatter(const uint32_t *owner, uint64_t n, uint32_t nr,
+                                 const uint32_t *hist_scan, uint32_t ntiles, uint32_t *perm,
+                                 cudaStream_t s);
+cudaError_t launch_list_offsets(const uint32_t *hist_scan, uint32_t nr, uint32_t ntiles, uint64_t n,
+                                uint64_t *offsets, cudaStream_t s);
+cudaError_t launch_list_radius(const uint64_t *offsets, const uint32_t *perm, const float *odist,
+                               uint32_t nr, float *radius, cudaStream_t s);
+
+// Device-wide exclusive scan of 32-bit counts (decoupled look-back).
+size_t scan_temp_bytes(uint64_t n);
+cudaError_t launch_exclusive_scan(const uint32_t *in, uint32_t *out, uint64_t n, void *temp,
+                                  uint32_t *err, cudaStream_t s);
+
+// One-shot lists (the reference's build): exact s-selection per row of a
+// rep x point distance block, then compaction in increasing point order.
+cudaError_t launch_row_select(const float *D, uint64_t ldD, uint32_t rows, uint64_t n, uint32_t s,
+                              uint32_t *thr_bits, uint32_t *need, cudaStream_t st);
+cudaError_t launch_row_compact(const float *D, uint64_t ldD, uint32_t rows, uint64_t n,
+                               const uint32_t *thr_bits, const uint32_t *need, uint32_t *lists,
+                               uint32_t lds, uint32_t *counts, cudaStream_t st);
+
+// Query planning.
+cudaError_t launch_row_topp(const float *D, uint64_t m, uint32_t nr, uint32_t P, uint32_t *probe,
+                            float *probed, cudaStream_t s);
+cudaError_t launch_group_by_list(const uint32_t *probe, uint64_t m, uint32_t P, uint32_t nr,
+                                 uint32_t *list_cnt, cudaStream_t s);
+struct PlanArgs {
+  const float *Dqr;        // m x nr query-to-rep distances (computed form)
+  const float *radius;     // nr list radii (computed form, max member distance)
+  const uint64_t *offsets; // nr+1 list offsets
+  const uint32_t *probe;   // m x P probed lists (first column = nearest rep)
+  const float *probed;     // m x P their distances
+  const uint32_t *tau;     // per-query k-th distance bits after the probe phase
+  uint64_t m;
+  uint32_t nr, P, metric, qtile;
+  double gamma;            // relative error bound of a computed distance
+  uint32_t *list_cnt;      // nr+1 counters (surviving queries per list)
+  uint32_t *list_cursor;   // nr fill cursors
+  uint32_t *pair_q;        // list-major surviving (query) entries
+  float *pair_thr;         // matching prune thresholds
+  uint32_t *tile_cnt;      // nr+1 query tiles per list
+  SearchItem *items;
+  uint32_t *nitems;
+  uint32_t phase;          // 0 = count, 1 = fill
+};
+// mode 0: the probe pairs (q, probe[q][p]); mode 1: every other pair whose
+// pruning bound survives.  a.phase 0 counts per list into a.list_cnt; phase 1
+// fills pair_q / pair_thr with a.list_cnt pointing at the scanned starts.
+cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s);
+cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, uint32_t nr, uint32_t qtile,
+                                  uint32_t *tile_cnt, cudaStream_t s);
+cudaError_t launch_plan_items(const uint32_t *list_cnt, const uint32_t *list_start,
+                              const uint32_t *tile_start, const uint64_t *offsets, uint32_t nr,
+                              uint32_t qtile, SearchItem *items, uint32_t *nitems, cudaStream_t s);
+
+// Synthetic data.
+cudaError_t launch_synth(int kind, uint64_t seed, uint64_t stream_id, uint64_t r0, uint64_t rows,
+                         uint32_t d, uint32_t ld, float *out, uint32_t ncomp, float sigma_lo,
+                         float sigma_hi, cudaStream_t s);
+void geometric_table(uint32_t num, uint32_t den, uint32_t *T);
+
+}  // namespace rbc

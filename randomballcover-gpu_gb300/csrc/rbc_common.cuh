@@ -1,0 +1,99 @@
+// rbc_common.cuh -- shared device helpers of the RBC engine.
+//
+// The distance arithmetic here is the engine's definition of a distance and
+// is bit-identical to the reference's distVec (utils.cu:183-191, with DIST
+// from defs.h:20-21): a float accumulator, dims visited in increasing order,
+// each term (q-x)*(q-x) (L2, squared) or |q-x| (L1) rounded on its own and
+// added with its own rounding.  The __f*_rn intrinsics are never contracted
+// into FMA by nvcc, so no build flag can change these bits.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/rbc_gb300.h"
+
+#define RBC_DUMMY 0xFFFFFFFFu
+
+namespace rbc {
+
+// Largest dimensionality the list-search kernels hold in shared memory.
+constexpr uint32_t kMaxDim = 512;
+// Internal width of every per-query neighbour list (KMAX in defs.h:9).
+constexpr int kListWidth = 32;
+
+__host__ __device__ inline uint32_t pad16(uint32_t v) { return (v + 15u) / 16u * 16u; }
+__host__ __device__ inline uint32_t pad4(uint32_t v) { return (v + 3u) / 4u * 4u; }
+
+// One coordinate term of the distance, rounded as the reference rounds it.
+template <int METRIC>
+__device__ __forceinline__ float term(float q, float x) {
+  float t = __fsub_rn(q, x);
+  if (METRIC == RBC_L1) return fabsf(t);
+  return __fmul_rn(t, t);
+}
+
+template <int METRIC>
+__device__ __forceinline__ float accum(float acc, float q, float x) {
+  return __fadd_rn(acc, term<METRIC>(q, x));
+}
+
+// (dist, id) lexicographic order: the tie rule of bruteCPU (brute.cu:104)
+// generalised to k neighbours.
+__device__ __forceinline__ bool pair_less(float da, uint32_t ia, float db, uint32_t ib) {
+  return da < db || (da == db && ia < ib);
+}
+
+// Non-negative floats order like their bit patterns; used for atomicMin/Max.
+__device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
+
+// Warp-wide bitonic sort of 32 (dist, id) pairs, ascending, one per lane.
+__device__ __forceinline__ void warp_sort32(float &d, uint32_t &id) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      float od = __shfl_xor_sync(0xffffffffu, d, j);
+      uint32_t oi = __shfl_xor_sync(0xffffffffu, id, j);
+      bool up = ((lane & k) == 0);
+      bool lower = ((lane & j) == 0);
+      // the lower lane of an ascending pair keeps the smaller element
+      bool take_other = (lower == up) ? pair_less(od, oi, d, id) : pair_less(d, id, od, oi);
+      if (take_other) { d = od; id = oi; }
+    }
+  }
+}
+
+// Sort a bitonic sequence of 32 pairs held one per lane, ascending.
+__device__ __forceinline__ void warp_bitonic_merge32(float &d, uint32_t &id) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    float od = __shfl_xor_sync(0xffffffffu, d, j);
+    uint32_t oi = __shfl_xor_sync(0xffffffffu, id, j);
+    bool lower = ((lane & j) == 0);
+    bool take_other = lower ? pair_less(od, oi, d, id) : pair_less(d, id, od, oi);
+    if (take_other) { d = od; id = oi; }
+  }
+}
+
+// Merge 32 unsorted candidates (one per lane, (FLT_MAX, DUMMY) for none)
+// into a sorted 32-entry list held one per lane: the list keeps the 32
+// smallest pairs of the union.
+__device__ __forceinline__ void warp_merge_into(float &ld, uint32_t &li, float cd, uint32_t ci) {
+  const int lane = threadIdx.x & 31;
+  warp_sort32(cd, ci);
+  float rd = __shfl_sync(0xffffffffu, cd, 31 - lane);
+  uint32_t ri = __shfl_sync(0xffffffffu, ci, 31 - lane);
+  if (pair_less(rd, ri, ld, li)) { ld = rd; li = ri; }
+  warp_bitonic_merge32(ld, li);
+}
+
+// Error word shared by kernels that bound their waits: the first error wins.
+__device__ __forceinline__ void raise_error(uint32_t *err, uint32_t code) {
+  if (err) atomicCAS(err, 0u, code);
+}
+
+}  // namespace rbc

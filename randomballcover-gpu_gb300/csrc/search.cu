@@ -1,0 +1,348 @@
+// search.cu -- exact list search: the engine's hot kernel.
+//
+// Counterpart of planKNNKernel / planNNKernel / knnKernel (kernels.cu:15-282
+// of the reference): queries are compared against runs of database rows and a
+// sorted 32-entry (dist, id) list is kept per query.  GB300 design:
+//   * persistent CTAs pull SearchItems from a device work counter, so no host
+//     round trip sits between the plan and the search and the whole query
+//     pipeline can run inside one CUDA graph;
+//   * list rows are contiguous (the build reorders the database by list) and
+//     are double-buffered into shared memory with cp.async;
+//   * a 256-thread CTA computes 16*TQ x 32 distance tiles in registers on the
+//     FP32 pipe with the reference's rounding (tile.cuh);
+//   * candidates are filtered against the query's current k-th distance and
+//     merged into the per-query list with warp-shuffle bitonic networks in
+//     place of the reference's shared-memory Batcher network (kernels.cu:479-625);
+//   * each CTA merges its lists into the global per-query lists under a short
+//     per-query lock whose wait is bounded (error word, never a hang).
+#include "kernels.cuh"
+#include "tile.cuh"
+
+namespace rbc {
+
+namespace {
+
+constexpr uint32_t kLockSpinLimit = 1u << 22;
+
+struct SearchSmem {
+  float *Qs, *Xs0, *Xs1, *cand_d, *list_d, *tau_s;
+  uint32_t *cand_i, *list_i, *cand_n;
+};
+
+template <int TQ>
+__device__ __forceinline__ SearchSmem carve(unsigned char *base, uint32_t S) {
+  constexpr int BQ = 16 * TQ;
+  SearchSmem sm;
+  float *f = reinterpret_cast<float *>(base);
+  sm.Qs = f;
+  f += BQ * S;
+  sm.Xs0 = f;
+  f += kTileCols * S;
+  sm.Xs1 = f;
+  f += kTileCols * S;
+  sm.cand_d = f;
+  f += BQ * kTileCols;
+  sm.list_d = f;
+  f += BQ * kListWidth;
+  sm.tau_s = f;
+  f += BQ;
+  uint32_t *u = reinterpret_cast<uint32_t *>(f);
+  sm.cand_i = u;
+  u += BQ * kTileCols;
+  sm.list_i = u;
+  u += BQ * kListWidth;
+  sm.cand_n = u;
+  return sm;
+}
+
+template <int TQ>
+size_t smem_bytes_tq(uint32_t dp) {
+  constexpr int BQ = 16 * TQ;
+  uint32_t S = dp + 4;
+  size_t floats = (size_t)BQ * S + 2 * kTileCols * S + BQ * kTileCols + BQ * kListWidth + BQ;
+  size_t words = (size_t)BQ * kTileCols + BQ * kListWidth + BQ;
+  return (floats + words) * 4;
+}
+
+template <int METRIC, int TQ>
+__global__ void __launch_bounds__(kTileThreads, 2) search_kernel(SearchArgs a) {
+  constexpr int BQ = 16 * TQ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t s_item;
+  const uint32_t S = a.dp + 4;
+  SearchSmem sm = carve<TQ>(smem_raw, S);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tq = tid >> 4, tx = tid & 15;
+  const uint32_t kk = a.k;
+  unsigned long long my_pairs = 0, my_lists = 0;
+
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(a.work, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    if (it >= *a.nitems) break;
+    const SearchItem item = a.items[it];
+
+    // ---- stage the query tile, thresholds and empty lists ----
+    for (uint32_t t = tid; t < BQ; t += kTileThreads) {
+      float ts = -1.f;  // < 0 marks an inactive slot
+      if (t < item.nq) {
+        uint32_t q = a.qidx[item.q0 + t];
+        float tq_now = __uint_as_float(__ldcg(a.tau + q));
+        ts = tq_now;
+        if (a.qthr && a.qthr[item.q0 + t] > tq_now) ts = -1.f;  // pruned since planning
+      }
+      sm.tau_s[t] = ts;
+      sm.cand_n[t] = 0;
+    }
+    for (uint32_t t = tid; t < BQ * kListWidth; t += kTileThreads) {
+      sm.list_d[t] = FLT_MAX;
+      sm.list_i[t] = RBC_DUMMY;
+    }
+    __syncthreads();
+    const int nactive = __syncthreads_count(tid < BQ && sm.tau_s[tid] >= 0.f);
+    if (nactive == 0) continue;
+    {
+      const uint32_t chunks = a.dp >> 2;
+      for (uint32_t t = tid; t < BQ * chunks; t += kTileThreads) {
+        uint32_t r = t / chunks, c = t - r * chunks;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (r < item.nq && sm.tau_s[r] >= 0.f)
+          v = __ldg(reinterpret_cast<const float4 *>(a.Q + (uint64_t)a.qidx[item.q0 + r] * a.ld) + c);
+        *reinterpret_cast<float4 *>(sm.Qs + r * S + 4 * c) = v;
+      }
+    }
+
+    // ---- stream the rows in tiles of 32 ----
+    const uint32_t ntiles = (item.np + kTileCols - 1) / kTileCols;
+    stage_rows_async(sm.Xs0, S, a.X, a.ld, item.p0, min((uint32_t)kTileCols, item.np), a.dp);
+    cp_async_commit();
+    for (uint32_t t = 0; t < ntiles; t++) {
+      float *cur = (t & 1) ? sm.Xs1 : sm.Xs0;
+      float *nxt = (t & 1) ? sm.Xs0 : sm.Xs1;
+      if (t + 1 < ntiles) {
+        uint32_t r0 = (t + 1) * kTileCols;
+        stage_rows_async(nxt, S, a.X, a.ld, item.p0 + r0, min((uint32_t)kTileCols, item.np - r0), a.dp);
+      }
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+
+      const uint32_t base = t * kTileCols;
+      const uint32_t valid = min((uint32_t)kTileCols, item.np - base);
+      float acc[TQ][2];
+      tile_distances<METRIC, TQ>(sm.Qs, cur, S, a.dp, tq, tx, acc);
+#pragma unroll
+      for (int i = 0; i < TQ; i++) {
+        const int slot = tq + 16 * i;
+        const float thr = sm.tau_s[slot];
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+          const uint32_t col = tx + 16 * j;
+          if (col < valid && thr >= 0.f && acc[i][j] <= thr) {
+            uint32_t pos = atomicAdd(&sm.cand_n[slot], 1u);
+            uint64_t row = item.p0 + base + col;
+            sm.cand_d[slot * kTileCols + pos] = acc[i][j];
+            sm.cand_i[slot * kTileCols + pos] = a.pid ? a.pid[row] : (uint32_t)row;
+          }
+        }
+      }
+      __syncthreads();
+
+      // ---- merge each slot's candidates into its list (one warp per slot) ----
+      for (int slot = warp; slot < BQ; slot += kTileThreads / 32) {
+        const uint32_t n = sm.cand_n[slot];
+        if (n == 0) continue;
+        float ld = sm.list_d[slot * kListWidth + lane];
+        uint32_t li = sm.list_i[slot * kListWidth + lane];
+        for (uint32_t b = 0; b < n; b += 32) {
+          float cd = FLT_MAX;
+          uint32_t ci = RBC_DUMMY;
+          if (b + lane < n) {
+            cd = sm.cand_d[slot * kTileCols + b + lane];
+            ci = sm.cand_i[slot * kTileCols + b + lane];
+          }
+          warp_merge_into(ld, li, cd, ci);
+        }
+        sm.list_d[slot * kListWidth + lane] = ld;
+        sm.list_i[slot * kListWidth + lane] = li;
+        float kth = __shfl_sync(0xffffffffu, ld, kk - 1);
+        if (lane == 0) {
+          sm.cand_n[slot] = 0;
+          if (kth < sm.tau_s[slot]) sm.tau_s[slot] = kth;
+        }
+      }
+      __syncthreads();
+    }
+    if (tid == 0) {
+      my_pairs += (unsigned long long)item.np * nactive;
+      my_lists += nactive;
+    }
+
+    // ---- publish: merge into the global per-query lists ----
+    for (int slot = warp; slot < (int)item.nq; slot += kTileThreads / 32) {
+      if (sm.tau_s[slot] < 0.f) continue;
+      const uint32_t q = a.qidx[item.q0 + slot];
+      float cd = (lane < (int)kk) ? sm.list_d[slot * kListWidth + lane] : FLT_MAX;
+      uint32_t ci = (lane < (int)kk) ? sm.list_i[slot * kListWidth + lane] : RBC_DUMMY;
+      float first = __shfl_sync(0xffffffffu, cd, 0);
+      uint32_t first_id = __shfl_sync(0xffffffffu, ci, 0);
+      float gtau = __shfl_sync(0xffffffffu, __uint_as_float(__ldcg(a.tau + q)), 0);
+      if (first_id == RBC_DUMMY || first > gtau) continue;
+      int got = 0;
+      if (lane == 0) {
+        uint32_t spins = 0;
+        while (atomicCAS(a.lock + q, 0u, 1u) != 0u) {
+          if (++spins > kLockSpinLimit) break;
+          __nanosleep(32);
+        }
+        got = spins <= kLockSpinLimit;
+        if (!got) raise_error(a.err, RBC_ERR_ITER_LIMIT);
+      }
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) continue;
+      __threadfence();
+      float gd = __ldcg(a.res_d + (uint64_t)q * kListWidth + lane);
+      uint32_t gi = __ldcg(a.res_i + (uint64_t)q * kListWidth + lane);
+      warp_merge_into(gd, gi, cd, ci);
+      a.res_d[(uint64_t)q * kListWidth + lane] = gd;
+      a.res_i[(uint64_t)q * kListWidth + lane] = gi;
+      float kth = __shfl_sync(0xffffffffu, gd, kk - 1);
+      __threadfence();
+      if (lane == 0) {
+        atomicMin(a.tau + q, fbits(kth));
+        __threadfence();
+        atomicExch(a.lock + q, 0u);
+      }
+    }
+    __syncthreads();
+  }
+  if (a.stats && tid == 0 && my_lists) {
+    atomicAdd(a.stats, my_pairs);
+    atomicAdd(a.stats + 1, my_lists);
+  }
+}
+
+template <int METRIC, int TQ>
+cudaError_t launch_tq(const SearchArgs &a, int grid, cudaStream_t s) {
+  size_t smem = smem_bytes_tq<TQ>(a.dp);
+  cudaError_t e = cudaFuncSetAttribute(search_kernel<METRIC, TQ>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  search_kernel<METRIC, TQ><<<grid, kTileThreads, smem, s>>>(a);
+  return launched();
+}
+
+template <int METRIC, int TQ>
+int grid_tq(uint32_t dp) {
+  size_t smem = smem_bytes_tq<TQ>(dp);
+  cudaFuncSetAttribute(search_kernel<METRIC, TQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, search_kernel<METRIC, TQ>, kTileThreads,
+                                                smem);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (per_sm < 1) per_sm = 1;
+  return per_sm * sms;
+}
+
+__global__ void init_results_kernel(float *res_d, uint32_t *res_i, uint32_t *tau, uint32_t *lock,
+                                    uint64_t m) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < m * kListWidth) {
+    res_d[i] = FLT_MAX;
+    res_i[i] = RBC_DUMMY;
+  }
+  if (i < m) {
+    tau[i] = fbits(FLT_MAX);
+    lock[i] = 0;
+  }
+}
+
+__global__ void write_results_kernel(const float *res_d, const uint32_t *res_i, uint64_t m, uint32_t k,
+                                     uint32_t *ids, float *dists, uint32_t ldo) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= m * k) return;
+  uint64_t q = i / k;
+  uint32_t j = (uint32_t)(i - q * k);
+  if (ids) ids[q * ldo + j] = res_i[q * kListWidth + j];
+  if (dists) dists[q * ldo + j] = res_d[q * kListWidth + j];
+}
+
+__global__ void brute_items_kernel(SearchItem *items, uint32_t *nitems, uint32_t *qidx, uint64_t n,
+                                   uint32_t chunk, uint64_t m, uint32_t qtile) {
+  const uint64_t nchunks = (n + chunk - 1) / chunk;
+  const uint64_t ntile = (m + qtile - 1) / qtile;
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < m) qidx[i] = (uint32_t)i;
+  if (i < nchunks * ntile) {
+    uint64_t c = i / ntile, t = i - c * ntile;  // chunk-major: a chunk stays hot in L2
+    SearchItem it;
+    it.p0 = c * chunk;
+    it.np = (uint32_t)min((uint64_t)chunk, n - c * chunk);
+    it.list = RBC_DUMMY;
+    it.q0 = (uint32_t)(t * qtile);
+    it.nq = (uint32_t)min((uint64_t)qtile, m - t * qtile);
+    items[i] = it;
+  }
+  if (i == 0) *nitems = (uint32_t)(nchunks * ntile);
+}
+
+}  // namespace
+
+int search_tq_for(uint32_t dp) { return dp <= 128 ? 4 : (dp <= 256 ? 2 : 1); }
+int search_query_tile(uint32_t dp) { return 16 * search_tq_for(dp); }
+
+size_t search_smem_bytes(uint32_t dp) {
+  switch (search_tq_for(dp)) {
+    case 4: return smem_bytes_tq<4>(dp);
+    case 2: return smem_bytes_tq<2>(dp);
+    default: return smem_bytes_tq<1>(dp);
+  }
+}
+
+int search_grid(int metric, uint32_t dp) {
+  int tqv = search_tq_for(dp);
+  if (metric == RBC_L1)
+    return tqv == 4 ? grid_tq<RBC_L1, 4>(dp) : tqv == 2 ? grid_tq<RBC_L1, 2>(dp) : grid_tq<RBC_L1, 1>(dp);
+  return tqv == 4 ? grid_tq<RBC_L2, 4>(dp) : tqv == 2 ? grid_tq<RBC_L2, 2>(dp) : grid_tq<RBC_L2, 1>(dp);
+}
+
+cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_t s) {
+  int tqv = search_tq_for(a.dp);
+  if (metric == RBC_L1)
+    return tqv == 4 ? launch_tq<RBC_L1, 4>(a, grid, s)
+                    : tqv == 2 ? launch_tq<RBC_L1, 2>(a, grid, s) : launch_tq<RBC_L1, 1>(a, grid, s);
+  return tqv == 4 ? launch_tq<RBC_L2, 4>(a, grid, s)
+                  : tqv == 2 ? launch_tq<RBC_L2, 2>(a, grid, s) : launch_tq<RBC_L2, 1>(a, grid, s);
+}
+
+cudaError_t launch_init_results(float *res_d, uint32_t *res_i, uint32_t *tau, uint32_t *lock,
+                                uint64_t m, cudaStream_t s) {
+  uint64_t total = m * kListWidth;
+  init_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(res_d, res_i, tau, lock, m);
+  return launched();
+}
+
+cudaError_t launch_write_results(const float *res_d, const uint32_t *res_i, uint64_t m, uint32_t k,
+                                 uint32_t *ids, float *dists, uint32_t ldo, cudaStream_t s) {
+  uint64_t total = m * k;
+  if (total == 0) return cudaSuccess;
+  write_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(res_d, res_i, m, k, ids,
+                                                                       dists, ldo);
+  return launched();
+}
+
+cudaError_t launch_brute_items(SearchItem *items, uint32_t *nitems, uint32_t *qidx, uint64_t n,
+                               uint32_t chunk, uint64_t m, uint32_t qtile, cudaStream_t s) {
+  uint64_t nchunks = (n + chunk - 1) / chunk;
+  uint64_t total = nchunks * ((m + qtile - 1) / qtile);
+  if (m > total) total = m;
+  if (total == 0) total = 1;
+  brute_items_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(items, nitems, qidx, n, chunk, m,
+                                                                     qtile);
+  return launched();
+}
+
+}  // namespace rbc

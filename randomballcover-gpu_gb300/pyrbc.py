@@ -1,0 +1,292 @@
+"""Python binding of librbcgb.so (the engine's C ABI, include/rbc_gb300.h).
+
+A thin ctypes layer for tests, the benchmark and scripting.  Device buffers
+are torch CUDA tensors (torch is used only to own device memory and streams);
+every computation happens in the engine's CUDA kernels.  If the library is
+missing the import of a function fails loudly -- there is no Python or CPU
+fallback for any engine operation.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librbcgb.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_ITER_LIMIT, ERR_UNSUPPORTED, ERR_IO = range(7)
+L2, L1 = 0, 1
+KMAX = 32
+BUILD_PARTITION, BUILD_ONESHOT = 1, 2
+QUERY_EXACT, QUERY_ONESHOT = 0, 1
+SYNTH_UNIFORM, SYNTH_MIXTURE, SYNTH_GEOMETRIC = 0, 1, 2
+DUMMY = 0xFFFFFFFF
+FLT_MAX = float(np.finfo(np.float32).max)
+
+
+class RBCError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"rbc error {code}: {msg}")
+        self.code = code
+
+
+class BuildParams(C.Structure):
+    _fields_ = [("num_reps", C.c_uint32), ("s", C.c_uint32), ("metric", C.c_int), ("flags", C.c_uint32),
+                ("seed", C.c_uint64), ("rep_ids", C.POINTER(C.c_uint32))]
+
+
+class IndexInfo(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("ld", C.c_uint32), ("num_reps", C.c_uint32),
+                ("s", C.c_uint32), ("metric", C.c_int), ("flags", C.c_uint32), ("min_list", C.c_uint64),
+                ("max_list", C.c_uint64), ("device_bytes", C.c_uint64)]
+
+
+class QueryStats(C.Structure):
+    _fields_ = [("queries", C.c_uint64), ("rep_pairs", C.c_uint64), ("lists_probed", C.c_uint64),
+                ("point_pairs", C.c_uint64)]
+
+
+class Profile(C.Structure):
+    _fields_ = [("search_launches", C.c_uint64), ("search_ms", C.c_double)]
+
+
+# Every symbol of include/rbc_gb300.h with its ctypes signature.
+_VP, _U32, _U64, _INT, _F = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_float
+SIGNATURES = {
+    "rbc_status_string": ([_INT], C.c_char_p),
+    "rbc_last_error": ([], C.c_char_p),
+    "rbc_version": ([], _INT),
+    "rbc_build": ([_VP, _U64, _U32, _U32, C.POINTER(BuildParams), _VP, C.POINTER(_VP)], _INT),
+    "rbc_build_host": ([_VP, _U64, _U32, _U32, C.POINTER(BuildParams), C.POINTER(_VP)], _INT),
+    "rbc_destroy": ([_VP], _INT),
+    "rbc_get_info": ([_VP, C.POINTER(IndexInfo)], _INT),
+    "rbc_get_reps": ([_VP, _VP], _INT),
+    "rbc_get_partition": ([_VP, _VP, _VP, _VP], _INT),
+    "rbc_get_oneshot": ([_VP, _VP, _VP], _INT),
+    "rbc_query": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP, _VP, _U32, _VP], _INT),
+    "rbc_query_host": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP, _VP, _U32], _INT),
+    "rbc_get_query_stats": ([_VP, C.POINTER(QueryStats)], _INT),
+    "rbc_set_profiling": ([_VP, _INT], _INT),
+    "rbc_get_profile": ([_VP, C.POINTER(Profile)], _INT),
+    "rbc_kernel_launches": ([], _U64),
+    "rbc_brute_knn": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _INT, _VP, _VP, _U32, _VP], _INT),
+    "rbc_brute_range_count": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _INT, _VP, _VP, _VP], _INT),
+    "rbc_synth": ([_INT, _U64, _U64, _U64, _U64, _U32, _U32, _VP, _U32, _F, _F, _VP], _INT),
+    "rbc_read_matrix_bin": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
+    "rbc_read_matrix_text": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
+    "rbc_write_matrix_bin": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
+    "rbc_write_neighbors_bin": ([C.c_char_p, _VP, _VP, _U64, _U32, _U32], _INT),
+    "rbc_write_neighbors_text": ([C.c_char_p, _VP, _VP, _U64, _U32, _U32], _INT),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the engine library (build it first with build_ext.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RBCError(ERR_CUDA, f"engine library not built: {LIB_PATH}")
+        L = C.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != OK:
+        raise RBCError(rc, lib().rbc_last_error().decode())
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data
+    return t.data_ptr()
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _dev(a, dtype=None):
+    import torch
+    if isinstance(a, np.ndarray):
+        a = torch.from_numpy(np.ascontiguousarray(a))
+    if dtype is not None:
+        a = a.to(dtype)
+    return a.cuda().contiguous()
+
+
+class Index:
+    """An RBC index over the rows of X (n x d float32, CUDA tensor or numpy)."""
+
+    def __init__(self, X, num_reps, s=0, metric=L2, flags=0, seed=0, rep_ids=None, stream=None):
+        import torch
+        X = _dev(X, torch.float32)
+        n, d = X.shape
+        p = BuildParams(num_reps, s, metric, flags, seed, None)
+        self._rep_buf = None
+        if rep_ids is not None:
+            self._rep_buf = np.ascontiguousarray(rep_ids, dtype=np.uint32)
+            p.rep_ids = self._rep_buf.ctypes.data_as(C.POINTER(C.c_uint32))
+        h = C.c_void_p()
+        check(lib().rbc_build(X.data_ptr(), n, d, X.stride(0), C.byref(p), _stream(stream), C.byref(h)))
+        self.h = h
+        self.n, self.d, self.metric = n, d, metric
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().rbc_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def query(self, Q, k, mode=QUERY_EXACT, stream=None, out=None):
+        """Returns (ids uint32-as-int32 tensor [m,k], dists float32 [m,k]) on the device."""
+        import torch
+        Q = _dev(Q, torch.float32)
+        m = Q.shape[0]
+        if out is None:
+            ids = torch.empty((m, k), dtype=torch.int32, device=Q.device)
+            dists = torch.empty((m, k), dtype=torch.float32, device=Q.device)
+        else:
+            ids, dists = out
+        check(lib().rbc_query(self.h, Q.data_ptr(), m, Q.stride(0), k, mode, ids.data_ptr(), dists.data_ptr(),
+                              ids.stride(0), _stream(stream)))
+        return ids, dists
+
+    def query_host(self, Q, k, mode=QUERY_EXACT, out=None):
+        """Host in, host out (the copies are part of the call)."""
+        Q = np.ascontiguousarray(Q, dtype=np.float32)
+        m = Q.shape[0]
+        if out is None:
+            ids = np.empty((m, k), np.uint32)
+            dists = np.empty((m, k), np.float32)
+        else:
+            ids, dists = out
+        check(lib().rbc_query_host(self.h, _ptr(Q), m, Q.shape[1], k, mode, _ptr(ids), _ptr(dists), ids.shape[1]))
+        return ids, dists
+
+    def info(self):
+        i = IndexInfo()
+        check(lib().rbc_get_info(self.h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in IndexInfo._fields_}
+
+    def reps(self):
+        nr = self.info()["num_reps"]
+        out = np.empty(nr, np.uint32)
+        check(lib().rbc_get_reps(self.h, out.ctypes.data))
+        return out
+
+    def partition(self):
+        inf = self.info()
+        off = np.empty(inf["num_reps"] + 1, np.uint64)
+        mem = np.empty(inf["n"], np.uint32)
+        rad = np.empty(inf["num_reps"], np.float32)
+        check(lib().rbc_get_partition(self.h, off.ctypes.data, mem.ctypes.data, rad.ctypes.data))
+        return off, mem, rad
+
+    def oneshot(self):
+        inf = self.info()
+        lists = np.empty((inf["num_reps"], inf["s"]), np.uint32)
+        counts = np.empty(inf["num_reps"], np.uint32)
+        check(lib().rbc_get_oneshot(self.h, lists.ctypes.data, counts.ctypes.data))
+        return lists, counts
+
+    def stats(self):
+        st = QueryStats()
+        check(lib().rbc_get_query_stats(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in QueryStats._fields_}
+
+    def set_profiling(self, enable=True):
+        check(lib().rbc_set_profiling(self.h, int(enable)))
+
+    def profile(self):
+        p = Profile()
+        check(lib().rbc_get_profile(self.h, C.byref(p)))
+        return {"search_launches": p.search_launches, "search_ms": p.search_ms}
+
+
+def kernel_launches():
+    return int(lib().rbc_kernel_launches())
+
+
+def brute_knn(X, Q, k, metric=L2, stream=None):
+    import torch
+    X = _dev(X, torch.float32)
+    Q = _dev(Q, torch.float32)
+    m = Q.shape[0]
+    ids = torch.empty((m, k), dtype=torch.int32, device=Q.device)
+    dists = torch.empty((m, k), dtype=torch.float32, device=Q.device)
+    check(lib().rbc_brute_knn(X.data_ptr(), X.shape[0], X.stride(0), Q.data_ptr(), m, Q.stride(0), Q.shape[1], k,
+                              metric, ids.data_ptr(), dists.data_ptr(), k, _stream(stream)))
+    return ids, dists
+
+
+def range_count(X, Q, ranges, metric=L2, stream=None):
+    import torch
+    X = _dev(X, torch.float32)
+    Q = _dev(Q, torch.float32)
+    r = _dev(ranges, torch.float32)
+    cnt = torch.empty(Q.shape[0], dtype=torch.int32, device=Q.device)
+    check(lib().rbc_brute_range_count(X.data_ptr(), X.shape[0], X.stride(0), Q.data_ptr(), Q.shape[0], Q.stride(0),
+                                      Q.shape[1], metric, r.data_ptr(), cnt.data_ptr(), _stream(stream)))
+    return cnt
+
+
+def synth(kind, seed, stream_id, rows, d, r0=0, ncomp=1, sigma_lo=0.0, sigma_hi=0.0, out=None, stream=None):
+    """Counter-based synthetic rows on the device (same bits as the CPU recipe)."""
+    import torch
+    if out is None:
+        out = torch.empty((rows, d), dtype=torch.float32, device="cuda")
+    check(lib().rbc_synth(kind, seed, stream_id, r0, rows, d, out.stride(0), out.data_ptr(), ncomp, sigma_lo,
+                          sigma_hi, _stream(stream)))
+    return out
+
+
+def u32(t):
+    """uint32 view of an int32 id tensor as numpy."""
+    a = t.cpu().numpy() if hasattr(t, "cpu") else np.asarray(t)
+    return a.view(np.uint32)
+
+
+# ---------------------------------------------------------------- file I/O
+def read_matrix_bin(path, rows, cols, ld=None):
+    ld = ld or cols
+    out = np.zeros((rows, ld), np.float32)
+    check(lib().rbc_read_matrix_bin(path.encode(), out.ctypes.data, rows, cols, ld))
+    return out
+
+
+def read_matrix_text(path, rows, cols, ld=None):
+    ld = ld or cols
+    out = np.zeros((rows, ld), np.float32)
+    check(lib().rbc_read_matrix_text(path.encode(), out.ctypes.data, rows, cols, ld))
+    return out
+
+
+def write_matrix_bin(path, A):
+    A = np.ascontiguousarray(A, np.float32)
+    check(lib().rbc_write_matrix_bin(path.encode(), A.ctypes.data, A.shape[0], A.shape[1], A.shape[1]))
+
+
+def write_neighbors_bin(path, ids, dists):
+    ids = np.ascontiguousarray(ids, np.uint32)
+    dists = np.ascontiguousarray(dists, np.float32)
+    check(lib().rbc_write_neighbors_bin(path.encode(), ids.ctypes.data, dists.ctypes.data, ids.shape[0],
+                                        ids.shape[1], ids.shape[1]))
+
+
+def write_neighbors_text(path, ids, dists):
+    ids = np.ascontiguousarray(ids, np.uint32)
+    dists = np.ascontiguousarray(dists, np.float32)
+    check(lib().rbc_write_neighbors_text(path.encode(), ids.ctypes.data, dists.ctypes.data, ids.shape[0],
+                                         ids.shape[1], ids.shape[1]))

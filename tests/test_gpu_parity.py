@@ -1,0 +1,220 @@
+"""GPU parity: the engine's CUDA kernels against the CPU oracle.
+
+Ids must be bit-exact and distances bit-exact (the engine computes every
+distance with the reference's float arithmetic); the stated tolerance is
+1e-6 relative and is what assert_dists checks when bit equality is not the
+point of a test.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, sample_inputs
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-6
+
+
+def assert_same(ids, dists, ref_ids, ref_dists, rbc):
+    ids = rbc.u32(ids)
+    dists = dists.cpu().numpy() if hasattr(dists, "cpu") else dists
+    np.testing.assert_array_equal(ids, ref_ids)
+    np.testing.assert_allclose(dists, ref_dists, rtol=RTOL, atol=0)
+    np.testing.assert_array_equal(dists, ref_dists)
+
+
+# ------------------------------------------------------------------ synthetic data
+@pytest.mark.parametrize("kind,ncomp,slo,shi", [(0, 1, 0, 0), (1, 7, 0.02, 0.1), (2, 1, 0, 0)])
+def test_synth_gpu_equals_cpu(rbc, oracle, kind, ncomp, slo, shi):
+    for d, rows, r0 in ((16, 1000, 0), (37, 333, 12345), (128, 200, 7)):
+        g = rbc.synth(kind, 9, 1, rows, d, r0=r0, ncomp=ncomp, sigma_lo=slo, sigma_hi=shi).cpu().numpy()
+        c = oracle.synth(kind, 9, 1, rows, d, r0=r0, ncomp=ncomp, sigma_lo=slo, sigma_hi=shi)
+        np.testing.assert_array_equal(g, c)
+
+
+# ------------------------------------------------------------------ brute force
+@pytest.mark.parametrize("metric", [0, 1])
+@pytest.mark.parametrize("n,m,d,k", [(1024, 128, 16, 32), (1000, 77, 3, 10), (3001, 65, 33, 1),
+                                     (500, 200, 128, 32), (20, 9, 7, 32), (40000, 64, 16, 10),
+                                     (2000, 30, 300, 5), (777, 33, 512, 8)])
+def test_brute_knn(rbc, oracle, metric, n, m, d, k):
+    rng = np.random.default_rng(n * 31 + d)
+    X = rng.standard_normal((n, d)).astype(np.float32)
+    Q = rng.standard_normal((m, d)).astype(np.float32)
+    ids, dists = rbc.brute_knn(X, Q, k, metric)
+    rid, rd = oracle.knn(X, Q, k, metric)
+    assert_same(ids, dists, rid, rd, rbc)
+
+
+def test_brute_ties_and_duplicates(rbc, oracle):
+    rng = np.random.default_rng(2)
+    X = rng.integers(0, 3, (5000, 8)).astype(np.float32)  # massive exact ties
+    Q = rng.integers(0, 3, (100, 8)).astype(np.float32)
+    for k in (1, 10, 32):
+        ids, dists = rbc.brute_knn(X, Q, k)
+        rid, rd = oracle.knn(X, Q, k)
+        assert_same(ids, dists, rid, rd, rbc)
+
+
+def test_range_count(rbc, oracle):
+    X, Q = sample_inputs()
+    g = load_golden("sample_input")
+    for col in (0, 9, 31):
+        ranges = g["dists_l2"][:, col].copy()
+        cnt = rbc.range_count(X, Q, ranges).cpu().numpy()
+        np.testing.assert_array_equal(cnt.astype(np.uint32), oracle.range_count(X, Q, ranges))
+
+
+# ------------------------------------------------------------------ golden fixtures
+def test_sample_input_golden(rbc):
+    X, Q = sample_inputs()
+    g = load_golden("sample_input")
+    for metric, tag in ((0, "l2"), (1, "l1")):
+        ids, dists = rbc.brute_knn(X, Q, 32, metric)
+        assert_same(ids, dists, g[f"ids_{tag}"], g[f"dists_{tag}"], rbc)
+        idx = rbc.Index(X, 128, metric=metric, rep_ids=g["rep_ids"])
+        ids, dists = idx.query(Q, 32)
+        assert_same(ids, dists, g[f"ids_{tag}"], g[f"dists_{tag}"], rbc)
+        idx.close()
+    np.testing.assert_array_equal(rbc.u32(rbc.brute_knn(X, Q, 1)[0])[:, 0], g["ref_bruteCPU_1nn"])
+
+
+@pytest.mark.parametrize("name", ["synth_uniform_c1mini", "synth_mixture_d32", "synth_geometric_d128"])
+def test_synth_golden(rbc, name):
+    g = load_golden(name)
+    kind, seed, n, m, d, k, ncomp, nr = (int(v) for v in g["spec"])
+    slo, shi = (float(v) for v in g["sigma"])
+    X = rbc.synth(kind, seed, 0, n, d, ncomp=ncomp, sigma_lo=slo, sigma_hi=shi)
+    Q = rbc.synth(kind, seed, 1, m, d, ncomp=ncomp, sigma_lo=slo, sigma_hi=shi)
+    for metric, tag in ((0, "l2"), (1, "l1")):
+        idx = rbc.Index(X, nr, metric=metric, rep_ids=g["rep_ids"])
+        ids, dists = idx.query(Q, k)
+        assert_same(ids, dists, g[f"ids_{tag}"], g[f"dists_{tag}"], rbc)
+        if metric == 0:
+            off, mem, rad = idx.partition()
+            np.testing.assert_array_equal(off, g["part_offsets"])
+            np.testing.assert_array_equal(mem, g["part_members"])
+            np.testing.assert_array_equal(rad, g["part_radius"])
+        idx.close()
+
+
+# ------------------------------------------------------------------ build structures
+def test_partition_equals_oracle(rbc, oracle):
+    rng = np.random.default_rng(4)
+    X = rng.random((20000, 20), dtype=np.float32)
+    X[100:140] = X[7]  # duplicates: owner ties go to the lower rep index
+    for metric in (0, 1):
+        idx = rbc.Index(X, 300, metric=metric, seed=12)
+        reps = idx.reps()
+        assert len(set(reps.tolist())) == 300 and reps.max() < 20000
+        off, mem, rad = idx.partition()
+        _, _, roff, rmem, rrad = oracle.partition(X, reps, metric)
+        np.testing.assert_array_equal(off, roff)
+        np.testing.assert_array_equal(mem, rmem)
+        np.testing.assert_array_equal(rad, rrad)
+        inf = idx.info()
+        sizes = np.diff(off.astype(np.int64))
+        assert inf["min_list"] == sizes.min() and inf["max_list"] == sizes.max()
+        idx.close()
+
+
+@pytest.mark.parametrize("n,nr,s", [(4096, 64, 64), (5000, 40, 333), (3000, 32, 3000), (100, 32, 500)])
+def test_oneshot_build_and_query_equal_oracle(rbc, oracle, n, nr, s):
+    rng = np.random.default_rng(n + s)
+    X = rng.integers(0, 6, (n, 12)).astype(np.float32)  # heavy ties at every radius
+    Q = rng.integers(0, 6, (70, 12)).astype(np.float32)
+    reps = rng.choice(n, nr, replace=False).astype(np.uint32)
+    idx = rbc.Index(X, nr, s=s, flags=rbc.BUILD_PARTITION | rbc.BUILD_ONESHOT, rep_ids=reps)
+    lists, counts = idx.oneshot()
+    rl, rc, _ = oracle.oneshot_build(X, reps, min(s, n))
+    np.testing.assert_array_equal(counts, rc)
+    np.testing.assert_array_equal(lists, rl)
+    ids, dists = idx.query(Q, 32, mode=rbc.QUERY_ONESHOT)
+    oi, od = oracle.oneshot_query(X, reps, rl, rc, Q, 32)
+    assert_same(ids, dists, oi, od, rbc)
+    ids, dists = idx.query(Q, 32)  # exact mode on the same index
+    ri, rd = oracle.knn(X, Q, 32)
+    assert_same(ids, dists, ri, rd, rbc)
+    idx.close()
+
+
+# ------------------------------------------------------------------ exact RBC queries
+@pytest.mark.parametrize("metric", [0, 1])
+@pytest.mark.parametrize("case", [
+    # kind, n, m, d, nr, k, ncomp, sigma
+    (0, 65536, 1024, 16, 256, 1, 1, 0.0),     # config 1 shape (uniform, d=16), queries subsampled
+    (1, 50000, 500, 128, 1024, 32, 1000, 0.05),  # config 2 distribution, smaller n
+    (2, 30000, 300, 128, 173, 10, 1, 0.0),    # config 3 distribution (integer, tied)
+    (1, 40000, 400, 64, 200, 10, 100, 0.08),
+    (0, 3000, 1000, 5, 50, 32, 1, 0.0),
+])
+def test_rbc_exact_equals_oracle(rbc, oracle, metric, case):
+    kind, n, m, d, nr, k, ncomp, sg = case
+    X = rbc.synth(kind, 21, 0, n, d, ncomp=ncomp, sigma_lo=sg, sigma_hi=sg)
+    Q = rbc.synth(kind, 21, 1, m, d, ncomp=ncomp, sigma_lo=sg, sigma_hi=sg)
+    idx = rbc.Index(X, nr, metric=metric, seed=3)
+    ids, dists = idx.query(Q, k)
+    ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), k, metric)
+    assert_same(ids, dists, ri, rd, rbc)
+    st = idx.stats()
+    assert st["queries"] == m and st["point_pairs"] > 0
+    idx.close()
+
+
+def test_rbc_exact_edge_cases(rbc, oracle):
+    rng = np.random.default_rng(8)
+    # n < k, nr == n, single rep, all-duplicate database, queries on top of points
+    for n, nr, k in ((7, 7, 32), (50, 1, 10), (64, 64, 32)):
+        X = rng.standard_normal((n, 9)).astype(np.float32)
+        Q = np.concatenate([X[:3], rng.standard_normal((20, 9)).astype(np.float32)])
+        idx = rbc.Index(X, nr, seed=1)
+        ids, dists = idx.query(Q, k)
+        ri, rd = oracle.knn(X, Q, k)
+        assert_same(ids, dists, ri, rd, rbc)
+        idx.close()
+    X = np.ones((300, 4), np.float32)
+    idx = rbc.Index(X, 32, seed=2)
+    ids, dists = idx.query(np.zeros((5, 4), np.float32), 32)
+    ri, rd = oracle.knn(X, np.zeros((5, 4), np.float32), 32)
+    assert_same(ids, dists, ri, rd, rbc)
+    idx.close()
+
+
+def test_query_strided_inputs_and_outputs(rbc, oracle):
+    import torch
+    rng = np.random.default_rng(9)
+    X = rng.standard_normal((3000, 20)).astype(np.float32)
+    Q = rng.standard_normal((100, 20)).astype(np.float32)
+    Xt = torch.zeros((3000, 27), device="cuda")
+    Xt[:, :20] = torch.from_numpy(X)
+    Xt[:, 20:] = 5.0  # garbage beyond d must be ignored
+    idx = rbc.Index(Xt[:, :20], 64, seed=4)
+    Qt = torch.full((100, 23), 7.0, device="cuda")
+    Qt[:, :20] = torch.from_numpy(Q)
+    ids = torch.zeros((100, 40), dtype=torch.int32, device="cuda")
+    dists = torch.zeros((100, 40), dtype=torch.float32, device="cuda")
+    idx.query(Qt[:, :20], 10, out=(ids, dists))
+    ri, rd = oracle.knn(X, Q, 10)
+    assert_same(ids[:, :10], dists[:, :10], ri, rd, rbc)
+    assert (ids[:, 10:] == 0).all()
+    idx.close()
+
+
+def test_query_host_api(rbc, oracle):
+    X, Q = sample_inputs()
+    idx = rbc.Index(X, 100, seed=5)
+    ids, dists = idx.query_host(Q, 32)
+    ri, rd = oracle.knn(X, Q, 32)
+    np.testing.assert_array_equal(ids, ri)
+    np.testing.assert_array_equal(dists, rd)
+    idx.close()
+
+
+def test_repeated_queries_are_deterministic(rbc):
+    X = rbc.synth(1, 5, 0, 20000, 32, ncomp=50, sigma_lo=0.05, sigma_hi=0.05)
+    Q = rbc.synth(1, 5, 1, 999, 32, ncomp=50, sigma_lo=0.05, sigma_hi=0.05)
+    idx = rbc.Index(X, 128, seed=6)
+    a = idx.query(Q, 10)
+    for _ in range(3):
+        b = idx.query(Q, 10)
+        assert (a[0] == b[0]).all() and (a[1] == b[1]).all()
+    idx.close()
