@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark: exact 10-NN queries/s at n = 10,000,000, d = 128 on GB300.
+
+Workload (the reference-benchmark configuration this engine is measured on):
+  database  n = 10,000,000 rows, d = 128, integer features drawn i.i.d. from a
+            geometric distribution with mean 20 clipped to 255 (stored as
+            float32), from the engine's counter-based generator, seed 3;
+  queries   m = 10,000 rows from the same distribution (independent stream);
+  search    exact 10-NN under squared L2, results sorted by (distance, id),
+            4,096 representatives.
+One step = one exact query call for all m queries with the index and the
+queries resident in HBM.  The 5.12 GB database is far larger than the 129 MB
+L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+Multi-GPU runs are independent replicas (queries do not need any exchange):
+one process per GPU under torchrun, each with its own index, value = all
+ranks' queries / the slowest rank's time.  `--impl reference` times the
+reference's CPU brute-force path on this host's cores instead.
+"""
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "randomballcover-gpu_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "exact 10-NN queries/s, n=10M d=128, learned+BF16 vs plain FP32 RBC, same GPU"
+UNIT = "queries/s"
+SEED = 3
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--n", type=int, default=10_000_000)
+    ap.add_argument("--m", type=int, default=10_000)
+    ap.add_argument("--d", type=int, default=128)
+    ap.add_argument("--k", type=int, default=10)
+    ap.add_argument("--reps", type=int, default=4096)
+    ap.add_argument("--cpu-queries-per-thread", type=int, default=6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def config(a, form):
+    return {"workload": f"exact {a.k}-NN, n={a.n:,} d={a.d} geometric(mean 20) integer features, "
+                        f"m={a.m:,} queries, squared L2",
+            "n": a.n, "d": a.d, "m": a.m, "k": a.k, "num_reps": a.reps, "form": form,
+            "l2_flush": "inputs larger than L2 (database 5.12 GB vs 129 MB L2); no flush between steps"}
+
+
+# ------------------------------------------------------------------ clocks
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={CLOCK_FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        sm = [float(r[1]) for r in rows if re.match(r"^[\d.]+$", r[1])]
+        mx = [float(r[2]) for r in rows if re.match(r"^[\d.]+$", r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ distributed
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        j = json.load(open(p))
+        return j["hbm_gbs"], j["bf16_tflops"], j.get("bf16_tflops_sustained"), "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def committed_traffic(kernel):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_traffic.md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([\d.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+# ------------------------------------------------------------------ CPU baselines
+def host_database(a, threads):
+    """The same synthetic matrices, generated on the host by the CPU recipe."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build(with_ref=False)
+    X = np.empty((a.n, a.d), np.float32)
+    T = oracle.geometric_table()
+    chunk = (a.n + threads - 1) // threads
+
+    def fill(t):
+        r0 = t * chunk
+        r1 = min(a.n, r0 + chunk)
+        if r1 > r0:
+            X[r0:r1] = oracle.synth(oracle.KIND_GEOMETRIC, SEED, 0, r1 - r0, a.d, r0=r0, table=T)
+
+    ths = [threading.Thread(target=fill, args=(t,)) for t in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    Q = oracle.synth(oracle.KIND_GEOMETRIC, SEED, 1, a.m, a.d, table=T)
+    return X, Q
+
+
+def cpu_knn_timed(X, Qs, k, threads):
+    """Time the reference's CPU path on Qs: its own bruteCPU (1-NN, compiled from
+    the reference sources) when that build is present, else the oracle's
+    restatement of the same distance loop with (dist, id) k-NN selection."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    if oracle.ref_available():
+        out = np.empty(Qs.shape[0], np.uint32)
+        shards = np.array_split(np.arange(Qs.shape[0]), threads)
+
+        def run(ix):
+            if len(ix):
+                q = np.ascontiguousarray(Qs[ix])
+                o = np.empty(len(ix), np.uint32)
+                oracle.ref_brute_cpu_raw(X, X.shape[0], X.shape[1], q, len(ix), o)
+                out[ix] = o
+
+        t0 = time.perf_counter()
+        ths = [threading.Thread(target=run, args=(ix,)) for ix in shards]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        return time.perf_counter() - t0, "reference", "bruteCPU (brute.cu:91-112), 1-NN"
+    t0 = time.perf_counter()
+    oracle.knn(X, Qs, k, threads=threads)
+    return time.perf_counter() - t0, "port", f"oracle restatement of distVec/bruteCPU, {k}-NN"
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    X, Q = host_database(a, threads)
+    per_step = 2 * threads
+    steps_done = 0
+
+    def step(i):
+        lo = (i * per_step) % a.m
+        qs = np.ascontiguousarray(Q[lo:lo + per_step])
+        if qs.shape[0] < per_step:
+            qs = np.ascontiguousarray(Q[:per_step])
+        return cpu_knn_timed(X, qs, a.k, threads)
+
+    for i in range(a.warmup):
+        step(i)
+    total = 0.0
+    kind = desc = None
+    for i in range(a.steps):
+        t, kind, desc = step(a.warmup + i)
+        total += t
+        steps_done += 1
+    value = per_step * steps_done / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * total / steps_done,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (counter-based generator, CPU recipe)", "config": config(a, "reference CPU brute force"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{per_step} queries per step over the full {a.n:,}-row database; {desc}"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ engine arm
+def run_engine(a):
+    import torch
+    import pyrbc
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def maxall(v):
+        if not dist:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    stream = torch.cuda.current_stream()
+    X = pyrbc.synth(pyrbc.SYNTH_GEOMETRIC, SEED, 0, a.n, a.d)
+    Q = pyrbc.synth(pyrbc.SYNTH_GEOMETRIC, SEED, 1, a.m, a.d)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    idx = pyrbc.Index(X, a.reps, seed=SEED)
+    build_s = time.perf_counter() - t0
+    info = idx.info()
+    idx.set_profiling(True)
+    ids = torch.empty((a.m, a.k), dtype=torch.int32, device="cuda")
+    dists = torch.empty((a.m, a.k), dtype=torch.float32, device="cuda")
+    for _ in range(a.warmup):
+        idx.query(Q, a.k, out=(ids, dists))
+    barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = pyrbc.kernel_launches()
+    search_ms = 0.0
+    search_launches = 0
+    point_pairs = 0
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(a.steps):
+        idx.query(Q, a.k, out=(ids, dists))
+        p = idx.profile()
+        search_ms += p["search_ms"]
+        search_launches += p["search_launches"]
+        point_pairs += idx.stats()["point_pairs"]
+    ev1.record(stream)
+    barrier()
+    launches = pyrbc.kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = maxall(ev0.elapsed_time(ev1))
+    value = world * a.m * a.steps / (ms / 1000.0)
+
+    # end to end through the host API: pinned host queries in, results out
+    Qh = Q.cpu().pin_memory()
+    ih = torch.empty((a.m, a.k), dtype=torch.int32).pin_memory()
+    dh = torch.empty((a.m, a.k), dtype=torch.float32).pin_memory()
+    idx.query_host(Qh.numpy(), a.k, out=(ih.numpy().view(np.uint32), dh.numpy()))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        idx.query_host(Qh.numpy(), a.k, out=(ih.numpy().view(np.uint32), dh.numpy()))
+    e2e_s = maxall(time.perf_counter() - t0)
+    e2e = {"value": world * a.m * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(a.m * a.d * 4),
+           "d2h_bytes_per_step": int(a.m * a.k * 8)}
+
+    # roofline of the dominant kernel (the list search)
+    hbm, bf16, bf16_sus, src = peaks()
+    flops_per_launch = point_pairs * 2 * a.d / max(search_launches, 1)
+    avg_launch_s = search_ms / max(search_launches, 1) / 1000.0
+    achieved = flops_per_launch / avg_launch_s / 1e12
+    sm_mhz = clk.get("sm_mhz") or 1920.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # FP32 CUDA-core FMA rate at the sampled clock
+    traffic = committed_traffic("search_kernel")
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                "frac": achieved / bf16, "traffic": traffic,
+                "kernel": "search_kernel (plain FP32 difference form)", "peak_source": f"{src} bf16 dense burst",
+                "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
+                "fp32_core": {"achieved_tflops": achieved, "peak_tflops": fp32_peak,
+                              "frac": achieved / fp32_peak,
+                              "note": "difference form costs sub+mul+add per pair-dim, 2 flops counted"}}
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        nq = a.cpu_queries_per_thread * threads
+        Xh = X.cpu().numpy()
+        Qs = Q[:nq].cpu().numpy()
+        t, kind, desc = cpu_knn_timed(Xh, Qs, a.k, threads)
+        cpu = {"value": nq / t, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"{nq} of the {a.m:,} queries over the full {a.n:,}-row database; {desc}"}
+
+    if rank == 0:
+        st = idx.stats()
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (counter-based generator on the GPU)",
+                "config": dict(config(a, "plain FP32 exact RBC"), parallelism=f"replicas{world}"),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+                "clocks": clk,
+                "extra": {"build_s": build_s, "min_list": info["min_list"], "max_list": info["max_list"],
+                          "point_pairs_per_query": st["point_pairs"] / a.m,
+                          "lists_per_query": st["lists_probed"] / a.m}}
+        print(json.dumps(line), flush=True)
+    idx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_engine(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -48,10 +48,15 @@ extern "C" {
 /* ---- build flags ---- */
 #define RBC_BUILD_PARTITION 1u /* nearest-representative lists for exact search */
 #define RBC_BUILD_ONESHOT 2u   /* the reference's lists: s nearest points per rep */
+#define RBC_BUILD_BF16 4u      /* BF16 copy of the lists for tensor-core search   */
 
 /* ---- query modes ---- */
-#define RBC_QUERY_EXACT 0u   /* exact k-NN: triangle-inequality pruning of lists */
-#define RBC_QUERY_ONESHOT 1u /* reference one-shot: only the nearest rep's list  */
+#define RBC_QUERY_EXACT 0u    /* exact k-NN: triangle-inequality pruning of lists */
+#define RBC_QUERY_ONESHOT 1u  /* reference one-shot: only the nearest rep's list  */
+#define RBC_QUERY_EXACT_TC 2u /* exact k-NN with BF16 tensor-core distance tiles, an
+                                 FP32 rerank of a 40-row shortlist and a certified
+                                 error bound (falls back per query when uncertain);
+                                 L2 only, needs RBC_BUILD_BF16                      */
 
 /* ---- synthetic data kinds (counter-based, identical bits on host and GPU) ---- */
 #define RBC_SYNTH_UNIFORM 0   /* i.i.d. U[0,1)                                     */
@@ -83,6 +88,7 @@ typedef struct {               /* work done by the last rbc_query on an index */
   uint64_t rep_pairs;          /* query-to-representative distances           */
   uint64_t lists_probed;       /* (query, list) pairs searched                */
   uint64_t point_pairs;        /* (query, point) distances computed in lists  */
+  uint64_t fallback_queries;   /* tensor-core mode: queries recomputed in FP32 */
 } rbc_query_stats;
 
 const char *rbc_status_string(int status);

@@ -279,6 +279,30 @@ int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc
     }
   }
 
+  if (flags & RBC_BUILD_BF16) {
+    if (!(flags & RBC_BUILD_PARTITION))
+      return fail(RBC_ERR_INVALID, "rbc_build: RBC_BUILD_BF16 needs RBC_BUILD_PARTITION");
+    if (idx->metric != RBC_L2) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: the tensor-core form is L2 only");
+    if (!tc_supported(idx->dp)) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: the tensor-core form needs d <= 128");
+    idx->kp = tc_kp(d);
+    idx->n_pad = (n + 127) / 128 * 128;
+    const size_t xb_bytes = (size_t)idx->n_pad * idx->kp * 2;
+    CK(cudaMalloc(&idx->Xb, xb_bytes));
+    CK(cudaMalloc(&idx->xn, idx->n_pad * 4));
+    idx->device_bytes += xb_bytes + idx->n_pad * 4;
+    DevBuf fl;
+    CK(fl.alloc(8, s));
+    CK(cudaMemsetAsync(fl.p, 0, 8, s));
+    CK(launch_to_bf16(idx->Xp, ld, n, idx->n_pad, d, idx->kp, idx->Xb, idx->xn, INFINITY, fl.as<uint32_t>(),
+                      fl.as<uint32_t>() + 1, s));
+    uint32_t h[2];
+    CK(cudaMemcpyAsync(h, fl.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    idx->x_inexact = h[0];
+    std::memcpy(&idx->maxnorm, &h[1], 4);
+    CK(tc_make_map(&idx->tmB, idx->Xb, idx->n_pad, idx->kp, 128));
+  }
+
   if (flags & RBC_BUILD_ONESHOT) {
     const uint32_t s_eff = (uint32_t)std::min<uint64_t>(p->s, n);
     idx->s = s_eff;
@@ -325,9 +349,13 @@ int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc
 }
 
 // ------------------------------------------------------------------ query
+int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, bool nosync, uint32_t *dIds,
+             float *dDists, uint32_t ldo, cudaStream_t s);
+
 // Exact mode: nearest-rep probe round, then the pruned round over every other
 // list (plan.cu).  One-shot mode: the probe round alone over the one-shot
 // lists, which is the reference's kqueryRBC algorithm (rbc.cu:72-123).
+// Tensor mode: query_tc.
 int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
                 uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s) {
   if (!idx) return fail(RBC_ERR_INVALID, "rbc_query: index is NULL");
@@ -352,6 +380,9 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     X = idx->Xo;
     pid = idx->os_ids;
     offsets = idx->os_offsets;
+  } else if (base == RBC_QUERY_EXACT_TC) {
+    if (!(idx->flags & RBC_BUILD_BF16)) return fail(RBC_ERR_INVALID, "rbc_query: index has no BF16 lists");
+    return query_tc(idx, dQ, m, ldq, k, nosync, dIds, dDists, ldo, s);
   } else {
     return fail(RBC_ERR_INVALID, "rbc_query: unknown mode");
   }
@@ -403,6 +434,7 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   }
   idx->stats.queries = m;
   idx->stats.rep_pairs = m * nr;
+  idx->stats.fallback_queries = 0;
   if (!nosync) {
     unsigned long long st[2] = {0, 0};
     uint32_t ctl[3] = {0, 0, 0};
@@ -421,6 +453,126 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
         idx->prof.search_ms += ms;
       }
     }
+  }
+  return RBC_OK;
+}
+
+// Tensor-core exact query (tc_search.cu): every 128-query tile is compared on
+// the tensor cores with every 128-row tile of the BF16 lists, work units are
+// (query tile, row chunk) pairs in chunk-major order so the CTAs in flight
+// share their B tiles through L2; then the FP32 rerank certifies each query
+// and the uncertified ones are recomputed by the plain exact path.
+int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, bool nosync, uint32_t *dIds,
+             float *dDists, uint32_t ldo, cudaStream_t s) {
+  pool_setup();
+  const uint32_t ld = idx->ld, kp = idx->kp;
+  const uint64_t m_pad = (m + 127) / 128 * 128;
+  const int grid = tc_grid();
+  DevBuf Qp, Qb, qn, qinex, sl_a, sl_row, sl_theta, sl_lock, units, ctl, failq;
+  CK(Qp.alloc(m * ld * 4, s));
+  CK(Qb.alloc(m_pad * kp * 2, s));
+  CK(qn.alloc(m_pad * 4, s));
+  CK(qinex.alloc(m, s));
+  CK(sl_a.alloc(m_pad * kShortlist * 4, s));
+  CK(sl_row.alloc(m_pad * kShortlist * 4, s));
+  CK(sl_theta.alloc(m_pad * 4, s));
+  CK(sl_lock.alloc(m_pad * 4, s));
+  CK(ctl.alloc(64, s));
+  CK(failq.alloc(m * 4, s));
+  CK(cudaMemsetAsync(ctl.p, 0, 64, s));
+  CK(launch_pad_rows(dQ, ldq, Qp.as<float>(), ld, m, idx->d, s));
+  CK(launch_to_bf16(Qp.as<float>(), ld, m, m_pad, idx->d, kp, Qb.p, qn.as<float>(), 0.f, nullptr, nullptr, s));
+  CK(launch_row_inexact(Qp.as<float>(), ld, m, idx->d, qinex.as<uint8_t>(), s));
+  CUtensorMap tmA;
+  CK(tc_make_map(&tmA, Qb.p, m_pad, kp, 128));
+  // units: chunk-major so that concurrent CTAs read the same rows
+  const uint32_t T = (uint32_t)(m_pad / 128);
+  const uint64_t nb = idx->n_pad / 128;
+  uint64_t nchunks = std::max<uint64_t>(1, std::min<uint64_t>(nb, ((uint64_t)grid * 32 + T - 1) / T));
+  const uint64_t per = (nb + nchunks - 1) / nchunks;
+  nchunks = (nb + per - 1) / per;
+  std::vector<TcUnit> hu;
+  hu.reserve(nchunks * T);
+  for (uint64_t c = 0; c < nchunks; c++)
+    for (uint32_t t = 0; t < T; t++) hu.push_back(TcUnit{t, 0, c * per * 128, std::min(nb, (c + 1) * per) * 128});
+  CK(units.alloc(hu.size() * sizeof(TcUnit), s));
+  CK(cudaMemcpyAsync(units.p, hu.data(), hu.size() * sizeof(TcUnit), cudaMemcpyHostToDevice, s));
+  CK(launch_sl_init(sl_a.as<float>(), sl_row.as<uint32_t>(), sl_theta.as<uint32_t>(), sl_lock.as<uint32_t>(), m_pad,
+                    s));
+  TcArgs ta{};
+  ta.units = units.as<TcUnit>();
+  ta.nunits = (uint32_t)hu.size();
+  ta.kblocks = kp / 64;
+  ta.xn = idx->xn;
+  ta.sl_a = sl_a.as<float>();
+  ta.sl_row = sl_row.as<uint32_t>();
+  ta.sl_theta = sl_theta.as<uint32_t>();
+  ta.sl_lock = sl_lock.as<uint32_t>();
+  ta.err = ctl.as<uint32_t>();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  idx->ev_used = 0;
+  if (idx->profile) {
+    while (idx->ev_pool.size() < 2) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      idx->ev_pool.push_back(e);
+    }
+    e0 = idx->ev_pool[0];
+    e1 = idx->ev_pool[1];
+    idx->ev_used = 2;
+    CK(cudaEventRecord(e0, s));
+  }
+  CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
+  if (e1) CK(cudaEventRecord(e1, s));
+  RerankArgs ra{};
+  ra.X = idx->Xp;
+  ra.pid = idx->perm;
+  ra.Q = Qp.as<float>();
+  ra.ld = ld;
+  ra.dp = idx->dp;
+  ra.k = k;
+  ra.m = m;
+  ra.sl_a = sl_a.as<float>();
+  ra.sl_row = sl_row.as<uint32_t>();
+  ra.qn = qn.as<float>();
+  ra.q_inexact = qinex.as<uint8_t>();
+  ra.x_inexact = idx->x_inexact;
+  ra.maxnorm = idx->maxnorm;
+  ra.ids = dIds;
+  ra.dists = dDists;
+  ra.ldo = ldo;
+  ra.nfail = ctl.as<uint32_t>() + 1;
+  ra.fail = failq.as<uint32_t>();
+  CK(launch_rerank(idx->metric, ra, s));
+  (void)nosync;  // the fallback decision needs the certificate count on the host
+  uint32_t hc[2];
+  CK(cudaMemcpyAsync(hc, ctl.p, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (hc[0]) return fail(RBC_ERR_ITER_LIMIT, "rbc_query: a bounded device wait ran out in the tensor search");
+  const uint32_t nfail = hc[1];
+  if (nfail) {
+    DevBuf Qf, fi, fd;
+    CK(Qf.alloc((uint64_t)nfail * ld * 4, s));
+    CK(fi.alloc((uint64_t)nfail * k * 4, s));
+    CK(fd.alloc((uint64_t)nfail * k * 4, s));
+    CK(launch_gather_rows(Qp.as<float>(), ld, failq.as<uint32_t>(), nfail, Qf.as<float>(), s));
+    rbc_profile keep = idx->prof;
+    TRY(query_index(idx, Qf.as<float>(), nfail, ld, k, RBC_QUERY_EXACT, fi.as<uint32_t>(), fd.as<float>(), k, s));
+    idx->prof = keep;
+    CK(launch_scatter_results(fi.as<uint32_t>(), fd.as<float>(), failq.as<uint32_t>(), nfail, k, dIds, dDists, ldo,
+                              s));
+    CK(cudaStreamSynchronize(s));
+  }
+  idx->stats.queries = m;
+  idx->stats.rep_pairs = 0;
+  idx->stats.lists_probed = m * (uint64_t)idx->nr;
+  idx->stats.point_pairs = m * idx->n;
+  idx->stats.fallback_queries = nfail;
+  if (idx->profile) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    idx->prof.search_launches = 1;
+    idx->prof.search_ms = ms;
   }
   return RBC_OK;
 }
@@ -555,8 +707,8 @@ int rbc_build_host(const float *hX, uint64_t n, uint32_t d, uint32_t ldx, const 
 
 int rbc_destroy(rbc_index *idx) {
   if (!idx) return RBC_OK;
-  void *ptrs[] = {idx->Xp, idx->perm, idx->offsets, idx->radius, idx->R, idx->os_lists,
-                  idx->os_counts, idx->os_ids, idx->os_offsets, idx->Xo, idx->Xi};
+  void *ptrs[] = {idx->Xp,      idx->perm,   idx->offsets, idx->radius,     idx->R,  idx->os_lists, idx->os_counts,
+                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->Xb, idx->xn};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : idx->ev_pool) cudaEventDestroy(e);

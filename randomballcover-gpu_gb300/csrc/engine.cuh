@@ -9,6 +9,7 @@
 
 #include "../../include/rbc_gb300.h"
 #include "kernels.cuh"
+#include "tc.cuh"
 
 namespace rbc {
 
@@ -65,6 +66,14 @@ struct rbc_index {
   uint32_t *os_ids = nullptr;     // nr x s packed ids: row -> id map of Xo
   uint64_t *os_offsets = nullptr; // nr + 1 rows of Xo per list
   float *Xo = nullptr;            // list-major copy of the one-shot lists' rows
+  // BF16 copy of the partition rows for tensor-core search (RBC_BUILD_BF16)
+  void *Xb = nullptr;             // n_pad x kp BF16, list-major, zero padded
+  float *xn = nullptr;            // n_pad squared row norms (+inf past n)
+  uint64_t n_pad = 0;
+  uint32_t kp = 0;
+  uint32_t x_inexact = 1;         // some value is not exact in BF16
+  float maxnorm = 0.f;            // largest row norm
+  CUtensorMap tmB;                // TMA map of Xb (128-row boxes, 128-byte swizzle)
   // padded copy of the input in original order (legacy rbcStruct.dx)
   float *Xi = nullptr;
   uint64_t xi_rows = 0;

@@ -55,6 +55,10 @@ cudaError_t launch_init_results(float *res_d, uint32_t *res_i, uint32_t *tau, ui
                                 uint64_t m, cudaStream_t s);
 cudaError_t launch_write_results(const float *res_d, const uint32_t *res_i, uint64_t m, uint32_t k,
                                  uint32_t *ids, float *dists, uint32_t ldo, cudaStream_t s);
+// ids[rows[r] * ldo + j] = src_i[r * k + j] (and the distances likewise).
+cudaError_t launch_scatter_results(const uint32_t *src_i, const float *src_d, const uint32_t *rows,
+                                   uint32_t nrows, uint32_t k, uint32_t *ids, float *dists, uint32_t ldo,
+                                   cudaStream_t s);
 cudaError_t launch_brute_items(SearchItem *items, uint32_t *nitems, uint32_t *qidx, uint64_t n,
                                uint32_t chunk, uint64_t m, uint32_t qtile, cudaStream_t s);
 

@@ -270,6 +270,15 @@ __global__ void write_results_kernel(const float *res_d, const uint32_t *res_i, 
   if (dists) dists[q * ldo + j] = res_d[q * kListWidth + j];
 }
 
+__global__ void scatter_results_kernel(const uint32_t *src_i, const float *src_d, const uint32_t *rows, uint32_t nrows,
+                                       uint32_t k, uint32_t *ids, float *dists, uint32_t ldo) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)nrows * k) return;
+  uint32_t r = (uint32_t)(i / k), j = (uint32_t)(i - (uint64_t)r * k);
+  if (ids) ids[(uint64_t)rows[r] * ldo + j] = src_i[i];
+  if (dists) dists[(uint64_t)rows[r] * ldo + j] = src_d[i];
+}
+
 __global__ void brute_items_kernel(SearchItem *items, uint32_t *nitems, uint32_t *qidx, uint64_t n,
                                    uint32_t chunk, uint64_t m, uint32_t qtile) {
   const uint64_t nchunks = (n + chunk - 1) / chunk;
@@ -331,6 +340,14 @@ cudaError_t launch_write_results(const float *res_d, const uint32_t *res_i, uint
   if (total == 0) return cudaSuccess;
   write_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(res_d, res_i, m, k, ids,
                                                                        dists, ldo);
+  return launched();
+}
+
+cudaError_t launch_scatter_results(const uint32_t *src_i, const float *src_d, const uint32_t *rows, uint32_t nrows,
+                                   uint32_t k, uint32_t *ids, float *dists, uint32_t ldo, cudaStream_t s) {
+  uint64_t total = (uint64_t)nrows * k;
+  if (total == 0) return cudaSuccess;
+  scatter_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(src_i, src_d, rows, nrows, k, ids, dists, ldo);
   return launched();
 }
 

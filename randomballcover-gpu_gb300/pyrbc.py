@@ -17,8 +17,8 @@ LIB_PATH = os.path.join(HERE, "librbcgb.so")
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_ITER_LIMIT, ERR_UNSUPPORTED, ERR_IO = range(7)
 L2, L1 = 0, 1
 KMAX = 32
-BUILD_PARTITION, BUILD_ONESHOT = 1, 2
-QUERY_EXACT, QUERY_ONESHOT = 0, 1
+BUILD_PARTITION, BUILD_ONESHOT, BUILD_BF16 = 1, 2, 4
+QUERY_EXACT, QUERY_ONESHOT, QUERY_EXACT_TC = 0, 1, 2
 SYNTH_UNIFORM, SYNTH_MIXTURE, SYNTH_GEOMETRIC = 0, 1, 2
 DUMMY = 0xFFFFFFFF
 FLT_MAX = float(np.finfo(np.float32).max)
@@ -43,7 +43,7 @@ class IndexInfo(C.Structure):
 
 class QueryStats(C.Structure):
     _fields_ = [("queries", C.c_uint64), ("rep_pairs", C.c_uint64), ("lists_probed", C.c_uint64),
-                ("point_pairs", C.c_uint64)]
+                ("point_pairs", C.c_uint64), ("fallback_queries", C.c_uint64)]
 
 
 class Profile(C.Structure):

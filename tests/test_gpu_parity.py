@@ -209,6 +209,41 @@ def test_query_host_api(rbc, oracle):
     idx.close()
 
 
+# ------------------------------------------------------------------ tensor-core (precision) form
+@pytest.mark.parametrize("case", [
+    # kind, n, m, d, nr, k, ncomp, sigma
+    (2, 60000, 300, 128, 256, 10, 1, 0.0),     # config 3 distribution: BF16-exact integers
+    (2, 20011, 257, 128, 100, 32, 1, 0.0),     # ragged n and m, k = 32
+    (1, 30000, 200, 128, 200, 10, 300, 0.05),  # float mixture: BF16 rounding, certificate + fallback
+    (0, 9000, 130, 16, 64, 1, 1, 0.0),         # d = 16 (one 64-wide K block, zero padded)
+    (2, 5000, 100, 100, 50, 10, 1, 0.0),       # d not a multiple of 64
+])
+def test_tensor_core_exact_equals_oracle(rbc, oracle, case):
+    kind, n, m, d, nr, k, ncomp, sg = case
+    X = rbc.synth(kind, 31, 0, n, d, ncomp=ncomp, sigma_lo=sg, sigma_hi=sg)
+    Q = rbc.synth(kind, 31, 1, m, d, ncomp=ncomp, sigma_lo=sg, sigma_hi=sg)
+    idx = rbc.Index(X, nr, seed=2, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    ids, dists = idx.query(Q, k, mode=rbc.QUERY_EXACT_TC)
+    ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), k)
+    assert_same(ids, dists, ri, rd, rbc)
+    st = idx.stats()
+    if kind == 2:
+        assert st["fallback_queries"] == 0, st  # integer data certifies every query
+    ids2, dists2 = idx.query(Q, k)  # the plain form on the same index agrees
+    assert (ids2 == ids).all() and (dists2 == dists).all()
+    idx.close()
+
+
+def test_tensor_core_rejects_l1_and_missing_lists(rbc):
+    X = rbc.synth(0, 1, 0, 1000, 16)
+    with pytest.raises(rbc.RBCError):
+        rbc.Index(X, 32, metric=rbc.L1, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    idx = rbc.Index(X, 32)
+    with pytest.raises(rbc.RBCError):
+        idx.query(X[:10], 5, mode=rbc.QUERY_EXACT_TC)
+    idx.close()
+
+
 def test_repeated_queries_are_deterministic(rbc):
     X = rbc.synth(1, 5, 0, 20000, 32, ncomp=50, sigma_lo=0.05, sigma_hi=0.05)
     Q = rbc.synth(1, 5, 1, 999, 32, ncomp=50, sigma_lo=0.05, sigma_hi=0.05)
