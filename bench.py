@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--reps", type=int, default=4096)
     ap.add_argument("--cpu-queries-per-thread", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", default="tensor", choices=["tensor", "plain"],
+                    help="headline form; 'tensor' also times the plain FP32 form on the same index")
     return ap.parse_args()
 
 
@@ -248,66 +250,84 @@ def run_engine(a):
     Q = pyrbc.synth(pyrbc.SYNTH_GEOMETRIC, SEED, 1, a.m, a.d)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    idx = pyrbc.Index(X, a.reps, seed=SEED)
+    idx = pyrbc.Index(X, a.reps, seed=SEED, flags=pyrbc.BUILD_PARTITION | pyrbc.BUILD_BF16)
     build_s = time.perf_counter() - t0
     info = idx.info()
     idx.set_profiling(True)
     ids = torch.empty((a.m, a.k), dtype=torch.int32, device="cuda")
     dists = torch.empty((a.m, a.k), dtype=torch.float32, device="cuda")
-    for _ in range(a.warmup):
-        idx.query(Q, a.k, out=(ids, dists))
-    barrier()
+    forms = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC}
+    head = "plain" if a.form == "plain" else "tensor"
 
-    clocks = ClockSampler(local)
-    clocks.start()
-    launches0 = pyrbc.kernel_launches()
-    search_ms = 0.0
-    search_launches = 0
-    point_pairs = 0
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(a.steps):
-        idx.query(Q, a.k, out=(ids, dists))
-        p = idx.profile()
-        search_ms += p["search_ms"]
-        search_launches += p["search_launches"]
-        point_pairs += idx.stats()["point_pairs"]
-    ev1.record(stream)
-    barrier()
-    launches = pyrbc.kernel_launches() - launches0
-    clk = clocks.stop()
-    ms = maxall(ev0.elapsed_time(ev1))
-    value = world * a.m * a.steps / (ms / 1000.0)
+    def timed(mode, steps, warmup, sample_clocks=False):
+        for _ in range(warmup):
+            idx.query(Q, a.k, mode=mode, out=(ids, dists))
+        barrier()
+        clocks = ClockSampler(local) if sample_clocks else None
+        if clocks:
+            clocks.start()
+        l0 = pyrbc.kernel_launches()
+        acc = {"search_ms": 0.0, "search_launches": 0, "point_pairs": 0, "fallback": 0}
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            idx.query(Q, a.k, mode=mode, out=(ids, dists))
+            p = idx.profile()
+            st = idx.stats()
+            acc["search_ms"] += p["search_ms"]
+            acc["search_launches"] += p["search_launches"]
+            acc["point_pairs"] += st["point_pairs"]
+            acc["fallback"] += st["fallback_queries"]
+        ev1.record(stream)
+        barrier()
+        acc["launches"] = pyrbc.kernel_launches() - l0
+        acc["clocks"] = clocks.stop() if clocks else None
+        acc["ms"] = maxall(ev0.elapsed_time(ev1))
+        acc["value"] = world * a.m * steps / (acc["ms"] / 1000.0)
+        return acc
+
+    other = "plain" if head == "tensor" else None
+    side = timed(forms[other], min(a.steps, 3), 1) if other else None
+    res = timed(forms[head], a.steps, a.warmup, sample_clocks=True)
+    ref_ids = ids.clone()
+    if side:  # both forms return the same exact neighbours
+        idx.query(Q, a.k, mode=forms[other], out=(ids, dists))
+        same_as_plain = bool((ids == ref_ids).all().item())
+    clk = res["clocks"]
+    value = res["value"]
+    ms = res["ms"]
+    launches = res["launches"]
 
     # end to end through the host API: pinned host queries in, results out
     Qh = Q.cpu().pin_memory()
     ih = torch.empty((a.m, a.k), dtype=torch.int32).pin_memory()
     dh = torch.empty((a.m, a.k), dtype=torch.float32).pin_memory()
-    idx.query_host(Qh.numpy(), a.k, out=(ih.numpy().view(np.uint32), dh.numpy()))
+    idx.query_host(Qh.numpy(), a.k, mode=forms[head], out=(ih.numpy().view(np.uint32), dh.numpy()))
     barrier()
     t0 = time.perf_counter()
     for _ in range(a.steps):
-        idx.query_host(Qh.numpy(), a.k, out=(ih.numpy().view(np.uint32), dh.numpy()))
+        idx.query_host(Qh.numpy(), a.k, mode=forms[head], out=(ih.numpy().view(np.uint32), dh.numpy()))
     e2e_s = maxall(time.perf_counter() - t0)
     e2e = {"value": world * a.m * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(a.m * a.d * 4),
            "d2h_bytes_per_step": int(a.m * a.k * 8)}
 
-    # roofline of the dominant kernel (the list search)
+    # roofline of the dominant kernel; algorithmic work = 2 d flops per
+    # (query, database row) pair the search evaluates
     hbm, bf16, bf16_sus, src = peaks()
-    flops_per_launch = point_pairs * 2 * a.d / max(search_launches, 1)
-    avg_launch_s = search_ms / max(search_launches, 1) / 1000.0
+    flops_per_launch = res["point_pairs"] * 2 * a.d / max(res["search_launches"], 1)
+    avg_launch_s = res["search_ms"] / max(res["search_launches"], 1) / 1000.0
     achieved = flops_per_launch / avg_launch_s / 1e12
-    sm_mhz = clk.get("sm_mhz") or 1920.0
+    sm_mhz = (clk or {}).get("sm_mhz") or 1920.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # FP32 CUDA-core FMA rate at the sampled clock
-    traffic = committed_traffic("search_kernel")
+    kernel = "tc_search_kernel" if head == "tensor" else "search_kernel"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                "frac": achieved / bf16, "traffic": traffic,
-                "kernel": "search_kernel (plain FP32 difference form)", "peak_source": f"{src} bf16 dense burst",
-                "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
-                "fp32_core": {"achieved_tflops": achieved, "peak_tflops": fp32_peak,
-                              "frac": achieved / fp32_peak,
-                              "note": "difference form costs sub+mul+add per pair-dim, 2 flops counted"}}
+                "frac": achieved / bf16, "traffic": committed_traffic(kernel), "kernel": kernel,
+                "peak_source": f"{src} bf16 dense burst (MEASURED_PEAKS.json)",
+                "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
+    if head == "plain":
+        roofline["fp32_core"] = {"achieved_tflops": achieved, "peak_tflops": fp32_peak, "frac": achieved / fp32_peak,
+                                 "note": "difference form costs sub+mul+add per pair-dim, 2 flops counted"}
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
@@ -320,17 +340,21 @@ def run_engine(a):
                "sample": f"{nq} of the {a.m:,} queries over the full {a.n:,}-row database; {desc}"}
 
     if rank == 0:
-        st = idx.stats()
+        form_name = {"tensor": "exact RBC, BF16 tcgen05 distance tiles + FP32 rerank (certified)",
+                     "plain": "plain FP32 exact RBC"}[head]
+        extra = {"build_s": build_s, "min_list": info["min_list"], "max_list": info["max_list"],
+                 "point_pairs_per_query": res["point_pairs"] / (a.m * a.steps),
+                 "fallback_queries_per_step": res["fallback"] / a.steps}
+        if side:
+            extra.update({"plain_fp32_value": side["value"], "plain_fp32_ms_per_step": side["ms"] / min(a.steps, 3),
+                          "speedup_vs_plain_fp32": value / side["value"], "same_ids_as_plain": same_as_plain})
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32" if head == "tensor" else "f32",
                 "data": "synthetic (counter-based generator on the GPU)",
-                "config": dict(config(a, "plain FP32 exact RBC"), parallelism=f"replicas{world}"),
+                "config": dict(config(a, form_name), parallelism=f"replicas{world}"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk,
-                "extra": {"build_s": build_s, "min_list": info["min_list"], "max_list": info["max_list"],
-                          "point_pairs_per_query": st["point_pairs"] / a.m,
-                          "lists_per_query": st["lists_probed"] / a.m}}
+                "clocks": clk, "extra": extra}
         print(json.dumps(line), flush=True)
     idx.close()
     if dist:
