@@ -137,6 +137,21 @@ uint64_t rbc_kernel_launches(void);
 int rbc_brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m,
                   uint32_t ldq, uint32_t d, uint32_t k, int metric, uint32_t *dIds, float *dDists,
                   uint32_t ldo, void *stream);
+/* Brute-force exact k-NN that allocates no memory (no counterpart in the
+ * reference).  For callers that cannot allocate device memory at call time:
+ * services whose memory budget is fully reserved up front by their own
+ * allocator, latency-bound callers that must not wait on an allocator, and
+ * code running inside another allocator's callback.  Results equal
+ * rbc_brute_knn's.  Its working memory is one fixed device array of about
+ * 2.4 MB held by every GPU that loads the library.  Limits: m <= 8192 queries
+ * per call, d a multiple of 4 and at most 512, ldx == ldq a multiple of 4,
+ * dX and dQ 16-byte aligned; other shapes return RBC_ERR_UNSUPPORTED.  All
+ * calls share the array, so calls that overlap on the GPU race: order them on
+ * one stream.  The first call on each device looks the array up and should
+ * come before any stream capture. */
+int rbc_brute_knn_noalloc(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m,
+                          uint32_t ldq, uint32_t d, uint32_t k, int metric, uint32_t *dIds,
+                          float *dDists, uint32_t ldo, void *stream);
 /* counts[i] = number of database rows with distance strictly below ranges[i]. */
 int rbc_brute_range_count(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m,
                           uint32_t ldq, uint32_t d, int metric, const float *dRanges,

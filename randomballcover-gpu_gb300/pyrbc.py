@@ -70,6 +70,7 @@ SIGNATURES = {
     "rbc_get_profile": ([_VP, C.POINTER(Profile)], _INT),
     "rbc_kernel_launches": ([], _U64),
     "rbc_brute_knn": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _INT, _VP, _VP, _U32, _VP], _INT),
+    "rbc_brute_knn_noalloc": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _INT, _VP, _VP, _U32, _VP], _INT),
     "rbc_brute_range_count": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _INT, _VP, _VP, _VP], _INT),
     "rbc_synth": ([_INT, _U64, _U64, _U64, _U64, _U32, _U32, _VP, _U32, _F, _F, _VP], _INT),
     "rbc_read_matrix_bin": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
