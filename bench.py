@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark: exact 10-NN queries/s at n = 10,000,000, d = 128 on GB300.
 
-Workload (the reference-benchmark configuration this engine is measured on):
+Workload (default, the configuration the headline metric is quoted on):
   database  n = 10,000,000 rows, d = 128, integer features drawn i.i.d. from a
             geometric distribution with mean 20 clipped to 255 (stored as
             float32), from the engine's counter-based generator, seed 3;
@@ -12,12 +12,24 @@ One step = one exact query call for all m queries with the index and the
 queries resident in HBM.  The 5.12 GB database is far larger than the 129 MB
 L2, so no flush is needed between steps.
 
+Forms timed on the same index (all exact, identical ids):
+  plain    FP32 list search on the CUDA cores (the plain RBC)
+  tensor   BF16 tcgen05 list search + FP32 rerank (certified)
+  learned  tensor form whose probe round follows the learned router, trained
+           on the GPU beforehand on queries labelled by the RBC itself
+The headline `value` is the learned+BF16 form, as the metric names it.
+
+`--workload c5` measures the learned-router configuration instead (n =
+4,194,304, 2,000-component Gaussian mixture with sigma ~ U[0.02, 0.1],
+4,096 representatives, router trained on 1,000,000 queries, 100,000 test
+queries) and reports probe recall and lists searched per query.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
 
-Multi-GPU runs are independent replicas (queries do not need any exchange):
-one process per GPU under torchrun, each with its own index, value = all
-ranks' queries / the slowest rank's time.  `--impl reference` times the
-reference's CPU brute-force path on this host's cores instead.
+Multi-GPU runs are independent replicas (queries need no exchange): one
+process per GPU under torchrun, each with its own index, value = all ranks'
+queries / the slowest rank's time.  `--impl reference` times the reference's
+CPU brute-force path on this host's cores instead.
 """
 import argparse
 import json
@@ -37,7 +49,16 @@ sys.path.insert(0, PKG)
 
 METRIC = "exact 10-NN queries/s, n=10M d=128, learned+BF16 vs plain FP32 RBC, same GPU"
 UNIT = "queries/s"
-SEED = 3
+
+WORKLOADS = {
+    # kind, seed, n, m, d, k, reps, ncomp, sigma_lo, sigma_hi, train queries, router epochs
+    "c3": dict(kind=2, seed=3, n=10_000_000, m=10_000, d=128, k=10, reps=4096, ncomp=1, slo=0.0, shi=0.0,
+               train=100_000, epochs=2,
+               desc="geometric(mean 20) integer features"),
+    "c5": dict(kind=1, seed=5, n=4_194_304, m=100_000, d=128, k=10, reps=4096, ncomp=2000, slo=0.02, shi=0.1,
+               train=1_000_000, epochs=3,
+               desc="2,000-component Gaussian mixture, sigma ~ U[0.02, 0.1]"),
+}
 
 
 def parse():
@@ -46,23 +67,30 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--n", type=int, default=10_000_000)
-    ap.add_argument("--m", type=int, default=10_000)
-    ap.add_argument("--d", type=int, default=128)
-    ap.add_argument("--k", type=int, default=10)
-    ap.add_argument("--reps", type=int, default=4096)
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--m", type=int, default=None)
+    ap.add_argument("--reps", type=int, default=None)
+    ap.add_argument("--train", type=int, default=None)
     ap.add_argument("--cpu-queries-per-thread", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", default="tensor", choices=["tensor", "plain"],
-                    help="headline form; 'tensor' also times the plain FP32 form on the same index")
-    return ap.parse_args()
+    ap.add_argument("--forms", default="plain,tensor,learned",
+                    help="forms to time; the last one listed is the headline")
+    a = ap.parse_args()
+    w = dict(WORKLOADS[a.workload])
+    for key in ("n", "m", "reps", "train"):
+        if getattr(a, key) is not None:
+            w[key] = getattr(a, key)
+    a.w = w
+    return a
 
 
 def config(a, form):
-    return {"workload": f"exact {a.k}-NN, n={a.n:,} d={a.d} geometric(mean 20) integer features, "
-                        f"m={a.m:,} queries, squared L2",
-            "n": a.n, "d": a.d, "m": a.m, "k": a.k, "num_reps": a.reps, "form": form,
-            "l2_flush": "inputs larger than L2 (database 5.12 GB vs 129 MB L2); no flush between steps"}
+    w = a.w
+    return {"workload": f"{a.workload}: exact {w['k']}-NN, n={w['n']:,} d={w['d']} {w['desc']}, "
+                        f"m={w['m']:,} queries, squared L2",
+            "n": w["n"], "d": w["d"], "m": w["m"], "k": w["k"], "num_reps": w["reps"], "form": form,
+            "l2_flush": "inputs larger than L2 (the database is GBs vs 129 MB L2); no flush between steps"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -109,7 +137,7 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-# ------------------------------------------------------------------ distributed
+# ------------------------------------------------------------------ helpers
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -132,28 +160,28 @@ def committed_traffic(kernel):
 
 
 # ------------------------------------------------------------------ CPU baselines
-def host_database(a, threads):
-    """The same synthetic matrices, generated on the host by the CPU recipe."""
+def host_matrix(w, stream, rows, threads):
+    """Rows of the synthetic matrix generated on the host by the CPU recipe."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build(with_ref=False)
-    X = np.empty((a.n, a.d), np.float32)
+    X = np.empty((rows, w["d"]), np.float32)
     T = oracle.geometric_table()
-    chunk = (a.n + threads - 1) // threads
+    chunk = (rows + threads - 1) // threads
 
     def fill(t):
         r0 = t * chunk
-        r1 = min(a.n, r0 + chunk)
+        r1 = min(rows, r0 + chunk)
         if r1 > r0:
-            X[r0:r1] = oracle.synth(oracle.KIND_GEOMETRIC, SEED, 0, r1 - r0, a.d, r0=r0, table=T)
+            X[r0:r1] = oracle.synth(w["kind"], w["seed"], stream, r1 - r0, w["d"], r0=r0, ncomp=w["ncomp"],
+                                    sigma_lo=w["slo"], sigma_hi=w["shi"], table=T)
 
     ths = [threading.Thread(target=fill, args=(t,)) for t in range(threads)]
     for t in ths:
         t.start()
     for t in ths:
         t.join()
-    Q = oracle.synth(oracle.KIND_GEOMETRIC, SEED, 1, a.m, a.d, table=T)
-    return X, Q
+    return X
 
 
 def cpu_knn_timed(X, Qs, k, threads):
@@ -190,17 +218,18 @@ def run_reference(a):
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    w = a.w
     threads = os.cpu_count() or 1
-    X, Q = host_database(a, threads)
+    X = host_matrix(w, 0, w["n"], threads)
+    Q = host_matrix(w, 1, min(w["m"], 4096), threads)
     per_step = 2 * threads
-    steps_done = 0
 
     def step(i):
-        lo = (i * per_step) % a.m
+        lo = (i * per_step) % Q.shape[0]
         qs = np.ascontiguousarray(Q[lo:lo + per_step])
         if qs.shape[0] < per_step:
             qs = np.ascontiguousarray(Q[:per_step])
-        return cpu_knn_timed(X, qs, a.k, threads)
+        return cpu_knn_timed(X, qs, w["k"], threads)
 
     for i in range(a.warmup):
         step(i)
@@ -209,14 +238,13 @@ def run_reference(a):
     for i in range(a.steps):
         t, kind, desc = step(a.warmup + i)
         total += t
-        steps_done += 1
-    value = per_step * steps_done / total
+    value = per_step * a.steps / total
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * total / steps_done,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * total / a.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (counter-based generator, CPU recipe)", "config": config(a, "reference CPU brute force"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": f"{per_step} queries per step over the full {a.n:,}-row database; {desc}"},
+                             "sample": f"{per_step} queries per step over the full {w['n']:,}-row database; {desc}"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -226,6 +254,7 @@ def run_engine(a):
     import torch
     import pyrbc
 
+    w = a.w
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     dist = None
@@ -246,86 +275,113 @@ def run_engine(a):
         return float(t.item())
 
     stream = torch.cuda.current_stream()
-    X = pyrbc.synth(pyrbc.SYNTH_GEOMETRIC, SEED, 0, a.n, a.d)
-    Q = pyrbc.synth(pyrbc.SYNTH_GEOMETRIC, SEED, 1, a.m, a.d)
+    synth = dict(ncomp=w["ncomp"], sigma_lo=w["slo"], sigma_hi=w["shi"])
+    X = pyrbc.synth(w["kind"], w["seed"], 0, w["n"], w["d"], **synth)
+    Q = pyrbc.synth(w["kind"], w["seed"], 1, w["m"], w["d"], **synth)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    idx = pyrbc.Index(X, a.reps, seed=SEED, flags=pyrbc.BUILD_PARTITION | pyrbc.BUILD_BF16)
+    idx = pyrbc.Index(X, w["reps"], seed=w["seed"], flags=pyrbc.BUILD_PARTITION | pyrbc.BUILD_BF16)
     build_s = time.perf_counter() - t0
     info = idx.info()
+    k, m = w["k"], w["m"]
+    forms = [f for f in a.forms.split(",") if f]
+    head = forms[-1]
+
+    # the learned router: trained on the GPU on queries the RBC labels
+    router_info = None
+    if "learned" in forms:
+        Qtr = pyrbc.synth(w["kind"], w["seed"], 2, w["train"], w["d"], **synth)
+        t0 = time.perf_counter()
+        labels = idx.owner_labels(Qtr)
+        torch.cuda.synchronize()
+        label_s = time.perf_counter() - t0
+        router = pyrbc.Router(w["d"], 512, w["reps"], seed=w["seed"])
+        t0 = time.perf_counter()
+        loss = router.train(Qtr, labels, epochs=w["epochs"], batch=1024, lr=2e-3, seed=w["seed"])
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t0
+        del Qtr, labels
+        test_labels = idx.owner_labels(Q).long()
+        top1 = router.logits(Q).argmax(1)
+        router_info = {"train_queries": w["train"], "epochs": w["epochs"], "label_s": label_s, "train_s": train_s,
+                       "final_loss": loss, "probe_recall_top1": (top1 == test_labels).float().mean().item(),
+                       "architecture": f"MLP {w['d']}->512->512->{w['reps']} GELU, BF16 weights, FP32 accumulate"}
+        idx.set_router(router, probes=2)
+
+    modes = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC,
+             "learned": pyrbc.QUERY_EXACT_TC | pyrbc.QUERY_ROUTED, "learned_plain": pyrbc.QUERY_EXACT | pyrbc.QUERY_ROUTED}
     idx.set_profiling(True)
-    ids = torch.empty((a.m, a.k), dtype=torch.int32, device="cuda")
-    dists = torch.empty((a.m, a.k), dtype=torch.float32, device="cuda")
-    forms = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC}
-    head = "plain" if a.form == "plain" else "tensor"
+    ids = torch.empty((m, k), dtype=torch.int32, device="cuda")
+    dists = torch.empty((m, k), dtype=torch.float32, device="cuda")
 
     def timed(mode, steps, warmup, sample_clocks=False):
         for _ in range(warmup):
-            idx.query(Q, a.k, mode=mode, out=(ids, dists))
+            idx.query(Q, k, mode=mode, out=(ids, dists))
         barrier()
         clocks = ClockSampler(local) if sample_clocks else None
         if clocks:
             clocks.start()
         l0 = pyrbc.kernel_launches()
-        acc = {"search_ms": 0.0, "search_launches": 0, "point_pairs": 0, "fallback": 0}
+        acc = {"search_ms": 0.0, "search_launches": 0, "point_pairs": 0, "lists": 0, "fallback": 0}
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
         for _ in range(steps):
-            idx.query(Q, a.k, mode=mode, out=(ids, dists))
+            idx.query(Q, k, mode=mode, out=(ids, dists))
             p = idx.profile()
             st = idx.stats()
             acc["search_ms"] += p["search_ms"]
             acc["search_launches"] += p["search_launches"]
             acc["point_pairs"] += st["point_pairs"]
+            acc["lists"] += st["lists_probed"]
             acc["fallback"] += st["fallback_queries"]
         ev1.record(stream)
         barrier()
         acc["launches"] = pyrbc.kernel_launches() - l0
         acc["clocks"] = clocks.stop() if clocks else None
         acc["ms"] = maxall(ev0.elapsed_time(ev1))
-        acc["value"] = world * a.m * steps / (acc["ms"] / 1000.0)
+        acc["steps"] = steps
+        acc["value"] = world * m * steps / (acc["ms"] / 1000.0)
+        acc["ids"] = ids.clone()
         return acc
 
-    other = "plain" if head == "tensor" else None
-    side = timed(forms[other], min(a.steps, 3), 1) if other else None
-    res = timed(forms[head], a.steps, a.warmup, sample_clocks=True)
-    ref_ids = ids.clone()
-    if side:  # both forms return the same exact neighbours
-        idx.query(Q, a.k, mode=forms[other], out=(ids, dists))
-        same_as_plain = bool((ids == ref_ids).all().item())
-    clk = res["clocks"]
-    value = res["value"]
-    ms = res["ms"]
-    launches = res["launches"]
+    results = {}
+    for f in forms:
+        if f == head:
+            results[f] = timed(modes[f], a.steps, a.warmup, sample_clocks=True)
+        else:
+            results[f] = timed(modes[f], min(a.steps, 3), 1)
+    res = results[head]
+    same = all(bool((r["ids"] == res["ids"]).all().item()) for r in results.values())
+    clk, value, ms, launches = res["clocks"], res["value"], res["ms"], res["launches"]
 
     # end to end through the host API: pinned host queries in, results out
     Qh = Q.cpu().pin_memory()
-    ih = torch.empty((a.m, a.k), dtype=torch.int32).pin_memory()
-    dh = torch.empty((a.m, a.k), dtype=torch.float32).pin_memory()
-    idx.query_host(Qh.numpy(), a.k, mode=forms[head], out=(ih.numpy().view(np.uint32), dh.numpy()))
+    ih = torch.empty((m, k), dtype=torch.int32).pin_memory()
+    dh = torch.empty((m, k), dtype=torch.float32).pin_memory()
+    idx.query_host(Qh.numpy(), k, mode=modes[head], out=(ih.numpy().view(np.uint32), dh.numpy()))
     barrier()
     t0 = time.perf_counter()
     for _ in range(a.steps):
-        idx.query_host(Qh.numpy(), a.k, mode=forms[head], out=(ih.numpy().view(np.uint32), dh.numpy()))
+        idx.query_host(Qh.numpy(), k, mode=modes[head], out=(ih.numpy().view(np.uint32), dh.numpy()))
     e2e_s = maxall(time.perf_counter() - t0)
-    e2e = {"value": world * a.m * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(a.m * a.d * 4),
-           "d2h_bytes_per_step": int(a.m * a.k * 8)}
+    e2e = {"value": world * m * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(m * w["d"] * 4),
+           "d2h_bytes_per_step": int(m * k * 8)}
 
     # roofline of the dominant kernel; algorithmic work = 2 d flops per
     # (query, database row) pair the search evaluates
     hbm, bf16, bf16_sus, src = peaks()
-    flops_per_launch = res["point_pairs"] * 2 * a.d / max(res["search_launches"], 1)
+    flops_per_launch = res["point_pairs"] * 2 * w["d"] / max(res["search_launches"], 1)
     avg_launch_s = res["search_ms"] / max(res["search_launches"], 1) / 1000.0
-    achieved = flops_per_launch / avg_launch_s / 1e12
+    achieved = flops_per_launch / avg_launch_s / 1e12 if avg_launch_s > 0 else 0.0
     sm_mhz = (clk or {}).get("sm_mhz") or 1920.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12  # FP32 CUDA-core FMA rate at the sampled clock
-    kernel = "tc_search_kernel" if head == "tensor" else "search_kernel"
+    kernel = "search_kernel" if head == "plain" else "tc_search_kernel"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
                 "frac": achieved / bf16, "traffic": committed_traffic(kernel), "kernel": kernel,
                 "peak_source": f"{src} bf16 dense burst (MEASURED_PEAKS.json)",
                 "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
     if head == "plain":
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
         roofline["fp32_core"] = {"achieved_tflops": achieved, "peak_tflops": fp32_peak, "frac": achieved / fp32_peak,
                                  "note": "difference form costs sub+mul+add per pair-dim, 2 flops counted"}
 
@@ -335,24 +391,28 @@ def run_engine(a):
         nq = a.cpu_queries_per_thread * threads
         Xh = X.cpu().numpy()
         Qs = Q[:nq].cpu().numpy()
-        t, kind, desc = cpu_knn_timed(Xh, Qs, a.k, threads)
+        t, kind, desc = cpu_knn_timed(Xh, Qs, k, threads)
         cpu = {"value": nq / t, "unit": UNIT, "cores": threads, "kind": kind,
-               "sample": f"{nq} of the {a.m:,} queries over the full {a.n:,}-row database; {desc}"}
+               "sample": f"{nq} of the {m:,} queries over the full {w['n']:,}-row database; {desc}"}
 
     if rank == 0:
-        form_name = {"tensor": "exact RBC, BF16 tcgen05 distance tiles + FP32 rerank (certified)",
-                     "plain": "plain FP32 exact RBC"}[head]
+        names = {"plain": "plain FP32 exact RBC", "tensor": "exact RBC, BF16 tcgen05 list search + FP32 rerank",
+                 "learned": "exact RBC, learned router + BF16 tcgen05 list search + FP32 rerank",
+                 "learned_plain": "exact RBC, learned router + FP32 list search"}
         extra = {"build_s": build_s, "min_list": info["min_list"], "max_list": info["max_list"],
-                 "point_pairs_per_query": res["point_pairs"] / (a.m * a.steps),
-                 "fallback_queries_per_step": res["fallback"] / a.steps}
-        if side:
-            extra.update({"plain_fp32_value": side["value"], "plain_fp32_ms_per_step": side["ms"] / min(a.steps, 3),
-                          "speedup_vs_plain_fp32": value / side["value"], "same_ids_as_plain": same_as_plain})
+                 "same_ids_all_forms": same, "router": router_info, "forms": {}}
+        for f, r in results.items():
+            extra["forms"][f] = {"value": r["value"], "ms_per_step": r["ms"] / r["steps"],
+                                 "lists_per_query": r["lists"] / (m * r["steps"]),
+                                 "pairs_per_query": r["point_pairs"] / (m * r["steps"]),
+                                 "fallback_queries_per_step": r["fallback"] / r["steps"]}
+        if "plain" in results:
+            extra["speedup_vs_plain_fp32"] = value / results["plain"]["value"]
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32" if head == "tensor" else "f32",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if head == "plain" else "bf16+f32",
                 "data": "synthetic (counter-based generator on the GPU)",
-                "config": dict(config(a, form_name), parallelism=f"replicas{world}"),
+                "config": dict(config(a, names[head]), parallelism=f"replicas{world}"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "extra": extra}
         print(json.dumps(line), flush=True)

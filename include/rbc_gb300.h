@@ -57,6 +57,10 @@ extern "C" {
                                  FP32 rerank of a 40-row shortlist and a certified
                                  error bound (falls back per query when uncertain);
                                  L2 only, needs RBC_BUILD_BF16                      */
+#define RBC_QUERY_ROUTED 0x1000u /* flag for RBC_QUERY_EXACT: search the attached
+                                    router's top lists (and the nearest
+                                    representative's) before pruning; results stay
+                                    exact whatever the router predicts               */
 
 /* ---- synthetic data kinds (counter-based, identical bits on host and GPU) ---- */
 #define RBC_SYNTH_UNIFORM 0   /* i.i.d. U[0,1)                                     */
@@ -105,6 +109,14 @@ int rbc_build_host(const float *hX, uint64_t n, uint32_t d, uint32_t ldx,
 int rbc_destroy(rbc_index *index);
 
 int rbc_get_info(const rbc_index *index, rbc_index_info *info);
+
+/* Index files (no counterpart in the reference, whose rbcStruct lives only in
+ * device memory, rbc.cu:363-368): build once, query from other processes.
+ * The file holds every list structure the index was built with; loading
+ * needs no rebuild.  Format: a fixed header (magic "RBCGB300", version,
+ * sizes, flags) followed by the arrays, little-endian. */
+int rbc_save(const rbc_index *index, const char *path);
+int rbc_load(const char *path, rbc_index **out);
 /* Copies of the index structure to host memory (for tests and tooling). */
 int rbc_get_reps(const rbc_index *index, uint32_t *h_rep_ids /* num_reps */);
 int rbc_get_partition(const rbc_index *index, uint64_t *h_offsets /* num_reps+1 */,
@@ -120,6 +132,58 @@ int rbc_query(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint3
 int rbc_query_host(rbc_index *index, const float *hQ, uint64_t m, uint32_t ldq, uint32_t k,
                    uint32_t mode, uint32_t *hIds, float *hDists, uint32_t ldo);
 int rbc_get_query_stats(const rbc_index *index, rbc_query_stats *stats);
+
+/* ---- batched queries over many indexes (no counterpart in the reference) ----
+ * Instances (index, device queries, k, outputs) are added, then rbc_batch_run
+ * answers all of them exactly: each round plans every instance, then one
+ * persistent search launch serves all instances' work.  The first run
+ * captures the whole sequence into a CUDA graph; later runs replay it, so
+ * new query values written into the same buffers are answered by one graph
+ * launch.  Instances must share the metric; m x num_reps <= 2^28 each. */
+typedef struct rbc_batch rbc_batch;
+int rbc_batch_create(rbc_batch **out);
+int rbc_batch_add(rbc_batch *batch, rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
+                  uint32_t *dIds, float *dDists, uint32_t ldo);
+int rbc_batch_run(rbc_batch *batch, void *stream);
+int rbc_batch_destroy(rbc_batch *batch);
+
+/* Search tuning of an index: rows per thread of the FP32 list-search tile
+ * (tq = 1, 2 or 4; 0 keeps the default) and the longest run of list rows
+ * one work item covers.  rbc_autotune times the candidates on sample queries
+ * and keeps the fastest; with cache_path non-NULL the choice is stored in
+ * and reused from that file, keyed by the index shape. */
+int rbc_set_tuning(rbc_index *index, int tq, uint32_t item_rows);
+int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
+                 const char *cache_path, void *stream);
+
+/* ---- learned list router (no counterpart in the reference) ----
+ * An MLP d -> hidden -> hidden -> num_lists (GELU), FP32 master weights with a
+ * BF16 copy used by its GEMMs (FP32 accumulation), trained on the GPU with
+ * softmax cross-entropy and Adam.  Parameters are one flat FP32 array
+ * [W1 (hidden x d), b1, W2 (hidden x hidden), b2, W3 (num_lists x hidden), b3]. */
+typedef struct rbc_router rbc_router;
+int rbc_router_create(uint32_t d, uint32_t hidden, uint32_t num_lists, uint64_t seed, rbc_router **out);
+int rbc_router_destroy(rbc_router *router);
+int rbc_router_num_params(const rbc_router *router, uint64_t *count);
+int rbc_router_get_params(const rbc_router *router, float *h_params);
+int rbc_router_set_params(rbc_router *router, const float *h_params);
+/* Mean loss and the gradients of one batch (no update). */
+int rbc_router_gradients(rbc_router *router, const float *dQ, uint32_t batch, uint32_t ldq,
+                         const uint32_t *dLabels, float *loss, float *h_grads, void *stream);
+/* Epochs of Adam over n labelled queries in shuffled batches. */
+int rbc_router_train(rbc_router *router, const float *dQ, uint64_t n, uint32_t ldq,
+                     const uint32_t *dLabels, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                     float *final_loss, void *stream);
+/* Logits of m queries into dLogits (m x num_lists). */
+int rbc_router_logits(rbc_router *router, const float *dQ, uint64_t m, uint32_t ldq, float *dLogits,
+                      void *stream);
+/* Training labels produced by the RBC: the list owning each query's exact
+ * nearest neighbour. */
+int rbc_owner_labels(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t *dLabels,
+                     void *stream);
+/* Attach (or detach, router = NULL) a router to an index; RBC_QUERY_ROUTED
+ * queries then probe its top `probes` (1..7) lists first. */
+int rbc_set_router(rbc_index *index, rbc_router *router, uint32_t probes);
 
 /* Benchmark instrumentation (no counterpart in the reference): with profiling
  * on, every list-search kernel launch of a query call is bracketed by CUDA

@@ -57,15 +57,31 @@ def build(force=False, verbose=False):
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     objs = [o for o, _ in results]
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs
+    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}{r.stderr}")
+    build_cli()
+    if verbose:
+        print("built", LIB, "and", CLI)
+    return LIB
+
+
+CLI = os.path.join(HERE, "testRBC")
+CLI_SRC = os.path.join(HERE, "cli", "testRBC.cu")
+
+
+def build_cli():
+    """The testRBC command-line driver, linked against the library (rpath $ORIGIN)."""
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(CLI_SRC), os.path.getmtime(LIB)):
+        return CLI
+    cmd = [NVCC, "-O2", "-std=c++17", f"-I{INCLUDE}", CLI_SRC, "-o", CLI, f"-L{HERE}", "-lrbcgb",
+           "-Xlinker=-rpath=$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}{r.stderr}")
-    if verbose:
-        print("built", LIB)
-    return LIB
+        raise RuntimeError(f"CLI build failed:\n{' '.join(cmd)}\n{r.stdout}{r.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -1,0 +1,285 @@
+// batch.cu -- many independent (index, query set) instances answered by one
+// persistent search launch per round, the whole sequence captured once into
+// a CUDA graph and replayed.
+//
+// Each instance keeps its own plan buffers and per-query results.  A round
+// (probe, then pruned) plans every instance (small kernels), concatenates all
+// instances' work items into one queue tagged with the instance, and runs a
+// single persistent list-search launch over the queue: the kernel reads the
+// instance's database, queries, lists and results from a device table.  The
+// captured graph replays the rounds for new query values in the same
+// buffers.  The reference runs one (database, query set) per call with a
+// host round trip between every kernel (rbc.cu:72-123).
+#include <algorithm>
+#include <memory>
+#include <vector>
+
+#include "engine.cuh"
+#include "rbc_common.cuh"
+
+namespace rbc {
+
+namespace {
+
+__global__ void batch_offsets_kernel(uint32_t *const *counts, uint32_t ninst, uint32_t *offsets, uint32_t *total) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  uint32_t s = 0;
+  for (uint32_t i = 0; i < ninst; i++) {
+    offsets[i] = s;
+    s += *counts[i];
+  }
+  *total = s;
+}
+
+__global__ void batch_concat_kernel(const SearchItem *const *src, uint32_t *const *counts, const uint32_t *offsets,
+                                    SearchItem *dst) {
+  const uint32_t i = blockIdx.y;
+  const uint32_t c = *counts[i];
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < c; j += gridDim.x * blockDim.x) {
+    SearchItem it = src[i][j];
+    it.inst = i;
+    dst[offsets[i] + j] = it;
+  }
+}
+
+template <typename T>
+T *dalloc(size_t n, std::vector<void *> &owned) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, n ? n * sizeof(T) : 16) != cudaSuccess) return nullptr;
+  owned.push_back(p);
+  return static_cast<T *>(p);
+}
+
+}  // namespace
+
+}  // namespace rbc
+
+using namespace rbc;
+
+struct BatchInstance {
+  rbc_index *idx;
+  const float *Q;
+  uint64_t m;
+  uint32_t ldq, k, ldo;
+  uint32_t *ids;
+  float *dists;
+  QueryBufs b;
+};
+
+struct rbc_batch {
+  std::vector<std::unique_ptr<BatchInstance>> inst;
+  std::vector<void *> owned;
+  bool ready = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cap = nullptr;
+  uint32_t *ctl = nullptr;  // [0] work, [1] items, [2] error
+  ~rbc_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    inst.clear();  // releases the per-instance buffers on the capture stream
+    if (cap) {
+      cudaStreamSynchronize(cap);
+      cudaStreamDestroy(cap);
+    }
+    for (void *p : owned) cudaFree(p);
+  }
+};
+
+namespace {
+
+#define BCK(expr)                                       \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #expr); \
+  } while (0)
+#define BTRY(expr)                  \
+  do {                              \
+    int rc_ = (expr);               \
+    if (rc_ != RBC_OK) return rc_;  \
+  } while (0)
+
+// Allocate every buffer, then record the whole two-round sequence on a
+// capture stream into a graph.
+int prepare(rbc_batch *bt) {
+  const uint32_t N = (uint32_t)bt->inst.size();
+  const int metric = bt->inst[0]->idx->metric;
+  // one tile geometry for the shared launch: the smallest query tile any instance needs
+  int tq = 4;
+  uint32_t dp_max = 0;
+  for (auto &ip : bt->inst) {
+    tq = std::min(tq, search_tq_for(ip->idx->dp, ip->idx->tune_tq));
+    dp_max = std::max(dp_max, ip->idx->dp);
+  }
+  const uint32_t qtile = (uint32_t)search_query_tile(dp_max, tq);
+  uint64_t item_total = 0;
+  cudaStream_t s;
+  BCK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  bt->cap = s;
+  std::vector<SearchArgs> args0(N), args1(N);
+  std::vector<SearchItem *> srcs(N);
+  std::vector<uint32_t *> counts(N);
+  for (uint32_t i = 0; i < N; i++) {
+    BatchInstance &in = *bt->inst[i];
+    rbc_index *idx = in.idx;
+    const uint32_t nr = idx->nr, ld = idx->ld;
+    QueryBufs &b = in.b;
+    const uint64_t mb = in.m, pair_cap = mb * nr, item_cap = item_capacity(idx, mb, qtile);
+    item_total += item_cap;
+    BCK(b.Qp.alloc(mb * ld * 4, s));
+    BCK(b.Dqr.alloc(mb * nr * 4, s));
+    BCK(b.probe.alloc(mb * 4, s));
+    BCK(b.probed.alloc(mb * 4, s));
+    BCK(b.res_d.alloc(mb * kListWidth * 4, s));
+    BCK(b.res_i.alloc(mb * kListWidth * 4, s));
+    BCK(b.tau.alloc(mb * 4, s));
+    BCK(b.lock.alloc(mb * 4, s));
+    BCK(b.cnt.alloc((nr + 1) * 4, s));
+    BCK(b.start.alloc((nr + 1) * 4, s));
+    BCK(b.cursor.alloc((nr + 1) * 4, s));
+    BCK(b.tcnt.alloc((nr + 1) * 4, s));
+    BCK(b.tstart.alloc((nr + 1) * 4, s));
+    BCK(b.pair_q.alloc(pair_cap * 4, s));
+    BCK(b.pair_thr.alloc(pair_cap * 4, s));
+    BCK(b.items.alloc(item_cap * sizeof(SearchItem), s));
+    BCK(b.ctl.alloc(64, s));
+    BCK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
+    srcs[i] = b.items.as<SearchItem>();
+    counts[i] = b.ctl.as<uint32_t>() + 1;
+    SearchArgs a{};
+    a.X = idx->Xp;
+    a.pid = idx->perm;
+    a.Q = b.Qp.as<float>();
+    a.qidx = b.pair_q.as<uint32_t>();
+    a.res_d = b.res_d.as<float>();
+    a.res_i = b.res_i.as<uint32_t>();
+    a.tau = b.tau.as<uint32_t>();
+    a.lock = b.lock.as<uint32_t>();
+    a.ld = ld;
+    a.dp = idx->dp;
+    a.k = in.k;
+    args0[i] = a;
+    a.qthr = b.pair_thr.as<float>();
+    args1[i] = a;
+  }
+  BCK(cudaStreamSynchronize(s));
+  SearchArgs *t0 = dalloc<SearchArgs>(N, bt->owned), *t1 = dalloc<SearchArgs>(N, bt->owned);
+  SearchItem **dsrc = dalloc<SearchItem *>(N, bt->owned);
+  uint32_t **dcnt = dalloc<uint32_t *>(N, bt->owned);
+  uint32_t *offs = dalloc<uint32_t>(N, bt->owned);
+  SearchItem *all = dalloc<SearchItem>(item_total, bt->owned);
+  bt->ctl = dalloc<uint32_t>(16, bt->owned);
+  if (!t0 || !t1 || !dsrc || !dcnt || !offs || !all || !bt->ctl)
+    return fail(RBC_ERR_NOMEM, "rbc_batch_run: device allocation failed");
+  BCK(cudaMemcpy(t0, args0.data(), N * sizeof(SearchArgs), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(t1, args1.data(), N * sizeof(SearchArgs), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(dsrc, srcs.data(), N * sizeof(void *), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(dcnt, counts.data(), N * sizeof(void *), cudaMemcpyHostToDevice));
+  const int grid = search_grid(metric, dp_max, tq);
+  SearchArgs g{};
+  g.items = all;
+  g.nitems = bt->ctl + 1;
+  g.work = bt->ctl;
+  g.err = bt->ctl + 2;
+  g.dp = dp_max;  // sizes the shared-memory tile of the shared launch
+  g.k = 1;
+
+  BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = RBC_OK;
+  auto capture = [&]() -> int {
+    BCK(cudaMemsetAsync(bt->ctl, 0, 64, s));
+    for (auto &ip : bt->inst) {
+      BatchInstance &in = *ip;
+      rbc_index *idx = in.idx;
+      QueryBufs &b = in.b;
+      BCK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
+      BCK(launch_pad_rows(in.Q, in.ldq, b.Qp.as<float>(), idx->ld, in.m, idx->d, s));
+      BCK(launch_dense_dist(idx->metric, b.Qp.as<float>(), in.m, idx->R, idx->nr, idx->ld, idx->dp,
+                            b.Dqr.as<float>(), idx->nr, s));
+      BCK(launch_row_topp(b.Dqr.as<float>(), in.m, idx->nr, 1, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+      BCK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
+                              b.lock.as<uint32_t>(), in.m, s));
+    }
+    for (uint32_t round = 0; round < 2; round++) {
+      for (auto &ip : bt->inst)
+        BTRY(plan_and_search(ip->idx, ip->b, ip->m, 1, ip->k, round, ip->idx->Xp, ip->idx->perm, ip->idx->offsets,
+                             ip->idx->radius, grid, nullptr, s, 1, tq));
+      batch_offsets_kernel<<<1, 1, 0, s>>>(dcnt, N, offs, bt->ctl + 1);
+      BCK(launched());
+      batch_concat_kernel<<<dim3(64, N), 256, 0, s>>>(dsrc, dcnt, offs, all);
+      BCK(launched());
+      BCK(cudaMemsetAsync(bt->ctl, 0, 4, s));
+      g.insts = round == 0 ? t0 : t1;
+      BCK(launch_search(metric, g, grid, s, tq));
+    }
+    for (auto &ip : bt->inst)
+      BCK(launch_write_results(ip->b.res_d.as<float>(), ip->b.res_i.as<uint32_t>(), ip->m, ip->k, ip->ids, ip->dists,
+                               ip->ldo, s));
+    return RBC_OK;
+  };
+  rc = capture();
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &graph);
+  if (rc != RBC_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "rbc_batch_run: graph capture");
+  bt->graph = graph;
+  BCK(cudaGraphInstantiate(&bt->exec, graph, 0));
+  bt->ready = true;
+  return RBC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rbc_batch_create(rbc_batch **out) {
+  if (!out) return fail(RBC_ERR_INVALID, "rbc_batch_create: out is NULL");
+  *out = new rbc_batch();
+  return RBC_OK;
+}
+
+int rbc_batch_add(rbc_batch *bt, rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
+                  uint32_t *dIds, float *dDists, uint32_t ldo) {
+  if (!bt || !idx) return fail(RBC_ERR_INVALID, "rbc_batch_add: NULL argument");
+  if (bt->ready) return fail(RBC_ERR_INVALID, "rbc_batch_add: the batch already ran; create a new one");
+  if (!(idx->flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_INVALID, "rbc_batch_add: index has no partition");
+  if (k < 1 || k > (uint32_t)kListWidth || ldo < k || ldq < idx->d || m == 0 || !dQ || (!dIds && !dDists))
+    return fail(RBC_ERR_INVALID, "rbc_batch_add: bad query arguments");
+  if (m * (uint64_t)idx->nr > (1ull << 28))
+    return fail(RBC_ERR_UNSUPPORTED, "rbc_batch_add: m x num_reps above 2^28 (split the query set)");
+  if (!bt->inst.empty() && bt->inst[0]->idx->metric != idx->metric)
+    return fail(RBC_ERR_INVALID, "rbc_batch_add: all instances must share the metric");
+  auto in = std::make_unique<BatchInstance>();
+  in->idx = idx;
+  in->Q = dQ;
+  in->m = m;
+  in->ldq = ldq;
+  in->k = k;
+  in->ldo = ldo;
+  in->ids = dIds;
+  in->dists = dDists;
+  bt->inst.push_back(std::move(in));
+  return RBC_OK;
+}
+
+int rbc_batch_run(rbc_batch *bt, void *stream) {
+  if (!bt || bt->inst.empty()) return fail(RBC_ERR_INVALID, "rbc_batch_run: empty batch");
+  if (!bt->ready) BTRY(prepare(bt));
+  cudaStream_t s = (cudaStream_t)stream;
+  BCK(cudaGraphLaunch(bt->exec, s));
+  uint32_t err = 0;
+  BCK(cudaMemcpyAsync(&err, bt->ctl + 2, 4, cudaMemcpyDeviceToHost, s));
+  BCK(cudaStreamSynchronize(s));
+  if (err) return fail(RBC_ERR_ITER_LIMIT, "rbc_batch_run: a bounded device wait ran out");
+  return RBC_OK;
+}
+
+int rbc_batch_destroy(rbc_batch *bt) {
+  delete bt;
+  return RBC_OK;
+}
+
+}  // extern "C"

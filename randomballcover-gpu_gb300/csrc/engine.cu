@@ -92,17 +92,16 @@ int check_dims(uint32_t d, uint32_t ld, const char *what) {
   return RBC_OK;
 }
 
-// Per-call buffers of one query batch.
-struct QueryBufs {
-  DevBuf Qp, Dqr, probe, probed, res_d, res_i, tau, lock, cnt, start, cursor, tcnt, tstart, pair_q,
-      pair_thr, items, ctl, scan_tmp;
-};
+}  // namespace
 
-// Build the list-major plan for one mode and run the search over it.
+// Build the list-major plan for one mode, then (stage >= 1) its work items
+// and (stage 2) run the search over them.  The plan stays in b.cnt / b.start
+// / b.pair_q / b.pair_thr, the items in b.items with their count in b.ctl[1].
 int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
-                    int grid, unsigned long long *stats, cudaStream_t s) {
-  const uint32_t nr = idx->nr, qtile = (uint32_t)search_query_tile(idx->dp);
+                    int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq) {
+  const int tqv = tq < 0 ? idx->tune_tq : tq;
+  const uint32_t nr = idx->nr, qtile = (uint32_t)search_query_tile(idx->dp, tqv);
   uint32_t *ctl = b.ctl.as<uint32_t>();  // [0] work, [1] nitems, [2] err
   PlanArgs a{};
   a.Dqr = b.Dqr.as<float>();
@@ -132,9 +131,11 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
   a.list_cnt = start;
   a.phase = 1;
   CK(launch_plan_pass(a, mode, s));
-  CK(launch_tiles_per_list(cnt, nr, qtile, tcnt, s));
+  if (stage == 0) return RBC_OK;
+  CK(launch_tiles_per_list(cnt, offsets, nr, qtile, idx->item_rows, tcnt, s));
   CK(launch_exclusive_scan(tcnt, tstart, nr + 1, b.scan_tmp.p, ctl + 2, s));
-  CK(launch_plan_items(cnt, start, tstart, offsets, nr, qtile, b.items.as<SearchItem>(), ctl + 1, s));
+  CK(launch_plan_items(cnt, start, tstart, offsets, nr, qtile, idx->item_rows, b.items.as<SearchItem>(), ctl + 1, s));
+  if (stage == 1) return RBC_OK;
 
   SearchArgs sa{};
   sa.X = X;
@@ -166,10 +167,17 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
     e1 = idx->ev_pool[idx->ev_used++];
     CK(cudaEventRecord(e0, s));
   }
-  CK(launch_search(idx->metric, sa, grid, s));
+  CK(launch_search(idx->metric, sa, grid, s, tqv));
   if (e1) CK(cudaEventRecord(e1, s));
   return RBC_OK;
 }
+
+uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile) {
+  const uint64_t chunks = idx->n / std::max<uint32_t>(idx->item_rows, 1) + idx->nr + 1;
+  return (mb / qtile + 1) * chunks + idx->nr + 1;
+}
+
+namespace {
 
 }  // namespace
 
@@ -246,28 +254,28 @@ int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc
   CK(launch_gather_rows(Xi, ld, rid.as<uint32_t>(), nr, idx->R, s));
 
   if (flags & RBC_BUILD_PARTITION) {
-    DevBuf owner, odist, hist, hscan, tmp;
+    DevBuf odist, hist, hscan, tmp;
     const uint32_t ntiles = (uint32_t)((n + owner_tile_rows() - 1) / owner_tile_rows());
     const uint64_t hn = (uint64_t)nr * ntiles;
-    CK(owner.alloc(n * 4, s));
     CK(odist.alloc(n * 4, s));
     CK(hist.alloc(hn * 4, s));
     CK(hscan.alloc(hn * 4, s));
     CK(tmp.alloc(scan_temp_bytes(hn), s));
+    CK(cudaMalloc(&idx->owner, n * 4));
     CK(cudaMalloc(&idx->perm, n * 4));
     CK(cudaMalloc(&idx->offsets, (nr + 1) * 8));
     CK(cudaMalloc(&idx->radius, nr * 4));
     CK(cudaMalloc(&idx->Xp, (size_t)n * ld * 4));
-    idx->device_bytes += n * 4 + (nr + 1) * 8 + nr * 4 + (size_t)n * ld * 4;
-    CK(launch_argmin(idx->metric, Xi, n, idx->R, nr, ld, idx->dp, owner.as<uint32_t>(), odist.as<float>(), s));
-    CK(launch_owner_hist(owner.as<uint32_t>(), n, nr, hist.as<uint32_t>(), ntiles, s));
+    idx->device_bytes += 2 * n * 4 + (nr + 1) * 8 + nr * 4 + (size_t)n * ld * 4;
+    CK(launch_argmin(idx->metric, Xi, n, idx->R, nr, ld, idx->dp, idx->owner, odist.as<float>(), s));
+    CK(launch_owner_hist(idx->owner, n, nr, hist.as<uint32_t>(), ntiles, s));
     CK(launch_exclusive_scan(hist.as<uint32_t>(), hscan.as<uint32_t>(), hn, tmp.p, nullptr, s));
-    CK(launch_owner_scatter(owner.as<uint32_t>(), n, nr, hscan.as<uint32_t>(), ntiles,
-                            idx->perm, s));
+    CK(launch_owner_scatter(idx->owner, n, nr, hscan.as<uint32_t>(), ntiles, idx->perm, s));
     CK(launch_list_offsets(hscan.as<uint32_t>(), nr, ntiles, n, idx->offsets, s));
     CK(launch_list_radius(idx->offsets, idx->perm, odist.as<float>(), nr, idx->radius, s));
     CK(launch_gather_rows(Xi, ld, idx->perm, n, idx->Xp, s));
-    std::vector<uint64_t> off(nr + 1);
+    std::vector<uint64_t> &off = idx->h_offsets;
+    off.resize(nr + 1);
     CK(cudaMemcpyAsync(off.data(), idx->offsets, (nr + 1) * 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     idx->min_list = UINT64_MAX;
@@ -349,7 +357,7 @@ int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc
 }
 
 // ------------------------------------------------------------------ query
-int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, bool nosync, uint32_t *dIds,
+int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode, uint32_t *dIds,
              float *dDists, uint32_t ldo, cudaStream_t s);
 
 // Exact mode: nearest-rep probe round, then the pruned round over every other
@@ -382,20 +390,23 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     offsets = idx->os_offsets;
   } else if (base == RBC_QUERY_EXACT_TC) {
     if (!(idx->flags & RBC_BUILD_BF16)) return fail(RBC_ERR_INVALID, "rbc_query: index has no BF16 lists");
-    return query_tc(idx, dQ, m, ldq, k, nosync, dIds, dDists, ldo, s);
+    return query_tc(idx, dQ, m, ldq, k, mode, dIds, dDists, ldo, s);
   } else {
     return fail(RBC_ERR_INVALID, "rbc_query: unknown mode");
   }
   pool_setup();
   const uint32_t nr = idx->nr, ld = idx->ld;
-  const uint32_t P = std::min(kDefaultProbes, nr);
-  const uint32_t qtile = (uint32_t)search_query_tile(idx->dp);
-  const int grid = search_grid(idx->metric, idx->dp);
+  const bool routed = (mode & RBC_QUERY_ROUTED) && base == RBC_QUERY_EXACT;
+  if (routed && !idx->router) return fail(RBC_ERR_INVALID, "rbc_query: RBC_QUERY_ROUTED without a router");
+  // probe table: column 0 the nearest representative, then the router's picks
+  const uint32_t P = routed ? 1 + idx->router_probes : std::min(kDefaultProbes, nr);
+  const uint32_t qtile = (uint32_t)search_query_tile(idx->dp, idx->tune_tq);
+  const int grid = search_grid(idx->metric, idx->dp, idx->tune_tq);
   // batch so the m x nr plan arrays stay near 2^27 entries
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
   QueryBufs b;
   const uint64_t pair_cap = mb * nr;
-  const uint64_t item_cap = pair_cap / qtile + nr + 1;
+  const uint64_t item_cap = item_capacity(idx, mb, qtile);
   CK(b.Qp.alloc(mb * ld * 4, s));
   CK(b.Dqr.alloc(mb * nr * 4, s));
   CK(b.probe.alloc(mb * P * 4, s));
@@ -414,7 +425,12 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   CK(b.items.alloc(item_cap * sizeof(SearchItem), s));
   CK(b.ctl.alloc(64, s));
   CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
-  DevBuf stats;
+  DevBuf stats, near, near_d, logits;
+  if (routed) {
+    CK(near.alloc(mb * 4, s));
+    CK(near_d.alloc(mb * 4, s));
+    CK(logits.alloc(mb * nr * 4, s));
+  }
   CK(stats.alloc(2 * sizeof(unsigned long long), s));
   CK(cudaMemsetAsync(stats.p, 0, 2 * sizeof(unsigned long long), s));
   CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
@@ -423,7 +439,20 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     const uint64_t mq = std::min(mb, m - b0);
     CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
     CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
-    CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+    if (routed) {
+      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, 1, near.as<uint32_t>(), near_d.as<float>(), s));
+      Router &rt = idx->router->r;
+      const uint32_t chunk = 4096;
+      CK(rt.alloc_batch(chunk, s));
+      for (uint64_t i = 0; i < mq; i += chunk) {
+        const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
+        CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+      }
+      CK(launch_router_probes(logits.as<float>(), mq, nr, idx->router_probes, near.as<uint32_t>(),
+                              near_d.as<float>(), b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+    } else {
+      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+    }
     CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
                            b.lock.as<uint32_t>(), mq, s));
     TRY(plan_and_search(idx, b, mq, P, k, 0, X, pid, offsets, idx->radius, grid, stats.as<unsigned long long>(), s));
@@ -457,60 +486,84 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   return RBC_OK;
 }
 
-// Tensor-core exact query (tc_search.cu): every 128-query tile is compared on
-// the tensor cores with every 128-row tile of the BF16 lists, work units are
-// (query tile, row chunk) pairs in chunk-major order so the CTAs in flight
-// share their B tiles through L2; then the FP32 rerank certifies each query
-// and the uncertified ones are recomputed by the plain exact path.
-int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, bool nosync, uint32_t *dIds,
+// Tensor-core exact query (tc_search.cu), an RBC query whose list search
+// runs on the tensor cores:
+//   1. query x representative distances, probe table (nearest representative,
+//      plus the router's picks when routed), exact FP32 search of the probed
+//      lists -> each query's k-th distance;
+//   2. the pruning plan (plan.cu) -> surviving (list, query) pairs;
+//   3. queries sorted by nearest representative into 128-query tiles; each
+//      tile's union of probed and surviving lists becomes row ranges (lists
+//      are contiguous in the list-major layout), cut into work units;
+//   4. tensor search of the units, exact rerank and certificate; uncertified
+//      queries are recomputed by the plain exact path.
+// Rows outside a tile's ranges were pruned by the exact bounds, so the
+// certificate covers everything.
+int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode, uint32_t *dIds,
              float *dDists, uint32_t ldo, cudaStream_t s) {
   pool_setup();
-  const uint32_t ld = idx->ld, kp = idx->kp;
-  const uint64_t m_pad = (m + 127) / 128 * 128;
-  const int grid = tc_grid();
-  DevBuf Qp, Qb, qn, qinex, sl_a, sl_row, sl_theta, sl_lock, units, ctl, failq;
-  CK(Qp.alloc(m * ld * 4, s));
-  CK(Qb.alloc(m_pad * kp * 2, s));
-  CK(qn.alloc(m_pad * 4, s));
-  CK(qinex.alloc(m, s));
-  CK(sl_a.alloc(m_pad * kShortlist * 4, s));
-  CK(sl_row.alloc(m_pad * kShortlist * 4, s));
-  CK(sl_theta.alloc(m_pad * 4, s));
-  CK(sl_lock.alloc(m_pad * 4, s));
+  const uint32_t nr = idx->nr, ld = idx->ld, kp = idx->kp;
+  const bool routed = (mode & RBC_QUERY_ROUTED) != 0;
+  if (routed && !idx->router) return fail(RBC_ERR_INVALID, "rbc_query: RBC_QUERY_ROUTED without a router");
+  const uint32_t P = routed ? 1 + idx->router_probes : 1;
+  const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
+  const uint32_t qtile = (uint32_t)search_query_tile(idx->dp, idx->tune_tq);
+  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(128, (1ull << 27) / nr));
+  const uint64_t mbp = (mb + 127) / 128 * 128, T = mbp / 128;
+  QueryBufs b;
+  const uint64_t pair_cap = mb * nr, item_cap = item_capacity(idx, mb, qtile);
+  CK(b.Qp.alloc(mb * ld * 4, s));
+  CK(b.Dqr.alloc(mb * nr * 4, s));
+  CK(b.probe.alloc(mb * P * 4, s));
+  CK(b.probed.alloc(mb * P * 4, s));
+  CK(b.res_d.alloc(mb * kListWidth * 4, s));
+  CK(b.res_i.alloc(mb * kListWidth * 4, s));
+  CK(b.tau.alloc(mb * 4, s));
+  CK(b.lock.alloc(mb * 4, s));
+  CK(b.cnt.alloc((nr + 1) * 4, s));
+  CK(b.start.alloc((nr + 1) * 4, s));
+  CK(b.cursor.alloc((nr + 1) * 4, s));
+  CK(b.tcnt.alloc((nr + 1) * 4, s));
+  CK(b.tstart.alloc((nr + 1) * 4, s));
+  CK(b.pair_q.alloc(pair_cap * 4, s));
+  CK(b.pair_thr.alloc(pair_cap * 4, s));
+  CK(b.items.alloc(item_cap * sizeof(SearchItem), s));
+  CK(b.ctl.alloc(64, s));
+  CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
+  DevBuf near, near_d, logits, order, slot_of, khist, kstart, kcursor, flags, Qs, Qb, qn, qinex, sl_a, sl_row, sl_sel,
+      sl_theta, sl_lock, units, ctl, failq;
+  if (routed) {
+    CK(near.alloc(mb * 4, s));
+    CK(near_d.alloc(mb * 4, s));
+    CK(logits.alloc(mb * nr * 4, s));
+  }
+  CK(order.alloc(mbp * 4, s));
+  CK(slot_of.alloc(mb * 4, s));
+  CK(khist.alloc((nr + 1) * 4, s));
+  CK(kstart.alloc((nr + 1) * 4, s));
+  CK(kcursor.alloc((nr + 1) * 4, s));
+  CK(flags.alloc(T * nr, s));
+  CK(Qs.alloc(mbp * ld * 4, s));
+  CK(Qb.alloc(mbp * kp * 2, s));
+  CK(qn.alloc(mbp * 4, s));
+  CK(qinex.alloc(mbp, s));
+  CK(sl_a.alloc(2 * mbp * kShortlist * 4, s));
+  CK(sl_row.alloc(2 * mbp * kShortlist * 4, s));
+  CK(sl_sel.alloc(mbp * 4, s));
+  CK(sl_theta.alloc(mbp * 4, s));
+  CK(sl_lock.alloc(mbp * 4, s));
   CK(ctl.alloc(64, s));
-  CK(failq.alloc(m * 4, s));
-  CK(cudaMemsetAsync(ctl.p, 0, 64, s));
-  CK(launch_pad_rows(dQ, ldq, Qp.as<float>(), ld, m, idx->d, s));
-  CK(launch_to_bf16(Qp.as<float>(), ld, m, m_pad, idx->d, kp, Qb.p, qn.as<float>(), 0.f, nullptr, nullptr, s));
-  CK(launch_row_inexact(Qp.as<float>(), ld, m, idx->d, qinex.as<uint8_t>(), s));
+  CK(failq.alloc(mb * 4, s));
+  DevBuf stats;
+  CK(stats.alloc(2 * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(stats.p, 0, 2 * sizeof(unsigned long long), s));
   CUtensorMap tmA;
-  CK(tc_make_map(&tmA, Qb.p, m_pad, kp, 128));
-  // units: chunk-major so that concurrent CTAs read the same rows
-  const uint32_t T = (uint32_t)(m_pad / 128);
-  const uint64_t nb = idx->n_pad / 128;
-  uint64_t nchunks = std::max<uint64_t>(1, std::min<uint64_t>(nb, ((uint64_t)grid * 32 + T - 1) / T));
-  const uint64_t per = (nb + nchunks - 1) / nchunks;
-  nchunks = (nb + per - 1) / per;
-  std::vector<TcUnit> hu;
-  hu.reserve(nchunks * T);
-  for (uint64_t c = 0; c < nchunks; c++)
-    for (uint32_t t = 0; t < T; t++) hu.push_back(TcUnit{t, 0, c * per * 128, std::min(nb, (c + 1) * per) * 128});
-  CK(units.alloc(hu.size() * sizeof(TcUnit), s));
-  CK(cudaMemcpyAsync(units.p, hu.data(), hu.size() * sizeof(TcUnit), cudaMemcpyHostToDevice, s));
-  CK(launch_sl_init(sl_a.as<float>(), sl_row.as<uint32_t>(), sl_theta.as<uint32_t>(), sl_lock.as<uint32_t>(), m_pad,
-                    s));
-  TcArgs ta{};
-  ta.units = units.as<TcUnit>();
-  ta.nunits = (uint32_t)hu.size();
-  ta.kblocks = kp / 64;
-  ta.xn = idx->xn;
-  ta.sl_a = sl_a.as<float>();
-  ta.sl_row = sl_row.as<uint32_t>();
-  ta.sl_theta = sl_theta.as<uint32_t>();
-  ta.sl_lock = sl_lock.as<uint32_t>();
-  ta.err = ctl.as<uint32_t>();
+  CK(tc_make_map(&tmA, Qb.p, mbp, kp, 128));
+  std::vector<uint8_t> hflags(T * nr);
+  const std::vector<uint64_t> &off = idx->h_offsets;
+  uint64_t tc_pairs = 0, tc_lists = 0, nfail_total = 0;
+  double tc_ms = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  idx->ev_used = 0;
   if (idx->profile) {
     while (idx->ev_pool.size() < 2) {
       cudaEvent_t e;
@@ -519,63 +572,169 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     }
     e0 = idx->ev_pool[0];
     e1 = idx->ev_pool[1];
-    idx->ev_used = 2;
-    CK(cudaEventRecord(e0, s));
   }
-  CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
-  if (e1) CK(cudaEventRecord(e1, s));
-  RerankArgs ra{};
-  ra.X = idx->Xp;
-  ra.pid = idx->perm;
-  ra.Q = Qp.as<float>();
-  ra.ld = ld;
-  ra.dp = idx->dp;
-  ra.k = k;
-  ra.m = m;
-  ra.sl_a = sl_a.as<float>();
-  ra.sl_row = sl_row.as<uint32_t>();
-  ra.qn = qn.as<float>();
-  ra.q_inexact = qinex.as<uint8_t>();
-  ra.x_inexact = idx->x_inexact;
-  ra.maxnorm = idx->maxnorm;
-  ra.ids = dIds;
-  ra.dists = dDists;
-  ra.ldo = ldo;
-  ra.nfail = ctl.as<uint32_t>() + 1;
-  ra.fail = failq.as<uint32_t>();
-  CK(launch_rerank(idx->metric, ra, s));
-  (void)nosync;  // the fallback decision needs the certificate count on the host
-  uint32_t hc[2];
-  CK(cudaMemcpyAsync(hc, ctl.p, 8, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  if (hc[0]) return fail(RBC_ERR_ITER_LIMIT, "rbc_query: a bounded device wait ran out in the tensor search");
-  const uint32_t nfail = hc[1];
-  if (nfail) {
-    DevBuf Qf, fi, fd;
-    CK(Qf.alloc((uint64_t)nfail * ld * 4, s));
-    CK(fi.alloc((uint64_t)nfail * k * 4, s));
-    CK(fd.alloc((uint64_t)nfail * k * 4, s));
-    CK(launch_gather_rows(Qp.as<float>(), ld, failq.as<uint32_t>(), nfail, Qf.as<float>(), s));
-    rbc_profile keep = idx->prof;
-    TRY(query_index(idx, Qf.as<float>(), nfail, ld, k, RBC_QUERY_EXACT, fi.as<uint32_t>(), fd.as<float>(), k, s));
-    idx->prof = keep;
-    CK(launch_scatter_results(fi.as<uint32_t>(), fd.as<float>(), failq.as<uint32_t>(), nfail, k, dIds, dDists, ldo,
-                              s));
+  idx->ev_used = 0;
+  for (uint64_t b0 = 0; b0 < m; b0 += mb) {
+    const uint64_t mq = std::min(mb, m - b0);
+    const uint64_t Tq = (mq + 127) / 128;
+    CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
+    CK(cudaMemsetAsync(ctl.p, 0, 64, s));
+    // 1. probe round
+    CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
+    CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
+    if (routed) {
+      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, 1, near.as<uint32_t>(), near_d.as<float>(), s));
+      Router &rt = idx->router->r;
+      const uint32_t chunk = 4096;
+      CK(rt.alloc_batch(chunk, s));
+      for (uint64_t i = 0; i < mq; i += chunk) {
+        const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
+        CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+      }
+      CK(launch_router_probes(logits.as<float>(), mq, nr, idx->router_probes, near.as<uint32_t>(),
+                              near_d.as<float>(), b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+    } else {
+      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, 1, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+    }
+    CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(),
+                           mq, s));
+    TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid,
+                        stats.as<unsigned long long>(), s));
+    // 2. pruning plan (no plain search)
+    TRY(plan_and_search(idx, b, mq, P, k, 1, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 0));
+    // 3. tiles of queries sorted by nearest representative, their list unions
+    CK(launch_sort_by_key(b.probe.as<uint32_t>(), P, mq, nr, khist.as<uint32_t>(), kstart.as<uint32_t>(),
+                          kcursor.as<uint32_t>(), b.scan_tmp.p, order.as<uint32_t>(), slot_of.as<uint32_t>(), s));
+    CK(cudaMemsetAsync(flags.p, 0, Tq * nr, s));
+    CK(launch_mark_tiles(b.start.as<uint32_t>(), b.cnt.as<uint32_t>(), b.pair_q.as<uint32_t>(), b.probe.as<uint32_t>(),
+                         mq, P, slot_of.as<uint32_t>(), nr, flags.as<uint8_t>(), s));
+    CK(cudaMemcpyAsync(hflags.data(), flags.p, Tq * nr, cudaMemcpyDeviceToHost, s));
+    // queries in tile order, BF16 rows and norms (slots past mq are zero rows)
+    CK(cudaMemsetAsync(Qs.p, 0, mbp * ld * 4, s));
+    CK(launch_gather_rows(b.Qp.as<float>(), ld, order.as<uint32_t>(), mq, Qs.as<float>(), s));
+    CK(launch_to_bf16(Qs.as<float>(), ld, mq, Tq * 128, idx->d, kp, Qb.p, qn.as<float>(), 0.f, nullptr, nullptr, s));
+    CK(launch_row_inexact(Qs.as<float>(), ld, mq, idx->d, qinex.as<uint8_t>(), s));
     CK(cudaStreamSynchronize(s));
+    std::vector<TcUnit> hu;
+    const uint64_t kUnitRows = 128 * 1024;
+    for (uint32_t t = 0; t < Tq; t++) {
+      const uint8_t *f = hflags.data() + (uint64_t)t * nr;
+      uint32_t r = 0;
+      uint64_t cur0 = 0, cur1 = 0;
+      bool open = false;
+      auto flush = [&]() {
+        for (uint64_t p = cur0; p < cur1; p += kUnitRows)
+          hu.push_back(TcUnit{t, 0, p, std::min(cur1, p + kUnitRows)});
+      };
+      while (r < nr) {
+        if (!f[r] || off[r + 1] == off[r]) {
+          r++;
+          continue;
+        }
+        uint32_t r1 = r;
+        while (r1 < nr && (f[r1] || off[r1 + 1] == off[r1])) r1++;
+        const uint64_t p0 = off[r] / 128 * 128, p1 = (off[r1] + 127) / 128 * 128;
+        if (open && p0 <= cur1) {
+          cur1 = std::max(cur1, p1);
+        } else {
+          if (open) flush();
+          cur0 = p0;
+          cur1 = p1;
+          open = true;
+        }
+        for (uint32_t j = r; j < r1; j++) tc_lists += f[j];
+        r = r1;
+      }
+      if (open) flush();
+    }
+    // units touching the same rows run together: they share B tiles in L2
+    std::stable_sort(hu.begin(), hu.end(), [](const TcUnit &x, const TcUnit &y) { return x.p0 < y.p0; });
+    for (const TcUnit &u : hu) tc_pairs += (u.p1 - u.p0) * std::min<uint64_t>(128, mq - (uint64_t)u.tile * 128);
+    CK(units.alloc(std::max<size_t>(hu.size(), 1) * sizeof(TcUnit), s));
+    if (!hu.empty()) CK(cudaMemcpyAsync(units.p, hu.data(), hu.size() * sizeof(TcUnit), cudaMemcpyHostToDevice, s));
+    // 4. tensor search, rerank, certificate
+    CK(launch_sl_init(sl_a.as<float>(), sl_row.as<uint32_t>(), sl_sel.as<uint32_t>(), sl_theta.as<uint32_t>(),
+                      sl_lock.as<uint32_t>(), Tq * 128, s));
+    TcArgs ta{};
+    ta.units = units.as<TcUnit>();
+    ta.nunits = (uint32_t)hu.size();
+    ta.kblocks = kp / 64;
+    ta.xn = idx->xn;
+    ta.m_pad = Tq * 128;
+    ta.sl_a = sl_a.as<float>();
+    ta.sl_row = sl_row.as<uint32_t>();
+    ta.sl_sel = sl_sel.as<uint32_t>();
+    ta.sl_theta = sl_theta.as<uint32_t>();
+    ta.sl_lock = sl_lock.as<uint32_t>();
+    ta.err = ctl.as<uint32_t>();
+    if (e0) CK(cudaEventRecord(e0, s));
+    CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
+    if (e1) CK(cudaEventRecord(e1, s));
+    RerankArgs ra{};
+    ra.X = idx->Xp;
+    ra.pid = idx->perm;
+    ra.Q = Qs.as<float>();
+    ra.order = order.as<uint32_t>();
+    ra.ld = ld;
+    ra.dp = idx->dp;
+    ra.k = k;
+    ra.m = mq;
+    ra.m_pad = Tq * 128;
+    ra.sl_a = sl_a.as<float>();
+    ra.sl_row = sl_row.as<uint32_t>();
+    ra.sl_sel = sl_sel.as<uint32_t>();
+    ra.qn = qn.as<float>();
+    ra.q_inexact = qinex.as<uint8_t>();
+    ra.x_inexact = idx->x_inexact;
+    ra.maxnorm = idx->maxnorm;
+    ra.ids = dIds ? dIds + b0 * ldo : nullptr;
+    ra.dists = dDists ? dDists + b0 * ldo : nullptr;
+    ra.ldo = ldo;
+    ra.nfail = ctl.as<uint32_t>() + 1;
+    ra.fail = failq.as<uint32_t>();
+    CK(launch_rerank(idx->metric, ra, s));
+    uint32_t hc[2], bc[3];
+    CK(cudaMemcpyAsync(hc, ctl.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(bc, b.ctl.p, 12, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (hc[0] || bc[2]) return fail(RBC_ERR_ITER_LIMIT, "rbc_query: a bounded device wait ran out");
+    if (e0) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      tc_ms += ms;
+    }
+    const uint32_t nfail = hc[1];
+    nfail_total += nfail;
+    if (nfail) {
+      DevBuf Qf, fi, fd;
+      CK(Qf.alloc((uint64_t)nfail * ld * 4, s));
+      CK(fi.alloc((uint64_t)nfail * k * 4, s));
+      CK(fd.alloc((uint64_t)nfail * k * 4, s));
+      CK(launch_gather_rows(b.Qp.as<float>(), ld, failq.as<uint32_t>(), nfail, Qf.as<float>(), s));
+      rbc_profile keep = idx->prof;
+      rbc_query_stats keep_stats = idx->stats;
+      TRY(query_index(idx, Qf.as<float>(), nfail, ld, k, RBC_QUERY_EXACT, fi.as<uint32_t>(), fd.as<float>(), k, s));
+      idx->prof = keep;
+      idx->stats = keep_stats;
+      CK(launch_scatter_results(fi.as<uint32_t>(), fd.as<float>(), failq.as<uint32_t>(), nfail, k,
+                                dIds ? dIds + b0 * ldo : nullptr, dDists ? dDists + b0 * ldo : nullptr, ldo, s));
+      CK(cudaStreamSynchronize(s));
+    }
   }
+  unsigned long long st[2] = {0, 0};
+  CK(cudaMemcpy(st, stats.p, sizeof(st), cudaMemcpyDeviceToHost));
   idx->stats.queries = m;
-  idx->stats.rep_pairs = 0;
-  idx->stats.lists_probed = m * (uint64_t)idx->nr;
-  idx->stats.point_pairs = m * idx->n;
-  idx->stats.fallback_queries = nfail;
+  idx->stats.rep_pairs = m * nr;
+  idx->stats.lists_probed = tc_lists;
+  idx->stats.point_pairs = tc_pairs;
+  idx->stats.fallback_queries = nfail_total;
   if (idx->profile) {
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, e0, e1));
-    idx->prof.search_launches = 1;
-    idx->prof.search_ms = ms;
+    idx->prof.search_launches = (m + mb - 1) / mb;
+    idx->prof.search_ms = tc_ms;
   }
   return RBC_OK;
 }
+
 
 // ------------------------------------------------------------------ brute force
 // One search over the whole database split into chunks (bruteK / bruteSearch,
@@ -708,7 +867,7 @@ int rbc_build_host(const float *hX, uint64_t n, uint32_t d, uint32_t ldx, const 
 int rbc_destroy(rbc_index *idx) {
   if (!idx) return RBC_OK;
   void *ptrs[] = {idx->Xp,      idx->perm,   idx->offsets, idx->radius,     idx->R,  idx->os_lists, idx->os_counts,
-                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->Xb, idx->xn};
+                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->Xb, idx->xn,       idx->owner};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : idx->ev_pool) cudaEventDestroy(e);
@@ -781,6 +940,31 @@ int rbc_query_host(rbc_index *idx, const float *hQ, uint64_t m, uint32_t ldq, ui
 int rbc_get_query_stats(const rbc_index *idx, rbc_query_stats *st) {
   if (!idx || !st) return fail(RBC_ERR_INVALID, "rbc_get_query_stats: NULL argument");
   *st = idx->stats;
+  return RBC_OK;
+}
+
+int rbc_set_router(rbc_index *idx, rbc_router *router, uint32_t probes) {
+  if (!idx) return fail(RBC_ERR_INVALID, "rbc_set_router: NULL index");
+  if (router && (router->r.d != idx->d || router->r.L != idx->nr))
+    return fail(RBC_ERR_INVALID, "rbc_set_router: router shape does not match the index (d, number of lists)");
+  if (router && (probes < 1 || probes > 7)) return fail(RBC_ERR_INVALID, "rbc_set_router: probes must be in [1, 7]");
+  idx->router = router;
+  idx->router_probes = router ? probes : 0;
+  return RBC_OK;
+}
+
+int rbc_owner_labels(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t *dLabels, void *stream) {
+  if (!idx || (m && (!dQ || !dLabels))) return fail(RBC_ERR_INVALID, "rbc_owner_labels: bad argument");
+  if (!(idx->flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_INVALID, "rbc_owner_labels: index has no partition");
+  if (m == 0) return RBC_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  DevBuf ids;
+  CK(ids.alloc(m * 4, s));
+  // exact either way; the tensor form is faster when the index has it
+  const uint32_t mode = (idx->flags & RBC_BUILD_BF16) ? RBC_QUERY_EXACT_TC : RBC_QUERY_EXACT;
+  TRY(query_index(idx, dQ, m, ldq, 1, mode, ids.as<uint32_t>(), nullptr, 1, s));
+  CK(launch_owner_lookup(ids.as<uint32_t>(), m, 1, idx->owner, dLabels, s));
+  CK(cudaStreamSynchronize(s));
   return RBC_OK;
 }
 

@@ -9,6 +9,7 @@
 
 #include "../../include/rbc_gb300.h"
 #include "kernels.cuh"
+#include "router.cuh"
 #include "tc.cuh"
 
 namespace rbc {
@@ -43,6 +44,27 @@ struct DevBuf {
   }
 };
 
+// Per-call buffers of one query batch.
+struct QueryBufs {
+  DevBuf Qp, Dqr, probe, probed, res_d, res_i, tau, lock, cnt, start, cursor, tcnt, tstart, pair_q,
+      pair_thr, items, ctl, scan_tmp;
+};
+
+}  // namespace rbc
+
+struct rbc_index;
+
+namespace rbc {
+// Plan one query round (mode 0 probe pairs, mode 1 pruned pairs); stage 0
+// stops after the plan, 1 after the work items, 2 also runs the search.
+// tq < 0 uses the index's tuned tile.
+int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
+                    const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
+                    int grid, unsigned long long *stats, cudaStream_t s, int stage = 2, int tq = -1);
+// Work items a plan of mb queries can produce (query tiles x row chunks).
+uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile);
+int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
+                uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s);
 }  // namespace rbc
 
 struct rbc_index {
@@ -54,9 +76,11 @@ struct rbc_index {
   uint32_t nr = 0, s = 0, lds = 0;
   std::vector<uint32_t> rep_ids;
   // partition (exact search)
+  uint32_t *owner = nullptr;    // original id -> list (nearest representative)
   float *Xp = nullptr;          // n x ld rows, list-major
   uint32_t *perm = nullptr;     // list-major row -> original id
   uint64_t *offsets = nullptr;  // nr + 1
+  std::vector<uint64_t> h_offsets;  // host copy of offsets (tensor-form work units)
   float *radius = nullptr;      // nr
   // representatives
   float *R = nullptr;           // pad16(nr) x ld
@@ -80,6 +104,13 @@ struct rbc_index {
   uint64_t min_list = 0, max_list = 0;
   uint64_t device_bytes = 0;
   rbc_query_stats stats{};
+  // search tuning (rbc_set_tuning / the autotuner): rows-per-thread of the
+  // list-search tile (0 = default) and the longest row run of one work item
+  int tune_tq = 0;
+  uint32_t item_rows = 16384;
+  // learned router (rbc_set_router): probes its top router_probes lists
+  rbc_router *router = nullptr;
+  uint32_t router_probes = 0;
   // benchmark instrumentation (rbc_set_profiling)
   bool profile = false;
   std::vector<cudaEvent_t> ev_pool;  // pairs of events around search launches

@@ -24,6 +24,8 @@ struct SearchItem {
   uint32_t list;  // list (representative) index, or RBC_DUMMY for brute chunks
   uint32_t q0;    // offset of the tile's first query slot in the slot arrays
   uint32_t nq;    // query slots in the tile
+  uint32_t inst;  // instance of a batched launch (0 otherwise)
+  uint32_t pad;
 };
 
 struct SearchArgs {
@@ -42,14 +44,19 @@ struct SearchArgs {
   uint32_t *err;          // error word
   unsigned long long *stats;  // [0] (query, point) pairs, [1] (query, list) pairs
   uint32_t ld, dp, k;
+  // batched launch: per-instance arguments (device array) indexed by item.inst;
+  // the work queue fields (items, nitems, work, err, stats) stay in this struct
+  const SearchArgs *insts;
 };
 
 // Tile geometry of the list-search kernel for a dimensionality.
-int search_tq_for(uint32_t dp);
-int search_query_tile(uint32_t dp);  // 16 * TQ
-size_t search_smem_bytes(uint32_t dp);
-cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_t s);
-int search_grid(int metric, uint32_t dp);
+// Tile geometry of the list-search kernel for a dimensionality; tq (1, 2, 4)
+// overrides the default rows-per-thread when it fits, 0 keeps the default.
+int search_tq_for(uint32_t dp, int tq = 0);
+int search_query_tile(uint32_t dp, int tq = 0);  // 16 * TQ
+size_t search_smem_bytes(uint32_t dp, int tq = 0);
+cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_t s, int tq = 0);
+int search_grid(int metric, uint32_t dp, int tq = 0);
 
 cudaError_t launch_init_results(float *res_d, uint32_t *res_i, uint32_t *tau, uint32_t *lock,
                                 uint64_t m, cudaStream_t s);
@@ -132,11 +139,23 @@ struct PlanArgs {
 // pruning bound survives.  a.phase 0 counts per list into a.list_cnt; phase 1
 // fills pair_q / pair_thr with a.list_cnt pointing at the scanned starts.
 cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s);
-cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, uint32_t nr, uint32_t qtile,
-                                  uint32_t *tile_cnt, cudaStream_t s);
+// Items per list: query tiles x chunks of at most max_rows list rows.
+cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, const uint64_t *offsets, uint32_t nr,
+                                  uint32_t qtile, uint32_t max_rows, uint32_t *tile_cnt, cudaStream_t s);
+// Counting sort of m queries by key[q * stride] in [0, nbins): order[slot] = q,
+// slot_of[q] = slot.  hist, start, cursor hold nbins + 1 words.
+cudaError_t launch_sort_by_key(const uint32_t *key, uint32_t stride, uint64_t m, uint32_t nbins,
+                               uint32_t *hist, uint32_t *start, uint32_t *cursor, void *scan_tmp,
+                               uint32_t *order, uint32_t *slot_of, cudaStream_t s);
+// flags[tile][list] = 1 (tile = slot / 128) for every surviving plan pair
+// (list_cnt may be null: probes only) and every probed pair.
+cudaError_t launch_mark_tiles(const uint32_t *list_start, const uint32_t *list_cnt, const uint32_t *pair_q,
+                              const uint32_t *probe, uint64_t m, uint32_t P, const uint32_t *slot_of,
+                              uint32_t nr, uint8_t *flags, cudaStream_t s);
 cudaError_t launch_plan_items(const uint32_t *list_cnt, const uint32_t *list_start,
                               const uint32_t *tile_start, const uint64_t *offsets, uint32_t nr,
-                              uint32_t qtile, SearchItem *items, uint32_t *nitems, cudaStream_t s);
+                              uint32_t qtile, uint32_t max_rows, SearchItem *items, uint32_t *nitems,
+                              cudaStream_t s);
 
 // Synthetic data.
 cudaError_t launch_synth(int kind, uint64_t seed, uint64_t stream_id, uint64_t r0, uint64_t rows,

@@ -156,35 +156,112 @@ __global__ void plan_kernel(PlanArgs a, uint32_t mode) {
   }
 }
 
-__global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, uint32_t nr, uint32_t qtile,
-                                      uint32_t *__restrict__ tile_cnt) {
+// Work items per list: query tiles x row chunks of at most max_rows rows
+// (long lists are cut so one item cannot hold up the whole launch).
+__device__ __forceinline__ uint32_t row_chunks(const uint64_t *offsets, uint32_t r, uint32_t max_rows) {
+  const uint64_t np = offsets[r + 1] - offsets[r];
+  return np == 0 ? 1u : (uint32_t)((np + max_rows - 1) / max_rows);
+}
+
+__global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, const uint64_t *__restrict__ offsets,
+                                      uint32_t nr, uint32_t qtile, uint32_t max_rows, uint32_t *__restrict__ tile_cnt) {
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < nr) tile_cnt[r] = (list_cnt[r] + qtile - 1) / qtile;
+  if (r < nr) tile_cnt[r] = (list_cnt[r] + qtile - 1) / qtile * row_chunks(offsets, r, max_rows);
   if (r == nr) tile_cnt[nr] = 0;
 }
 
-// items for list r: its query tiles, in list order.
+// items for list r: its query tiles x row chunks, in list order.
 __global__ void plan_items_kernel(const uint32_t *__restrict__ list_cnt, const uint32_t *__restrict__ list_start,
                                   const uint32_t *__restrict__ tile_start, const uint64_t *__restrict__ offsets,
-                                  uint32_t nr, uint32_t qtile, SearchItem *__restrict__ items,
+                                  uint32_t nr, uint32_t qtile, uint32_t max_rows, SearchItem *__restrict__ items,
                                   uint32_t *__restrict__ nitems) {
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r == nr) *nitems = tile_start[nr];
   if (r >= nr) return;
-  uint32_t cnt = list_cnt[r];
-  uint32_t nt = (cnt + qtile - 1) / qtile;
-  for (uint32_t t = 0; t < nt; t++) {
-    SearchItem it;
-    it.p0 = offsets[r];
-    it.np = (uint32_t)(offsets[r + 1] - offsets[r]);
-    it.list = r;
-    it.q0 = list_start[r] + t * qtile;
-    it.nq = min(qtile, cnt - t * qtile);
-    items[tile_start[r] + t] = it;
+  const uint32_t cnt = list_cnt[r];
+  const uint32_t nt = (cnt + qtile - 1) / qtile, nc = row_chunks(offsets, r, max_rows);
+  const uint64_t p0 = offsets[r], np = offsets[r + 1] - offsets[r];
+  uint32_t slot = tile_start[r];
+  for (uint32_t c = 0; c < nc; c++) {
+    for (uint32_t t = 0; t < nt; t++) {
+      SearchItem it;
+      it.p0 = p0 + (uint64_t)c * max_rows;
+      it.np = (uint32_t)min((uint64_t)max_rows, np - (uint64_t)c * max_rows);
+      it.list = r;
+      it.q0 = list_start[r] + t * qtile;
+      it.nq = min(qtile, cnt - t * qtile);
+      it.inst = 0;
+      it.pad = 0;
+      items[slot++] = it;
+    }
   }
 }
 
+// Counting sort of query indices by key (their nearest list): order[slot] = q.
+__global__ void key_hist_kernel(const uint32_t *__restrict__ key, uint32_t stride, uint64_t m,
+                                uint32_t *__restrict__ hist) {
+  uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (q < m) atomicAdd(hist + key[q * stride], 1u);
+}
+
+__global__ void key_scatter_kernel(const uint32_t *__restrict__ key, uint32_t stride, uint64_t m,
+                                   const uint32_t *__restrict__ start, uint32_t *__restrict__ cursor,
+                                   uint32_t *__restrict__ order, uint32_t *__restrict__ slot_of) {
+  uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  const uint32_t k = key[q * stride];
+  const uint32_t slot = start[k] + atomicAdd(cursor + k, 1u);
+  order[slot] = (uint32_t)q;
+  slot_of[q] = slot;
+}
+
+// flags[tile][list] = 1 for every surviving (list, query) pair of the plan
+// (one block per list) and for every probed (query, list) pair.
+__global__ void mark_pairs_kernel(const uint32_t *__restrict__ list_start, const uint32_t *__restrict__ list_cnt,
+                                  const uint32_t *__restrict__ pair_q, const uint32_t *__restrict__ slot_of,
+                                  uint32_t nr, uint8_t *__restrict__ flags) {
+  const uint32_t r = blockIdx.x;
+  const uint32_t s0 = list_start[r], c = list_cnt[r];
+  for (uint32_t i = threadIdx.x; i < c; i += blockDim.x) flags[(uint64_t)(slot_of[pair_q[s0 + i]] / 128) * nr + r] = 1;
+}
+
+__global__ void mark_probes_kernel(const uint32_t *__restrict__ probe, uint64_t m, uint32_t P,
+                                   const uint32_t *__restrict__ slot_of, uint32_t nr, uint8_t *__restrict__ flags) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= m * P) return;
+  const uint64_t q = i / P;
+  const uint32_t r = probe[i];
+  if (r < nr) flags[(uint64_t)(slot_of[q] / 128) * nr + r] = 1;
+}
+
 }  // namespace
+
+cudaError_t launch_sort_by_key(const uint32_t *key, uint32_t stride, uint64_t m, uint32_t nbins, uint32_t *hist,
+                               uint32_t *start, uint32_t *cursor, void *scan_tmp, uint32_t *order, uint32_t *slot_of,
+                               cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(hist, 0, (nbins + 1) * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(cursor, 0, (nbins + 1) * 4, s);
+  if (e != cudaSuccess) return e;
+  key_hist_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(key, stride, m, hist);
+  if ((e = launched()) != cudaSuccess) return e;
+  if ((e = launch_exclusive_scan(hist, start, nbins + 1, scan_tmp, nullptr, s)) != cudaSuccess) return e;
+  key_scatter_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(key, stride, m, start, cursor, order, slot_of);
+  return launched();
+}
+
+cudaError_t launch_mark_tiles(const uint32_t *list_start, const uint32_t *list_cnt, const uint32_t *pair_q,
+                              const uint32_t *probe, uint64_t m, uint32_t P, const uint32_t *slot_of, uint32_t nr,
+                              uint8_t *flags, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  if (list_cnt) {
+    mark_pairs_kernel<<<nr, 128, 0, s>>>(list_start, list_cnt, pair_q, slot_of, nr, flags);
+    if ((e = launched()) != cudaSuccess) return e;
+  }
+  mark_probes_kernel<<<(unsigned)((m * P + 255) / 256), 256, 0, s>>>(probe, m, P, slot_of, nr, flags);
+  return launched();
+}
 
 cudaError_t launch_row_topp(const float *D, uint64_t m, uint32_t nr, uint32_t P, uint32_t *probe, float *probed,
                             cudaStream_t s) {
@@ -203,17 +280,17 @@ cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s) {
   return launched();
 }
 
-cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, uint32_t nr, uint32_t qtile, uint32_t *tile_cnt,
-                                  cudaStream_t s) {
-  tiles_per_list_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, nr, qtile, tile_cnt);
+cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, const uint64_t *offsets, uint32_t nr, uint32_t qtile,
+                                  uint32_t max_rows, uint32_t *tile_cnt, cudaStream_t s) {
+  tiles_per_list_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, offsets, nr, qtile, max_rows, tile_cnt);
   return launched();
 }
 
 cudaError_t launch_plan_items(const uint32_t *list_cnt, const uint32_t *list_start, const uint32_t *tile_start,
-                              const uint64_t *offsets, uint32_t nr, uint32_t qtile, SearchItem *items,
+                              const uint64_t *offsets, uint32_t nr, uint32_t qtile, uint32_t max_rows, SearchItem *items,
                               uint32_t *nitems, cudaStream_t s) {
   plan_items_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, list_start, tile_start, offsets, nr, qtile,
-                                                         items, nitems);
+                                                         max_rows, items, nitems);
   return launched();
 }
 

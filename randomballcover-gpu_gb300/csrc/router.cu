@@ -1,0 +1,574 @@
+// router.cu -- the learned list router: a small MLP trained on the GPU with
+// hand-written forward, backward and optimiser kernels.
+//
+// Model: d -> H -> H -> L (L = number of lists), GELU after the two hidden
+// layers, logits out.  Master weights are FP32; the forward and backward
+// passes read a BF16 copy of the weights (refreshed after every update) and
+// accumulate in FP32.  Training minimises softmax cross-entropy against the
+// list that owns each training query's exact nearest neighbour -- a label the
+// RBC itself produces (rbc_owner_labels) -- with Adam.  At query time the
+// router's top-P lists are searched first, so the k-th distance is tight
+// before the pruning round; exact pruning still decides every other list, so
+// results stay exact whatever the router predicts.
+//
+// Kernels:
+//   gemm_kernel      C = op(A) op(B) (+ bias), 64x64 tiles, 4x4 per thread,
+//                    FP32 or BF16 operands staged as FP32 in shared memory
+//   bias_gelu        h = x + b, a = GELU(h) (exact erf form), h kept
+//   gelu_backward    dh = da * GELU'(h)
+//   softmax_xent     per row: loss and dz = (softmax(z) - onehot(y)) / B
+//   colsum           bias gradients
+//   adam             m, v, w updates and the BF16 weight copy
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "engine.cuh"
+#include "rbc_common.cuh"
+#include "router.cuh"
+
+namespace rbc {
+
+namespace {
+
+constexpr int kGT = 64, kGK = 16;  // GEMM tile (M, N) and K step
+
+template <typename T>
+__device__ __forceinline__ float ldf(const T *p) {
+  return static_cast<float>(*p);
+}
+template <>
+__device__ __forceinline__ float ldf<__nv_bfloat16>(const __nv_bfloat16 *p) {
+  return __bfloat162float(*p);
+}
+
+// C[m][n] = sum_k A(m,k) B(k,n) + bias[n];  A(m,k) = TA ? A[k lda + m] : A[m lda + k],
+// B(k,n) = TB ? B[n ldb + k] : B[k ldb + n].  accumulate: C += instead of =.
+template <bool TA, bool TB, typename AT, typename BT>
+__global__ void __launch_bounds__(256) gemm_kernel(const AT *__restrict__ A, uint32_t lda, const BT *__restrict__ B,
+                                                   uint32_t ldb, float *__restrict__ C, uint32_t ldc, uint32_t M,
+                                                   uint32_t N, uint32_t K, const float *__restrict__ bias,
+                                                   int accumulate) {
+  __shared__ float As[kGK][kGT + 4];
+  __shared__ float Bs[kGK][kGT + 4];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const uint32_t m0 = blockIdx.y * kGT, n0 = blockIdx.x * kGT;
+  float acc[4][4] = {};
+  for (uint32_t k0 = 0; k0 < K; k0 += kGK) {
+    for (int t = threadIdx.x; t < kGK * kGT; t += 256) {
+      int kk, mm;
+      if (TA) {
+        kk = t / kGT;
+        mm = t % kGT;
+      } else {
+        mm = t / kGK;
+        kk = t % kGK;
+      }
+      const uint32_t gm = m0 + mm, gk = k0 + kk;
+      float v = 0.f;
+      if (gm < M && gk < K) v = TA ? ldf(A + (uint64_t)gk * lda + gm) : ldf(A + (uint64_t)gm * lda + gk);
+      As[kk][mm] = v;
+    }
+    for (int t = threadIdx.x; t < kGK * kGT; t += 256) {
+      int kk, nn;
+      if (TB) {
+        nn = t / kGK;
+        kk = t % kGK;
+      } else {
+        kk = t / kGT;
+        nn = t % kGT;
+      }
+      const uint32_t gn = n0 + nn, gk = k0 + kk;
+      float v = 0.f;
+      if (gn < N && gk < K) v = TB ? ldf(B + (uint64_t)gn * ldb + gk) : ldf(B + (uint64_t)gk * ldb + gn);
+      Bs[kk][nn] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kGK; kk++) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const uint32_t gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const uint32_t gn = n0 + tx + 16 * j;
+      if (gn >= N) continue;
+      float v = acc[i][j] + (bias ? bias[gn] : 0.f);
+      float *c = C + (uint64_t)gm * ldc + gn;
+      *c = accumulate ? *c + v : v;
+    }
+  }
+}
+
+template <bool TA, bool TB, typename AT, typename BT>
+cudaError_t gemm(const AT *A, uint32_t lda, const BT *B, uint32_t ldb, float *C, uint32_t ldc, uint32_t M, uint32_t N,
+                 uint32_t K, const float *bias, bool accumulate, cudaStream_t s) {
+  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
+  gemm_kernel<TA, TB, AT, BT><<<grid, 256, 0, s>>>(A, lda, B, ldb, C, ldc, M, N, K, bias, accumulate ? 1 : 0);
+  return launched();
+}
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.3989422804014327f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+// a = GELU(h), in place on h's copy: h stays the pre-activation.
+__global__ void gelu_kernel(const float *__restrict__ h, float *__restrict__ a, uint64_t total) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < total) a[i] = gelu(h[i]);
+}
+
+__global__ void gelu_backward_kernel(const float *__restrict__ h, float *__restrict__ g, uint64_t total) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < total) g[i] *= gelu_grad(h[i]);
+}
+
+// One block per row: loss_i = logsumexp(z) - z_y; dz = (softmax(z) - onehot(y)) * scale.
+__global__ void softmax_xent_kernel(float *__restrict__ z, uint32_t L, const uint32_t *__restrict__ y,
+                                    float *__restrict__ loss, float scale, int want_grad) {
+  __shared__ float red[32];
+  const uint64_t r = blockIdx.x;
+  float *row = z + r * L;
+  float mx = -INFINITY;
+  for (uint32_t j = threadIdx.x; j < L; j += blockDim.x) mx = fmaxf(mx, row[j]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = -INFINITY;
+  for (uint32_t w = 0; w < blockDim.x / 32; w++) mx = fmaxf(mx, red[w]);
+  __syncthreads();
+  float se = 0.f;
+  for (uint32_t j = threadIdx.x; j < L; j += blockDim.x) se += expf(row[j] - mx);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) se += __shfl_xor_sync(0xffffffffu, se, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = se;
+  __syncthreads();
+  se = 0.f;
+  for (uint32_t w = 0; w < blockDim.x / 32; w++) se += red[w];
+  const float lse = mx + logf(se);
+  const uint32_t yl = y[r];
+  if (threadIdx.x == 0 && loss) loss[r] = lse - row[yl];
+  __syncthreads();
+  if (!want_grad) return;
+  for (uint32_t j = threadIdx.x; j < L; j += blockDim.x) {
+    float p = expf(row[j] - lse);
+    row[j] = (p - (j == yl ? 1.f : 0.f)) * scale;
+  }
+}
+
+// out[n] = sum over rows of g[r][n] (bias gradients).
+__global__ void colsum_kernel(const float *__restrict__ g, uint32_t rows, uint32_t N, float *__restrict__ out) {
+  uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float s = 0.f;
+  for (uint32_t r = 0; r < rows; r++) s += g[(uint64_t)r * N + n];
+  out[n] = s;
+}
+
+__global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m1,
+                            float *__restrict__ m2, __nv_bfloat16 *__restrict__ wb, uint64_t total, float lr, float b1,
+                            float b2, float eps, float c1, float c2) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  float gi = g[i];
+  float a = b1 * m1[i] + (1.f - b1) * gi;
+  float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+  m1[i] = a;
+  m2[i] = b;
+  float wi = w[i] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+  w[i] = wi;
+  wb[i] = __float2bfloat16_rn(wi);
+}
+
+__global__ void to_bf16_flat(const float *__restrict__ w, __nv_bfloat16 *__restrict__ wb, uint64_t total) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < total) wb[i] = __float2bfloat16_rn(w[i]);
+}
+
+// Deterministic initialisation: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) from a counter hash.
+__global__ void init_kernel(float *__restrict__ w, uint64_t total, uint64_t seed, uint64_t offset, float scale) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  uint64_t z = seed * 0x9E3779B97F4A7C15ull + offset + i;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  float u = (float)(z >> 40) * 5.9604644775390625e-08f;
+  w[i] = (2.f * u - 1.f) * scale;
+}
+
+// Gather rows of the training set for a batch (order[] holds row indices).
+__global__ void gather_batch_kernel(const float *__restrict__ Q, uint32_t ldq, uint32_t d,
+                                    const uint32_t *__restrict__ order, const uint32_t *__restrict__ labels,
+                                    uint32_t batch, float *__restrict__ X, uint32_t *__restrict__ y) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)batch * d) return;
+  uint32_t r = (uint32_t)(i / d), c = (uint32_t)(i - (uint64_t)r * d);
+  uint32_t src = order[r];
+  X[i] = Q[(uint64_t)src * ldq + c];
+  if (c == 0) y[r] = labels[src];
+}
+
+unsigned blocks(uint64_t total, unsigned t = 256) { return (unsigned)((total + t - 1) / t); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+size_t Router::nparams() const {
+  return (size_t)H * d + H + (size_t)H * H + H + (size_t)L * H + L;
+}
+
+cudaError_t Router::alloc_batch(uint32_t b, cudaStream_t s) {
+  if (b <= cap) return cudaSuccess;
+  for (void *p : {(void *)X, (void *)y, (void *)h1, (void *)a1, (void *)h2, (void *)a2, (void *)z, (void *)ga,
+                  (void *)gb, (void *)loss})
+    if (p) cudaFreeAsync(p, s);
+  cudaError_t e = cudaSuccess;
+  auto al = [&](auto **p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)p, bytes, s);
+  };
+  al(&X, (size_t)b * d * 4);
+  al(&y, (size_t)b * 4);
+  al(&h1, (size_t)b * H * 4);
+  al(&a1, (size_t)b * H * 4);
+  al(&h2, (size_t)b * H * 4);
+  al(&a2, (size_t)b * H * 4);
+  al(&z, (size_t)b * L * 4);
+  al(&ga, (size_t)b * H * 4);
+  al(&gb, (size_t)b * H * 4);
+  al(&loss, (size_t)b * 4);
+  cap = e == cudaSuccess ? b : 0;
+  return e;
+}
+
+// Forward pass of `b` rows of X (b x d, stride d) into logits z (b x L).
+cudaError_t Router::forward(const float *Xin, uint32_t ldx, uint32_t b, float *zout, cudaStream_t s) {
+  const __nv_bfloat16 *W1 = wb, *W2 = wb + (size_t)H * d + H, *W3 = W2 + (size_t)H * H + H;
+  const float *b1 = w + (size_t)H * d, *b2 = b1 + H + (size_t)H * H, *b3 = b2 + H + (size_t)L * H;
+  cudaError_t e = gemm<false, true>(Xin, ldx, W1, d, h1, H, b, H, d, b1, false, s);
+  if (e == cudaSuccess) {
+    gelu_kernel<<<blocks((uint64_t)b * H), 256, 0, s>>>(h1, a1, (uint64_t)b * H);
+    e = launched();
+  }
+  if (e == cudaSuccess) e = gemm<false, true>(a1, H, W2, H, h2, H, b, H, H, b2, false, s);
+  if (e == cudaSuccess) {
+    gelu_kernel<<<blocks((uint64_t)b * H), 256, 0, s>>>(h2, a2, (uint64_t)b * H);
+    e = launched();
+  }
+  if (e == cudaSuccess) e = gemm<false, true>(a2, H, W3, H, zout, L, b, L, H, b3, false, s);
+  return e;
+}
+
+// Loss and gradients (into g) of the batch already in X / y; z is overwritten by dz.
+cudaError_t Router::forward_backward(uint32_t b, cudaStream_t s) {
+  const __nv_bfloat16 *W2 = wb + (size_t)H * d + H, *W3 = W2 + (size_t)H * H + H;
+  float *gW1 = g, *gb1 = g + (size_t)H * d, *gW2 = gb1 + H, *gb2 = gW2 + (size_t)H * H, *gW3 = gb2 + H,
+        *gb3 = gW3 + (size_t)L * H;
+  cudaError_t e = forward(X, d, b, z, s);
+  if (e != cudaSuccess) return e;
+  softmax_xent_kernel<<<b, 256, 0, s>>>(z, L, y, loss, 1.f / b, 1);
+  if ((e = launched()) != cudaSuccess) return e;
+  // layer 3: dW3 = dz^T a2, db3 = colsum dz, da2 = dz W3
+  if ((e = gemm<true, false>(z, L, a2, H, gW3, H, L, H, b, nullptr, false, s)) != cudaSuccess) return e;
+  colsum_kernel<<<blocks(L), 256, 0, s>>>(z, b, L, gb3);
+  if ((e = launched()) != cudaSuccess) return e;
+  if ((e = gemm<false, false>(z, L, W3, H, ga, H, b, H, L, nullptr, false, s)) != cudaSuccess) return e;
+  gelu_backward_kernel<<<blocks((uint64_t)b * H), 256, 0, s>>>(h2, ga, (uint64_t)b * H);
+  if ((e = launched()) != cudaSuccess) return e;
+  // layer 2
+  if ((e = gemm<true, false>(ga, H, a1, H, gW2, H, H, H, b, nullptr, false, s)) != cudaSuccess) return e;
+  colsum_kernel<<<blocks(H), 256, 0, s>>>(ga, b, H, gb2);
+  if ((e = launched()) != cudaSuccess) return e;
+  if ((e = gemm<false, false>(ga, H, W2, H, gb, H, b, H, H, nullptr, false, s)) != cudaSuccess) return e;
+  gelu_backward_kernel<<<blocks((uint64_t)b * H), 256, 0, s>>>(h1, gb, (uint64_t)b * H);
+  if ((e = launched()) != cudaSuccess) return e;
+  // layer 1
+  if ((e = gemm<true, false>(gb, H, X, d, gW1, d, H, d, b, nullptr, false, s)) != cudaSuccess) return e;
+  colsum_kernel<<<blocks(H), 256, 0, s>>>(gb, b, H, gb1);
+  return launched();
+}
+
+cudaError_t Router::adam_step(float lr, cudaStream_t s) {
+  step++;
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  const uint64_t P = nparams();
+  adam_kernel<<<blocks(P), 256, 0, s>>>(w, g, m1, m2, wb, P, lr, b1, b2, eps, c1, c2);
+  return launched();
+}
+
+cudaError_t Router::refresh_bf16(cudaStream_t s) {
+  const uint64_t P = nparams();
+  to_bf16_flat<<<blocks(P), 256, 0, s>>>(w, wb, P);
+  return launched();
+}
+
+cudaError_t Router::init(uint64_t seed, cudaStream_t s) {
+  const uint64_t sizes[6] = {(uint64_t)H * d, H, (uint64_t)H * H, H, (uint64_t)L * H, L};
+  const float fan[6] = {(float)d, (float)d, (float)H, (float)H, (float)H, (float)H};
+  uint64_t off = 0;
+  for (int i = 0; i < 6; i++) {
+    init_kernel<<<blocks(sizes[i]), 256, 0, s>>>(w + off, sizes[i], seed, off, 1.f / sqrtf(fan[i]));
+    cudaError_t e = launched();
+    if (e != cudaSuccess) return e;
+    off += sizes[i];
+  }
+  cudaError_t e = cudaMemsetAsync(m1, 0, nparams() * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m2, 0, nparams() * 4, s);
+  step = 0;
+  return e == cudaSuccess ? refresh_bf16(s) : e;
+}
+
+cudaError_t Router::gather(const float *Q, uint32_t ldq, const uint32_t *order, const uint32_t *labels, uint32_t b,
+                           cudaStream_t s) {
+  gather_batch_kernel<<<blocks((uint64_t)b * d), 256, 0, s>>>(Q, ldq, d, order, labels, b, X, y);
+  return launched();
+}
+
+Router::~Router() {
+  for (void *p : {(void *)w, (void *)g, (void *)m1, (void *)m2, (void *)wb, (void *)X, (void *)y, (void *)h1,
+                  (void *)a1, (void *)h2, (void *)a2, (void *)z, (void *)ga, (void *)gb, (void *)loss})
+    if (p) cudaFree(p);
+}
+
+namespace {
+
+// One warp per row: the P largest logits (ties to the lower list index) into
+// columns 1..P, the nearest representative into column 0.
+__global__ void router_probes_kernel(const float *__restrict__ z, uint64_t m, uint32_t L, uint32_t P,
+                                     const uint32_t *__restrict__ nearest, const float *__restrict__ nearest_d,
+                                     uint32_t *__restrict__ probe, float *__restrict__ probed) {
+  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (q >= m) return;
+  const float *row = z + q * L;
+  const uint32_t W = 1 + P;
+  uint32_t taken[8];
+  for (uint32_t p = 0; p < P; p++) {
+    float bv = -INFINITY;
+    uint32_t bi = RBC_DUMMY;
+    for (uint32_t j = lane; j < L; j += 32) {
+      bool used = false;
+      for (uint32_t t = 0; t < p; t++) used |= taken[t] == j;
+      float v = row[j];
+      if (!used && (v > bv || (v == bv && j < bi))) {
+        bv = v;
+        bi = j;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    taken[p] = bi;
+    if (lane == 0) {
+      probe[q * W + 1 + p] = bi;
+      probed[q * W + 1 + p] = 0.f;
+    }
+  }
+  if (lane == 0) {
+    probe[q * W] = nearest[q];
+    probed[q * W] = nearest_d[q];
+  }
+}
+
+__global__ void owner_lookup_kernel(const uint32_t *__restrict__ ids, uint64_t m, uint32_t ldo,
+                                    const uint32_t *__restrict__ owner, uint32_t *__restrict__ labels) {
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i < m) {
+    uint32_t id = ids[i * ldo];
+    labels[i] = id == RBC_DUMMY ? 0u : owner[id];
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_router_probes(const float *logits, uint64_t m, uint32_t L, uint32_t P, const uint32_t *nearest,
+                                 const float *nearest_d, uint32_t *probe, float *probed, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  router_probes_kernel<<<blocks(m * 32), 256, 0, s>>>(logits, m, L, P, nearest, nearest_d, probe, probed);
+  return launched();
+}
+
+cudaError_t launch_owner_lookup(const uint32_t *ids, uint64_t m, uint32_t ldo, const uint32_t *owner,
+                                uint32_t *labels, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  owner_lookup_kernel<<<blocks(m), 256, 0, s>>>(ids, m, ldo, owner, labels);
+  return launched();
+}
+
+}  // namespace rbc
+
+// ====================================================================== C ABI
+using namespace rbc;
+
+#define RCK(expr)                                       \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #expr); \
+  } while (0)
+
+extern "C" {
+
+int rbc_router_create(uint32_t d, uint32_t hidden, uint32_t num_lists, uint64_t seed, rbc_router **out) {
+  if (!out) return fail(RBC_ERR_INVALID, "rbc_router_create: out is NULL");
+  *out = nullptr;
+  if (d == 0 || hidden == 0 || num_lists == 0) return fail(RBC_ERR_INVALID, "rbc_router_create: zero size");
+  rbc_router *rt = new rbc_router();
+  Router &r = rt->r;
+  r.d = d;
+  r.H = hidden;
+  r.L = num_lists;
+  const size_t P = r.nparams();
+  cudaError_t e = cudaMalloc(&r.w, P * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&r.g, P * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&r.m1, P * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&r.m2, P * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&r.wb, P * 2);
+  if (e == cudaSuccess) e = r.init(seed, nullptr);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
+  if (e != cudaSuccess) {
+    delete rt;
+    return cuda_fail(e, "rbc_router_create");
+  }
+  *out = rt;
+  return RBC_OK;
+}
+
+int rbc_router_destroy(rbc_router *router) {
+  delete router;
+  return RBC_OK;
+}
+
+int rbc_router_num_params(const rbc_router *router, uint64_t *count) {
+  if (!router || !count) return fail(RBC_ERR_INVALID, "rbc_router_num_params: NULL argument");
+  *count = router->r.nparams();
+  return RBC_OK;
+}
+
+int rbc_router_get_params(const rbc_router *router, float *h_params) {
+  if (!router || !h_params) return fail(RBC_ERR_INVALID, "rbc_router_get_params: NULL argument");
+  RCK(cudaMemcpy(h_params, router->r.w, router->r.nparams() * 4, cudaMemcpyDeviceToHost));
+  return RBC_OK;
+}
+
+int rbc_router_set_params(rbc_router *router, const float *h_params) {
+  if (!router || !h_params) return fail(RBC_ERR_INVALID, "rbc_router_set_params: NULL argument");
+  RCK(cudaMemcpy(router->r.w, h_params, router->r.nparams() * 4, cudaMemcpyHostToDevice));
+  RCK(router->r.refresh_bf16(nullptr));
+  RCK(cudaStreamSynchronize(nullptr));
+  return RBC_OK;
+}
+
+int rbc_router_gradients(rbc_router *router, const float *dQ, uint32_t batch, uint32_t ldq, const uint32_t *dLabels,
+                         float *loss, float *h_grads, void *stream) {
+  if (!router || !dQ || !dLabels || batch == 0) return fail(RBC_ERR_INVALID, "rbc_router_gradients: bad argument");
+  if (ldq < router->r.d) return fail(RBC_ERR_INVALID, "rbc_router_gradients: ldq < d");
+  Router &r = router->r;
+  cudaStream_t s = (cudaStream_t)stream;
+  RCK(r.alloc_batch(batch, s));
+  std::vector<uint32_t> order(batch);
+  for (uint32_t i = 0; i < batch; i++) order[i] = i;
+  uint32_t *dorder = nullptr;
+  RCK(cudaMallocAsync(&dorder, batch * 4, s));
+  RCK(cudaMemcpyAsync(dorder, order.data(), batch * 4, cudaMemcpyHostToDevice, s));
+  RCK(r.gather(dQ, ldq, dorder, dLabels, batch, s));
+  RCK(r.forward_backward(batch, s));
+  std::vector<float> l(batch);
+  RCK(cudaMemcpyAsync(l.data(), r.loss, batch * 4, cudaMemcpyDeviceToHost, s));
+  if (h_grads) RCK(cudaMemcpyAsync(h_grads, r.g, r.nparams() * 4, cudaMemcpyDeviceToHost, s));
+  RCK(cudaFreeAsync(dorder, s));
+  RCK(cudaStreamSynchronize(s));
+  if (loss) {
+    double t = 0;
+    for (float v : l) t += v;
+    *loss = (float)(t / batch);
+  }
+  return RBC_OK;
+}
+
+int rbc_router_train(rbc_router *router, const float *dQ, uint64_t n, uint32_t ldq, const uint32_t *dLabels,
+                     uint32_t epochs, uint32_t batch, float lr, uint64_t seed, float *final_loss, void *stream) {
+  if (!router || !dQ || !dLabels || n == 0 || batch == 0) return fail(RBC_ERR_INVALID, "rbc_router_train: bad argument");
+  if (ldq < router->r.d) return fail(RBC_ERR_INVALID, "rbc_router_train: ldq < d");
+  if (n >= 0xFFFFFFFFull) return fail(RBC_ERR_INVALID, "rbc_router_train: too many samples");
+  Router &r = router->r;
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t b = (uint32_t)std::min<uint64_t>(batch, n);
+  RCK(r.alloc_batch(b, s));
+  std::vector<uint32_t> order(n);
+  uint32_t *dorder = nullptr;
+  RCK(cudaMallocAsync(&dorder, n * 4, s));
+  uint64_t state = seed * 0x9E3779B97F4A7C15ull + 1;
+  auto next = [&]() {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  double last = 0;
+  for (uint32_t ep = 0; ep < epochs; ep++) {
+    for (uint64_t i = 0; i < n; i++) order[i] = (uint32_t)i;
+    for (uint64_t i = n - 1; i > 0; i--) std::swap(order[i], order[next() % (i + 1)]);
+    RCK(cudaMemcpyAsync(dorder, order.data(), n * 4, cudaMemcpyHostToDevice, s));
+    RCK(cudaStreamSynchronize(s));  // order[] is reshuffled next epoch
+    const uint64_t steps = n / b;
+    for (uint64_t t = 0; t < steps; t++) {
+      RCK(r.gather(dQ, ldq, dorder + t * b, dLabels, b, s));
+      RCK(r.forward_backward(b, s));
+      RCK(r.adam_step(lr, s));
+    }
+  }
+  if (final_loss) {
+    std::vector<float> l(b);
+    RCK(cudaMemcpyAsync(l.data(), r.loss, b * 4, cudaMemcpyDeviceToHost, s));
+    RCK(cudaStreamSynchronize(s));
+    for (float v : l) last += v;
+    *final_loss = (float)(last / b);
+  }
+  RCK(cudaFreeAsync(dorder, s));
+  RCK(cudaStreamSynchronize(s));
+  return RBC_OK;
+}
+
+int rbc_router_logits(rbc_router *router, const float *dQ, uint64_t m, uint32_t ldq, float *dLogits, void *stream) {
+  if (!router || (m && (!dQ || !dLogits))) return fail(RBC_ERR_INVALID, "rbc_router_logits: bad argument");
+  Router &r = router->r;
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t chunk = 4096;
+  RCK(r.alloc_batch(chunk, s));
+  for (uint64_t i = 0; i < m; i += chunk) {
+    const uint32_t b = (uint32_t)std::min<uint64_t>(chunk, m - i);
+    RCK(r.forward(dQ + i * ldq, ldq, b, dLogits + i * r.L, s));
+  }
+  RCK(cudaStreamSynchronize(s));
+  return RBC_OK;
+}
+
+}  // extern "C"

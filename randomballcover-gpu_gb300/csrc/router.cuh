@@ -1,0 +1,49 @@
+// router.cuh -- the learned list router (router.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace rbc {
+
+// MLP d -> H -> H -> L with GELU; parameters flat [W1 b1 W2 b2 W3 b3], FP32
+// master copy w, gradients g, Adam moments m1 m2, BF16 weight copy wb.
+struct Router {
+  uint32_t d = 0, H = 0, L = 0;
+  float *w = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;
+  __nv_bfloat16 *wb = nullptr;
+  uint64_t step = 0;
+  // batch workspace
+  uint32_t cap = 0;
+  float *X = nullptr;
+  uint32_t *y = nullptr;
+  float *h1 = nullptr, *a1 = nullptr, *h2 = nullptr, *a2 = nullptr, *z = nullptr, *ga = nullptr, *gb = nullptr,
+        *loss = nullptr;
+
+  size_t nparams() const;
+  cudaError_t init(uint64_t seed, cudaStream_t s);
+  cudaError_t alloc_batch(uint32_t b, cudaStream_t s);
+  cudaError_t gather(const float *Q, uint32_t ldq, const uint32_t *order, const uint32_t *labels, uint32_t b,
+                     cudaStream_t s);
+  cudaError_t forward(const float *X, uint32_t ldx, uint32_t b, float *z, cudaStream_t s);
+  cudaError_t forward_backward(uint32_t b, cudaStream_t s);
+  cudaError_t adam_step(float lr, cudaStream_t s);
+  cudaError_t refresh_bf16(cudaStream_t s);
+  ~Router();
+};
+
+// Top-P lists of each row of router logits (largest first, ties to the lower
+// list), written to columns [1, 1+P) of a probe table of width 1+P whose
+// column 0 holds the nearest representative.
+cudaError_t launch_router_probes(const float *logits, uint64_t m, uint32_t L, uint32_t P, const uint32_t *nearest,
+                                 const float *nearest_d, uint32_t *probe, float *probed, cudaStream_t s);
+// labels[i] = owner[ids[i]]
+cudaError_t launch_owner_lookup(const uint32_t *ids, uint64_t m, uint32_t ldo, const uint32_t *owner,
+                                uint32_t *labels, cudaStream_t s);
+
+}  // namespace rbc
+
+struct rbc_router {
+  rbc::Router r;
+};

@@ -64,24 +64,27 @@ size_t smem_bytes_tq(uint32_t dp) {
   return (floats + words) * 4;
 }
 
+// g holds the work queue; each item's data come from g itself or, in a
+// batched launch over many independent indexes, from g.insts[item.inst].
 template <int METRIC, int TQ>
-__global__ void __launch_bounds__(kTileThreads, 2) search_kernel(SearchArgs a) {
+__global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_constant__ SearchArgs g) {
   constexpr int BQ = 16 * TQ;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ uint32_t s_item;
-  const uint32_t S = a.dp + 4;
-  SearchSmem sm = carve<TQ>(smem_raw, S);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int tq = tid >> 4, tx = tid & 15;
-  const uint32_t kk = a.k;
   unsigned long long my_pairs = 0, my_lists = 0;
 
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(a.work, 1u);
+    if (tid == 0) s_item = atomicAdd(g.work, 1u);
     __syncthreads();
     const uint32_t it = s_item;
-    if (it >= *a.nitems) break;
-    const SearchItem item = a.items[it];
+    if (it >= *g.nitems) break;
+    const SearchItem item = g.items[it];
+    const SearchArgs &a = g.insts ? g.insts[item.inst] : g;
+    const uint32_t S = a.dp + 4;
+    const SearchSmem sm = carve<TQ>(smem_raw, S);
+    const uint32_t kk = a.k;
 
     // ---- stage the query tile, thresholds and empty lists ----
     for (uint32_t t = tid; t < BQ; t += kTileThreads) {
@@ -197,7 +200,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(SearchArgs a) {
           __nanosleep(32);
         }
         got = spins <= kLockSpinLimit;
-        if (!got) raise_error(a.err, RBC_ERR_ITER_LIMIT);
+        if (!got) raise_error(g.err, RBC_ERR_ITER_LIMIT);
       }
       got = __shfl_sync(0xffffffffu, got, 0);
       if (!got) continue;
@@ -217,9 +220,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(SearchArgs a) {
     }
     __syncthreads();
   }
-  if (a.stats && tid == 0 && my_lists) {
-    atomicAdd(a.stats, my_pairs);
-    atomicAdd(a.stats + 1, my_lists);
+  if (g.stats && tid == 0 && my_lists) {
+    atomicAdd(g.stats, my_pairs);
+    atomicAdd(g.stats + 1, my_lists);
   }
 }
 
@@ -293,6 +296,8 @@ __global__ void brute_items_kernel(SearchItem *items, uint32_t *nitems, uint32_t
     it.list = RBC_DUMMY;
     it.q0 = (uint32_t)(t * qtile);
     it.nq = (uint32_t)min((uint64_t)qtile, m - t * qtile);
+    it.inst = 0;
+    it.pad = 0;
     items[i] = it;
   }
   if (i == 0) *nitems = (uint32_t)(nchunks * ntile);
@@ -300,26 +305,32 @@ __global__ void brute_items_kernel(SearchItem *items, uint32_t *nitems, uint32_t
 
 }  // namespace
 
-int search_tq_for(uint32_t dp) { return dp <= 128 ? 4 : (dp <= 256 ? 2 : 1); }
-int search_query_tile(uint32_t dp) { return 16 * search_tq_for(dp); }
+// Rows per thread in the query dimension (query tile = 16 TQ).  The default
+// keeps the shared-memory tile under ~100 KB; `tq` (1, 2 or 4) overrides it
+// when that tile still fits (the autotuner's knob).
+int search_tq_for(uint32_t dp, int tq) {
+  if ((tq == 1 || tq == 2 || tq == 4) && (tq == 1 || dp <= 256 / (tq / 2))) return tq;
+  return dp <= 128 ? 4 : (dp <= 256 ? 2 : 1);
+}
+int search_query_tile(uint32_t dp, int tq) { return 16 * search_tq_for(dp, tq); }
 
-size_t search_smem_bytes(uint32_t dp) {
-  switch (search_tq_for(dp)) {
+size_t search_smem_bytes(uint32_t dp, int tq) {
+  switch (search_tq_for(dp, tq)) {
     case 4: return smem_bytes_tq<4>(dp);
     case 2: return smem_bytes_tq<2>(dp);
     default: return smem_bytes_tq<1>(dp);
   }
 }
 
-int search_grid(int metric, uint32_t dp) {
-  int tqv = search_tq_for(dp);
+int search_grid(int metric, uint32_t dp, int tq) {
+  int tqv = search_tq_for(dp, tq);
   if (metric == RBC_L1)
     return tqv == 4 ? grid_tq<RBC_L1, 4>(dp) : tqv == 2 ? grid_tq<RBC_L1, 2>(dp) : grid_tq<RBC_L1, 1>(dp);
   return tqv == 4 ? grid_tq<RBC_L2, 4>(dp) : tqv == 2 ? grid_tq<RBC_L2, 2>(dp) : grid_tq<RBC_L2, 1>(dp);
 }
 
-cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_t s) {
-  int tqv = search_tq_for(a.dp);
+cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_t s, int tq) {
+  int tqv = search_tq_for(a.dp, tq);
   if (metric == RBC_L1)
     return tqv == 4 ? launch_tq<RBC_L1, 4>(a, grid, s)
                     : tqv == 2 ? launch_tq<RBC_L1, 2>(a, grid, s) : launch_tq<RBC_L1, 1>(a, grid, s);

@@ -22,8 +22,10 @@ struct TcArgs {
   uint32_t nunits;
   uint32_t kblocks;     // K / 64 (BF16 elements per 128-byte swizzled row)
   const float *xn;      // squared norm per database row (padded rows: +inf)
-  float *sl_a;          // per query: SL approx values (without ||q||^2), ascending
-  uint32_t *sl_row;     // per query: SL database rows
+  uint64_t m_pad;       // query slots (multiple of 128)
+  float *sl_a;          // [2][m_pad][SL] approx values (without ||q||^2), ascending
+  uint32_t *sl_row;     // [2][m_pad][SL] database rows
+  uint32_t *sl_sel;     // per query: which of the two buffers is current
   uint32_t *sl_theta;   // per query: largest approx kept once SL rows are held
   uint32_t *sl_lock;
   uint32_t *err;
@@ -32,11 +34,13 @@ struct TcArgs {
 struct RerankArgs {
   const float *X;        // FP32 database rows (list-major), stride ld
   const uint32_t *pid;   // row -> original id
-  const float *Q;        // FP32 query rows, stride ld
+  const float *Q;        // FP32 query rows in slot order, stride ld
+  const uint32_t *order; // slot -> query index (output row); nullptr: identity
   uint32_t ld, dp, k;
-  uint64_t m;
+  uint64_t m, m_pad;
   const float *sl_a;
   const uint32_t *sl_row;
+  const uint32_t *sl_sel;
   const float *qn;
   const uint8_t *q_inexact;
   uint32_t x_inexact;
@@ -83,8 +87,8 @@ cudaError_t launch_to_bf16(const float *src, uint32_t ld, uint64_t rows, uint64_
                            uint32_t *maxnorm_bits, cudaStream_t s);
 cudaError_t launch_row_inexact(const float *src, uint32_t ld, uint64_t rows, uint32_t d, uint8_t *flag,
                                cudaStream_t s);
-cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *lock, uint64_t m,
-                           cudaStream_t s);
+cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
+                           uint64_t m, cudaStream_t s);
 cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
                              cudaStream_t s);
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s);

@@ -16,19 +16,22 @@
 // so the result equals the FP32 oracle's; otherwise the query is recomputed
 // by the plain FP32 path.  Either way the ids are bit-exact.
 //
-// Kernel structure (one persistent CTA per SM, 256 threads):
+// Kernel structure (one persistent CTA per SM, 384 threads):
 //   warp 0      TMA producer: the 128-query A tile of each work unit, then
 //               128-row B tiles of the unit's row range into a 3-stage ring
-//               (128-byte swizzled, K-major);
+//               (128-byte swizzled, K-major), and each B tile's row norms
+//               (one 512-byte bulk copy) into a 4-slot ring;
 //   warp 1      tcgen05.mma issuer: 128x128xK per B tile into one of four
 //               128-column TMEM accumulators; tcgen05.commit frees the smem
 //               stage and hands the accumulator to the epilogue;
-//   warps 4-7   epilogue: tcgen05.ld of the accumulator row of its query
-//               (one TMEM lane per thread), approx via one FMA with the row
-//               norm, filter against the query's running threshold, sorted
-//               insertion into a per-thread shortlist in shared memory; at the
-//               end of a unit the shortlist is merged into the query's global
-//               shortlist under a bounded per-query lock.
+//   warps 4-11  epilogue, two warpgroups taking alternate tiles: tcgen05.ld
+//               of the accumulator row of its query (one TMEM lane per
+//               thread), approx via one FMA with the row norm, a running
+//               minimum per 32 columns against the query's threshold (one
+//               branch per 32 values), sorted insertion into a per-thread
+//               shortlist in shared memory; at the end of a unit the
+//               shortlist is merged into the query's global shortlist
+//               (double-buffered) under a bounded per-query lock.
 // All mbarrier waits are bounded (sm100.cuh); a timeout sets the error word.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -47,7 +50,8 @@ namespace {
 
 using namespace sm100;
 
-constexpr int kBM = 128, kBN = 128, kStages = 3, kBufs = 4;
+constexpr int kBM = 128, kBN = 128, kStages = 3, kBufs = 4, kEpiGroups = 2;
+constexpr int kThreads = 128 + 128 * kEpiGroups;
 constexpr int kSL = kShortlist, kLST = kShortlist + 1;  // odd stride: no bank conflicts across threads
 constexpr uint32_t kTile16K = 16384;                    // 128 rows x 128 bytes (one 64-wide K block)
 constexpr uint32_t kLockSpin = 1u << 22;
@@ -84,21 +88,75 @@ __device__ __forceinline__ bool row_less(float a, uint32_t ra, float b, uint32_t
   return a < b || (a == b && ra < rb);
 }
 
-__global__ void __launch_bounds__(256, 1)
+// Merge a thread's sorted local shortlist into the query's global one (the
+// current buffer is read, the merged list goes to the other buffer, then the
+// buffers swap), under the query's lock.
+__device__ void publish(const TcArgs &a, uint32_t q, const float *myla, const uint32_t *myli, uint32_t nl) {
+  uint32_t spins = 0;
+  while (atomicCAS(a.sl_lock + q, 0u, 1u) != 0u) {
+    if (++spins > kLockSpin) {
+      raise_error(a.err, RBC_ERR_ITER_LIMIT);
+      return;
+    }
+    __nanosleep(64);
+  }
+  __threadfence();
+  const uint32_t sel = __ldcg(a.sl_sel + q);
+  const float *ga = a.sl_a + ((uint64_t)sel * a.m_pad + q) * kSL;
+  const uint32_t *gi = a.sl_row + ((uint64_t)sel * a.m_pad + q) * kSL;
+  float *oa = a.sl_a + ((uint64_t)(sel ^ 1u) * a.m_pad + q) * kSL;
+  uint32_t *oi = a.sl_row + ((uint64_t)(sel ^ 1u) * a.m_pad + q) * kSL;
+  float cur_a[kSL];
+  uint32_t cur_i[kSL];
+  uint32_t ng = 0;
+#pragma unroll
+  for (int t = 0; t < kSL; t++) {
+    cur_a[t] = __ldcg(ga + t);
+    cur_i[t] = __ldcg(gi + t);
+  }
+  for (int t = 0; t < kSL; t++) ng += cur_i[t] != RBC_DUMMY;
+  uint32_t i = 0, j = 0, t = 0;
+  float last = FLT_MAX;
+  for (; t < kSL && (i < nl || j < ng); t++) {
+    const bool take_local = j >= ng || (i < nl && row_less(myla[i], myli[i], cur_a[j], cur_i[j]));
+    if (take_local) {
+      oa[t] = last = myla[i];
+      oi[t] = myli[i];
+      i++;
+    } else {
+      oa[t] = last = cur_a[j];
+      oi[t] = cur_i[j];
+      j++;
+    }
+  }
+  // FLT_MAX, not +inf, while the list is short: padded rows (norm +inf)
+  // must never pass the filter.
+  const float newtheta = t == kSL ? last : FLT_MAX;
+  for (; t < kSL; t++) {
+    oa[t] = INFINITY;
+    oi[t] = RBC_DUMMY;
+  }
+  a.sl_theta[q] = __float_as_uint(newtheta);
+  a.sl_sel[q] = sel ^ 1u;
+  __threadfence();
+  atomicExch(a.sl_lock + q, 0u);
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_a_full, bar_a_empty, bar_b_full[kStages], bar_b_empty[kStages],
-      bar_t_full[kBufs], bar_t_empty[kBufs];
+      bar_t_full[kBufs], bar_t_empty[kBufs], bar_x_full[kBufs];
   __shared__ uint32_t tmem_slot;
 
-  unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char *base =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const uint32_t kb = a.kblocks;
   unsigned char *sA = base;
   unsigned char *sB = sA + kb * kTile16K;
-  float *la = reinterpret_cast<float *>(sB + kStages * kb * kTile16K);
-  uint32_t *li = reinterpret_cast<uint32_t *>(la + kBM * kLST);
-  float *sa = reinterpret_cast<float *>(li + kBM * kLST);
-  uint32_t *si = reinterpret_cast<uint32_t *>(sa + kBM * kLST);
+  float *xs = reinterpret_cast<float *>(sB + kStages * kb * kTile16K);  // kBufs x 128 row norms
+  float *la = xs + kBufs * kBN;                                          // per epilogue thread: kLST approx
+  uint32_t *li = reinterpret_cast<uint32_t *>(la + kEpiGroups * kBM * kLST);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 1) {
@@ -115,6 +173,7 @@ __global__ void __launch_bounds__(256, 1)
     for (int b = 0; b < kBufs; b++) {
       mbar_init(&bar_t_full[b], 1);
       mbar_init(&bar_t_empty[b], 4);
+      mbar_init(&bar_x_full[b], 1);
     }
     fence_barrier_init();
   }
@@ -138,17 +197,22 @@ __global__ void __launch_bounds__(256, 1)
         for (uint32_t k = 0; k < kb; k++)
           tma_load_2d(sA + k * kTile16K, &tmA, (int32_t)(k * 64), (int32_t)(un.tile * kBM), &bar_a_full);
         for (uint64_t p = un.p0; p < un.p1; p += kBN, it++) {
-          const uint32_t s = it % kStages, use = it / kStages;
+          const uint32_t s = it % kStages, use = it / kStages, b = it % kBufs;
           if (use > 0 && !(ok = mbar_wait(&bar_b_empty[s], (use - 1) & 1, a.err))) break;
           mbar_expect_tx(&bar_b_full[s], bytes_b);
           for (uint32_t k = 0; k < kb; k++)
             tma_load_2d(sB + (s * kb + k) * kTile16K, &tmB, (int32_t)(k * 64), (int32_t)p, &bar_b_full[s]);
+          // the norm slot b is free once the epilogue released tile it - kBufs
+          if (it >= kBufs && !(ok = mbar_wait(&bar_t_empty[b], ((it / kBufs) - 1) & 1, a.err))) break;
+          mbar_expect_tx(&bar_x_full[b], kBN * 4);
+          bulk_load(xs + b * kBN, a.xn + p, kBN * 4, &bar_x_full[b]);
         }
       }
       // drain: wait (bounded) for the copies still in flight before leaving
-      for (uint32_t j = 0; j < kStages && j < it; j++) {
+      for (uint32_t j = 0; j < kBufs && j < it; j++) {
         const uint32_t t = it - 1 - j;
-        mbar_wait(&bar_b_full[t % kStages], (t / kStages) & 1, nullptr);
+        if (j < kStages) mbar_wait(&bar_b_full[t % kStages], (t / kStages) & 1, nullptr);
+        mbar_wait(&bar_x_full[t % kBufs], (t / kBufs) & 1, nullptr);
       }
     }
   } else if (warp == 1) {
@@ -180,15 +244,14 @@ __global__ void __launch_bounds__(256, 1)
       }
     }
   } else if (warp >= 4) {
-    // ------------------------------------------------ epilogue
-    const uint32_t et = tid - 128, ew = warp - 4;
-    float *myla = la + et * kLST;
-    uint32_t *myli = li + et * kLST;
+    // ------------------------------------------------ epilogue (two warpgroups)
+    const uint32_t grp = (warp - 4) >> 2, ew = warp & 3, et = ew * 32 + lane;
+    float *myla = la + (grp * kBM + et) * kLST;
+    uint32_t *myli = li + (grp * kBM + et) * kLST;
     TileSeq cur;
     cur.start(a.units, blockIdx.x, a.nunits, gridDim.x);
-    uint32_t it = 0, nl = 0;
+    uint32_t it = 0, nl = 0, q = 0;
     float theta = 0.f;
-    uint32_t q = 0;
     bool ok = true;
     for (; cur.valid() && ok; cur.advance(), it++) {
       if (cur.first()) {
@@ -196,31 +259,34 @@ __global__ void __launch_bounds__(256, 1)
         nl = 0;
         theta = __uint_as_float(__ldcg(a.sl_theta + q));
       }
-      // row norms of this tile: the same 128 values for every thread, read as
-      // broadcast float4 loads (L1 hits after the first warp)
-      const float4 *xg = reinterpret_cast<const float4 *>(a.xn + cur.p);
-      const uint32_t b = it % kBufs;
-      if (!(ok = mbar_wait(&bar_t_full[b], (it / kBufs) & 1, a.err))) break;
-      tc_fence_after();
+      if ((it & 1u) == grp) {
+        const uint32_t b = it % kBufs;
+        if (!(ok = mbar_wait(&bar_t_full[b], (it / kBufs) & 1, a.err))) break;
+        if (!(ok = mbar_wait(&bar_x_full[b], (it / kBufs) & 1, a.err))) break;
+        tc_fence_after();
+        const float *xr = xs + b * kBN;
+        const uint32_t taddr = tmem + ((32u * ew) << 16) + b * kBN;
 #pragma unroll 1
-      for (uint32_t c = 0; c < kBN / 32; c++) {
-        float4 xq[8];
+        for (uint32_t c = 0; c < kBN / 32; c++) {
+          uint32_t r[32];
+          tmem_ld32(taddr + c * 32, r);
+          tmem_wait_ld();
+          float v[32];
+          float mn = INFINITY;
 #pragma unroll
-        for (int j4 = 0; j4 < 8; j4++) xq[j4] = __ldg(xg + c * 8 + j4);
-        uint32_t r[32];
-        tmem_ld32(tmem + ((32u * ew) << 16) + b * kBN + c * 32, r);
-        tmem_wait_ld();
+          for (int j4 = 0; j4 < 8; j4++) {
+            const float4 x4 = *reinterpret_cast<const float4 *>(xr + c * 32 + 4 * j4);
+            v[4 * j4 + 0] = fmaf(-2.f, __uint_as_float(r[4 * j4 + 0]), x4.x);
+            v[4 * j4 + 1] = fmaf(-2.f, __uint_as_float(r[4 * j4 + 1]), x4.y);
+            v[4 * j4 + 2] = fmaf(-2.f, __uint_as_float(r[4 * j4 + 2]), x4.z);
+            v[4 * j4 + 3] = fmaf(-2.f, __uint_as_float(r[4 * j4 + 3]), x4.w);
+            mn = fminf(mn, fminf(fminf(v[4 * j4], v[4 * j4 + 1]), fminf(v[4 * j4 + 2], v[4 * j4 + 3])));
+          }
+          if (mn <= theta) {
 #pragma unroll
-        for (int j4 = 0; j4 < 8; j4++) {
-          const float4 x4 = xq[j4];
-          const float v[4] = {fmaf(-2.f, __uint_as_float(r[4 * j4 + 0]), x4.x),
-                              fmaf(-2.f, __uint_as_float(r[4 * j4 + 1]), x4.y),
-                              fmaf(-2.f, __uint_as_float(r[4 * j4 + 2]), x4.z),
-                              fmaf(-2.f, __uint_as_float(r[4 * j4 + 3]), x4.w)};
-#pragma unroll
-          for (int e = 0; e < 4; e++) {
-            if (v[e] <= theta) {
-              const uint32_t row = (uint32_t)(cur.p + c * 32 + 4 * j4 + e);
+            for (int e = 0; e < 32; e++) {
+              if (!(v[e] <= theta)) continue;
+              const uint32_t row = (uint32_t)(cur.p + c * 32 + e);
               // sorted insertion by (approx, row) into the thread's shortlist
               if (nl == kSL && !row_less(v[e], row, myla[kSL - 1], myli[kSL - 1])) continue;
               int pos = nl < kSL ? (int)nl++ : kSL - 1;
@@ -235,57 +301,11 @@ __global__ void __launch_bounds__(256, 1)
             }
           }
         }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bar_t_empty[b]);
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&bar_t_empty[b]);
-
-      if (cur.last() && nl > 0) {
-        // merge the local shortlist into the query's global one
-        uint32_t spins = 0;
-        while (atomicCAS(a.sl_lock + q, 0u, 1u) != 0u) {
-          if (++spins > kLockSpin) break;
-          __nanosleep(64);
-        }
-        if (spins > kLockSpin) {
-          raise_error(a.err, RBC_ERR_ITER_LIMIT);
-          continue;
-        }
-        __threadfence();
-        float *ga = a.sl_a + (uint64_t)q * kSL;
-        uint32_t *gi = a.sl_row + (uint64_t)q * kSL;
-        float *mysa = sa + et * kLST;
-        uint32_t *mysi = si + et * kLST;
-        uint32_t ng = 0;
-        for (uint32_t t = 0; t < kSL; t++) {
-          mysa[t] = __ldcg(ga + t);
-          mysi[t] = __ldcg(gi + t);
-          ng += mysi[t] != RBC_DUMMY;
-        }
-        uint32_t i = 0, j = 0, t = 0;
-        for (; t < kSL && (i < nl || j < ng); t++) {
-          bool take_local = j >= ng || (i < nl && row_less(myla[i], myli[i], mysa[j], mysi[j]));
-          if (take_local) {
-            ga[t] = myla[i];
-            gi[t] = myli[i];
-            i++;
-          } else {
-            ga[t] = mysa[j];
-            gi[t] = mysi[j];
-            j++;
-          }
-        }
-        // FLT_MAX, not +inf, while the list is short: padded rows (norm +inf)
-        // must never pass the filter.
-        const float newtheta = t == kSL ? __ldcg(ga + kSL - 1) : FLT_MAX;
-        for (; t < kSL; t++) {
-          ga[t] = INFINITY;
-          gi[t] = RBC_DUMMY;
-        }
-        a.sl_theta[q] = __float_as_uint(newtheta);
-        __threadfence();
-        atomicExch(a.sl_lock + q, 0u);
-      }
+      if (cur.last() && nl > 0) publish(a, q, myla, myli, nl);
     }
   }
   tc_fence_before();
@@ -344,27 +364,33 @@ __global__ void row_inexact_kernel(const float *__restrict__ src, uint32_t ld, u
   if (lane == 0) flag[r] = (uint8_t)bad;
 }
 
-__global__ void sl_init_kernel(float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *lock, uint64_t m) {
+// Both shortlist buffers empty, buffer 0 current, thresholds open, locks free.
+__global__ void sl_init_kernel(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
+                               uint64_t m) {
   uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (i < m * kSL) {
+  if (i < 2 * m * kSL) {
     sl_a[i] = INFINITY;
     sl_row[i] = RBC_DUMMY;
   }
   if (i < m) {
+    sel[i] = 0;
     theta[i] = __float_as_uint(FLT_MAX);
     lock[i] = 0;
   }
 }
 
-// Exact rerank of each query's shortlist and the certificate (one warp per query).
+// Exact rerank of each query slot's shortlist and the certificate (one warp
+// per slot); results and failures are reported under the slot's query index.
 template <int METRIC>
 __global__ void rerank_kernel(RerankArgs a) {
-  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t sq = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (q >= a.m) return;
-  const float *qrow = a.Q + q * a.ld;
-  const float *sa_q = a.sl_a + q * kSL;
-  const uint32_t *sr_q = a.sl_row + q * kSL;
+  if (sq >= a.m) return;
+  const uint64_t q = a.order ? a.order[sq] : sq;
+  const float *qrow = a.Q + sq * a.ld;
+  const uint64_t slot = ((uint64_t)a.sl_sel[sq] * a.m_pad + sq) * kSL;
+  const float *sa_q = a.sl_a + slot;
+  const uint32_t *sr_q = a.sl_row + slot;
   float ld = FLT_MAX, cd = FLT_MAX;
   uint32_t li = RBC_DUMMY, ci = RBC_DUMMY;
   uint32_t valid = 0;
@@ -405,17 +431,17 @@ __global__ void rerank_kernel(RerankArgs a) {
   const float tau = __shfl_sync(0xffffffffu, ld, a.k - 1);
   bool certified = true;
   if (valid == kSL) {
-    const double a_last = (double)sa_q[kSL - 1] + (double)a.qn[q];
-    const double E = tc_error_bound(a.qn[q], a.maxnorm, a.q_inexact ? a.q_inexact[q] : 1, a.x_inexact, a.dp);
+    const double a_last = (double)sa_q[kSL - 1] + (double)a.qn[sq];
+    const double E = tc_error_bound(a.qn[sq], a.maxnorm, a.q_inexact ? a.q_inexact[sq] : 1, a.x_inexact, a.dp);
     certified = a_last - E > (double)tau;
   }
   if (lane < (int)a.k) {
-    a.ids[q * a.ldo + lane] = li;
-    a.dists[q * a.ldo + lane] = ld;
+    if (a.ids) a.ids[q * a.ldo + lane] = li;
+    if (a.dists) a.dists[q * a.ldo + lane] = ld;
   }
   if (lane == 0 && !certified) {
-    uint32_t slot = atomicAdd(a.nfail, 1u);
-    a.fail[slot] = (uint32_t)q;
+    uint32_t s = atomicAdd(a.nfail, 1u);
+    a.fail[s] = (uint32_t)q;
   }
 }
 
@@ -430,7 +456,8 @@ uint32_t tc_kp(uint32_t d) { return (d + 63) / 64 * 64; }
 
 size_t tc_smem_bytes(uint32_t kp) {
   const uint32_t kb = kp / 64;
-  return 1024 + (size_t)(1 + kStages) * kb * kTile16K + 4 * (size_t)kBM * kLST * 4;
+  return 1024 + (size_t)(1 + kStages) * kb * kTile16K + (size_t)kBufs * kBN * 4 +
+         (size_t)kEpiGroups * kBM * kLST * 8;
 }
 
 cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32_t kp, uint32_t box_rows) {
@@ -468,10 +495,10 @@ cudaError_t launch_row_inexact(const float *src, uint32_t ld, uint64_t rows, uin
   return launched();
 }
 
-cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *lock, uint64_t m,
-                           cudaStream_t s) {
-  const uint64_t total = std::max<uint64_t>(m * kSL, 1);
-  sl_init_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sl_a, sl_row, theta, lock, m);
+cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
+                           uint64_t m, cudaStream_t s) {
+  const uint64_t total = std::max<uint64_t>(2 * m * kSL, 1);
+  sl_init_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sl_a, sl_row, sel, theta, lock, m);
   return launched();
 }
 
@@ -488,7 +515,7 @@ cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, con
   cudaError_t e = cudaFuncSetAttribute(tc_search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   if (a.nunits == 0) return cudaSuccess;
-  tc_search_kernel<<<grid, 256, smem, s>>>(tmA, tmB, a);
+  tc_search_kernel<<<grid, kThreads, smem, s>>>(tmA, tmB, a);
   return launched();
 }
 

@@ -19,6 +19,7 @@ L2, L1 = 0, 1
 KMAX = 32
 BUILD_PARTITION, BUILD_ONESHOT, BUILD_BF16 = 1, 2, 4
 QUERY_EXACT, QUERY_ONESHOT, QUERY_EXACT_TC = 0, 1, 2
+QUERY_ROUTED = 0x1000
 SYNTH_UNIFORM, SYNTH_MIXTURE, SYNTH_GEOMETRIC = 0, 1, 2
 DUMMY = 0xFFFFFFFF
 FLT_MAX = float(np.finfo(np.float32).max)
@@ -60,12 +61,30 @@ SIGNATURES = {
     "rbc_build_host": ([_VP, _U64, _U32, _U32, C.POINTER(BuildParams), C.POINTER(_VP)], _INT),
     "rbc_destroy": ([_VP], _INT),
     "rbc_get_info": ([_VP, C.POINTER(IndexInfo)], _INT),
+    "rbc_save": ([_VP, C.c_char_p], _INT),
+    "rbc_load": ([C.c_char_p, C.POINTER(_VP)], _INT),
     "rbc_get_reps": ([_VP, _VP], _INT),
     "rbc_get_partition": ([_VP, _VP, _VP, _VP], _INT),
     "rbc_get_oneshot": ([_VP, _VP, _VP], _INT),
     "rbc_query": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP, _VP, _U32, _VP], _INT),
     "rbc_query_host": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP, _VP, _U32], _INT),
     "rbc_get_query_stats": ([_VP, C.POINTER(QueryStats)], _INT),
+    "rbc_batch_create": ([C.POINTER(_VP)], _INT),
+    "rbc_batch_add": ([_VP, _VP, _VP, _U64, _U32, _U32, _VP, _VP, _U32], _INT),
+    "rbc_batch_run": ([_VP, _VP], _INT),
+    "rbc_batch_destroy": ([_VP], _INT),
+    "rbc_set_tuning": ([_VP, _INT, _U32], _INT),
+    "rbc_autotune": ([_VP, _VP, _U64, _U32, _U32, C.c_char_p, _VP], _INT),
+    "rbc_router_create": ([_U32, _U32, _U32, _U64, C.POINTER(_VP)], _INT),
+    "rbc_router_destroy": ([_VP], _INT),
+    "rbc_router_num_params": ([_VP, C.POINTER(_U64)], _INT),
+    "rbc_router_get_params": ([_VP, _VP], _INT),
+    "rbc_router_set_params": ([_VP, _VP], _INT),
+    "rbc_router_gradients": ([_VP, _VP, _U32, _U32, _VP, C.POINTER(_F), _VP, _VP], _INT),
+    "rbc_router_train": ([_VP, _VP, _U64, _U32, _VP, _U32, _U32, _F, _U64, C.POINTER(_F), _VP], _INT),
+    "rbc_router_logits": ([_VP, _VP, _U64, _U32, _VP, _VP], _INT),
+    "rbc_owner_labels": ([_VP, _VP, _U64, _U32, _VP, _VP], _INT),
+    "rbc_set_router": ([_VP, _VP, _U32], _INT),
     "rbc_set_profiling": ([_VP, _INT], _INT),
     "rbc_get_profile": ([_VP, C.POINTER(Profile)], _INT),
     "rbc_kernel_launches": ([], _U64),
@@ -143,6 +162,21 @@ class Index:
         self.h = h
         self.n, self.d, self.metric = n, d, metric
 
+    @classmethod
+    def load(cls, path):
+        """An index read from a file written by save()."""
+        self = cls.__new__(cls)
+        h = C.c_void_p()
+        check(lib().rbc_load(path.encode(), C.byref(h)))
+        self.h = h
+        self._rep_buf = None
+        inf = self.info()
+        self.n, self.d, self.metric = inf["n"], inf["d"], inf["metric"]
+        return self
+
+    def save(self, path):
+        check(lib().rbc_save(self.h, path.encode()))
+
     def close(self):
         if getattr(self, "h", None):
             lib().rbc_destroy(self.h)
@@ -210,6 +244,27 @@ class Index:
     def set_profiling(self, enable=True):
         check(lib().rbc_set_profiling(self.h, int(enable)))
 
+    def owner_labels(self, Q, stream=None):
+        """The list owning each query's exact nearest neighbour (router training labels)."""
+        import torch
+        Q = _dev(Q, torch.float32)
+        lab = torch.empty(Q.shape[0], dtype=torch.int32, device=Q.device)
+        check(lib().rbc_owner_labels(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), lab.data_ptr(), _stream(stream)))
+        return lab
+
+    def set_tuning(self, tq=0, item_rows=0):
+        check(lib().rbc_set_tuning(self.h, tq, item_rows))
+
+    def autotune(self, Q, k, cache_path=None, stream=None):
+        import torch
+        Q = _dev(Q, torch.float32)
+        check(lib().rbc_autotune(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), k,
+                                 cache_path.encode() if cache_path else None, _stream(stream)))
+
+    def set_router(self, router, probes=1):
+        self._router = router
+        check(lib().rbc_set_router(self.h, router.h if router is not None else None, probes))
+
     def profile(self):
         p = Profile()
         check(lib().rbc_get_profile(self.h, C.byref(p)))
@@ -218,6 +273,95 @@ class Index:
 
 def kernel_launches():
     return int(lib().rbc_kernel_launches())
+
+
+class Batch:
+    """Many (index, queries) instances answered by one CUDA graph per run."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().rbc_batch_create(C.byref(h)))
+        self.h = h
+        self.keep = []
+
+    def add(self, index, Q, k):
+        """Queries Q (CUDA tensor, kept alive by the batch); returns (ids, dists) filled by run()."""
+        import torch
+        m = Q.shape[0]
+        ids = torch.empty((m, k), dtype=torch.int32, device=Q.device)
+        dists = torch.empty((m, k), dtype=torch.float32, device=Q.device)
+        check(lib().rbc_batch_add(self.h, index.h, Q.data_ptr(), m, Q.stride(0), k, ids.data_ptr(),
+                                  dists.data_ptr(), k))
+        self.keep.append((index, Q, ids, dists))
+        return ids, dists
+
+    def run(self, stream=None):
+        check(lib().rbc_batch_run(self.h, _stream(stream)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().rbc_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+class Router:
+    """The learned list router (MLP d -> hidden -> hidden -> lists, GELU)."""
+
+    def __init__(self, d, hidden, num_lists, seed=0):
+        h = C.c_void_p()
+        check(lib().rbc_router_create(d, hidden, num_lists, seed, C.byref(h)))
+        self.h = h
+        self.d, self.hidden, self.num_lists = d, hidden, num_lists
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().rbc_router_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def num_params(self):
+        n = C.c_uint64()
+        check(lib().rbc_router_num_params(self.h, C.byref(n)))
+        return n.value
+
+    def get_params(self):
+        p = np.empty(self.num_params(), np.float32)
+        check(lib().rbc_router_get_params(self.h, p.ctypes.data))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        check(lib().rbc_router_set_params(self.h, p.ctypes.data))
+
+    def gradients(self, Q, labels, stream=None):
+        import torch
+        Q = _dev(Q, torch.float32)
+        lab = _dev(np.asarray(labels, np.int32) if isinstance(labels, np.ndarray) else labels, torch.int32)
+        g = np.empty(self.num_params(), np.float32)
+        loss = C.c_float()
+        check(lib().rbc_router_gradients(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), lab.data_ptr(),
+                                         C.byref(loss), g.ctypes.data, _stream(stream)))
+        return loss.value, g
+
+    def train(self, Q, labels, epochs=1, batch=1024, lr=1e-3, seed=0, stream=None):
+        import torch
+        Q = _dev(Q, torch.float32)
+        lab = _dev(labels, torch.int32)
+        loss = C.c_float()
+        check(lib().rbc_router_train(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), lab.data_ptr(), epochs, batch,
+                                     lr, seed, C.byref(loss), _stream(stream)))
+        return loss.value
+
+    def logits(self, Q, stream=None):
+        import torch
+        Q = _dev(Q, torch.float32)
+        out = torch.empty((Q.shape[0], self.num_lists), dtype=torch.float32, device=Q.device)
+        check(lib().rbc_router_logits(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), out.data_ptr(),
+                                      _stream(stream)))
+        return out
 
 
 def brute_knn(X, Q, k, metric=L2, stream=None):

@@ -1,0 +1,143 @@
+"""Batched search and the autotuner.
+
+rbc_batch answers many independent (index, query set) instances with one
+persistent search launch per round, captured once into a CUDA graph and
+replayed; every instance's answer must equal the oracle's exactly, on the
+first run and on replays with new query values.  Every tuning the autotuner
+can pick must keep the results exact.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def check_exact(ids, dists, X, Q, k, metric, rbc, oracle):
+    rid, rd = oracle.knn(X, Q, k, metric)
+    np.testing.assert_array_equal(rbc.u32(ids), rid)
+    np.testing.assert_array_equal(dists.cpu().numpy(), rd)
+
+
+def clustered(rng, n, d, centers=20, spread=0.2):
+    C = rng.standard_normal((centers, d)).astype(np.float32) * 3
+    lab = rng.integers(0, centers, n)
+    return (C[lab] + spread * rng.standard_normal((n, d))).astype(np.float32)
+
+
+@pytest.mark.parametrize("metric", [0, 1])
+def test_batch_heterogeneous_instances(rbc, oracle, metric):
+    """Instances of different sizes, dimensions, k and list counts in one launch."""
+    rng = np.random.default_rng(40 + metric)
+    shapes = [(3000, 16, 64, 200, 10), (5000, 37, 100, 333, 32), (2000, 128, 45, 64, 1),
+              (800, 3, 30, 97, 5)]
+    batch = rbc.Batch()
+    cases = []
+    for n, d, nr, m, k in shapes:
+        X = clustered(rng, n, d)
+        Q = clustered(rng, m, d)
+        idx = rbc.Index(X, nr, metric=metric, seed=n)
+        Qd = torch.from_numpy(Q).cuda()
+        ids, dists = batch.add(idx, Qd, k)
+        cases.append((idx, X, Qd, k, ids, dists))
+    batch.run()
+    torch.cuda.synchronize()
+    for idx, X, Qd, k, ids, dists in cases:
+        check_exact(ids, dists, X, Qd.cpu().numpy(), k, metric, rbc, oracle)
+    # replay the captured graph with new query values in the same buffers
+    for rep in range(2):
+        for idx, X, Qd, k, ids, dists in cases:
+            Qd.copy_(torch.from_numpy(clustered(rng, Qd.shape[0], Qd.shape[1])))
+        batch.run()
+        torch.cuda.synchronize()
+        for idx, X, Qd, k, ids, dists in cases:
+            check_exact(ids, dists, X, Qd.cpu().numpy(), k, metric, rbc, oracle)
+    batch.close()
+    for c in cases:
+        c[0].close()
+
+
+def test_batch_shares_an_index(rbc, oracle):
+    """The same index in several instances (many clients of one database)."""
+    rng = np.random.default_rng(7)
+    X = clustered(rng, 6000, 24)
+    idx = rbc.Index(X, 80)
+    batch = rbc.Batch()
+    outs = []
+    for m, k in ((100, 4), (257, 32), (1, 1)):
+        Qd = torch.from_numpy(clustered(rng, m, 24)).cuda()
+        outs.append((Qd, k) + batch.add(idx, Qd, k))
+    batch.run()
+    torch.cuda.synchronize()
+    for Qd, k, ids, dists in outs:
+        check_exact(ids, dists, X, Qd.cpu().numpy(), k, 0, rbc, oracle)
+    batch.close()
+    idx.close()
+
+
+def test_batch_rejects_bad_use(rbc):
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((500, 8)).astype(np.float32)
+    a = rbc.Index(X, 20, metric=0)
+    b = rbc.Index(X, 20, metric=1)
+    Qd = torch.from_numpy(X[:10].copy()).cuda()
+    batch = rbc.Batch()
+    batch.add(a, Qd, 3)
+    with pytest.raises(rbc.RBCError):
+        batch.add(b, Qd, 3)  # metrics differ
+    with pytest.raises(rbc.RBCError):
+        batch.add(a, Qd, 33)  # k above the list width
+    batch.run()
+    with pytest.raises(rbc.RBCError):
+        batch.add(a, Qd, 3)  # the batch already ran
+    batch.close()
+    empty = rbc.Batch()
+    with pytest.raises(rbc.RBCError):
+        empty.run()
+    empty.close()
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("d", [16, 100, 300])
+def test_every_tuning_is_exact(rbc, oracle, d):
+    rng = np.random.default_rng(d)
+    X = clustered(rng, 20000, d)
+    Q = clustered(rng, 300, d)
+    idx = rbc.Index(X, 140)
+    rid, rd = oracle.knn(X, Q, 10)
+    for tq in (0, 1, 2, 4):
+        for rows in (32, 1000, 0):
+            idx.set_tuning(tq, rows)
+            ids, dists = idx.query(Q, 10)
+            np.testing.assert_array_equal(rbc.u32(ids), rid)
+            np.testing.assert_array_equal(dists.cpu().numpy(), rd)
+    with pytest.raises(rbc.RBCError):
+        idx.set_tuning(3, 0)
+    with pytest.raises(rbc.RBCError):
+        idx.set_tuning(0, 8)
+    idx.close()
+
+
+def test_autotune_and_cache(rbc, oracle, tmp_path):
+    rng = np.random.default_rng(11)
+    X = clustered(rng, 30000, 64)
+    Q = clustered(rng, 500, 64)
+    cache = str(tmp_path / "tune.txt")
+    idx = rbc.Index(X, 170)
+    idx.autotune(Q, 10, cache_path=cache)
+    lines = open(cache).read().splitlines()
+    assert len(lines) == 1
+    n, d, nr, k, metric, tq, rows, ms = lines[0].split()
+    assert (int(n), int(d), int(nr), int(k), int(metric)) == (30000, 64, 170, 10, 0)
+    assert int(tq) in (1, 2, 4) and int(rows) >= 32 and float(ms) > 0
+    ids, dists = idx.query(Q, 10)
+    check_exact(ids, dists, X, Q, 10, 0, rbc, oracle)
+    # a second index of the same shape takes the cached choice without timing
+    idx2 = rbc.Index(X, 170, seed=5)
+    idx2.autotune(Q, 10, cache_path=cache)
+    assert len(open(cache).read().splitlines()) == 1
+    ids, dists = idx2.query(Q, 10)
+    check_exact(ids, dists, X, Q, 10, 0, rbc, oracle)
+    idx.close()
+    idx2.close()
