@@ -51,12 +51,25 @@ METRIC = "exact 10-NN queries/s, n=10M d=128, learned+BF16 vs plain FP32 RBC, sa
 UNIT = "queries/s"
 
 WORKLOADS = {
-    # kind, seed, n, m, d, k, reps, ncomp, sigma_lo, sigma_hi, train queries, router epochs
+    # kind, seed, n, m, d, k, reps, ncomp, sigma_lo, sigma_hi, train queries, router epochs, forms
+    "c1": dict(kind=0, seed=1, n=65_536, m=8_192, d=16, k=1, reps=256, ncomp=1, slo=0.0, shi=0.0,
+               train=0, epochs=0, forms="tensor,plain",
+               metric="exact 1-NN queries/s, n=65,536 d=16 uniform, plain FP32 RBC",
+               desc="i.i.d. uniform [0,1)"),
+    "c2": dict(kind=1, seed=2, n=1_048_576, m=100_000, d=128, k=32, reps=1024, ncomp=1000, slo=0.05, shi=0.05,
+               train=0, epochs=0, forms="tensor,plain",
+               metric="exact 32-NN queries/s, n=1,048,576 d=128 mixture, plain FP32 RBC",
+               desc="1,000-component Gaussian mixture, sigma 0.05"),
     "c3": dict(kind=2, seed=3, n=10_000_000, m=10_000, d=128, k=10, reps=4096, ncomp=1, slo=0.0, shi=0.0,
-               train=100_000, epochs=2,
+               train=100_000, epochs=2, forms="plain,tensor,learned", metric=METRIC,
                desc="geometric(mean 20) integer features"),
+    "c4": dict(kind=1, seed=4, instances=64, n_lo=10_000, n_hi=2_000_000, dims=(32, 64, 128), ks=(1, 10, 32),
+               comp_lo=100, comp_hi=1000, slo=0.05, shi=0.05, forms="batch",
+               metric="exact k-NN queries/s over 64 batched heterogeneous RBC instances (one graph), plain FP32",
+               desc="64 instances, n log-uniform in [1e4, 2e6], d in {32, 64, 128}, k in {1, 10, 32}, m = n/100"),
     "c5": dict(kind=1, seed=5, n=4_194_304, m=100_000, d=128, k=10, reps=4096, ncomp=2000, slo=0.02, shi=0.1,
-               train=1_000_000, epochs=3,
+               train=1_000_000, epochs=3, forms="plain,tensor,learned",
+               metric="exact 10-NN queries/s, n=4,194,304 d=128 mixture, learned router + BF16 vs plain FP32 RBC",
                desc="2,000-component Gaussian mixture, sigma ~ U[0.02, 0.1]"),
 }
 
@@ -74,19 +87,24 @@ def parse():
     ap.add_argument("--train", type=int, default=None)
     ap.add_argument("--cpu-queries-per-thread", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--forms", default="plain,tensor,learned",
-                    help="forms to time; the last one listed is the headline")
+    ap.add_argument("--forms", default=None,
+                    help="forms to time; the last one listed is the headline (default: per workload)")
     a = ap.parse_args()
     w = dict(WORKLOADS[a.workload])
     for key in ("n", "m", "reps", "train"):
         if getattr(a, key) is not None:
             w[key] = getattr(a, key)
+    if a.forms is None:
+        a.forms = w["forms"]
     a.w = w
     return a
 
 
 def config(a, form):
     w = a.w
+    if a.workload == "c4":
+        return {"workload": f"c4: {w['desc']}, squared L2", "instances": w["instances"], "form": form,
+                "l2_flush": "inputs larger than L2 (GBs of databases vs 129 MB L2); no flush between steps"}
     return {"workload": f"{a.workload}: exact {w['k']}-NN, n={w['n']:,} d={w['d']} {w['desc']}, "
                         f"m={w['m']:,} queries, squared L2",
             "n": w["n"], "d": w["d"], "m": w["m"], "k": w["k"], "num_reps": w["reps"], "form": form,
@@ -159,6 +177,23 @@ def committed_traffic(kernel):
     return float(m.group(1)) if m else None
 
 
+def fp64_error(X, Q, ids, dists, sample=512):
+    """Largest |d - d64| / d64 of the returned squared L2 distances over a
+    query sample, d64 recomputed in float64 from the same rows."""
+    import torch
+    S = min(sample, Q.shape[0])
+    sel = torch.linspace(0, Q.shape[0] - 1, S, device=Q.device).long()
+    I = ids[sel].long()
+    valid = I >= 0  # unfilled slots hold 0xFFFFFFFF
+    rows = X[I.clamp(min=0)].double()
+    d64 = ((rows - Q[sel].double()[:, None, :]) ** 2).sum(-1)
+    d32 = dists[sel].double()
+    pos = valid & (d64 > 0)
+    if bool((valid & (d64 == 0) & (d32 != 0)).any().item()):
+        return float("inf")
+    return float(((d32 - d64).abs() / d64)[pos].max().item()) if bool(pos.any().item()) else 0.0
+
+
 # ------------------------------------------------------------------ CPU baselines
 def host_matrix(w, stream, rows, threads):
     """Rows of the synthetic matrix generated on the host by the CPU recipe."""
@@ -219,6 +254,12 @@ def run_reference(a):
     if rank != 0:
         return
     w = a.w
+    if a.workload == "c4":  # the largest instance of the batch stands for the workload
+        specs = batch_instances(w)
+        i = max(range(len(specs)), key=lambda j: specs[j][0])
+        n, d, k, m, ncomp, _ = specs[i]
+        w = dict(w, seed=w["seed"] * 1000 + i, n=n, d=d, k=k, m=m, ncomp=ncomp)
+        a.w = dict(w, reps=0)
     threads = os.cpu_count() or 1
     X = host_matrix(w, 0, w["n"], threads)
     Q = host_matrix(w, 1, min(w["m"], 4096), threads)
@@ -343,6 +384,7 @@ def run_engine(a):
         acc["steps"] = steps
         acc["value"] = world * m * steps / (acc["ms"] / 1000.0)
         acc["ids"] = ids.clone()
+        acc["fp64"] = fp64_error(X, Q, ids, dists)
         return acc
 
     results = {}
@@ -405,10 +447,11 @@ def run_engine(a):
             extra["forms"][f] = {"value": r["value"], "ms_per_step": r["ms"] / r["steps"],
                                  "lists_per_query": r["lists"] / (m * r["steps"]),
                                  "pairs_per_query": r["point_pairs"] / (m * r["steps"]),
-                                 "fallback_queries_per_step": r["fallback"] / r["steps"]}
+                                 "fallback_queries_per_step": r["fallback"] / r["steps"],
+                                 "max_rel_dist_error_vs_fp64": r["fp64"]}
         if "plain" in results:
             extra["speedup_vs_plain_fp32"] = value / results["plain"]["value"]
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        line = {"metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if head == "plain" else "bf16+f32",
                 "data": "synthetic (counter-based generator on the GPU)",
@@ -421,10 +464,153 @@ def run_engine(a):
         dist.destroy_process_group()
 
 
+def batch_instances(w):
+    """The heterogeneous instances of the batched workload: (n, d, k, m, ncomp, reps)."""
+    rng = np.random.default_rng(w["seed"])
+    out = []
+    for _ in range(w["instances"]):
+        n = int(round(np.exp(rng.uniform(np.log(w["n_lo"]), np.log(w["n_hi"])))))
+        d = int(rng.choice(w["dims"]))
+        k = int(rng.choice(w["ks"]))
+        ncomp = int(rng.integers(w["comp_lo"], w["comp_hi"] + 1))
+        reps = int(min(4096, max(64, round(2 * np.sqrt(n)))))
+        out.append((n, d, k, max(1, n // 100), ncomp, reps))
+    return out
+
+
+def run_batch(a):
+    """64 independent (database, query set) instances answered by one captured
+    graph per step (rbc_batch); compared with answering them one by one."""
+    import torch
+    import pyrbc
+
+    w = a.w
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    stream = torch.cuda.current_stream()
+    specs = batch_instances(w)
+    inst = []
+    t0 = time.perf_counter()
+    for i, (n, d, k, m, ncomp, reps) in enumerate(specs):
+        syn = dict(ncomp=ncomp, sigma_lo=w["slo"], sigma_hi=w["shi"])
+        X = pyrbc.synth(w["kind"], w["seed"] * 1000 + i, 0, n, d, **syn)
+        Q = pyrbc.synth(w["kind"], w["seed"] * 1000 + i, 1, m, d, **syn)
+        idx = pyrbc.Index(X, reps, seed=i)
+        idx.autotune(Q, k)
+        inst.append({"X": X, "Q": Q, "idx": idx, "k": k, "m": m, "n": n, "d": d})
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    total_m = sum(r["m"] for r in inst)
+
+    # one by one (the same exact query per instance), for comparison and the pair counts
+    pairs = flops = 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    seq = []
+    for r in inst:
+        seq.append(r["idx"].query(r["Q"], r["k"]))
+        st = r["idx"].stats()
+        pairs += st["point_pairs"]
+        flops += st["point_pairs"] * 2 * r["d"]
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(a.steps):
+        for r in inst:
+            r["idx"].query(r["Q"], r["k"], out=None)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    seq_ms = ev0.elapsed_time(ev1) / a.steps
+
+    batch = pyrbc.Batch()
+    outs = [batch.add(r["idx"], r["Q"], r["k"]) for r in inst]
+    for _ in range(a.warmup):
+        batch.run()
+    torch.cuda.synchronize()
+    same = all(bool((o[0] == s[0]).all().item()) and bool((o[1] == s[1]).all().item()) for o, s in zip(outs, seq))
+    fp64 = max(fp64_error(r["X"], r["Q"], o[0], o[1], sample=64) for r, o in zip(inst, outs))
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = pyrbc.kernel_launches()
+    ev0.record(stream)
+    for _ in range(a.steps):
+        batch.run()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = pyrbc.kernel_launches() - l0
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * total_m * a.steps / (ms / 1000.0)
+
+    # end to end: pinned host queries copied in, results copied out, every step
+    hq = [r["Q"].cpu().pin_memory() for r in inst]
+    hi = [torch.empty_like(o[0], device="cpu").pin_memory() for o in outs]
+    hd = [torch.empty_like(o[1], device="cpu").pin_memory() for o in outs]
+    h2d = sum(q.numel() * 4 for q in hq)
+    d2h = sum(o[0].numel() * 8 for o in outs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        for r, q in zip(inst, hq):
+            r["Q"].copy_(q, non_blocking=True)
+        batch.run()
+        for o, i_, d_ in zip(outs, hi, hd):
+            i_.copy_(o[0], non_blocking=True)
+            d_.copy_(o[1], non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * total_m * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h)}
+    hbm, bf16, bf16_sus, src = peaks()
+    sm_mhz = clk.get("sm_mhz") or 1920.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    achieved = flops / (ms / a.steps / 1000.0) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
+                "traffic": committed_traffic("search_kernel_batch"), "kernel": "search_kernel (whole graph step)",
+                "peak_source": f"{src} bf16 dense burst (MEASURED_PEAKS.json)",
+                "fp32_core": {"achieved_tflops": achieved, "peak_tflops": fp32_peak, "frac": achieved / fp32_peak},
+                "note": "achieved = evaluated (query, row) pairs x 2d over the whole graph step"}
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        r = max(inst, key=lambda z: z["n"])
+        nq = min(r["m"], 2 * threads)
+        t, kind, desc = cpu_knn_timed(r["X"].cpu().numpy(), r["Q"][:nq].cpu().numpy(), r["k"], threads)
+        cpu = {"value": nq / t, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"{nq} queries of the largest instance (n={r['n']:,}, d={r['d']}); {desc}"}
+    if rank == 0:
+        extra = {"build_and_tune_s": build_s, "queries_per_step": total_m, "pairs_per_step": pairs,
+                 "one_by_one_ms_per_step": seq_ms, "one_by_one_value": world * total_m / (seq_ms / 1000.0),
+                 "batched_speedup": seq_ms / (ms / a.steps), "same_ids_as_one_by_one": same,
+                 "max_rel_dist_error_vs_fp64": fp64,
+                 "instances": [{"n": r["n"], "d": r["d"], "k": r["k"], "m": r["m"]} for r in inst]}
+        line = {"metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (counter-based generator on the GPU)",
+                "config": dict(config(a, "batched exact RBC, FP32 list search, CUDA graph"),
+                               parallelism=f"replicas{world}"),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+                "clocks": clk, "extra": extra}
+        print(json.dumps(line), flush=True)
+    batch.close()
+    for r in inst:
+        r["idx"].close()
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "c4":
+        run_batch(a)
     else:
         run_engine(a)
 

@@ -48,15 +48,22 @@ extern "C" {
 /* ---- build flags ---- */
 #define RBC_BUILD_PARTITION 1u /* nearest-representative lists for exact search */
 #define RBC_BUILD_ONESHOT 2u   /* the reference's lists: s nearest points per rep */
-#define RBC_BUILD_BF16 4u      /* BF16 copy of the lists for tensor-core search   */
+#define RBC_BUILD_BF16 4u      /* half-precision tensor-core operands of the lists:
+                                  rows centered on their representative, in BF16
+                                  when every value is exact in it, else FP16
+                                  hi + lo halves (RBC_TC_* in rbc_index_info)     */
+
+/* ---- tensor-core operand formats (rbc_index_info.tc_format) ---- */
+#define RBC_TC_BF16 0u       /* one BF16 product per pair (data exact in BF16)   */
+#define RBC_TC_FP16_SPLIT 1u /* three FP16 products (hi.hi + hi.lo + lo.hi)      */
 
 /* ---- query modes ---- */
 #define RBC_QUERY_EXACT 0u    /* exact k-NN: triangle-inequality pruning of lists */
 #define RBC_QUERY_ONESHOT 1u  /* reference one-shot: only the nearest rep's list  */
-#define RBC_QUERY_EXACT_TC 2u /* exact k-NN with BF16 tensor-core distance tiles, an
-                                 FP32 rerank of a 40-row shortlist and a certified
-                                 error bound (falls back per query when uncertain);
-                                 L2 only, needs RBC_BUILD_BF16                      */
+#define RBC_QUERY_EXACT_TC 2u /* exact k-NN whose list search runs on the tensor
+                                 cores (operands of RBC_BUILD_BF16), an FP32 rerank
+                                 of a 40-row shortlist and a certified error bound
+                                 (falls back per query when uncertain); L2 only    */
 #define RBC_QUERY_ROUTED 0x1000u /* flag for RBC_QUERY_EXACT: search the attached
                                     router's top lists (and the nearest
                                     representative's) before pruning; results stay
@@ -85,6 +92,7 @@ typedef struct {
   uint32_t flags;
   uint64_t min_list, max_list; /* partition list sizes                  */
   uint64_t device_bytes;       /* device memory held by the index        */
+  uint32_t tc_format;          /* RBC_TC_* (with RBC_BUILD_BF16)         */
 } rbc_index_info;
 
 typedef struct {               /* work done by the last rbc_query on an index */

@@ -74,6 +74,7 @@ struct rbc_batch {
   cudaGraphExec_t exec = nullptr;
   cudaStream_t cap = nullptr;
   uint32_t *ctl = nullptr;  // [0] work, [1] items, [2] error
+  unsigned long long graph_kernels = 0;  // kernel nodes one replay runs
   ~rbc_batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -184,6 +185,9 @@ int prepare(rbc_batch *bt) {
   g.dp = dp_max;  // sizes the shared-memory tile of the shared launch
   g.k = 1;
 
+  // launches recorded during capture run only when the graph replays:
+  // the launch counter is charged per replay instead
+  const unsigned long long l0 = g_kernel_launches.load();
   BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int rc = RBC_OK;
   auto capture = [&]() -> int {
@@ -220,6 +224,8 @@ int prepare(rbc_batch *bt) {
   rc = capture();
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamEndCapture(s, &graph);
+  bt->graph_kernels = g_kernel_launches.load() - l0;
+  g_kernel_launches.fetch_sub(bt->graph_kernels);
   if (rc != RBC_OK) {
     if (graph) cudaGraphDestroy(graph);
     return rc;
@@ -270,6 +276,7 @@ int rbc_batch_run(rbc_batch *bt, void *stream) {
   if (!bt->ready) BTRY(prepare(bt));
   cudaStream_t s = (cudaStream_t)stream;
   BCK(cudaGraphLaunch(bt->exec, s));
+  g_kernel_launches.fetch_add(bt->graph_kernels, std::memory_order_relaxed);
   uint32_t err = 0;
   BCK(cudaMemcpyAsync(&err, bt->ctl + 2, 4, cudaMemcpyDeviceToHost, s));
   BCK(cudaStreamSynchronize(s));

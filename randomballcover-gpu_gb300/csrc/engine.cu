@@ -97,11 +97,22 @@ int check_dims(uint32_t d, uint32_t ld, const char *what) {
 // Build the list-major plan for one mode, then (stage >= 1) its work items
 // and (stage 2) run the search over them.  The plan stays in b.cnt / b.start
 // / b.pair_q / b.pair_thr, the items in b.items with their count in b.ctl[1].
+// The float nearest to v on the side away from (up) or towards (down) zero,
+// for positive v.
+static float round_up_f(double v) {
+  float f = (float)v;
+  return (double)f < v ? std::nextafter(f, INFINITY) : f;
+}
+static float round_down_f(double v) {
+  float f = (float)v;
+  return (double)f > v ? std::nextafter(f, 0.f) : f;
+}
+
 int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
-                    int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq) {
+                    int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq, uint32_t qtile_over) {
   const int tqv = tq < 0 ? idx->tune_tq : tq;
-  const uint32_t nr = idx->nr, qtile = (uint32_t)search_query_tile(idx->dp, tqv);
+  const uint32_t nr = idx->nr, qtile = qtile_over ? qtile_over : (uint32_t)search_query_tile(idx->dp, tqv);
   uint32_t *ctl = b.ctl.as<uint32_t>();  // [0] work, [1] nitems, [2] err
   PlanArgs a{};
   a.Dqr = b.Dqr.as<float>();
@@ -115,7 +126,11 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
   a.P = P;
   a.metric = (uint32_t)idx->metric;
   a.qtile = qtile;
-  a.gamma = (double)(idx->dp + 8) * 1.1920928955078125e-07;
+  const double g = (double)(idx->dp + 8) * 1.1920928955078125e-07;
+  a.opg_ru = round_up_f(1.0 + g);
+  a.omg_rd = round_down_f(1.0 - g);
+  a.c_ru = round_up_f(1.0 + 3.0 * g);
+  a.opc_ru = round_up_f(2.0 + 3.0 * g);
   a.list_cursor = b.cursor.as<uint32_t>();
   a.pair_q = b.pair_q.as<uint32_t>();
   a.pair_thr = b.pair_thr.as<float>();
@@ -182,6 +197,18 @@ namespace {
 }  // namespace
 
 // ------------------------------------------------------------------ build
+int build_tc(rbc_index *idx, cudaStream_t s) {
+  if (idx->metric != RBC_L2) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: the tensor-core form is L2 only");
+  if (!tc_supported(idx->dp)) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: the tensor-core form needs d <= 128");
+  idx->kp = tc_kp(idx->d);
+  idx->n_pad = (idx->n + 127) / 128 * 128;
+  TRY(tc_build(idx->Xp, idx->offsets, idx->R, idx->radius, idx->n, idx->n_pad, idx->nr, idx->d, idx->ld, idx->kp,
+               &idx->tc, &idx->device_bytes, s));
+  CK(tc_make_map(&idx->tmB, idx->tc.Xh, idx->n_pad, idx->tc.cols, 128));
+  CK(cudaStreamSynchronize(s));
+  return RBC_OK;
+}
+
 int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *p,
                 cudaStream_t s, rbc_index **out) {
   if (!out) return fail(RBC_ERR_INVALID, "rbc_build: out is NULL");
@@ -290,25 +317,7 @@ int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc
   if (flags & RBC_BUILD_BF16) {
     if (!(flags & RBC_BUILD_PARTITION))
       return fail(RBC_ERR_INVALID, "rbc_build: RBC_BUILD_BF16 needs RBC_BUILD_PARTITION");
-    if (idx->metric != RBC_L2) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: the tensor-core form is L2 only");
-    if (!tc_supported(idx->dp)) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: the tensor-core form needs d <= 128");
-    idx->kp = tc_kp(d);
-    idx->n_pad = (n + 127) / 128 * 128;
-    const size_t xb_bytes = (size_t)idx->n_pad * idx->kp * 2;
-    CK(cudaMalloc(&idx->Xb, xb_bytes));
-    CK(cudaMalloc(&idx->xn, idx->n_pad * 4));
-    idx->device_bytes += xb_bytes + idx->n_pad * 4;
-    DevBuf fl;
-    CK(fl.alloc(8, s));
-    CK(cudaMemsetAsync(fl.p, 0, 8, s));
-    CK(launch_to_bf16(idx->Xp, ld, n, idx->n_pad, d, idx->kp, idx->Xb, idx->xn, INFINITY, fl.as<uint32_t>(),
-                      fl.as<uint32_t>() + 1, s));
-    uint32_t h[2];
-    CK(cudaMemcpyAsync(h, fl.p, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    idx->x_inexact = h[0];
-    std::memcpy(&idx->maxnorm, &h[1], 4);
-    CK(tc_make_map(&idx->tmB, idx->Xb, idx->n_pad, idx->kp, 128));
+    TRY(build_tc(idx, s));
   }
 
   if (flags & RBC_BUILD_ONESHOT) {
@@ -486,30 +495,29 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   return RBC_OK;
 }
 
-// Tensor-core exact query (tc_search.cu), an RBC query whose list search
-// runs on the tensor cores:
+// Tensor-core exact query (tc_search.cu): an RBC query whose list search runs
+// on the tensor cores, in two rounds like the plain form:
 //   1. query x representative distances, probe table (nearest representative,
-//      plus the router's picks when routed), exact FP32 search of the probed
-//      lists -> each query's k-th distance;
-//   2. the pruning plan (plan.cu) -> surviving (list, query) pairs;
-//   3. queries sorted by nearest representative into 128-query tiles; each
-//      tile's union of probed and surviving lists becomes row ranges (lists
-//      are contiguous in the list-major layout), cut into work units;
-//   4. tensor search of the units, exact rerank and certificate; uncertified
-//      queries are recomputed by the plain exact path.
-// Rows outside a tile's ranges were pruned by the exact bounds, so the
-// certificate covers everything.
+//      plus the router's picks when routed);
+//   2. probe round: tensor search of the probed lists, exact rerank of the
+//      shortlists -> each query's k-th distance (an upper bound on the true
+//      one, so pruning with it is safe);
+//   3. pruned round: the pruning plan over every other list, tensor search of
+//      the surviving (list, query) items into the same shortlists, exact
+//      rerank and certificate; uncertified queries are recomputed by the
+//      plain exact path.
+// Rows of pruned lists cannot be in the top k (exact bounds), so the
+// certificate covers everything.  The rounds need no host round trip.
 int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode, uint32_t *dIds,
              float *dDists, uint32_t ldo, cudaStream_t s) {
   pool_setup();
-  const uint32_t nr = idx->nr, ld = idx->ld, kp = idx->kp;
+  const uint32_t nr = idx->nr, ld = idx->ld, kp = idx->kp, fmt = idx->tc.format, cols = idx->tc.cols;
   const bool routed = (mode & RBC_QUERY_ROUTED) != 0;
   if (routed && !idx->router) return fail(RBC_ERR_INVALID, "rbc_query: RBC_QUERY_ROUTED without a router");
   const uint32_t P = routed ? 1 + idx->router_probes : 1;
   const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
-  const uint32_t qtile = (uint32_t)search_query_tile(idx->dp, idx->tune_tq);
-  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(128, (1ull << 27) / nr));
-  const uint64_t mbp = (mb + 127) / 128 * 128, T = mbp / 128;
+  const uint32_t qtile = tc_query_tile(fmt);
+  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
   QueryBufs b;
   const uint64_t pair_cap = mb * nr, item_cap = item_capacity(idx, mb, qtile);
   CK(b.Qp.alloc(mb * ld * 4, s));
@@ -530,56 +538,41 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(b.items.alloc(item_cap * sizeof(SearchItem), s));
   CK(b.ctl.alloc(64, s));
   CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
-  DevBuf near, near_d, logits, order, slot_of, khist, kstart, kcursor, flags, Qs, Qb, qn, qinex, sl_a, sl_row, sl_sel,
-      sl_theta, sl_lock, units, ctl, failq;
+  DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
+      stats;
   if (routed) {
     CK(near.alloc(mb * 4, s));
     CK(near_d.alloc(mb * 4, s));
     CK(logits.alloc(mb * nr * 4, s));
   }
-  CK(order.alloc(mbp * 4, s));
-  CK(slot_of.alloc(mb * 4, s));
-  CK(khist.alloc((nr + 1) * 4, s));
-  CK(kstart.alloc((nr + 1) * 4, s));
-  CK(kcursor.alloc((nr + 1) * 4, s));
-  CK(flags.alloc(T * nr, s));
-  CK(Qs.alloc(mbp * ld * 4, s));
-  CK(Qb.alloc(mbp * kp * 2, s));
-  CK(qn.alloc(mbp * 4, s));
-  CK(qinex.alloc(mbp, s));
-  CK(sl_a.alloc(2 * mbp * kShortlist * 4, s));
-  CK(sl_row.alloc(2 * mbp * kShortlist * 4, s));
-  CK(sl_sel.alloc(mbp * 4, s));
-  CK(sl_theta.alloc(mbp * 4, s));
-  CK(sl_lock.alloc(mbp * 4, s));
+  CK(Qh.alloc((mb + 1) * cols * 2, s));
+  CK(qscale.alloc((mb + 1) * 4, s));
+  CK(qnorm.alloc((mb + 1) * 4, s));
+  CK(qinex.alloc(mb + 1, s));
+  CK(sl_a.alloc(2 * mb * kShortlist * 4, s));
+  CK(sl_row.alloc(2 * mb * kShortlist * 4, s));
+  CK(sl_sel.alloc(mb * 4, s));
+  CK(sl_theta.alloc(mb * 4, s));
+  CK(sl_lock.alloc(mb * 4, s));
+  CK(emax.alloc(mb * 4, s));
   CK(ctl.alloc(64, s));
   CK(failq.alloc(mb * 4, s));
-  DevBuf stats;
   CK(stats.alloc(2 * sizeof(unsigned long long), s));
   CK(cudaMemsetAsync(stats.p, 0, 2 * sizeof(unsigned long long), s));
-  CUtensorMap tmA;
-  CK(tc_make_map(&tmA, Qb.p, mbp, kp, 128));
-  std::vector<uint8_t> hflags(T * nr);
-  const std::vector<uint64_t> &off = idx->h_offsets;
-  uint64_t tc_pairs = 0, tc_lists = 0, nfail_total = 0;
+  uint64_t nfail_total = 0;
   double tc_ms = 0;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (idx->profile) {
-    while (idx->ev_pool.size() < 2) {
-      cudaEvent_t e;
-      CK(cudaEventCreate(&e));
-      idx->ev_pool.push_back(e);
-    }
-    e0 = idx->ev_pool[0];
-    e1 = idx->ev_pool[1];
+  uint32_t tc_launches = 0;
+  while (idx->ev_pool.size() < 4 && idx->profile) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    idx->ev_pool.push_back(e);
   }
   idx->ev_used = 0;
   for (uint64_t b0 = 0; b0 < m; b0 += mb) {
     const uint64_t mq = std::min(mb, m - b0);
-    const uint64_t Tq = (mq + 127) / 128;
     CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
     CK(cudaMemsetAsync(ctl.p, 0, 64, s));
-    // 1. probe round
+    // 1. distances to the representatives, probe table
     CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
     CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
     if (routed) {
@@ -598,114 +591,96 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     }
     CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(),
                            mq, s));
-    TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid,
-                        stats.as<unsigned long long>(), s));
-    // 2. pruning plan (no plain search)
-    TRY(plan_and_search(idx, b, mq, P, k, 1, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 0));
-    // 3. tiles of queries sorted by nearest representative, their list unions
-    CK(launch_sort_by_key(b.probe.as<uint32_t>(), P, mq, nr, khist.as<uint32_t>(), kstart.as<uint32_t>(),
-                          kcursor.as<uint32_t>(), b.scan_tmp.p, order.as<uint32_t>(), slot_of.as<uint32_t>(), s));
-    CK(cudaMemsetAsync(flags.p, 0, Tq * nr, s));
-    CK(launch_mark_tiles(b.start.as<uint32_t>(), b.cnt.as<uint32_t>(), b.pair_q.as<uint32_t>(), b.probe.as<uint32_t>(),
-                         mq, P, slot_of.as<uint32_t>(), nr, flags.as<uint8_t>(), s));
-    CK(cudaMemcpyAsync(hflags.data(), flags.p, Tq * nr, cudaMemcpyDeviceToHost, s));
-    // queries in tile order, BF16 rows and norms (slots past mq are zero rows)
-    CK(cudaMemsetAsync(Qs.p, 0, mbp * ld * 4, s));
-    CK(launch_gather_rows(b.Qp.as<float>(), ld, order.as<uint32_t>(), mq, Qs.as<float>(), s));
-    CK(launch_to_bf16(Qs.as<float>(), ld, mq, Tq * 128, idx->d, kp, Qb.p, qn.as<float>(), 0.f, nullptr, nullptr, s));
-    CK(launch_row_inexact(Qs.as<float>(), ld, mq, idx->d, qinex.as<uint8_t>(), s));
-    CK(cudaStreamSynchronize(s));
-    std::vector<TcUnit> hu;
-    const uint64_t kUnitRows = 128 * 1024;
-    for (uint32_t t = 0; t < Tq; t++) {
-      const uint8_t *f = hflags.data() + (uint64_t)t * nr;
-      uint32_t r = 0;
-      uint64_t cur0 = 0, cur1 = 0;
-      bool open = false;
-      auto flush = [&]() {
-        for (uint64_t p = cur0; p < cur1; p += kUnitRows)
-          hu.push_back(TcUnit{t, 0, p, std::min(cur1, p + kUnitRows)});
-      };
-      while (r < nr) {
-        if (!f[r] || off[r + 1] == off[r]) {
-          r++;
-          continue;
-        }
-        uint32_t r1 = r;
-        while (r1 < nr && (f[r1] || off[r1 + 1] == off[r1])) r1++;
-        const uint64_t p0 = off[r] / 128 * 128, p1 = (off[r1] + 127) / 128 * 128;
-        if (open && p0 <= cur1) {
-          cur1 = std::max(cur1, p1);
-        } else {
-          if (open) flush();
-          cur0 = p0;
-          cur1 = p1;
-          open = true;
-        }
-        for (uint32_t j = r; j < r1; j++) tc_lists += f[j];
-        r = r1;
-      }
-      if (open) flush();
-    }
-    // units touching the same rows run together: they share B tiles in L2
-    std::stable_sort(hu.begin(), hu.end(), [](const TcUnit &x, const TcUnit &y) { return x.p0 < y.p0; });
-    for (const TcUnit &u : hu) tc_pairs += (u.p1 - u.p0) * std::min<uint64_t>(128, mq - (uint64_t)u.tile * 128);
-    CK(units.alloc(std::max<size_t>(hu.size(), 1) * sizeof(TcUnit), s));
-    if (!hu.empty()) CK(cudaMemcpyAsync(units.p, hu.data(), hu.size() * sizeof(TcUnit), cudaMemcpyHostToDevice, s));
-    // 4. tensor search, rerank, certificate
+    // query operands (row mq is the zero row gathered for empty item slots)
+    CK(launch_tc_queries(b.Qp.as<float>(), ld, mq, idx->d, kp, fmt, Qh.p, qscale.as<float>(), qnorm.as<float>(),
+                         qinex.as<uint8_t>(), s));
+    CUtensorMap tmA;
+    CK(tc_make_map(&tmA, Qh.p, mq + 1, cols, 1));
     CK(launch_sl_init(sl_a.as<float>(), sl_row.as<uint32_t>(), sl_sel.as<uint32_t>(), sl_theta.as<uint32_t>(),
-                      sl_lock.as<uint32_t>(), Tq * 128, s));
+                      sl_lock.as<uint32_t>(), emax.as<uint32_t>(), mq, s));
     TcArgs ta{};
-    ta.units = units.as<TcUnit>();
-    ta.nunits = (uint32_t)hu.size();
-    ta.kblocks = kp / 64;
-    ta.xn = idx->xn;
-    ta.m_pad = Tq * 128;
+    ta.items = b.items.as<SearchItem>();
+    ta.nitems = b.ctl.as<uint32_t>() + 1;
+    ta.qidx = b.pair_q.as<uint32_t>();
+    ta.Dqr = b.Dqr.as<float>();
+    ta.nr = nr;
+    ta.kb = kp / 64;
+    ta.zero_row = (uint32_t)mq;
+    ta.d = idx->d;
+    ta.w = idx->tc.w;
+    ta.lscale = idx->tc.lscale;
+    ta.lxmax = idx->tc.lxmax;
+    ta.lcnorm = idx->tc.lcnorm;
+    ta.qscale = qscale.as<float>();
+    ta.qnorm = qnorm.as<float>();
+    ta.q_inexact = qinex.as<uint8_t>();
+    ta.x_inexact = idx->tc.x_inexact;
+    ta.format = fmt;
     ta.sl_a = sl_a.as<float>();
     ta.sl_row = sl_row.as<uint32_t>();
     ta.sl_sel = sl_sel.as<uint32_t>();
     ta.sl_theta = sl_theta.as<uint32_t>();
     ta.sl_lock = sl_lock.as<uint32_t>();
+    ta.emax = emax.as<uint32_t>();
+    ta.m = mq;
+    ta.offsets = idx->offsets;
+    ta.stats = stats.as<unsigned long long>();
     ta.err = ctl.as<uint32_t>();
-    if (e0) CK(cudaEventRecord(e0, s));
-    CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
-    if (e1) CK(cudaEventRecord(e1, s));
     RerankArgs ra{};
     ra.X = idx->Xp;
     ra.pid = idx->perm;
-    ra.Q = Qs.as<float>();
-    ra.order = order.as<uint32_t>();
+    ra.Q = b.Qp.as<float>();
     ra.ld = ld;
     ra.dp = idx->dp;
     ra.k = k;
     ra.m = mq;
-    ra.m_pad = Tq * 128;
     ra.sl_a = sl_a.as<float>();
     ra.sl_row = sl_row.as<uint32_t>();
     ra.sl_sel = sl_sel.as<uint32_t>();
-    ra.qn = qn.as<float>();
-    ra.q_inexact = qinex.as<uint8_t>();
-    ra.x_inexact = idx->x_inexact;
-    ra.maxnorm = idx->maxnorm;
-    ra.ids = dIds ? dIds + b0 * ldo : nullptr;
-    ra.dists = dDists ? dDists + b0 * ldo : nullptr;
+    ra.emax = emax.as<uint32_t>();
     ra.ldo = ldo;
     ra.nfail = ctl.as<uint32_t>() + 1;
     ra.fail = failq.as<uint32_t>();
-    CK(launch_rerank(idx->metric, ra, s));
+    for (uint32_t round = 0; round < 2; round++) {
+      // the plan's work items: list-major, query tiles of the tensor kernel
+      TRY(plan_and_search(idx, b, mq, P, k, round, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s,
+                          1, -1, qtile));
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if (idx->profile) {
+        e0 = idx->ev_pool[2 * round];
+        e1 = idx->ev_pool[2 * round + 1];
+        CK(cudaEventRecord(e0, s));
+      }
+      CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
+      if (e1) CK(cudaEventRecord(e1, s));
+      if (round == 0) {
+        ra.tau = b.tau.as<uint32_t>();
+        ra.ids = nullptr;
+        ra.dists = nullptr;
+      } else {
+        ra.tau = nullptr;
+        ra.ids = dIds ? dIds + b0 * ldo : nullptr;
+        ra.dists = dDists ? dDists + b0 * ldo : nullptr;
+        if (!ra.ids && !ra.dists) ra.dists = b.res_d.as<float>();  // the certificate still runs
+      }
+      CK(launch_rerank(idx->metric, ra, s));
+    }
     uint32_t hc[2], bc[3];
     CK(cudaMemcpyAsync(hc, ctl.p, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(bc, b.ctl.p, 12, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (hc[0] || bc[2]) return fail(RBC_ERR_ITER_LIMIT, "rbc_query: a bounded device wait ran out");
-    if (e0) {
-      float ms = 0;
-      CK(cudaEventElapsedTime(&ms, e0, e1));
-      tc_ms += ms;
+    if (idx->profile) {
+      for (int r = 0; r < 2; r++) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, idx->ev_pool[2 * r], idx->ev_pool[2 * r + 1]));
+        tc_ms += ms;
+      }
+      tc_launches += 2;
     }
     const uint32_t nfail = hc[1];
     nfail_total += nfail;
-    if (nfail) {
+    if (nfail && (dIds || dDists)) {
       DevBuf Qf, fi, fd;
       CK(Qf.alloc((uint64_t)nfail * ld * 4, s));
       CK(fi.alloc((uint64_t)nfail * k * 4, s));
@@ -725,16 +700,15 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(cudaMemcpy(st, stats.p, sizeof(st), cudaMemcpyDeviceToHost));
   idx->stats.queries = m;
   idx->stats.rep_pairs = m * nr;
-  idx->stats.lists_probed = tc_lists;
-  idx->stats.point_pairs = tc_pairs;
+  idx->stats.point_pairs = st[0];
+  idx->stats.lists_probed = st[1];
   idx->stats.fallback_queries = nfail_total;
   if (idx->profile) {
-    idx->prof.search_launches = (m + mb - 1) / mb;
+    idx->prof.search_launches = tc_launches;
     idx->prof.search_ms = tc_ms;
   }
   return RBC_OK;
 }
-
 
 // ------------------------------------------------------------------ brute force
 // One search over the whole database split into chunks (bruteK / bruteSearch,
@@ -867,7 +841,8 @@ int rbc_build_host(const float *hX, uint64_t n, uint32_t d, uint32_t ldx, const 
 int rbc_destroy(rbc_index *idx) {
   if (!idx) return RBC_OK;
   void *ptrs[] = {idx->Xp,      idx->perm,   idx->offsets, idx->radius,     idx->R,  idx->os_lists, idx->os_counts,
-                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->Xb, idx->xn,       idx->owner};
+                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->tc.Xh, idx->tc.w,  idx->owner,
+                  idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : idx->ev_pool) cudaEventDestroy(e);
@@ -887,6 +862,7 @@ int rbc_get_info(const rbc_index *idx, rbc_index_info *info) {
   info->min_list = idx->min_list;
   info->max_list = idx->max_list;
   info->device_bytes = idx->device_bytes;
+  info->tc_format = idx->tc.format;
   return RBC_OK;
 }
 

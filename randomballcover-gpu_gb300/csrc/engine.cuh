@@ -58,9 +58,13 @@ namespace rbc {
 // Plan one query round (mode 0 probe pairs, mode 1 pruned pairs); stage 0
 // stops after the plan, 1 after the work items, 2 also runs the search.
 // tq < 0 uses the index's tuned tile.
+// qtile > 0 overrides the query tile of the work items.
 int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
-                    int grid, unsigned long long *stats, cudaStream_t s, int stage = 2, int tq = -1);
+                    int grid, unsigned long long *stats, cudaStream_t s, int stage = 2, int tq = -1,
+                    uint32_t qtile = 0);
+// Build the tensor-core operands of an index that has its partition.
+int build_tc(rbc_index *idx, cudaStream_t s);
 // Work items a plan of mb queries can produce (query tiles x row chunks).
 uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile);
 int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
@@ -90,14 +94,12 @@ struct rbc_index {
   uint32_t *os_ids = nullptr;     // nr x s packed ids: row -> id map of Xo
   uint64_t *os_offsets = nullptr; // nr + 1 rows of Xo per list
   float *Xo = nullptr;            // list-major copy of the one-shot lists' rows
-  // BF16 copy of the partition rows for tensor-core search (RBC_BUILD_BF16)
-  void *Xb = nullptr;             // n_pad x kp BF16, list-major, zero padded
-  float *xn = nullptr;            // n_pad squared row norms (+inf past n)
+  // tensor-core operands of the partition rows (RBC_BUILD_BF16): rows centered
+  // on their representative, in BF16 (exact data) or FP16 hi|lo (tc.cuh)
+  rbc::TcBuild tc{};
   uint64_t n_pad = 0;
   uint32_t kp = 0;
-  uint32_t x_inexact = 1;         // some value is not exact in BF16
-  float maxnorm = 0.f;            // largest row norm
-  CUtensorMap tmB;                // TMA map of Xb (128-row boxes, 128-byte swizzle)
+  CUtensorMap tmB;                // TMA map of tc.Xh (128-row boxes, 128-byte swizzle)
   // padded copy of the input in original order (legacy rbcStruct.dx)
   float *Xi = nullptr;
   uint64_t xi_rows = 0;

@@ -125,7 +125,9 @@ struct PlanArgs {
   const uint32_t *tau;     // per-query k-th distance bits after the probe phase
   uint64_t m;
   uint32_t nr, P, metric, qtile;
-  double gamma;            // relative error bound of a computed distance
+  float opg_ru, omg_rd;    // 1 + gamma rounded up, 1 - gamma rounded down (gamma: relative
+                           // error bound of a computed distance)
+  float c_ru, opc_ru;      // c = 1 + 3 gamma and 1 + c, rounded up
   uint32_t *list_cnt;      // nr+1 counters (surviving queries per list)
   uint32_t *list_cursor;   // nr fill cursors
   uint32_t *pair_q;        // list-major surviving (query) entries
@@ -142,16 +144,6 @@ cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s);
 // Items per list: query tiles x chunks of at most max_rows list rows.
 cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, const uint64_t *offsets, uint32_t nr,
                                   uint32_t qtile, uint32_t max_rows, uint32_t *tile_cnt, cudaStream_t s);
-// Counting sort of m queries by key[q * stride] in [0, nbins): order[slot] = q,
-// slot_of[q] = slot.  hist, start, cursor hold nbins + 1 words.
-cudaError_t launch_sort_by_key(const uint32_t *key, uint32_t stride, uint64_t m, uint32_t nbins,
-                               uint32_t *hist, uint32_t *start, uint32_t *cursor, void *scan_tmp,
-                               uint32_t *order, uint32_t *slot_of, cudaStream_t s);
-// flags[tile][list] = 1 (tile = slot / 128) for every surviving plan pair
-// (list_cnt may be null: probes only) and every probed pair.
-cudaError_t launch_mark_tiles(const uint32_t *list_start, const uint32_t *list_cnt, const uint32_t *pair_q,
-                              const uint32_t *probe, uint64_t m, uint32_t P, const uint32_t *slot_of,
-                              uint32_t nr, uint8_t *flags, cudaStream_t s);
 cudaError_t launch_plan_items(const uint32_t *list_cnt, const uint32_t *list_start,
                               const uint32_t *tile_start, const uint64_t *offsets, uint32_t nr,
                               uint32_t qtile, uint32_t max_rows, SearchItem *items, uint32_t *nitems,

@@ -4,7 +4,8 @@
 // every process (rbc.cu:126-208, 363-368).  An index file lets one process
 // build and others query.  Layout: a fixed 128-byte header, then the index's
 // arrays in a fixed order, each written only if the index has it (the flags
-// in the header say which).  All values little-endian, as in memory.
+// in the header say which).  All values little-endian, as in memory.  The
+// tensor-core operands are not stored: loading derives them from the lists.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -17,16 +18,15 @@ namespace rbc {
 namespace {
 
 constexpr char kMagic[8] = {'R', 'B', 'C', 'G', 'B', '3', '0', '0'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
 
 struct FileHeader {
   char magic[8];
   uint32_t version;
-  uint32_t d, ld, dp, nr, s, lds, kp, flags, x_inexact;
+  uint32_t d, ld, dp, nr, s, lds, kp, flags, reserved0;
   int32_t metric;
   uint64_t n, n_pad, xi_rows, min_list, max_list;
-  float maxnorm;
-  uint32_t reserved[7];
+  uint32_t reserved[8];
 };
 static_assert(sizeof(FileHeader) == 128, "index file header is 128 bytes");
 
@@ -87,14 +87,12 @@ extern "C" int rbc_save(const rbc_index *idx, const char *path) {
   h.lds = idx->lds;
   h.kp = idx->kp;
   h.flags = idx->flags;
-  h.x_inexact = idx->x_inexact;
   h.metric = idx->metric;
   h.n = idx->n;
   h.n_pad = idx->n_pad;
   h.xi_rows = idx->Xi ? idx->xi_rows : 0;
   h.min_list = idx->min_list;
   h.max_list = idx->max_list;
-  h.maxnorm = idx->maxnorm;
   if (std::fwrite(&h, sizeof(h), 1, fp) != 1) return fail(RBC_ERR_IO, "rbc_save: short write");
   if (std::fwrite(idx->rep_ids.data(), 4, idx->nr, fp) != idx->nr) return fail(RBC_ERR_IO, "rbc_save: short write");
   std::vector<unsigned char> stage(kStage);
@@ -114,10 +112,6 @@ extern "C" int rbc_save(const rbc_index *idx, const char *path) {
     if (rc == RBC_OK) rc = write_dev(fp, idx->os_ids, total * 4, stage);
     if (rc == RBC_OK) rc = write_dev(fp, idx->os_offsets, (nr + 1) * 8, stage);
     if (rc == RBC_OK) rc = write_dev(fp, idx->Xo, total * ld * 4, stage);
-  }
-  if (rc == RBC_OK && (idx->flags & RBC_BUILD_BF16)) {
-    rc = write_dev(fp, idx->Xb, (size_t)idx->n_pad * idx->kp * 2, stage);
-    if (rc == RBC_OK) rc = write_dev(fp, idx->xn, idx->n_pad * 4, stage);
   }
   if (rc == RBC_OK && idx->Xi) rc = write_dev(fp, idx->Xi, (size_t)idx->xi_rows * ld * 4, stage);
   if (rc != RBC_OK) return rc;
@@ -157,8 +151,6 @@ extern "C" int rbc_load(const char *path, rbc_index **out) {
   idx->lds = h.lds;
   idx->kp = h.kp;
   idx->n_pad = h.n_pad;
-  idx->x_inexact = h.x_inexact;
-  idx->maxnorm = h.maxnorm;
   idx->min_list = h.min_list;
   idx->max_list = h.max_list;
   idx->xi_rows = h.xi_rows;
@@ -188,16 +180,13 @@ extern "C" int rbc_load(const char *path, rbc_index **out) {
     if (rc == RBC_OK) rc = read_dev(fp, &idx->os_offsets, (nr + 1) * 8, stage, tot);
     if (rc == RBC_OK) rc = read_dev(fp, &idx->Xo, total * ld * 4, stage, tot);
   }
-  if (rc == RBC_OK && (h.flags & RBC_BUILD_BF16)) {
-    rc = read_dev(fp, reinterpret_cast<unsigned char **>(&idx->Xb), (size_t)h.n_pad * h.kp * 2, stage, tot);
-    if (rc == RBC_OK) rc = read_dev(fp, &idx->xn, h.n_pad * 4, stage, tot);
-    if (rc == RBC_OK) {
-      e = tc_make_map(&idx->tmB, idx->Xb, idx->n_pad, idx->kp, 128);
-      if (e != cudaSuccess) rc = cuda_fail(e, "rbc_load: tensor map");
-    }
-  }
   if (rc == RBC_OK && h.xi_rows) rc = read_dev(fp, &idx->Xi, (size_t)h.xi_rows * ld * 4, stage, tot);
   if (rc != RBC_OK) return rc;
+  if (h.flags & RBC_BUILD_BF16) {
+    if (!(h.flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_IO, "rbc_load: corrupt header");
+    rc = build_tc(idx, nullptr);
+    if (rc != RBC_OK) return rc;
+  }
   *out = idx;
   idx = nullptr;
   return RBC_OK;

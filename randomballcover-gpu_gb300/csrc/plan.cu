@@ -92,34 +92,46 @@ __global__ void row_topp_kernel(const float *__restrict__ D, uint64_t m, uint32_
   }
 }
 
-__device__ __forceinline__ float prune_threshold(float dqr, float dq0, float psi, uint32_t metric,
-                                                 double g) {
-  const double c = 1.0 + 3.0 * g;
-  double lo, hi0, hpsi;
-  if (metric == RBC_L1) {
-    lo = (double)dqr / (1.0 + g);
-    hi0 = (double)dq0 / (1.0 - g);
-    hpsi = (double)psi / (1.0 - g);
+// Lower bound on the computed distance of any member of list r, in the
+// comparison space (squared L2 or L1), evaluated in FP32 with every operation
+// rounded in the safe direction:
+//   lo   = D(q,r)/(1+g) (sqrt for L2), rounded down
+//   hi0  = D(q,r0)/(1-g) (sqrt for L2), rounded up
+//   hpsi = psi_r/(1-g) (sqrt for L2), rounded up
+//   lb   = max(lo - hpsi, (lo - c hi0) / (1 + c)), rounded down
+//   thr  = lb^2 (1-g) (L2) or lb (1-g) (L1), rounded down.
+__device__ __forceinline__ float prune_threshold(float dqr, float dq0, float hpsi, const PlanArgs &a) {
+  float lo, hi0;
+  if (a.metric == RBC_L1) {
+    lo = __fdiv_rd(dqr, a.opg_ru);
+    hi0 = __fdiv_ru(dq0, a.omg_rd);
   } else {
-    lo = sqrt((double)dqr / (1.0 + g));
-    hi0 = sqrt((double)dq0 / (1.0 - g));
-    hpsi = sqrt((double)psi / (1.0 - g));
+    lo = __fsqrt_rd(__fdiv_rd(dqr, a.opg_ru));
+    hi0 = __fsqrt_ru(__fdiv_ru(dq0, a.omg_rd));
   }
-  double lb = fmax(lo - hpsi, (lo - c * hi0) / (1.0 + c));
-  if (!(lb > 0.0)) return 0.f;
-  double t = (metric == RBC_L1 ? lb : lb * lb) * (1.0 - g) * (1.0 - 1e-12);
-  return __double2float_rd(t);
+  const float lb1 = __fsub_rd(lo, hpsi);
+  const float num = __fsub_rd(lo, __fmul_ru(a.c_ru, hi0));
+  const float lb2 = num > 0.f ? __fdiv_rd(num, a.opc_ru) : 0.f;
+  const float lb = fmaxf(lb1, lb2);
+  if (!(lb > 0.f)) return 0.f;
+  return a.metric == RBC_L1 ? __fmul_rd(lb, a.omg_rd) : __fmul_rd(__fmul_rd(lb, lb), a.omg_rd);
 }
 
-// mode 0: the pairs (q, probe[q][p]); mode 1: all other pairs whose bound
-// survives.  pass 0 counts per list, pass 1 writes the list-major entries.
-__global__ void plan_kernel(PlanArgs a, uint32_t mode) {
+// Bound on the radius term of list r (see prune_threshold), rounded up.
+__device__ __forceinline__ float psi_bound(float psi, const PlanArgs &a) {
+  const float t = __fdiv_ru(psi, a.omg_rd);
+  return a.metric == RBC_L1 ? t : __fsqrt_ru(t);
+}
+
+// mode 1: every (query, list) pair except the probed ones whose bound
+// survives; pass 0 counts per list, pass 1 writes the list-major entries.
+__global__ void plan_kernel(PlanArgs a) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t q0 = (uint64_t)blockIdx.y * kPlanQueries;
   const uint64_t q1 = min(a.m, q0 + kPlanQueries);
   const bool rv = r < a.nr;
   const bool nonempty = rv && a.offsets[r + 1] > a.offsets[r];
-  const float psi = (rv && mode == 1) ? a.radius[r] : 0.f;
+  const float hpsi = rv ? psi_bound(a.radius[r], a) : 0.f;
   uint32_t cnt = 0;
   for (int sweep = 0; sweep < (a.phase == 0 ? 1 : 2); sweep++) {
     uint32_t pos = 0;
@@ -131,19 +143,10 @@ __global__ void plan_kernel(PlanArgs a, uint32_t mode) {
       if (!nonempty) break;
       bool member = false;
       for (uint32_t p = 0; p < a.P; p++) member |= a.probe[q * a.P + p] == r;
-      bool surv;
-      float thr = 0.f;
-      if (mode == 0) {
-        surv = member;
-      } else {
-        surv = !member;
-        if (surv) {
-          float tau = __uint_as_float(a.tau[q]);
-          thr = prune_threshold(a.Dqr[q * a.nr + r], a.probed[q * a.P], psi, a.metric, a.gamma);
-          surv = !(thr > tau);
-        }
-      }
-      if (!surv) continue;
+      if (member) continue;
+      const float tau = __uint_as_float(a.tau[q]);
+      const float thr = prune_threshold(a.Dqr[q * a.nr + r], a.probed[q * a.P], hpsi, a);
+      if (thr > tau) continue;
       if (sweep == 0) {
         cnt++;
       } else {
@@ -153,6 +156,26 @@ __global__ void plan_kernel(PlanArgs a, uint32_t mode) {
       }
     }
     if (sweep == 0 && a.phase == 0 && cnt) atomicAdd(a.list_cnt + r, cnt);
+  }
+}
+
+// mode 0: the probe pairs (q, probe[q][p]) of non-empty lists, each list once
+// per query; one thread per probe entry.
+__global__ void plan_probe_kernel(PlanArgs a) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= a.m * a.P) return;
+  const uint64_t q = i / a.P;
+  const uint32_t p = (uint32_t)(i - q * a.P);
+  const uint32_t r = a.probe[i];
+  if (r >= a.nr || a.offsets[r + 1] == a.offsets[r]) return;
+  for (uint32_t t = 0; t < p; t++)
+    if (a.probe[q * a.P + t] == r) return;
+  if (a.phase == 0) {
+    atomicAdd(a.list_cnt + r, 1u);
+  } else {
+    const uint32_t pos = a.list_cnt[r] + atomicAdd(a.list_cursor + r, 1u);
+    a.pair_q[pos] = (uint32_t)q;
+    a.pair_thr[pos] = 0.f;
   }
 }
 
@@ -197,71 +220,7 @@ __global__ void plan_items_kernel(const uint32_t *__restrict__ list_cnt, const u
   }
 }
 
-// Counting sort of query indices by key (their nearest list): order[slot] = q.
-__global__ void key_hist_kernel(const uint32_t *__restrict__ key, uint32_t stride, uint64_t m,
-                                uint32_t *__restrict__ hist) {
-  uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (q < m) atomicAdd(hist + key[q * stride], 1u);
-}
-
-__global__ void key_scatter_kernel(const uint32_t *__restrict__ key, uint32_t stride, uint64_t m,
-                                   const uint32_t *__restrict__ start, uint32_t *__restrict__ cursor,
-                                   uint32_t *__restrict__ order, uint32_t *__restrict__ slot_of) {
-  uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (q >= m) return;
-  const uint32_t k = key[q * stride];
-  const uint32_t slot = start[k] + atomicAdd(cursor + k, 1u);
-  order[slot] = (uint32_t)q;
-  slot_of[q] = slot;
-}
-
-// flags[tile][list] = 1 for every surviving (list, query) pair of the plan
-// (one block per list) and for every probed (query, list) pair.
-__global__ void mark_pairs_kernel(const uint32_t *__restrict__ list_start, const uint32_t *__restrict__ list_cnt,
-                                  const uint32_t *__restrict__ pair_q, const uint32_t *__restrict__ slot_of,
-                                  uint32_t nr, uint8_t *__restrict__ flags) {
-  const uint32_t r = blockIdx.x;
-  const uint32_t s0 = list_start[r], c = list_cnt[r];
-  for (uint32_t i = threadIdx.x; i < c; i += blockDim.x) flags[(uint64_t)(slot_of[pair_q[s0 + i]] / 128) * nr + r] = 1;
-}
-
-__global__ void mark_probes_kernel(const uint32_t *__restrict__ probe, uint64_t m, uint32_t P,
-                                   const uint32_t *__restrict__ slot_of, uint32_t nr, uint8_t *__restrict__ flags) {
-  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (i >= m * P) return;
-  const uint64_t q = i / P;
-  const uint32_t r = probe[i];
-  if (r < nr) flags[(uint64_t)(slot_of[q] / 128) * nr + r] = 1;
-}
-
 }  // namespace
-
-cudaError_t launch_sort_by_key(const uint32_t *key, uint32_t stride, uint64_t m, uint32_t nbins, uint32_t *hist,
-                               uint32_t *start, uint32_t *cursor, void *scan_tmp, uint32_t *order, uint32_t *slot_of,
-                               cudaStream_t s) {
-  if (m == 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(hist, 0, (nbins + 1) * 4, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(cursor, 0, (nbins + 1) * 4, s);
-  if (e != cudaSuccess) return e;
-  key_hist_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(key, stride, m, hist);
-  if ((e = launched()) != cudaSuccess) return e;
-  if ((e = launch_exclusive_scan(hist, start, nbins + 1, scan_tmp, nullptr, s)) != cudaSuccess) return e;
-  key_scatter_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(key, stride, m, start, cursor, order, slot_of);
-  return launched();
-}
-
-cudaError_t launch_mark_tiles(const uint32_t *list_start, const uint32_t *list_cnt, const uint32_t *pair_q,
-                              const uint32_t *probe, uint64_t m, uint32_t P, const uint32_t *slot_of, uint32_t nr,
-                              uint8_t *flags, cudaStream_t s) {
-  if (m == 0) return cudaSuccess;
-  cudaError_t e = cudaSuccess;
-  if (list_cnt) {
-    mark_pairs_kernel<<<nr, 128, 0, s>>>(list_start, list_cnt, pair_q, slot_of, nr, flags);
-    if ((e = launched()) != cudaSuccess) return e;
-  }
-  mark_probes_kernel<<<(unsigned)((m * P + 255) / 256), 256, 0, s>>>(probe, m, P, slot_of, nr, flags);
-  return launched();
-}
 
 cudaError_t launch_row_topp(const float *D, uint64_t m, uint32_t nr, uint32_t P, uint32_t *probe, float *probed,
                             cudaStream_t s) {
@@ -275,8 +234,13 @@ cudaError_t launch_row_topp(const float *D, uint64_t m, uint32_t nr, uint32_t P,
 // a.list_cnt pointing at the scanned list starts and list_cursor zeroed.
 cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s) {
   if (a.m == 0) return cudaSuccess;
-  dim3 grid((a.nr + 255) / 256, (unsigned)((a.m + kPlanQueries - 1) / kPlanQueries));
-  plan_kernel<<<grid, 256, 0, s>>>(a, mode);
+  if (mode == 0) {
+    const uint64_t total = a.m * a.P;
+    plan_probe_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(a);
+  } else {
+    dim3 grid((a.nr + 255) / 256, (unsigned)((a.m + kPlanQueries - 1) / kPlanQueries));
+    plan_kernel<<<grid, 256, 0, s>>>(a);
+  }
   return launched();
 }
 

@@ -87,6 +87,18 @@ __device__ __forceinline__ void tma_load_2d(void *smem, const CUtensorMap *map, 
       : "memory");
 }
 
+// Four rows r0..r3 (any order, any row indices) of a 2-D tensor whose box is
+// one row high, columns [c0, c0 + box width), into 4 consecutive box rows at
+// smem; the map's swizzle applies as for a 4-row tile at that address.
+__device__ __forceinline__ void tma_gather4(void *smem, const CUtensorMap *map, int32_t c0, int32_t r0, int32_t r1,
+                                            int32_t r2, int32_t r3, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_u32(smem)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // 1-D bulk copy global -> shared (16-byte aligned addresses, size % 16 == 0).
 __device__ __forceinline__ void bulk_load(void *smem, const void *gmem, uint32_t bytes, uint64_t *bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -174,6 +186,13 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
   return (1u << 4)            // D format F32
          | (1u << 7)          // A format BF16
          | (1u << 10)         // B format BF16
+         | ((N >> 3) << 17)   // N / 8
+         | ((M >> 4) << 24);  // M / 16
+}
+
+// Instruction descriptor of kind::f16: FP16 x FP16 -> F32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16_f32(uint32_t M, uint32_t N) {
+  return (1u << 4)            // D format F32 (A and B format F16 = 0)
          | ((N >> 3) << 17)   // N / 8
          | ((M >> 4) << 24);  // M / 16
 }

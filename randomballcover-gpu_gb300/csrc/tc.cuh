@@ -1,94 +1,138 @@
-// tc.cuh -- interface of the tensor-core (precision form) search.
+// tc.cuh -- interface of the tensor-core (precision form) list search.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda.h>
 #include <cuda_runtime.h>
+
+#include "kernels.cuh"
 
 namespace rbc {
 
 constexpr int kShortlist = 40;  // rows kept per query by the tensor pass (4k for k = 10)
 
-// A work unit: one 128-query tile against database rows [p0, p1), both
-// multiples of 128 (the B tile height).
-struct TcUnit {
-  uint32_t tile;
-  uint32_t pad;
-  uint64_t p0, p1;
-};
+// Operand format of the tensor form, chosen at build from the data:
+//   kTcExact  every centered database value is exact in BF16 (e.g. integer
+//             features): one BF16 x BF16 product per pair;
+//   kTcSplit  otherwise: FP16 hi + lo halves of power-of-two scaled values,
+//             three products (hi.hi + hi.lo + lo.hi) per pair.
+enum TcFormat : uint32_t { kTcExact = 0, kTcSplit = 1 };
 
+// Tensor-core search of list-major work items (the planner's SearchItems):
+// item = rows [p0, p0 + np) of one list x up to 128 * mt queries qidx[q0 ..).
 struct TcArgs {
-  const TcUnit *units;
-  uint32_t nunits;
-  uint32_t kblocks;     // K / 64 (BF16 elements per 128-byte swizzled row)
-  const float *xn;      // squared norm per database row (padded rows: +inf)
-  uint64_t m_pad;       // query slots (multiple of 128)
-  float *sl_a;          // [2][m_pad][SL] approx values (without ||q||^2), ascending
-  uint32_t *sl_row;     // [2][m_pad][SL] database rows
-  uint32_t *sl_sel;     // per query: which of the two buffers is current
-  uint32_t *sl_theta;   // per query: largest approx kept once SL rows are held
+  const SearchItem *items;
+  const uint32_t *nitems;   // device count written by the planner
+  const uint32_t *qidx;     // item query slots -> query index (batch-local)
+  const float *Dqr;         // m x nr query-representative distances (exact FP32)
+  uint32_t nr;
+  uint32_t kb;              // 64-wide K blocks of one operand half (kp / 64)
+  uint32_t zero_row;        // an all-zero row of the query operand (gathered for empty slots)
+  uint32_t d;
+  const float *w;           // per database row: ||x'||^2 + 2 c.x' (x' = x - c, c its representative)
+  const float *lscale;      // per list: power-of-two scale of the stored halves
+  const float *lxmax;       // per list: bound on ||x'||
+  const float *lcnorm;      // per list: ||c||
+  const float *qscale;      // per query: power-of-two scale of its halves
+  const float *qnorm;       // per query: ||q||
+  const uint8_t *q_inexact; // per query: some value not exact in the operand format
+  uint32_t x_inexact;
+  uint32_t format;          // TcFormat
+  float *sl_a;              // [2][m][SL] approx distances, ascending
+  uint32_t *sl_row;         // [2][m][SL] database rows (list-major index)
+  uint32_t *sl_sel;         // per query: current buffer
+  uint32_t *sl_theta;       // per query: largest approx kept once SL rows are held (float bits)
   uint32_t *sl_lock;
+  uint32_t *emax;           // per query: max error bound over the lists searched (float bits)
+  uint64_t m;
+  const uint64_t *offsets;  // list starts (for the work counters)
+  unsigned long long *stats;  // [0] (query, row) pairs, [1] (query, list) pairs; may be null
   uint32_t *err;
+  uint32_t a_stages, b_stages;  // set by launch_tc_search from the shared-memory budget
 };
 
 struct RerankArgs {
   const float *X;        // FP32 database rows (list-major), stride ld
   const uint32_t *pid;   // row -> original id
-  const float *Q;        // FP32 query rows in slot order, stride ld
-  const uint32_t *order; // slot -> query index (output row); nullptr: identity
+  const float *Q;        // FP32 query rows, stride ld
   uint32_t ld, dp, k;
-  uint64_t m, m_pad;
+  uint64_t m;
   const float *sl_a;
   const uint32_t *sl_row;
   const uint32_t *sl_sel;
-  const float *qn;
-  const uint8_t *q_inexact;
-  uint32_t x_inexact;
-  float maxnorm;
-  uint32_t *ids;
+  const uint32_t *emax;
+  uint32_t *tau;         // if set: the k-th exact distance (float bits) -> pruning threshold
+  uint32_t *ids;         // if set (with dists): results and certificate
   float *dists;
   uint32_t ldo;
   uint32_t *nfail;
   uint32_t *fail;
 };
 
-// Upper bound on |approx(q,x) - exact(q,x)| for every database row x, where
-// exact is the reference's sequential FP32 difference-form distance and
-// approx = fl(fl(||x||^2 - 2 q.x) + ||q||^2) with q.x from BF16 operands and
-// FP32 tensor-core accumulation.  Terms (u = 2^-24, b = 2^-8 the BF16 unit
-// roundoff, applied only to operands that are not exact in BF16):
-//   operand rounding      (b_q + b_x + b_q b_x) |q| |x|, twice (the -2 q.x)
-//   accumulation          d 2^-22 sum|q_i x_i| (twice the truncating bound), twice
-//   two final roundings   2u (|q|^2 + |x|^2 + 2|q||x|)
-//   norms and the exact
-//   distance's own error  gamma_d (|q|^2 + |x|^2) and gamma_d |q - x|^2
-// The total is doubled as a margin.
-__host__ __device__ inline double tc_error_bound(float qn, float maxnorm, uint32_t q_inexact, uint32_t x_inexact,
-                                                 uint32_t d) {
-  const double u = 5.9604644775390625e-08;
-  const double b = 1.0 / 256.0;
-  const double gd = (d + 2) * u / (1.0 - (d + 2) * u);
-  const double bq = q_inexact ? b : 0.0, bx = x_inexact ? b : 0.0;
-  const double nq = sqrt((double)qn / (1.0 - gd)), X = (double)maxnorm * (1.0 + gd);
-  const double quant = bq + bx + bq * bx;
-  const double accum = (double)d * 4.0 * u * (1.0 + bq) * (1.0 + bx);
-  const double A = 2.0 * quant + 2.0 * accum + 4.0 * u + 2.0 * gd;
-  const double B = 2.0 * gd + 2.0 * u;
-  return 2.0 * (A * nq * X + B * (nq * nq + X * X));
+// Upper bound on |approx(q, x) - exact(q, x)| for every row x of list r, where
+//   approx = fl(Dqr + fl(alpha D + w)),  alpha D ~ -2 q.x'  (tensor cores),
+//   Dqr ~ ||q - c||^2, w ~ ||x'||^2 + 2 c.x', x' = x - c,
+// and exact is the reference's sequential FP32 difference-form distance.
+// Inputs: Dqr (computed), qn = ||q||, X = bound on ||x'||, C = ||c||.
+// Terms, with u = 2^-24 and g = gamma_{d+3}:
+//   operand representation   eps_rep |q| |x'|           (BF16 rounding of
+//                            inexact operands, or the hi/lo residuals)
+//   accumulation             nacc 2^-22 |q| |x'|        (twice the bound of
+//                            truncating FP32 accumulation of nacc products)
+//   centering                u |q| |x'|                 (x' rounded to FP32)
+//   ||q-c||^2 and w          g (||q-c||^2 + ||x'||^2 + 2 C |x'|)
+//   two final roundings      u (||q-c||^2 + 2 (2|q||x'| + ||x'||^2 + 2C|x'|))
+//   the exact distance       g (||q-c|| + |x'|)^2
+// doubled as a margin.
+__host__ __device__ inline float tc_error_bound(float Dqr, float qn, float X, float C, uint32_t q_inexact,
+                                                uint32_t x_inexact, uint32_t format, uint32_t d) {
+  const float u = 5.9604644775390625e-08f;
+  const float g = (d + 3) * u / (1.f - (d + 3) * u);
+  float eps, nacc;
+  if (format == kTcSplit) {
+    // hi = fl16(v), lo = fl16(v - hi): |v - hi - lo| <= 2^-22 |v|; lo.lo omitted <= 2^-22
+    eps = 3.f * 2.384185791015625e-07f + d * 5.9604644775390625e-08f;  // + FP16 underflow margin
+    nacc = 3.f * d * 1.01f;
+  } else {
+    const float b = 1.f / 256.f;
+    const float bq = q_inexact ? b : 0.f, bx = x_inexact ? b : 0.f;
+    eps = bq + bx + bq * bx;
+    nacc = d * (1.f + bq) * (1.f + bx);
+  }
+  const float qc2 = Dqr * (1.f + g), Q = qn * (1.f + g), Cb = C * (1.f + g);
+  const float qx = Q * X;
+  const float A = 2.f * (eps + nacc * 2.384185791015625e-07f + u) * qx;
+  const float B = g * (qc2 + X * X + 2.f * Cb * X);
+  const float R = u * (qc2 + 2.f * (2.f * qx + X * X + 2.f * Cb * X));
+  const float F = g * (sqrtf(qc2) + X) * (sqrtf(qc2) + X);
+  // the float evaluation of this bound errs by far less than the final factor 2 covers
+  return 2.f * (A + B + R + F) * (1.f + 1e-5f);
 }
 
 bool tc_supported(uint32_t dp);
 uint32_t tc_kp(uint32_t d);
-size_t tc_smem_bytes(uint32_t kp);
 int tc_grid();
-cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32_t kp, uint32_t box_rows);
-cudaError_t launch_to_bf16(const float *src, uint32_t ld, uint64_t rows, uint64_t rows_pad, uint32_t d,
-                           uint32_t kp, void *dst, float *norm, float pad_norm, uint32_t *inexact,
-                           uint32_t *maxnorm_bits, cudaStream_t s);
-cudaError_t launch_row_inexact(const float *src, uint32_t ld, uint64_t rows, uint32_t d, uint8_t *flag,
-                               cudaStream_t s);
+uint32_t tc_query_tile(uint32_t format);  // queries per work item (128 x tiles per CTA)
+cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32_t cols, uint32_t box_rows);
+
+// Build: centered rows of each list (x' = x - c_r), the format check, per-list
+// scales and bounds, the half-precision operand rows and w.
+struct TcBuild {
+  void *Xh;          // n_pad x cols halves (cols = kp, or 2 kp for the split format)
+  float *w;          // n_pad + 128
+  float *lscale, *lxmax, *lcnorm;  // nr each
+  uint32_t format, x_inexact, cols;
+};
+int tc_build(const float *Xp, const uint64_t *offsets, const float *R, const float *radius, uint64_t n,
+             uint64_t n_pad, uint32_t nr, uint32_t d, uint32_t ld, uint32_t kp, TcBuild *out, uint64_t *bytes,
+             cudaStream_t s);
+
+// Queries: half-precision operand rows (m rows + one zero row), scales, norms, flags.
+cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp, uint32_t format,
+                              void *Qh, float *qscale, float *qnorm, uint8_t *q_inexact, cudaStream_t s);
 cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
-                           uint64_t m, cudaStream_t s);
+                           uint32_t *emax, uint64_t m, cudaStream_t s);
 cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
                              cudaStream_t s);
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s);

@@ -19,6 +19,7 @@ L2, L1 = 0, 1
 KMAX = 32
 BUILD_PARTITION, BUILD_ONESHOT, BUILD_BF16 = 1, 2, 4
 QUERY_EXACT, QUERY_ONESHOT, QUERY_EXACT_TC = 0, 1, 2
+TC_BF16, TC_FP16_SPLIT = 0, 1
 QUERY_ROUTED = 0x1000
 SYNTH_UNIFORM, SYNTH_MIXTURE, SYNTH_GEOMETRIC = 0, 1, 2
 DUMMY = 0xFFFFFFFF
@@ -39,7 +40,7 @@ class BuildParams(C.Structure):
 class IndexInfo(C.Structure):
     _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("ld", C.c_uint32), ("num_reps", C.c_uint32),
                 ("s", C.c_uint32), ("metric", C.c_int), ("flags", C.c_uint32), ("min_list", C.c_uint64),
-                ("max_list", C.c_uint64), ("device_bytes", C.c_uint64)]
+                ("max_list", C.c_uint64), ("device_bytes", C.c_uint64), ("tc_format", C.c_uint32)]
 
 
 class QueryStats(C.Structure):

@@ -57,6 +57,36 @@ def test_batch_heterogeneous_instances(rbc, oracle, metric):
         c[0].close()
 
 
+def test_batch_64_instances_config_shape(rbc, oracle):
+    """The batched configuration's shape scaled down: 64 instances, n log-uniform,
+    d in {32, 64, 128}, k in {1, 10, 32}, m = n / 100, Gaussian mixtures with
+    100-1,000 components, each index autotuned."""
+    rng = np.random.default_rng(4)
+    batch = rbc.Batch()
+    cases = []
+    for i in range(64):
+        n = int(np.exp(rng.uniform(np.log(2000), np.log(40000))))
+        d = int(rng.choice([32, 64, 128]))
+        k = int(rng.choice([1, 10, 32]))
+        m = max(1, n // 100)
+        nc = int(rng.integers(100, 1001))
+        X = rbc.synth(1, 400 + i, 0, n, d, ncomp=nc, sigma_lo=0.05, sigma_hi=0.05)
+        Q = rbc.synth(1, 400 + i, 1, m, d, ncomp=nc, sigma_lo=0.05, sigma_hi=0.05)
+        idx = rbc.Index(X, int(max(64, 2 * np.sqrt(n))), seed=i)
+        idx.autotune(Q, k)
+        cases.append((idx, X, Q, k) + batch.add(idx, Q, k))
+    launches = rbc.kernel_launches()
+    batch.run()
+    batch.run()
+    torch.cuda.synchronize()
+    assert rbc.kernel_launches() > launches  # replays are counted
+    for idx, X, Q, k, ids, dists in cases:
+        check_exact(ids, dists, X.cpu().numpy(), Q.cpu().numpy(), k, 0, rbc, oracle)
+    batch.close()
+    for c in cases:
+        c[0].close()
+
+
 def test_batch_shares_an_index(rbc, oracle):
     """The same index in several instances (many clients of one database)."""
     rng = np.random.default_rng(7)

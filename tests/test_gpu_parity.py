@@ -227,8 +227,13 @@ def test_tensor_core_exact_equals_oracle(rbc, oracle, case):
     ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), k)
     assert_same(ids, dists, ri, rd, rbc)
     st = idx.stats()
+    fmt = idx.info()["tc_format"]
     if kind == 2:
+        assert fmt == rbc.TC_BF16  # integers stay exact in BF16 after centering
         assert st["fallback_queries"] == 0, st  # integer data certifies every query
+    else:
+        assert fmt == rbc.TC_FP16_SPLIT
+        assert st["fallback_queries"] <= m // 20, st  # the split format certifies nearly every query
     ids2, dists2 = idx.query(Q, k)  # the plain form on the same index agrees
     assert (ids2 == ids).all() and (dists2 == dists).all()
     idx.close()
