@@ -53,11 +53,11 @@ UNIT = "queries/s"
 WORKLOADS = {
     # kind, seed, n, m, d, k, reps, ncomp, sigma_lo, sigma_hi, train queries, router epochs, forms
     "c1": dict(kind=0, seed=1, n=65_536, m=8_192, d=16, k=1, reps=256, ncomp=1, slo=0.0, shi=0.0,
-               train=0, epochs=0, forms="tensor,plain",
+               train=0, epochs=0, forms="oneshot,tensor,plain",
                metric="exact 1-NN queries/s, n=65,536 d=16 uniform, plain FP32 RBC",
                desc="i.i.d. uniform [0,1)"),
     "c2": dict(kind=1, seed=2, n=1_048_576, m=100_000, d=128, k=32, reps=1024, ncomp=1000, slo=0.05, shi=0.05,
-               train=0, epochs=0, forms="tensor,plain",
+               train=0, epochs=0, forms="oneshot,tensor,plain",
                metric="exact 32-NN queries/s, n=1,048,576 d=128 mixture, plain FP32 RBC",
                desc="1,000-component Gaussian mixture, sigma 0.05"),
     "c3": dict(kind=2, seed=3, n=10_000_000, m=10_000, d=128, k=10, reps=4096, ncomp=1, slo=0.0, shi=0.0,
@@ -321,12 +321,13 @@ def run_engine(a):
     Q = pyrbc.synth(w["kind"], w["seed"], 1, w["m"], w["d"], **synth)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    idx = pyrbc.Index(X, w["reps"], seed=w["seed"], flags=pyrbc.BUILD_PARTITION | pyrbc.BUILD_BF16)
+    forms = [f for f in a.forms.split(",") if f]
+    head = forms[-1]
+    flags = pyrbc.BUILD_PARTITION | pyrbc.BUILD_BF16 | (pyrbc.BUILD_ONESHOT if "oneshot" in forms else 0)
+    idx = pyrbc.Index(X, w["reps"], s=w["reps"], seed=w["seed"], flags=flags)
     build_s = time.perf_counter() - t0
     info = idx.info()
     k, m = w["k"], w["m"]
-    forms = [f for f in a.forms.split(",") if f]
-    head = forms[-1]
 
     # the learned router: trained on the GPU on queries the RBC labels
     router_info = None
@@ -349,7 +350,7 @@ def run_engine(a):
                        "architecture": f"MLP {w['d']}->512->512->{w['reps']} GELU, BF16 weights, FP32 accumulate"}
         idx.set_router(router, probes=2)
 
-    modes = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC,
+    modes = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC, "oneshot": pyrbc.QUERY_ONESHOT,
              "learned": pyrbc.QUERY_EXACT_TC | pyrbc.QUERY_ROUTED, "learned_plain": pyrbc.QUERY_EXACT | pyrbc.QUERY_ROUTED}
     idx.set_profiling(True)
     ids = torch.empty((m, k), dtype=torch.int32, device="cuda")
@@ -384,6 +385,7 @@ def run_engine(a):
         acc["steps"] = steps
         acc["value"] = world * m * steps / (acc["ms"] / 1000.0)
         acc["ids"] = ids.clone()
+        acc["dists"] = dists.clone()
         acc["fp64"] = fp64_error(X, Q, ids, dists)
         return acc
 
@@ -394,7 +396,28 @@ def run_engine(a):
         else:
             results[f] = timed(modes[f], min(a.steps, 3), 1)
     res = results[head]
-    same = all(bool((r["ids"] == res["ids"]).all().item()) for r in results.values())
+    exact_forms = [f for f in results if f != "oneshot"]
+    same = all(bool((results[f]["ids"] == results[exact_forms[-1]]["ids"]).all().item()) for f in exact_forms)
+    oneshot_recall = None
+    if "oneshot" in results and exact_forms:
+        # the reference's one-shot algorithm is approximate: share of the exact k-NN it returns
+        ex, os_ = results[exact_forms[-1]]["ids"].long(), results["oneshot"]["ids"].long()
+        hit = (os_[:, :, None] == ex[:, None, :]).any(2).float().mean().item()
+        oneshot_recall = hit
+    range_count = None
+    if a.workload in ("c1", "c2"):
+        # brute-force range count (bruteRangeCount) of a query sample, ranges = the k-th exact distance
+        nq = min(m, 2048)
+        ranges = results[exact_forms[-1]]["dists"][:nq, k - 1].contiguous() if exact_forms else None
+        if ranges is not None:
+            pyrbc.range_count(X, Q[:nq], ranges)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            cnt = pyrbc.range_count(X, Q[:nq], ranges)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            range_count = {"queries": nq, "ms": dt * 1e3, "pairs_per_s": nq * w["n"] / dt,
+                           "all_counts_at_least_k_minus_1": bool((cnt >= k - 1).all().item())}
     clk, value, ms, launches = res["clocks"], res["value"], res["ms"], res["launches"]
 
     # end to end through the host API: pinned host queries in, results out
@@ -439,10 +462,12 @@ def run_engine(a):
 
     if rank == 0:
         names = {"plain": "plain FP32 exact RBC", "tensor": "exact RBC, BF16 tcgen05 list search + FP32 rerank",
+                 "oneshot": "the reference's one-shot RBC (approximate)",
                  "learned": "exact RBC, learned router + BF16 tcgen05 list search + FP32 rerank",
                  "learned_plain": "exact RBC, learned router + FP32 list search"}
         extra = {"build_s": build_s, "min_list": info["min_list"], "max_list": info["max_list"],
-                 "same_ids_all_forms": same, "router": router_info, "forms": {}}
+                 "tc_format": ["bf16", "fp16_split"][info["tc_format"]], "same_ids_all_exact_forms": same,
+                 "router": router_info, "oneshot_recall": oneshot_recall, "range_count": range_count, "forms": {}}
         for f, r in results.items():
             extra["forms"][f] = {"value": r["value"], "ms_per_step": r["ms"] / r["steps"],
                                  "lists_per_query": r["lists"] / (m * r["steps"]),

@@ -263,26 +263,49 @@ __global__ void __launch_bounds__(kSelThreads) row_select_kernel(const float *__
   }
 }
 
+// Ids of row b's selected entries, increasing: every value below the s-th
+// smallest, and the first `need` values equal to it.  Each thread holds 4
+// consecutive values (one 16-byte load); chunks of 4 x 1024 values with no
+// value at or below the threshold -- nearly all of them, s << n -- cost one
+// block vote; the others take two block scans.
 __global__ void __launch_bounds__(kSelThreads) row_compact_kernel(const float *__restrict__ D, uint64_t ldD,
                                                                   uint64_t n, const uint32_t *__restrict__ thr_bits,
                                                                   const uint32_t *__restrict__ need,
                                                                   uint32_t *__restrict__ lists, uint32_t lds,
                                                                   uint32_t *__restrict__ counts) {
   __shared__ uint32_t ws[32];
-  const uint32_t *row = reinterpret_cast<const uint32_t *>(D + blockIdx.x * ldD);
+  const uint4 *row = reinterpret_cast<const uint4 *>(D + blockIdx.x * ldD);  // ldD % 4 == 0
   const uint32_t t = thr_bits[blockIdx.x], nd = need[blockIdx.x];
   uint32_t *out = lists + (uint64_t)blockIdx.x * lds;
   uint32_t taken = 0, eq_seen = 0;
-  for (uint64_t b = 0; b < n; b += kSelThreads) {
-    uint64_t i = b + threadIdx.x;
-    uint32_t v = i < n ? row[i] : 0xFFFFFFFFu;
-    uint32_t is_eq = (i < n) && v == t;
+  for (uint64_t b = 0; b < n; b += 4 * kSelThreads) {
+    const uint64_t i0 = b + 4 * threadIdx.x;
+    uint4 v4 = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    if (i0 < n) v4 = row[i0 >> 2];
+    uint32_t v[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (i0 + j >= n) v[j] = 0xFFFFFFFFu;
+    const bool has = v[0] <= t || v[1] <= t || v[2] <= t || v[3] <= t;
+    if (!__syncthreads_or(has)) continue;
+    uint32_t neq = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) neq += v[j] == t;
     uint32_t eq_total;
-    uint32_t eq_rank = eq_seen + block_exclusive_scan(is_eq, ws, eq_total);
-    uint32_t sel = (i < n) && (v < t || (is_eq && eq_rank < nd));
+    uint32_t eq_rank = eq_seen + block_exclusive_scan(neq, ws, eq_total);
+    uint32_t sel[4], nsel = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const bool is_eq = v[j] == t;
+      sel[j] = v[j] < t || (is_eq && eq_rank < nd);
+      eq_rank += is_eq;
+      nsel += sel[j];
+    }
     uint32_t sel_total;
-    uint32_t pos = taken + block_exclusive_scan(sel, ws, sel_total);
-    if (sel) out[pos] = (uint32_t)i;
+    uint32_t pos = taken + block_exclusive_scan(nsel, ws, sel_total);
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (sel[j]) out[pos++] = (uint32_t)(i0 + j);
     taken += sel_total;
     eq_seen += eq_total;
   }

@@ -549,8 +549,9 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(qscale.alloc((mb + 1) * 4, s));
   CK(qnorm.alloc((mb + 1) * 4, s));
   CK(qinex.alloc(mb + 1, s));
-  CK(sl_a.alloc(2 * mb * kShortlist * 4, s));
-  CK(sl_row.alloc(2 * mb * kShortlist * 4, s));
+  const uint32_t sl = tc_shortlist(k);
+  CK(sl_a.alloc(2 * mb * sl * 4, s));
+  CK(sl_row.alloc(2 * mb * sl * 4, s));
   CK(sl_sel.alloc(mb * 4, s));
   CK(sl_theta.alloc(mb * 4, s));
   CK(sl_lock.alloc(mb * 4, s));
@@ -592,12 +593,12 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(),
                            mq, s));
     // query operands (row mq is the zero row gathered for empty item slots)
-    CK(launch_tc_queries(b.Qp.as<float>(), ld, mq, idx->d, kp, fmt, Qh.p, qscale.as<float>(), qnorm.as<float>(),
-                         qinex.as<uint8_t>(), s));
+    CK(launch_tc_queries(b.Qp.as<float>(), ld, mq, idx->d, kp, fmt, idx->tc.mu, Qh.p, qscale.as<float>(),
+                         qnorm.as<float>(), qinex.as<uint8_t>(), s));
     CUtensorMap tmA;
     CK(tc_make_map(&tmA, Qh.p, mq + 1, cols, 1));
     CK(launch_sl_init(sl_a.as<float>(), sl_row.as<uint32_t>(), sl_sel.as<uint32_t>(), sl_theta.as<uint32_t>(),
-                      sl_lock.as<uint32_t>(), emax.as<uint32_t>(), mq, s));
+                      sl_lock.as<uint32_t>(), emax.as<uint32_t>(), mq, sl, s));
     TcArgs ta{};
     ta.items = b.items.as<SearchItem>();
     ta.nitems = b.ctl.as<uint32_t>() + 1;
@@ -616,6 +617,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     ta.q_inexact = qinex.as<uint8_t>();
     ta.x_inexact = idx->tc.x_inexact;
     ta.format = fmt;
+    ta.sl = sl;
     ta.sl_a = sl_a.as<float>();
     ta.sl_row = sl_row.as<uint32_t>();
     ta.sl_sel = sl_sel.as<uint32_t>();
@@ -633,6 +635,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     ra.ld = ld;
     ra.dp = idx->dp;
     ra.k = k;
+    ra.sl = sl;
     ra.m = mq;
     ra.sl_a = sl_a.as<float>();
     ra.sl_row = sl_row.as<uint32_t>();
@@ -842,7 +845,7 @@ int rbc_destroy(rbc_index *idx) {
   if (!idx) return RBC_OK;
   void *ptrs[] = {idx->Xp,      idx->perm,   idx->offsets, idx->radius,     idx->R,  idx->os_lists, idx->os_counts,
                   idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->tc.Xh, idx->tc.w,  idx->owner,
-                  idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm};
+                  idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm, idx->tc.mu};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : idx->ev_pool) cudaEventDestroy(e);

@@ -10,13 +10,21 @@
 
 namespace rbc {
 
-constexpr int kShortlist = 40;  // rows kept per query by the tensor pass (4k for k = 10)
+// Rows kept per query by the tensor pass: 4k, at least 40 and at most 56 (the
+// warp merge holds 64 pairs: the list plus one lane's 8 candidates).
+constexpr uint32_t kShortlistMin = 40, kShortlistMax = 56;
+inline uint32_t tc_shortlist(uint32_t k) {
+  const uint32_t s = 4 * k;
+  return s < kShortlistMin ? kShortlistMin : (s > kShortlistMax ? kShortlistMax : s);
+}
 
 // Operand format of the tensor form, chosen at build from the data:
 //   kTcExact  every centered database value is exact in BF16 (e.g. integer
 //             features): one BF16 x BF16 product per pair;
 //   kTcSplit  otherwise: FP16 hi + lo halves of power-of-two scaled values,
-//             three products (hi.hi + hi.lo + lo.hi) per pair.
+//             three products per pair, hi.hi into one accumulator and the
+//             corrections hi.lo + lo.hi into another; queries are centered on
+//             mu (the mean of the representatives) before splitting.
 enum TcFormat : uint32_t { kTcExact = 0, kTcSplit = 1 };
 
 // Tensor-core search of list-major work items (the planner's SearchItems):
@@ -33,12 +41,13 @@ struct TcArgs {
   const float *w;           // per database row: ||x'||^2 + 2 c.x' (x' = x - c, c its representative)
   const float *lscale;      // per list: power-of-two scale of the stored halves
   const float *lxmax;       // per list: bound on ||x'||
-  const float *lcnorm;      // per list: ||c||
+  const float *lcnorm;      // per list: ||c - mu||
   const float *qscale;      // per query: power-of-two scale of its halves
-  const float *qnorm;       // per query: ||q||
+  const float *qnorm;       // per query: ||q - mu||
   const uint8_t *q_inexact; // per query: some value not exact in the operand format
   uint32_t x_inexact;
   uint32_t format;          // TcFormat
+  uint32_t sl;              // shortlist length SL
   float *sl_a;              // [2][m][SL] approx distances, ascending
   uint32_t *sl_row;         // [2][m][SL] database rows (list-major index)
   uint32_t *sl_sel;         // per query: current buffer
@@ -56,7 +65,7 @@ struct RerankArgs {
   const float *X;        // FP32 database rows (list-major), stride ld
   const uint32_t *pid;   // row -> original id
   const float *Q;        // FP32 query rows, stride ld
-  uint32_t ld, dp, k;
+  uint32_t ld, dp, k, sl;
   uint64_t m;
   const float *sl_a;
   const uint32_t *sl_row;
@@ -71,18 +80,20 @@ struct RerankArgs {
 };
 
 // Upper bound on |approx(q, x) - exact(q, x)| for every row x of list r, where
-//   approx = fl(Dqr + fl(alpha D + w)),  alpha D ~ -2 q.x'  (tensor cores),
-//   Dqr ~ ||q - c||^2, w ~ ||x'||^2 + 2 c.x', x' = x - c,
-// and exact is the reference's sequential FP32 difference-form distance.
-// Inputs: Dqr (computed), qn = ||q||, X = bound on ||x'||, C = ||c||.
-// Terms, with u = 2^-24 and g = gamma_{d+3}:
-//   operand representation   eps_rep |q| |x'|           (BF16 rounding of
+//   approx = fl(Dqr + fl(alpha D + w)),  alpha D ~ -2 (q - mu).x'  (tensor cores),
+//   Dqr ~ ||q - c||^2, w ~ ||x'||^2 + 2 (c - mu).x', x' = x - c,
+// (mu = 0 in the exact format) and exact is the reference's sequential FP32
+// difference-form distance.  Inputs: Dqr (computed), qn = ||q - mu||,
+// X = bound on ||x'||, C = ||c - mu||.  Terms, with u = 2^-24, g = gamma_{d+3}:
+//   operand representation   eps_rep |q-mu| |x'|       (BF16 rounding of
 //                            inexact operands, or the hi/lo residuals)
-//   accumulation             nacc 2^-22 |q| |x'|        (twice the bound of
-//                            truncating FP32 accumulation of nacc products)
-//   centering                u |q| |x'|                 (x' rounded to FP32)
+//   accumulation             nacc 2^-22 |q-mu| |x'|    (twice the bound of
+//                            truncating FP32 accumulation of nacc products;
+//                            the split format's correction accumulator holds
+//                            terms 2^-10 smaller)
+//   centering                2u |q-mu| |x'|            (x', q - mu rounded)
 //   ||q-c||^2 and w          g (||q-c||^2 + ||x'||^2 + 2 C |x'|)
-//   two final roundings      u (||q-c||^2 + 2 (2|q||x'| + ||x'||^2 + 2C|x'|))
+//   three final roundings    u (||q-c||^2 + 3 (2|q-mu||x'| + ||x'||^2 + 2C|x'|))
 //   the exact distance       g (||q-c|| + |x'|)^2
 // doubled as a margin.
 __host__ __device__ inline float tc_error_bound(float Dqr, float qn, float X, float C, uint32_t q_inexact,
@@ -93,7 +104,7 @@ __host__ __device__ inline float tc_error_bound(float Dqr, float qn, float X, fl
   if (format == kTcSplit) {
     // hi = fl16(v), lo = fl16(v - hi): |v - hi - lo| <= 2^-22 |v|; lo.lo omitted <= 2^-22
     eps = 3.f * 2.384185791015625e-07f + d * 5.9604644775390625e-08f;  // + FP16 underflow margin
-    nacc = 3.f * d * 1.01f;
+    nacc = d * 1.01f;
   } else {
     const float b = 1.f / 256.f;
     const float bq = q_inexact ? b : 0.f, bx = x_inexact ? b : 0.f;
@@ -102,9 +113,9 @@ __host__ __device__ inline float tc_error_bound(float Dqr, float qn, float X, fl
   }
   const float qc2 = Dqr * (1.f + g), Q = qn * (1.f + g), Cb = C * (1.f + g);
   const float qx = Q * X;
-  const float A = 2.f * (eps + nacc * 2.384185791015625e-07f + u) * qx;
+  const float A = 2.f * (eps + nacc * 2.384185791015625e-07f + 2.f * u) * qx;
   const float B = g * (qc2 + X * X + 2.f * Cb * X);
-  const float R = u * (qc2 + 2.f * (2.f * qx + X * X + 2.f * Cb * X));
+  const float R = u * (qc2 + 3.f * (2.f * qx + X * X + 2.f * Cb * X));
   const float F = g * (sqrtf(qc2) + X) * (sqrtf(qc2) + X);
   // the float evaluation of this bound errs by far less than the final factor 2 covers
   return 2.f * (A + B + R + F) * (1.f + 1e-5f);
@@ -122,6 +133,7 @@ struct TcBuild {
   void *Xh;          // n_pad x cols halves (cols = kp, or 2 kp for the split format)
   float *w;          // n_pad + 128
   float *lscale, *lxmax, *lcnorm;  // nr each
+  float *mu;         // kp: the query centering vector (zero in the exact format)
   uint32_t format, x_inexact, cols;
 };
 int tc_build(const float *Xp, const uint64_t *offsets, const float *R, const float *radius, uint64_t n,
@@ -130,9 +142,10 @@ int tc_build(const float *Xp, const uint64_t *offsets, const float *R, const flo
 
 // Queries: half-precision operand rows (m rows + one zero row), scales, norms, flags.
 cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp, uint32_t format,
-                              void *Qh, float *qscale, float *qnorm, uint8_t *q_inexact, cudaStream_t s);
+                              const float *mu, void *Qh, float *qscale, float *qnorm, uint8_t *q_inexact,
+                              cudaStream_t s);
 cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
-                           uint32_t *emax, uint64_t m, cudaStream_t s);
+                           uint32_t *emax, uint64_t m, uint32_t sl, cudaStream_t s);
 cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
                              cudaStream_t s);
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s);

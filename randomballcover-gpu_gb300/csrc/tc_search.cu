@@ -15,7 +15,10 @@
 //   exact  every x' value is exact in BF16 (e.g. integer features): one
 //          BF16 x BF16 product; q in BF16 (exact for integer queries);
 //   split  FP16 hi + lo halves of power-of-two scaled values (per list for x',
-//          per query for q), three products hi.hi + hi.lo + lo.hi.
+//          per query for q - mu, mu the mean of the representatives; the
+//          identity then carries w = ||x'||^2 + 2 (c - mu).x'), three products:
+//          hi.hi into one tensor-memory accumulator, hi.lo + lo.hi into a
+//          second one, so the large accumulation runs over d terms only.
 // Each query keeps the SL = 40 rows of smallest approx (a shortlist of 4k for
 // k = 10).  The rerank computes their exact distances and sorts by
 // (distance, id).  |approx - exact| <= E(q) over every row searched, with E
@@ -29,9 +32,10 @@
 //   warp 0      TMA producer: the item's query rows gathered from the half-
 //               precision query matrix with tile::gather4 (128-byte swizzled,
 //               K-major), then 128-row B tiles of the item into a ring;
-//   warp 1      tcgen05.mma issuer: per B tile MT accumulators of 128 x 128
-//               in tensor memory (four 128-column slots), commits free the
-//               B stage and hand the slot to the epilogue;
+//   warp 1      tcgen05.mma issuer: per B tile MT x ACC accumulators of
+//               128 x 128 in tensor memory (512 columns hold 4 / (MT ACC)
+//               slots), commits free the B stage and hand the slot to the
+//               epilogue;
 //   warp 2      stages each B tile's row constants w into shared memory
 //               (cp.async; +inf past the item's rows, which masks them);
 //   warps 4-11  epilogue, two warpgroups (MT = 2: one per query tile; MT = 1:
@@ -48,6 +52,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 
 #include "engine.cuh"
 #include "sm100.cuh"
@@ -61,8 +67,7 @@ using namespace sm100;
 
 constexpr int kBM = 128, kBN = 128, kEpiGroups = 2;
 constexpr int kThreads = 128 + 128 * kEpiGroups;
-constexpr int kSL = kShortlist;
-constexpr int kLocal = 12, kLST = kLocal + 1;  // per-thread candidate buffer (odd stride: no bank conflicts)
+constexpr int kLocal = 8, kLST = kLocal + 1;  // per-thread candidate buffer (odd stride: no bank conflicts)
 constexpr uint32_t kTile16K = 16384;           // 128 rows x 128 bytes (one 64-wide K block of halves)
 constexpr uint32_t kLockSpin = 1u << 22;
 constexpr uint32_t kMaxA = 2, kMaxB = 4;
@@ -79,75 +84,84 @@ __device__ __forceinline__ float v_threshold(float theta, float dq) {
   return fminf(t, FLT_MAX);  // never +inf: masked columns carry v = +inf
 }
 
-// Merge a thread's sorted candidates into the query's global shortlist (the
-// current buffer is read, the merged list goes to the other buffer, then the
-// buffers swap), under the query's lock.  Returns the query's threshold.
-__device__ float publish(const TcArgs &a, uint32_t q, const float *myla, const uint32_t *myli, uint32_t nl) {
-  uint32_t spins = 0;
-  while (atomicCAS(a.sl_lock + q, 0u, 1u) != 0u) {
-    if (++spins > kLockSpin) {
-      raise_error(a.err, RBC_ERR_ITER_LIMIT);
-      return __uint_as_float(__ldcg(a.sl_theta + q));
-    }
-    __nanosleep(64);
-  }
-  __threadfence();
-  const uint32_t sel = __ldcg(a.sl_sel + q);
-  const float *ga = a.sl_a + ((uint64_t)sel * a.m + q) * kSL;
-  const uint32_t *gi = a.sl_row + ((uint64_t)sel * a.m + q) * kSL;
-  float *oa = a.sl_a + ((uint64_t)(sel ^ 1u) * a.m + q) * kSL;
-  uint32_t *oi = a.sl_row + ((uint64_t)(sel ^ 1u) * a.m + q) * kSL;
-  uint32_t i = 0, j = 0, t = 0;
-  float last = FLT_MAX;
-  float ca = __ldcg(ga);
-  uint32_t ci = __ldcg(gi);
-  for (; t < kSL; t++) {
-    const bool have_g = j < kSL && ci != RBC_DUMMY;
-    if (i >= nl && !have_g) break;
-    const bool take_local = !have_g || (i < nl && row_less(myla[i], myli[i], ca, ci));
-    if (take_local) {
-      oa[t] = last = myla[i];
-      oi[t] = myli[i];
-      i++;
-    } else {
-      oa[t] = last = ca;
-      oi[t] = ci;
-      j++;
-      if (j < kSL) {
-        ca = __ldcg(ga + j);
-        ci = __ldcg(gi + j);
+// Merge one lane's sorted candidates (nl <= kLocal entries at la/li in shared
+// memory) into query q's global shortlist, with the whole warp: the current
+// buffer (40 sorted entries) and the candidates form 64 (approx, row) pairs,
+// two per lane, which a bitonic network sorts; the 40 smallest go to the
+// other buffer, then the buffers swap, under the query's lock.  Called by all
+// 32 lanes with the same arguments; returns the query's new threshold.
+__device__ float warp_publish(const TcArgs &a, uint32_t q, const float *la, const uint32_t *li, uint32_t nl,
+                              uint32_t owner) {
+  const uint32_t lane = threadIdx.x & 31;
+  uint32_t got = 1;
+  if (lane == owner) {
+    uint32_t spins = 0;
+    while (atomicCAS(a.sl_lock + q, 0u, 1u) != 0u) {
+      if (++spins > kLockSpin) {
+        raise_error(a.err, RBC_ERR_ITER_LIMIT);
+        got = 0;
+        break;
       }
+      __nanosleep(64);
     }
+    __threadfence();
   }
+  got = __shfl_sync(0xffffffffu, got, owner);
+  __syncwarp();
+  if (!got) return __uint_as_float(__ldcg(a.sl_theta + q));
+  const uint32_t sel = __ldcg(a.sl_sel + q);
+  const uint32_t SL = a.sl, tail = SL - 32;  // entries past the first 32
+  const uint64_t cur = ((uint64_t)sel * a.m + q) * SL, nxt = ((uint64_t)(sel ^ 1u) * a.m + q) * SL;
+  float a0 = __ldcg(a.sl_a + cur + lane);
+  uint32_t i0 = __ldcg(a.sl_row + cur + lane);
+  float a1 = INFINITY;
+  uint32_t i1 = RBC_DUMMY;
+  if (lane < tail) {
+    a1 = __ldcg(a.sl_a + cur + 32 + lane);
+    i1 = __ldcg(a.sl_row + cur + 32 + lane);
+  } else if (lane - tail < nl) {
+    a1 = la[lane - tail];
+    i1 = li[lane - tail];
+  }
+  warp_sort32(a1, i1);  // the list's tail and the candidates, ascending
+  // bitonic merge of two ascending 32-lists: lower half = ranks 0..31
+  const float ra = __shfl_sync(0xffffffffu, a1, 31 - lane);
+  const uint32_t ri = __shfl_sync(0xffffffffu, i1, 31 - lane);
+  if (pair_less(ra, ri, a0, i0)) {
+    a1 = a0;
+    i1 = i0;
+    a0 = ra;
+    i0 = ri;
+  } else {
+    a1 = ra;
+    i1 = ri;
+  }
+  warp_bitonic_merge32(a0, i0);
+  warp_bitonic_merge32(a1, i1);
+  a.sl_a[nxt + lane] = a0;
+  a.sl_row[nxt + lane] = i0;
+  if (lane < tail) {
+    a.sl_a[nxt + 32 + lane] = a1;
+    a.sl_row[nxt + 32 + lane] = i1;
+  }
+  const float alast = __shfl_sync(0xffffffffu, a1, tail - 1);
+  const uint32_t ilast = __shfl_sync(0xffffffffu, i1, tail - 1);
   // FLT_MAX, not +inf, while the list is short
-  const float theta = t == kSL ? last : FLT_MAX;
-  for (; t < kSL; t++) {
-    oa[t] = INFINITY;
-    oi[t] = RBC_DUMMY;
-  }
-  a.sl_theta[q] = __float_as_uint(theta);
-  a.sl_sel[q] = sel ^ 1u;
+  const float theta = ilast != RBC_DUMMY ? alast : FLT_MAX;
   __threadfence();
-  atomicExch(a.sl_lock + q, 0u);
+  __syncwarp();
+  if (lane == owner) {
+    a.sl_theta[q] = __float_as_uint(theta);
+    a.sl_sel[q] = sel ^ 1u;
+    __threadfence();
+    atomicExch(a.sl_lock + q, 0u);
+  }
   return theta;
 }
 
-struct Cand {
-  uint32_t nl;
-  float thv;
-};
-
-// Sorted insertion of (dq + v, row) into a thread's candidate buffer; a full
-// buffer is first merged into the global shortlist, which tightens the filter.
-__device__ __noinline__ Cand insert_candidate(const TcArgs &a, uint32_t q, float *myla, uint32_t *myli, uint32_t nl,
-                                              float thv, float dq, float v, uint32_t row) {
-  if (nl == kLocal) {
-    thv = v_threshold(publish(a, q, myla, myli, nl), dq);
-    nl = 0;
-    if (!(v <= thv)) return Cand{nl, thv};
-  }
-  const float av = dq + v;
-  int pos = (int)nl++;
+// Sorted insertion of (av, row) into a lane's candidate buffer (nl < kLocal).
+__device__ __noinline__ uint32_t insert_local(float *myla, uint32_t *myli, uint32_t nl, float av, uint32_t row) {
+  int pos = (int)nl;
   while (pos > 0 && row_less(av, row, myla[pos - 1], myli[pos - 1])) {
     myla[pos] = myla[pos - 1];
     myli[pos] = myli[pos - 1];
@@ -155,8 +169,14 @@ __device__ __noinline__ Cand insert_candidate(const TcArgs &a, uint32_t q, float
   }
   myla[pos] = av;
   myli[pos] = row;
-  return Cand{nl, thv};
+  return nl + 1;
 }
+
+// Per-item state of one query row, staged by warp 3 for the epilogue.
+struct RowState {
+  uint32_t q;
+  float dq, thv, alpha;
+};
 
 __device__ const float g_inf = INFINITY;
 
@@ -174,10 +194,11 @@ template <int MT, bool SPLIT>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const __grid_constant__ TcArgs a) {
-  constexpr uint32_t NSLOT = 4 / MT;  // tensor-memory slots of MT x 128 columns
+  constexpr uint32_t ACC = SPLIT ? 2 : 1;     // accumulators per query tile: hi.hi (+ corrections)
+  constexpr uint32_t NSLOT = 4 / (MT * ACC);  // tensor-memory slots of MT x ACC x 128 columns
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_a_full[kMaxA], bar_a_empty[kMaxA], bar_b_full[kMaxB], bar_b_empty[kMaxB],
-      bar_t_full[4], bar_t_empty[4], bar_x_full[4];
+      bar_t_full[4], bar_t_empty[4], bar_x_full[4], bar_r_full[2], bar_r_empty[2];
   __shared__ uint32_t tmem_slot;
 
   unsigned char *base =
@@ -188,7 +209,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char *sA = base;
   unsigned char *sB = sA + AS * a_stage;
   float *xs = reinterpret_cast<float *>(sB + BS * b_stage);  // NSLOT x 128 row constants
-  float *la = xs + NSLOT * kBN;                                // per epilogue thread: kLST approx
+  RowState *rs = reinterpret_cast<RowState *>(xs + NSLOT * kBN);  // 2 x 256 staged row states
+  float *la = reinterpret_cast<float *>(rs + 2 * 2 * kBM);       // per epilogue thread: kLST approx
   uint32_t *li = reinterpret_cast<uint32_t *>(la + kEpiGroups * kBM * kLST);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -210,6 +232,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&bar_t_empty[b], MT == 2 ? 8 : 4);
       mbar_init(&bar_x_full[b], 32);
     }
+    for (uint32_t b = 0; b < 2; b++) {
+      mbar_init(&bar_r_full[b], 1);
+      mbar_init(&bar_r_empty[b], 8);
+    }
     fence_barrier_init();
   }
   tc_fence_before();
@@ -219,41 +245,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t nitems = *a.nitems;
 
   if (warp == 0) {
-    // ------------------------------------------------ TMA producer
+    // ------------------------------------------------ TMA producer of the B tiles
     if (lane == 0) {
-      prefetch_tensormap(&tmA);
       prefetch_tensormap(&tmB);
-    }
-    uint32_t ai = 0, bi = 0;
-    unsigned long long pairs = 0, lists = 0;
-    bool ok = true;
-    for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
-      const SearchItem item = a.items[it];
-      const uint32_t sa = ai % AS;
-      if (ai >= AS) ok = mbar_wait(&bar_a_empty[sa], ((ai / AS) - 1) & 1, a.err);
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) break;
-      if (lane == 0) mbar_expect_tx(&bar_a_full[sa], a_stage);
-      __syncwarp();
-      unsigned char *dA = sA + sa * a_stage;
-#pragma unroll
-      for (int g = 0; g < MT; g++) {
-        int32_t rr[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const uint32_t slot = g * kBM + 4 * lane + j;
-          rr[j] = (int32_t)(slot < item.nq ? a.qidx[item.q0 + slot] : a.zero_row);
-        }
-        for (uint32_t k = 0; k < kbh; k++)
-          tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[0], rr[1], rr[2],
-                      rr[3], &bar_a_full[sa]);
-      }
-      const uint32_t ntiles = (item.np + kBN - 1) / kBN;
-      if (lane == 0) {
+      uint32_t bi = 0;
+      unsigned long long pairs = 0, lists = 0;
+      bool ok = true;
+      for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+        const SearchItem item = a.items[it];
+        const uint32_t ntiles = (item.np + kBN - 1) / kBN;
         pairs += (unsigned long long)item.nq * item.np;
         if (a.offsets && item.p0 == a.offsets[item.list]) lists += item.nq;
-        for (uint32_t t = 0; t < ntiles; t++) {
-          const uint32_t b = bi + t, sb = b % BS, use = b / BS;
+        for (uint32_t t = 0; t < ntiles; t++, bi++) {
+          const uint32_t sb = bi % BS, use = bi / BS;
           if (use > 0 && !(ok = mbar_wait(&bar_b_empty[sb], (use - 1) & 1, a.err))) break;
           mbar_expect_tx(&bar_b_full[sb], b_stage);
           const int32_t row = (int32_t)(item.p0 + (uint64_t)t * kBN);
@@ -261,18 +265,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             tma_load_2d(sB + sb * b_stage + k * kTile16K, &tmB, (int32_t)(k * 64), row, &bar_b_full[sb]);
         }
       }
-      bi += ntiles;
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-    }
-    if (lane == 0) {
       // drain: wait (bounded) for the copies still in flight before leaving
       for (uint32_t j = 0; j < BS && j < bi; j++) {
         const uint32_t b = bi - 1 - j;
         mbar_wait(&bar_b_full[b % BS], (b / BS) & 1, nullptr);
-      }
-      for (uint32_t j = 0; j < AS && j < ai; j++) {
-        const uint32_t i = ai - 1 - j;
-        mbar_wait(&bar_a_full[i % AS], (i / AS) & 1, nullptr);
       }
       if (a.stats && pairs) {
         atomicAdd(a.stats, pairs);
@@ -298,17 +294,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t b0 = smem_u32(sB + sb * b_stage);
 #pragma unroll
           for (int g = 0; g < MT; g++) {
-            const uint32_t d = tmem + (slot * MT + g) * kBN;
+            const uint32_t d = tmem + (slot * MT + g) * ACC * kBN;
             const uint32_t a0 = smem_u32(sA + sa * a_stage + g * a_tile);
             for (uint32_t k = 0; k < kb; k++) {
 #pragma unroll
               for (uint32_t kk = 0; kk < 4; kk++) {
                 const uint32_t off = k * kTile16K + kk * 32;
-                mma_bf16(d, sw128_desc(a0 + off), sw128_desc(b0 + off), idesc, (k | kk) != 0);
+                const uint32_t acc = (k | kk) != 0;
+                mma_bf16(d, sw128_desc(a0 + off), sw128_desc(b0 + off), idesc, acc);
                 if (SPLIT) {
                   const uint32_t lo = kb * kTile16K;
-                  mma_bf16(d, sw128_desc(a0 + off), sw128_desc(b0 + lo + off), idesc, 1);
-                  mma_bf16(d, sw128_desc(a0 + lo + off), sw128_desc(b0 + off), idesc, 1);
+                  mma_bf16(d + kBN, sw128_desc(a0 + off), sw128_desc(b0 + lo + off), idesc, acc);
+                  mma_bf16(d + kBN, sw128_desc(a0 + lo + off), sw128_desc(b0 + off), idesc, 1);
                 }
               }
             }
@@ -343,74 +340,179 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
     cp_async_wait_all();
+  } else if (warp == 3) {
+    // ------------------------------------------------ per item: row states and the query tile gather
+    if (lane == 0) prefetch_tensormap(&tmA);
+    uint32_t ai = 0;
+    bool ok = true;
+    for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
+      const SearchItem item = a.items[it];
+      const uint32_t slot = ai & 1, sa = ai % AS;
+      if (ai >= 2) ok = mbar_wait(&bar_r_empty[slot], ((ai >> 1) - 1) & 1, a.err);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      // lane l owns rows 4l..4l+3 of each query tile (one gather4 per tile and K block)
+      int32_t rr[MT][4];
+      RowState *dst = rs + slot * 2 * kBM;
+      const float ls = SPLIT ? a.lscale[item.list] : 1.f;
+      const float X = a.lxmax[item.list], C = a.lcnorm[item.list];
+#pragma unroll
+      for (int g = 0; g < MT; g++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const uint32_t row = g * kBM + 4 * lane + j;
+          RowState st{0u, 0.f, -FLT_MAX, -2.f};  // rows past the item's queries: no value passes
+          rr[g][j] = (int32_t)a.zero_row;
+          if (row < item.nq) {
+            const uint32_t q = a.qidx[item.q0 + row];
+            const float dq = a.Dqr[(uint64_t)q * a.nr + item.list];
+            rr[g][j] = (int32_t)q;
+            st.q = q;
+            st.dq = dq;
+            st.thv = v_threshold(__uint_as_float(__ldcg(a.sl_theta + q)), dq);
+            if (SPLIT) st.alpha = -2.f / (a.qscale[q] * ls);
+            const float E = tc_error_bound(dq, a.qnorm[q], X, C, a.q_inexact ? a.q_inexact[q] : 1u, a.x_inexact,
+                                           a.format, a.d);
+            atomicMax(a.emax + q, __float_as_uint(E));
+          }
+          dst[row] = st;
+        }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bar_r_full[slot]);
+      if (ai >= AS) ok = mbar_wait(&bar_a_empty[sa], ((ai / AS) - 1) & 1, a.err);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      if (lane == 0) mbar_expect_tx(&bar_a_full[sa], a_stage);
+      __syncwarp();
+      unsigned char *dA = sA + sa * a_stage;
+#pragma unroll
+      for (int g = 0; g < MT; g++)
+        for (uint32_t k = 0; k < kbh; k++)
+          tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
+                      rr[g][2], rr[g][3], &bar_a_full[sa]);
+    }
+    if (lane == 0) {
+      // drain: wait (bounded) for the gathers still in flight before leaving
+      for (uint32_t j = 0; j < AS && j < ai; j++) {
+        const uint32_t i = ai - 1 - j;
+        mbar_wait(&bar_a_full[i % AS], (i / AS) & 1, nullptr);
+      }
+    }
   } else if (warp >= 4) {
     // ------------------------------------------------ epilogue (two warpgroups)
     const uint32_t grp = (warp - 4) >> 2, ew = warp & 3, et = ew * 32 + lane;
-    float *myla = la + (grp * kBM + et) * kLST;
-    uint32_t *myli = li + (grp * kBM + et) * kLST;
+    float *wla = la + (grp * kBM + ew * 32) * kLST;  // this warp's candidate buffers
+    uint32_t *wli = li + (grp * kBM + ew * 32) * kLST;
+    float *myla = wla + lane * kLST;
+    uint32_t *myli = wli + lane * kLST;
     const uint32_t arow = (MT == 2 ? grp * kBM : 0) + et;  // this thread's row of the item's query tiles
-    uint32_t bi = 0;
+    uint32_t ai = 0, bi = 0;
     bool ok = true;
-    for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+    // merge the buffers of the lanes in `need` into their queries' shortlists
+    auto flush = [&](uint32_t need, uint32_t q, uint32_t &nl, float &thv, float dq) {
+      while (need) {
+        const uint32_t l = __ffs(need) - 1;
+        need &= need - 1;
+        const float th = warp_publish(a, __shfl_sync(0xffffffffu, q, l), wla + l * kLST, wli + l * kLST,
+                                      __shfl_sync(0xffffffffu, nl, l), l);
+        if (lane == l) {
+          nl = 0;
+          thv = v_threshold(th, dq);
+        }
+      }
+    };
+    for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
       const SearchItem item = a.items[it];
       const uint32_t ntiles = (item.np + kBN - 1) / kBN;
-      const bool valid = arow < item.nq;
-      bool have = false;
-      uint32_t q = 0, nl = 0;
-      // rows past the item's queries keep a threshold no value passes
-      float dq = 0.f, alpha = -2.f, thv = -FLT_MAX;
-      for (uint32_t t = 0; t < ntiles; t++, bi++) {
+      const uint32_t rslot = ai & 1;
+      if (!(ok = mbar_wait(&bar_r_full[rslot], (ai >> 1) & 1, a.err))) break;
+      const RowState st = rs[rslot * 2 * kBM + arow];
+      const uint32_t q = st.q;
+      const float dq = st.dq, alpha = st.alpha;
+      float thv = st.thv;
+      uint32_t nl = 0;
+      for (uint32_t t = 0; t < ntiles && ok; t++, bi++) {
         if (MT == 1 && (bi & 1u) != grp) continue;
         const uint32_t slot = bi % NSLOT;
-        if (!have && valid) {
-          q = a.qidx[item.q0 + arow];
-          dq = a.Dqr[(uint64_t)q * a.nr + item.list];
-          thv = v_threshold(__uint_as_float(__ldcg(a.sl_theta + q)), dq);
-          if (SPLIT) alpha = -2.f / (a.qscale[q] * a.lscale[item.list]);
-          const float E = tc_error_bound(dq, a.qnorm[q], a.lxmax[item.list], a.lcnorm[item.list],
-                                         a.q_inexact ? a.q_inexact[q] : 1u, a.x_inexact, a.format, a.d);
-          atomicMax(a.emax + q, __float_as_uint(E));
-        }
-        have = true;
         if (!(ok = mbar_wait(&bar_t_full[slot], (bi / NSLOT) & 1, a.err))) break;
         if (!(ok = mbar_wait(&bar_x_full[slot], (bi / NSLOT) & 1, a.err))) break;
         tc_fence_after();
         const float *xr = xs + slot * kBN;
-        const uint32_t taddr = tmem + ((32u * ew) << 16) + (slot * MT + (MT == 2 ? grp : 0)) * kBN;
-        const uint64_t p = item.p0 + (uint64_t)t * kBN;
-#pragma unroll 1
-        for (uint32_t c = 0; c < kBN / 32; c++) {
-          uint32_t r[32];
-          __syncwarp();
-          tmem_ld32(taddr + c * 32, r);
-          tmem_wait_ld();
+        const uint32_t taddr = tmem + ((32u * ew) << 16) + (slot * MT + (MT == 2 ? grp : 0)) * ACC * kBN;
+        const uint32_t p = (uint32_t)(item.p0 + (uint64_t)t * kBN);
+        // one 32-column chunk of the accumulator(s): approx, filter, candidates
+        auto chunk = [&](const uint32_t(&r)[32], const uint32_t(&r2)[SPLIT ? 32 : 1], uint32_t c) {
           float v[32];
           float mn = INFINITY;
 #pragma unroll
           for (int j4 = 0; j4 < 8; j4++) {
             const float4 x4 = *reinterpret_cast<const float4 *>(xr + c * 32 + 4 * j4);
-            v[4 * j4 + 0] = fmaf(alpha, __uint_as_float(r[4 * j4 + 0]), x4.x);
-            v[4 * j4 + 1] = fmaf(alpha, __uint_as_float(r[4 * j4 + 1]), x4.y);
-            v[4 * j4 + 2] = fmaf(alpha, __uint_as_float(r[4 * j4 + 2]), x4.z);
-            v[4 * j4 + 3] = fmaf(alpha, __uint_as_float(r[4 * j4 + 3]), x4.w);
+            const float xw[4] = {x4.x, x4.y, x4.z, x4.w};
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+              float tv = fmaf(alpha, __uint_as_float(r[4 * j4 + e]), xw[e]);
+              if (SPLIT) tv = fmaf(alpha, __uint_as_float(r2[(4 * j4 + e) % (SPLIT ? 32 : 1)]), tv);
+              v[4 * j4 + e] = tv;
+            }
             mn = fminf(mn, fminf(fminf(v[4 * j4], v[4 * j4 + 1]), fminf(v[4 * j4 + 2], v[4 * j4 + 3])));
           }
-          if (mn <= thv) {
+          if (!__any_sync(0xffffffffu, mn <= thv)) return;
+          // candidates: into the lane's buffer; full buffers are merged by the
+          // warp, which tightens the filter, until none are left
+          uint32_t pend = 0;
+#pragma unroll
+          for (int e = 0; e < 32; e++) pend |= (uint32_t)(v[e] <= thv) << e;
+          while (__any_sync(0xffffffffu, pend != 0)) {
 #pragma unroll
             for (int e = 0; e < 32; e++) {
-              if (v[e] <= thv) {
-                const Cand cs = insert_candidate(a, q, myla, myli, nl, thv, dq, v[e], (uint32_t)(p + c * 32 + e));
-                nl = cs.nl;
-                thv = cs.thv;
+              if (((pend >> e) & 1u) && nl < (uint32_t)kLocal) {
+                nl = insert_local(myla, myli, nl, dq + v[e], p + c * 32 + e);
+                pend &= ~(1u << e);
               }
             }
+            flush(__ballot_sync(0xffffffffu, pend != 0), q, nl, thv, dq);
+#pragma unroll
+            for (int e = 0; e < 32; e++)
+              if (!(v[e] <= thv)) pend &= ~(1u << e);
+          }
+        };
+        if (!SPLIT) {
+          // tensor-memory loads double-buffered: chunk c + 1 is in flight while c is processed
+          uint32_t ra[32], rb[32], nil[SPLIT ? 32 : 1];
+          __syncwarp();
+          tmem_ld32(taddr, ra);
+          tmem_wait_ld();
+#pragma unroll
+          for (uint32_t c = 0; c < kBN / 32; c += 2) {
+            __syncwarp();
+            tmem_ld32(taddr + (c + 1) * 32, rb);
+            chunk(ra, nil, c);
+            tmem_wait_ld();
+            if (c + 2 < kBN / 32) {
+              __syncwarp();
+              tmem_ld32(taddr + (c + 2) * 32, ra);
+            }
+            chunk(rb, nil, c + 1);
+            tmem_wait_ld();
+          }
+        } else {
+#pragma unroll 1
+          for (uint32_t c = 0; c < kBN / 32; c++) {
+            uint32_t r[32], r2[SPLIT ? 32 : 1];
+            __syncwarp();
+            tmem_ld32(taddr + c * 32, r);
+            tmem_ld32(taddr + kBN + c * 32, *reinterpret_cast<uint32_t(*)[32]>(r2));
+            tmem_wait_ld();
+            chunk(r, r2, c);
           }
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&bar_t_empty[slot]);
       }
-      if (valid && nl > 0) publish(a, q, myla, myli, nl);
+      flush(__ballot_sync(0xffffffffu, nl > 0), q, nl, thv, dq);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bar_r_empty[rslot]);
     }
   }
   tc_fence_before();
@@ -442,62 +544,73 @@ __device__ __forceinline__ float half_scale(float maxabs) {
   return ldexpf(1.f, e);
 }
 
-// One warp per row: x' = x - c (FP32), w = ||x'||^2 + 2 c.x', the BF16
-// exactness flag and the largest |x'_i| of the list.
+// One warp per row: whether every x' = x - c (FP32) value is exact in BF16,
+// and the largest |x'_i| of the list.
 __global__ void tc_center_kernel(const float *__restrict__ Xp, uint32_t ld, const uint64_t *__restrict__ off,
                                  uint32_t nr, const float *__restrict__ R, uint64_t n, uint32_t d,
-                                 float *__restrict__ w, uint32_t *__restrict__ inexact,
-                                 uint32_t *__restrict__ lmax_bits) {
+                                 uint32_t *__restrict__ inexact, uint32_t *__restrict__ lmax_bits) {
   const uint64_t p = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31;
   if (p >= n) return;
   const uint32_t r = list_of(off, nr, p);
   const float *x = Xp + p * ld, *c = R + (uint64_t)r * ld;
-  float sxx = 0.f, scx = 0.f, mx = 0.f;
+  float mx = 0.f;
   uint32_t bad = 0;
   for (uint32_t i = lane; i < d; i += 32) {
     const float v = __fsub_rn(x[i], c[i]);
     bad |= __bfloat162float(__float2bfloat16_rn(v)) != v;
-    sxx = fmaf(v, v, sxx);
-    scx = fmaf(c[i], v, scx);
     mx = fmaxf(mx, fabsf(v));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    sxx += __shfl_xor_sync(0xffffffffu, sxx, o);
-    scx += __shfl_xor_sync(0xffffffffu, scx, o);
     mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     bad |= __shfl_xor_sync(0xffffffffu, bad, o);
   }
   if (lane == 0) {
-    w[p] = sxx + 2.f * scx;
     if (bad) atomicOr(inexact, 1u);
     atomicMax(lmax_bits + r, __float_as_uint(mx));
   }
 }
 
+// mu: the mean of the representatives per coordinate (split format; zero in
+// the exact format, whose operands must stay exact), zero past d.
+__global__ void tc_mu_kernel(const float *__restrict__ R, uint32_t ld, uint32_t nr, uint32_t d, uint32_t kp,
+                             uint32_t format, float *__restrict__ mu) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kp) return;
+  double s = 0.0;
+  if (format == kTcSplit && i < d)
+    for (uint32_t r = 0; r < nr; r++) s += R[(uint64_t)r * ld + i];
+  mu[i] = (float)(s / nr);
+}
+
 // Per list: the operand scale, a bound on ||x'|| from the list radius (the
-// largest member distance, relative error <= gamma_{d+1}) and ||c||.
+// largest member distance, relative error <= gamma_{d+1}) and ||c - mu||.
 __global__ void tc_list_params_kernel(const float *__restrict__ R, uint32_t ld, uint32_t nr, uint32_t d,
                                       const float *__restrict__ radius, const uint32_t *__restrict__ lmax_bits,
-                                      uint32_t format, float *__restrict__ lscale, float *__restrict__ lxmax,
-                                      float *__restrict__ lcnorm) {
+                                      const float *__restrict__ mu, uint32_t format, float *__restrict__ lscale,
+                                      float *__restrict__ lxmax, float *__restrict__ lcnorm) {
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nr) return;
   const double u = 5.9604644775390625e-08, g = (d + 3) * u / (1.0 - (d + 3) * u);
   lscale[r] = format == kTcSplit ? half_scale(__uint_as_float(lmax_bits[r])) : 1.f;
   lxmax[r] = __double2float_ru(sqrt((double)radius[r] / (1.0 - g)) * (1.0 + g));
   double cc = 0.0;
-  for (uint32_t i = 0; i < d; i++) cc += (double)R[(uint64_t)r * ld + i] * R[(uint64_t)r * ld + i];
-  lcnorm[r] = __double2float_ru(sqrt(cc));
+  for (uint32_t i = 0; i < d; i++) {
+    const double t = (double)R[(uint64_t)r * ld + i] - (double)mu[i];
+    cc += t * t;
+  }
+  lcnorm[r] = __double2float_ru(sqrt(cc) * (1.0 + 4.0 * u));
 }
 
 // One warp per row of the padded operand: BF16 x' (exact format) or FP16
-// hi | lo of s_r x' (split format); rows past n are zero.
+// hi | lo of s_r x' (split format), and w = ||x'||^2 + 2 (c - mu).x'; rows
+// past n are zero.
 __global__ void tc_convert_kernel(const float *__restrict__ Xp, uint32_t ld, const uint64_t *__restrict__ off,
-                                  uint32_t nr, const float *__restrict__ R, uint64_t n, uint64_t n_pad, uint32_t d,
-                                  uint32_t kp, uint32_t format, const float *__restrict__ lscale,
-                                  uint16_t *__restrict__ Xh) {
+                                  uint32_t nr, const float *__restrict__ R, const float *__restrict__ mu, uint64_t n,
+                                  uint64_t n_pad, uint32_t d, uint32_t kp, uint32_t format,
+                                  const float *__restrict__ lscale, uint16_t *__restrict__ Xh,
+                                  float *__restrict__ w) {
   const uint64_t p = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31;
   if (p >= n_pad) return;
@@ -510,8 +623,13 @@ __global__ void tc_convert_kernel(const float *__restrict__ Xp, uint32_t ld, con
   const uint32_t r = list_of(off, nr, p);
   const float *x = Xp + p * ld, *c = R + (uint64_t)r * ld;
   const float s = lscale[r];
+  float sxx = 0.f, scx = 0.f;
   for (uint32_t i = lane; i < kp; i += 32) {
     const float v = i < d ? __fsub_rn(x[i], c[i]) : 0.f;
+    if (i < d) {
+      sxx = fmaf(v, v, sxx);
+      scx = fmaf(c[i] - mu[i], v, scx);
+    }
     if (format == kTcSplit) {
       const float sv = v * s;
       const __half hi = __float2half_rn(sv);
@@ -522,13 +640,19 @@ __global__ void tc_convert_kernel(const float *__restrict__ Xp, uint32_t ld, con
       dst[i] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
     }
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sxx += __shfl_xor_sync(0xffffffffu, sxx, o);
+    scx += __shfl_xor_sync(0xffffffffu, scx, o);
+  }
+  if (lane == 0) w[p] = sxx + 2.f * scx;
 }
 
-// One warp per query row (row m is the zero row): the operand row, its scale,
-// ||q|| and whether some value is not exact in BF16.
+// One warp per query row (row m is the zero row): the operand row of q - mu,
+// its scale, ||q - mu|| and whether some value is not exact in BF16.
 __global__ void tc_query_kernel(const float *__restrict__ Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp,
-                                uint32_t format, uint16_t *__restrict__ Qh, float *__restrict__ qscale,
-                                float *__restrict__ qnorm, uint8_t *__restrict__ qinex) {
+                                uint32_t format, const float *__restrict__ mu, uint16_t *__restrict__ Qh,
+                                float *__restrict__ qscale, float *__restrict__ qnorm, uint8_t *__restrict__ qinex) {
   const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31;
   if (q > m) return;
@@ -542,7 +666,7 @@ __global__ void tc_query_kernel(const float *__restrict__ Q, uint32_t ld, uint64
   float ss = 0.f, mx = 0.f;
   uint32_t bad = 0;
   for (uint32_t i = lane; i < d; i += 32) {
-    const float v = x[i];
+    const float v = __fsub_rn(x[i], mu[i]);
     ss = fmaf(v, v, ss);
     mx = fmaxf(mx, fabsf(v));
     bad |= __bfloat162float(__float2bfloat16_rn(v)) != v;
@@ -555,7 +679,7 @@ __global__ void tc_query_kernel(const float *__restrict__ Q, uint32_t ld, uint64
   }
   const float t = format == kTcSplit ? half_scale(mx) : 1.f;
   for (uint32_t i = lane; i < kp; i += 32) {
-    const float v = i < d ? x[i] : 0.f;
+    const float v = i < d ? __fsub_rn(x[i], mu[i]) : 0.f;
     if (format == kTcSplit) {
       const float sv = v * t;
       const __half hi = __float2half_rn(sv);
@@ -576,9 +700,9 @@ __global__ void tc_query_kernel(const float *__restrict__ Q, uint32_t ld, uint64
 // Both shortlist buffers empty, buffer 0 current, thresholds open, locks free,
 // error bounds zero.
 __global__ void sl_init_kernel(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
-                               uint32_t *emax, uint64_t m) {
+                               uint32_t *emax, uint64_t m, uint32_t sl) {
   uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (i < 2 * m * kSL) {
+  if (i < 2 * m * sl) {
     sl_a[i] = INFINITY;
     sl_row[i] = RBC_DUMMY;
   }
@@ -598,7 +722,7 @@ __global__ void rerank_kernel(RerankArgs a) {
   const int lane = threadIdx.x & 31;
   if (q >= a.m) return;
   const float *qrow = a.Q + q * a.ld;
-  const uint64_t slot = ((uint64_t)a.sl_sel[q] * a.m + q) * kSL;
+  const uint64_t slot = ((uint64_t)a.sl_sel[q] * a.m + q) * a.sl;
   const float *sa_q = a.sl_a + slot;
   const uint32_t *sr_q = a.sl_row + slot;
   float ld = FLT_MAX, cd = FLT_MAX;
@@ -608,7 +732,7 @@ __global__ void rerank_kernel(RerankArgs a) {
     const int t = round * 32 + lane;
     float dv = FLT_MAX;
     uint32_t id = RBC_DUMMY;
-    if (t < kSL) {
+    if (t < (int)a.sl) {
       const uint32_t row = sr_q[t];
       if (row != RBC_DUMMY) {
         const float *xr = a.X + (uint64_t)row * a.ld;
@@ -642,8 +766,8 @@ __global__ void rerank_kernel(RerankArgs a) {
   // certificate: every row searched but not in the shortlist has approx >=
   // a_last, so its exact distance is >= a_last - E > kth when certified
   bool certified = true;
-  if (valid == kSL) {
-    const double a_last = (double)sa_q[kSL - 1];
+  if (valid == a.sl) {
+    const double a_last = (double)sa_q[a.sl - 1];
     const double E = (double)__uint_as_float(a.emax[q]);
     certified = a_last - E > (double)kth;
   }
@@ -662,21 +786,33 @@ PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 template <int MT, bool SPLIT>
 size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs) {
   const size_t kbh = SPLIT ? 2 * kb : kb;
-  return 1024 + (size_t)as * MT * kbh * kTile16K + (size_t)bs * kbh * kTile16K + (size_t)(4 / MT) * kBN * 4 +
-         (size_t)kEpiGroups * kBM * kLST * 8;
+  const size_t nslot = 4 / (MT * (SPLIT ? 2 : 1));
+  return 1024 + (size_t)as * MT * kbh * kTile16K + (size_t)bs * kbh * kTile16K + nslot * kBN * 4 +
+         2 * 2 * kBM * sizeof(RowState) + (size_t)kEpiGroups * kBM * kLST * 8;
 }
 
 template <int MT, bool SPLIT>
 cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s) {
-  uint32_t as = kMaxA, bs = kMaxB;
-  while (smem_bytes<MT, SPLIT>(a.kb, as, bs) > kSmemLimit) {
-    if (bs > 2)
-      bs--;
-    else if (as > 1)
-      as--;
-    else
-      return cudaErrorInvalidConfiguration;
+  // deepest pipeline that fits: B depth first (it hides the L2 latency of
+  // every tile), then a second query stage (it hides the gather at item starts)
+  static const uint32_t pref[][2] = {{2, 4}, {2, 3}, {1, 4}, {1, 3}, {2, 2}, {1, 2}};
+  uint32_t as = 0, bs = 0;
+  for (const auto &c : pref)
+    if (smem_bytes<MT, SPLIT>(a.kb, c[0], c[1]) <= kSmemLimit) {
+      as = c[0];
+      bs = c[1];
+      break;
+    }
+  // RBC_TC_STAGES="a,b" overrides the choice (tuning experiments) when it fits
+  if (const char *env = std::getenv("RBC_TC_STAGES")) {
+    unsigned ea = 0, eb = 0;
+    if (std::sscanf(env, "%u,%u", &ea, &eb) == 2 && ea >= 1 && ea <= kMaxA && eb >= 2 && eb <= kMaxB &&
+        smem_bytes<MT, SPLIT>(a.kb, ea, eb) <= kSmemLimit) {
+      as = ea;
+      bs = eb;
+    }
   }
+  if (!as) return cudaErrorInvalidConfiguration;
   a.a_stages = as;
   a.b_stages = bs;
   const size_t smem = smem_bytes<MT, SPLIT>(a.kb, as, bs);
@@ -727,7 +863,7 @@ int tc_build(const float *Xp, const uint64_t *offsets, const float *R, const flo
   if (e == cudaSuccess) e = cudaMemsetAsync(t.w, 0, (n_pad + kBN) * 4, s);
   if (e != cudaSuccess) return cuda_fail(e, "rbc_build: tensor-form buffers");
   const unsigned grid_n = (unsigned)((n * 32 + 255) / 256);
-  tc_center_kernel<<<grid_n, 256, 0, s>>>(Xp, ld, offsets, nr, R, n, d, t.w, fl.as<uint32_t>(), lmax.as<uint32_t>());
+  tc_center_kernel<<<grid_n, 256, 0, s>>>(Xp, ld, offsets, nr, R, n, d, fl.as<uint32_t>(), lmax.as<uint32_t>());
   if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: centering");
   uint32_t inexact = 0;
   if ((e = cudaMemcpyAsync(&inexact, fl.p, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
@@ -741,30 +877,34 @@ int tc_build(const float *Xp, const uint64_t *offsets, const float *R, const flo
   if (e == cudaSuccess) e = cudaMalloc(&t.lscale, nr * 4);
   if (e == cudaSuccess) e = cudaMalloc(&t.lxmax, nr * 4);
   if (e == cudaSuccess) e = cudaMalloc(&t.lcnorm, nr * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&t.mu, kp * 4);
   if (e != cudaSuccess) return cuda_fail(e, "rbc_build: tensor-form operands");
-  *bytes += xh_bytes + (n_pad + kBN) * 4 + 3ull * nr * 4;
-  tc_list_params_kernel<<<(nr + 127) / 128, 128, 0, s>>>(R, ld, nr, d, radius, lmax.as<uint32_t>(), t.format,
+  *bytes += xh_bytes + (n_pad + kBN) * 4 + 3ull * nr * 4 + kp * 4;
+  tc_mu_kernel<<<(kp + 127) / 128, 128, 0, s>>>(R, ld, nr, d, kp, t.format, t.mu);
+  if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: centering vector");
+  tc_list_params_kernel<<<(nr + 127) / 128, 128, 0, s>>>(R, ld, nr, d, radius, lmax.as<uint32_t>(), t.mu, t.format,
                                                         t.lscale, t.lxmax, t.lcnorm);
   if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: list parameters");
   tc_convert_kernel<<<(unsigned)((n_pad * 32 + 255) / 256), 256, 0, s>>>(
-      Xp, ld, offsets, nr, R, n, n_pad, d, kp, t.format, t.lscale, static_cast<uint16_t *>(t.Xh));
+      Xp, ld, offsets, nr, R, t.mu, n, n_pad, d, kp, t.format, t.lscale, static_cast<uint16_t *>(t.Xh), t.w);
   if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: operand rows");
   return RBC_OK;
 }
 
 cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp, uint32_t format,
-                              void *Qh, float *qscale, float *qnorm, uint8_t *q_inexact, cudaStream_t s) {
+                              const float *mu, void *Qh, float *qscale, float *qnorm, uint8_t *q_inexact,
+                              cudaStream_t s) {
   const uint64_t threads = (m + 1) * 32;
-  tc_query_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(Q, ld, m, d, kp, format,
+  tc_query_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(Q, ld, m, d, kp, format, mu,
                                                                     static_cast<uint16_t *>(Qh), qscale, qnorm,
                                                                     q_inexact);
   return launched();
 }
 
 cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
-                           uint32_t *emax, uint64_t m, cudaStream_t s) {
-  const uint64_t total = std::max<uint64_t>(2 * m * kSL, 1);
-  sl_init_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sl_a, sl_row, sel, theta, lock, emax, m);
+                           uint32_t *emax, uint64_t m, uint32_t sl, cudaStream_t s) {
+  const uint64_t total = std::max<uint64_t>(2 * m * sl, 1);
+  sl_init_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(sl_a, sl_row, sel, theta, lock, emax, m, sl);
   return launched();
 }
 
