@@ -160,6 +160,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(v, dist, device):
+    """The largest of every rank's v (v itself without a process group)."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(per_rank_units, steps, world, slowest_ms):
+    """Whole-job rate of N independent replicas: every rank's units over the
+    slowest rank's time (weak scaling: each rank holds the full per-GPU work)."""
+    return world * per_rank_units * steps / (slowest_ms / 1000.0)
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -309,11 +325,7 @@ def run_engine(a):
         torch.cuda.synchronize()
 
     def maxall(v):
-        if not dist:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(v, dist, "cuda")
 
     stream = torch.cuda.current_stream()
     synth = dict(ncomp=w["ncomp"], sigma_lo=w["slo"], sigma_hi=w["shi"])
@@ -383,7 +395,7 @@ def run_engine(a):
         acc["clocks"] = clocks.stop() if clocks else None
         acc["ms"] = maxall(ev0.elapsed_time(ev1))
         acc["steps"] = steps
-        acc["value"] = world * m * steps / (acc["ms"] / 1000.0)
+        acc["value"] = replica_rate(m, steps, world, acc["ms"])
         acc["ids"] = ids.clone()
         acc["dists"] = dists.clone()
         acc["fp64"] = fp64_error(X, Q, ids, dists)
@@ -566,12 +578,8 @@ def run_batch(a):
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = pyrbc.kernel_launches() - l0
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * total_m * a.steps / (ms / 1000.0)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
+    value = replica_rate(total_m, a.steps, world, ms)
 
     # end to end: pinned host queries copied in, results copied out, every step
     hq = [r["Q"].cpu().pin_memory() for r in inst]
