@@ -434,14 +434,23 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (uint32_t t = 0; t < ntiles && ok; t++, bi++) {
         if (MT == 1 && (bi & 1u) != grp) continue;
         const uint32_t slot = bi % NSLOT;
+        // other CTAs tighten the query's shortlist all the time: refresh the filter
+        const float th_now = arow < item.nq ? __uint_as_float(__ldcg(a.sl_theta + q)) : FLT_MAX;
         if (!(ok = mbar_wait(&bar_t_full[slot], (bi / NSLOT) & 1, a.err))) break;
         if (!(ok = mbar_wait(&bar_x_full[slot], (bi / NSLOT) & 1, a.err))) break;
+        if (arow < item.nq) thv = fminf(thv, v_threshold(th_now, dq));
         tc_fence_after();
         const float *xr = xs + slot * kBN;
         const uint32_t taddr = tmem + ((32u * ew) << 16) + (slot * MT + (MT == 2 ? grp : 0)) * ACC * kBN;
         const uint32_t p = (uint32_t)(item.p0 + (uint64_t)t * kBN);
         // one 32-column chunk of the accumulator(s): approx, filter, candidates
-        auto chunk = [&](const uint32_t(&r)[32], const uint32_t(&r2)[SPLIT ? 32 : 1], uint32_t c) {
+#pragma unroll 1
+        for (uint32_t c = 0; c < kBN / 32; c++) {
+          uint32_t r[32], r2[SPLIT ? 32 : 1];
+          __syncwarp();
+          tmem_ld32(taddr + c * 32, r);
+          if (SPLIT) tmem_ld32(taddr + kBN + c * 32, *reinterpret_cast<uint32_t(*)[32]>(r2));
+          tmem_wait_ld();
           float v[32];
           float mn = INFINITY;
 #pragma unroll
@@ -456,54 +465,25 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             mn = fminf(mn, fminf(fminf(v[4 * j4], v[4 * j4 + 1]), fminf(v[4 * j4 + 2], v[4 * j4 + 3])));
           }
-          if (!__any_sync(0xffffffffu, mn <= thv)) return;
-          // candidates: into the lane's buffer; full buffers are merged by the
-          // warp, which tightens the filter, until none are left
+          if (!__any_sync(0xffffffffu, mn <= thv)) continue;
+          // candidates: the chunk's values go to a per-thread copy (indexed by
+          // the candidate bits), then into the lane's buffer; full buffers are
+          // merged by the warp, which tightens the filter, until none are left
+          float vs[32];
           uint32_t pend = 0;
 #pragma unroll
-          for (int e = 0; e < 32; e++) pend |= (uint32_t)(v[e] <= thv) << e;
+          for (int e = 0; e < 32; e++) {
+            vs[e] = v[e];
+            pend |= (uint32_t)(v[e] <= thv) << e;
+          }
+          const uint32_t rbase = p + c * 32;
           while (__any_sync(0xffffffffu, pend != 0)) {
-#pragma unroll
-            for (int e = 0; e < 32; e++) {
-              if (((pend >> e) & 1u) && nl < (uint32_t)kLocal) {
-                nl = insert_local(myla, myli, nl, dq + v[e], p + c * 32 + e);
-                pend &= ~(1u << e);
-              }
+            while (pend && nl < (uint32_t)kLocal) {
+              const int e = __ffs(pend) - 1;
+              pend &= pend - 1;
+              if (vs[e] <= thv) nl = insert_local(myla, myli, nl, dq + vs[e], rbase + e);
             }
             flush(__ballot_sync(0xffffffffu, pend != 0), q, nl, thv, dq);
-#pragma unroll
-            for (int e = 0; e < 32; e++)
-              if (!(v[e] <= thv)) pend &= ~(1u << e);
-          }
-        };
-        if (!SPLIT) {
-          // tensor-memory loads double-buffered: chunk c + 1 is in flight while c is processed
-          uint32_t ra[32], rb[32], nil[SPLIT ? 32 : 1];
-          __syncwarp();
-          tmem_ld32(taddr, ra);
-          tmem_wait_ld();
-#pragma unroll
-          for (uint32_t c = 0; c < kBN / 32; c += 2) {
-            __syncwarp();
-            tmem_ld32(taddr + (c + 1) * 32, rb);
-            chunk(ra, nil, c);
-            tmem_wait_ld();
-            if (c + 2 < kBN / 32) {
-              __syncwarp();
-              tmem_ld32(taddr + (c + 2) * 32, ra);
-            }
-            chunk(rb, nil, c + 1);
-            tmem_wait_ld();
-          }
-        } else {
-#pragma unroll 1
-          for (uint32_t c = 0; c < kBN / 32; c++) {
-            uint32_t r[32], r2[SPLIT ? 32 : 1];
-            __syncwarp();
-            tmem_ld32(taddr + c * 32, r);
-            tmem_ld32(taddr + kBN + c * 32, *reinterpret_cast<uint32_t(*)[32]>(r2));
-            tmem_wait_ld();
-            chunk(r, r2, c);
           }
         }
         tc_fence_before();
