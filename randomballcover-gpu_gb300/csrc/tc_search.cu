@@ -67,7 +67,7 @@ using namespace sm100;
 
 constexpr int kBM = 128, kBN = 128, kEpiGroups = 2;
 constexpr int kThreads = 128 + 128 * kEpiGroups;
-constexpr int kLocal = 8, kLST = kLocal + 1;  // per-thread candidate buffer (odd stride: no bank conflicts)
+constexpr int kLocal = 8;  // per-thread candidate buffer, in registers
 constexpr uint32_t kTile16K = 16384;           // 128 rows x 128 bytes (one 64-wide K block of halves)
 constexpr uint32_t kLockSpin = 1u << 22;
 constexpr uint32_t kMaxA = 2, kMaxB = 4;
@@ -84,14 +84,15 @@ __device__ __forceinline__ float v_threshold(float theta, float dq) {
   return fminf(t, FLT_MAX);  // never +inf: masked columns carry v = +inf
 }
 
-// Merge one lane's sorted candidates (nl <= kLocal entries at la/li in shared
-// memory) into query q's global shortlist, with the whole warp: the current
+// Merge one lane's sorted candidates (nl <= kLocal entries in the owner
+// lane's registers la/li) into query q's global shortlist, with the whole
+// warp: the current
 // buffer (40 sorted entries) and the candidates form 64 (approx, row) pairs,
 // two per lane, which a bitonic network sorts; the 40 smallest go to the
 // other buffer, then the buffers swap, under the query's lock.  Called by all
 // 32 lanes with the same arguments; returns the query's new threshold.
-__device__ float warp_publish(const TcArgs &a, uint32_t q, const float *la, const uint32_t *li, uint32_t nl,
-                              uint32_t owner) {
+__device__ __forceinline__ float warp_publish(const TcArgs &a, uint32_t q, const float (&la)[kLocal],
+                                              const uint32_t (&li)[kLocal], uint32_t nl, uint32_t owner) {
   const uint32_t lane = threadIdx.x & 31;
   uint32_t got = 1;
   if (lane == owner) {
@@ -119,9 +120,15 @@ __device__ float warp_publish(const TcArgs &a, uint32_t q, const float *la, cons
   if (lane < tail) {
     a1 = __ldcg(a.sl_a + cur + 32 + lane);
     i1 = __ldcg(a.sl_row + cur + 32 + lane);
-  } else if (lane - tail < nl) {
-    a1 = la[lane - tail];
-    i1 = li[lane - tail];
+  }
+#pragma unroll
+  for (uint32_t j = 0; j < (uint32_t)kLocal; j++) {  // the owner's candidates to lanes tail ..
+    const float ca = __shfl_sync(0xffffffffu, la[j], owner);
+    const uint32_t ci = __shfl_sync(0xffffffffu, li[j], owner);
+    if (lane == tail + j && j < nl) {
+      a1 = ca;
+      i1 = ci;
+    }
   }
   warp_sort32(a1, i1);  // the list's tail and the candidates, ascending
   // bitonic merge of two ascending 32-lists: lower half = ranks 0..31
@@ -159,17 +166,20 @@ __device__ float warp_publish(const TcArgs &a, uint32_t q, const float *la, cons
   return theta;
 }
 
-// Sorted insertion of (av, row) into a lane's candidate buffer (nl < kLocal).
-__device__ __noinline__ uint32_t insert_local(float *myla, uint32_t *myli, uint32_t nl, float av, uint32_t row) {
-  int pos = (int)nl;
-  while (pos > 0 && row_less(av, row, myla[pos - 1], myli[pos - 1])) {
-    myla[pos] = myla[pos - 1];
-    myli[pos] = myli[pos - 1];
-    pos--;
+// Sorted insertion of (av, row) into a lane's register buffer (ascending,
+// empty slots +inf); the caller guarantees a free slot.
+__device__ __forceinline__ void insert_local(float (&la)[kLocal], uint32_t (&li)[kLocal], float av, uint32_t row) {
+#pragma unroll
+  for (int j = kLocal - 1; j > 0; j--) {
+    const bool shift = row_less(av, row, la[j - 1], li[j - 1]);
+    const bool here = !shift && row_less(av, row, la[j], li[j]);
+    la[j] = shift ? la[j - 1] : (here ? av : la[j]);
+    li[j] = shift ? li[j - 1] : (here ? row : li[j]);
   }
-  myla[pos] = av;
-  myli[pos] = row;
-  return nl + 1;
+  if (row_less(av, row, la[0], li[0])) {
+    la[0] = av;
+    li[0] = row;
+  }
 }
 
 // Per-item state of one query row, staged by warp 3 for the epilogue.
@@ -210,8 +220,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char *sB = sA + AS * a_stage;
   float *xs = reinterpret_cast<float *>(sB + BS * b_stage);  // NSLOT x 128 row constants
   RowState *rs = reinterpret_cast<RowState *>(xs + NSLOT * kBN);  // 2 x 256 staged row states
-  float *la = reinterpret_cast<float *>(rs + 2 * 2 * kBM);       // per epilogue thread: kLST approx
-  uint32_t *li = reinterpret_cast<uint32_t *>(la + kEpiGroups * kBM * kLST);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 1) {
@@ -401,10 +409,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp >= 4) {
     // ------------------------------------------------ epilogue (two warpgroups)
     const uint32_t grp = (warp - 4) >> 2, ew = warp & 3, et = ew * 32 + lane;
-    float *wla = la + (grp * kBM + ew * 32) * kLST;  // this warp's candidate buffers
-    uint32_t *wli = li + (grp * kBM + ew * 32) * kLST;
-    float *myla = wla + lane * kLST;
-    uint32_t *myli = wli + lane * kLST;
+    float myla[kLocal];  // this lane's candidates, ascending (approx, row)
+    uint32_t myli[kLocal];
+#pragma unroll
+    for (int j = 0; j < kLocal; j++) {
+      myla[j] = INFINITY;
+      myli[j] = RBC_DUMMY;
+    }
     const uint32_t arow = (MT == 2 ? grp * kBM : 0) + et;  // this thread's row of the item's query tiles
     uint32_t ai = 0, bi = 0;
     bool ok = true;
@@ -413,11 +424,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       while (need) {
         const uint32_t l = __ffs(need) - 1;
         need &= need - 1;
-        const float th = warp_publish(a, __shfl_sync(0xffffffffu, q, l), wla + l * kLST, wli + l * kLST,
+        const float th = warp_publish(a, __shfl_sync(0xffffffffu, q, l), myla, myli,
                                       __shfl_sync(0xffffffffu, nl, l), l);
         if (lane == l) {
           nl = 0;
           thv = v_threshold(th, dq);
+#pragma unroll
+          for (int j = 0; j < kLocal; j++) {
+            myla[j] = INFINITY;
+            myli[j] = RBC_DUMMY;
+          }
         }
       }
     };
@@ -443,47 +459,62 @@ __global__ void __launch_bounds__(kThreads, 1)
         const float *xr = xs + slot * kBN;
         const uint32_t taddr = tmem + ((32u * ew) << 16) + (slot * MT + (MT == 2 ? grp : 0)) * ACC * kBN;
         const uint32_t p = (uint32_t)(item.p0 + (uint64_t)t * kBN);
-        // one 32-column chunk of the accumulator(s): approx, filter, candidates
+        // CW columns of the accumulator(s) per tensor-memory read (64 in the BF16
+        // format, 32 with the split format's two accumulators): approx, filter,
+        // candidates
+        constexpr uint32_t CW = SPLIT ? 32 : 64;
 #pragma unroll 1
-        for (uint32_t c = 0; c < kBN / 32; c++) {
-          uint32_t r[32], r2[SPLIT ? 32 : 1];
+        for (uint32_t c = 0; c < kBN / CW; c++) {
+          uint32_t r[CW], r2[SPLIT ? 32 : 1];
           __syncwarp();
-          tmem_ld32(taddr + c * 32, r);
-          if (SPLIT) tmem_ld32(taddr + kBN + c * 32, *reinterpret_cast<uint32_t(*)[32]>(r2));
+          if (SPLIT) {
+            tmem_ld32(taddr + c * CW, *reinterpret_cast<uint32_t(*)[32]>(r));
+            tmem_ld32(taddr + kBN + c * CW, *reinterpret_cast<uint32_t(*)[32]>(r2));
+          } else {
+            tmem_ld64(taddr + c * CW, *reinterpret_cast<uint32_t(*)[64]>(r));
+          }
           tmem_wait_ld();
-          float v[32];
+          // v in place of the accumulator values
           float mn = INFINITY;
 #pragma unroll
-          for (int j4 = 0; j4 < 8; j4++) {
-            const float4 x4 = *reinterpret_cast<const float4 *>(xr + c * 32 + 4 * j4);
+          for (uint32_t j4 = 0; j4 < CW / 4; j4++) {
+            const float4 x4 = *reinterpret_cast<const float4 *>(xr + c * CW + 4 * j4);
             const float xw[4] = {x4.x, x4.y, x4.z, x4.w};
 #pragma unroll
             for (int e = 0; e < 4; e++) {
               float tv = fmaf(alpha, __uint_as_float(r[4 * j4 + e]), xw[e]);
               if (SPLIT) tv = fmaf(alpha, __uint_as_float(r2[(4 * j4 + e) % (SPLIT ? 32 : 1)]), tv);
-              v[4 * j4 + e] = tv;
+              r[4 * j4 + e] = __float_as_uint(tv);
             }
-            mn = fminf(mn, fminf(fminf(v[4 * j4], v[4 * j4 + 1]), fminf(v[4 * j4 + 2], v[4 * j4 + 3])));
+            mn = fminf(mn, fminf(fminf(__uint_as_float(r[4 * j4]), __uint_as_float(r[4 * j4 + 1])),
+                                 fminf(__uint_as_float(r[4 * j4 + 2]), __uint_as_float(r[4 * j4 + 3]))));
           }
           if (!__any_sync(0xffffffffu, mn <= thv)) continue;
-          // candidates: the chunk's values go to a per-thread copy (indexed by
-          // the candidate bits), then into the lane's buffer; full buffers are
-          // merged by the warp, which tightens the filter, until none are left
-          float vs[32];
-          uint32_t pend = 0;
+          // candidates, 32 columns at a time: the values go to a per-thread copy
+          // (indexed by the candidate bits), then into the lane's buffer; full
+          // buffers are merged by the warp, which tightens the filter, until
+          // none are left
 #pragma unroll
-          for (int e = 0; e < 32; e++) {
-            vs[e] = v[e];
-            pend |= (uint32_t)(v[e] <= thv) << e;
-          }
-          const uint32_t rbase = p + c * 32;
-          while (__any_sync(0xffffffffu, pend != 0)) {
-            while (pend && nl < (uint32_t)kLocal) {
-              const int e = __ffs(pend) - 1;
-              pend &= pend - 1;
-              if (vs[e] <= thv) nl = insert_local(myla, myli, nl, dq + vs[e], rbase + e);
+          for (uint32_t h = 0; h < CW / 32; h++) {
+            float vs[32];
+            uint32_t pend = 0;
+#pragma unroll
+            for (int e = 0; e < 32; e++) {
+              vs[e] = __uint_as_float(r[32 * h + e]);
+              pend |= (uint32_t)(vs[e] <= thv) << e;
             }
-            flush(__ballot_sync(0xffffffffu, pend != 0), q, nl, thv, dq);
+            const uint32_t rbase = p + c * CW + 32 * h;
+            while (__any_sync(0xffffffffu, pend != 0)) {
+              while (pend && nl < (uint32_t)kLocal) {
+                const int e = __ffs(pend) - 1;
+                pend &= pend - 1;
+                if (vs[e] <= thv) {
+                  insert_local(myla, myli, dq + vs[e], rbase + e);
+                  nl++;
+                }
+              }
+              flush(__ballot_sync(0xffffffffu, pend != 0), q, nl, thv, dq);
+            }
           }
         }
         tc_fence_before();
@@ -768,7 +799,7 @@ size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs) {
   const size_t kbh = SPLIT ? 2 * kb : kb;
   const size_t nslot = 4 / (MT * (SPLIT ? 2 : 1));
   return 1024 + (size_t)as * MT * kbh * kTile16K + (size_t)bs * kbh * kTile16K + nslot * kBN * 4 +
-         2 * 2 * kBM * sizeof(RowState) + (size_t)kEpiGroups * kBM * kLST * 8;
+         2 * 2 * kBM * sizeof(RowState);
 }
 
 template <int MT, bool SPLIT>
