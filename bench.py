@@ -360,7 +360,7 @@ def run_engine(a):
         router_info = {"train_queries": w["train"], "epochs": w["epochs"], "label_s": label_s, "train_s": train_s,
                        "final_loss": loss, "probe_recall_top1": (top1 == test_labels).float().mean().item(),
                        "architecture": f"MLP {w['d']}->512->512->{w['reps']} GELU, BF16 weights, FP32 accumulate"}
-        idx.set_router(router, probes=2)
+        idx.set_router(router, probes=7)
 
     modes = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC, "oneshot": pyrbc.QUERY_ONESHOT,
              "learned": pyrbc.QUERY_EXACT_TC | pyrbc.QUERY_ROUTED, "learned_plain": pyrbc.QUERY_EXACT | pyrbc.QUERY_ROUTED}

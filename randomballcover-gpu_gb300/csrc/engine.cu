@@ -7,6 +7,7 @@
 // error word.  There is no CPU fallback: if a kernel cannot run, the call
 // fails with RBC_ERR_CUDA.
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <unordered_map>
@@ -44,6 +45,7 @@ int cuda_fail(cudaError_t e, const char *what) {
 namespace {
 
 constexpr uint32_t kDefaultProbes = 1;  // lists searched before planning (the one-shot plan)
+constexpr uint32_t kTcProbes = 8;       // the tensor form: a tighter start for its shortlists
 
 void pool_setup() {
   static bool done[64] = {};
@@ -514,7 +516,12 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   const uint32_t nr = idx->nr, ld = idx->ld, kp = idx->kp, fmt = idx->tc.format, cols = idx->tc.cols;
   const bool routed = (mode & RBC_QUERY_ROUTED) != 0;
   if (routed && !idx->router) return fail(RBC_ERR_INVALID, "rbc_query: RBC_QUERY_ROUTED without a router");
-  const uint32_t P = routed ? 1 + idx->router_probes : 1;
+  // lists searched in the probe round: the nearest representatives' (or the
+  // nearest plus the router's picks); RBC_TC_PROBES overrides the count
+  uint32_t P = routed ? 1 + idx->router_probes : kTcProbes;
+  if (!routed)
+    if (const char *env = std::getenv("RBC_TC_PROBES")) P = std::max(1, std::min(8, std::atoi(env)));
+  P = std::min(P, nr);
   const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
   const uint32_t qtile = tc_query_tile(fmt);
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
@@ -588,7 +595,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       CK(launch_router_probes(logits.as<float>(), mq, nr, idx->router_probes, near.as<uint32_t>(),
                               near_d.as<float>(), b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     } else {
-      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, 1, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     }
     CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(),
                            mq, s));

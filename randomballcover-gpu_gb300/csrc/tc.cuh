@@ -59,6 +59,7 @@ struct TcArgs {
   unsigned long long *stats;  // [0] (query, row) pairs, [1] (query, list) pairs; may be null
   uint32_t *err;
   uint32_t a_stages, b_stages;  // set by launch_tc_search from the shared-memory budget
+  uint32_t stage_words;         // set by launch_tc_search: per-thread merge staging (0: none)
 };
 
 struct RerankArgs {

@@ -182,6 +182,62 @@ __device__ __forceinline__ void insert_local(float (&la)[kLocal], uint32_t (&li)
   }
 }
 
+// Merge one lane's candidates into its own query's shortlist, every lane of
+// the warp at once (each on its own query): the current buffer is copied into
+// the lane's shared-memory staging area with 16-byte loads (one round trip),
+// the candidates are inserted there, the result goes to the other buffer and
+// the buffers swap, under the query's lock.  Returns the new threshold.
+__device__ __forceinline__ float lane_merge(const TcArgs &a, uint32_t q, const float (&la)[kLocal],
+                                            const uint32_t (&li)[kLocal], uint32_t nl, float *stage) {
+  uint32_t spins = 0;
+  while (atomicCAS(a.sl_lock + q, 0u, 1u) != 0u) {
+    if (++spins > kLockSpin) {
+      raise_error(a.err, RBC_ERR_ITER_LIMIT);
+      return __uint_as_float(__ldcg(a.sl_theta + q));
+    }
+    __nanosleep(64);
+  }
+  __threadfence();
+  const uint32_t SL = a.sl, sel = __ldcg(a.sl_sel + q);
+  const uint64_t cur = ((uint64_t)sel * a.m + q) * SL, nxt = ((uint64_t)(sel ^ 1u) * a.m + q) * SL;
+  float *sa = stage;
+  uint32_t *sr = reinterpret_cast<uint32_t *>(stage + SL);
+  // SL is a multiple of 4, so every list starts on a 16-byte boundary
+  for (uint32_t j = 0; j < SL / 4; j++) {
+    const float4 va = __ldcg(reinterpret_cast<const float4 *>(a.sl_a + cur) + j);
+    const uint4 vr = __ldcg(reinterpret_cast<const uint4 *>(a.sl_row + cur) + j);
+    sa[4 * j] = va.x; sa[4 * j + 1] = va.y; sa[4 * j + 2] = va.z; sa[4 * j + 3] = va.w;
+    sr[4 * j] = vr.x; sr[4 * j + 1] = vr.y; sr[4 * j + 2] = vr.z; sr[4 * j + 3] = vr.w;
+  }
+#pragma unroll
+  for (uint32_t e = 0; e < (uint32_t)kLocal; e++) {
+    if (e >= nl) break;
+    const float av = la[e];
+    const uint32_t ar = li[e];
+    if (!row_less(av, ar, sa[SL - 1], sr[SL - 1])) break;  // candidates ascend: the rest do not fit either
+    int pos = (int)SL - 1;
+    while (pos > 0 && row_less(av, ar, sa[pos - 1], sr[pos - 1])) {
+      sa[pos] = sa[pos - 1];
+      sr[pos] = sr[pos - 1];
+      pos--;
+    }
+    sa[pos] = av;
+    sr[pos] = ar;
+  }
+  for (uint32_t j = 0; j < SL / 4; j++) {
+    reinterpret_cast<float4 *>(a.sl_a + nxt)[j] = make_float4(sa[4 * j], sa[4 * j + 1], sa[4 * j + 2], sa[4 * j + 3]);
+    reinterpret_cast<uint4 *>(a.sl_row + nxt)[j] = make_uint4(sr[4 * j], sr[4 * j + 1], sr[4 * j + 2], sr[4 * j + 3]);
+  }
+  // FLT_MAX, not +inf, while the list is short
+  const float theta = sr[SL - 1] != RBC_DUMMY ? sa[SL - 1] : FLT_MAX;
+  __threadfence();
+  a.sl_theta[q] = __float_as_uint(theta);
+  a.sl_sel[q] = sel ^ 1u;
+  __threadfence();
+  atomicExch(a.sl_lock + q, 0u);
+  return theta;
+}
+
 // Per-item state of one query row, staged by warp 3 for the epilogue.
 struct RowState {
   uint32_t q;
@@ -220,6 +276,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char *sB = sA + AS * a_stage;
   float *xs = reinterpret_cast<float *>(sB + BS * b_stage);  // NSLOT x 128 row constants
   RowState *rs = reinterpret_cast<RowState *>(xs + NSLOT * kBN);  // 2 x 256 staged row states
+  float *mstage = reinterpret_cast<float *>(rs + 2 * 2 * kBM);     // per epilogue thread: a.stage_words
+                                                                   // of merge staging (or none)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 1) {
@@ -419,8 +477,24 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t arow = (MT == 2 ? grp * kBM : 0) + et;  // this thread's row of the item's query tiles
     uint32_t ai = 0, bi = 0;
     bool ok = true;
-    // merge the buffers of the lanes in `need` into their queries' shortlists
+    float *mystage = mstage + (grp * kBM + et) * a.stage_words;
+    // merge the buffers of the lanes in `need` into their queries' shortlists:
+    // every lane at once on its own query (BF16 format), or one lane at a
+    // time with the whole warp (when shared memory holds no staging areas)
     auto flush = [&](uint32_t need, uint32_t q, uint32_t &nl, float &thv, float dq) {
+      if (a.stage_words) {
+        if ((need >> lane) & 1u) {
+          thv = v_threshold(lane_merge(a, q, myla, myli, nl, mystage), dq);
+          nl = 0;
+#pragma unroll
+          for (int j = 0; j < kLocal; j++) {
+            myla[j] = INFINITY;
+            myli[j] = RBC_DUMMY;
+          }
+        }
+        __syncwarp();
+        return;
+      }
       while (need) {
         const uint32_t l = __ffs(need) - 1;
         need &= need - 1;
@@ -795,30 +869,38 @@ __global__ void rerank_kernel(RerankArgs a) {
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
 template <int MT, bool SPLIT>
-size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs) {
+size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs, uint32_t stage_words) {
   const size_t kbh = SPLIT ? 2 * kb : kb;
   const size_t nslot = 4 / (MT * (SPLIT ? 2 : 1));
   return 1024 + (size_t)as * MT * kbh * kTile16K + (size_t)bs * kbh * kTile16K + nslot * kBN * 4 +
-         2 * 2 * kBM * sizeof(RowState);
+         2 * 2 * kBM * sizeof(RowState) + (size_t)kEpiGroups * kBM * stage_words * 4;
 }
 
 template <int MT, bool SPLIT>
 cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s) {
   // deepest pipeline that fits: B depth first (it hides the L2 latency of
   // every tile), then a second query stage (it hides the gather at item starts)
+  // merge staging (2 SL + 1 words per epilogue thread) first: the lane-parallel
+  // shortlist merges matter more than pipeline depth
   static const uint32_t pref[][2] = {{2, 4}, {2, 3}, {1, 4}, {1, 3}, {2, 2}, {1, 2}};
   uint32_t as = 0, bs = 0;
-  for (const auto &c : pref)
-    if (smem_bytes<MT, SPLIT>(a.kb, c[0], c[1]) <= kSmemLimit) {
-      as = c[0];
-      bs = c[1];
+  for (uint32_t sw : {2 * a.sl + 1, 0u}) {
+    for (const auto &c : pref)
+      if (smem_bytes<MT, SPLIT>(a.kb, c[0], c[1], sw) <= kSmemLimit) {
+        as = c[0];
+        bs = c[1];
+        break;
+      }
+    if (as) {
+      a.stage_words = sw;
       break;
     }
+  }
   // RBC_TC_STAGES="a,b" overrides the choice (tuning experiments) when it fits
   if (const char *env = std::getenv("RBC_TC_STAGES")) {
     unsigned ea = 0, eb = 0;
     if (std::sscanf(env, "%u,%u", &ea, &eb) == 2 && ea >= 1 && ea <= kMaxA && eb >= 2 && eb <= kMaxB &&
-        smem_bytes<MT, SPLIT>(a.kb, ea, eb) <= kSmemLimit) {
+        smem_bytes<MT, SPLIT>(a.kb, ea, eb, a.stage_words) <= kSmemLimit) {
       as = ea;
       bs = eb;
     }
@@ -826,7 +908,7 @@ cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, 
   if (!as) return cudaErrorInvalidConfiguration;
   a.a_stages = as;
   a.b_stages = bs;
-  const size_t smem = smem_bytes<MT, SPLIT>(a.kb, as, bs);
+  const size_t smem = smem_bytes<MT, SPLIT>(a.kb, as, bs, a.stage_words);
   cudaError_t e =
       cudaFuncSetAttribute(tc_search_kernel<MT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
