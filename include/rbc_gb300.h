@@ -182,7 +182,9 @@ int rbc_router_gradients(rbc_router *router, const float *dQ, uint32_t batch, ui
 int rbc_router_train(rbc_router *router, const float *dQ, uint64_t n, uint32_t ldq,
                      const uint32_t *dLabels, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
                      float *final_loss, void *stream);
-/* Logits of m queries into dLogits (m x num_lists). */
+/* Logits of m queries into dLogits (m x num_lists): the inference the routed
+ * queries use -- tensor-core GEMMs with BF16 activations when hidden is a
+ * multiple of 64, else the training kernels' FP32-activation forward. */
 int rbc_router_logits(rbc_router *router, const float *dQ, uint64_t m, uint32_t ldq, float *dLogits,
                       void *stream);
 /* Training labels produced by the RBC: the list owning each query's exact

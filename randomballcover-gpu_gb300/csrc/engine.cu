@@ -409,8 +409,9 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   const uint32_t nr = idx->nr, ld = idx->ld;
   const bool routed = (mode & RBC_QUERY_ROUTED) && base == RBC_QUERY_EXACT;
   if (routed && !idx->router) return fail(RBC_ERR_INVALID, "rbc_query: RBC_QUERY_ROUTED without a router");
-  // probe table: column 0 the nearest representative, then the router's picks
-  const uint32_t P = routed ? 1 + idx->router_probes : std::min(kDefaultProbes, nr);
+  // probe table: the nearest representative, then (routed) the router's picks
+  const uint32_t Pn = std::min(kDefaultProbes, nr);
+  const uint32_t P = routed ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
   const uint32_t qtile = (uint32_t)search_query_tile(idx->dp, idx->tune_tq);
   const int grid = search_grid(idx->metric, idx->dp, idx->tune_tq);
   // batch so the m x nr plan arrays stay near 2^27 entries
@@ -438,8 +439,8 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
   DevBuf stats, near, near_d, logits;
   if (routed) {
-    CK(near.alloc(mb * 4, s));
-    CK(near_d.alloc(mb * 4, s));
+    CK(near.alloc(mb * Pn * 4, s));
+    CK(near_d.alloc(mb * Pn * 4, s));
     CK(logits.alloc(mb * nr * 4, s));
   }
   CK(stats.alloc(2 * sizeof(unsigned long long), s));
@@ -451,16 +452,20 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
     CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
     if (routed) {
-      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, 1, near.as<uint32_t>(), near_d.as<float>(), s));
+      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, Pn, near.as<uint32_t>(), near_d.as<float>(), s));
       Router &rt = idx->router->r;
-      const uint32_t chunk = 4096;
-      CK(rt.alloc_batch(chunk, s));
-      for (uint64_t i = 0; i < mq; i += chunk) {
-        const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
-        CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+      if (rt.tc_ok()) {
+        CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
+      } else {
+        const uint32_t chunk = 4096;
+        CK(rt.alloc_batch(chunk, s));
+        for (uint64_t i = 0; i < mq; i += chunk) {
+          const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
+          CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+        }
       }
-      CK(launch_router_probes(logits.as<float>(), mq, nr, idx->router_probes, near.as<uint32_t>(),
-                              near_d.as<float>(), b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+      CK(launch_router_probes(logits.as<float>(), mq, nr, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
+                              b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     } else {
       CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     }
@@ -516,12 +521,13 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   const uint32_t nr = idx->nr, ld = idx->ld, kp = idx->kp, fmt = idx->tc.format, cols = idx->tc.cols;
   const bool routed = (mode & RBC_QUERY_ROUTED) != 0;
   if (routed && !idx->router) return fail(RBC_ERR_INVALID, "rbc_query: RBC_QUERY_ROUTED without a router");
-  // lists searched in the probe round: the nearest representatives' (or the
-  // nearest plus the router's picks); RBC_TC_PROBES overrides the count
-  uint32_t P = routed ? 1 + idx->router_probes : kTcProbes;
-  if (!routed)
-    if (const char *env = std::getenv("RBC_TC_PROBES")) P = std::max(1, std::min(8, std::atoi(env)));
-  P = std::min(P, nr);
+  // lists searched in the probe round: the nearest representatives' (plus,
+  // routed, the router's picks among the others); RBC_TC_PROBES overrides the
+  // number of nearest ones
+  uint32_t Pn = kTcProbes;
+  if (const char *env = std::getenv("RBC_TC_PROBES")) Pn = std::max(1, std::min(8, std::atoi(env)));
+  Pn = std::min(Pn, nr);
+  const uint32_t P = routed ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
   const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
   const uint32_t qtile = tc_query_tile(fmt);
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
@@ -548,8 +554,8 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
       stats;
   if (routed) {
-    CK(near.alloc(mb * 4, s));
-    CK(near_d.alloc(mb * 4, s));
+    CK(near.alloc(mb * Pn * 4, s));
+    CK(near_d.alloc(mb * Pn * 4, s));
     CK(logits.alloc(mb * nr * 4, s));
   }
   CK(Qh.alloc((mb + 1) * cols * 2, s));
@@ -584,16 +590,20 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
     CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
     if (routed) {
-      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, 1, near.as<uint32_t>(), near_d.as<float>(), s));
+      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, Pn, near.as<uint32_t>(), near_d.as<float>(), s));
       Router &rt = idx->router->r;
-      const uint32_t chunk = 4096;
-      CK(rt.alloc_batch(chunk, s));
-      for (uint64_t i = 0; i < mq; i += chunk) {
-        const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
-        CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+      if (rt.tc_ok()) {
+        CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
+      } else {
+        const uint32_t chunk = 4096;
+        CK(rt.alloc_batch(chunk, s));
+        for (uint64_t i = 0; i < mq; i += chunk) {
+          const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
+          CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+        }
       }
-      CK(launch_router_probes(logits.as<float>(), mq, nr, idx->router_probes, near.as<uint32_t>(),
-                              near_d.as<float>(), b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+      CK(launch_router_probes(logits.as<float>(), mq, nr, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
+                              b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     } else {
       CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     }

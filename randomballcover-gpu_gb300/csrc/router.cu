@@ -310,6 +310,7 @@ cudaError_t Router::forward_backward(uint32_t b, cudaStream_t s) {
 
 cudaError_t Router::adam_step(float lr, cudaStream_t s) {
   step++;
+  version++;
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
   const uint64_t P = nparams();
@@ -318,6 +319,7 @@ cudaError_t Router::adam_step(float lr, cudaStream_t s) {
 }
 
 cudaError_t Router::refresh_bf16(cudaStream_t s) {
+  version++;
   const uint64_t P = nparams();
   to_bf16_flat<<<blocks(P), 256, 0, s>>>(w, wb, P);
   return launched();
@@ -347,29 +349,38 @@ cudaError_t Router::gather(const float *Q, uint32_t ldq, const uint32_t *order, 
 
 Router::~Router() {
   for (void *p : {(void *)w, (void *)g, (void *)m1, (void *)m2, (void *)wb, (void *)X, (void *)y, (void *)h1,
-                  (void *)a1, (void *)h2, (void *)a2, (void *)z, (void *)ga, (void *)gb, (void *)loss})
+                  (void *)a1, (void *)h2, (void *)a2, (void *)z, (void *)ga, (void *)gb, (void *)loss, (void *)xb,
+                  (void *)h1b, (void *)h2b, (void *)w1p})
     if (p) cudaFree(p);
 }
 
 namespace {
 
-// One warp per row: the P largest logits (ties to the lower list index) into
-// columns 1..P, the nearest representative into column 0.
-__global__ void router_probes_kernel(const float *__restrict__ z, uint64_t m, uint32_t L, uint32_t P,
+// One warp per row: columns [0, Pn) of the probe table take the Pn nearest
+// representatives (table `nearest`, Pn wide), columns [Pn, Pn + P) the P
+// largest logits (ties to the lower list index) that are not among them.
+__global__ void router_probes_kernel(const float *__restrict__ z, uint64_t m, uint32_t L, uint32_t P, uint32_t Pn,
                                      const uint32_t *__restrict__ nearest, const float *__restrict__ nearest_d,
                                      uint32_t *__restrict__ probe, float *__restrict__ probed) {
   const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31;
   if (q >= m) return;
   const float *row = z + q * L;
-  const uint32_t W = 1 + P;
-  uint32_t taken[8];
+  const uint32_t W = Pn + P;
+  uint32_t taken[16];
+  for (uint32_t p = 0; p < Pn; p++) {
+    taken[p] = nearest[q * Pn + p];
+    if (lane == 0) {
+      probe[q * W + p] = taken[p];
+      probed[q * W + p] = nearest_d[q * Pn + p];
+    }
+  }
   for (uint32_t p = 0; p < P; p++) {
     float bv = -INFINITY;
     uint32_t bi = RBC_DUMMY;
     for (uint32_t j = lane; j < L; j += 32) {
       bool used = false;
-      for (uint32_t t = 0; t < p; t++) used |= taken[t] == j;
+      for (uint32_t t = 0; t < Pn + p; t++) used |= taken[t] == j;
       float v = row[j];
       if (!used && (v > bv || (v == bv && j < bi))) {
         bv = v;
@@ -385,15 +396,11 @@ __global__ void router_probes_kernel(const float *__restrict__ z, uint64_t m, ui
         bi = oi;
       }
     }
-    taken[p] = bi;
+    taken[Pn + p] = bi;
     if (lane == 0) {
-      probe[q * W + 1 + p] = bi;
-      probed[q * W + 1 + p] = 0.f;
+      probe[q * W + Pn + p] = bi;
+      probed[q * W + Pn + p] = 0.f;
     }
-  }
-  if (lane == 0) {
-    probe[q * W] = nearest[q];
-    probed[q * W] = nearest_d[q];
   }
 }
 
@@ -408,10 +415,12 @@ __global__ void owner_lookup_kernel(const uint32_t *__restrict__ ids, uint64_t m
 
 }  // namespace
 
-cudaError_t launch_router_probes(const float *logits, uint64_t m, uint32_t L, uint32_t P, const uint32_t *nearest,
-                                 const float *nearest_d, uint32_t *probe, float *probed, cudaStream_t s) {
+cudaError_t launch_router_probes(const float *logits, uint64_t m, uint32_t L, uint32_t P, uint32_t Pn,
+                                 const uint32_t *nearest, const float *nearest_d, uint32_t *probe, float *probed,
+                                 cudaStream_t s) {
   if (m == 0) return cudaSuccess;
-  router_probes_kernel<<<blocks(m * 32), 256, 0, s>>>(logits, m, L, P, nearest, nearest_d, probe, probed);
+  if (Pn + P > 16) return cudaErrorInvalidValue;
+  router_probes_kernel<<<blocks(m * 32), 256, 0, s>>>(logits, m, L, P, Pn, nearest, nearest_d, probe, probed);
   return launched();
 }
 
@@ -561,6 +570,21 @@ int rbc_router_logits(rbc_router *router, const float *dQ, uint64_t m, uint32_t 
   if (!router || (m && (!dQ || !dLogits))) return fail(RBC_ERR_INVALID, "rbc_router_logits: bad argument");
   Router &r = router->r;
   cudaStream_t s = (cudaStream_t)stream;
+  if (r.tc_ok()) {  // the inference the queries use: tensor-core GEMMs
+    uint32_t *err = nullptr, herr = 0;
+    RCK(cudaMallocAsync(&err, 4, s));
+    RCK(cudaMemsetAsync(err, 0, 4, s));
+    const uint32_t chunk = 1u << 20;
+    for (uint64_t i = 0; i < m; i += chunk) {
+      const uint32_t b = (uint32_t)std::min<uint64_t>(chunk, m - i);
+      RCK(r.forward_tc(dQ + i * ldq, ldq, b, dLogits + i * r.L, err, s));
+    }
+    RCK(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
+    RCK(cudaFreeAsync(err, s));
+    RCK(cudaStreamSynchronize(s));
+    if (herr) return fail(RBC_ERR_ITER_LIMIT, "rbc_router_logits: a bounded device wait ran out");
+    return RBC_OK;
+  }
   const uint32_t chunk = 4096;
   RCK(r.alloc_batch(chunk, s));
   for (uint64_t i = 0; i < m; i += chunk) {

@@ -30,14 +30,22 @@ struct Router {
   cudaError_t forward_backward(uint32_t b, cudaStream_t s);
   cudaError_t adam_step(float lr, cudaStream_t s);
   cudaError_t refresh_bf16(cudaStream_t s);
+  // inference on the tensor cores (router_tc.cu): needs H a multiple of 64
+  uint64_t version = 0;  // bumped whenever the BF16 weights change
+  uint32_t tc_cap = 0;
+  __nv_bfloat16 *xb = nullptr, *h1b = nullptr, *h2b = nullptr, *w1p = nullptr;
+  uint64_t w1p_version = ~0ull;
+  bool tc_ok() const;
+  cudaError_t forward_tc(const float *X, uint32_t ldx, uint32_t b, float *z, uint32_t *err, cudaStream_t s);
   ~Router();
 };
 
-// Top-P lists of each row of router logits (largest first, ties to the lower
-// list), written to columns [1, 1+P) of a probe table of width 1+P whose
-// column 0 holds the nearest representative.
-cudaError_t launch_router_probes(const float *logits, uint64_t m, uint32_t L, uint32_t P, const uint32_t *nearest,
-                                 const float *nearest_d, uint32_t *probe, float *probed, cudaStream_t s);
+// Probe table of width Pn + P: the Pn nearest representatives (a Pn-wide
+// table, nearest first) then the top-P lists of each row of router logits not
+// among them (largest first, ties to the lower list).  Pn + P <= 16.
+cudaError_t launch_router_probes(const float *logits, uint64_t m, uint32_t L, uint32_t P, uint32_t Pn,
+                                 const uint32_t *nearest, const float *nearest_d, uint32_t *probe, float *probed,
+                                 cudaStream_t s);
 // labels[i] = owner[ids[i]]
 cudaError_t launch_owner_lookup(const uint32_t *ids, uint64_t m, uint32_t ldo, const uint32_t *owner,
                                 uint32_t *labels, cudaStream_t s);

@@ -1,0 +1,219 @@
+// router_tc.cu -- the router's inference on the tensor cores.
+//
+// Each layer of the MLP is Y = act(X W^T + b) with X (M x K) the activations
+// and W (N x K) the layer's weights, both row-major with K contiguous: exactly
+// the K-major operands tcgen05.mma reads.  mlp_gemm_kernel computes one
+// 128 x 128 tile of Y per CTA: one thread streams 64-wide K blocks of X and W
+// with TMA (128-byte swizzle) into a 3-stage ring and issues
+// 128 x 128 x 16 BF16 MMAs into a tensor-memory accumulator; the four warps
+// then read the accumulator rows (one TMEM lane per thread), add the bias,
+// apply GELU (exact erf form, as the training kernels) and store BF16 (hidden
+// layers) or FP32 (logits).  Activations between layers are BF16, so the
+// logits differ from the FP32-activation training forward in low bits; they
+// only choose which lists to probe first, and the search stays exact.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "engine.cuh"
+#include "sm100.cuh"
+
+namespace rbc {
+
+namespace {
+
+using namespace sm100;
+
+constexpr uint32_t kGS = 3;              // pipeline stages
+constexpr uint32_t kGTile = 16384;       // 128 rows x 64 BF16
+constexpr size_t kGSmem = 1024 + kGS * 2 * kGTile;
+
+template <bool GELU, bool OUT_BF16>
+__global__ void __launch_bounds__(128, 1)
+    mlp_gemm_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
+                    const float *__restrict__ bias, void *__restrict__ out, uint32_t M, uint32_t N, uint32_t ldo,
+                    uint32_t KB, uint32_t *err) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t full[kGS], empty[kGS], done;
+  __shared__ uint32_t tslot;
+  unsigned char *base =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t m0 = blockIdx.y * 128, n0 = blockIdx.x * 128;
+  if (warp == 0) {
+    tmem_alloc(&tslot, 128);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    for (uint32_t s = 0; s < kGS; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    fence_barrier_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tslot;
+  bool ok = true;
+  if (threadIdx.x == 0) {
+    prefetch_tensormap(&tmX);
+    prefetch_tensormap(&tmW);
+    const uint32_t idesc = idesc_bf16_f32(128, 128);
+    auto load = [&](uint32_t kb) {
+      const uint32_t s = kb % kGS;
+      unsigned char *sa = base + s * 2 * kGTile;
+      mbar_expect_tx(&full[s], 2 * kGTile);
+      tma_load_2d(sa, &tmX, (int32_t)(kb * 64), (int32_t)m0, &full[s]);
+      tma_load_2d(sa + kGTile, &tmW, (int32_t)(kb * 64), (int32_t)n0, &full[s]);
+    };
+    uint32_t issued = 0;
+    for (; issued < KB && issued < kGS; issued++) load(issued);
+    for (uint32_t kb = 0; kb < KB && ok; kb++) {
+      const uint32_t s = kb % kGS;
+      if (!(ok = mbar_wait(&full[s], (kb / kGS) & 1, err))) break;
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(base + s * 2 * kGTile), b0 = a0 + kGTile;
+#pragma unroll
+      for (uint32_t kk = 0; kk < 4; kk++)
+        mma_bf16(tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc, (kb | kk) != 0);
+      mma_commit(&empty[s]);
+      // refill the previous stage once its MMAs are done (one stage of slack)
+      if (kb >= 1 && issued < KB) {
+        const uint32_t ps = (kb - 1) % kGS;
+        if (!(ok = mbar_wait(&empty[ps], ((kb - 1) / kGS) & 1, err))) break;
+        load(issued++);
+      }
+    }
+    mma_commit(&done);
+    // drain: every load issued has landed before the CTA may leave
+    for (uint32_t j = 0; j < kGS && j < issued; j++) {
+      const uint32_t kb = issued - 1 - j;
+      mbar_wait(&full[kb % kGS], (kb / kGS) & 1, nullptr);
+    }
+  }
+  __syncwarp();
+  ok = mbar_wait(&done, 0, err);
+  tc_fence_after();
+  const uint32_t row = m0 + warp * 32 + lane;
+#pragma unroll 1
+  for (uint32_t c = 0; c < 4 && ok; c++) {
+    uint32_t r[32];
+    __syncwarp();
+    tmem_ld32(tmem + ((warp * 32) << 16) + c * 32, r);
+    tmem_wait_ld();
+    const uint32_t nb = n0 + c * 32;
+    if (row >= M || nb >= N) continue;
+    float v[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      const uint32_t n = nb + j;
+      float t = __uint_as_float(r[j]) + (n < N ? bias[n] : 0.f);
+      if (GELU) t = 0.5f * t * (1.f + erff(t * 0.70710678118654752f));
+      v[j] = t;
+    }
+    if (OUT_BF16) {
+      __nv_bfloat16 *o = reinterpret_cast<__nv_bfloat16 *>(out) + (uint64_t)row * ldo + nb;
+      if (nb + 32 <= N) {
+        uint32_t pk[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          pk[j] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * j])) |
+                  ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * j + 1])) << 16);
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          reinterpret_cast<uint4 *>(o)[j] = make_uint4(pk[4 * j], pk[4 * j + 1], pk[4 * j + 2], pk[4 * j + 3]);
+      } else {
+        for (uint32_t j = 0; j < 32 && nb + j < N; j++) o[j] = __float2bfloat16_rn(v[j]);
+      }
+    } else {
+      float *o = reinterpret_cast<float *>(out) + (uint64_t)row * ldo + nb;
+#pragma unroll
+      for (int j = 0; j < 32; j++)
+        if (nb + j < N) o[j] = v[j];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 128);
+  }
+}
+
+// rows x cols FP32 (row stride ld) -> rows x kp BF16, zero beyond cols.
+__global__ void pad_bf16_kernel(const float *__restrict__ src, uint32_t ld, uint64_t rows, uint32_t cols,
+                                uint32_t kp, __nv_bfloat16 *__restrict__ dst) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= rows * kp) return;
+  const uint64_t r = i / kp;
+  const uint32_t c = (uint32_t)(i - r * kp);
+  dst[i] = __float2bfloat16_rn(c < cols ? src[r * ld + c] : 0.f);
+}
+
+// W1 (H x d BF16) -> H x kp BF16, zero beyond d.
+__global__ void pad_w1_kernel(const __nv_bfloat16 *__restrict__ w1, uint32_t H, uint32_t d, uint32_t kp,
+                              __nv_bfloat16 *__restrict__ dst) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)H * kp) return;
+  const uint64_t r = i / kp;
+  const uint32_t c = (uint32_t)(i - r * kp);
+  dst[i] = c < d ? w1[r * d + c] : __float2bfloat16_rn(0.f);
+}
+
+template <bool GELU, bool OUT_BF16>
+cudaError_t gemm_tc(const void *X, uint32_t M, uint32_t K, const void *W, uint32_t N, const float *bias, void *out,
+                    uint32_t ldo, uint32_t *err, cudaStream_t s) {
+  CUtensorMap tmX, tmW;
+  cudaError_t e = tc_make_map(&tmX, X, M, K, 128);
+  if (e == cudaSuccess) e = tc_make_map(&tmW, W, N, K, 128);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(mlp_gemm_kernel<GELU, OUT_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kGSmem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((N + 127) / 128, (M + 127) / 128);
+  mlp_gemm_kernel<GELU, OUT_BF16><<<grid, 128, kGSmem, s>>>(tmX, tmW, bias, out, M, N, ldo, K / 64, err);
+  return launched();
+}
+
+}  // namespace
+
+bool Router::tc_ok() const { return H % 64 == 0 && H >= 64; }
+
+cudaError_t Router::forward_tc(const float *Xin, uint32_t ldx, uint32_t b, float *zout, uint32_t *err,
+                               cudaStream_t s) {
+  if (!tc_ok()) return cudaErrorInvalidValue;
+  const uint32_t kp = (d + 63) / 64 * 64;
+  cudaError_t e = cudaSuccess;
+  if (b > tc_cap) {
+    for (void *p : {(void *)xb, (void *)h1b, (void *)h2b})
+      if (p) cudaFreeAsync(p, s);
+    xb = h1b = h2b = nullptr;
+    e = cudaMallocAsync((void **)&xb, (size_t)b * kp * 2, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h1b, (size_t)b * H * 2, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h2b, (size_t)b * H * 2, s);
+    tc_cap = e == cudaSuccess ? b : 0;
+    if (e != cudaSuccess) return e;
+  }
+  if (!w1p) {
+    e = cudaMalloc((void **)&w1p, (size_t)H * kp * 2);
+    if (e != cudaSuccess) return e;
+  }
+  if (w1p_version != version) {  // the padded W1 follows the BF16 weights
+    pad_w1_kernel<<<(unsigned)(((uint64_t)H * kp + 255) / 256), 256, 0, s>>>(wb, H, d, kp, w1p);
+    if ((e = launched()) != cudaSuccess) return e;
+    w1p_version = version;
+  }
+  const __nv_bfloat16 *W2 = wb + (size_t)H * d + H, *W3 = W2 + (size_t)H * H + H;
+  const float *b1 = w + (size_t)H * d, *b2 = b1 + H + (size_t)H * H, *b3 = b2 + H + (size_t)L * H;
+  pad_bf16_kernel<<<(unsigned)(((uint64_t)b * kp + 255) / 256), 256, 0, s>>>(Xin, ldx, b, d, kp, xb);
+  if ((e = launched()) != cudaSuccess) return e;
+  if ((e = gemm_tc<true, true>(xb, b, kp, w1p, H, b1, h1b, H, err, s)) != cudaSuccess) return e;
+  if ((e = gemm_tc<true, true>(h1b, b, H, W2, H, b2, h2b, H, err, s)) != cudaSuccess) return e;
+  return gemm_tc<false, false>(h2b, b, H, W3, L, b3, zout, L, err, s);
+}
+
+}  // namespace rbc

@@ -124,3 +124,26 @@ def test_routed_queries_are_exact_and_probe_fewer_lists(rbc, oracle):
     assert routed["point_pairs"] < plain["point_pairs"]
     idx.close()
     r.close()
+
+
+def test_tensor_core_inference_matches_training_forward(rbc):
+    """The routed queries' tensor-core inference (BF16 activations) against an
+    FP64 restatement of the training forward: same argmax nearly everywhere,
+    logits within BF16 rounding of the activations."""
+    from scipy.special import erf
+    rng = np.random.default_rng(5)
+    d, H, L, B = 72, 128, 300, 700
+    r = rbc.Router(d, H, L, seed=9)
+    p = r.get_params()
+    X = rng.standard_normal((B, d)).astype(np.float32)
+    z = r.logits(X).cpu().numpy().astype(np.float64)
+    W1, b1, W2, b2, W3, b3 = unpack(p.astype(np.float64), d, H, L)
+    W1, W2, W3 = bf16_round(W1), bf16_round(W2), bf16_round(W3)
+    gelu = lambda x: 0.5 * x * (1 + erf(x / np.sqrt(2)))
+    a1 = bf16_round(gelu(bf16_round(X) @ W1.T + b1))
+    a2 = bf16_round(gelu(a1 @ W2.T + b2))
+    ref = a2 @ W3.T + b3
+    scale = np.abs(ref).max()
+    assert np.abs(z - ref).max() <= 2e-2 * scale
+    assert (z.argmax(1) == ref.argmax(1)).mean() > 0.97
+    r.close()
