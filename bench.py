@@ -87,6 +87,7 @@ def parse():
     ap.add_argument("--train", type=int, default=None)
     ap.add_argument("--cpu-queries-per-thread", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--router-probes", type=int, default=2, help="lists the learned form adds from the router")
     ap.add_argument("--forms", default=None,
                     help="forms to time; the last one listed is the headline (default: per workload)")
     a = ap.parse_args()
@@ -360,7 +361,7 @@ def run_engine(a):
         router_info = {"train_queries": w["train"], "epochs": w["epochs"], "label_s": label_s, "train_s": train_s,
                        "final_loss": loss, "probe_recall_top1": (top1 == test_labels).float().mean().item(),
                        "architecture": f"MLP {w['d']}->512->512->{w['reps']} GELU, BF16 weights, FP32 accumulate"}
-        idx.set_router(router, probes=7)
+        idx.set_router(router, probes=a.router_probes)
 
     modes = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC, "oneshot": pyrbc.QUERY_ONESHOT,
              "learned": pyrbc.QUERY_EXACT_TC | pyrbc.QUERY_ROUTED, "learned_plain": pyrbc.QUERY_EXACT | pyrbc.QUERY_ROUTED}
