@@ -43,7 +43,10 @@ extern "C" {
 #define RBC_L2 0 /* sum of (q-x)^2: squared Euclidean, never square-rooted */
 #define RBC_L1 1 /* sum of |q-x|                                           */
 
-#define RBC_KMAX 32 /* neighbours per query held by the engine (defs.h:9) */
+#define RBC_KMAX 32 /* neighbours per query of the reference's engine (defs.h:9) */
+#define RBC_K_LIMIT 128 /* largest k of rbc_query / rbc_brute_knn; RBC_KMAX for
+                           rbc_query_batch, rbc_brute_knn_noalloc and the
+                           tensor-core search (wider k there takes the FP32 one) */
 
 /* ---- build flags ---- */
 #define RBC_BUILD_PARTITION 1u /* nearest-representative lists for exact search */
@@ -134,7 +137,8 @@ int rbc_get_oneshot(const rbc_index *index, uint32_t *h_lists /* num_reps x s */
 
 /* k-NN of m queries (rows of d floats, stride ldq).  Results are sorted by
  * (distance, id); row i of dIds/dDists (stride ldo >= k) holds query i.
- * Missing neighbours are (FLT_MAX, 0xFFFFFFFF).  1 <= k <= RBC_KMAX. */
+ * Missing neighbours are (FLT_MAX, 0xFFFFFFFF).  1 <= k <= RBC_K_LIMIT; the
+ * tensor-core mode answers k > RBC_KMAX with the FP32 exact search. */
 int rbc_query(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
               uint32_t *dIds, float *dDists, uint32_t ldo, void *stream);
 int rbc_query_host(rbc_index *index, const float *hQ, uint64_t m, uint32_t ldq, uint32_t k,
@@ -207,7 +211,8 @@ int rbc_get_profile(const rbc_index *index, rbc_profile *profile);
 /* Number of kernels this library has launched in this process. */
 uint64_t rbc_kernel_launches(void);
 
-/* Brute-force exact k-NN of every query over every database row. */
+/* Brute-force exact k-NN of every query over every database row;
+ * 1 <= k <= RBC_K_LIMIT. */
 int rbc_brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m,
                   uint32_t ldq, uint32_t d, uint32_t k, int metric, uint32_t *dIds, float *dDists,
                   uint32_t ldo, void *stream);

@@ -4,7 +4,7 @@
 //
 //   testRBC -x db.bin -q queries.bin -n N -m M -d D -r numReps [-o out.bin] [-g gpu] [-b] [-e]
 //   text input/output: -X / -Q / -O in place of -x / -q / -o
-//   extensions: -k K      neighbours per query written (default 32)
+//   extensions: -k K      neighbours per query written (default 32, at most RBC_K_LIMIT = 128)
 //               -M mode   exact (default) | tc (BF16 tensor cores, exact) | oneshot (reference algorithm)
 //               -s seed   representative sampling seed
 //               -l        L1 distance instead of squared L2
@@ -121,8 +121,8 @@ void parse(int argc, char **argv) {
     std::fprintf(stderr, "number of representatives must be at least 32\n");
     std::exit(1);
   }
-  if (k < 1 || k > RBC_KMAX) {
-    std::fprintf(stderr, "k must be in [1, 32].. exiting\n");
+  if (k < 1 || k > RBC_K_LIMIT) {
+    std::fprintf(stderr, "k must be in [1, %d].. exiting\n", RBC_K_LIMIT);
     std::exit(1);
   }
 }
@@ -170,18 +170,21 @@ int main(int argc, char **argv) {
   std::printf("\t.. build time = %6.4f \n", now() - t0);
   if (saveIdx) check(rbc_save(idx, saveIdx), "saving the index");
 
-  std::vector<uint32_t> ids(m * RBC_KMAX);
-  std::vector<float> dists(m * RBC_KMAX);
+  // K columns per query: the reference's 32, or k when more are asked for;
+  // the evaluation reads the first 32
+  const uint32_t K = k > RBC_KMAX ? k : RBC_KMAX;
+  std::vector<uint32_t> ids(m * K);
+  std::vector<float> dists(m * K);
   t0 = now();
-  check(rbc_query_host(idx, q.data(), m, ld, RBC_KMAX, mode, ids.data(), dists.data(), RBC_KMAX), "kqueryRBC");
+  check(rbc_query_host(idx, q.data(), m, ld, K, mode, ids.data(), dists.data(), K), "kqueryRBC");
   std::printf("\t.. query time for krbc = %6.4f \n", now() - t0);
 
   std::vector<uint32_t> bids;
   std::vector<float> bdists;
   if (runBrute || runEval) {
     std::printf("running k-brute force..\n");
-    bids.resize(m * RBC_KMAX);
-    bdists.resize(m * RBC_KMAX);
+    bids.resize(m * K);
+    bdists.resize(m * K);
     void *dx = nullptr, *dq = nullptr, *di = nullptr, *dd = nullptr;
     cudaMalloc(&dx, x.size() * 4);
     cudaMalloc(&dq, q.size() * 4);
@@ -190,8 +193,8 @@ int main(int argc, char **argv) {
     t0 = now();
     cudaMemcpy(dx, x.data(), x.size() * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(dq, q.data(), q.size() * 4, cudaMemcpyHostToDevice);
-    check(rbc_brute_knn((float *)dx, n, ld, (float *)dq, m, ld, d, RBC_KMAX, metric, (uint32_t *)di, (float *)dd,
-                        RBC_KMAX, nullptr),
+    check(rbc_brute_knn((float *)dx, n, ld, (float *)dq, m, ld, d, K, metric, (uint32_t *)di, (float *)dd, K,
+                        nullptr),
           "bruteK");
     cudaMemcpy(bids.data(), di, bids.size() * 4, cudaMemcpyDeviceToHost);
     cudaMemcpy(bdists.data(), dd, bdists.size() * 4, cudaMemcpyDeviceToHost);
@@ -204,14 +207,14 @@ int main(int argc, char **argv) {
       for (uint64_t i = 0; i < m; i++) {
         uint32_t ol = 0;
         for (uint32_t j = 0; j < RBC_KMAX; j++)
-          for (uint32_t t = 0; t < RBC_KMAX; t++) ol += ids[i * RBC_KMAX + j] == bids[i * RBC_KMAX + t];
+          for (uint32_t t = 0; t < RBC_KMAX; t++) ol += ids[i * K + j] == bids[i * K + t];
         sum += ol;
         sum2 += (double)ol * ol;
       }
       double mean = sum / m;
       std::printf("\tavg overlap = %6.4f/%d; std dev = %6.4f \n", mean, RBC_KMAX, std::sqrt(sum2 / m - mean * mean));
       std::vector<float> ranges(m);
-      for (uint64_t i = 0; i < m; i++) ranges[i] = dists[i * RBC_KMAX + RBC_KMAX - 1];
+      for (uint64_t i = 0; i < m; i++) ranges[i] = dists[i * K + RBC_KMAX - 1];
       void *dr = nullptr, *dc = nullptr;
       cudaMalloc(&dr, m * 4);
       cudaMalloc(&dc, m * 4);
@@ -240,8 +243,8 @@ int main(int argc, char **argv) {
   cudaError_t cE = cudaGetLastError();
   if (cE != cudaSuccess) std::printf("Execution failed; error type: %s \n", cudaGetErrorString(cE));
 
-  if (outB) check(rbc_write_neighbors_bin(outB, ids.data(), dists.data(), m, k, RBC_KMAX), "writing the output");
-  if (outT) check(rbc_write_neighbors_text(outT, ids.data(), dists.data(), m, k, RBC_KMAX), "writing the output");
+  if (outB) check(rbc_write_neighbors_bin(outB, ids.data(), dists.data(), m, k, K), "writing the output");
+  if (outT) check(rbc_write_neighbors_text(outT, ids.data(), dists.data(), m, k, K), "writing the output");
   rbc_destroy(idx);
   return 0;
 }

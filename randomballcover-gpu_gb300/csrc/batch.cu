@@ -183,7 +183,7 @@ int prepare(rbc_batch *bt) {
   g.work = bt->ctl;
   g.err = bt->ctl + 2;
   g.dp = dp_max;  // sizes the shared-memory tile of the shared launch
-  g.k = 1;
+  g.k = 1;  // every instance has k <= 32: lists of 32 entries
 
   // launches recorded during capture run only when the graph replays:
   // the launch counter is charged per replay instead
@@ -202,7 +202,7 @@ int prepare(rbc_batch *bt) {
                             b.Dqr.as<float>(), idx->nr, s));
       BCK(launch_row_topp(b.Dqr.as<float>(), in.m, idx->nr, 1, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
       BCK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
-                              b.lock.as<uint32_t>(), in.m, s));
+                              b.lock.as<uint32_t>(), in.m, kListWidth, s));
     }
     for (uint32_t round = 0; round < 2; round++) {
       for (auto &ip : bt->inst)
@@ -217,7 +217,8 @@ int prepare(rbc_batch *bt) {
       BCK(launch_search(metric, g, grid, s, tq));
     }
     for (auto &ip : bt->inst)
-      BCK(launch_write_results(ip->b.res_d.as<float>(), ip->b.res_i.as<uint32_t>(), ip->m, ip->k, ip->ids, ip->dists,
+      BCK(launch_write_results(ip->b.res_d.as<float>(), ip->b.res_i.as<uint32_t>(), ip->m, ip->k, kListWidth, ip->ids,
+                               ip->dists,
                                ip->ldo, s));
     return RBC_OK;
   };

@@ -114,7 +114,7 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
                     int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq, uint32_t qtile_over) {
   const int tqv = tq < 0 ? idx->tune_tq : tq;
-  const uint32_t nr = idx->nr, qtile = qtile_over ? qtile_over : (uint32_t)search_query_tile(idx->dp, tqv);
+  const uint32_t nr = idx->nr, qtile = qtile_over ? qtile_over : (uint32_t)search_query_tile(idx->dp, tqv, list_width_for(k));
   uint32_t *ctl = b.ctl.as<uint32_t>();  // [0] work, [1] nitems, [2] err
   PlanArgs a{};
   a.Dqr = b.Dqr.as<float>();
@@ -378,7 +378,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
 int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
                 uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s) {
   if (!idx) return fail(RBC_ERR_INVALID, "rbc_query: index is NULL");
-  if (k < 1 || k > (uint32_t)kListWidth) return fail(RBC_ERR_INVALID, "rbc_query: k must be in [1, 32]");
+  if (k < 1 || k > (uint32_t)kMaxListWidth) return fail(RBC_ERR_INVALID, "rbc_query: k must be in [1, 128]");
   if (ldo < k) return fail(RBC_ERR_INVALID, "rbc_query: ldo < k");
   if (ldq < idx->d) return fail(RBC_ERR_INVALID, "rbc_query: ldq < d");
   if (m == 0) return RBC_OK;
@@ -401,7 +401,10 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     offsets = idx->os_offsets;
   } else if (base == RBC_QUERY_EXACT_TC) {
     if (!(idx->flags & RBC_BUILD_BF16)) return fail(RBC_ERR_INVALID, "rbc_query: index has no BF16 lists");
-    return query_tc(idx, dQ, m, ldq, k, mode, dIds, dDists, ldo, s);
+    if (k <= kTcMaxK) return query_tc(idx, dQ, m, ldq, k, mode, dIds, dDists, ldo, s);
+    // wider k: the shortlists stop at 56 entries; the FP32 exact search over
+    // the same partition lists answers (a BF16 index always has them)
+    return query_index(idx, dQ, m, ldq, k, (mode & ~0xFFu) | RBC_QUERY_EXACT, dIds, dDists, ldo, s);
   } else {
     return fail(RBC_ERR_INVALID, "rbc_query: unknown mode");
   }
@@ -412,8 +415,9 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   // probe table: the nearest representative, then (routed) the router's picks
   const uint32_t Pn = std::min(kDefaultProbes, nr);
   const uint32_t P = routed ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
-  const uint32_t qtile = (uint32_t)search_query_tile(idx->dp, idx->tune_tq);
-  const int grid = search_grid(idx->metric, idx->dp, idx->tune_tq);
+  const uint32_t kw = list_width_for(k);
+  const uint32_t qtile = (uint32_t)search_query_tile(idx->dp, idx->tune_tq, kw);
+  const int grid = search_grid(idx->metric, idx->dp, idx->tune_tq, kw);
   // batch so the m x nr plan arrays stay near 2^27 entries
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
   QueryBufs b;
@@ -423,8 +427,8 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   CK(b.Dqr.alloc(mb * nr * 4, s));
   CK(b.probe.alloc(mb * P * 4, s));
   CK(b.probed.alloc(mb * P * 4, s));
-  CK(b.res_d.alloc(mb * kListWidth * 4, s));
-  CK(b.res_i.alloc(mb * kListWidth * 4, s));
+  CK(b.res_d.alloc(mb * kw * 4, s));
+  CK(b.res_i.alloc(mb * kw * 4, s));
   CK(b.tau.alloc(mb * 4, s));
   CK(b.lock.alloc(mb * 4, s));
   CK(b.cnt.alloc((nr + 1) * 4, s));
@@ -470,11 +474,11 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
       CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     }
     CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
-                           b.lock.as<uint32_t>(), mq, s));
+                           b.lock.as<uint32_t>(), mq, kw, s));
     TRY(plan_and_search(idx, b, mq, P, k, 0, X, pid, offsets, idx->radius, grid, stats.as<unsigned long long>(), s));
     if (base == RBC_QUERY_EXACT)
       TRY(plan_and_search(idx, b, mq, P, k, 1, X, pid, offsets, idx->radius, grid, stats.as<unsigned long long>(), s));
-    CK(launch_write_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), mq, k, dIds ? dIds + b0 * ldo : nullptr,
+    CK(launch_write_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), mq, k, kw, dIds ? dIds + b0 * ldo : nullptr,
                             dDists ? dDists + b0 * ldo : nullptr, ldo, s));
   }
   idx->stats.queries = m;
@@ -529,7 +533,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   Pn = std::min(Pn, nr);
   const uint32_t P = routed ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
   const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
-  const uint32_t qtile = tc_query_tile(fmt);
+  const uint32_t qtile = tc_query_tile(fmt), kw = kListWidth;
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
   QueryBufs b;
   const uint64_t pair_cap = mb * nr, item_cap = item_capacity(idx, mb, qtile);
@@ -537,8 +541,8 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(b.Dqr.alloc(mb * nr * 4, s));
   CK(b.probe.alloc(mb * P * 4, s));
   CK(b.probed.alloc(mb * P * 4, s));
-  CK(b.res_d.alloc(mb * kListWidth * 4, s));
-  CK(b.res_i.alloc(mb * kListWidth * 4, s));
+  CK(b.res_d.alloc(mb * kw * 4, s));
+  CK(b.res_i.alloc(mb * kw * 4, s));
   CK(b.tau.alloc(mb * 4, s));
   CK(b.lock.alloc(mb * 4, s));
   CK(b.cnt.alloc((nr + 1) * 4, s));
@@ -608,7 +612,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     }
     CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(),
-                           mq, s));
+                           mq, kw, s));
     // query operands (row mq is the zero row gathered for empty item slots)
     CK(launch_tc_queries(b.Qp.as<float>(), ld, mq, idx->d, kp, fmt, idx->tc.mu, Qh.p, qscale.as<float>(),
                          qnorm.as<float>(), qinex.as<uint8_t>(), s));
@@ -736,7 +740,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
 int brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,
               uint32_t k, int metric, uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s) {
   TRY(check_dims(d, std::min(ldx, ldq), "rbc_brute_knn"));
-  if (k < 1 || k > (uint32_t)kListWidth) return fail(RBC_ERR_INVALID, "rbc_brute_knn: k must be in [1, 32]");
+  if (k < 1 || k > (uint32_t)kMaxListWidth) return fail(RBC_ERR_INVALID, "rbc_brute_knn: k must be in [1, 128]");
   if (ldo < k) return fail(RBC_ERR_INVALID, "rbc_brute_knn: ldo < k");
   if (metric != RBC_L2 && metric != RBC_L1) return fail(RBC_ERR_INVALID, "rbc_brute_knn: unknown metric");
   if (m == 0) return RBC_OK;
@@ -744,13 +748,14 @@ int brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64
   if (n >= 0xFFFFFFFFull || m >= 0xFFFFFFFFull) return fail(RBC_ERR_INVALID, "rbc_brute_knn: n, m must be below 2^32-1");
   pool_setup();
   const uint32_t ld = pad16(d), dp = pad4(d);
-  const uint32_t qtile = (uint32_t)search_query_tile(dp);
-  const int grid = search_grid(metric, dp);
+  const uint32_t kw = list_width_for(k);
+  const uint32_t qtile = (uint32_t)search_query_tile(dp, 0, kw);
+  const int grid = search_grid(metric, dp, 0, kw);
   DevBuf Xp, Qp, res_d, res_i, tau, lock, qidx, items, ctl;
   CK(Xp.alloc(std::max<uint64_t>(n, 1) * ld * 4, s));
   CK(Qp.alloc(m * ld * 4, s));
-  CK(res_d.alloc(m * kListWidth * 4, s));
-  CK(res_i.alloc(m * kListWidth * 4, s));
+  CK(res_d.alloc(m * kw * 4, s));
+  CK(res_i.alloc(m * kw * 4, s));
   CK(tau.alloc(m * 4, s));
   CK(lock.alloc(m * 4, s));
   CK(qidx.alloc(m * 4, s));
@@ -758,7 +763,7 @@ int brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64
   CK(cudaMemsetAsync(ctl.p, 0, 64, s));
   CK(launch_pad_rows(dX, ldx, Xp.as<float>(), ld, n, d, s));
   CK(launch_pad_rows(dQ, ldq, Qp.as<float>(), ld, m, d, s));
-  CK(launch_init_results(res_d.as<float>(), res_i.as<uint32_t>(), tau.as<uint32_t>(), lock.as<uint32_t>(), m, s));
+  CK(launch_init_results(res_d.as<float>(), res_i.as<uint32_t>(), tau.as<uint32_t>(), lock.as<uint32_t>(), m, kw, s));
   const uint64_t qtiles = (m + qtile - 1) / qtile;
   uint64_t nchunks = std::max<uint64_t>(1, (4ull * grid + qtiles - 1) / qtiles);
   nchunks = std::min<uint64_t>(nchunks, std::max<uint64_t>(1, n / 256));
@@ -787,7 +792,7 @@ int brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64
   sa.dp = dp;
   sa.k = k;
   if (n) CK(launch_search(metric, sa, grid, s));
-  CK(launch_write_results(res_d.as<float>(), res_i.as<uint32_t>(), m, k, dIds, dDists, ldo, s));
+  CK(launch_write_results(res_d.as<float>(), res_i.as<uint32_t>(), m, k, kw, dIds, dDists, ldo, s));
   uint32_t hctl[3];
   CK(cudaMemcpyAsync(hctl, ctl.p, sizeof(hctl), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));

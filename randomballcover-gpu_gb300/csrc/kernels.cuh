@@ -37,7 +37,7 @@ struct SearchArgs {
   const SearchItem *items;
   const uint32_t *nitems; // device-side item count
   uint32_t *work;         // work counter, zero at launch
-  float *res_d;           // per-query lists [m][32], sorted by (dist, id)
+  float *res_d;           // per-query lists [m][KW], sorted by (dist, id); KW = list_width_for(k)
   uint32_t *res_i;
   uint32_t *tau;          // per-query k-th distance (float bits)
   uint32_t *lock;         // per-query lock words, zero at rest
@@ -49,19 +49,20 @@ struct SearchArgs {
   const SearchArgs *insts;
 };
 
-// Tile geometry of the list-search kernel for a dimensionality.
-// Tile geometry of the list-search kernel for a dimensionality; tq (1, 2, 4)
-// overrides the default rows-per-thread when it fits, 0 keeps the default.
-int search_tq_for(uint32_t dp, int tq = 0);
-int search_query_tile(uint32_t dp, int tq = 0);  // 16 * TQ
-size_t search_smem_bytes(uint32_t dp, int tq = 0);
+// Tile geometry of the list-search kernel for a dimensionality and list
+// width kw (32, 64, 128); tq (1, 2, 4) overrides the default rows-per-thread
+// when it fits, 0 keeps the default.  launch_search takes kw from a.k.
+int search_tq_for(uint32_t dp, int tq = 0, uint32_t kw = 32);
+int search_query_tile(uint32_t dp, int tq = 0, uint32_t kw = 32);  // 16 * TQ
+size_t search_smem_bytes(uint32_t dp, int tq = 0, uint32_t kw = 32);
 cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_t s, int tq = 0);
-int search_grid(int metric, uint32_t dp, int tq = 0);
+int search_grid(int metric, uint32_t dp, int tq = 0, uint32_t kw = 32);
 
+// Per-query lists of kw entries: m x kw (dist, id) pairs, tau and lock words.
 cudaError_t launch_init_results(float *res_d, uint32_t *res_i, uint32_t *tau, uint32_t *lock,
-                                uint64_t m, cudaStream_t s);
+                                uint64_t m, uint32_t kw, cudaStream_t s);
 cudaError_t launch_write_results(const float *res_d, const uint32_t *res_i, uint64_t m, uint32_t k,
-                                 uint32_t *ids, float *dists, uint32_t ldo, cudaStream_t s);
+                                 uint32_t kw, uint32_t *ids, float *dists, uint32_t ldo, cudaStream_t s);
 // ids[rows[r] * ldo + j] = src_i[r * k + j] (and the distances likewise).
 cudaError_t launch_scatter_results(const uint32_t *src_i, const float *src_d, const uint32_t *rows,
                                    uint32_t nrows, uint32_t k, uint32_t *ids, float *dists, uint32_t ldo,

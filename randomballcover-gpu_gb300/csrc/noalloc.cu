@@ -126,7 +126,7 @@ extern "C" int rbc_brute_knn_noalloc(const float *dX, uint64_t n, uint32_t ldx, 
 
   // the array keeps the previous call's contents: reset what must start at zero
   cudaError_t e = cudaMemsetAsync(ctl, 0, 64, s);
-  if (e == cudaSuccess) e = launch_init_results(res_d, res_i, tau, lock, m, s);
+  if (e == cudaSuccess) e = launch_init_results(res_d, res_i, tau, lock, m, kListWidth, s);
   if (e == cudaSuccess) e = launch_brute_items(items, ctl + 1, qidx, n, chunk, m, qtile, s);
   if (e != cudaSuccess) return cuda_fail(e, "rbc_brute_knn_noalloc: set-up launches");
   SearchArgs sa{};
@@ -151,7 +151,7 @@ extern "C" int rbc_brute_knn_noalloc(const float *dX, uint64_t n, uint32_t ldx, 
     e = launch_search(metric, sa, grid, s);
     if (e != cudaSuccess) return cuda_fail(e, "rbc_brute_knn_noalloc: search launch");
   }
-  e = launch_write_results(res_d, res_i, m, k, dIds, dDists, ldo, s);
+  e = launch_write_results(res_d, res_i, m, k, kListWidth, dIds, dDists, ldo, s);
   if (e != cudaSuccess) return cuda_fail(e, "rbc_brute_knn_noalloc: result launch");
   uint32_t err_word = 0;
   e = cudaMemcpyAsync(&err_word, ctl + 2, sizeof(err_word), cudaMemcpyDeviceToHost, s);

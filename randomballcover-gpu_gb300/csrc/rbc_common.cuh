@@ -91,6 +91,95 @@ __device__ __forceinline__ void warp_merge_into(float &ld, uint32_t &li, float c
   warp_bitonic_merge32(ld, li);
 }
 
+// Lists of KW = 32 W pairs held by a warp, W per lane: entry 32 w + lane is
+// register w of that lane, the whole list ascending.
+constexpr int kMaxListWidth = 128;
+inline uint32_t list_width_for(uint32_t k) { return k <= 32 ? 32 : (k <= 64 ? 64 : 128); }
+
+// Merge 32 unsorted candidates (one per lane) into a sorted KW-entry list,
+// keeping the KW smallest pairs.  Every entry of the first KW - 32 stays (at
+// most 32 + KW - 33 pairs can precede it), so the candidates compete only with
+// the last 32: u = the 32 smallest of (last block, candidates); then u is
+// merged down through the earlier blocks, each merge of two sorted 32-blocks
+// passing its upper half up.
+template <int W>
+__device__ __forceinline__ void warp_merge_into_w(float (&ld)[W], uint32_t (&li)[W], float cd, uint32_t ci) {
+  const int lane = threadIdx.x & 31;
+  warp_sort32(cd, ci);
+  float ud = __shfl_sync(0xffffffffu, cd, 31 - lane);
+  uint32_t ui = __shfl_sync(0xffffffffu, ci, 31 - lane);
+  if (!pair_less(ud, ui, ld[W - 1], li[W - 1])) {
+    ud = ld[W - 1];
+    ui = li[W - 1];
+  }
+  warp_bitonic_merge32(ud, ui);
+#pragma unroll
+  for (int j = W - 2; j >= 0; j--) {
+    const float rd = __shfl_sync(0xffffffffu, ud, 31 - lane);
+    const uint32_t ri = __shfl_sync(0xffffffffu, ui, 31 - lane);
+    float hd, lo_d;
+    uint32_t hi, lo_i;
+    if (pair_less(rd, ri, ld[j], li[j])) {
+      lo_d = rd;
+      lo_i = ri;
+      hd = ld[j];
+      hi = li[j];
+    } else {
+      lo_d = ld[j];
+      lo_i = li[j];
+      hd = rd;
+      hi = ri;
+    }
+    warp_bitonic_merge32(lo_d, lo_i);
+    warp_bitonic_merge32(hd, hi);
+    ld[j + 1] = hd;
+    li[j + 1] = hi;
+    ud = lo_d;
+    ui = lo_i;
+  }
+  ld[0] = ud;
+  li[0] = ui;
+}
+
+// g := the KW smallest pairs of two sorted KW-entry lists g and l, sorted:
+// the elementwise minimum of g and reversed l is bitonic; a bitonic merge
+// over KW entries (blocks compared within the lane, then lanes by shuffles)
+// sorts it.
+template <int W>
+__device__ __forceinline__ void warp_merge_lists_w(float (&gd)[W], uint32_t (&gi)[W], const float (&ld)[W],
+                                                   const uint32_t (&li)[W]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int w = 0; w < W; w++) {
+    const float rd = __shfl_sync(0xffffffffu, ld[W - 1 - w], 31 - lane);
+    const uint32_t ri = __shfl_sync(0xffffffffu, li[W - 1 - w], 31 - lane);
+    if (pair_less(rd, ri, gd[w], gi[w])) {
+      gd[w] = rd;
+      gi[w] = ri;
+    }
+  }
+  constexpr int kLog2W = W >= 4 ? 2 : (W >= 2 ? 1 : 0);
+  static_assert((1 << kLog2W) == W, "W must be 1, 2 or 4");
+#pragma unroll
+  for (int t = 0; t < kLog2W; t++) {
+    const int jb = (W >> 1) >> t;
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+      const int p = w ^ jb;
+      if (p > w && pair_less(gd[p], gi[p], gd[w], gi[w])) {
+        const float td = gd[w];
+        const uint32_t ti = gi[w];
+        gd[w] = gd[p];
+        gi[w] = gi[p];
+        gd[p] = td;
+        gi[p] = ti;
+      }
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < W; w++) warp_bitonic_merge32(gd[w], gi[w]);
+}
+
 // Error word shared by kernels that bound their waits: the first error wins.
 __device__ __forceinline__ void raise_error(uint32_t *err, uint32_t code) {
   if (err) atomicCAS(err, 0u, code);

@@ -2,7 +2,8 @@
 //
 // Counterpart of planKNNKernel / planNNKernel / knnKernel (kernels.cu:15-282
 // of the reference): queries are compared against runs of database rows and a
-// sorted 32-entry (dist, id) list is kept per query.  GB300 design:
+// sorted (dist, id) list of KW = 32, 64 or 128 entries (the smallest width
+// >= k) is kept per query.  GB300 design:
 //   * persistent CTAs pull SearchItems from a device work counter, so no host
 //     round trip sits between the plan and the search and the whole query
 //     pipeline can run inside one CUDA graph;
@@ -15,6 +16,8 @@
 //     place of the reference's shared-memory Batcher network (kernels.cu:479-625);
 //   * each CTA merges its lists into the global per-query lists under a short
 //     per-query lock whose wait is bounded (error word, never a hang).
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "tile.cuh"
 
@@ -23,15 +26,18 @@ namespace rbc {
 namespace {
 
 constexpr uint32_t kLockSpinLimit = 1u << 22;
+// Largest tile that still lets two search CTAs share an SM (228 KB per SM,
+// 1 KB reserved per CTA).
+constexpr size_t kTwoCtaSmem = 113 * 1024;
 
 struct SearchSmem {
   float *Qs, *Xs0, *Xs1, *cand_d, *list_d, *tau_s;
   uint32_t *cand_i, *list_i, *cand_n;
 };
 
-template <int TQ>
+template <int TQ, int W>
 __device__ __forceinline__ SearchSmem carve(unsigned char *base, uint32_t S) {
-  constexpr int BQ = 16 * TQ;
+  constexpr int BQ = 16 * TQ, KW = 32 * W;
   SearchSmem sm;
   float *f = reinterpret_cast<float *>(base);
   sm.Qs = f;
@@ -43,32 +49,39 @@ __device__ __forceinline__ SearchSmem carve(unsigned char *base, uint32_t S) {
   sm.cand_d = f;
   f += BQ * kTileCols;
   sm.list_d = f;
-  f += BQ * kListWidth;
+  f += BQ * KW;
   sm.tau_s = f;
   f += BQ;
   uint32_t *u = reinterpret_cast<uint32_t *>(f);
   sm.cand_i = u;
   u += BQ * kTileCols;
   sm.list_i = u;
-  u += BQ * kListWidth;
+  u += BQ * KW;
   sm.cand_n = u;
   return sm;
 }
 
-template <int TQ>
-size_t smem_bytes_tq(uint32_t dp) {
-  constexpr int BQ = 16 * TQ;
-  uint32_t S = dp + 4;
-  size_t floats = (size_t)BQ * S + 2 * kTileCols * S + BQ * kTileCols + BQ * kListWidth + BQ;
-  size_t words = (size_t)BQ * kTileCols + BQ * kListWidth + BQ;
+size_t smem_bytes(int tq, uint32_t dp, uint32_t kw) {
+  const size_t BQ = 16 * (size_t)tq, S = dp + 4;
+  size_t floats = BQ * S + 2 * kTileCols * S + BQ * kTileCols + BQ * kw + BQ;
+  size_t words = BQ * kTileCols + BQ * kw + BQ;
   return (floats + words) * 4;
+}
+
+// The kth entry (0-based) of a KW list held W registers per lane.
+template <int W>
+__device__ __forceinline__ float list_entry(const float (&ld)[W], uint32_t kth) {
+  float v = ld[0];
+#pragma unroll
+  for (int w = 1; w < W; w++) v = kth >= 32u * w ? ld[w] : v;  // selects, no indexed local array
+  return __shfl_sync(0xffffffffu, v, kth & 31);
 }
 
 // g holds the work queue; each item's data come from g itself or, in a
 // batched launch over many independent indexes, from g.insts[item.inst].
-template <int METRIC, int TQ>
+template <int METRIC, int TQ, int W>
 __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_constant__ SearchArgs g) {
-  constexpr int BQ = 16 * TQ;
+  constexpr int BQ = 16 * TQ, KW = 32 * W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ uint32_t s_item;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -83,7 +96,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_co
     const SearchItem item = g.items[it];
     const SearchArgs &a = g.insts ? g.insts[item.inst] : g;
     const uint32_t S = a.dp + 4;
-    const SearchSmem sm = carve<TQ>(smem_raw, S);
+    const SearchSmem sm = carve<TQ, W>(smem_raw, S);
     const uint32_t kk = a.k;
 
     // ---- stage the query tile, thresholds and empty lists ----
@@ -98,7 +111,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_co
       sm.tau_s[t] = ts;
       sm.cand_n[t] = 0;
     }
-    for (uint32_t t = tid; t < BQ * kListWidth; t += kTileThreads) {
+    for (uint32_t t = tid; t < BQ * KW; t += kTileThreads) {
       sm.list_d[t] = FLT_MAX;
       sm.list_i[t] = RBC_DUMMY;
     }
@@ -156,8 +169,13 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_co
       for (int slot = warp; slot < BQ; slot += kTileThreads / 32) {
         const uint32_t n = sm.cand_n[slot];
         if (n == 0) continue;
-        float ld = sm.list_d[slot * kListWidth + lane];
-        uint32_t li = sm.list_i[slot * kListWidth + lane];
+        float ld[W];
+        uint32_t li[W];
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+          ld[w] = sm.list_d[slot * KW + 32 * w + lane];
+          li[w] = sm.list_i[slot * KW + 32 * w + lane];
+        }
         for (uint32_t b = 0; b < n; b += 32) {
           float cd = FLT_MAX;
           uint32_t ci = RBC_DUMMY;
@@ -165,11 +183,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_co
             cd = sm.cand_d[slot * kTileCols + b + lane];
             ci = sm.cand_i[slot * kTileCols + b + lane];
           }
-          warp_merge_into(ld, li, cd, ci);
+          warp_merge_into_w<W>(ld, li, cd, ci);
         }
-        sm.list_d[slot * kListWidth + lane] = ld;
-        sm.list_i[slot * kListWidth + lane] = li;
-        float kth = __shfl_sync(0xffffffffu, ld, kk - 1);
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+          sm.list_d[slot * KW + 32 * w + lane] = ld[w];
+          sm.list_i[slot * KW + 32 * w + lane] = li[w];
+        }
+        const float kth = list_entry<W>(ld, kk - 1);
         if (lane == 0) {
           sm.cand_n[slot] = 0;
           if (kth < sm.tau_s[slot]) sm.tau_s[slot] = kth;
@@ -186,10 +207,17 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_co
     for (int slot = warp; slot < (int)item.nq; slot += kTileThreads / 32) {
       if (sm.tau_s[slot] < 0.f) continue;
       const uint32_t q = a.qidx[item.q0 + slot];
-      float cd = (lane < (int)kk) ? sm.list_d[slot * kListWidth + lane] : FLT_MAX;
-      uint32_t ci = (lane < (int)kk) ? sm.list_i[slot * kListWidth + lane] : RBC_DUMMY;
-      float first = __shfl_sync(0xffffffffu, cd, 0);
-      uint32_t first_id = __shfl_sync(0xffffffffu, ci, 0);
+      // the slot's list cut to k entries (still sorted: the tail is the maximum pair)
+      float cd[W];
+      uint32_t ci[W];
+#pragma unroll
+      for (int w = 0; w < W; w++) {
+        const bool keep = 32 * w + lane < (int)kk;
+        cd[w] = keep ? sm.list_d[slot * KW + 32 * w + lane] : FLT_MAX;
+        ci[w] = keep ? sm.list_i[slot * KW + 32 * w + lane] : RBC_DUMMY;
+      }
+      float first = __shfl_sync(0xffffffffu, cd[0], 0);
+      uint32_t first_id = __shfl_sync(0xffffffffu, ci[0], 0);
       float gtau = __shfl_sync(0xffffffffu, __uint_as_float(__ldcg(a.tau + q)), 0);
       if (first_id == RBC_DUMMY || first > gtau) continue;
       int got = 0;
@@ -205,12 +233,20 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_co
       got = __shfl_sync(0xffffffffu, got, 0);
       if (!got) continue;
       __threadfence();
-      float gd = __ldcg(a.res_d + (uint64_t)q * kListWidth + lane);
-      uint32_t gi = __ldcg(a.res_i + (uint64_t)q * kListWidth + lane);
-      warp_merge_into(gd, gi, cd, ci);
-      a.res_d[(uint64_t)q * kListWidth + lane] = gd;
-      a.res_i[(uint64_t)q * kListWidth + lane] = gi;
-      float kth = __shfl_sync(0xffffffffu, gd, kk - 1);
+      float gd[W];
+      uint32_t gi[W];
+#pragma unroll
+      for (int w = 0; w < W; w++) {
+        gd[w] = __ldcg(a.res_d + (uint64_t)q * KW + 32 * w + lane);
+        gi[w] = __ldcg(a.res_i + (uint64_t)q * KW + 32 * w + lane);
+      }
+      warp_merge_lists_w<W>(gd, gi, cd, ci);
+#pragma unroll
+      for (int w = 0; w < W; w++) {
+        a.res_d[(uint64_t)q * KW + 32 * w + lane] = gd[w];
+        a.res_i[(uint64_t)q * KW + 32 * w + lane] = gi[w];
+      }
+      const float kth = list_entry<W>(gd, kk - 1);
       __threadfence();
       if (lane == 0) {
         atomicMin(a.tau + q, fbits(kth));
@@ -226,23 +262,23 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_co
   }
 }
 
-template <int METRIC, int TQ>
+template <int METRIC, int TQ, int W>
 cudaError_t launch_tq(const SearchArgs &a, int grid, cudaStream_t s) {
-  size_t smem = smem_bytes_tq<TQ>(a.dp);
-  cudaError_t e = cudaFuncSetAttribute(search_kernel<METRIC, TQ>,
+  size_t smem = smem_bytes(TQ, a.dp, 32 * W);
+  cudaError_t e = cudaFuncSetAttribute(search_kernel<METRIC, TQ, W>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  search_kernel<METRIC, TQ><<<grid, kTileThreads, smem, s>>>(a);
+  search_kernel<METRIC, TQ, W><<<grid, kTileThreads, smem, s>>>(a);
   return launched();
 }
 
-template <int METRIC, int TQ>
+template <int METRIC, int TQ, int W>
 int grid_tq(uint32_t dp) {
-  size_t smem = smem_bytes_tq<TQ>(dp);
-  cudaFuncSetAttribute(search_kernel<METRIC, TQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  size_t smem = smem_bytes(TQ, dp, 32 * W);
+  cudaFuncSetAttribute(search_kernel<METRIC, TQ, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem);
   int per_sm = 0, dev = 0, sms = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, search_kernel<METRIC, TQ>, kTileThreads,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, search_kernel<METRIC, TQ, W>, kTileThreads,
                                                 smem);
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -251,9 +287,9 @@ int grid_tq(uint32_t dp) {
 }
 
 __global__ void init_results_kernel(float *res_d, uint32_t *res_i, uint32_t *tau, uint32_t *lock,
-                                    uint64_t m) {
+                                    uint64_t m, uint32_t kw) {
   uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (i < m * kListWidth) {
+  if (i < m * kw) {
     res_d[i] = FLT_MAX;
     res_i[i] = RBC_DUMMY;
   }
@@ -264,13 +300,13 @@ __global__ void init_results_kernel(float *res_d, uint32_t *res_i, uint32_t *tau
 }
 
 __global__ void write_results_kernel(const float *res_d, const uint32_t *res_i, uint64_t m, uint32_t k,
-                                     uint32_t *ids, float *dists, uint32_t ldo) {
+                                     uint32_t kw, uint32_t *ids, float *dists, uint32_t ldo) {
   uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (i >= m * k) return;
   uint64_t q = i / k;
   uint32_t j = (uint32_t)(i - q * k);
-  if (ids) ids[q * ldo + j] = res_i[q * kListWidth + j];
-  if (dists) dists[q * ldo + j] = res_d[q * kListWidth + j];
+  if (ids) ids[q * ldo + j] = res_i[q * kw + j];
+  if (dists) dists[q * ldo + j] = res_d[q * kw + j];
 }
 
 __global__ void scatter_results_kernel(const uint32_t *src_i, const float *src_d, const uint32_t *rows, uint32_t nrows,
@@ -307,49 +343,65 @@ __global__ void brute_items_kernel(SearchItem *items, uint32_t *nitems, uint32_t
 
 // Rows per thread in the query dimension (query tile = 16 TQ).  The default
 // keeps the shared-memory tile under ~100 KB; `tq` (1, 2 or 4) overrides it
-// when that tile still fits (the autotuner's knob).
-int search_tq_for(uint32_t dp, int tq) {
-  if ((tq == 1 || tq == 2 || tq == 4) && (tq == 1 || dp <= 256 / (tq / 2))) return tq;
-  return dp <= 128 ? 4 : (dp <= 256 ? 2 : 1);
-}
-int search_query_tile(uint32_t dp, int tq) { return 16 * search_tq_for(dp, tq); }
-
-size_t search_smem_bytes(uint32_t dp, int tq) {
-  switch (search_tq_for(dp, tq)) {
-    case 4: return smem_bytes_tq<4>(dp);
-    case 2: return smem_bytes_tq<2>(dp);
-    default: return smem_bytes_tq<1>(dp);
+// when that tile still fits (the autotuner's knob).  Wider lists (kw 64, 128)
+// take TQ <= 2, halved further while the tile would keep two CTAs off an SM.
+int search_tq_for(uint32_t dp, int tq, uint32_t kw) {
+  int t = (tq == 1 || tq == 2 || tq == 4) && (tq == 1 || dp <= 256 / (tq / 2))
+              ? tq
+              : (dp <= 128 ? 4 : (dp <= 256 ? 2 : 1));
+  if (kw > 32) {
+    t = std::min(t, 2);
+    while (t > 1 && smem_bytes(t, dp, kw) > kTwoCtaSmem) t /= 2;
   }
+  return t;
+}
+int search_query_tile(uint32_t dp, int tq, uint32_t kw) { return 16 * search_tq_for(dp, tq, kw); }
+
+size_t search_smem_bytes(uint32_t dp, int tq, uint32_t kw) {
+  return smem_bytes(search_tq_for(dp, tq, kw), dp, list_width_for(kw));
 }
 
-int search_grid(int metric, uint32_t dp, int tq) {
-  int tqv = search_tq_for(dp, tq);
-  if (metric == RBC_L1)
-    return tqv == 4 ? grid_tq<RBC_L1, 4>(dp) : tqv == 2 ? grid_tq<RBC_L1, 2>(dp) : grid_tq<RBC_L1, 1>(dp);
-  return tqv == 4 ? grid_tq<RBC_L2, 4>(dp) : tqv == 2 ? grid_tq<RBC_L2, 2>(dp) : grid_tq<RBC_L2, 1>(dp);
+#define RBC_SEARCH_DISPATCH(metric, tqv, w, FN, ...)                                                   \
+  do {                                                                                                 \
+    if ((w) == 1) {                                                                                    \
+      if ((metric) == RBC_L1)                                                                          \
+        return (tqv) == 4 ? FN<RBC_L1, 4, 1>(__VA_ARGS__)                                              \
+                          : (tqv) == 2 ? FN<RBC_L1, 2, 1>(__VA_ARGS__) : FN<RBC_L1, 1, 1>(__VA_ARGS__); \
+      return (tqv) == 4 ? FN<RBC_L2, 4, 1>(__VA_ARGS__)                                                \
+                        : (tqv) == 2 ? FN<RBC_L2, 2, 1>(__VA_ARGS__) : FN<RBC_L2, 1, 1>(__VA_ARGS__);   \
+    }                                                                                                  \
+    if ((w) == 2) {                                                                                    \
+      if ((metric) == RBC_L1) return (tqv) == 2 ? FN<RBC_L1, 2, 2>(__VA_ARGS__) : FN<RBC_L1, 1, 2>(__VA_ARGS__); \
+      return (tqv) == 2 ? FN<RBC_L2, 2, 2>(__VA_ARGS__) : FN<RBC_L2, 1, 2>(__VA_ARGS__);               \
+    }                                                                                                  \
+    if ((metric) == RBC_L1) return (tqv) == 2 ? FN<RBC_L1, 2, 4>(__VA_ARGS__) : FN<RBC_L1, 1, 4>(__VA_ARGS__); \
+    return (tqv) == 2 ? FN<RBC_L2, 2, 4>(__VA_ARGS__) : FN<RBC_L2, 1, 4>(__VA_ARGS__);                 \
+  } while (0)
+
+int search_grid(int metric, uint32_t dp, int tq, uint32_t kw) {
+  const uint32_t w = list_width_for(kw) / 32;
+  const int tqv = search_tq_for(dp, tq, 32 * w);
+  RBC_SEARCH_DISPATCH(metric, tqv, w, grid_tq, dp);
 }
 
 cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_t s, int tq) {
-  int tqv = search_tq_for(a.dp, tq);
-  if (metric == RBC_L1)
-    return tqv == 4 ? launch_tq<RBC_L1, 4>(a, grid, s)
-                    : tqv == 2 ? launch_tq<RBC_L1, 2>(a, grid, s) : launch_tq<RBC_L1, 1>(a, grid, s);
-  return tqv == 4 ? launch_tq<RBC_L2, 4>(a, grid, s)
-                  : tqv == 2 ? launch_tq<RBC_L2, 2>(a, grid, s) : launch_tq<RBC_L2, 1>(a, grid, s);
+  const uint32_t w = list_width_for(a.k) / 32;
+  const int tqv = search_tq_for(a.dp, tq, 32 * w);
+  RBC_SEARCH_DISPATCH(metric, tqv, w, launch_tq, a, grid, s);
 }
 
 cudaError_t launch_init_results(float *res_d, uint32_t *res_i, uint32_t *tau, uint32_t *lock,
-                                uint64_t m, cudaStream_t s) {
-  uint64_t total = m * kListWidth;
-  init_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(res_d, res_i, tau, lock, m);
+                                uint64_t m, uint32_t kw, cudaStream_t s) {
+  uint64_t total = std::max<uint64_t>(m * kw, 1);
+  init_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(res_d, res_i, tau, lock, m, kw);
   return launched();
 }
 
 cudaError_t launch_write_results(const float *res_d, const uint32_t *res_i, uint64_t m, uint32_t k,
-                                 uint32_t *ids, float *dists, uint32_t ldo, cudaStream_t s) {
+                                 uint32_t kw, uint32_t *ids, float *dists, uint32_t ldo, cudaStream_t s) {
   uint64_t total = m * k;
   if (total == 0) return cudaSuccess;
-  write_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(res_d, res_i, m, k, ids,
+  write_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(res_d, res_i, m, k, kw, ids,
                                                                        dists, ldo);
   return launched();
 }

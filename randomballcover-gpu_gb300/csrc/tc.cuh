@@ -13,6 +13,8 @@ namespace rbc {
 // Rows kept per query by the tensor pass: 4k, at least 40 and at most 56 (the
 // warp merge holds 64 pairs: the list plus one lane's 8 candidates).
 constexpr uint32_t kShortlistMin = 40, kShortlistMax = 56;
+// Largest k the tensor pass answers; wider queries take the FP32 search.
+constexpr uint32_t kTcMaxK = 32;
 inline uint32_t tc_shortlist(uint32_t k) {
   const uint32_t s = 4 * k;
   return s < kShortlistMin ? kShortlistMin : (s > kShortlistMax ? kShortlistMax : s);

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "librbcgb.so")
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_ITER_LIMIT, ERR_UNSUPPORTED, ERR_IO = range(7)
 L2, L1 = 0, 1
 KMAX = 32
+K_LIMIT = 128  # largest k of query / brute_knn (KMAX for batches and the no-alloc call)
 BUILD_PARTITION, BUILD_ONESHOT, BUILD_BF16 = 1, 2, 4
 QUERY_EXACT, QUERY_ONESHOT, QUERY_EXACT_TC = 0, 1, 2
 TC_BF16, TC_FP16_SPLIT = 0, 1

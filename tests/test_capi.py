@@ -77,7 +77,8 @@ def test_status_strings_and_argument_errors(engine_lib):
     assert L.rbc_build(x.ctypes.data, 10, 4, 4, C.byref(p), None, C.byref(h)) == engine_lib.ERR_INVALID
     assert L.rbc_query(None, None, 1, 4, 1, 0, None, None, 1, None) == engine_lib.ERR_INVALID
     assert L.rbc_brute_knn(None, 1, 4, None, 1, 4, 4, 0, 0, None, None, 1, None) == engine_lib.ERR_INVALID
-    assert L.rbc_brute_knn(None, 1, 4, None, 1, 4, 4, 33, 0, None, None, 33, None) == engine_lib.ERR_INVALID
+    assert L.rbc_brute_knn(None, 1, 4, None, 1, 4, 4, 129, 0, None, None, 129, None) == engine_lib.ERR_INVALID
+    assert b"[1, 128]" in L.rbc_last_error()
     assert L.rbc_synth(9, 0, 0, 0, 1, 4, 4, None, 1, 0.0, 0.0, None) == engine_lib.ERR_INVALID
     assert L.rbc_destroy(None) == 0
 
