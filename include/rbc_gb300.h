@@ -55,6 +55,7 @@ extern "C" {
                                   rows centered on their representative, in BF16
                                   when every value is exact in it, else FP16
                                   hi + lo halves (RBC_TC_* in rbc_index_info)     */
+#define RBC_BUILD_F64 8u       /* set (never passed) on indexes built by rbc_build_f64 */
 
 /* ---- tensor-core operand formats (rbc_index_info.tc_format) ---- */
 #define RBC_TC_BF16 0u       /* one BF16 product per pair (data exact in BF16)   */
@@ -103,7 +104,8 @@ typedef struct {               /* work done by the last rbc_query on an index */
   uint64_t rep_pairs;          /* query-to-representative distances           */
   uint64_t lists_probed;       /* (query, list) pairs searched                */
   uint64_t point_pairs;        /* (query, point) distances computed in lists  */
-  uint64_t fallback_queries;   /* tensor-core mode: queries recomputed in FP32 */
+  uint64_t fallback_queries;   /* tensor-core mode: queries recomputed in FP32;
+                                  rbc_query_f64: queries searched in double    */
 } rbc_query_stats;
 
 const char *rbc_status_string(int status);
@@ -235,6 +237,38 @@ int rbc_brute_knn_noalloc(const float *dX, uint64_t n, uint32_t ldx, const float
 int rbc_brute_range_count(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m,
                           uint32_t ldq, uint32_t d, int metric, const float *dRanges,
                           uint32_t *dCounts, void *stream);
+
+/* ---- double-precision variant: the reference built with real = double
+ * (defs.h:27-31, readme.txt:134-152).  Inputs, distances and results are
+ * double, equal to the double build's sequential arithmetic (each subtract,
+ * multiply and add rounded to double; ties to the lower id).  The FP32 engine
+ * searches float-rounded copies for a shortlist of max(2k, k+16) rows per
+ * query (at most 128), the shortlist is reranked in double, and a certified
+ * error bound proves the double top k lies inside it; a query the bound
+ * cannot settle is searched in double over the whole database.  Missing
+ * neighbours are (DBL_MAX, 0xFFFFFFFF).  1 <= k <= RBC_K_LIMIT. */
+/* Index over n double rows (stride ldx).  Values must be finite and within
+ * +-2^56 (else RBC_ERR_UNSUPPORTED); RBC_BUILD_ONESHOT is not available.  The
+ * index keeps a double copy of the rows (n x d x 8 bytes) besides the FP32
+ * structures; info.flags carries RBC_BUILD_F64.  rbc_query refuses it. */
+int rbc_build_f64(const double *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *params,
+                  void *stream, rbc_index **out);
+/* Exact k-NN in double over an rbc_build_f64 index: mode RBC_QUERY_EXACT or
+ * RBC_QUERY_EXACT_TC (optionally | RBC_QUERY_ROUTED) selects the FP32 search
+ * behind the shortlists.  rbc_get_query_stats' fallback_queries counts the
+ * queries searched in double. */
+int rbc_query_f64(rbc_index *index, const double *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
+                  uint32_t *dIds, double *dDists, uint32_t ldo, void *stream);
+/* Brute-force exact k-NN in double; *open_queries (optional) receives the
+ * number of queries searched in double (all of them when a value is outside
+ * the float range). */
+int rbc_brute_knn_f64(const double *dX, uint64_t n, uint32_t ldx, const double *dQ, uint64_t m, uint32_t ldq,
+                      uint32_t d, uint32_t k, int metric, uint32_t *dIds, double *dDists, uint32_t ldo,
+                      uint64_t *open_queries, void *stream);
+/* counts[i] = number of rows whose double distance is strictly below ranges[i]. */
+int rbc_brute_range_count_f64(const double *dX, uint64_t n, uint32_t ldx, const double *dQ, uint64_t m,
+                              uint32_t ldq, uint32_t d, int metric, const double *dRanges, uint32_t *dCounts,
+                              void *stream);
 
 /* Rows [r0, r0+rows) of a synthetic matrix into dOut (stride ld, padding
  * columns zeroed).  stream_id separates independent draws (database 0,

@@ -14,6 +14,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "librbc_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
+REF64_PATH = os.path.join(HERE, "_ref", "libref_f64.so")  # the reference built with real = double
 REF_DIR = "/root/reference"
 
 L2, L1 = 0, 1
@@ -22,10 +23,12 @@ FLT_MAX = np.finfo(np.float32).max
 
 _lib = None
 _ref = None
+_ref64 = None
 
 F32P = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 U32P = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 U64P = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+F64P = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 
 
 def build(with_ref=None):
@@ -63,6 +66,15 @@ def lib():
         L.orc_distance.restype = C.c_float
         L.orc_distance_f64.argtypes = [F32P, F32P, C.c_uint32, C.c_int]
         L.orc_distance_f64.restype = C.c_double
+        L.orc_knn_f64.argtypes = [F64P, C.c_uint64, C.c_uint32, F64P, C.c_uint64, C.c_uint32,
+                                  C.c_uint32, C.c_uint32, C.c_int, U32P, F64P, C.c_uint32, C.c_int]
+        L.orc_knn_f64.restype = C.c_int
+        L.orc_brute_1nn_f64.argtypes = [F64P, C.c_uint64, C.c_uint32, F64P, C.c_uint64, C.c_uint32,
+                                        C.c_uint32, C.c_int, U32P]
+        L.orc_range_count_f64.argtypes = [F64P, C.c_uint64, C.c_uint32, F64P, C.c_uint64, C.c_uint32,
+                                          C.c_uint32, C.c_int, F64P, U32P]
+        L.orc_distance64.argtypes = [F64P, F64P, C.c_uint32, C.c_int]
+        L.orc_distance64.restype = C.c_double
         L.orc_geometric_table.argtypes = [C.c_uint32, C.c_uint32, U32P]
         L.orc_synth.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint32,
                                 C.c_uint32, F32P, C.c_uint32, C.c_float, C.c_float, U32P]
@@ -96,8 +108,55 @@ def ref_lib():
     return _ref
 
 
+def ref64_available():
+    return os.path.exists(REF64_PATH)
+
+
+def ref64_lib():
+    """The reference's double-precision build (oracle/Makefile `ref`, real = double)."""
+    global _ref64
+    if _ref64 is None:
+        R = C.CDLL(REF64_PATH)
+        fn = getattr(R, "_Z8bruteCPU6matrixS_Pj")   # void bruteCPU(matrix, matrix, unint*)
+        fn.argtypes = [RefMatrix, RefMatrix, C.c_void_p]
+        fn.restype = None
+        dv = getattr(R, "_Z7distVec6matrixS_jj")    # real distVec(matrix, matrix, unint, unint)
+        dv.argtypes = [RefMatrix, RefMatrix, C.c_uint32, C.c_uint32]
+        dv.restype = C.c_double
+        _ref64 = (R, fn, dv)
+    return _ref64
+
+
 def pad16(v):
     return (v + 15) // 16 * 16
+
+
+def ref_brute_cpu_f64(X, Q):
+    """The double build's bruteCPU on logical X (n x d), Q (m x d) float64."""
+    _, fn, _ = ref64_lib()
+    n, d = X.shape
+    m = Q.shape[0]
+    pc = pad16(d)
+    Xp = np.zeros((pad16(n), pc), np.float64)
+    Xp[:n, :d] = X
+    Qp = np.zeros((pad16(m), pc), np.float64)
+    Qp[:m, :d] = Q
+    mx = RefMatrix(Xp.ctypes.data, n, d, Xp.shape[0], pc, pc)
+    mq = RefMatrix(Qp.ctypes.data, m, d, Qp.shape[0], pc, pc)
+    out = np.zeros(m, np.uint32)
+    fn(mx, mq, out.ctypes.data)
+    return out
+
+
+def ref_dist_vec_f64(Q, X, i, j):
+    """The double build's distVec(Q, X, i, j) on logical float64 arrays of equal width."""
+    _, _, dv = ref64_lib()
+    d = X.shape[1]
+    Qc = np.ascontiguousarray(Q, np.float64)
+    Xc = np.ascontiguousarray(X, np.float64)
+    mq = RefMatrix(Qc.ctypes.data, Qc.shape[0], d, Qc.shape[0], d, d)
+    mx = RefMatrix(Xc.ctypes.data, Xc.shape[0], d, Xc.shape[0], d, d)
+    return dv(mq, mx, i, j)
 
 
 def ref_brute_cpu(X, Q):
@@ -158,6 +217,44 @@ def knn(X, Q, k, metric=L2, threads=None):
     rc = lib().orc_knn(X, n, d, Q, m, d, d, k, metric, ids, dists, k, threads)
     assert rc == 0
     return ids, dists
+
+
+def knn_f64(X, Q, k, metric=L2, threads=None):
+    """Exact k-NN of the double build under (dist, id): (ids[m,k] uint32, dists[m,k] float64)."""
+    X = _c(X, np.float64)
+    Q = _c(Q, np.float64)
+    n, d = X.shape
+    m = Q.shape[0]
+    ids = np.empty((m, k), np.uint32)
+    dists = np.empty((m, k), np.float64)
+    if threads is None:
+        threads = os.cpu_count() or 1
+    rc = lib().orc_knn_f64(X, n, d, Q, m, d, d, k, metric, ids, dists, k, threads)
+    assert rc == 0
+    return ids, dists
+
+
+def brute_1nn_f64(X, Q, metric=L2):
+    X = _c(X, np.float64)
+    Q = _c(Q, np.float64)
+    out = np.empty(Q.shape[0], np.uint32)
+    lib().orc_brute_1nn_f64(X, X.shape[0], X.shape[1], Q, Q.shape[0], Q.shape[1], X.shape[1], metric, out)
+    return out
+
+
+def range_count_f64(X, Q, ranges, metric=L2):
+    X = _c(X, np.float64)
+    Q = _c(Q, np.float64)
+    out = np.empty(Q.shape[0], np.uint32)
+    lib().orc_range_count_f64(X, X.shape[0], X.shape[1], Q, Q.shape[0], Q.shape[1], X.shape[1], metric,
+                              _c(ranges, np.float64), out)
+    return out
+
+
+def distance64(a, b, metric=L2):
+    a = _c(a, np.float64)
+    b = _c(b, np.float64)
+    return lib().orc_distance64(a, b, a.shape[0], metric)
 
 
 def brute_1nn(X, Q, metric=L2):

@@ -32,6 +32,8 @@
  *   partition    : the exact-search structure: each point belongs to the list
  *                  of its nearest representative (ties to the lower rep
  *                  index), with the list radius = largest member distance.
+ *   double build : the reference compiled with real = double (defs.h:27-31):
+ *                  the same loops in double, MAX_REAL = DBL_MAX padding.
  *   synthetic data: the counter-based generator the engine uses on the GPU
  *                  (integer hashing, exactly representable floats, fixed
  *                  summation order) so both sides draw identical bits.
@@ -361,5 +363,110 @@ void orc_synth(int kind, uint64_t seed, uint64_t stream, uint64_t r0, uint64_t r
       }
     }
     for (uint32_t c = d; c < ld; c++) row[c] = 0.0f;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* double-precision variant: the reference built with real = double    */
+/* (defs.h:27-31, readme.txt:134-152): the same sequential sum, every  */
+/* subtract, multiply and add rounded to double on its own.            */
+/* ------------------------------------------------------------------ */
+static inline double orc_dist64(const double *a, const double *b, uint32_t d, int metric) {
+  double acc = 0.0;
+  for (uint32_t i = 0; i < d; i++) {
+    double t = a[i] - b[i];
+    double term = metric == ORC_L1 ? fabs(t) : t * t;
+    acc = acc + term;
+  }
+  return acc;
+}
+
+double orc_distance64(const double *a, const double *b, uint32_t d, int metric) {
+  return orc_dist64(a, b, d, metric);
+}
+
+static inline int orc_less64(double da, uint32_t ia, double db, uint32_t ib) {
+  return da < db || (da == db && ia < ib);
+}
+
+typedef struct {
+  const double *X; uint64_t n; uint32_t ldx;
+  const double *Q; uint64_t m; uint32_t ldq;
+  uint32_t d, k; int metric;
+  uint32_t *ids; double *dists; uint32_t ldo;
+  uint64_t q0, q1;
+} orc_knn64_job;
+
+static void *orc_knn64_worker(void *arg) {
+  orc_knn64_job *j = (orc_knn64_job *)arg;
+  for (uint64_t qi = j->q0; qi < j->q1; qi++) {
+    double *dk = j->dists + qi * j->ldo;
+    uint32_t *ik = j->ids + qi * j->ldo;
+    for (uint32_t t = 0; t < j->k; t++) { dk[t] = DBL_MAX; ik[t] = ORC_DUMMY; }
+    const double *q = j->Q + qi * j->ldq;
+    for (uint64_t xi = 0; xi < j->n; xi++) {
+      double dv = orc_dist64(q, j->X + xi * j->ldx, j->d, j->metric);
+      uint32_t iv = (uint32_t)xi;
+      if (!orc_less64(dv, iv, dk[j->k - 1], ik[j->k - 1])) continue;
+      int32_t p = (int32_t)j->k - 1;
+      while (p > 0 && orc_less64(dv, iv, dk[p - 1], ik[p - 1])) {
+        dk[p] = dk[p - 1];
+        ik[p] = ik[p - 1];
+        p--;
+      }
+      dk[p] = dv;
+      ik[p] = iv;
+    }
+  }
+  return NULL;
+}
+
+/* Exact k-NN in double under (dist, id); missing entries are DBL_MAX /
+ * 0xFFFFFFFF (MAX_REAL of the double build). */
+int orc_knn_f64(const double *X, uint64_t n, uint32_t ldx, const double *Q, uint64_t m, uint32_t ldq,
+                uint32_t d, uint32_t k, int metric, uint32_t *ids, double *dists, uint32_t ldo,
+                int nthreads) {
+  if (k == 0 || ldo < k) return -1;
+  if (nthreads < 1) nthreads = 1;
+  if ((uint64_t)nthreads > m) nthreads = m ? (int)m : 1;
+  pthread_t *th = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+  orc_knn64_job *jobs = (orc_knn64_job *)calloc((size_t)nthreads, sizeof(orc_knn64_job));
+  if (!th || !jobs) { free(th); free(jobs); return -2; }
+  for (int t = 0; t < nthreads; t++) {
+    orc_knn64_job *j = &jobs[t];
+    j->X = X; j->n = n; j->ldx = ldx; j->Q = Q; j->m = m; j->ldq = ldq;
+    j->d = d; j->k = k; j->metric = metric; j->ids = ids; j->dists = dists; j->ldo = ldo;
+    j->q0 = m * (uint64_t)t / (uint64_t)nthreads;
+    j->q1 = m * (uint64_t)(t + 1) / (uint64_t)nthreads;
+  }
+  for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, orc_knn64_worker, &jobs[t]);
+  orc_knn64_worker(&jobs[0]);
+  for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+  free(th);
+  free(jobs);
+  return 0;
+}
+
+/* bruteCPU of the double build (brute.cu:91-112): strict '<' from DBL_MAX. */
+void orc_brute_1nn_f64(const double *X, uint64_t n, uint32_t ldx, const double *Q, uint64_t m,
+                       uint32_t ldq, uint32_t d, int metric, uint32_t *nns) {
+  for (uint64_t i = 0; i < m; i++) {
+    double best = DBL_MAX;
+    nns[i] = 0;
+    for (uint64_t j = 0; j < n; j++) {
+      double t = orc_dist64(Q + i * ldq, X + j * ldx, d, metric);
+      if (t < best) { best = t; nns[i] = (uint32_t)j; }
+    }
+  }
+}
+
+/* bruteRangeCount of the double build: count of rows with dist < range. */
+void orc_range_count_f64(const double *X, uint64_t n, uint32_t ldx, const double *Q, uint64_t m,
+                         uint32_t ldq, uint32_t d, int metric, const double *ranges, uint32_t *cnts) {
+  for (uint64_t i = 0; i < m; i++) {
+    uint32_t c = 0;
+    for (uint64_t j = 0; j < n; j++)
+      c += orc_dist64(Q + i * ldq, X + j * ldx, d, metric) < ranges[i];
+    cnts[i] = c;
   }
 }

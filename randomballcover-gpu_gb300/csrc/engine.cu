@@ -867,7 +867,7 @@ int rbc_destroy(rbc_index *idx) {
   if (!idx) return RBC_OK;
   void *ptrs[] = {idx->Xp,      idx->perm,   idx->offsets, idx->radius,     idx->R,  idx->os_lists, idx->os_counts,
                   idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->tc.Xh, idx->tc.w,  idx->owner,
-                  idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm, idx->tc.mu};
+                  idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm, idx->tc.mu, idx->X64, idx->norm64};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : idx->ev_pool) cudaEventDestroy(e);
@@ -916,12 +916,14 @@ int rbc_get_oneshot(const rbc_index *idx, uint32_t *h_lists, uint32_t *h_counts)
 
 int rbc_query(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode, uint32_t *dIds,
               float *dDists, uint32_t ldo, void *stream) {
+  if (idx && (idx->flags & RBC_BUILD_F64)) return fail(RBC_ERR_INVALID, "rbc_query: index holds doubles: rbc_query_f64");
   return query_index(idx, dQ, m, ldq, k, mode, dIds, dDists, ldo, (cudaStream_t)stream);
 }
 
 int rbc_query_host(rbc_index *idx, const float *hQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
                    uint32_t *hIds, float *hDists, uint32_t ldo) {
   if (!idx) return fail(RBC_ERR_INVALID, "rbc_query_host: index is NULL");
+  if (idx->flags & RBC_BUILD_F64) return fail(RBC_ERR_INVALID, "rbc_query_host: index holds doubles: rbc_query_f64");
   if (m == 0) return RBC_OK;
   if (!hQ || (!hIds && !hDists)) return fail(RBC_ERR_INVALID, "rbc_query_host: NULL buffer");
   if (ldq < idx->d || ldo < k) return query_index(idx, hQ, m, ldq, k, mode, nullptr, nullptr, ldo, nullptr);

@@ -69,6 +69,10 @@ int build_tc(rbc_index *idx, cudaStream_t s);
 uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile);
 int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
                 uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s);
+int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *p,
+                cudaStream_t s, rbc_index **out);
+int brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,
+              uint32_t k, int metric, uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s);
 }  // namespace rbc
 
 struct rbc_index {
@@ -100,6 +104,11 @@ struct rbc_index {
   uint64_t n_pad = 0;
   uint32_t kp = 0;
   CUtensorMap tmB;                // TMA map of tc.Xh (128-row boxes, 128-byte swizzle)
+  // double-precision variant (rbc_build_f64, flag RBC_BUILD_F64): the double
+  // rows in original order (stride ld64) and their largest L2 / L1 norms
+  double *X64 = nullptr;
+  uint32_t ld64 = 0;
+  unsigned long long *norm64 = nullptr;
   // padded copy of the input in original order (legacy rbcStruct.dx)
   float *Xi = nullptr;
   uint64_t xi_rows = 0;

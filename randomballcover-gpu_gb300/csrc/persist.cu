@@ -6,6 +6,7 @@
 // arrays in a fixed order, each written only if the index has it (the flags
 // in the header say which).  All values little-endian, as in memory.  The
 // tensor-core operands are not stored: loading derives them from the lists.
+// A double-precision index (RBC_BUILD_F64) adds its double rows and norms.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -23,7 +24,7 @@ constexpr uint32_t kVersion = 2;
 struct FileHeader {
   char magic[8];
   uint32_t version;
-  uint32_t d, ld, dp, nr, s, lds, kp, flags, reserved0;
+  uint32_t d, ld, dp, nr, s, lds, kp, flags, ld64;  // ld64: double rows (RBC_BUILD_F64)
   int32_t metric;
   uint64_t n, n_pad, xi_rows, min_list, max_list;
   uint32_t reserved[8];
@@ -87,6 +88,7 @@ extern "C" int rbc_save(const rbc_index *idx, const char *path) {
   h.lds = idx->lds;
   h.kp = idx->kp;
   h.flags = idx->flags;
+  h.ld64 = idx->ld64;
   h.metric = idx->metric;
   h.n = idx->n;
   h.n_pad = idx->n_pad;
@@ -114,6 +116,10 @@ extern "C" int rbc_save(const rbc_index *idx, const char *path) {
     if (rc == RBC_OK) rc = write_dev(fp, idx->Xo, total * ld * 4, stage);
   }
   if (rc == RBC_OK && idx->Xi) rc = write_dev(fp, idx->Xi, (size_t)idx->xi_rows * ld * 4, stage);
+  if (rc == RBC_OK && (idx->flags & RBC_BUILD_F64)) {
+    rc = write_dev(fp, idx->X64, n * idx->ld64 * 8, stage);
+    if (rc == RBC_OK) rc = write_dev(fp, idx->norm64, 16, stage);
+  }
   if (rc != RBC_OK) return rc;
   FILE *f = closer.fp;
   closer.fp = nullptr;
@@ -181,6 +187,12 @@ extern "C" int rbc_load(const char *path, rbc_index **out) {
     if (rc == RBC_OK) rc = read_dev(fp, &idx->Xo, total * ld * 4, stage, tot);
   }
   if (rc == RBC_OK && h.xi_rows) rc = read_dev(fp, &idx->Xi, (size_t)h.xi_rows * ld * 4, stage, tot);
+  if (rc == RBC_OK && (h.flags & RBC_BUILD_F64)) {
+    if (h.ld64 < h.d || h.ld64 % 2) return fail(RBC_ERR_IO, "rbc_load: corrupt header");
+    idx->ld64 = h.ld64;
+    rc = read_dev(fp, &idx->X64, n * h.ld64 * 8, stage, tot);
+    if (rc == RBC_OK) rc = read_dev(fp, &idx->norm64, 16, stage, tot);
+  }
   if (rc != RBC_OK) return rc;
   if (h.flags & RBC_BUILD_BF16) {
     if (!(h.flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_IO, "rbc_load: corrupt header");

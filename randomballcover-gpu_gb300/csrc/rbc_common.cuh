@@ -44,18 +44,24 @@ __device__ __forceinline__ float accum(float acc, float q, float x) {
 __device__ __forceinline__ bool pair_less(float da, uint32_t ia, float db, uint32_t ib) {
   return da < db || (da == db && ia < ib);
 }
+__device__ __forceinline__ bool pair_less(double da, uint32_t ia, double db, uint32_t ib) {
+  return da < db || (da == db && ia < ib);
+}
 
 // Non-negative floats order like their bit patterns; used for atomicMin/Max.
 __device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
 
+// The warp networks below sort (dist, id) pairs with dist a float or, for the
+// double-precision variant, a double.
 // Warp-wide bitonic sort of 32 (dist, id) pairs, ascending, one per lane.
-__device__ __forceinline__ void warp_sort32(float &d, uint32_t &id) {
+template <typename D>
+__device__ __forceinline__ void warp_sort32(D &d, uint32_t &id) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int k = 2; k <= 32; k <<= 1) {
 #pragma unroll
     for (int j = k >> 1; j > 0; j >>= 1) {
-      float od = __shfl_xor_sync(0xffffffffu, d, j);
+      D od = __shfl_xor_sync(0xffffffffu, d, j);
       uint32_t oi = __shfl_xor_sync(0xffffffffu, id, j);
       bool up = ((lane & k) == 0);
       bool lower = ((lane & j) == 0);
@@ -67,11 +73,12 @@ __device__ __forceinline__ void warp_sort32(float &d, uint32_t &id) {
 }
 
 // Sort a bitonic sequence of 32 pairs held one per lane, ascending.
-__device__ __forceinline__ void warp_bitonic_merge32(float &d, uint32_t &id) {
+template <typename D>
+__device__ __forceinline__ void warp_bitonic_merge32(D &d, uint32_t &id) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int j = 16; j > 0; j >>= 1) {
-    float od = __shfl_xor_sync(0xffffffffu, d, j);
+    D od = __shfl_xor_sync(0xffffffffu, d, j);
     uint32_t oi = __shfl_xor_sync(0xffffffffu, id, j);
     bool lower = ((lane & j) == 0);
     bool take_other = lower ? pair_less(od, oi, d, id) : pair_less(d, id, od, oi);
@@ -102,11 +109,11 @@ inline uint32_t list_width_for(uint32_t k) { return k <= 32 ? 32 : (k <= 64 ? 64
 // the last 32: u = the 32 smallest of (last block, candidates); then u is
 // merged down through the earlier blocks, each merge of two sorted 32-blocks
 // passing its upper half up.
-template <int W>
-__device__ __forceinline__ void warp_merge_into_w(float (&ld)[W], uint32_t (&li)[W], float cd, uint32_t ci) {
+template <int W, typename D>
+__device__ __forceinline__ void warp_merge_into_w(D (&ld)[W], uint32_t (&li)[W], D cd, uint32_t ci) {
   const int lane = threadIdx.x & 31;
   warp_sort32(cd, ci);
-  float ud = __shfl_sync(0xffffffffu, cd, 31 - lane);
+  D ud = __shfl_sync(0xffffffffu, cd, 31 - lane);
   uint32_t ui = __shfl_sync(0xffffffffu, ci, 31 - lane);
   if (!pair_less(ud, ui, ld[W - 1], li[W - 1])) {
     ud = ld[W - 1];
@@ -115,9 +122,9 @@ __device__ __forceinline__ void warp_merge_into_w(float (&ld)[W], uint32_t (&li)
   warp_bitonic_merge32(ud, ui);
 #pragma unroll
   for (int j = W - 2; j >= 0; j--) {
-    const float rd = __shfl_sync(0xffffffffu, ud, 31 - lane);
+    const D rd = __shfl_sync(0xffffffffu, ud, 31 - lane);
     const uint32_t ri = __shfl_sync(0xffffffffu, ui, 31 - lane);
-    float hd, lo_d;
+    D hd, lo_d;
     uint32_t hi, lo_i;
     if (pair_less(rd, ri, ld[j], li[j])) {
       lo_d = rd;
@@ -145,13 +152,13 @@ __device__ __forceinline__ void warp_merge_into_w(float (&ld)[W], uint32_t (&li)
 // the elementwise minimum of g and reversed l is bitonic; a bitonic merge
 // over KW entries (blocks compared within the lane, then lanes by shuffles)
 // sorts it.
-template <int W>
-__device__ __forceinline__ void warp_merge_lists_w(float (&gd)[W], uint32_t (&gi)[W], const float (&ld)[W],
+template <int W, typename D>
+__device__ __forceinline__ void warp_merge_lists_w(D (&gd)[W], uint32_t (&gi)[W], const D (&ld)[W],
                                                    const uint32_t (&li)[W]) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int w = 0; w < W; w++) {
-    const float rd = __shfl_sync(0xffffffffu, ld[W - 1 - w], 31 - lane);
+    const D rd = __shfl_sync(0xffffffffu, ld[W - 1 - w], 31 - lane);
     const uint32_t ri = __shfl_sync(0xffffffffu, li[W - 1 - w], 31 - lane);
     if (pair_less(rd, ri, gd[w], gi[w])) {
       gd[w] = rd;
@@ -167,7 +174,7 @@ __device__ __forceinline__ void warp_merge_lists_w(float (&gd)[W], uint32_t (&gi
     for (int w = 0; w < W; w++) {
       const int p = w ^ jb;
       if (p > w && pair_less(gd[p], gi[p], gd[w], gi[w])) {
-        const float td = gd[w];
+        const D td = gd[w];
         const uint32_t ti = gi[w];
         gd[w] = gd[p];
         gi[w] = gi[p];

@@ -18,7 +18,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_ITER_LIMIT, ERR_UNSUPPORTED, ERR_IO = 
 L2, L1 = 0, 1
 KMAX = 32
 K_LIMIT = 128  # largest k of query / brute_knn (KMAX for batches and the no-alloc call)
-BUILD_PARTITION, BUILD_ONESHOT, BUILD_BF16 = 1, 2, 4
+BUILD_PARTITION, BUILD_ONESHOT, BUILD_BF16, BUILD_F64 = 1, 2, 4, 8
 QUERY_EXACT, QUERY_ONESHOT, QUERY_EXACT_TC = 0, 1, 2
 TC_BF16, TC_FP16_SPLIT = 0, 1
 QUERY_ROUTED = 0x1000
@@ -93,6 +93,11 @@ SIGNATURES = {
     "rbc_brute_knn": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _INT, _VP, _VP, _U32, _VP], _INT),
     "rbc_brute_knn_noalloc": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _INT, _VP, _VP, _U32, _VP], _INT),
     "rbc_brute_range_count": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _INT, _VP, _VP, _VP], _INT),
+    "rbc_build_f64": ([_VP, _U64, _U32, _U32, C.POINTER(BuildParams), _VP, C.POINTER(_VP)], _INT),
+    "rbc_query_f64": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP, _VP, _U32, _VP], _INT),
+    "rbc_brute_knn_f64": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _INT, _VP, _VP, _U32, C.POINTER(_U64), _VP],
+                          _INT),
+    "rbc_brute_range_count_f64": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _INT, _VP, _VP, _VP], _INT),
     "rbc_synth": ([_INT, _U64, _U64, _U64, _U64, _U32, _U32, _VP, _U32, _F, _F, _VP], _INT),
     "rbc_read_matrix_bin": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
     "rbc_read_matrix_text": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
@@ -138,6 +143,12 @@ def _stream(stream):
     return s.cuda_stream
 
 
+def _is_f64(a):
+    import torch
+    return (isinstance(a, np.ndarray) and a.dtype == np.float64) or \
+        (isinstance(a, torch.Tensor) and a.dtype == torch.float64)
+
+
 def _dev(a, dtype=None):
     import torch
     if isinstance(a, np.ndarray):
@@ -148,11 +159,14 @@ def _dev(a, dtype=None):
 
 
 class Index:
-    """An RBC index over the rows of X (n x d float32, CUDA tensor or numpy)."""
+    """An RBC index over the rows of X (n x d, CUDA tensor or numpy).  float64
+    data builds the double-precision variant (rbc_build_f64): its queries take
+    and return doubles."""
 
     def __init__(self, X, num_reps, s=0, metric=L2, flags=0, seed=0, rep_ids=None, stream=None):
         import torch
-        X = _dev(X, torch.float32)
+        self.f64 = _is_f64(X)
+        X = _dev(X, torch.float64 if self.f64 else torch.float32)
         n, d = X.shape
         p = BuildParams(num_reps, s, metric, flags, seed, None)
         self._rep_buf = None
@@ -160,7 +174,8 @@ class Index:
             self._rep_buf = np.ascontiguousarray(rep_ids, dtype=np.uint32)
             p.rep_ids = self._rep_buf.ctypes.data_as(C.POINTER(C.c_uint32))
         h = C.c_void_p()
-        check(lib().rbc_build(X.data_ptr(), n, d, X.stride(0), C.byref(p), _stream(stream), C.byref(h)))
+        build = lib().rbc_build_f64 if self.f64 else lib().rbc_build
+        check(build(X.data_ptr(), n, d, X.stride(0), C.byref(p), _stream(stream), C.byref(h)))
         self.h = h
         self.n, self.d, self.metric = n, d, metric
 
@@ -174,6 +189,7 @@ class Index:
         self._rep_buf = None
         inf = self.info()
         self.n, self.d, self.metric = inf["n"], inf["d"], inf["metric"]
+        self.f64 = bool(inf["flags"] & BUILD_F64)
         return self
 
     def save(self, path):
@@ -187,17 +203,20 @@ class Index:
     __del__ = close
 
     def query(self, Q, k, mode=QUERY_EXACT, stream=None, out=None):
-        """Returns (ids uint32-as-int32 tensor [m,k], dists float32 [m,k]) on the device."""
+        """Returns (ids uint32-as-int32 tensor [m,k], dists float32 [m,k]) on the device
+        (float64 dists on a double-precision index)."""
         import torch
-        Q = _dev(Q, torch.float32)
+        dt = torch.float64 if self.f64 else torch.float32
+        Q = _dev(Q, dt)
         m = Q.shape[0]
         if out is None:
             ids = torch.empty((m, k), dtype=torch.int32, device=Q.device)
-            dists = torch.empty((m, k), dtype=torch.float32, device=Q.device)
+            dists = torch.empty((m, k), dtype=dt, device=Q.device)
         else:
             ids, dists = out
-        check(lib().rbc_query(self.h, Q.data_ptr(), m, Q.stride(0), k, mode, ids.data_ptr(), dists.data_ptr(),
-                              ids.stride(0), _stream(stream)))
+        fn = lib().rbc_query_f64 if self.f64 else lib().rbc_query
+        check(fn(self.h, Q.data_ptr(), m, Q.stride(0), k, mode, ids.data_ptr(), dists.data_ptr(), ids.stride(0),
+                 _stream(stream)))
         return ids, dists
 
     def query_host(self, Q, k, mode=QUERY_EXACT, out=None):
@@ -366,8 +385,25 @@ class Router:
         return out
 
 
-def brute_knn(X, Q, k, metric=L2, stream=None):
+def brute_knn_f64(X, Q, k, metric=L2, stream=None):
+    """Double-precision brute force: (ids, float64 dists, queries searched in double)."""
     import torch
+    X = _dev(X, torch.float64)
+    Q = _dev(Q, torch.float64)
+    m = Q.shape[0]
+    ids = torch.empty((m, k), dtype=torch.int32, device=Q.device)
+    dists = torch.empty((m, k), dtype=torch.float64, device=Q.device)
+    nopen = C.c_uint64()
+    check(lib().rbc_brute_knn_f64(X.data_ptr(), X.shape[0], X.stride(0), Q.data_ptr(), m, Q.stride(0), Q.shape[1],
+                                  k, metric, ids.data_ptr(), dists.data_ptr(), k, C.byref(nopen), _stream(stream)))
+    return ids, dists, nopen.value
+
+
+def brute_knn(X, Q, k, metric=L2, stream=None):
+    """Brute-force exact k-NN; float64 inputs take the double-precision variant."""
+    import torch
+    if _is_f64(X):
+        return brute_knn_f64(X, Q, k, metric, stream)[:2]
     X = _dev(X, torch.float32)
     Q = _dev(Q, torch.float32)
     m = Q.shape[0]
@@ -380,6 +416,15 @@ def brute_knn(X, Q, k, metric=L2, stream=None):
 
 def range_count(X, Q, ranges, metric=L2, stream=None):
     import torch
+    if _is_f64(X):
+        X = _dev(X, torch.float64)
+        Q = _dev(Q, torch.float64)
+        r = _dev(ranges, torch.float64)
+        cnt = torch.empty(Q.shape[0], dtype=torch.int32, device=Q.device)
+        check(lib().rbc_brute_range_count_f64(X.data_ptr(), X.shape[0], X.stride(0), Q.data_ptr(), Q.shape[0],
+                                              Q.stride(0), Q.shape[1], metric, r.data_ptr(), cnt.data_ptr(),
+                                              _stream(stream)))
+        return cnt
     X = _dev(X, torch.float32)
     Q = _dev(Q, torch.float32)
     r = _dev(ranges, torch.float32)

@@ -13,6 +13,10 @@ Inputs:
                                          generated bytes are stored.
 Outputs are .npz files with ids (uint32) and distances (float32) sorted by
 (distance, id), plus build structures for fixed representative ids.
+
+f64_cases.npz holds the double-precision variant's fixtures (the reference
+built with real = double): inputs stored as float64, ids and float64
+distances from the double oracle, and the double build's own bruteCPU 1-NN.
 """
 import hashlib
 import os
@@ -91,7 +95,33 @@ def main():
         owner, odist, offsets, members, radius = O.partition(X, reps)
         res.update(rep_ids=reps, part_offsets=offsets, part_members=members, part_radius=radius)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **res)
+    f64_cases(have_ref and O.ref64_available())
     print("golden fixtures written; reference cross-check:", "yes" if have_ref else "no (reference absent)")
+
+
+def f64_cases(have_ref64):
+    """Double-precision fixtures.  'sample': the sample input plus offsets
+    below float resolution; 'near': points 1e-7 apart around 100, which all
+    round to the same float (the float shortlist cannot separate them)."""
+    Xs, Qs = sample_inputs()
+    ii = np.arange(1024)[:, None] * 7919 + np.arange(16)[None, :] * 104729
+    jj = np.arange(128)[:, None] * 7919 + np.arange(16)[None, :] * 104729 + 3
+    X1 = Xs.astype(np.float64) + ((ii % 2001) - 1000) * 2.0 ** -40
+    Q1 = Qs.astype(np.float64) + ((jj % 2001) - 1000) * 2.0 ** -40
+    rng = np.random.default_rng(64)
+    X2 = 100.0 + 1e-7 * rng.integers(-50, 51, (600, 8)).astype(np.float64)
+    Q2 = 100.0 + 1e-7 * rng.integers(-50, 51, (40, 8)).astype(np.float64)
+    out = {}
+    for tag, X, Q in (("sample", X1, Q1), ("near", X2, Q2)):
+        out[f"{tag}_X"], out[f"{tag}_Q"] = X, Q
+        for metric, mt in ((O.L2, "l2"), (O.L1, "l1")):
+            ids, dists = O.knn_f64(X, Q, 32, metric)
+            out[f"{tag}_ids_{mt}"], out[f"{tag}_dists_{mt}"] = ids, dists
+        if have_ref64:
+            ref1 = O.ref_brute_cpu_f64(X, Q)
+            assert (ref1 == out[f"{tag}_ids_l2"][:, 0]).all(), f"{tag}: double oracle disagrees with bruteCPU"
+            out[f"{tag}_ref_bruteCPU_1nn"] = ref1
+    np.savez_compressed(os.path.join(HERE, "f64_cases.npz"), **out)
 
 
 if __name__ == "__main__":

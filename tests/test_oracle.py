@@ -155,3 +155,52 @@ def test_range_count_matches_fp32_definition(oracle):
     assert (cnt <= 9).all()
     ids = g["ids_l2"]
     assert (cnt >= (g["dists_l2"][:, :9] < ranges[:, None]).sum(1)).all()
+
+
+# ------------------------------------------------------------------ double-precision variant
+@pytest.mark.skipif(not __import__("oracle").ref64_available(), reason="reference double build not present")
+def test_f64_oracle_equals_reference_double_build(oracle):
+    """The double oracle against the reference compiled with real = double (defs.h:27-31)."""
+    rng = np.random.default_rng(64)
+    for n, m, d in ((901, 31, 7), (2048, 40, 16), (300, 12, 130)):
+        X = rng.standard_normal((n, d))
+        Q = rng.standard_normal((m, d))
+        X[11] = X[2]  # duplicates: the lower id wins
+        np.testing.assert_array_equal(oracle.brute_1nn_f64(X, Q), oracle.ref_brute_cpu_f64(X, Q))
+        ids, _ = oracle.knn_f64(X, Q, 1)
+        np.testing.assert_array_equal(ids[:, 0], oracle.ref_brute_cpu_f64(X, Q))
+        for i in (0, m - 1):
+            for j in (0, 11, n - 1):
+                assert oracle.distance64(Q[i], X[j]) == oracle.ref_dist_vec_f64(Q, X, i, j)
+
+
+def test_f64_golden(oracle):
+    g = load_golden("f64_cases")
+    for tag in ("sample", "near"):
+        X, Q = g[f"{tag}_X"], g[f"{tag}_Q"]
+        np.testing.assert_array_equal(g[f"{tag}_ids_l2"][:, 0], g[f"{tag}_ref_bruteCPU_1nn"])
+        for metric, mt in ((oracle.L2, "l2"), (oracle.L1, "l1")):
+            ids, dists = oracle.knn_f64(X, Q, 32, metric)
+            np.testing.assert_array_equal(ids, g[f"{tag}_ids_{mt}"])
+            np.testing.assert_array_equal(dists, g[f"{tag}_dists_{mt}"])
+
+
+def test_f64_near_case_defeats_float_ranking(oracle):
+    """In the 'near' fixture the 101 distinct coordinates round to three
+    floats: the float order says almost nothing, the double order decides."""
+    g = load_golden("f64_cases")
+    X = g["near_X"]
+    assert len(np.unique(X)) > 90 and len(np.unique(X.astype(np.float32))) <= 3
+    d = g["near_dists_l2"]
+    assert (d[:, 1:] >= d[:, :-1]).all() and (d[:, 0] > 0).any()
+
+
+def test_f64_range_count_definition(oracle):
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((700, 9))
+    Q = rng.standard_normal((20, 9))
+    ids, dists = oracle.knn_f64(X, Q, 10)
+    cnt = oracle.range_count_f64(X, Q, dists[:, 9])
+    assert (cnt <= 9).all() and (cnt >= 0).all()
+    cnt2 = oracle.range_count_f64(X, Q, np.nextafter(dists[:, 9], np.inf))
+    assert (cnt2 >= 10).all()
