@@ -87,6 +87,8 @@ def parse():
     ap.add_argument("--train", type=int, default=None)
     ap.add_argument("--cpu-queries-per-thread", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side", action="store_true",
+                    help="skip the c2 side measurements (k = 128 and the double-precision variant)")
     ap.add_argument("--router-probes", type=int, default=2, help="lists the learned form adds from the router")
     ap.add_argument("--forms", default=None,
                     help="forms to time; the last one listed is the headline (default: per workload)")
@@ -431,6 +433,7 @@ def run_engine(a):
             dt = time.perf_counter() - t0
             range_count = {"queries": nq, "ms": dt * 1e3, "pairs_per_s": nq * w["n"] / dt,
                            "all_counts_at_least_k_minus_1": bool((cnt >= k - 1).all().item())}
+    side = side_measurements(a, idx, X, Q, results, exact_forms) if (a.workload == "c2" and not a.no_side) else None
     clk, value, ms, launches = res["clocks"], res["value"], res["ms"], res["launches"]
 
     # end to end through the host API: pinned host queries in, results out
@@ -480,7 +483,8 @@ def run_engine(a):
                  "learned_plain": "exact RBC, learned router + FP32 list search"}
         extra = {"build_s": build_s, "min_list": info["min_list"], "max_list": info["max_list"],
                  "tc_format": ["bf16", "fp16_split"][info["tc_format"]], "same_ids_all_exact_forms": same,
-                 "router": router_info, "oneshot_recall": oneshot_recall, "range_count": range_count, "forms": {}}
+                 "router": router_info, "oneshot_recall": oneshot_recall, "range_count": range_count, "forms": {},
+                 "side": side}
         for f, r in results.items():
             extra["forms"][f] = {"value": r["value"], "ms_per_step": r["ms"] / r["steps"],
                                  "lists_per_query": r["lists"] / (m * r["steps"]),
@@ -500,6 +504,54 @@ def run_engine(a):
     idx.close()
     if dist:
         dist.destroy_process_group()
+
+
+def side_measurements(a, idx, X, Q, results, exact_forms):
+    """Paths beyond the headline, on a query sample of the same workload:
+    k = 128 (FP32 lists of 128 entries) and the double-precision variant
+    (FP32 shortlists reranked in double, certified), plus the double brute
+    force's own rate (range count in double: every pair in FP64)."""
+    import torch
+    import pyrbc
+    w = a.w
+    k, ms = w["k"], min(w["m"], 20_000)
+    Qs = Q[:ms].contiguous()
+
+    def clock(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    out = {"queries": ms}
+    (i128, d128), dt = clock(lambda: idx.query(Qs, 128))
+    st = idx.stats()
+    ref = results[exact_forms[-1]]["ids"][:ms] if exact_forms else None
+    out["k128"] = {"value": ms / dt, "unit": UNIT, "pairs_per_query": st["point_pairs"] / ms,
+                   "first_k_equal_k_query": bool((i128[:, :k] == ref).all().item()) if ref is not None else None,
+                   "sorted": bool((d128[:, 1:] >= d128[:, :-1]).all().item())}
+    t0 = time.perf_counter()
+    idx64 = pyrbc.Index(X.double(), w["reps"], seed=w["seed"])
+    torch.cuda.synchronize()
+    build64 = time.perf_counter() - t0
+    Q64 = Qs.double()
+    (i64, d64), dt = clock(lambda: idx64.query(Q64, k))
+    st = idx64.stats()
+    out["f64"] = {"value": ms / dt, "unit": UNIT, "k": k, "build_s": build64,
+                  "queries_searched_in_double": st["fallback_queries"],
+                  "ids_equal_fp32_answer": (i64 == ref).float().mean().item() if ref is not None else None}
+    idx64.close()
+    nq = 256
+    r = d64[:nq, k - 1].contiguous()
+    X64 = X.double()
+    _, dt = clock(lambda: pyrbc.range_count(X64, Q64[:nq], r))
+    out["f64_scan"] = {"queries": nq, "pairs_per_s": nq * w["n"] / dt,
+                       "fp64_gflops": nq * w["n"] * 3 * w["d"] / dt / 1e9,
+                       "note": "double brute force (range count): sub, mul, add per pair-dim, all FP64"}
+    del X64
+    return out
 
 
 def batch_instances(w):

@@ -290,6 +290,15 @@ int rbc_write_neighbors_bin(const char *path, const uint32_t *hIds, const float 
                             uint32_t k, uint32_t ld);
 int rbc_write_neighbors_text(const char *path, const uint32_t *hIds, const float *hDists,
                              uint64_t m, uint32_t k, uint32_t ld);
+/* The same formats in the double build (real = double): 8-byte values. */
+int rbc_read_matrix_bin_f64(const char *path, double *hBuf, uint64_t rows, uint32_t cols, uint32_t ld);
+int rbc_read_matrix_text_f64(const char *path, double *hBuf, uint64_t rows, uint32_t cols, uint32_t ld);
+int rbc_write_matrix_bin_f64(const char *path, const double *hBuf, uint64_t rows, uint32_t cols,
+                             uint32_t ld);
+int rbc_write_neighbors_bin_f64(const char *path, const uint32_t *hIds, const double *hDists, uint64_t m,
+                                uint32_t k, uint32_t ld);
+int rbc_write_neighbors_text_f64(const char *path, const uint32_t *hIds, const double *hDists,
+                                 uint64_t m, uint32_t k, uint32_t ld);
 
 #ifdef __cplusplus
 }

@@ -9,6 +9,8 @@
 //               -s seed   representative sampling seed
 //               -l        L1 distance instead of squared L2
 //               -S file   save the built index;  -L file  load an index instead of building
+//               -D        the double build (real = double, defs.h:27-31): 8-byte input and
+//                         output values, distances in double
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -25,7 +27,7 @@ namespace {
 
 const char *dbX = nullptr, *dbQ = nullptr, *dbXt = nullptr, *dbQt = nullptr, *outB = nullptr, *outT = nullptr;
 const char *saveIdx = nullptr, *loadIdx = nullptr;
-bool runBrute = false, runEval = false;
+bool runBrute = false, runEval = false, useDouble = false;
 uint64_t n = 0, m = 0;
 uint32_t d = 0, numReps = 0, k = RBC_KMAX;
 int device = 0, metric = RBC_L2;
@@ -60,7 +62,8 @@ void usage() {
   std::printf("\tuse -e to run the evaluation routine (implicitly runs brute force)\n");
   std::printf("\n\tTo input/output data in text format (instead of bin), use the \n\t-X and -Q and -O switches in "
               "place of -x and -q and -o (respectively).\n");
-  std::printf("\n\textensions: -k K, -M exact|tc|oneshot, -s seed, -l (L1), -S indexfile, -L indexfile\n\n");
+  std::printf("\n\textensions: -k K, -M exact|tc|oneshot, -s seed, -l (L1), -S indexfile, -L indexfile,\n"
+              "\t            -D (double precision: 8-byte values in and out)\n\n");
   std::exit(0);
 }
 
@@ -91,6 +94,7 @@ void parse(int argc, char **argv) {
     else if (a == "-k") k = (uint32_t)std::atoi(next());
     else if (a == "-s") seed = std::strtoull(next(), nullptr, 0);
     else if (a == "-l") metric = RBC_L1;
+    else if (a == "-D") useDouble = true;
     else if (a == "-S") saveIdx = next();
     else if (a == "-L") loadIdx = next();
     else if (a == "-M") {
@@ -121,10 +125,196 @@ void parse(int argc, char **argv) {
     std::fprintf(stderr, "number of representatives must be at least 32\n");
     std::exit(1);
   }
+  if (useDouble && mode == RBC_QUERY_ONESHOT) {
+    std::fprintf(stderr, "the one-shot lists are not available in double precision.. exiting\n");
+    std::exit(1);
+  }
   if (k < 1 || k > RBC_K_LIMIT) {
     std::fprintf(stderr, "k must be in [1, %d].. exiting\n", RBC_K_LIMIT);
     std::exit(1);
   }
+}
+
+// The library calls of one precision: float (the reference's default build)
+// or double (its real = double build).
+template <typename R>
+struct Api;
+template <>
+struct Api<float> {
+  static int read_bin(const char *p, float *h, uint64_t r, uint32_t c, uint32_t ld) {
+    return rbc_read_matrix_bin(p, h, r, c, ld);
+  }
+  static int read_text(const char *p, float *h, uint64_t r, uint32_t c, uint32_t ld) {
+    return rbc_read_matrix_text(p, h, r, c, ld);
+  }
+  static int build(const float *dX, uint64_t n, uint32_t d, uint32_t ld, const rbc_build_params *p, rbc_index **o) {
+    return rbc_build(dX, n, d, ld, p, nullptr, o);
+  }
+  static int query(rbc_index *i, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode, uint32_t *ids,
+                   float *dists, uint32_t ldo) {
+    return rbc_query(i, dQ, m, ldq, k, mode, ids, dists, ldo, nullptr);
+  }
+  static int brute(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,
+                   uint32_t k, int metric, uint32_t *ids, float *dists, uint32_t ldo) {
+    return rbc_brute_knn(dX, n, ldx, dQ, m, ldq, d, k, metric, ids, dists, ldo, nullptr);
+  }
+  static int range(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,
+                   int metric, const float *r, uint32_t *c) {
+    return rbc_brute_range_count(dX, n, ldx, dQ, m, ldq, d, metric, r, c, nullptr);
+  }
+  static int write_bin(const char *p, const uint32_t *i, const float *dd, uint64_t m, uint32_t k, uint32_t ld) {
+    return rbc_write_neighbors_bin(p, i, dd, m, k, ld);
+  }
+  static int write_text(const char *p, const uint32_t *i, const float *dd, uint64_t m, uint32_t k, uint32_t ld) {
+    return rbc_write_neighbors_text(p, i, dd, m, k, ld);
+  }
+};
+template <>
+struct Api<double> {
+  static int read_bin(const char *p, double *h, uint64_t r, uint32_t c, uint32_t ld) {
+    return rbc_read_matrix_bin_f64(p, h, r, c, ld);
+  }
+  static int read_text(const char *p, double *h, uint64_t r, uint32_t c, uint32_t ld) {
+    return rbc_read_matrix_text_f64(p, h, r, c, ld);
+  }
+  static int build(const double *dX, uint64_t n, uint32_t d, uint32_t ld, const rbc_build_params *p, rbc_index **o) {
+    return rbc_build_f64(dX, n, d, ld, p, nullptr, o);
+  }
+  static int query(rbc_index *i, const double *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
+                   uint32_t *ids, double *dists, uint32_t ldo) {
+    return rbc_query_f64(i, dQ, m, ldq, k, mode, ids, dists, ldo, nullptr);
+  }
+  static int brute(const double *dX, uint64_t n, uint32_t ldx, const double *dQ, uint64_t m, uint32_t ldq,
+                   uint32_t d, uint32_t k, int metric, uint32_t *ids, double *dists, uint32_t ldo) {
+    return rbc_brute_knn_f64(dX, n, ldx, dQ, m, ldq, d, k, metric, ids, dists, ldo, nullptr, nullptr);
+  }
+  static int range(const double *dX, uint64_t n, uint32_t ldx, const double *dQ, uint64_t m, uint32_t ldq,
+                   uint32_t d, int metric, const double *r, uint32_t *c) {
+    return rbc_brute_range_count_f64(dX, n, ldx, dQ, m, ldq, d, metric, r, c, nullptr);
+  }
+  static int write_bin(const char *p, const uint32_t *i, const double *dd, uint64_t m, uint32_t k, uint32_t ld) {
+    return rbc_write_neighbors_bin_f64(p, i, dd, m, k, ld);
+  }
+  static int write_text(const char *p, const uint32_t *i, const double *dd, uint64_t m, uint32_t k, uint32_t ld) {
+    return rbc_write_neighbors_text_f64(p, i, dd, m, k, ld);
+  }
+};
+
+// Read, build (or load), query, optionally brute force and evaluate, write.
+template <typename R>
+int run() {
+  using A = Api<R>;
+  double t0;
+  const uint32_t ld = (d + 15) / 16 * 16;
+  std::vector<R> x(n * ld), q(m * ld);
+  check(dbXt ? A::read_text(dbXt, x.data(), n, d, ld) : A::read_bin(dbX, x.data(), n, d, ld), "reading the database");
+  check(dbQt ? A::read_text(dbQt, q.data(), m, d, ld) : A::read_bin(dbQ, q.data(), m, d, ld), "reading the queries");
+  void *dx = nullptr, *dq = nullptr;
+  if (cudaMalloc(&dx, x.size() * sizeof(R)) != cudaSuccess || cudaMalloc(&dq, q.size() * sizeof(R)) != cudaSuccess) {
+    std::fprintf(stderr, "not enough device memory for the database and queries.. exiting\n");
+    return 1;
+  }
+
+  rbc_index *idx = nullptr;
+  std::printf("building the rbc..\n");
+  t0 = now();
+  if (loadIdx) {
+    check(rbc_load(loadIdx, &idx), "loading the index");
+    rbc_index_info info{};
+    check(rbc_get_info(idx, &info), "reading the index");
+    if (((info.flags & RBC_BUILD_F64) != 0) != (sizeof(R) == 8)) {
+      std::fprintf(stderr, "the index file was built in the other precision (-D).. exiting\n");
+      return 1;
+    }
+  } else {
+    rbc_build_params p{};
+    p.num_reps = numReps;
+    p.s = numReps;
+    p.metric = metric;
+    p.flags = RBC_BUILD_PARTITION | (mode == RBC_QUERY_ONESHOT ? RBC_BUILD_ONESHOT : 0u) |
+              (mode == RBC_QUERY_EXACT_TC ? RBC_BUILD_BF16 : 0u);
+    p.seed = seed;
+    cudaMemcpy(dx, x.data(), x.size() * sizeof(R), cudaMemcpyHostToDevice);
+    check(A::build((const R *)dx, n, d, ld, &p, &idx), "buildRBC");
+  }
+  std::printf("\t.. build time = %6.4f \n", now() - t0);
+  if (saveIdx) check(rbc_save(idx, saveIdx), "saving the index");
+
+  // K columns per query: the reference's 32, or k when more are asked for;
+  // the evaluation reads the first 32
+  const uint32_t K = k > RBC_KMAX ? k : RBC_KMAX;
+  std::vector<uint32_t> ids(m * K);
+  std::vector<R> dists(m * K);
+  void *di = nullptr, *dd = nullptr;
+  cudaMalloc(&di, ids.size() * 4);
+  cudaMalloc(&dd, dists.size() * sizeof(R));
+  t0 = now();
+  cudaMemcpy(dq, q.data(), q.size() * sizeof(R), cudaMemcpyHostToDevice);
+  check(A::query(idx, (const R *)dq, m, ld, K, mode, (uint32_t *)di, (R *)dd, K), "kqueryRBC");
+  cudaMemcpy(ids.data(), di, ids.size() * 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(dists.data(), dd, dists.size() * sizeof(R), cudaMemcpyDeviceToHost);
+  std::printf("\t.. query time for krbc = %6.4f \n", now() - t0);
+
+  std::vector<uint32_t> bids;
+  std::vector<R> bdists;
+  if (runBrute || runEval) {
+    std::printf("running k-brute force..\n");
+    bids.resize(m * K);
+    bdists.resize(m * K);
+    t0 = now();
+    cudaMemcpy(dx, x.data(), x.size() * sizeof(R), cudaMemcpyHostToDevice);
+    cudaMemcpy(dq, q.data(), q.size() * sizeof(R), cudaMemcpyHostToDevice);
+    check(A::brute((const R *)dx, n, ld, (const R *)dq, m, ld, d, K, metric, (uint32_t *)di, (R *)dd, K), "bruteK");
+    cudaMemcpy(bids.data(), di, bids.size() * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(bdists.data(), dd, bdists.size() * sizeof(R), cudaMemcpyDeviceToHost);
+    std::printf("\t.. time elapsed = %6.4f \n", now() - t0);
+    if (runEval) {
+      // overlap of the returned 32 ids with brute force, and the rank of the
+      // returned 32nd neighbour (driver.cu:283-349)
+      std::printf("\nComputing error rates (this might take a while)\n");
+      double sum = 0, sum2 = 0;
+      for (uint64_t i = 0; i < m; i++) {
+        uint32_t ol = 0;
+        for (uint32_t j = 0; j < RBC_KMAX; j++)
+          for (uint32_t t = 0; t < RBC_KMAX; t++) ol += ids[i * K + j] == bids[i * K + t];
+        sum += ol;
+        sum2 += (double)ol * ol;
+      }
+      double mean = sum / m;
+      std::printf("\tavg overlap = %6.4f/%d; std dev = %6.4f \n", mean, RBC_KMAX, std::sqrt(sum2 / m - mean * mean));
+      std::vector<R> ranges(m);
+      for (uint64_t i = 0; i < m; i++) ranges[i] = dists[i * K + RBC_KMAX - 1];
+      void *dr = nullptr, *dc = nullptr;
+      cudaMalloc(&dr, m * sizeof(R));
+      cudaMalloc(&dc, m * 4);
+      cudaMemcpy(dr, ranges.data(), m * sizeof(R), cudaMemcpyHostToDevice);
+      check(A::range((const R *)dx, n, ld, (const R *)dq, m, ld, d, metric, (const R *)dr, (uint32_t *)dc),
+            "bruteRangeCount");
+      std::vector<uint32_t> cnt(m);
+      cudaMemcpy(cnt.data(), dc, m * 4, cudaMemcpyDeviceToHost);
+      sum = sum2 = 0;
+      for (uint64_t i = 0; i < m; i++) {
+        sum += cnt[i];
+        sum2 += (double)cnt[i] * cnt[i];
+      }
+      mean = sum / m;
+      std::printf("\tavg actual rank of 32nd NN returned by the RBC = %6.4f; std dev = %6.4f \n\n", mean,
+                  std::sqrt(std::max(0.0, sum2 / m - mean * mean)));
+      cudaFree(dr);
+      cudaFree(dc);
+    }
+  }
+  cudaFree(dx);
+  cudaFree(dq);
+  cudaFree(di);
+  cudaFree(dd);
+  cudaError_t cE = cudaGetLastError();
+  if (cE != cudaSuccess) std::printf("Execution failed; error type: %s \n", cudaGetErrorString(cE));
+
+  if (outB) check(A::write_bin(outB, ids.data(), dists.data(), m, k, K), "writing the output");
+  if (outT) check(A::write_text(outT, ids.data(), dists.data(), m, k, K), "writing the output");
+  rbc_destroy(idx);
+  return 0;
 }
 
 }  // namespace
@@ -145,106 +335,5 @@ int main(int argc, char **argv) {
   std::printf("GPU memory free = %lu/%lu (MB) \n", (unsigned long)(memFree >> 20), (unsigned long)(memTot >> 20));
   std::printf(" init time: %6.2f \n", now() - t0);
 
-  const uint32_t ld = (d + 15) / 16 * 16;
-  std::vector<float> x(n * ld), q(m * ld);
-  check(dbXt ? rbc_read_matrix_text(dbXt, x.data(), n, d, ld) : rbc_read_matrix_bin(dbX, x.data(), n, d, ld),
-        "reading the database");
-  check(dbQt ? rbc_read_matrix_text(dbQt, q.data(), m, d, ld) : rbc_read_matrix_bin(dbQ, q.data(), m, d, ld),
-        "reading the queries");
-
-  rbc_index *idx = nullptr;
-  std::printf("building the rbc..\n");
-  t0 = now();
-  if (loadIdx) {
-    check(rbc_load(loadIdx, &idx), "loading the index");
-  } else {
-    rbc_build_params p{};
-    p.num_reps = numReps;
-    p.s = numReps;
-    p.metric = metric;
-    p.flags = RBC_BUILD_PARTITION | (mode == RBC_QUERY_ONESHOT ? RBC_BUILD_ONESHOT : 0u) |
-              (mode == RBC_QUERY_EXACT_TC ? RBC_BUILD_BF16 : 0u);
-    p.seed = seed;
-    check(rbc_build_host(x.data(), n, d, ld, &p, &idx), "buildRBC");
-  }
-  std::printf("\t.. build time = %6.4f \n", now() - t0);
-  if (saveIdx) check(rbc_save(idx, saveIdx), "saving the index");
-
-  // K columns per query: the reference's 32, or k when more are asked for;
-  // the evaluation reads the first 32
-  const uint32_t K = k > RBC_KMAX ? k : RBC_KMAX;
-  std::vector<uint32_t> ids(m * K);
-  std::vector<float> dists(m * K);
-  t0 = now();
-  check(rbc_query_host(idx, q.data(), m, ld, K, mode, ids.data(), dists.data(), K), "kqueryRBC");
-  std::printf("\t.. query time for krbc = %6.4f \n", now() - t0);
-
-  std::vector<uint32_t> bids;
-  std::vector<float> bdists;
-  if (runBrute || runEval) {
-    std::printf("running k-brute force..\n");
-    bids.resize(m * K);
-    bdists.resize(m * K);
-    void *dx = nullptr, *dq = nullptr, *di = nullptr, *dd = nullptr;
-    cudaMalloc(&dx, x.size() * 4);
-    cudaMalloc(&dq, q.size() * 4);
-    cudaMalloc(&di, ids.size() * 4);
-    cudaMalloc(&dd, dists.size() * 4);
-    t0 = now();
-    cudaMemcpy(dx, x.data(), x.size() * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(dq, q.data(), q.size() * 4, cudaMemcpyHostToDevice);
-    check(rbc_brute_knn((float *)dx, n, ld, (float *)dq, m, ld, d, K, metric, (uint32_t *)di, (float *)dd, K,
-                        nullptr),
-          "bruteK");
-    cudaMemcpy(bids.data(), di, bids.size() * 4, cudaMemcpyDeviceToHost);
-    cudaMemcpy(bdists.data(), dd, bdists.size() * 4, cudaMemcpyDeviceToHost);
-    std::printf("\t.. time elapsed = %6.4f \n", now() - t0);
-    if (runEval) {
-      // overlap of the returned 32 ids with brute force, and the rank of the
-      // returned 32nd neighbour (driver.cu:283-349)
-      std::printf("\nComputing error rates (this might take a while)\n");
-      double sum = 0, sum2 = 0;
-      for (uint64_t i = 0; i < m; i++) {
-        uint32_t ol = 0;
-        for (uint32_t j = 0; j < RBC_KMAX; j++)
-          for (uint32_t t = 0; t < RBC_KMAX; t++) ol += ids[i * K + j] == bids[i * K + t];
-        sum += ol;
-        sum2 += (double)ol * ol;
-      }
-      double mean = sum / m;
-      std::printf("\tavg overlap = %6.4f/%d; std dev = %6.4f \n", mean, RBC_KMAX, std::sqrt(sum2 / m - mean * mean));
-      std::vector<float> ranges(m);
-      for (uint64_t i = 0; i < m; i++) ranges[i] = dists[i * K + RBC_KMAX - 1];
-      void *dr = nullptr, *dc = nullptr;
-      cudaMalloc(&dr, m * 4);
-      cudaMalloc(&dc, m * 4);
-      cudaMemcpy(dr, ranges.data(), m * 4, cudaMemcpyHostToDevice);
-      check(rbc_brute_range_count((float *)dx, n, ld, (float *)dq, m, ld, d, metric, (float *)dr, (uint32_t *)dc,
-                                  nullptr),
-            "bruteRangeCount");
-      std::vector<uint32_t> cnt(m);
-      cudaMemcpy(cnt.data(), dc, m * 4, cudaMemcpyDeviceToHost);
-      sum = sum2 = 0;
-      for (uint64_t i = 0; i < m; i++) {
-        sum += cnt[i];
-        sum2 += (double)cnt[i] * cnt[i];
-      }
-      mean = sum / m;
-      std::printf("\tavg actual rank of 32nd NN returned by the RBC = %6.4f; std dev = %6.4f \n\n", mean,
-                  std::sqrt(std::max(0.0, sum2 / m - mean * mean)));
-      cudaFree(dr);
-      cudaFree(dc);
-    }
-    cudaFree(dx);
-    cudaFree(dq);
-    cudaFree(di);
-    cudaFree(dd);
-  }
-  cudaError_t cE = cudaGetLastError();
-  if (cE != cudaSuccess) std::printf("Execution failed; error type: %s \n", cudaGetErrorString(cE));
-
-  if (outB) check(rbc_write_neighbors_bin(outB, ids.data(), dists.data(), m, k, K), "writing the output");
-  if (outT) check(rbc_write_neighbors_text(outT, ids.data(), dists.data(), m, k, K), "writing the output");
-  rbc_destroy(idx);
-  return 0;
+  return useDouble ? run<double>() : run<float>();
 }

@@ -7,7 +7,9 @@
 // row) followed by all distances (float32, k per row); the text form prints
 // "%u " / "%f " per value and a newline per row (writeNeighbs,
 // driver.cu:352-393).  Padding columns of the buffer are zeroed, which the
-// distance kernels rely on.
+// distance kernels rely on.  The _f64 forms are the same formats with
+// real = double (the reference's double build, defs.h:27-31): 8-byte values
+// in the binary files, text read as double without rounding.
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -20,51 +22,54 @@ int fail(int code, const std::string &msg);
 
 using rbc::fail;
 
-extern "C" {
+namespace {
 
-int rbc_read_matrix_bin(const char *path, float *h, uint64_t rows, uint32_t cols, uint32_t ld) {
-  if (!path || (rows && !h) || ld < cols) return fail(RBC_ERR_INVALID, "rbc_read_matrix_bin: bad argument");
+template <typename T>
+int read_matrix_bin(const char *what, const char *path, T *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  if (!path || (rows && !h) || ld < cols) return fail(RBC_ERR_INVALID, std::string(what) + ": bad argument");
   FILE *fp = std::fopen(path, "rb");
   if (!fp) return fail(RBC_ERR_IO, std::string("cannot open ") + path);
   for (uint64_t r = 0; r < rows; r++) {
-    float *row = h + r * ld;
-    size_t got = std::fread(row, sizeof(float), cols, fp);
+    T *row = h + r * ld;
+    size_t got = std::fread(row, sizeof(T), cols, fp);
     if (got != cols) {
       std::fclose(fp);
       return fail(RBC_ERR_IO, std::string("short read in ") + path + " at row " + std::to_string(r));
     }
-    if (ld > cols) std::memset(row + cols, 0, (ld - cols) * sizeof(float));
+    if (ld > cols) std::memset(row + cols, 0, (ld - cols) * sizeof(T));
   }
   std::fclose(fp);
   return RBC_OK;
 }
 
-int rbc_read_matrix_text(const char *path, float *h, uint64_t rows, uint32_t cols, uint32_t ld) {
-  if (!path || (rows && !h) || ld < cols) return fail(RBC_ERR_INVALID, "rbc_read_matrix_text: bad argument");
+template <typename T>
+int read_matrix_text(const char *what, const char *path, T *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  if (!path || (rows && !h) || ld < cols) return fail(RBC_ERR_INVALID, std::string(what) + ": bad argument");
   FILE *fp = std::fopen(path, "r");
   if (!fp) return fail(RBC_ERR_IO, std::string("cannot open ") + path);
   for (uint64_t r = 0; r < rows; r++) {
-    float *row = h + r * ld;
+    T *row = h + r * ld;
     for (uint32_t c = 0; c < cols; c++) {
       double t;
       if (std::fscanf(fp, "%lf", &t) != 1) {
         std::fclose(fp);
         return fail(RBC_ERR_IO, std::string("short read in ") + path + " at row " + std::to_string(r));
       }
-      row[c] = (float)t;
+      row[c] = (T)t;
     }
-    if (ld > cols) std::memset(row + cols, 0, (ld - cols) * sizeof(float));
+    if (ld > cols) std::memset(row + cols, 0, (ld - cols) * sizeof(T));
   }
   std::fclose(fp);
   return RBC_OK;
 }
 
-int rbc_write_matrix_bin(const char *path, const float *h, uint64_t rows, uint32_t cols, uint32_t ld) {
-  if (!path || (rows && !h) || ld < cols) return fail(RBC_ERR_INVALID, "rbc_write_matrix_bin: bad argument");
+template <typename T>
+int write_matrix_bin(const char *what, const char *path, const T *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  if (!path || (rows && !h) || ld < cols) return fail(RBC_ERR_INVALID, std::string(what) + ": bad argument");
   FILE *fp = std::fopen(path, "wb");
   if (!fp) return fail(RBC_ERR_IO, std::string("cannot open ") + path);
   for (uint64_t r = 0; r < rows; r++) {
-    if (std::fwrite(h + r * ld, sizeof(float), cols, fp) != cols) {
+    if (std::fwrite(h + r * ld, sizeof(T), cols, fp) != cols) {
       std::fclose(fp);
       return fail(RBC_ERR_IO, std::string("short write to ") + path);
     }
@@ -72,21 +77,23 @@ int rbc_write_matrix_bin(const char *path, const float *h, uint64_t rows, uint32
   return std::fclose(fp) == 0 ? RBC_OK : fail(RBC_ERR_IO, std::string("close failed: ") + path);
 }
 
-int rbc_write_neighbors_bin(const char *path, const uint32_t *ids, const float *dists, uint64_t m, uint32_t k,
-                            uint32_t ld) {
-  if (!path || (m && (!ids || !dists)) || ld < k) return fail(RBC_ERR_INVALID, "rbc_write_neighbors_bin: bad argument");
+template <typename T>
+int write_neighbors_bin(const char *what, const char *path, const uint32_t *ids, const T *dists, uint64_t m,
+                        uint32_t k, uint32_t ld) {
+  if (!path || (m && (!ids || !dists)) || ld < k) return fail(RBC_ERR_INVALID, std::string(what) + ": bad argument");
   FILE *fp = std::fopen(path, "wb");
   if (!fp) return fail(RBC_ERR_IO, std::string("cannot open ") + path);
   bool ok = true;
   for (uint64_t i = 0; i < m && ok; i++) ok = std::fwrite(ids + i * ld, sizeof(uint32_t), k, fp) == k;
-  for (uint64_t i = 0; i < m && ok; i++) ok = std::fwrite(dists + i * ld, sizeof(float), k, fp) == k;
+  for (uint64_t i = 0; i < m && ok; i++) ok = std::fwrite(dists + i * ld, sizeof(T), k, fp) == k;
   if (std::fclose(fp) != 0) ok = false;
   return ok ? RBC_OK : fail(RBC_ERR_IO, std::string("short write to ") + path);
 }
 
-int rbc_write_neighbors_text(const char *path, const uint32_t *ids, const float *dists, uint64_t m, uint32_t k,
-                             uint32_t ld) {
-  if (!path || (m && (!ids || !dists)) || ld < k) return fail(RBC_ERR_INVALID, "rbc_write_neighbors_text: bad argument");
+template <typename T>
+int write_neighbors_text(const char *what, const char *path, const uint32_t *ids, const T *dists, uint64_t m,
+                         uint32_t k, uint32_t ld) {
+  if (!path || (m && (!ids || !dists)) || ld < k) return fail(RBC_ERR_INVALID, std::string(what) + ": bad argument");
   FILE *fp = std::fopen(path, "w");
   if (!fp) return fail(RBC_ERR_IO, std::string("cannot open ") + path);
   for (uint64_t i = 0; i < m; i++) {
@@ -94,10 +101,50 @@ int rbc_write_neighbors_text(const char *path, const uint32_t *ids, const float 
     std::fprintf(fp, "\n");
   }
   for (uint64_t i = 0; i < m; i++) {
-    for (uint32_t j = 0; j < k; j++) std::fprintf(fp, "%f ", dists[i * ld + j]);
+    for (uint32_t j = 0; j < k; j++) std::fprintf(fp, "%f ", (double)dists[i * ld + j]);
     std::fprintf(fp, "\n");
   }
   return std::fclose(fp) == 0 ? RBC_OK : fail(RBC_ERR_IO, std::string("close failed: ") + path);
+}
+
+}  // namespace
+
+extern "C" {
+
+int rbc_read_matrix_bin(const char *path, float *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  return read_matrix_bin("rbc_read_matrix_bin", path, h, rows, cols, ld);
+}
+int rbc_read_matrix_text(const char *path, float *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  return read_matrix_text("rbc_read_matrix_text", path, h, rows, cols, ld);
+}
+int rbc_write_matrix_bin(const char *path, const float *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  return write_matrix_bin("rbc_write_matrix_bin", path, h, rows, cols, ld);
+}
+int rbc_write_neighbors_bin(const char *path, const uint32_t *ids, const float *dists, uint64_t m, uint32_t k,
+                            uint32_t ld) {
+  return write_neighbors_bin("rbc_write_neighbors_bin", path, ids, dists, m, k, ld);
+}
+int rbc_write_neighbors_text(const char *path, const uint32_t *ids, const float *dists, uint64_t m, uint32_t k,
+                             uint32_t ld) {
+  return write_neighbors_text("rbc_write_neighbors_text", path, ids, dists, m, k, ld);
+}
+
+int rbc_read_matrix_bin_f64(const char *path, double *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  return read_matrix_bin("rbc_read_matrix_bin_f64", path, h, rows, cols, ld);
+}
+int rbc_read_matrix_text_f64(const char *path, double *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  return read_matrix_text("rbc_read_matrix_text_f64", path, h, rows, cols, ld);
+}
+int rbc_write_matrix_bin_f64(const char *path, const double *h, uint64_t rows, uint32_t cols, uint32_t ld) {
+  return write_matrix_bin("rbc_write_matrix_bin_f64", path, h, rows, cols, ld);
+}
+int rbc_write_neighbors_bin_f64(const char *path, const uint32_t *ids, const double *dists, uint64_t m, uint32_t k,
+                                uint32_t ld) {
+  return write_neighbors_bin("rbc_write_neighbors_bin_f64", path, ids, dists, m, k, ld);
+}
+int rbc_write_neighbors_text_f64(const char *path, const uint32_t *ids, const double *dists, uint64_t m, uint32_t k,
+                                 uint32_t ld) {
+  return write_neighbors_text("rbc_write_neighbors_text_f64", path, ids, dists, m, k, ld);
 }
 
 }  // extern "C"

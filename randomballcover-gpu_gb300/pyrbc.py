@@ -104,6 +104,11 @@ SIGNATURES = {
     "rbc_write_matrix_bin": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
     "rbc_write_neighbors_bin": ([C.c_char_p, _VP, _VP, _U64, _U32, _U32], _INT),
     "rbc_write_neighbors_text": ([C.c_char_p, _VP, _VP, _U64, _U32, _U32], _INT),
+    "rbc_read_matrix_bin_f64": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
+    "rbc_read_matrix_text_f64": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
+    "rbc_write_matrix_bin_f64": ([C.c_char_p, _VP, _U64, _U32, _U32], _INT),
+    "rbc_write_neighbors_bin_f64": ([C.c_char_p, _VP, _VP, _U64, _U32, _U32], _INT),
+    "rbc_write_neighbors_text_f64": ([C.c_char_p, _VP, _VP, _U64, _U32, _U32], _INT),
 }
 
 _lib = None

@@ -26,6 +26,12 @@ def test_cli_usage_and_argument_errors(engine_lib):
     assert r.returncode == 1 and "more representatives than points" in r.stderr
     r = subprocess.run([exe, "-Z"], capture_output=True, text=True)
     assert r.returncode == 1 and "unrecognized option" in r.stderr
+    r = subprocess.run([exe, "-D", "-M", "oneshot", "-x", "a", "-q", "b", "-n", "100", "-m", "10", "-d", "4", "-r",
+                        "32"], capture_output=True, text=True)
+    assert r.returncode == 1 and "double precision" in r.stderr
+    r = subprocess.run([exe, "-x", "a", "-q", "b", "-n", "100", "-m", "10", "-d", "4", "-r", "32", "-k", "129"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "k must be in [1, 128]" in r.stderr
 
 
 def test_load_rejects_bad_files(engine_lib, tmp_path):
@@ -98,3 +104,34 @@ def test_index_file_round_trip(rbc, tmp_path):
     assert e.value.code == rbc.ERR_IO
     idx.close()
     back.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["exact", "tc"])
+def test_cli_double_build(engine_lib, rbc, tmp_path, mode):
+    """-D: the reference's real = double build: 8-byte values in and out."""
+    exe = cli(engine_lib)
+    g = load_golden("f64_cases")
+    xf, qf, out = str(tmp_path / "x64.bin"), str(tmp_path / "q64.bin"), str(tmp_path / "out64.bin")
+    g["sample_X"].astype(np.float64).tofile(xf)
+    g["sample_Q"].astype(np.float64).tofile(qf)
+    idxf = str(tmp_path / "x64.idx")
+    args = [exe, "-D", "-x", xf, "-q", qf, "-n", "1024", "-m", "128", "-d", "16", "-r", "128", "-o", out, "-M", mode,
+            "-S", idxf, "-e"]
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = np.fromfile(out, np.uint8)
+    assert raw.size == 128 * 32 * (4 + 8)
+    ids = raw[: 128 * 32 * 4].view(np.uint32).reshape(128, 32)
+    dists = raw[128 * 32 * 4:].view(np.float64).reshape(128, 32)
+    np.testing.assert_array_equal(ids, g["sample_ids_l2"])
+    np.testing.assert_array_equal(dists, g["sample_dists_l2"])
+    assert "avg overlap = 32.0000/32" in r.stdout
+    out2 = str(tmp_path / "out64b.bin")
+    r = subprocess.run(args[:args.index("-r")] + ["-L", idxf, "-o", out2, "-M", mode], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert open(out, "rb").read() == open(out2, "rb").read()
+    # an index of one precision is refused by the other
+    r = subprocess.run([a for a in args[:args.index("-r")] if a != "-D"] + ["-L", idxf], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "other precision" in r.stderr
