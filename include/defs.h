@@ -26,8 +26,16 @@
  * (rbc_set_legacy_metric); this macro is the default L2 term. */
 #define DIST(i, j) (((i) - (j)) * ((i) - (j)))
 
+/* The reference switches to double by editing these two lines
+ * (defs.h:27-31, readme.txt:134-152); here RBC_REAL_DOUBLE selects the double
+ * build, whose library is librbcgb_f64.so. */
+#ifdef RBC_REAL_DOUBLE
+typedef double real;
+#define MAX_REAL DBL_MAX
+#else
 typedef float real;
 #define MAX_REAL FLT_MAX
+#endif
 
 #define MEM_USABLE .95
 #define DUMMY_IDX UINT_MAX

@@ -1,5 +1,7 @@
 """Build librbcgb.so in-tree: every csrc/*.cu / *.cpp compiled for sm_103a with
-nvcc (in parallel), linked into one shared library next to this file.
+nvcc (in parallel), linked into one shared library next to this file.  The
+legacy C++ API is compiled a second time with RBC_REAL_DOUBLE (the reference's
+real = double build) and linked with the same objects into librbcgb_f64.so.
 
     python randomballcover-gpu_gb300/build_ext.py [--force]
 """
@@ -12,6 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librbcgb.so")
+LIB64 = os.path.join(HERE, "librbcgb_f64.so")
+LEGACY = os.path.join(CSRC, "legacy.cu")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -31,12 +35,13 @@ def headers():
     return hs
 
 
-def _compile(src):
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(job):
+    src, defs = job if isinstance(job, tuple) else (job, [])
+    obj = os.path.join(BUILD, os.path.basename(src) + ("".join(d.replace("-D", ".") for d in defs)) + ".o")
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in headers()])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj, None
-    cmd = [NVCC] + ARCH + COMMON + ["-c", src, "-o", obj]
+    cmd = [NVCC] + ARCH + COMMON + defs + ["-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd = [NVCC] + COMMON + ["-x", "c++", "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -51,17 +56,21 @@ def build(force=False, verbose=False):
         for f in os.listdir(BUILD):
             os.remove(os.path.join(BUILD, f))
     srcs = sources()
-    with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        results = list(ex.map(_compile, srcs))
+    jobs = srcs + [(LEGACY, ["-DRBC_REAL_DOUBLE"])]
+    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+        results = list(ex.map(_compile, jobs))
     errors = [e for _, e in results if e]
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    objs = [o for o, _ in results]
-    if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}{r.stderr}")
+    objs = [o for o, _ in results[:len(srcs)]]
+    legacy_obj = objs[srcs.index(LEGACY)]
+    objs64 = [o for o in objs if o != legacy_obj] + [results[-1][0]]
+    for lib, parts in ((LIB, objs), (LIB64, objs64)):
+        if not (os.path.exists(lib) and os.path.getmtime(lib) >= max(os.path.getmtime(o) for o in parts)):
+            cmd = [NVCC] + ARCH + ["-shared", "-o", lib] + parts
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}{r.stderr}")
     build_cli()
     if verbose:
         print("built", LIB, "and", CLI)

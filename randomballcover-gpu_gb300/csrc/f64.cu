@@ -350,6 +350,15 @@ __global__ void __launch_bounds__(256) f64_range_kernel(const ScanArgs64 a) {
   }
 }
 
+// D[i][j] = double distance of row i of A and row j of B (16 x 16 threads
+// per block, one pair each).
+template <int METRIC>
+__global__ void f64_dense_kernel(const double *__restrict__ A, uint64_t na, const double *__restrict__ B, uint64_t nb,
+                                 uint32_t lda, uint32_t ldb, uint32_t d, double *__restrict__ D, uint64_t ldD) {
+  const uint64_t i = blockIdx.y * 16ull + threadIdx.y, j = blockIdx.x * 16ull + threadIdx.x;
+  if (i < na && j < nb) D[i * ldD + j] = dist64<METRIC>(A + i * lda, B + j * ldb, d);
+}
+
 uint32_t scan_chunks(uint64_t n, uint32_t nslots) {
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
@@ -487,6 +496,22 @@ int check_f64_args(uint32_t d, uint32_t ldx, uint32_t ldq, uint32_t k, uint32_t 
 
 }  // namespace
 
+cudaError_t launch_dense_dist64(int metric, const double *A, uint64_t na, const double *B, uint64_t nb, uint32_t ld,
+                                uint32_t d, double *D, uint64_t ldD, cudaStream_t s) {
+  if (na == 0 || nb == 0) return cudaSuccess;
+  for (uint64_t i0 = 0; i0 < na; i0 += 16ull * 65535) {
+    const uint64_t rows = std::min<uint64_t>(na - i0, 16ull * 65535);
+    const dim3 grid((unsigned)((nb + 15) / 16), (unsigned)((rows + 15) / 16));
+    if (metric == RBC_L1)
+      f64_dense_kernel<RBC_L1><<<grid, dim3(16, 16), 0, s>>>(A + i0 * ld, rows, B, nb, ld, ld, d, D + i0 * ldD, ldD);
+    else
+      f64_dense_kernel<RBC_L2><<<grid, dim3(16, 16), 0, s>>>(A + i0 * ld, rows, B, nb, ld, ld, d, D + i0 * ldD, ldD);
+    cudaError_t e = launched();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // Build from double rows: the FP32 index over the float-rounded rows, plus
 // the double rows (original order) and their largest norms for the rerank.
 int build_index_f64(const double *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *p,
@@ -500,15 +525,22 @@ int build_index_f64(const double *dX, uint64_t n, uint32_t d, uint32_t ldx, cons
   if (n == 0 || n >= 0xFFFFFFFFull) return fail(RBC_ERR_INVALID, "rbc_build_f64: n must be in [1, 2^32-1)");
   if (p->flags & RBC_BUILD_ONESHOT)
     return fail(RBC_ERR_UNSUPPORTED, "rbc_build_f64: one-shot lists are built from float distances only");
-  const uint32_t ld32 = pad16(d), ld64 = (d + 1) / 2 * 2;
+  // the legacy API's layout (kBuildKeepInput): rows of pad16(d) doubles and
+  // pad16(n) rows, the padding zero, exposed as its rbcStruct.dx
+  const bool legacy = (p->flags & kBuildKeepInput) != 0;
+  rbc_build_params pf = *p;
+  pf.flags &= ~kBuildKeepInput;
+  const uint32_t ld32 = pad16(d), ld64 = legacy ? pad16(d) : (d + 1) / 2 * 2;
+  const uint64_t rows64 = legacy ? (n + 15) / 16 * 16 : n;
   DevBuf Xf, ctl;
   double *X64 = nullptr;
   unsigned long long *nm = nullptr;
   FCK(Xf.alloc(n * ld32 * 4, s));
   FCK(ctl.alloc(16, s));
   FCK(cudaMemsetAsync(ctl.p, 0, 16, s));
-  FCK(cudaMalloc((void **)&X64, n * ld64 * 8));
-  cudaError_t e = cudaMalloc((void **)&nm, 16);
+  FCK(cudaMalloc((void **)&X64, rows64 * ld64 * 8));
+  cudaError_t e = rows64 > n ? cudaMemsetAsync(X64 + n * ld64, 0, (rows64 - n) * ld64 * 8, s) : cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc((void **)&nm, 16);
   if (e == cudaSuccess) e = cudaMemsetAsync(nm, 0, 16, s);
   if (e == cudaSuccess) e = launch_prep(dX, ldx, n, d, Xf.as<float>(), ld32, X64, ld64, nm, ctl.as<uint32_t>(), s);
   uint32_t flag = 0;
@@ -518,7 +550,7 @@ int build_index_f64(const double *dX, uint64_t n, uint32_t d, uint32_t ldx, cons
   if (rc == RBC_OK && flag)
     rc = fail(RBC_ERR_UNSUPPORTED, "rbc_build_f64: values must be finite and within +-2^56");
   rbc_index *idx = nullptr;
-  if (rc == RBC_OK) rc = build_index(Xf.as<float>(), n, d, ld32, p, s, &idx);
+  if (rc == RBC_OK) rc = build_index(Xf.as<float>(), n, d, ld32, &pf, s, &idx);
   if (rc != RBC_OK) {
     cudaFree(X64);
     if (nm) cudaFree(nm);
@@ -528,7 +560,7 @@ int build_index_f64(const double *dX, uint64_t n, uint32_t d, uint32_t ldx, cons
   idx->ld64 = ld64;
   idx->norm64 = nm;
   idx->flags |= RBC_BUILD_F64;
-  idx->device_bytes += n * ld64 * 8 + 16;
+  idx->device_bytes += rows64 * ld64 * 8 + 16;
   *out = idx;
   return RBC_OK;
 }

@@ -79,6 +79,9 @@ cudaError_t launch_gather_rows(const float *src, uint32_t ld, const uint32_t *ro
 // Dense distances: D[i][j] = dist(A row i, B row j) for i < na, j < nb.
 cudaError_t launch_dense_dist(int metric, const float *A, uint64_t na, const float *B, uint64_t nb,
                               uint32_t ld, uint32_t dp, float *D, uint64_t ldD, cudaStream_t s);
+// The same in double, the double build's arithmetic (f64.cu).
+cudaError_t launch_dense_dist64(int metric, const double *A, uint64_t na, const double *B, uint64_t nb, uint32_t ld,
+                                uint32_t d, double *D, uint64_t ldD, cudaStream_t s);
 // Nearest row of B for every row of A under (dist, index).
 cudaError_t launch_argmin(int metric, const float *A, uint64_t na, const float *B, uint32_t nb,
                           uint32_t ld, uint32_t dp, uint32_t *best, float *bestd, cudaStream_t s);

@@ -9,6 +9,12 @@
 // also holds the partition for exact search is found again from rbcS.dx.mat,
 // so the caller-allocated rbcStruct layout is unchanged.  Errors follow the
 // reference's checkErr convention: a message on stderr and exit(1).
+//
+// Compiled a second time with RBC_REAL_DOUBLE (librbcgb_f64.so), this file is
+// the API of the reference's double build (real = double, defs.h:27-31): the
+// same functions over double matrices, answered by the library's double-
+// precision calls.  The one-shot lists are float-only there: rbcS.dxMap stays
+// empty and the one-shot query mode is refused.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -64,14 +70,52 @@ rbc_index *lookup(const rbcStruct &r) {
   return it->second;
 }
 
-float dist_host(const float *a, const float *b, unint d) {
-  float acc = 0.f;
+real dist_host(const real *a, const real *b, unint d) {
+  real acc = 0;
   for (unint i = 0; i < d; i++) {
-    volatile float t = a[i] - b[i];  // keep each operation rounded on its own
-    volatile float term = g_metric == RBC_L1 ? std::fabs(t) : t * t;
+    volatile real t = a[i] - b[i];  // keep each operation rounded on its own
+    volatile real term = g_metric == RBC_L1 ? std::fabs(t) : t * t;
     acc = acc + term;
   }
   return acc;
+}
+
+// The engine's calls of each precision, chosen by the type of `real`.
+int eng_brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,
+                  uint32_t k, uint32_t *ids, float *dists, uint32_t ldo) {
+  return rbc_brute_knn(dX, n, ldx, dQ, m, ldq, d, k, g_metric, ids, dists, ldo, nullptr);
+}
+int eng_brute_knn(const double *dX, uint64_t n, uint32_t ldx, const double *dQ, uint64_t m, uint32_t ldq, uint32_t d,
+                  uint32_t k, uint32_t *ids, double *dists, uint32_t ldo) {
+  return rbc_brute_knn_f64(dX, n, ldx, dQ, m, ldq, d, k, g_metric, ids, dists, ldo, nullptr, nullptr);
+}
+int eng_range_count(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,
+                    const float *r, uint32_t *c) {
+  return rbc_brute_range_count(dX, n, ldx, dQ, m, ldq, d, g_metric, r, c, nullptr);
+}
+int eng_range_count(const double *dX, uint64_t n, uint32_t ldx, const double *dQ, uint64_t m, uint32_t ldq,
+                    uint32_t d, const double *r, uint32_t *c) {
+  return rbc_brute_range_count_f64(dX, n, ldx, dQ, m, ldq, d, g_metric, r, c, nullptr);
+}
+int eng_query_host(rbc_index *idx, const float *hQ, uint64_t m, uint32_t ldq, uint32_t k, unsigned mode,
+                   uint32_t *hIds, float *hD, uint32_t ldo) {
+  return rbc_query_host(idx, hQ, m, ldq, k, mode, hIds, hD, ldo);
+}
+int eng_query_host(rbc_index *idx, const double *hQ, uint64_t m, uint32_t ldq, uint32_t k, unsigned mode,
+                   uint32_t *hIds, double *hD, uint32_t ldo) {
+  void *q = nullptr, *ids = nullptr, *dd = nullptr;
+  cudaError_t e = cudaMalloc(&q, m * ldq * 8 + 16);
+  if (e == cudaSuccess) e = cudaMalloc(&ids, m * ldo * 4 + 16);
+  if (e == cudaSuccess) e = cudaMalloc(&dd, m * ldo * 8 + 16);
+  if (e == cudaSuccess) e = cudaMemcpy(q, hQ, m * ldq * 8, cudaMemcpyHostToDevice);
+  int rc = e == cudaSuccess ? RBC_OK : RBC_ERR_CUDA;
+  if (rc == RBC_OK) rc = rbc_query_f64(idx, (const double *)q, m, ldq, k, mode, (uint32_t *)ids, (double *)dd, ldo, nullptr);
+  if (rc == RBC_OK && cudaMemcpy(hIds, ids, m * ldo * 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = RBC_ERR_CUDA;
+  if (rc == RBC_OK && cudaMemcpy(hD, dd, m * ldo * 8, cudaMemcpyDeviceToHost) != cudaSuccess) rc = RBC_ERR_CUDA;
+  cudaFree(q);
+  cudaFree(ids);
+  cudaFree(dd);
+  return rc;
 }
 
 }  // namespace
@@ -92,9 +136,46 @@ void buildRBC(const matrix x, rbcStruct *rbcS, unint numReps, unint s) {
   p.num_reps = numReps;
   p.s = s;
   p.metric = g_metric;
-  p.flags = RBC_BUILD_PARTITION | RBC_BUILD_ONESHOT | rbc::kBuildKeepInput;
   p.seed = legacy_seed();
   rbc_index *idx = nullptr;
+#ifdef RBC_REAL_DOUBLE
+  // the double build: the partition over double rows (kept in the padded
+  // legacy layout as rbcS.dx); no one-shot lists
+  p.flags = RBC_BUILD_PARTITION | rbc::kBuildKeepInput;
+  double *dX = nullptr;
+  checkErr(cudaMalloc(&dX, (size_t)x.r * x.ld * sizeof(real) + 16));
+  checkErr(cudaMemcpy(dX, x.mat, (size_t)x.r * x.ld * sizeof(real), cudaMemcpyHostToDevice));
+  int rc = rbc_build_f64(dX, x.r, x.c, x.ld, &p, nullptr, &idx);
+  cudaFree(dX);
+  check("buildRBC", rc);
+  rbcS->dx.mat = idx->X64;
+  rbcS->dx.r = x.r;
+  rbcS->dx.c = x.c;
+  rbcS->dx.pr = PAD(x.r);
+  rbcS->dx.pc = rbcS->dx.ld = idx->ld64;
+  {
+    matrix r;
+    r.r = numReps;
+    r.pr = PAD(numReps);
+    r.c = x.c;
+    r.pc = r.ld = PAD(x.c);
+    std::vector<real> buf((size_t)r.pr * r.pc, 0);
+    r.mat = buf.data();
+    for (unint i = 0; i < numReps; i++)
+      copyVector(&r.mat[IDX(i, 0, r.ld)], &x.mat[IDX(idx->rep_ids[i], 0, x.ld)], x.c);
+    copyAndMove(&rbcS->dr, &r);
+  }
+  rbcS->dxMap.mat = nullptr;
+  rbcS->dxMap.r = numReps;
+  rbcS->dxMap.c = 0;
+  rbcS->dxMap.pr = PAD(numReps);
+  rbcS->dxMap.pc = rbcS->dxMap.ld = 0;
+  rbcS->groupCount = (unint *)std::calloc(PAD(numReps), sizeof(unint));
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_indexes[idx->X64] = idx;
+  (void)s;
+#else
+  p.flags = RBC_BUILD_PARTITION | RBC_BUILD_ONESHOT | rbc::kBuildKeepInput;
   check("buildRBC", rbc_build_host(x.mat, x.r, x.c, x.ld, &p, &idx));
   rbcS->dx.mat = idx->Xi;
   rbcS->dx.r = x.r;
@@ -115,17 +196,18 @@ void buildRBC(const matrix x, rbcStruct *rbcS, unint numReps, unint s) {
   check("buildRBC", rbc_get_oneshot(idx, nullptr, rbcS->groupCount));
   std::lock_guard<std::mutex> lk(g_mu);
   g_indexes[idx->Xi] = idx;
+#endif
 }
 
 void queryRBC(const matrix q, const rbcStruct rbcS, unint *NNs, real *NNdists) {
   rbc_index *idx = lookup(rbcS);
-  std::vector<float> d(q.r);
-  check("queryRBC", rbc_query_host(idx, q.mat, q.r, q.ld, 1, g_query_mode, NNs, NNdists ? NNdists : d.data(), 1));
+  std::vector<real> d(q.r);
+  check("queryRBC", eng_query_host(idx, q.mat, q.r, q.ld, 1, g_query_mode, NNs, NNdists ? NNdists : d.data(), 1));
 }
 
 void kqueryRBC(const matrix q, const rbcStruct rbcS, intMatrix NNs, matrix NNdists) {
   rbc_index *idx = lookup(rbcS);
-  check("kqueryRBC", rbc_query_host(idx, q.mat, q.r, q.ld, KMAX, g_query_mode, NNs.mat, NNdists.mat, NNs.ld));
+  check("kqueryRBC", eng_query_host(idx, q.mat, q.r, q.ld, KMAX, g_query_mode, NNs.mat, NNdists.mat, NNs.ld));
   if (NNdists.ld != NNs.ld)
     die("kqueryRBC: NNs and NNdists must share the leading dimension", RBC_ERR_INVALID);
 }
@@ -142,6 +224,9 @@ void destroyRBC(rbcStruct *rbcS) {
     }
   }
   rbc_destroy(idx);
+#ifdef RBC_REAL_DOUBLE
+  cudaFree(rbcS->dr.mat);  // the double representatives belong to this layer
+#endif
   std::free(rbcS->groupCount);
   rbcS->groupCount = nullptr;
   rbcS->dx.mat = nullptr;
@@ -153,8 +238,13 @@ void destroyRBC(rbcStruct *rbcS) {
 // the device matrix dD (rbc.cu:356-360).
 void distSubMat(matrix dr, matrix dx, matrix dD, unint start, unint length) {
   if (dr.ld != dx.ld || dr.ld % 4) die("distSubMat: operands must share a padded leading dimension", RBC_ERR_INVALID);
+#ifdef RBC_REAL_DOUBLE
+  cudaError_t e = rbc::launch_dense_dist64(g_metric, dr.mat + (size_t)start * dr.ld, length, dx.mat, dx.pr, dx.ld, dx.c,
+                                           dD.mat, dD.ld, nullptr);
+#else
   cudaError_t e = rbc::launch_dense_dist(g_metric, dr.mat + (size_t)start * dr.ld, length, dx.mat, dx.pr, dx.ld,
                                          rbc::pad4(dx.c), dD.mat, dD.ld, nullptr);
+#endif
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) checkErr(e);
 }
@@ -162,12 +252,20 @@ void distSubMat(matrix dr, matrix dx, matrix dD, unint start, unint length) {
 // Nearest row of dr for every row of dq, results on the host (rbc.cu:233-247).
 void computeReps(matrix dq, matrix dr, unint *repIDs, real *distToReps) {
   unint *dIds = nullptr;
-  float *dD = nullptr;
+  real *dD = nullptr;
   checkErr(cudaMalloc(&dIds, (size_t)dq.r * 4));
-  checkErr(cudaMalloc(&dD, (size_t)dq.r * 4));
+  checkErr(cudaMalloc(&dD, (size_t)dq.r * sizeof(real)));
+#ifdef RBC_REAL_DOUBLE
+  // nearest representative under (dist, index) in double
+  const int rc = rbc_brute_knn_f64(dr.mat, dr.r, dr.ld, dq.mat, dq.r, dq.ld, dq.c, 1, g_metric, dIds, dD, 1, nullptr,
+                                   nullptr);
+  if (rc != RBC_OK) die("computeReps", rc);
+  cudaError_t e = cudaSuccess;
+#else
   cudaError_t e = rbc::launch_argmin(g_metric, dq.mat, dq.r, dr.mat, dr.r, dq.ld, rbc::pad4(dq.c), dIds, dD, nullptr);
+#endif
   if (e == cudaSuccess) e = cudaMemcpy(repIDs, dIds, (size_t)dq.r * 4, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess && distToReps) e = cudaMemcpy(distToReps, dD, (size_t)dq.r * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && distToReps) e = cudaMemcpy(distToReps, dD, (size_t)dq.r * sizeof(real), cudaMemcpyDeviceToHost);
   cudaFree(dIds);
   cudaFree(dD);
   if (e != cudaSuccess) checkErr(e);
@@ -213,7 +311,7 @@ void setupReps(matrix x, rbcStruct *rbcS, unint numReps) {
   r.pr = PAD(numReps);
   r.c = x.c;
   r.pc = r.ld = PAD(x.c);
-  std::vector<real> buf((size_t)r.pr * r.pc, 0.f);
+  std::vector<real> buf((size_t)r.pr * r.pc, 0);
   r.mat = buf.data();
   for (unint i = 0; i < numReps; i++) copyVector(&r.mat[IDX(i, 0, r.ld)], &x.mat[IDX(ids[i], 0, x.ld)], x.c);
   copyAndMove(&rbcS->dr, &r);
@@ -222,7 +320,7 @@ void setupReps(matrix x, rbcStruct *rbcS, unint numReps) {
 // ------------------------------------------------------------------ brute.h
 namespace {
 struct DevMat {
-  float *p = nullptr;
+  real *p = nullptr;
   DevMat(const matrix &m) {
     size_t b = (size_t)m.pr * m.pc * sizeof(real);
     checkErr(cudaMalloc(&p, b ? b : 16));
@@ -234,12 +332,12 @@ struct DevMat {
 
 void bruteRangeCount(matrix x, matrix q, real *ranges, unint *cnts) {
   DevMat dx(x), dq(q);
-  float *dr = nullptr;
+  real *dr = nullptr;
   unint *dc = nullptr;
-  checkErr(cudaMalloc(&dr, (size_t)q.pr * 4));
+  checkErr(cudaMalloc(&dr, (size_t)q.pr * sizeof(real)));
   checkErr(cudaMalloc(&dc, (size_t)q.pr * 4));
-  checkErr(cudaMemcpy(dr, ranges, (size_t)q.r * 4, cudaMemcpyHostToDevice));
-  int rc = rbc_brute_range_count(dx.p, x.r, x.ld, dq.p, q.r, q.ld, x.c, g_metric, dr, dc, nullptr);
+  checkErr(cudaMemcpy(dr, ranges, (size_t)q.r * sizeof(real), cudaMemcpyHostToDevice));
+  int rc = eng_range_count(dx.p, x.r, x.ld, dq.p, q.r, q.ld, x.c, dr, dc);
   if (rc == RBC_OK) checkErr(cudaMemcpy(cnts, dc, (size_t)q.r * 4, cudaMemcpyDeviceToHost));
   cudaFree(dr);
   cudaFree(dc);
@@ -250,7 +348,7 @@ void bruteSearch(matrix x, matrix q, unint *NNs) {
   DevMat dx(x), dq(q);
   unint *di = nullptr;
   checkErr(cudaMalloc(&di, (size_t)q.pr * 4));
-  int rc = rbc_brute_knn(dx.p, x.r, x.ld, dq.p, q.r, q.ld, x.c, 1, g_metric, di, nullptr, 1, nullptr);
+  int rc = eng_brute_knn(dx.p, x.r, x.ld, dq.p, q.r, q.ld, x.c, 1, di, (real *)nullptr, 1);
   if (rc == RBC_OK) checkErr(cudaMemcpy(NNs, di, (size_t)q.r * 4, cudaMemcpyDeviceToHost));
   cudaFree(di);
   check("bruteSearch", rc);
@@ -259,13 +357,14 @@ void bruteSearch(matrix x, matrix q, unint *NNs) {
 void bruteK(matrix x, matrix q, intMatrix NNs, matrix NNdists) {
   DevMat dx(x), dq(q);
   unint *di = nullptr;
-  float *dd = nullptr;
+  real *dd = nullptr;
   checkErr(cudaMalloc(&di, (size_t)q.pr * NNs.ld * 4));
-  checkErr(cudaMalloc(&dd, (size_t)q.pr * NNdists.ld * 4));
-  int rc = rbc_brute_knn(dx.p, x.r, x.ld, dq.p, q.r, q.ld, x.c, KMAX, g_metric, di, dd, NNs.ld, nullptr);
+  checkErr(cudaMalloc(&dd, (size_t)q.pr * NNs.ld * sizeof(real)));
+  int rc = eng_brute_knn(dx.p, x.r, x.ld, dq.p, q.r, q.ld, x.c, KMAX, di, dd, NNs.ld);
   if (rc == RBC_OK) {
     checkErr(cudaMemcpy(NNs.mat, di, (size_t)q.r * NNs.ld * 4, cudaMemcpyDeviceToHost));
-    checkErr(cudaMemcpy2D(NNdists.mat, NNdists.ld * 4, dd, NNs.ld * 4, KMAX * 4, q.r, cudaMemcpyDeviceToHost));
+    checkErr(cudaMemcpy2D(NNdists.mat, NNdists.ld * sizeof(real), dd, NNs.ld * sizeof(real), KMAX * sizeof(real), q.r,
+                          cudaMemcpyDeviceToHost));
   }
   cudaFree(di);
   cudaFree(dd);
@@ -275,10 +374,10 @@ void bruteK(matrix x, matrix q, intMatrix NNs, matrix NNdists) {
 // Host 1-NN, ids scanned upward with a strict '<' (brute.cu:91-112).
 void bruteCPU(matrix X, matrix Q, unint *NNs) {
   for (unint i = 0; i < Q.r; i++) {
-    float best = MAX_REAL;
+    real best = MAX_REAL;
     NNs[i] = 0;
     for (unint j = 0; j < X.r; j++) {
-      float t = dist_host(&Q.mat[IDX(i, 0, Q.ld)], &X.mat[IDX(j, 0, X.ld)], Q.c);
+      real t = dist_host(&Q.mat[IDX(i, 0, Q.ld)], &X.mat[IDX(j, 0, X.ld)], Q.c);
       if (t < best) {
         best = t;
         NNs[i] = j;

@@ -1,12 +1,22 @@
 // A program written against the reference's C++ API (the calls driver.cu
-// makes, in the same order) and linked against librbcgb.so.  Used by
-// tests/test_gpu_legacy.py.
+// makes, in the same order) and linked against librbcgb.so -- or, compiled
+// with RBC_REAL_DOUBLE (real = double), against librbcgb_f64.so.  Used by
+// tests/test_legacy_api.py.
 //
 //   legacy_driver db.bin q.bin n m d numReps out_rbc.bin out_brute.bin out_1nn.bin
 #include <cstdio>
 #include <cstdlib>
 
 #include "rbc_include.h"
+
+// ids block, then distances block (writeNeighbs, driver.cu:352-393), in real
+static int write_neighbors(const char *path, intMatrix ids, matrix dists, unint m) {
+  FILE *fp = fopen(path, "wb");
+  if (!fp) return 1;
+  for (unint i = 0; i < m; i++) fwrite(&ids.mat[IDX(i, 0, ids.ld)], sizeof(unint), KMAX, fp);
+  for (unint i = 0; i < m; i++) fwrite(&dists.mat[IDX(i, 0, dists.ld)], sizeof(real), KMAX, fp);
+  return fclose(fp) != 0;
+}
 
 static void read_bin(const char *path, matrix x) {
   FILE *fp = fopen(path, "rb");
@@ -68,8 +78,8 @@ int main(int argc, char **argv) {
     printf("Execution failed; error type: %s \n", cudaGetErrorString(cE));
     return 1;
   }
-  if (rbc_write_neighbors_bin(argv[7], nnsRBC.mat, distsRBC.mat, m, KMAX, nnsRBC.ld) != RBC_OK) return 1;
-  if (rbc_write_neighbors_bin(argv[8], nnsB.mat, distsB.mat, m, KMAX, nnsB.ld) != RBC_OK) return 1;
+  if (write_neighbors(argv[7], nnsRBC, distsRBC, m)) return 1;
+  if (write_neighbors(argv[8], nnsB, distsB, m)) return 1;
   FILE *fp = fopen(argv[9], "wb");
   fwrite(nnCPU, sizeof(unint), m, fp);
   fwrite(nnGPU, sizeof(unint), m, fp);
