@@ -46,6 +46,11 @@ namespace {
 
 constexpr uint32_t kDefaultProbes = 1;  // lists searched before planning (the one-shot plan)
 constexpr uint32_t kTcProbes = 8;       // the tensor form: a tighter start for its shortlists
+// The tensor form's probe round searches lists of fewer rows than this on the
+// FP32 path (few queries share a probed list; small tensor items are
+// dominated by fixed costs and shortlist merges) and larger ones on the
+// tensor cores.  RBC_TC_PROBE_ROWS overrides it.
+constexpr uint64_t kTcProbeRows = 8192;
 
 void pool_setup() {
   static bool done[64] = {};
@@ -112,7 +117,8 @@ static float round_down_f(double v) {
 
 int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
-                    int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq, uint32_t qtile_over) {
+                    int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq, uint32_t qtile_over,
+                    uint64_t list_lo, uint64_t list_hi) {
   const int tqv = tq < 0 ? idx->tune_tq : tq;
   const uint32_t nr = idx->nr, qtile = qtile_over ? qtile_over : (uint32_t)search_query_tile(idx->dp, tqv, list_width_for(k));
   uint32_t *ctl = b.ctl.as<uint32_t>();  // [0] work, [1] nitems, [2] err
@@ -149,9 +155,10 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
   a.phase = 1;
   CK(launch_plan_pass(a, mode, s));
   if (stage == 0) return RBC_OK;
-  CK(launch_tiles_per_list(cnt, offsets, nr, qtile, idx->item_rows, tcnt, s));
+  CK(launch_tiles_per_list(cnt, offsets, nr, qtile, idx->item_rows, list_lo, list_hi, tcnt, s));
   CK(launch_exclusive_scan(tcnt, tstart, nr + 1, b.scan_tmp.p, ctl + 2, s));
-  CK(launch_plan_items(cnt, start, tstart, offsets, nr, qtile, idx->item_rows, b.items.as<SearchItem>(), ctl + 1, s));
+  CK(launch_plan_items(cnt, start, tstart, offsets, nr, qtile, idx->item_rows, list_lo, list_hi,
+                       b.items.as<SearchItem>(), ctl + 1, s));
   if (stage == 1) return RBC_OK;
 
   SearchArgs sa{};
@@ -204,8 +211,8 @@ int build_tc(rbc_index *idx, cudaStream_t s) {
   if (!tc_supported(idx->dp)) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: the tensor-core form needs d <= 128");
   idx->kp = tc_kp(idx->d);
   idx->n_pad = (idx->n + 127) / 128 * 128;
-  TRY(tc_build(idx->Xp, idx->offsets, idx->R, idx->radius, idx->n, idx->n_pad, idx->nr, idx->d, idx->ld, idx->kp,
-               &idx->tc, &idx->device_bytes, s));
+  TRY(tc_build(idx->Xp, idx->perm, idx->offsets, idx->R, idx->radius, idx->n, idx->n_pad, idx->nr, idx->d, idx->ld,
+               idx->kp, &idx->tc, &idx->device_bytes, s));
   CK(tc_make_map(&idx->tmB, idx->tc.Xh, idx->n_pad, idx->tc.cols, 128));
   CK(cudaStreamSynchronize(s));
   return RBC_OK;
@@ -506,13 +513,15 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   return RBC_OK;
 }
 
-// Tensor-core exact query (tc_search.cu): an RBC query whose list search runs
-// on the tensor cores, in two rounds like the plain form:
-//   1. query x representative distances, probe table (nearest representative,
-//      plus the router's picks when routed);
-//   2. probe round: tensor search of the probed lists, exact rerank of the
-//      shortlists -> each query's k-th distance (an upper bound on the true
-//      one, so pruning with it is safe);
+// Tensor-core exact query (tc_search.cu): an RBC query whose bulk list search
+// runs on the tensor cores, in two rounds like the plain form:
+//   1. query x representative distances, probe table (the nearest
+//      representatives, plus the router's picks when routed);
+//   2. probe round: the probed lists searched exactly on the FP32 path for
+//      each query's top-sl (a probed list holds few queries, so the tensor
+//      tiles would run nearly empty); that list seeds the query's shortlist
+//      and its k-th distance (an upper bound on the true one) is the pruning
+//      threshold;
 //   3. pruned round: the pruning plan over every other list, tensor search of
 //      the surviving (list, query) items into the same shortlists, exact
 //      rerank and certificate; uncertified queries are recomputed by the
@@ -533,7 +542,13 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   Pn = std::min(Pn, nr);
   const uint32_t P = routed ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
   const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
-  const uint32_t qtile = tc_query_tile(fmt), kw = kListWidth;
+  // the probe round's FP32 lists hold a whole shortlist; few queries share a
+  // probed list, so its query tiles are 16 wide (TQ = 1)
+  const uint32_t sl = tc_shortlist(k), kw = list_width_for(sl);
+  const int pgrid = search_grid(idx->metric, idx->dp, 1, kw);
+  uint64_t probe_rows = kTcProbeRows;
+  if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) probe_rows = std::strtoull(env, nullptr, 10);
+  const uint32_t qtile = tc_query_tile(fmt);
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
   QueryBufs b;
   const uint64_t pair_cap = mb * nr, item_cap = item_capacity(idx, mb, qtile);
@@ -566,7 +581,6 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(qscale.alloc((mb + 1) * 4, s));
   CK(qnorm.alloc((mb + 1) * 4, s));
   CK(qinex.alloc(mb + 1, s));
-  const uint32_t sl = tc_shortlist(k);
   CK(sl_a.alloc(2 * mb * sl * 4, s));
   CK(sl_row.alloc(2 * mb * sl * 4, s));
   CK(sl_sel.alloc(mb * 4, s));
@@ -588,6 +602,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   idx->ev_used = 0;
   for (uint64_t b0 = 0; b0 < m; b0 += mb) {
     const uint64_t mq = std::min(mb, m - b0);
+    bool tc_probe = false;
     CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
     CK(cudaMemsetAsync(ctl.p, 0, 64, s));
     // 1. distances to the representatives, probe table
@@ -665,42 +680,61 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     ra.ldo = ldo;
     ra.nfail = ctl.as<uint32_t>() + 1;
     ra.fail = failq.as<uint32_t>();
-    for (uint32_t round = 0; round < 2; round++) {
-      // the plan's work items: list-major, query tiles of the tensor kernel
-      TRY(plan_and_search(idx, b, mq, P, k, round, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s,
-                          1, -1, qtile));
-      cudaEvent_t e0 = nullptr, e1 = nullptr;
-      if (idx->profile) {
-        e0 = idx->ev_pool[2 * round];
-        e1 = idx->ev_pool[2 * round + 1];
-        CK(cudaEventRecord(e0, s));
-      }
+    // probe round, small lists: searched exactly on the FP32 path; every
+    // query's exact top-sl there seeds its shortlist, and its k-th distance
+    // the pruning threshold
+    {
+      const bool prof = idx->profile;
+      idx->profile = false;
+      const int rc = plan_and_search(idx, b, mq, P, sl, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, pgrid,
+                                     nullptr, s, 2, 1, 0, 0, probe_rows);
+      idx->profile = prof;
+      TRY(rc);
+    }
+    CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, mq, sl, k, sl_a.as<float>(),
+                      sl_row.as<uint32_t>(), sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));
+    // probe round, large lists: tensor search into the seeded shortlists, then
+    // the k-th exact distance of each shortlist tightens the threshold
+    if (idx->max_list >= probe_rows) {
+      TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
+                          -1, qtile, probe_rows, UINT64_MAX));
+      if (idx->profile) CK(cudaEventRecord(idx->ev_pool[2], s));
       CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
-      if (e1) CK(cudaEventRecord(e1, s));
-      if (round == 0) {
-        ra.tau = b.tau.as<uint32_t>();
-        ra.ids = nullptr;
-        ra.dists = nullptr;
-      } else {
-        ra.tau = nullptr;
-        ra.ids = dIds ? dIds + b0 * ldo : nullptr;
-        ra.dists = dDists ? dDists + b0 * ldo : nullptr;
-        if (!ra.ids && !ra.dists) ra.dists = b.res_d.as<float>();  // the certificate still runs
+      if (idx->profile) {
+        CK(cudaEventRecord(idx->ev_pool[3], s));
+        tc_probe = true;
       }
+      ra.tau = b.tau.as<uint32_t>();
+      ra.ids = nullptr;
+      ra.dists = nullptr;
       CK(launch_rerank(idx->metric, ra, s));
     }
+    // pruned round: every other list whose bound survives, on the tensor
+    // cores, into the same shortlists; exact rerank and certificate
+    TRY(plan_and_search(idx, b, mq, P, k, 1, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
+                        -1, qtile));
+    if (idx->profile) CK(cudaEventRecord(idx->ev_pool[0], s));
+    CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
+    if (idx->profile) CK(cudaEventRecord(idx->ev_pool[1], s));
+    ra.tau = nullptr;
+    ra.ids = dIds ? dIds + b0 * ldo : nullptr;
+    ra.dists = dDists ? dDists + b0 * ldo : nullptr;
+    CK(launch_rerank(idx->metric, ra, s));
     uint32_t hc[2], bc[3];
     CK(cudaMemcpyAsync(hc, ctl.p, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(bc, b.ctl.p, 12, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (hc[0] || bc[2]) return fail(RBC_ERR_ITER_LIMIT, "rbc_query: a bounded device wait ran out");
     if (idx->profile) {
-      for (int r = 0; r < 2; r++) {
-        float ms = 0;
-        CK(cudaEventElapsedTime(&ms, idx->ev_pool[2 * r], idx->ev_pool[2 * r + 1]));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, idx->ev_pool[0], idx->ev_pool[1]));
+      tc_ms += ms;
+      tc_launches += 1;
+      if (tc_probe) {
+        CK(cudaEventElapsedTime(&ms, idx->ev_pool[2], idx->ev_pool[3]));
         tc_ms += ms;
+        tc_launches += 1;
       }
-      tc_launches += 2;
     }
     const uint32_t nfail = hc[1];
     nfail_total += nfail;
@@ -867,7 +901,7 @@ int rbc_destroy(rbc_index *idx) {
   if (!idx) return RBC_OK;
   void *ptrs[] = {idx->Xp,      idx->perm,   idx->offsets, idx->radius,     idx->R,  idx->os_lists, idx->os_counts,
                   idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->tc.Xh, idx->tc.w,  idx->owner,
-                  idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm, idx->tc.mu, idx->X64, idx->norm64};
+                  idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm, idx->tc.mu, idx->tc.iperm, idx->X64, idx->norm64};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : idx->ev_pool) cudaEventDestroy(e);

@@ -58,11 +58,12 @@ namespace rbc {
 // Plan one query round (mode 0 probe pairs, mode 1 pruned pairs); stage 0
 // stops after the plan, 1 after the work items, 2 also runs the search.
 // tq < 0 uses the index's tuned tile.
-// qtile > 0 overrides the query tile of the work items.
+// qtile > 0 overrides the query tile of the work items; only lists of
+// list_lo <= rows < list_hi get items.
 int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
                     int grid, unsigned long long *stats, cudaStream_t s, int stage = 2, int tq = -1,
-                    uint32_t qtile = 0);
+                    uint32_t qtile = 0, uint64_t list_lo = 0, uint64_t list_hi = UINT64_MAX);
 // Build the tensor-core operands of an index that has its partition.
 int build_tc(rbc_index *idx, cudaStream_t s);
 // Work items a plan of mb queries can produce (query tiles x row chunks).

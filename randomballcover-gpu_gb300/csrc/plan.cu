@@ -186,21 +186,30 @@ __device__ __forceinline__ uint32_t row_chunks(const uint64_t *offsets, uint32_t
   return np == 0 ? 1u : (uint32_t)((np + max_rows - 1) / max_rows);
 }
 
+// Lists whose row count lies outside [lo, hi) get no items.
+__device__ __forceinline__ bool list_selected(const uint64_t *offsets, uint32_t r, uint64_t lo, uint64_t hi) {
+  const uint64_t np = offsets[r + 1] - offsets[r];
+  return np >= lo && np < hi;
+}
+
 __global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, const uint64_t *__restrict__ offsets,
-                                      uint32_t nr, uint32_t qtile, uint32_t max_rows, uint32_t *__restrict__ tile_cnt) {
+                                      uint32_t nr, uint32_t qtile, uint32_t max_rows, uint64_t lo, uint64_t hi,
+                                      uint32_t *__restrict__ tile_cnt) {
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < nr) tile_cnt[r] = (list_cnt[r] + qtile - 1) / qtile * row_chunks(offsets, r, max_rows);
+  if (r < nr)
+    tile_cnt[r] = list_selected(offsets, r, lo, hi) ? (list_cnt[r] + qtile - 1) / qtile * row_chunks(offsets, r, max_rows)
+                                                     : 0;
   if (r == nr) tile_cnt[nr] = 0;
 }
 
 // items for list r: its query tiles x row chunks, in list order.
 __global__ void plan_items_kernel(const uint32_t *__restrict__ list_cnt, const uint32_t *__restrict__ list_start,
                                   const uint32_t *__restrict__ tile_start, const uint64_t *__restrict__ offsets,
-                                  uint32_t nr, uint32_t qtile, uint32_t max_rows, SearchItem *__restrict__ items,
-                                  uint32_t *__restrict__ nitems) {
+                                  uint32_t nr, uint32_t qtile, uint32_t max_rows, uint64_t lo, uint64_t hi,
+                                  SearchItem *__restrict__ items, uint32_t *__restrict__ nitems) {
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r == nr) *nitems = tile_start[nr];
-  if (r >= nr) return;
+  if (r >= nr || !list_selected(offsets, r, lo, hi)) return;
   const uint32_t cnt = list_cnt[r];
   const uint32_t nt = (cnt + qtile - 1) / qtile, nc = row_chunks(offsets, r, max_rows);
   const uint64_t p0 = offsets[r], np = offsets[r + 1] - offsets[r];
@@ -245,16 +254,17 @@ cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s) {
 }
 
 cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, const uint64_t *offsets, uint32_t nr, uint32_t qtile,
-                                  uint32_t max_rows, uint32_t *tile_cnt, cudaStream_t s) {
-  tiles_per_list_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, offsets, nr, qtile, max_rows, tile_cnt);
+                                  uint32_t max_rows, uint64_t lo, uint64_t hi, uint32_t *tile_cnt, cudaStream_t s) {
+  tiles_per_list_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, offsets, nr, qtile, max_rows, lo, hi,
+                                                             tile_cnt);
   return launched();
 }
 
 cudaError_t launch_plan_items(const uint32_t *list_cnt, const uint32_t *list_start, const uint32_t *tile_start,
-                              const uint64_t *offsets, uint32_t nr, uint32_t qtile, uint32_t max_rows, SearchItem *items,
-                              uint32_t *nitems, cudaStream_t s) {
+                              const uint64_t *offsets, uint32_t nr, uint32_t qtile, uint32_t max_rows, uint64_t lo,
+                              uint64_t hi, SearchItem *items, uint32_t *nitems, cudaStream_t s) {
   plan_items_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, list_start, tile_start, offsets, nr, qtile,
-                                                         max_rows, items, nitems);
+                                                         max_rows, lo, hi, items, nitems);
   return launched();
 }
 

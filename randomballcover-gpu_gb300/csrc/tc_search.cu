@@ -799,6 +799,33 @@ __global__ void sl_init_kernel(float *sl_a, uint32_t *sl_row, uint32_t *sel, uin
   }
 }
 
+// One thread per query: the shortlist's current buffer (sel = 0 after
+// sl_init_kernel) takes the query's exact top-sl over its probed lists.
+// Those rows are exact, so they add nothing to the error bound; a probed row
+// left out ranks after the sl-th under (distance, id), hence after every
+// shortlist entry's value, which the certificate already covers.
+__global__ void sl_seed_kernel(const float *__restrict__ res_d, const uint32_t *__restrict__ res_i, uint32_t kw,
+                               const uint32_t *__restrict__ iperm, uint64_t m, uint32_t sl, uint32_t k,
+                               float *__restrict__ sl_a, uint32_t *__restrict__ sl_row, uint32_t *__restrict__ theta,
+                               uint32_t *__restrict__ tau) {
+  const uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  const float *rd = res_d + q * kw;
+  const uint32_t *ri = res_i + q * kw;
+  for (uint32_t j = 0; j < sl; j++) {
+    const uint32_t id = ri[j];
+    sl_a[q * sl + j] = id != RBC_DUMMY ? rd[j] : INFINITY;
+    sl_row[q * sl + j] = id != RBC_DUMMY ? iperm[id] : RBC_DUMMY;
+  }
+  theta[q] = __float_as_uint(ri[sl - 1] != RBC_DUMMY ? rd[sl - 1] : FLT_MAX);
+  tau[q] = fbits(rd[k - 1]);
+}
+
+__global__ void iperm_kernel(const uint32_t *__restrict__ perm, uint64_t n, uint32_t *__restrict__ iperm) {
+  const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (p < n) iperm[perm[p]] = (uint32_t)p;
+}
+
 // Exact rerank of each query's shortlist (one warp per query): the k-th exact
 // distance as a pruning threshold, or the results and the certificate.
 template <int METRIC>
@@ -943,9 +970,9 @@ cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-int tc_build(const float *Xp, const uint64_t *offsets, const float *R, const float *radius, uint64_t n,
-             uint64_t n_pad, uint32_t nr, uint32_t d, uint32_t ld, uint32_t kp, TcBuild *out, uint64_t *bytes,
-             cudaStream_t s) {
+int tc_build(const float *Xp, const uint32_t *perm, const uint64_t *offsets, const float *R, const float *radius,
+             uint64_t n, uint64_t n_pad, uint32_t nr, uint32_t d, uint32_t ld, uint32_t kp, TcBuild *out,
+             uint64_t *bytes, cudaStream_t s) {
   TcBuild &t = *out;
   DevBuf fl, lmax;
   cudaError_t e = fl.alloc(4, s);
@@ -971,8 +998,11 @@ int tc_build(const float *Xp, const uint64_t *offsets, const float *R, const flo
   if (e == cudaSuccess) e = cudaMalloc(&t.lxmax, nr * 4);
   if (e == cudaSuccess) e = cudaMalloc(&t.lcnorm, nr * 4);
   if (e == cudaSuccess) e = cudaMalloc(&t.mu, kp * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&t.iperm, n * 4);
   if (e != cudaSuccess) return cuda_fail(e, "rbc_build: tensor-form operands");
-  *bytes += xh_bytes + (n_pad + kBN) * 4 + 3ull * nr * 4 + kp * 4;
+  *bytes += xh_bytes + (n_pad + kBN) * 4 + 3ull * nr * 4 + kp * 4 + n * 4;
+  iperm_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(perm, n, t.iperm);
+  if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: row map");
   tc_mu_kernel<<<(kp + 127) / 128, 128, 0, s>>>(R, ld, nr, d, kp, t.format, t.mu);
   if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: centering vector");
   tc_list_params_kernel<<<(nr + 127) / 128, 128, 0, s>>>(R, ld, nr, d, radius, lmax.as<uint32_t>(), t.mu, t.format,
@@ -991,6 +1021,15 @@ cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t 
   tc_query_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(Q, ld, m, d, kp, format, mu,
                                                                     static_cast<uint16_t *>(Qh), qscale, qnorm,
                                                                     q_inexact);
+  return launched();
+}
+
+cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *iperm, uint64_t m,
+                           uint32_t sl, uint32_t k, float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau,
+                           cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  sl_seed_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(res_d, res_i, kw, iperm, m, sl, k, sl_a, sl_row, theta,
+                                                            tau);
   return launched();
 }
 

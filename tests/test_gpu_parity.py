@@ -258,3 +258,22 @@ def test_repeated_queries_are_deterministic(rbc):
         b = idx.query(Q, 10)
         assert (a[0] == b[0]).all() and (a[1] == b[1]).all()
     idx.close()
+
+
+@pytest.mark.parametrize("probe_rows", ["0", "300", "100000"])
+def test_tensor_core_probe_round_split(rbc, oracle, probe_rows, monkeypatch):
+    """The tensor form's probe round searches small probed lists on the FP32
+    path (seeding the shortlists) and large ones on the tensor cores; every
+    split gives the oracle's answer (0: all on the tensor cores, 100000: all
+    on the FP32 path, 300: both, since list sizes spread around it)."""
+    monkeypatch.setenv("RBC_TC_PROBE_ROWS", probe_rows)
+    for kind, k in ((2, 10), (1, 32)):
+        X = rbc.synth(kind, 33, 0, 40000, 64, ncomp=150, sigma_lo=0.05, sigma_hi=0.05)
+        Q = rbc.synth(kind, 33, 1, 300, 64, ncomp=150, sigma_lo=0.05, sigma_hi=0.05)
+        idx = rbc.Index(X, 150, seed=4, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+        inf = idx.info()
+        assert inf["min_list"] < 300 <= inf["max_list"]
+        ids, dists = idx.query(Q, k, mode=rbc.QUERY_EXACT_TC)
+        ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), k)
+        assert_same(ids, dists, ri, rd, rbc)
+        idx.close()
