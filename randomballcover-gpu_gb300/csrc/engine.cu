@@ -45,7 +45,7 @@ int cuda_fail(cudaError_t e, const char *what) {
 namespace {
 
 constexpr uint32_t kDefaultProbes = 1;  // lists searched before planning (the one-shot plan)
-constexpr uint32_t kTcProbes = 8;       // the tensor form: a tighter start for its shortlists
+constexpr uint32_t kTcProbes = 4;       // the tensor form: a tighter start for its shortlists
 // The tensor form's probe round searches lists of fewer rows than this on the
 // FP32 path (few queries share a probed list; small tensor items are
 // dominated by fixed costs and shortlist merges) and larger ones on the
