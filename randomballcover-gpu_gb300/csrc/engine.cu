@@ -696,10 +696,11 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     // probe round, large lists: tensor search into the seeded shortlists, then
     // the k-th exact distance of each shortlist tightens the threshold
     if (idx->max_list >= probe_rows) {
+      // few queries share a probed list: one 128-query tile per B tile
       TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
-                          -1, qtile, probe_rows, UINT64_MAX));
+                          -1, tc_query_tile(kTcSplit), probe_rows, UINT64_MAX));
       if (idx->profile) CK(cudaEventRecord(idx->ev_pool[2], s));
-      CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
+      CK(launch_tc_search(tmA, idx->tmB, ta, grid, s, true));
       if (idx->profile) {
         CK(cudaEventRecord(idx->ev_pool[3], s));
         tc_probe = true;

@@ -1048,9 +1048,10 @@ int tc_grid() {
 }
 
 cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
-                             cudaStream_t s) {
+                             cudaStream_t s, bool narrow) {
   if (a.kb < 1 || a.kb > 2) return cudaErrorInvalidValue;
-  return a.format == kTcSplit ? launch_tc<1, true>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
+  if (a.format == kTcSplit) return launch_tc<1, true>(tmA, tmB, a, grid, s);
+  return narrow ? launch_tc<1, false>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
 }
 
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s) {
