@@ -521,11 +521,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       const float dq = st.dq, alpha = st.alpha;
       float thv = st.thv;
       uint32_t nl = 0;
+      // other CTAs tighten the query's shortlist all the time: each tile
+      // refreshes the filter with the threshold read one tile earlier (a
+      // larger, older value only lets more candidates through), so the read's
+      // latency hides behind a tile of work
+      float th_next = arow < item.nq ? __uint_as_float(__ldcg(a.sl_theta + q)) : FLT_MAX;
       for (uint32_t t = 0; t < ntiles && ok; t++, bi++) {
         if (MT == 1 && (bi & 1u) != grp) continue;
         const uint32_t slot = bi % NSLOT;
-        // other CTAs tighten the query's shortlist all the time: refresh the filter
-        const float th_now = arow < item.nq ? __uint_as_float(__ldcg(a.sl_theta + q)) : FLT_MAX;
+        const float th_now = th_next;
+        th_next = arow < item.nq ? __uint_as_float(__ldcg(a.sl_theta + q)) : FLT_MAX;
         if (!(ok = mbar_wait(&bar_t_full[slot], (bi / NSLOT) & 1, a.err))) break;
         if (!(ok = mbar_wait(&bar_x_full[slot], (bi / NSLOT) & 1, a.err))) break;
         if (arow < item.nq) thv = fminf(thv, v_threshold(th_now, dq));
