@@ -212,6 +212,12 @@ int rbc_set_profiling(rbc_index *index, int enable);
 int rbc_get_profile(const rbc_index *index, rbc_profile *profile);
 /* Number of kernels this library has launched in this process. */
 uint64_t rbc_kernel_launches(void);
+/* Exercises the failure path of the kernels' bounded waits without a fault:
+ * one kernel waits on an mbarrier nobody arrives on (50 ms limit), one on a
+ * lock nobody releases (16,384 attempts); each records its error word and
+ * returns.  Both statuses come back as RBC_ERR_ITER_LIMIT, and the context
+ * stays usable for the next call. */
+int rbc_selftest_bounded_wait(uint32_t *mbar_status, uint32_t *lock_status, void *stream);
 
 /* Brute-force exact k-NN of every query over every database row;
  * 1 <= k <= RBC_K_LIMIT. */

@@ -253,6 +253,7 @@ int rbc_batch_add(rbc_batch *bt, rbc_index *idx, const float *dQ, uint64_t m, ui
   if (!bt || !idx) return fail(RBC_ERR_INVALID, "rbc_batch_add: NULL argument");
   if (bt->ready) return fail(RBC_ERR_INVALID, "rbc_batch_add: the batch already ran; create a new one");
   if (!(idx->flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_INVALID, "rbc_batch_add: index has no partition");
+  if (idx->flags & RBC_BUILD_F64) return fail(RBC_ERR_INVALID, "rbc_batch_add: index holds doubles: rbc_query_f64");
   if (k < 1 || k > (uint32_t)kListWidth || ldo < k || ldq < idx->d || m == 0 || !dQ || (!dIds && !dDists))
     return fail(RBC_ERR_INVALID, "rbc_batch_add: bad query arguments");
   if (m * (uint64_t)idx->nr > (1ull << 28))

@@ -192,4 +192,18 @@ __device__ __forceinline__ void raise_error(uint32_t *err, uint32_t code) {
   if (err) atomicCAS(err, 0u, code);
 }
 
+// Take a lock word (0 -> 1) with at most `limit` failed attempts; when they
+// run out, record RBC_ERR_ITER_LIMIT and return false (never a hang).
+__device__ __forceinline__ bool lock_bounded(uint32_t *lock, uint32_t limit, uint32_t *err) {
+  uint32_t spins = 0;
+  while (atomicCAS(lock, 0u, 1u) != 0u) {
+    if (++spins > limit) {
+      raise_error(err, RBC_ERR_ITER_LIMIT);
+      return false;
+    }
+    __nanosleep(32);
+  }
+  return true;
+}
+
 }  // namespace rbc

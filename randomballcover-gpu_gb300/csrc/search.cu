@@ -221,15 +221,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) search_kernel(const __grid_co
       float gtau = __shfl_sync(0xffffffffu, __uint_as_float(__ldcg(a.tau + q)), 0);
       if (first_id == RBC_DUMMY || first > gtau) continue;
       int got = 0;
-      if (lane == 0) {
-        uint32_t spins = 0;
-        while (atomicCAS(a.lock + q, 0u, 1u) != 0u) {
-          if (++spins > kLockSpinLimit) break;
-          __nanosleep(32);
-        }
-        got = spins <= kLockSpinLimit;
-        if (!got) raise_error(g.err, RBC_ERR_ITER_LIMIT);
-      }
+      if (lane == 0) got = lock_bounded(a.lock + q, kLockSpinLimit, g.err);
       got = __shfl_sync(0xffffffffu, got, 0);
       if (!got) continue;
       __threadfence();

@@ -63,15 +63,18 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 // Bounded wait for the phase with the given parity to complete: gives up
 // after kWaitLimitNs of wall time (or kSpinLimit polls, whichever is first).
 constexpr uint64_t kWaitLimitNs = 4000000000ull;
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err) {
+__device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, uint32_t parity, uint32_t *err, uint64_t limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer_ns();
   for (uint32_t i = 1; i < kSpinLimit; i++) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) break;
+    if ((i & 255u) == 0 && globaltimer_ns() - t0 > limit_ns) break;
   }
   raise_error(err, RBC_ERR_ITER_LIMIT);
   return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err) {
+  return mbar_wait_for(bar, parity, err, kWaitLimitNs);
 }
 
 // ---------------------------------------------------------------- TMA

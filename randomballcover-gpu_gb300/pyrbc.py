@@ -90,6 +90,7 @@ SIGNATURES = {
     "rbc_set_profiling": ([_VP, _INT], _INT),
     "rbc_get_profile": ([_VP, C.POINTER(Profile)], _INT),
     "rbc_kernel_launches": ([], _U64),
+    "rbc_selftest_bounded_wait": ([C.POINTER(_U32), C.POINTER(_U32), _VP], _INT),
     "rbc_brute_knn": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _INT, _VP, _VP, _U32, _VP], _INT),
     "rbc_brute_knn_noalloc": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _U32, _INT, _VP, _VP, _U32, _VP], _INT),
     "rbc_brute_range_count": ([_VP, _U64, _U32, _VP, _U64, _U32, _U32, _INT, _VP, _VP, _VP], _INT),

@@ -148,6 +148,10 @@ def test_f64_index_api_rules(rbc, tmp_path):
     assert rbc.lib().rbc_query(idx.h, Qf.data_ptr(), 1, 10, 1, 0, out.data_ptr(), None, 1, None) == rbc.ERR_INVALID
     with pytest.raises(rbc.RBCError):
         idx.query(Q, 5, mode=rbc.QUERY_ONESHOT)
+    b = rbc.Batch()
+    with pytest.raises(rbc.RBCError):  # batches run the float search
+        b.add(idx, torch.zeros((4, 10), device="cuda"), 5)
+    b.close()
     with pytest.raises(rbc.RBCError):
         rbc.Index(X, 64, s=64, flags=rbc.BUILD_PARTITION | rbc.BUILD_ONESHOT)
     a = idx.query(Q, 12)

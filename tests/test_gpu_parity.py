@@ -277,3 +277,19 @@ def test_tensor_core_probe_round_split(rbc, oracle, probe_rows, monkeypatch):
         ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), k)
         assert_same(ids, dists, ri, rd, rbc)
         idx.close()
+
+
+def test_bounded_waits_end_with_a_status_not_a_hang(rbc, oracle):
+    """A wait that can never complete (an mbarrier nobody arrives on, a lock
+    nobody releases) runs out, records RBC_ERR_ITER_LIMIT and returns; the
+    context stays usable for the next query."""
+    import ctypes as C
+    mb, lk = C.c_uint32(), C.c_uint32()
+    rbc.check(rbc.lib().rbc_selftest_bounded_wait(C.byref(mb), C.byref(lk), None))
+    assert mb.value == rbc.ERR_ITER_LIMIT and lk.value == rbc.ERR_ITER_LIMIT
+    rng = np.random.default_rng(1)
+    X = rng.standard_normal((2000, 8)).astype(np.float32)
+    Q = rng.standard_normal((20, 8)).astype(np.float32)
+    ids, dists = rbc.brute_knn(X, Q, 5)
+    ri, rd = oracle.knn(X, Q, 5)
+    assert_same(ids, dists, ri, rd, rbc)
