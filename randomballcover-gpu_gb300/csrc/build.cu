@@ -246,10 +246,16 @@ __global__ void __launch_bounds__(kSelThreads) row_select_kernel(const float *__
     for (uint32_t b = threadIdx.x; b < nb; b += kSelThreads) hist[b] = 0;
     __syncthreads();
     const int hi_shift = shifts[p] + widths[p];  // bits above this pass must equal prefix
-    for (uint64_t i = threadIdx.x; i < n; i += kSelThreads) {
-      uint32_t v = row[i];
-      bool match = (p == 0) || ((v >> hi_shift) == prefix);
-      if (match) atomicAdd(&hist[(v >> shifts[p]) & (nb - 1)], 1u);
+    // 16-byte loads (ldD % 4 == 0), four values per thread and step
+    const uint4 *row4 = reinterpret_cast<const uint4 *>(row);
+    for (uint64_t i = 4 * (uint64_t)threadIdx.x; i < n; i += 4 * kSelThreads) {
+      const uint4 q = row4[i >> 2];
+      const uint32_t v[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const bool match = i + j < n && (p == 0 || (v[j] >> hi_shift) == prefix);
+        if (match) atomicAdd(&hist[(v[j] >> shifts[p]) & (nb - 1)], 1u);
+      }
     }
     __syncthreads();
     find_bin(hist, nb, want, ws, &s_bin, &s_before);
@@ -264,10 +270,11 @@ __global__ void __launch_bounds__(kSelThreads) row_select_kernel(const float *__
 }
 
 // Ids of row b's selected entries, increasing: every value below the s-th
-// smallest, and the first `need` values equal to it.  Each thread holds 4
-// consecutive values (one 16-byte load); chunks of 4 x 1024 values with no
-// value at or below the threshold -- nearly all of them, s << n -- cost one
-// block vote; the others take two block scans.
+// smallest, and the first `need` values equal to it.  Each thread holds 8
+// consecutive values (two 16-byte loads) per chunk of 8 x kSelThreads values;
+// one block scan per chunk of the packed counts (equal values << 16 | values
+// below) places every selected id, the first `need` equal ones included.
+constexpr int kCompactPer = 8;
 __global__ void __launch_bounds__(kSelThreads) row_compact_kernel(const float *__restrict__ D, uint64_t ldD,
                                                                   uint64_t n, const uint32_t *__restrict__ thr_bits,
                                                                   const uint32_t *__restrict__ need,
@@ -278,36 +285,38 @@ __global__ void __launch_bounds__(kSelThreads) row_compact_kernel(const float *_
   const uint32_t t = thr_bits[blockIdx.x], nd = need[blockIdx.x];
   uint32_t *out = lists + (uint64_t)blockIdx.x * lds;
   uint32_t taken = 0, eq_seen = 0;
-  for (uint64_t b = 0; b < n; b += 4 * kSelThreads) {
-    const uint64_t i0 = b + 4 * threadIdx.x;
-    uint4 v4 = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
-    if (i0 < n) v4 = row[i0 >> 2];
-    uint32_t v[4] = {v4.x, v4.y, v4.z, v4.w};
+  constexpr uint64_t kChunk = kCompactPer * kSelThreads;
+  for (uint64_t c0 = 0; c0 < n; c0 += kChunk) {
+    const uint64_t i0 = c0 + kCompactPer * threadIdx.x;
+    uint32_t v[kCompactPer];
 #pragma unroll
-    for (int j = 0; j < 4; j++)
-      if (i0 + j >= n) v[j] = 0xFFFFFFFFu;
-    const bool has = v[0] <= t || v[1] <= t || v[2] <= t || v[3] <= t;
-    if (!__syncthreads_or(has)) continue;
-    uint32_t neq = 0;
-#pragma unroll
-    for (int j = 0; j < 4; j++) neq += v[j] == t;
-    uint32_t eq_total;
-    uint32_t eq_rank = eq_seen + block_exclusive_scan(neq, ws, eq_total);
-    uint32_t sel[4], nsel = 0;
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const bool is_eq = v[j] == t;
-      sel[j] = v[j] < t || (is_eq && eq_rank < nd);
-      eq_rank += is_eq;
-      nsel += sel[j];
+    for (int h = 0; h < kCompactPer / 4; h++) {
+      const uint4 q = i0 + 4 * h < n ? row[(i0 >> 2) + h] : make_uint4(~0u, ~0u, ~0u, ~0u);
+      v[4 * h] = q.x;
+      v[4 * h + 1] = q.y;
+      v[4 * h + 2] = q.z;
+      v[4 * h + 3] = q.w;
     }
-    uint32_t sel_total;
-    uint32_t pos = taken + block_exclusive_scan(nsel, ws, sel_total);
+    uint32_t nlt = 0, neq = 0;
 #pragma unroll
-    for (int j = 0; j < 4; j++)
-      if (sel[j]) out[pos++] = (uint32_t)(i0 + j);
-    taken += sel_total;
-    eq_seen += eq_total;
+    for (int j = 0; j < kCompactPer; j++) {
+      if (i0 + j >= n) v[j] = ~0u;  // above any distance's bits: never selected
+      nlt += v[j] < t;
+      neq += v[j] == t;
+    }
+    uint32_t tot;
+    const uint32_t pre = block_exclusive_scan((neq << 16) | nlt, ws, tot);  // both fields < 2^16
+    const uint32_t eq_left = nd > eq_seen ? nd - eq_seen : 0;  // equal values still to take
+    uint32_t eq_pos = pre >> 16;
+    uint32_t pos = taken + (pre & 0xFFFFu) + min(eq_pos, eq_left);
+#pragma unroll
+    for (int j = 0; j < kCompactPer; j++) {
+      const bool eq = v[j] == t;
+      if (v[j] < t || (eq && eq_pos < eq_left)) out[pos++] = (uint32_t)(i0 + j);
+      eq_pos += eq;
+    }
+    taken += (tot & 0xFFFFu) + min(tot >> 16, eq_left);
+    eq_seen += tot >> 16;
   }
   if (threadIdx.x == 0) counts[blockIdx.x] = taken;
 }
