@@ -9,6 +9,8 @@
 // nearest-row search go to the lower row index, the (dist, index) order of
 // bruteCPU (brute.cu:104) -- the reference's nnKernel keeps the lower thread
 // slot instead, which is not an order on indices.
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "tile.cuh"
 
@@ -155,12 +157,14 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   }
 }
 
-// counts[i] = #{j : dist(Q_i, X_j) < ranges[i]}; one CTA per 16*TQ queries.
+// counts[i] += #{j in chunk : dist(Q_i, X_j) < ranges[i]}; one CTA per 16*TQ
+// queries (blockIdx.x) and chunk of `chunk` rows (blockIdx.y), so a small
+// query set still fills the GPU.
 template <int METRIC, int TQ>
 __global__ void __launch_bounds__(kTileThreads, 2)
     range_count_kernel(const float *__restrict__ Q, uint64_t m, const float *__restrict__ X, uint64_t n,
                        uint32_t ld, uint32_t dp, const float *__restrict__ ranges,
-                       uint32_t *__restrict__ counts) {
+                       uint32_t *__restrict__ counts, uint64_t chunk) {
   constexpr uint32_t BQ = 16 * TQ;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const uint32_t S = dp + 4;
@@ -178,26 +182,27 @@ __global__ void __launch_bounds__(kTileThreads, 2)
     rg[i] = r < rvalid ? ranges[r0 + r] : 0.f;
     cnt[i] = 0;
   }
-  const uint64_t ntiles = (n + kTileCols - 1) / kTileCols;
-  stage_rows_async(Cs0, S, X, ld, 0, (uint32_t)min((uint64_t)kTileCols, n), dp);
+  const uint64_t c0 = (uint64_t)blockIdx.y * chunk, c1 = min(n, c0 + chunk);
+  const uint64_t ntiles = (c1 - c0 + kTileCols - 1) / kTileCols;
+  stage_rows_async(Cs0, S, X, ld, c0, (uint32_t)min((uint64_t)kTileCols, c1 - c0), dp);
   cp_async_commit();
   for (uint64_t t = 0; t < ntiles; t++) {
     float *cur = (t & 1) ? Cs1 : Cs0;
     float *nxt = (t & 1) ? Cs0 : Cs1;
     if (t + 1 < ntiles) {
-      uint64_t b0 = (t + 1) * kTileCols;
-      stage_rows_async(nxt, S, X, ld, b0, (uint32_t)min((uint64_t)kTileCols, n - b0), dp);
+      uint64_t b0 = c0 + (t + 1) * kTileCols;
+      stage_rows_async(nxt, S, X, ld, b0, (uint32_t)min((uint64_t)kTileCols, c1 - b0), dp);
     }
     cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
     float acc[TQ][2];
     tile_distances<METRIC, TQ>(Rs, cur, S, dp, tq, tx, acc);
-    const uint64_t cb = t * kTileCols;
+    const uint64_t cb = c0 + t * kTileCols;
 #pragma unroll
     for (int i = 0; i < TQ; i++)
 #pragma unroll
-      for (int j = 0; j < 2; j++) cnt[i] += (cb + tx + 16 * j < n) && (acc[i][j] < rg[i]);
+      for (int j = 0; j < 2; j++) cnt[i] += (cb + tx + 16 * j < c1) && (acc[i][j] < rg[i]);
     __syncthreads();
   }
 #pragma unroll
@@ -206,7 +211,7 @@ __global__ void __launch_bounds__(kTileThreads, 2)
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     uint32_t r = tq + 16 * i;
-    if (tx == 0 && r < rvalid) counts[r0 + r] = c;
+    if (tx == 0 && r < rvalid && c) atomicAdd(counts + r0 + r, c);
   }
 }
 
@@ -243,10 +248,24 @@ cudaError_t range_tq(const float *Q, uint64_t m, const float *X, uint64_t n, uin
                      const float *ranges, uint32_t *counts, cudaStream_t s) {
   size_t smem = rows_smem_bytes<TQ>(dp);
   cudaError_t e = prep(range_count_kernel<METRIC, TQ>, smem);
-  if (e != cudaSuccess) return e;
-  unsigned grid = (unsigned)((m + 16 * TQ - 1) / (16 * TQ));
-  range_count_kernel<METRIC, TQ><<<grid, kTileThreads, smem, s>>>(Q, m, X, n, ld, dp, ranges, counts);
-  return launched();
+  if (e == cudaSuccess) e = cudaMemsetAsync(counts, 0, m * sizeof(uint32_t), s);
+  if (e != cudaSuccess || n == 0) return e;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // row chunks so that query tiles x chunks covers the SMs about four times over
+  const uint64_t qtiles = (m + 16 * TQ - 1) / (16 * TQ);
+  uint64_t nchunks = std::min<uint64_t>((4ull * sms + qtiles - 1) / qtiles, (n + 1023) / 1024);
+  nchunks = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, 65535));
+  const uint64_t chunk = ((n + nchunks - 1) / nchunks + kTileCols - 1) / kTileCols * kTileCols;
+  nchunks = (n + chunk - 1) / chunk;
+  for (uint64_t q0 = 0; q0 < qtiles; q0 += 1u << 30) {  // grid.x limit
+    const uint64_t nt = std::min<uint64_t>(qtiles - q0, 1u << 30);
+    range_count_kernel<METRIC, TQ><<<dim3((unsigned)nt, (unsigned)nchunks), kTileThreads, smem, s>>>(
+        Q + q0 * 16 * TQ * ld, m - q0 * 16 * TQ, X, n, ld, dp, ranges + q0 * 16 * TQ, counts + q0 * 16 * TQ, chunk);
+    if ((e = launched()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 #define RBC_DISPATCH(metric, dp, FN, ...)                                               \
