@@ -143,6 +143,7 @@ int prepare(rbc_batch *bt) {
     BCK(b.pair_q.alloc(pair_cap * 4, s));
     BCK(b.pair_thr.alloc(pair_cap * 4, s));
     BCK(b.items.alloc(item_cap * sizeof(SearchItem), s));
+    b.item_cap = item_cap;
     BCK(b.ctl.alloc(64, s));
     BCK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
     srcs[i] = b.items.as<SearchItem>();

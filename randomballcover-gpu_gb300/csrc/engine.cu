@@ -118,7 +118,7 @@ static float round_down_f(double v) {
 int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
                     int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq, uint32_t qtile_over,
-                    uint64_t list_lo, uint64_t list_hi) {
+                    ListFilter filter) {
   const int tqv = tq < 0 ? idx->tune_tq : tq;
   const uint32_t nr = idx->nr, qtile = qtile_over ? qtile_over : (uint32_t)search_query_tile(idx->dp, tqv, list_width_for(k));
   uint32_t *ctl = b.ctl.as<uint32_t>();  // [0] work, [1] nitems, [2] err
@@ -155,10 +155,10 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
   a.phase = 1;
   CK(launch_plan_pass(a, mode, s));
   if (stage == 0) return RBC_OK;
-  CK(launch_tiles_per_list(cnt, offsets, nr, qtile, idx->item_rows, list_lo, list_hi, tcnt, s));
+  CK(launch_tiles_per_list(cnt, offsets, nr, qtile, idx->item_rows, filter, tcnt, s));
   CK(launch_exclusive_scan(tcnt, tstart, nr + 1, b.scan_tmp.p, ctl + 2, s));
-  CK(launch_plan_items(cnt, start, tstart, offsets, nr, qtile, idx->item_rows, list_lo, list_hi,
-                       b.items.as<SearchItem>(), ctl + 1, s));
+  CK(launch_plan_items(cnt, start, tstart, offsets, nr, qtile, idx->item_rows, filter, b.items.as<SearchItem>(),
+                       b.item_cap, ctl + 1, ctl + 2, s));
   if (stage == 1) return RBC_OK;
 
   SearchArgs sa{};
@@ -196,9 +196,17 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
   return RBC_OK;
 }
 
-uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile) {
-  const uint64_t chunks = idx->n / std::max<uint32_t>(idx->item_rows, 1) + idx->nr + 1;
-  return (mb / qtile + 1) * chunks + idx->nr + 1;
+// List r contributes ceil(cnt_r / qtile) x c_r items, c_r = its row chunks
+// (sum over lists <= n / item_rows + nr + 1); cnt_r <= mb, and in a probe
+// round sum cnt_r <= mb x probes, which bounds the tiles by
+// mb x probes / qtile + nr and each list's chunks by the largest list's.
+uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile, uint32_t probes) {
+  const uint64_t rows = std::max<uint32_t>(idx->item_rows, 1);
+  const uint64_t chunks = idx->n / rows + idx->nr + 1;
+  const uint64_t any = (mb / qtile + 1) * chunks + idx->nr + 1;
+  if (!probes) return any;
+  const uint64_t max_chunks = idx->max_list / rows + 1;
+  return std::min(any, (mb * probes / qtile + idx->nr + 1) * max_chunks + idx->nr + 1);
 }
 
 namespace {
@@ -446,6 +454,7 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   CK(b.pair_q.alloc(pair_cap * 4, s));
   CK(b.pair_thr.alloc(pair_cap * 4, s));
   CK(b.items.alloc(item_cap * sizeof(SearchItem), s));
+  b.item_cap = item_cap;
   CK(b.ctl.alloc(64, s));
   CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
   DevBuf stats, near, near_d, logits;
@@ -499,7 +508,7 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     CK(cudaStreamSynchronize(s));
     idx->stats.point_pairs = st[0];
     idx->stats.lists_probed = st[1];
-    if (ctl[2]) return fail((int)ctl[2], "rbc_query: a bounded device wait ran out");
+    if (ctl[2]) return fail((int)ctl[2], "rbc_query: a device-side check failed (bounded wait or work-list size)");
     if (idx->profile) {
       idx->prof.search_launches = idx->ev_used / 2;
       idx->prof.search_ms = 0;
@@ -551,7 +560,11 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   const uint32_t qtile = tc_query_tile(fmt);
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
   QueryBufs b;
-  const uint64_t pair_cap = mb * nr, item_cap = item_capacity(idx, mb, qtile);
+  // work items of the three plans: pruned round (query tiles of qtile), probe
+  // round on the FP32 path (16) and on the tensor cores (128)
+  const uint64_t pair_cap = mb * nr,
+                 item_cap = std::max({item_capacity(idx, mb, qtile), item_capacity(idx, mb, 16, P),
+                                      item_capacity(idx, mb, tc_query_tile(kTcSplit), P)});
   CK(b.Qp.alloc(mb * ld * 4, s));
   CK(b.Dqr.alloc(mb * nr * 4, s));
   CK(b.probe.alloc(mb * P * 4, s));
@@ -568,6 +581,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(b.pair_q.alloc(pair_cap * 4, s));
   CK(b.pair_thr.alloc(pair_cap * 4, s));
   CK(b.items.alloc(item_cap * sizeof(SearchItem), s));
+  b.item_cap = item_cap;
   CK(b.ctl.alloc(64, s));
   CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
   DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
@@ -686,19 +700,24 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     {
       const bool prof = idx->profile;
       idx->profile = false;
+      ListFilter small;
+      small.rows_hi = probe_rows;
       const int rc = plan_and_search(idx, b, mq, P, sl, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, pgrid,
-                                     nullptr, s, 2, 1, 0, 0, probe_rows);
+                                     nullptr, s, 2, 1, 0, small);
       idx->profile = prof;
       TRY(rc);
     }
     CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, mq, sl, k, sl_a.as<float>(),
                       sl_row.as<uint32_t>(), sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));
-    // probe round, large lists: tensor search into the seeded shortlists, then
-    // the k-th exact distance of each shortlist tightens the threshold
+    // probe round, large lists: tensor search into the seeded shortlists, one
+    // 128-query tile per B tile (measured faster than two-tile items even for
+    // the busiest probed lists), then the k-th exact distance of each
+    // shortlist tightens the threshold
     if (idx->max_list >= probe_rows) {
-      // few queries share a probed list: one 128-query tile per B tile
+      ListFilter large;
+      large.rows_lo = probe_rows;
       TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
-                          -1, tc_query_tile(kTcSplit), probe_rows, UINT64_MAX));
+                          -1, tc_query_tile(kTcSplit), large));
       if (idx->profile) CK(cudaEventRecord(idx->ev_pool[2], s));
       CK(launch_tc_search(tmA, idx->tmB, ta, grid, s, true));
       if (idx->profile) {
@@ -725,7 +744,8 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     CK(cudaMemcpyAsync(hc, ctl.p, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(bc, b.ctl.p, 12, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    if (hc[0] || bc[2]) return fail(RBC_ERR_ITER_LIMIT, "rbc_query: a bounded device wait ran out");
+    if (hc[0] || bc[2])
+      return fail(hc[0] ? (int)hc[0] : (int)bc[2], "rbc_query: a device-side check failed (bounded wait or work-list size)");
     if (idx->profile) {
       float ms = 0;
       CK(cudaEventElapsedTime(&ms, idx->ev_pool[0], idx->ev_pool[1]));

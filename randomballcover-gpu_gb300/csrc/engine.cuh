@@ -44,10 +44,11 @@ struct DevBuf {
   }
 };
 
-// Per-call buffers of one query batch.
+// Per-call buffers of one query batch; items holds item_cap work items.
 struct QueryBufs {
   DevBuf Qp, Dqr, probe, probed, res_d, res_i, tau, lock, cnt, start, cursor, tcnt, tstart, pair_q,
       pair_thr, items, ctl, scan_tmp;
+  uint64_t item_cap = 0;
 };
 
 }  // namespace rbc
@@ -58,16 +59,18 @@ namespace rbc {
 // Plan one query round (mode 0 probe pairs, mode 1 pruned pairs); stage 0
 // stops after the plan, 1 after the work items, 2 also runs the search.
 // tq < 0 uses the index's tuned tile.
-// qtile > 0 overrides the query tile of the work items; only lists of
-// list_lo <= rows < list_hi get items.
+// qtile > 0 overrides the query tile of the work items; only the lists the
+// filter selects get items.
 int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
                     int grid, unsigned long long *stats, cudaStream_t s, int stage = 2, int tq = -1,
-                    uint32_t qtile = 0, uint64_t list_lo = 0, uint64_t list_hi = UINT64_MAX);
+                    uint32_t qtile = 0, ListFilter filter = ListFilter());
 // Build the tensor-core operands of an index that has its partition.
 int build_tc(rbc_index *idx, cudaStream_t s);
-// Work items a plan of mb queries can produce (query tiles x row chunks).
-uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile);
+// Work items a plan of mb queries can produce with query tiles of qtile
+// (query tiles x row chunks); probes > 0 bounds a probe-round plan, whose
+// (query, list) pairs number at most mb x probes.
+uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile, uint32_t probes = 0);
 int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
                 uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s);
 int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *p,

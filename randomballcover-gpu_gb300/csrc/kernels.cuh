@@ -145,15 +145,21 @@ struct PlanArgs {
 // pruning bound survives.  a.phase 0 counts per list into a.list_cnt; phase 1
 // fills pair_q / pair_thr with a.list_cnt pointing at the scanned starts.
 cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s);
+// Which lists of a plan get work items: rows_lo <= rows < rows_hi and
+// cnt_lo <= planned queries < cnt_hi.
+struct ListFilter {
+  uint64_t rows_lo = 0, rows_hi = UINT64_MAX;
+  uint32_t cnt_lo = 0, cnt_hi = UINT32_MAX;
+};
 // Items per list: query tiles x chunks of at most max_rows list rows, for
-// the lists of lo <= rows < hi only.
+// the lists the filter selects only.
 cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, const uint64_t *offsets, uint32_t nr,
-                                  uint32_t qtile, uint32_t max_rows, uint64_t lo, uint64_t hi, uint32_t *tile_cnt,
+                                  uint32_t qtile, uint32_t max_rows, ListFilter f, uint32_t *tile_cnt,
                                   cudaStream_t s);
 cudaError_t launch_plan_items(const uint32_t *list_cnt, const uint32_t *list_start,
                               const uint32_t *tile_start, const uint64_t *offsets, uint32_t nr,
-                              uint32_t qtile, uint32_t max_rows, uint64_t lo, uint64_t hi, SearchItem *items,
-                              uint32_t *nitems, cudaStream_t s);
+                              uint32_t qtile, uint32_t max_rows, ListFilter f, SearchItem *items,
+                              uint64_t cap, uint32_t *nitems, uint32_t *err, cudaStream_t s);
 
 // Synthetic data.
 cudaError_t launch_synth(int kind, uint64_t seed, uint64_t stream_id, uint64_t r0, uint64_t rows,

@@ -186,30 +186,41 @@ __device__ __forceinline__ uint32_t row_chunks(const uint64_t *offsets, uint32_t
   return np == 0 ? 1u : (uint32_t)((np + max_rows - 1) / max_rows);
 }
 
-// Lists whose row count lies outside [lo, hi) get no items.
-__device__ __forceinline__ bool list_selected(const uint64_t *offsets, uint32_t r, uint64_t lo, uint64_t hi) {
+// Lists the filter leaves out get no items.
+__device__ __forceinline__ bool list_selected(const uint64_t *offsets, const uint32_t *list_cnt, uint32_t r,
+                                              const ListFilter &f) {
   const uint64_t np = offsets[r + 1] - offsets[r];
-  return np >= lo && np < hi;
+  const uint32_t c = list_cnt[r];
+  return np >= f.rows_lo && np < f.rows_hi && c >= f.cnt_lo && c < f.cnt_hi;
 }
 
 __global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, const uint64_t *__restrict__ offsets,
-                                      uint32_t nr, uint32_t qtile, uint32_t max_rows, uint64_t lo, uint64_t hi,
+                                      uint32_t nr, uint32_t qtile, uint32_t max_rows, ListFilter f,
                                       uint32_t *__restrict__ tile_cnt) {
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < nr)
-    tile_cnt[r] = list_selected(offsets, r, lo, hi) ? (list_cnt[r] + qtile - 1) / qtile * row_chunks(offsets, r, max_rows)
-                                                     : 0;
+    tile_cnt[r] = list_selected(offsets, list_cnt, r, f)
+                      ? (list_cnt[r] + qtile - 1) / qtile * row_chunks(offsets, r, max_rows)
+                      : 0;
   if (r == nr) tile_cnt[nr] = 0;
 }
 
-// items for list r: its query tiles x row chunks, in list order.
+// items for list r: its query tiles x row chunks, in list order.  A plan
+// with more items than the buffer holds writes none, records RBC_ERR_NOMEM
+// and leaves an empty work list (the caller sizes the buffer so this cannot
+// happen; the check keeps every write in bounds regardless).
 __global__ void plan_items_kernel(const uint32_t *__restrict__ list_cnt, const uint32_t *__restrict__ list_start,
                                   const uint32_t *__restrict__ tile_start, const uint64_t *__restrict__ offsets,
-                                  uint32_t nr, uint32_t qtile, uint32_t max_rows, uint64_t lo, uint64_t hi,
-                                  SearchItem *__restrict__ items, uint32_t *__restrict__ nitems) {
+                                  uint32_t nr, uint32_t qtile, uint32_t max_rows, ListFilter f,
+                                  SearchItem *__restrict__ items, uint64_t cap, uint32_t *__restrict__ nitems,
+                                  uint32_t *__restrict__ err) {
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r == nr) *nitems = tile_start[nr];
-  if (r >= nr || !list_selected(offsets, r, lo, hi)) return;
+  const uint32_t total = tile_start[nr];
+  if (r == nr) {
+    *nitems = total <= cap ? total : 0u;
+    if (total > cap) raise_error(err, RBC_ERR_NOMEM);
+  }
+  if (total > cap || r >= nr || !list_selected(offsets, list_cnt, r, f)) return;
   const uint32_t cnt = list_cnt[r];
   const uint32_t nt = (cnt + qtile - 1) / qtile, nc = row_chunks(offsets, r, max_rows);
   const uint64_t p0 = offsets[r], np = offsets[r + 1] - offsets[r];
@@ -254,17 +265,16 @@ cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s) {
 }
 
 cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, const uint64_t *offsets, uint32_t nr, uint32_t qtile,
-                                  uint32_t max_rows, uint64_t lo, uint64_t hi, uint32_t *tile_cnt, cudaStream_t s) {
-  tiles_per_list_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, offsets, nr, qtile, max_rows, lo, hi,
-                                                             tile_cnt);
+                                  uint32_t max_rows, ListFilter f, uint32_t *tile_cnt, cudaStream_t s) {
+  tiles_per_list_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, offsets, nr, qtile, max_rows, f, tile_cnt);
   return launched();
 }
 
 cudaError_t launch_plan_items(const uint32_t *list_cnt, const uint32_t *list_start, const uint32_t *tile_start,
-                              const uint64_t *offsets, uint32_t nr, uint32_t qtile, uint32_t max_rows, uint64_t lo,
-                              uint64_t hi, SearchItem *items, uint32_t *nitems, cudaStream_t s) {
+                              const uint64_t *offsets, uint32_t nr, uint32_t qtile, uint32_t max_rows, ListFilter f,
+                              SearchItem *items, uint64_t cap, uint32_t *nitems, uint32_t *err, cudaStream_t s) {
   plan_items_kernel<<<(nr + 1 + 255) / 256, 256, 0, s>>>(list_cnt, list_start, tile_start, offsets, nr, qtile,
-                                                         max_rows, lo, hi, items, nitems);
+                                                         max_rows, f, items, cap, nitems, err);
   return launched();
 }
 

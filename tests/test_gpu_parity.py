@@ -293,3 +293,21 @@ def test_bounded_waits_end_with_a_status_not_a_hang(rbc, oracle):
     ids, dists = rbc.brute_knn(X, Q, 5)
     ri, rd = oracle.knn(X, Q, 5)
     assert_same(ids, dists, ri, rd, rbc)
+
+
+def test_tensor_core_probe_round_busy_lists(rbc, oracle, monkeypatch):
+    """Large probed lists go to the tensor cores with one 128-query tile per
+    B tile -- lists probed by more than 128 queries take several items --
+    and small ones to the FP32 path; 60 lists and 3,000 queries x 4 probes
+    give both kinds."""
+    monkeypatch.setenv("RBC_TC_PROBE_ROWS", "500")
+    X = rbc.synth(2, 35, 0, 60000, 128)
+    Q = rbc.synth(2, 35, 1, 3000, 128)
+    idx = rbc.Index(X, 60, seed=8, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    inf = idx.info()
+    assert inf["min_list"] < 500 <= inf["max_list"]
+    ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
+    ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), 10)
+    assert_same(ids, dists, ri, rd, rbc)
+    assert idx.stats()["fallback_queries"] == 0
+    idx.close()
