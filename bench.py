@@ -89,7 +89,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-side", action="store_true",
                     help="skip the c2 side measurements (k = 128 and the double-precision variant)")
-    ap.add_argument("--router-probes", type=int, default=2, help="lists the learned form adds from the router")
+    ap.add_argument("--router-probes", type=int, default=1, help="lists the learned form adds from the router")
     ap.add_argument("--forms", default=None,
                     help="forms to time; the last one listed is the headline (default: per workload)")
     a = ap.parse_args()
