@@ -139,6 +139,11 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
   a.omg_rd = round_down_f(1.0 - g);
   a.c_ru = round_up_f(1.0 + 3.0 * g);
   a.opc_ru = round_up_f(2.0 + 3.0 * g);
+  // reciprocals, nudged by 2^-50 so the float rounding lands on the safe side
+  // of the exact value whatever the double evaluation's last bit
+  a.inv_opg_rd = round_down_f(1.0 / (1.0 + g) * (1.0 - 0x1p-50));
+  a.inv_omg_ru = round_up_f(1.0 / (1.0 - g) * (1.0 + 0x1p-50));
+  a.inv_opc_rd = round_down_f(1.0 / (2.0 + 3.0 * g) * (1.0 - 0x1p-50));
   a.list_cursor = b.cursor.as<uint32_t>();
   a.pair_q = b.pair_q.as<uint32_t>();
   a.pair_thr = b.pair_thr.as<float>();
@@ -551,14 +556,16 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   Pn = std::min(Pn, nr);
   const uint32_t P = routed ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
   const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
-  // the probe round's FP32 lists hold a whole shortlist; few queries share a
-  // probed list, so its query tiles are 16 wide (TQ = 1)
+  // the probe round's FP32 lists hold a whole shortlist; its query tiles
+  // follow the probed queries per list (16 wide when few share a list)
   const uint32_t sl = tc_shortlist(k), kw = list_width_for(sl);
-  const int pgrid = search_grid(idx->metric, idx->dp, 1, kw);
   uint64_t probe_rows = kTcProbeRows;
   if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) probe_rows = std::strtoull(env, nullptr, 10);
   const uint32_t qtile = tc_query_tile(fmt);
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
+  const uint64_t probe_per_list = mb * P / nr;
+  const int ptq = search_tq_for(idx->dp, probe_per_list >= 48 ? 4 : (probe_per_list >= 24 ? 2 : 1), kw);
+  const int pgrid = search_grid(idx->metric, idx->dp, ptq, kw);
   QueryBufs b;
   // work items of the three plans: pruned round (query tiles of qtile), probe
   // round on the FP32 path (16) and on the tensor cores (128)
@@ -703,7 +710,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       ListFilter small;
       small.rows_hi = probe_rows;
       const int rc = plan_and_search(idx, b, mq, P, sl, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, pgrid,
-                                     nullptr, s, 2, 1, 0, small);
+                                     nullptr, s, 2, ptq, 0, small);
       idx->profile = prof;
       TRY(rc);
     }
@@ -767,9 +774,14 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       CK(launch_gather_rows(b.Qp.as<float>(), ld, failq.as<uint32_t>(), nfail, Qf.as<float>(), s));
       rbc_profile keep = idx->prof;
       rbc_query_stats keep_stats = idx->stats;
-      TRY(query_index(idx, Qf.as<float>(), nfail, ld, k, RBC_QUERY_EXACT, fi.as<uint32_t>(), fd.as<float>(), k, s));
+      const int keep_tq = idx->tune_tq;
+      idx->tune_tq = 1;  // a handful of queries: 16-query tiles
+      const int rc = query_index(idx, Qf.as<float>(), nfail, ld, k, RBC_QUERY_EXACT, fi.as<uint32_t>(), fd.as<float>(),
+                                 k, s);
+      idx->tune_tq = keep_tq;
       idx->prof = keep;
       idx->stats = keep_stats;
+      TRY(rc);
       CK(launch_scatter_results(fi.as<uint32_t>(), fd.as<float>(), failq.as<uint32_t>(), nfail, k,
                                 dIds ? dIds + b0 * ldo : nullptr, dDists ? dDists + b0 * ldo : nullptr, ldo, s));
       CK(cudaStreamSynchronize(s));

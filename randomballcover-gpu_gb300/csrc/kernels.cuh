@@ -132,6 +132,7 @@ struct PlanArgs {
   float opg_ru, omg_rd;    // 1 + gamma rounded up, 1 - gamma rounded down (gamma: relative
                            // error bound of a computed distance)
   float c_ru, opc_ru;      // c = 1 + 3 gamma and 1 + c, rounded up
+  float inv_opg_rd, inv_omg_ru, inv_opc_rd;  // 1/(1+gamma) and 1/(1+c) rounded down, 1/(1-gamma) up
   uint32_t *list_cnt;      // nr+1 counters (surviving queries per list)
   uint32_t *list_cursor;   // nr fill cursors
   uint32_t *pair_q;        // list-major surviving (query) entries

@@ -94,24 +94,25 @@ __global__ void row_topp_kernel(const float *__restrict__ D, uint64_t m, uint32_
 
 // Lower bound on the computed distance of any member of list r, in the
 // comparison space (squared L2 or L1), evaluated in FP32 with every operation
-// rounded in the safe direction:
+// rounded in the safe direction (divisions as products with reciprocals
+// rounded the safe way, a fraction of an ulp looser):
 //   lo   = D(q,r)/(1+g) (sqrt for L2), rounded down
-//   hi0  = D(q,r0)/(1-g) (sqrt for L2), rounded up
+//   hi0  = D(q,r0)/(1-g) (sqrt for L2), rounded up; c hi0 rounded up is the
+//          per-query term chi0 (query_term)
 //   hpsi = psi_r/(1-g) (sqrt for L2), rounded up
 //   lb   = max(lo - hpsi, (lo - c hi0) / (1 + c)), rounded down
 //   thr  = lb^2 (1-g) (L2) or lb (1-g) (L1), rounded down.
-__device__ __forceinline__ float prune_threshold(float dqr, float dq0, float hpsi, const PlanArgs &a) {
-  float lo, hi0;
-  if (a.metric == RBC_L1) {
-    lo = __fdiv_rd(dqr, a.opg_ru);
-    hi0 = __fdiv_ru(dq0, a.omg_rd);
-  } else {
-    lo = __fsqrt_rd(__fdiv_rd(dqr, a.opg_ru));
-    hi0 = __fsqrt_ru(__fdiv_ru(dq0, a.omg_rd));
-  }
+__device__ __forceinline__ float query_term(float dq0, const PlanArgs &a) {
+  const float t = __fmul_ru(dq0, a.inv_omg_ru);
+  return __fmul_ru(a.c_ru, a.metric == RBC_L1 ? t : __fsqrt_ru(t));
+}
+
+__device__ __forceinline__ float prune_threshold(float dqr, float chi0, float hpsi, const PlanArgs &a) {
+  const float t = __fmul_rd(dqr, a.inv_opg_rd);
+  const float lo = a.metric == RBC_L1 ? t : __fsqrt_rd(t);
   const float lb1 = __fsub_rd(lo, hpsi);
-  const float num = __fsub_rd(lo, __fmul_ru(a.c_ru, hi0));
-  const float lb2 = num > 0.f ? __fdiv_rd(num, a.opc_ru) : 0.f;
+  const float num = __fsub_rd(lo, chi0);
+  const float lb2 = num > 0.f ? __fmul_rd(num, a.inv_opc_rd) : 0.f;
   const float lb = fmaxf(lb1, lb2);
   if (!(lb > 0.f)) return 0.f;
   return a.metric == RBC_L1 ? __fmul_rd(lb, a.omg_rd) : __fmul_rd(__fmul_rd(lb, lb), a.omg_rd);
@@ -126,9 +127,16 @@ __device__ __forceinline__ float psi_bound(float psi, const PlanArgs &a) {
 // mode 1: every (query, list) pair except the probed ones whose bound
 // survives; pass 0 counts per list, pass 1 writes the list-major entries.
 __global__ void plan_kernel(PlanArgs a) {
+  __shared__ float s_tau[kPlanQueries], s_chi0[kPlanQueries];
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t q0 = (uint64_t)blockIdx.y * kPlanQueries;
   const uint64_t q1 = min(a.m, q0 + kPlanQueries);
+  // the per-query terms, once per block
+  for (uint32_t j = threadIdx.x; j < q1 - q0; j += blockDim.x) {
+    s_tau[j] = __uint_as_float(a.tau[q0 + j]);
+    s_chi0[j] = query_term(a.probed[(q0 + j) * a.P], a);
+  }
+  __syncthreads();
   const bool rv = r < a.nr;
   const bool nonempty = rv && a.offsets[r + 1] > a.offsets[r];
   const float hpsi = rv ? psi_bound(a.radius[r], a) : 0.f;
@@ -144,9 +152,8 @@ __global__ void plan_kernel(PlanArgs a) {
       bool member = false;
       for (uint32_t p = 0; p < a.P; p++) member |= a.probe[q * a.P + p] == r;
       if (member) continue;
-      const float tau = __uint_as_float(a.tau[q]);
-      const float thr = prune_threshold(a.Dqr[q * a.nr + r], a.probed[q * a.P], hpsi, a);
-      if (thr > tau) continue;
+      const float thr = prune_threshold(a.Dqr[q * a.nr + r], s_chi0[q - q0], hpsi, a);
+      if (thr > s_tau[q - q0]) continue;
       if (sweep == 0) {
         cnt++;
       } else {

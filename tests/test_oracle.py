@@ -204,3 +204,25 @@ def test_f64_range_count_definition(oracle):
     assert (cnt <= 9).all() and (cnt >= 0).all()
     cnt2 = oracle.range_count_f64(X, Q, np.nextafter(dists[:, 9], np.inf))
     assert (cnt2 >= 10).all()
+
+
+def test_pruning_reciprocals_round_the_safe_way():
+    """The plan's pruning bound multiplies by reciprocals of 1 + gamma, 1 - gamma
+    and 1 + c; the host rounds each (after a 2^-50 nudge) so the float is on
+    the safe side of the exact rational value, for every padded dimension."""
+    from fractions import Fraction as Fr
+
+    def up(v):
+        f = np.float32(v)
+        return np.nextafter(f, np.float32(np.inf)) if float(f) < v else f
+
+    def down(v):
+        f = np.float32(v)
+        return np.nextafter(f, np.float32(0)) if float(f) > v else f
+
+    for dp in range(4, 516, 4):
+        g = (dp + 8) * 2.0 ** -23
+        G = Fr(dp + 8, 2 ** 23)
+        assert Fr(float(down(1.0 / (1.0 + g) * (1.0 - 2.0 ** -50)))) <= 1 / (1 + G)
+        assert Fr(float(up(1.0 / (1.0 - g) * (1.0 + 2.0 ** -50)))) >= 1 / (1 - G)
+        assert Fr(float(down(1.0 / (2.0 + 3.0 * g) * (1.0 - 2.0 ** -50)))) <= 1 / (2 + 3 * G)
