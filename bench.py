@@ -371,7 +371,15 @@ def run_engine(a):
     ids = torch.empty((m, k), dtype=torch.int32, device="cuda")
     dists = torch.empty((m, k), dtype=torch.float32, device="cuda")
 
+    # the tensor form's knobs are tuned per form on queries drawn apart from
+    # the timed ones (same distribution), outside the timed region
+    Qtune = pyrbc.synth(w["kind"], w["seed"], 3, min(m, 20_000), w["d"], **synth)
+    tuning = {}
+
     def timed(mode, steps, warmup, sample_clocks=False):
+        if mode & pyrbc.QUERY_EXACT_TC and k <= 32:
+            idx.autotune_tc(Qtune, k, mode)
+            tuning[mode] = idx.tc_tuning()
         for _ in range(warmup):
             idx.query(Q, k, mode=mode, out=(ids, dists))
         barrier()
@@ -487,6 +495,7 @@ def run_engine(a):
                  "side": side}
         for f, r in results.items():
             extra["forms"][f] = {"value": r["value"], "ms_per_step": r["ms"] / r["steps"],
+                                 "tc_probes_and_probe_rows": tuning.get(modes[f]),
                                  "lists_per_query": r["lists"] / (m * r["steps"]),
                                  "pairs_per_query": r["point_pairs"] / (m * r["steps"]),
                                  "fallback_queries_per_step": r["fallback"] / r["steps"],

@@ -551,7 +551,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   // lists searched in the probe round: the nearest representatives' (plus,
   // routed, the router's picks among the others); RBC_TC_PROBES overrides the
   // number of nearest ones
-  uint32_t Pn = kTcProbes;
+  uint32_t Pn = idx->tc_probes ? idx->tc_probes : kTcProbes;
   if (const char *env = std::getenv("RBC_TC_PROBES")) Pn = std::max(1, std::min(8, std::atoi(env)));
   Pn = std::min(Pn, nr);
   const uint32_t P = routed ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
@@ -559,7 +559,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   // the probe round's FP32 lists hold a whole shortlist; its query tiles
   // follow the probed queries per list (16 wide when few share a list)
   const uint32_t sl = tc_shortlist(k), kw = list_width_for(sl);
-  uint64_t probe_rows = kTcProbeRows;
+  uint64_t probe_rows = idx->tc_probe_rows ? idx->tc_probe_rows : kTcProbeRows;
   if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) probe_rows = std::strtoull(env, nullptr, 10);
   const uint32_t qtile = tc_query_tile(fmt);
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));

@@ -123,6 +123,11 @@ struct rbc_index {
   // list-search tile (0 = default) and the longest row run of one work item
   int tune_tq = 0;
   uint32_t item_rows = 16384;
+  // tensor-form tuning (rbc_set_tc_tuning / rbc_autotune_tc): nearest lists
+  // searched in the probe round and the row count from which a probed list
+  // goes to the tensor cores (0: the defaults)
+  uint32_t tc_probes = 0;
+  uint64_t tc_probe_rows = 0;
   // learned router (rbc_set_router): probes its top router_probes lists
   rbc_router *router = nullptr;
   uint32_t router_probes = 0;

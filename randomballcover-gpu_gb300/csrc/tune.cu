@@ -1,4 +1,4 @@
-// tune.cu -- the autotuner of the FP32 list search.
+// tune.cu -- the autotuners of the FP32 list search and of the tensor form.
 //
 // Two knobs shape the plain search: the query tile (16 x TQ queries per CTA,
 // TQ rows per thread) and the longest run of list rows a work item covers
@@ -6,6 +6,12 @@
 // balanced).  rbc_autotune times every valid pair on sample queries with CUDA
 // events and keeps the fastest; a cache file (one line per index shape:
 // "n d reps k metric tq item_rows ms") lets later processes skip the timing.
+//
+// The tensor form has two knobs of its own: how many nearest lists the probe
+// round searches (more gives the pruned round a tighter start, at the
+// probe round's cost) and from how many rows a probed list goes to the
+// tensor cores rather than the FP32 path.  rbc_autotune_tc times a small grid
+// of both on sample queries and keeps the fastest.
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -120,6 +126,74 @@ int rbc_autotune(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint
     std::fprintf(fp, "%s %d %u %.4f\n", key.c_str(), best_tq, best_rows, best);
     std::fclose(fp);
   }
+  return RBC_OK;
+}
+
+int rbc_set_tc_tuning(rbc_index *idx, uint32_t probes, uint64_t probe_rows) {
+  if (!idx) return fail(RBC_ERR_INVALID, "rbc_set_tc_tuning: NULL index");
+  if (probes > 8) return fail(RBC_ERR_INVALID, "rbc_set_tc_tuning: probes must be at most 8");
+  idx->tc_probes = probes;
+  idx->tc_probe_rows = probe_rows;
+  return RBC_OK;
+}
+
+int rbc_get_tc_tuning(const rbc_index *idx, uint32_t *probes, uint64_t *probe_rows) {
+  if (!idx || !probes || !probe_rows) return fail(RBC_ERR_INVALID, "rbc_get_tc_tuning: NULL argument");
+  *probes = idx->tc_probes;
+  *probe_rows = idx->tc_probe_rows;
+  return RBC_OK;
+}
+
+int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
+                    void *stream) {
+  if (!idx || !dQ || m == 0) return fail(RBC_ERR_INVALID, "rbc_autotune_tc: bad argument");
+  if (!(idx->flags & RBC_BUILD_BF16)) return fail(RBC_ERR_INVALID, "rbc_autotune_tc: index has no BF16 lists");
+  if ((mode & 0xFFu) != RBC_QUERY_EXACT_TC) return fail(RBC_ERR_INVALID, "rbc_autotune_tc: mode must be RBC_QUERY_EXACT_TC");
+  cudaStream_t s = (cudaStream_t)stream;
+  DevBuf ids, dists;
+  cudaError_t e = ids.alloc(m * k * 4, s);
+  if (e == cudaSuccess) e = dists.alloc(m * k * 4, s);
+  if (e != cudaSuccess) return cuda_fail(e, "rbc_autotune_tc: buffers");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const bool keep_profile = idx->profile;
+  const rbc_query_stats keep_stats = idx->stats;
+  idx->profile = false;
+  double best = 1e30;
+  uint32_t best_p = 0;
+  uint64_t best_rows = 0;
+  int rc = RBC_OK;
+  for (uint32_t p : {2u, 4u, 8u}) {
+    for (uint64_t r : {2048ull, 8192ull, 32768ull}) {
+      idx->tc_probes = p;
+      idx->tc_probe_rows = r;
+      double ms_min = 1e30;
+      for (int rep = 0; rep < 3 && rc == RBC_OK; rep++) {  // the first run warms up
+        cudaEventRecord(e0, s);
+        rc = query_index(idx, dQ, m, ldq, k, mode, ids.as<uint32_t>(), dists.as<float>(), k, s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep) ms_min = std::min(ms_min, (double)ms);
+      }
+      if (rc != RBC_OK) break;
+      if (ms_min < best) {
+        best = ms_min;
+        best_p = p;
+        best_rows = r;
+      }
+    }
+    if (rc != RBC_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  idx->profile = keep_profile;
+  idx->stats = keep_stats;
+  if (rc != RBC_OK) return rc;
+  idx->tc_probes = best_p;
+  idx->tc_probe_rows = best_rows;
   return RBC_OK;
 }
 

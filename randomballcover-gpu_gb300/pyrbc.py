@@ -77,6 +77,9 @@ SIGNATURES = {
     "rbc_batch_destroy": ([_VP], _INT),
     "rbc_set_tuning": ([_VP, _INT, _U32], _INT),
     "rbc_autotune": ([_VP, _VP, _U64, _U32, _U32, C.c_char_p, _VP], _INT),
+    "rbc_set_tc_tuning": ([_VP, _U32, _U64], _INT),
+    "rbc_autotune_tc": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP], _INT),
+    "rbc_get_tc_tuning": ([_VP, C.POINTER(_U32), C.POINTER(_U64)], _INT),
     "rbc_router_create": ([_U32, _U32, _U32, _U64, C.POINTER(_VP)], _INT),
     "rbc_router_destroy": ([_VP], _INT),
     "rbc_router_num_params": ([_VP, C.POINTER(_U64)], _INT),
@@ -287,6 +290,21 @@ class Index:
         Q = _dev(Q, torch.float32)
         check(lib().rbc_autotune(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), k,
                                  cache_path.encode() if cache_path else None, _stream(stream)))
+
+    def set_tc_tuning(self, probes=0, probe_rows=0):
+        check(lib().rbc_set_tc_tuning(self.h, probes, probe_rows))
+
+    def tc_tuning(self):
+        """(probes, probe_rows) of the tensor form; 0 means the default."""
+        p, r = C.c_uint32(), C.c_uint64()
+        check(lib().rbc_get_tc_tuning(self.h, C.byref(p), C.byref(r)))
+        return p.value, r.value
+
+    def autotune_tc(self, Q, k, mode=QUERY_EXACT_TC, stream=None):
+        """Tensor-form knobs (probed lists, FP32/tensor split) timed on sample queries."""
+        import torch
+        Q = _dev(Q, torch.float32)
+        check(lib().rbc_autotune_tc(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), k, mode, _stream(stream)))
 
     def set_router(self, router, probes=1):
         self._router = router

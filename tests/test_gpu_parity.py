@@ -311,3 +311,27 @@ def test_tensor_core_probe_round_busy_lists(rbc, oracle, monkeypatch):
     assert_same(ids, dists, ri, rd, rbc)
     assert idx.stats()["fallback_queries"] == 0
     idx.close()
+
+
+def test_tensor_core_autotune(rbc, oracle):
+    """rbc_autotune_tc picks the probe count and the FP32 / tensor split on
+    sample queries; answers stay the oracle's whatever it picks."""
+    X = rbc.synth(1, 37, 0, 30000, 64, ncomp=100, sigma_lo=0.05, sigma_hi=0.05)
+    Q = rbc.synth(1, 37, 1, 300, 64, ncomp=100, sigma_lo=0.05, sigma_hi=0.05)
+    Qt = rbc.synth(1, 37, 3, 500, 64, ncomp=100, sigma_lo=0.05, sigma_hi=0.05)
+    idx = rbc.Index(X, 200, seed=4, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    assert idx.tc_tuning() == (0, 0)
+    idx.autotune_tc(Qt, 10)
+    p, r = idx.tc_tuning()
+    assert p in (2, 4, 8) and r in (2048, 8192, 32768)
+    ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
+    ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), 10)
+    assert_same(ids, dists, ri, rd, rbc)
+    idx.set_tc_tuning(1, 100)  # manual setting, then back to the defaults
+    ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
+    assert_same(ids, dists, ri, rd, rbc)
+    idx.set_tc_tuning()
+    assert idx.tc_tuning() == (0, 0)
+    with pytest.raises(rbc.RBCError):
+        idx.set_tc_tuning(9, 0)
+    idx.close()
