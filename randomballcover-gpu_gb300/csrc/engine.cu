@@ -227,6 +227,10 @@ int build_tc(rbc_index *idx, cudaStream_t s) {
   TRY(tc_build(idx->Xp, idx->perm, idx->offsets, idx->R, idx->radius, idx->n, idx->n_pad, idx->nr, idx->d, idx->ld,
                idx->kp, &idx->tc, &idx->device_bytes, s));
   CK(tc_make_map(&idx->tmB, idx->tc.Xh, idx->n_pad, idx->tc.cols, 128));
+  if (idx->tc.Wh)
+    CK(tc_make_map_w(&idx->tmW, idx->tc.Wh, idx->n_pad));
+  else
+    idx->tmW = idx->tmB;  // the split format reads no w operand
   CK(cudaStreamSynchronize(s));
   return RBC_OK;
 }
@@ -726,7 +730,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
                           -1, tc_query_tile(kTcSplit), large));
       if (idx->profile) CK(cudaEventRecord(idx->ev_pool[2], s));
-      CK(launch_tc_search(tmA, idx->tmB, ta, grid, s, true));
+      CK(launch_tc_search(tmA, idx->tmB, idx->tmW, ta, grid, s, true));
       if (idx->profile) {
         CK(cudaEventRecord(idx->ev_pool[3], s));
         tc_probe = true;
@@ -741,7 +745,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     TRY(plan_and_search(idx, b, mq, P, k, 1, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
                         -1, qtile));
     if (idx->profile) CK(cudaEventRecord(idx->ev_pool[0], s));
-    CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
+    CK(launch_tc_search(tmA, idx->tmB, idx->tmW, ta, grid, s));
     if (idx->profile) CK(cudaEventRecord(idx->ev_pool[1], s));
     ra.tau = nullptr;
     ra.ids = dIds ? dIds + b0 * ldo : nullptr;
@@ -933,7 +937,7 @@ int rbc_build_host(const float *hX, uint64_t n, uint32_t d, uint32_t ldx, const 
 int rbc_destroy(rbc_index *idx) {
   if (!idx) return RBC_OK;
   void *ptrs[] = {idx->Xp,      idx->perm,   idx->offsets, idx->radius,     idx->R,  idx->os_lists, idx->os_counts,
-                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->tc.Xh, idx->tc.w,  idx->owner,
+                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->tc.Xh, idx->tc.w,  idx->tc.Wh, idx->owner,
                   idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm, idx->tc.mu, idx->tc.iperm, idx->X64, idx->norm64};
   for (void *p : ptrs)
     if (p) cudaFree(p);

@@ -203,6 +203,19 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t smem_addr) {
   return d;
 }
 
+// Shared-memory matrix descriptor of a K-major tile of 16 halves per row in
+// 32-byte swizzled rows (K = 16, one MMA step): 8-row groups 256 bytes apart,
+// layout SWIZZLE_32B (6).
+__device__ __forceinline__ uint64_t sw32_desc(uint32_t smem_addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((smem_addr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)(16u >> 4) << 16;               // leading byte offset (unused: K fits one swizzle row)
+  d |= (uint64_t)(256u >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)1 << 46;                        // descriptor version
+  d |= (uint64_t)6 << 61;                        // SWIZZLE_32B
+  return d;
+}
+
 // Instruction descriptor of kind::f16: BF16 x BF16 -> F32, both K-major.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
   return (1u << 4)            // D format F32

@@ -98,6 +98,11 @@ struct RerankArgs {
 //   ||q-c||^2 and w          g (||q-c||^2 + ||x'||^2 + 2 C |x'|)
 //   three final roundings    u (||q-c||^2 + 3 (2|q-mu||x'| + ||x'||^2 + 2C|x'|))
 //   the exact distance       g (||q-c|| + |x'|)^2
+//   BF16 format only, where w is folded into the product (D = q.x' - w/2,
+//   the three BF16 pieces of w added by a last MMA step of 16 terms):
+//     the pieces' residual   2^-24 W,  W = ||x'||^2 + 2C|x'| >= |w|
+//     that step's rounding   2 * 16 2^-22 (|q-mu||x'| + 0.51 W)
+//     pieces underflowing    2^-120 (absolute)
 // doubled as a margin.
 __host__ __device__ inline float tc_error_bound(float Dqr, float qn, float X, float C, uint32_t q_inexact,
                                                 uint32_t x_inexact, uint32_t format, uint32_t d) {
@@ -120,8 +125,13 @@ __host__ __device__ inline float tc_error_bound(float Dqr, float qn, float X, fl
   const float B = g * (qc2 + X * X + 2.f * Cb * X);
   const float R = u * (qc2 + 3.f * (2.f * qx + X * X + 2.f * Cb * X));
   const float F = g * (sqrtf(qc2) + X) * (sqrtf(qc2) + X);
+  float Wf = 0.f;
+  if (format != kTcSplit) {
+    const float W = X * X + 2.f * Cb * X;
+    Wf = 5.9604644775390625e-08f * W + 32.f * 2.384185791015625e-07f * (qx + 0.51f * W) + 7.52316384526264e-37f;
+  }
   // the float evaluation of this bound errs by far less than the final factor 2 covers
-  return 2.f * (A + B + R + F) * (1.f + 1e-5f);
+  return 2.f * (A + B + R + F + Wf) * (1.f + 1e-5f);
 }
 
 bool tc_supported(uint32_t dp);
@@ -129,11 +139,14 @@ uint32_t tc_kp(uint32_t d);
 int tc_grid();
 uint32_t tc_query_tile(uint32_t format);  // queries per work item (128 x tiles per CTA)
 cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32_t cols, uint32_t box_rows);
+// TMA map of the BF16 format's w operand rows (16 halves, 128-row boxes, 32-byte swizzle)
+cudaError_t tc_make_map_w(CUtensorMap *map, const void *ptr, uint64_t rows);
 
 // Build: centered rows of each list (x' = x - c_r), the format check, per-list
 // scales and bounds, the half-precision operand rows and w.
 struct TcBuild {
   void *Xh;          // n_pad x cols halves (cols = kp, or 2 kp for the split format)
+  void *Wh;          // BF16 format: n_pad x 16 halves, the w operand of the folded product
   float *w;          // n_pad + 128
   float *lscale, *lxmax, *lcnorm;  // nr each
   float *mu;         // kp: the query centering vector (zero in the exact format)
@@ -159,8 +172,9 @@ cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t k
                            cudaStream_t s);
 // narrow: one 128-query tile per B tile in the BF16 format as well (items
 // planned with query tiles of 128), for item sets whose tiles run sparse.
-cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
-                             cudaStream_t s, bool narrow = false);
+// tmW: the w operand rows (BF16 format; unused by the split format).
+cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUtensorMap &tmW,
+                             const TcArgs &a, int grid, cudaStream_t s, bool narrow = false);
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s);
 
 }  // namespace rbc

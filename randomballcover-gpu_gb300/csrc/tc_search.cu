@@ -69,6 +69,7 @@ constexpr int kBM = 128, kBN = 128, kEpiGroups = 2;
 constexpr int kThreads = 128 + 128 * kEpiGroups;
 constexpr int kLocal = 8;  // per-thread candidate buffer, in registers
 constexpr uint32_t kTile16K = 16384;           // 128 rows x 128 bytes (one 64-wide K block of halves)
+constexpr uint32_t kWTile = 4096;              // 128 rows x 32 bytes: the folded w operand of one B tile
 constexpr uint32_t kLockSpin = 1u << 22;
 constexpr uint32_t kMaxA = 2, kMaxB = 4;
 constexpr size_t kSmemLimit = 232448;
@@ -238,13 +239,25 @@ __device__ __forceinline__ float lane_merge(const TcArgs &a, uint32_t q, const f
   return theta;
 }
 
-// Per-item state of one query row, staged by warp 3 for the epilogue.
+// Per-item state of one query row, staged by warp 3 for the epilogue (split
+// format; the BF16 format needs only the query and Dqr).
 struct RowState {
   uint32_t q;
   float dq, thv, alpha;
 };
+struct RowStateF {
+  uint32_t q;
+  float dq;
+};
 
 __device__ const float g_inf = INFINITY;
+
+// max(a, b, c) in one instruction (sm_100 and later)
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
 
 __device__ __forceinline__ void cp_async4(float *smem, const float *gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
@@ -259,9 +272,15 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 template <int MT, bool SPLIT>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                     const __grid_constant__ TcArgs a) {
+                     const __grid_constant__ CUtensorMap tmW, const __grid_constant__ TcArgs a) {
   constexpr uint32_t ACC = SPLIT ? 2 : 1;     // accumulators per query tile: hi.hi (+ corrections)
   constexpr uint32_t NSLOT = 4 / (MT * ACC);  // tensor-memory slots of MT x ACC x 128 columns
+  // BF16 format: w is folded into the product.  Each B stage carries the
+  // tile's w operand (three BF16 pieces per row, by TMA from tmW) and one
+  // more MMA per accumulator multiplies it by a constant -1/4 tile, so the
+  // accumulator holds D = q.x' - w / 2 and v = -2 D needs no per-value work
+  // in the epilogue.  The split format adds w in the epilogue instead.
+  constexpr bool FOLD = !SPLIT;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_a_full[kMaxA], bar_a_empty[kMaxA], bar_b_full[kMaxB], bar_b_empty[kMaxB],
       bar_t_full[4], bar_t_empty[4], bar_x_full[4], bar_r_full[2], bar_r_empty[2];
@@ -271,13 +290,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const uint32_t kb = a.kb, kbh = SPLIT ? 2 * kb : kb;  // K blocks of a stored row (hi [+ lo])
   const uint32_t AS = a.a_stages, BS = a.b_stages;
-  const uint32_t a_tile = kbh * kTile16K, a_stage = MT * a_tile, b_stage = kbh * kTile16K;
+  const uint32_t a_tile = kbh * kTile16K, a_stage = MT * a_tile, b_bytes = kbh * kTile16K;
+  const uint32_t b_stage = b_bytes + (FOLD ? kWTile : 0u);  // B tile [+ its w operand]
   unsigned char *sA = base;
   unsigned char *sB = sA + AS * a_stage;
-  float *xs = reinterpret_cast<float *>(sB + BS * b_stage);  // NSLOT x 128 row constants
-  RowState *rs = reinterpret_cast<RowState *>(xs + NSLOT * kBN);  // 2 x 256 staged row states
-  float *mstage = reinterpret_cast<float *>(rs + 2 * 2 * kBM);     // per epilogue thread: a.stage_words
-                                                                   // of merge staging (or none)
+  unsigned char *sC = sB + BS * b_stage;
+  // split: NSLOT x 128 row constants; BF16: the constant tile of the w product
+  float *xs = reinterpret_cast<float *>(sC);
+  unsigned char *sK = sC;
+  unsigned char *sR = sC + (FOLD ? kWTile : NSLOT * kBN * 4);
+  RowState *rs = reinterpret_cast<RowState *>(sR);    // 2 x 256 staged row states
+  RowStateF *rsf = reinterpret_cast<RowStateF *>(sR);
+  float *mstage = reinterpret_cast<float *>(sR + 2 * 2 * kBM * (FOLD ? sizeof(RowStateF) : sizeof(RowState)));
+  // per epilogue thread: a.stage_words of merge staging (or none)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == 1) {
@@ -304,6 +329,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     fence_barrier_init();
   }
+  if (FOLD && tid < (int)(kWTile / 16)) {
+    // every row of the constant tile is -1/4 at halves 0-2 and 8-10, zero
+    // elsewhere (the w operand rows hold w1 w2 w3 at the same places), so the
+    // layout of the 16-half rows does not matter
+    const uint32_t m4 = 0xBE80BE80u, m1 = 0x0000BE80u;  // BF16 -0.25
+    reinterpret_cast<uint4 *>(sK)[tid] = make_uint4(m4, m1, 0u, 0u);
+    fence_proxy_async();
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -314,6 +347,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ------------------------------------------------ TMA producer of the B tiles
     if (lane == 0) {
       prefetch_tensormap(&tmB);
+      if (FOLD) prefetch_tensormap(&tmW);
       uint32_t bi = 0;
       unsigned long long pairs = 0, lists = 0;
       bool ok = true;
@@ -329,6 +363,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int32_t row = (int32_t)(item.p0 + (uint64_t)t * kBN);
           for (uint32_t k = 0; k < kbh; k++)
             tma_load_2d(sB + sb * b_stage + k * kTile16K, &tmB, (int32_t)(k * 64), row, &bar_b_full[sb]);
+          if (FOLD) tma_load_2d(sB + sb * b_stage + b_bytes, &tmW, 0, row, &bar_b_full[sb]);
         }
       }
       // drain: wait (bounded) for the copies still in flight before leaving
@@ -375,6 +410,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 }
               }
             }
+            // -w / 2 last: the products' partial sums stay at the scale of |q| |x'|
+            if (FOLD) mma_bf16(d, sw32_desc(smem_u32(sK)), sw32_desc(b0 + b_bytes), idesc, 1);
           }
           mma_commit(&bar_b_empty[sb]);
           mma_commit(&bar_t_full[slot]);
@@ -382,8 +419,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (ok) mma_commit(&bar_a_empty[sa]);
       }
     }
-  } else if (warp == 2) {
-    // ------------------------------------------------ row constants of each B tile
+  } else if (warp == 2 && !FOLD) {
+    // ------------------------------------------------ row constants of each B tile (split format)
     uint32_t bi = 0;
     bool ok = true;
     for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
@@ -420,6 +457,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // lane l owns rows 4l..4l+3 of each query tile (one gather4 per tile and K block)
       int32_t rr[MT][4];
       RowState *dst = rs + slot * 2 * kBM;
+      RowStateF *dstf = rsf + slot * 2 * kBM;
       const float ls = SPLIT ? a.lscale[item.list] : 1.f;
       const float X = a.lxmax[item.list], C = a.lcnorm[item.list];
 #pragma unroll
@@ -435,13 +473,16 @@ __global__ void __launch_bounds__(kThreads, 1)
             rr[g][j] = (int32_t)q;
             st.q = q;
             st.dq = dq;
-            st.thv = v_threshold(__uint_as_float(__ldcg(a.sl_theta + q)), dq);
+            if (!FOLD) st.thv = v_threshold(__uint_as_float(__ldcg(a.sl_theta + q)), dq);
             if (SPLIT) st.alpha = -2.f / (a.qscale[q] * ls);
             const float E = tc_error_bound(dq, a.qnorm[q], X, C, a.q_inexact ? a.q_inexact[q] : 1u, a.x_inexact,
                                            a.format, a.d);
             atomicMax(a.emax + q, __float_as_uint(E));
           }
-          dst[row] = st;
+          if (FOLD)
+            dstf[row] = RowStateF{st.q, st.dq};
+          else
+            dst[row] = st;
         }
       __syncwarp();
       if (lane == 0) mbar_arrive(&bar_r_full[slot]);
@@ -516,10 +557,20 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t ntiles = (item.np + kBN - 1) / kBN;
       const uint32_t rslot = ai & 1;
       if (!(ok = mbar_wait(&bar_r_full[rslot], (ai >> 1) & 1, a.err))) break;
-      const RowState st = rs[rslot * 2 * kBM + arow];
-      const uint32_t q = st.q;
-      const float dq = st.dq, alpha = st.alpha;
-      float thv = st.thv;
+      uint32_t q;
+      float dq, alpha = -2.f, thv;
+      if (FOLD) {
+        const RowStateF st = rsf[rslot * 2 * kBM + arow];
+        q = st.q;
+        dq = st.dq;
+        thv = arow < item.nq ? FLT_MAX : -FLT_MAX;  // the first tile's refresh sets it
+      } else {
+        const RowState st = rs[rslot * 2 * kBM + arow];
+        q = st.q;
+        dq = st.dq;
+        alpha = st.alpha;
+        thv = st.thv;
+      }
       uint32_t nl = 0;
       // other CTAs tighten the query's shortlist all the time: each tile
       // refreshes the filter with the threshold read one tile earlier (a
@@ -532,12 +583,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         const float th_now = th_next;
         th_next = arow < item.nq ? __uint_as_float(__ldcg(a.sl_theta + q)) : FLT_MAX;
         if (!(ok = mbar_wait(&bar_t_full[slot], (bi / NSLOT) & 1, a.err))) break;
-        if (!(ok = mbar_wait(&bar_x_full[slot], (bi / NSLOT) & 1, a.err))) break;
+        if (!FOLD && !(ok = mbar_wait(&bar_x_full[slot], (bi / NSLOT) & 1, a.err))) break;
         if (arow < item.nq) thv = fminf(thv, v_threshold(th_now, dq));
         tc_fence_after();
         const float *xr = xs + slot * kBN;
         const uint32_t taddr = tmem + ((32u * ew) << 16) + (slot * MT + (MT == 2 ? grp : 0)) * ACC * kBN;
         const uint32_t p = (uint32_t)(item.p0 + (uint64_t)t * kBN);
+        // BF16 format: columns past the item's rows hold other rows' values
+        const uint32_t valid = min((uint32_t)kBN, item.np - t * kBN);
+        // v = -2 D <= thv  <=>  D >= -thv / 2 (rounded down: never misses a value)
+        const float tD = __fmul_rd(-0.5f, thv);
         // CW columns of the accumulator(s) per tensor-memory read (64 in the BF16
         // format, 32 with the split format's two accumulators): approx, filter,
         // candidates
@@ -553,22 +608,36 @@ __global__ void __launch_bounds__(kThreads, 1)
             tmem_ld64(taddr + c * CW, *reinterpret_cast<uint32_t(*)[64]>(r));
           }
           tmem_wait_ld();
-          // v in place of the accumulator values
-          float mn = INFINITY;
+          if (FOLD) {
+            if (valid < kBN) {
 #pragma unroll
-          for (uint32_t j4 = 0; j4 < CW / 4; j4++) {
-            const float4 x4 = *reinterpret_cast<const float4 *>(xr + c * CW + 4 * j4);
-            const float xw[4] = {x4.x, x4.y, x4.z, x4.w};
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-              float tv = fmaf(alpha, __uint_as_float(r[4 * j4 + e]), xw[e]);
-              if (SPLIT) tv = fmaf(alpha, __uint_as_float(r2[(4 * j4 + e) % (SPLIT ? 32 : 1)]), tv);
-              r[4 * j4 + e] = __float_as_uint(tv);
+              for (uint32_t j = 0; j < CW; j++)
+                if (c * CW + j >= valid) r[j] = 0xff800000u;  // -inf: v = +inf, never a candidate
             }
-            mn = fminf(mn, fminf(fminf(__uint_as_float(r[4 * j4]), __uint_as_float(r[4 * j4 + 1])),
-                                 fminf(__uint_as_float(r[4 * j4 + 2]), __uint_as_float(r[4 * j4 + 3]))));
+            float mx = -INFINITY;
+#pragma unroll
+            for (uint32_t j = 0; j < CW; j += 2) mx = fmax3(mx, __uint_as_float(r[j]), __uint_as_float(r[j + 1]));
+            if (!__any_sync(0xffffffffu, mx >= tD)) continue;
+#pragma unroll
+            for (uint32_t j = 0; j < CW; j++) r[j] = __float_as_uint(-2.f * __uint_as_float(r[j]));
+          } else {
+            // v in place of the accumulator values
+            float mn = INFINITY;
+#pragma unroll
+            for (uint32_t j4 = 0; j4 < CW / 4; j4++) {
+              const float4 x4 = *reinterpret_cast<const float4 *>(xr + c * CW + 4 * j4);
+              const float xw[4] = {x4.x, x4.y, x4.z, x4.w};
+#pragma unroll
+              for (int e = 0; e < 4; e++) {
+                float tv = fmaf(alpha, __uint_as_float(r[4 * j4 + e]), xw[e]);
+                if (SPLIT) tv = fmaf(alpha, __uint_as_float(r2[(4 * j4 + e) % (SPLIT ? 32 : 1)]), tv);
+                r[4 * j4 + e] = __float_as_uint(tv);
+              }
+              mn = fminf(mn, fminf(fminf(__uint_as_float(r[4 * j4]), __uint_as_float(r[4 * j4 + 1])),
+                                   fminf(__uint_as_float(r[4 * j4 + 2]), __uint_as_float(r[4 * j4 + 3]))));
+            }
+            if (!__any_sync(0xffffffffu, mn <= thv)) continue;
           }
-          if (!__any_sync(0xffffffffu, mn <= thv)) continue;
           // candidates, 32 columns at a time: the values go to a per-thread copy
           // (indexed by the candidate bits), then into the lane's buffer; full
           // buffers are merged by the warp, which tightens the filter, until
@@ -738,6 +807,27 @@ __global__ void tc_convert_kernel(const float *__restrict__ Xp, uint32_t ld, con
   if (lane == 0) w[p] = sxx + 2.f * scx;
 }
 
+// One thread per padded row: the w operand of the BF16 format's folded
+// product.  w is split into three BF16 pieces, w1 = bf16(w), w2 = bf16(w -
+// w1), w3 = bf16(w - w1 - w2) (both differences exact in FP32), so |w - w1 -
+// w2 - w3| <= 2^-24 |w|.  The 16-half row holds w1 w2 w3 0 0 0 0 0 twice; with
+// the constant tile's -1/4 at the same places the product is -(w1 + w2 + w3)
+// / 2, whichever order the two 8-half chunks take in the swizzled layout.
+__global__ void tc_wrows_kernel(const float *__restrict__ w, uint64_t n_pad, uint4 *__restrict__ Wh) {
+  const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (p >= n_pad) return;
+  const float v = w[p];
+  const __nv_bfloat16 b1 = __float2bfloat16_rn(v);
+  const float r1 = __fsub_rn(v, __bfloat162float(b1));
+  const __nv_bfloat16 b2 = __float2bfloat16_rn(r1);
+  const float r2 = __fsub_rn(r1, __bfloat162float(b2));
+  const __nv_bfloat16 b3 = __float2bfloat16_rn(r2);
+  const uint32_t lo = (uint32_t)__bfloat16_as_ushort(b1) | ((uint32_t)__bfloat16_as_ushort(b2) << 16);
+  const uint4 c = make_uint4(lo, (uint32_t)__bfloat16_as_ushort(b3), 0u, 0u);
+  Wh[2 * p] = c;
+  Wh[2 * p + 1] = c;
+}
+
 // One warp per query row (row m is the zero row): the operand row of q - mu,
 // its scale, ||q - mu|| and whether some value is not exact in BF16.
 __global__ void tc_query_kernel(const float *__restrict__ Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp,
@@ -904,12 +994,16 @@ template <int MT, bool SPLIT>
 size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs, uint32_t stage_words) {
   const size_t kbh = SPLIT ? 2 * kb : kb;
   const size_t nslot = 4 / (MT * (SPLIT ? 2 : 1));
-  return 1024 + (size_t)as * MT * kbh * kTile16K + (size_t)bs * kbh * kTile16K + nslot * kBN * 4 +
-         2 * 2 * kBM * sizeof(RowState) + (size_t)kEpiGroups * kBM * stage_words * 4;
+  const size_t b_stage = kbh * kTile16K + (SPLIT ? 0 : kWTile);
+  const size_t consts = SPLIT ? nslot * kBN * 4 : kWTile;  // row constants, or the w product's constant tile
+  const size_t states = 2 * 2 * kBM * (SPLIT ? sizeof(RowState) : sizeof(RowStateF));
+  return 1024 + (size_t)as * MT * kbh * kTile16K + (size_t)bs * b_stage + consts + states +
+         (size_t)kEpiGroups * kBM * stage_words * 4;
 }
 
 template <int MT, bool SPLIT>
-cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s) {
+cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUtensorMap &tmW, TcArgs a, int grid,
+                      cudaStream_t s) {
   // deepest pipeline that fits: B depth first (it hides the L2 latency of
   // every tile), then a second query stage (it hides the gather at item starts)
   // merge staging (2 SL + 1 words per epilogue thread) first: the lane-parallel
@@ -944,7 +1038,7 @@ cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, 
   cudaError_t e =
       cudaFuncSetAttribute(tc_search_kernel<MT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  tc_search_kernel<MT, SPLIT><<<grid, kThreads, smem, s>>>(tmA, tmB, a);
+  tc_search_kernel<MT, SPLIT><<<grid, kThreads, smem, s>>>(tmA, tmB, tmW, a);
   return launched();
 }
 
@@ -957,7 +1051,8 @@ uint32_t tc_kp(uint32_t d) { return (d + 63) / 64 * 64; }
 
 uint32_t tc_query_tile(uint32_t format) { return format == kTcSplit ? kBM : 2 * kBM; }
 
-cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32_t cols, uint32_t box_rows) {
+namespace {
+cudaError_t resolve_encode() {
   if (!g_encode) {
     cudaDriverEntryPointQueryResult qr;
     cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", (void **)&g_encode, 12000,
@@ -965,12 +1060,32 @@ cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32
     if (e != cudaSuccess) return e;
     if (qr != cudaDriverEntryPointSuccess || !g_encode) return cudaErrorNotSupported;
   }
+  return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32_t cols, uint32_t box_rows) {
+  cudaError_t e = resolve_encode();
+  if (e != cudaSuccess) return e;
   cuuint64_t dims[2] = {cols, rows};
   cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
   cuuint32_t box[2] = {64, box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(ptr), dims, strides, box, es,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+cudaError_t tc_make_map_w(CUtensorMap *map, const void *ptr, uint64_t rows) {
+  cudaError_t e = resolve_encode();
+  if (e != cudaSuccess) return e;
+  cuuint64_t dims[2] = {16, rows};
+  cuuint64_t strides[1] = {32};
+  cuuint32_t box[2] = {16, 128};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(ptr), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -1016,6 +1131,12 @@ int tc_build(const float *Xp, const uint32_t *perm, const uint64_t *offsets, con
   tc_convert_kernel<<<(unsigned)((n_pad * 32 + 255) / 256), 256, 0, s>>>(
       Xp, ld, offsets, nr, R, t.mu, n, n_pad, d, kp, t.format, t.lscale, static_cast<uint16_t *>(t.Xh), t.w);
   if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: operand rows");
+  if (t.format == kTcExact) {
+    if ((e = cudaMalloc(&t.Wh, n_pad * 32)) != cudaSuccess) return cuda_fail(e, "rbc_build: w operand rows");
+    *bytes += n_pad * 32;
+    tc_wrows_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(t.w, n_pad, static_cast<uint4 *>(t.Wh));
+    if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: w operand rows");
+  }
   return RBC_OK;
 }
 
@@ -1052,11 +1173,11 @@ int tc_grid() {
   return sms > 0 ? sms : 1;
 }
 
-cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
-                             cudaStream_t s, bool narrow) {
+cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUtensorMap &tmW,
+                             const TcArgs &a, int grid, cudaStream_t s, bool narrow) {
   if (a.kb < 1 || a.kb > 2) return cudaErrorInvalidValue;
-  if (a.format == kTcSplit) return launch_tc<1, true>(tmA, tmB, a, grid, s);
-  return narrow ? launch_tc<1, false>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
+  if (a.format == kTcSplit) return launch_tc<1, true>(tmA, tmB, tmW, a, grid, s);
+  return narrow ? launch_tc<1, false>(tmA, tmB, tmW, a, grid, s) : launch_tc<2, false>(tmA, tmB, tmW, a, grid, s);
 }
 
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s) {
