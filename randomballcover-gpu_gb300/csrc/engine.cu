@@ -224,8 +224,11 @@ int build_tc(rbc_index *idx, cudaStream_t s) {
   if (!tc_supported(idx->dp)) return fail(RBC_ERR_UNSUPPORTED, "rbc_build: the tensor-core form needs d <= 128");
   idx->kp = tc_kp(idx->d);
   idx->n_pad = (idx->n + 127) / 128 * 128;
-  TRY(tc_build(idx->Xp, idx->perm, idx->offsets, idx->R, idx->radius, idx->n, idx->n_pad, idx->nr, idx->d, idx->ld,
-               idx->kp, &idx->tc, &idx->device_bytes, s));
+  DevBuf rid;
+  CK(rid.alloc(idx->nr * 4ull, s));
+  CK(cudaMemcpyAsync(rid.p, idx->rep_ids.data(), idx->nr * 4ull, cudaMemcpyHostToDevice, s));
+  TRY(tc_build(idx->Xp, idx->perm, idx->offsets, idx->R, idx->radius, rid.as<uint32_t>(), idx->n, idx->n_pad,
+               idx->nr, idx->d, idx->ld, idx->kp, &idx->tc, &idx->device_bytes, s));
   CK(tc_make_map(&idx->tmB, idx->tc.Xh, idx->n_pad, idx->tc.cols, 128));
   if (idx->tc.Wh)
     CK(tc_make_map_w(&idx->tmW, idx->tc.Wh, idx->n_pad));
@@ -596,7 +599,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(b.ctl.alloc(64, s));
   CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
   DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
-      stats;
+      stats, seed_a, seed_row;
   if (routed) {
     CK(near.alloc(mb * Pn * 4, s));
     CK(near_d.alloc(mb * Pn * 4, s));
@@ -607,6 +610,8 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(qnorm.alloc((mb + 1) * 4, s));
   CK(qinex.alloc(mb + 1, s));
   CK(sl_a.alloc(2 * mb * sl * 4, s));
+  CK(seed_a.alloc(mb * sl * 4, s));
+  CK(seed_row.alloc(mb * sl * 4, s));
   CK(sl_row.alloc(2 * mb * sl * 4, s));
   CK(sl_sel.alloc(mb * 4, s));
   CK(sl_theta.alloc(mb * 4, s));
@@ -718,8 +723,11 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       idx->profile = prof;
       TRY(rc);
     }
-    CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, mq, sl, k, sl_a.as<float>(),
-                      sl_row.as<uint32_t>(), sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));
+    CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(), seed_row.as<uint32_t>(),
+                       s));
+    CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, seed_a.as<float>(),
+                      seed_row.as<uint32_t>(), mq, sl, k, sl_a.as<float>(), sl_row.as<uint32_t>(),
+                      sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));
     // probe round, large lists: tensor search into the seeded shortlists, one
     // 128-query tile per B tile (measured faster than two-tile items even for
     // the busiest probed lists), then the k-th exact distance of each
@@ -937,7 +945,7 @@ int rbc_build_host(const float *hX, uint64_t n, uint32_t d, uint32_t ldx, const 
 int rbc_destroy(rbc_index *idx) {
   if (!idx) return RBC_OK;
   void *ptrs[] = {idx->Xp,      idx->perm,   idx->offsets, idx->radius,     idx->R,  idx->os_lists, idx->os_counts,
-                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->tc.Xh, idx->tc.w,  idx->tc.Wh, idx->owner,
+                  idx->os_ids, idx->os_offsets, idx->Xo,   idx->Xi,        idx->tc.Xh, idx->tc.w,  idx->tc.Wh, idx->tc.rep_rows, idx->owner,
                   idx->tc.lscale, idx->tc.lxmax, idx->tc.lcnorm, idx->tc.mu, idx->tc.iperm, idx->X64, idx->norm64};
   for (void *p : ptrs)
     if (p) cudaFree(p);

@@ -151,11 +151,14 @@ struct TcBuild {
   float *lscale, *lxmax, *lcnorm;  // nr each
   float *mu;         // kp: the query centering vector (zero in the exact format)
   uint32_t *iperm;   // n: original id -> list-major row (shortlist rows are list-major)
+  uint32_t *rep_rows;  // nr: list-major row of each representative; w = +inf there, so the
+                       // tensor search never meets these rows (each query's shortlist
+                       // starts with its nearest representatives instead)
   uint32_t format, x_inexact, cols;
 };
 int tc_build(const float *Xp, const uint32_t *perm, const uint64_t *offsets, const float *R, const float *radius,
-             uint64_t n, uint64_t n_pad, uint32_t nr, uint32_t d, uint32_t ld, uint32_t kp, TcBuild *out,
-             uint64_t *bytes, cudaStream_t s);
+             const uint32_t *rep_ids, uint64_t n, uint64_t n_pad, uint32_t nr, uint32_t d, uint32_t ld, uint32_t kp,
+             TcBuild *out, uint64_t *bytes, cudaStream_t s);
 
 // Queries: half-precision operand rows (m rows + one zero row), scales, norms, flags.
 cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp, uint32_t format,
@@ -163,13 +166,20 @@ cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t 
                               cudaStream_t s);
 cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
                            uint32_t *emax, uint64_t m, uint32_t sl, cudaStream_t s);
+// Each query's sl nearest representatives under (Dqr, representative index),
+// as (exact distance, list-major row) pairs sorted by distance: the rows the
+// tensor search leaves out (w = +inf), which start every shortlist.
+cudaError_t launch_rep_seed(const float *Dqr, uint64_t m, uint32_t nr, const uint32_t *rep_rows, uint32_t sl,
+                            float *seed_a, uint32_t *seed_row, cudaStream_t s);
 // Seed the shortlists (after launch_sl_init) with each query's exact top-sl
 // over its probed lists (res_d / res_i: kw-wide lists of original ids, from
-// the FP32 search): rows become list-major through iperm, the shortlist
-// threshold becomes the sl-th distance and tau the k-th (float bits).
-cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *iperm, uint64_t m,
-                           uint32_t sl, uint32_t k, float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau,
-                           cudaStream_t s);
+// the FP32 search; rows become list-major through iperm) merged with its
+// nearest representatives (seed_a / seed_row, sl per query), each row once;
+// the shortlist threshold becomes the sl-th distance and tau the k-th (float
+// bits).
+cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *iperm,
+                           const float *seed_a, const uint32_t *seed_row, uint64_t m, uint32_t sl, uint32_t k,
+                           float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, cudaStream_t s);
 // narrow: one 128-query tile per B tile in the BF16 format as well (items
 // planned with query tiles of 128), for item sets whose tiles run sparse.
 // tmW: the w operand rows (BF16 format; unused by the split format).

@@ -20,7 +20,13 @@
 //          hi.hi into one tensor-memory accumulator, hi.lo + lo.hi into a
 //          second one, so the large accumulation runs over d terms only.
 // Each query keeps the SL = 40 rows of smallest approx (a shortlist of 4k for
-// k = 10).  The rerank computes their exact distances and sorts by
+// k = 10).  Every shortlist starts with the query's SL nearest
+// representatives (database rows whose exact distances Dqr the pruning already
+// has), merged with the exact probe results of the FP32 path; the
+// representatives' rows carry w = +inf, so the tensor search never meets them
+// again.  A representative outside the seed is no nearer than the seed's
+// largest distance, which bounds the shortlist's from above, so the
+// certificate below covers it like any other row left out.  The rerank computes their exact distances and sorts by
 // (distance, id).  |approx - exact| <= E(q) over every row searched, with E
 // from tc_error_bound; if the shortlist's largest approx minus E is above the
 // k-th exact distance, no other row can be in the top k, so the result equals
@@ -818,7 +824,8 @@ __global__ void tc_wrows_kernel(const float *__restrict__ w, uint64_t n_pad, uin
   if (p >= n_pad) return;
   const float v = w[p];
   const __nv_bfloat16 b1 = __float2bfloat16_rn(v);
-  const float r1 = __fsub_rn(v, __bfloat162float(b1));
+  // a representative's row (w = +inf): D = -inf, never a candidate
+  const float r1 = isinf(v) ? 0.f : __fsub_rn(v, __bfloat162float(b1));
   const __nv_bfloat16 b2 = __float2bfloat16_rn(r1);
   const float r2 = __fsub_rn(r1, __bfloat162float(b2));
   const __nv_bfloat16 b3 = __float2bfloat16_rn(r2);
@@ -900,20 +907,125 @@ __global__ void sl_init_kernel(float *sl_a, uint32_t *sl_row, uint32_t *sel, uin
 // left out ranks after the sl-th under (distance, id), hence after every
 // shortlist entry's value, which the certificate already covers.
 __global__ void sl_seed_kernel(const float *__restrict__ res_d, const uint32_t *__restrict__ res_i, uint32_t kw,
-                               const uint32_t *__restrict__ iperm, uint64_t m, uint32_t sl, uint32_t k,
+                               const uint32_t *__restrict__ iperm, const float *__restrict__ seed_a,
+                               const uint32_t *__restrict__ seed_row, uint64_t m, uint32_t sl, uint32_t k,
                                float *__restrict__ sl_a, uint32_t *__restrict__ sl_row, uint32_t *__restrict__ theta,
                                uint32_t *__restrict__ tau) {
   const uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (q >= m) return;
   const float *rd = res_d + q * kw;
   const uint32_t *ri = res_i + q * kw;
-  for (uint32_t j = 0; j < sl; j++) {
-    const uint32_t id = ri[j];
-    sl_a[q * sl + j] = id != RBC_DUMMY ? rd[j] : INFINITY;
-    sl_row[q * sl + j] = id != RBC_DUMMY ? iperm[id] : RBC_DUMMY;
+  const float *sa = seed_a + q * sl;
+  const uint32_t *sr = seed_row + q * sl;
+  float *oa = sl_a + q * sl;
+  uint32_t *orow = sl_row + q * sl;
+  // two sorted lists (by distance) merged; a row in both (a representative
+  // in a probed list) has the same exact distance in both and is kept once
+  uint32_t i = 0, j = 0, n = 0;
+  while (n < sl) {
+    const bool ha = i < sl && ri[i] != RBC_DUMMY, hb = j < sl && sr[j] != RBC_DUMMY;
+    if (!ha && !hb) break;
+    const float va = ha ? rd[i] : INFINITY, vb = hb ? sa[j] : INFINITY;
+    const bool take_a = ha && (!hb || va <= vb);
+    const float v = take_a ? va : vb;
+    const uint32_t r = take_a ? iperm[ri[i]] : sr[j];
+    if (take_a)
+      i++;
+    else
+      j++;
+    bool dup = false;
+    for (uint32_t t = n; t > 0 && oa[t - 1] == v && !dup; t--) dup = orow[t - 1] == r;
+    if (!dup) {
+      oa[n] = v;
+      orow[n] = r;
+      n++;
+    }
   }
-  theta[q] = __float_as_uint(ri[sl - 1] != RBC_DUMMY ? rd[sl - 1] : FLT_MAX);
-  tau[q] = fbits(rd[k - 1]);
+  for (uint32_t t = n; t < sl; t++) {
+    oa[t] = INFINITY;
+    orow[t] = RBC_DUMMY;
+  }
+  theta[q] = __float_as_uint(n == sl ? oa[sl - 1] : FLT_MAX);
+  tau[q] = fbits(n >= k ? oa[k - 1] : FLT_MAX);
+}
+
+// The representatives' list-major rows, and w = +inf there (the tensor
+// search leaves them to the shortlist seed).
+__global__ void rep_mask_kernel(const uint32_t *__restrict__ rep_ids, uint32_t nr, const uint32_t *__restrict__ iperm,
+                                float *__restrict__ w, uint32_t *__restrict__ rep_rows) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nr) return;
+  const uint32_t p = iperm[rep_ids[r]];
+  rep_rows[r] = p;
+  w[p] = INFINITY;
+}
+
+// One warp per query: its sl (<= 64) nearest representatives under (Dqr,
+// representative index).  Each lane keeps the 8 nearest of its own entries
+// (sorted, in registers); the lanes' lists then merge into a sorted 64-entry
+// warp list (entry 32 w + lane in register w).  That list is exact unless a
+// lane that dropped entries holds an 8th entry ahead of the list's last; such
+// queries (rare) redo the merge over every 32-wide chunk of Dqr.
+__global__ void rep_seed_kernel(const float *__restrict__ Dqr, uint64_t m, uint32_t nr,
+                                const uint32_t *__restrict__ rep_rows, uint32_t sl, float *__restrict__ seed_a,
+                                uint32_t *__restrict__ seed_row) {
+  constexpr int L = 8;
+  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (q >= m) return;
+  const float *row = Dqr + q * nr;
+  float pd[L];
+  uint32_t pi[L];
+#pragma unroll
+  for (int j = 0; j < L; j++) {
+    pd[j] = INFINITY;
+    pi[j] = RBC_DUMMY;
+  }
+  uint32_t seen = 0;
+  for (uint32_t r = lane; r < nr; r += 32, seen++) {
+    float cv = row[r];
+    uint32_t ci = r;
+    if (!pair_less(cv, ci, pd[L - 1], pi[L - 1])) continue;
+#pragma unroll
+    for (int j = 0; j < L; j++)
+      if (pair_less(cv, ci, pd[j], pi[j])) {
+        const float td = pd[j];
+        const uint32_t ti = pi[j];
+        pd[j] = cv;
+        pi[j] = ci;
+        cv = td;
+        ci = ti;
+      }
+  }
+  float ld[2] = {INFINITY, INFINITY};
+  uint32_t li[2] = {RBC_DUMMY, RBC_DUMMY};
+#pragma unroll
+  for (int j = 0; j < L; j++) warp_merge_into_w<2>(ld, li, pd[j], pi[j]);
+  const float wd = __shfl_sync(0xffffffffu, ld[1], 31);
+  const uint32_t wi = __shfl_sync(0xffffffffu, li[1], 31);
+  // a lane that saw more than L entries dropped only entries behind its L-th
+  const bool unsure = seen > (uint32_t)L && pair_less(pd[L - 1], pi[L - 1], wd, wi);
+  if (__any_sync(0xffffffffu, unsure)) {
+    ld[0] = ld[1] = INFINITY;
+    li[0] = li[1] = RBC_DUMMY;
+    for (uint32_t r0 = 0; r0 < nr; r0 += 32) {
+      const uint32_t r = r0 + lane;
+      const float v = r < nr ? row[r] : INFINITY;
+      const uint32_t id = r < nr ? r : RBC_DUMMY;
+      const float td = __shfl_sync(0xffffffffu, ld[1], 31);
+      const uint32_t ti = __shfl_sync(0xffffffffu, li[1], 31);
+      if (!__any_sync(0xffffffffu, pair_less(v, id, td, ti))) continue;
+      warp_merge_into_w<2>(ld, li, v, id);
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < 2; w++) {
+    const uint32_t j = 32 * w + lane;
+    if (j < sl) {
+      seed_a[q * sl + j] = li[w] != RBC_DUMMY ? ld[w] : INFINITY;
+      seed_row[q * sl + j] = li[w] != RBC_DUMMY ? rep_rows[li[w]] : RBC_DUMMY;
+    }
+  }
 }
 
 __global__ void iperm_kernel(const uint32_t *__restrict__ perm, uint64_t n, uint32_t *__restrict__ iperm) {
@@ -1091,8 +1203,8 @@ cudaError_t tc_make_map_w(CUtensorMap *map, const void *ptr, uint64_t rows) {
 }
 
 int tc_build(const float *Xp, const uint32_t *perm, const uint64_t *offsets, const float *R, const float *radius,
-             uint64_t n, uint64_t n_pad, uint32_t nr, uint32_t d, uint32_t ld, uint32_t kp, TcBuild *out,
-             uint64_t *bytes, cudaStream_t s) {
+             const uint32_t *rep_ids, uint64_t n, uint64_t n_pad, uint32_t nr, uint32_t d, uint32_t ld, uint32_t kp,
+             TcBuild *out, uint64_t *bytes, cudaStream_t s) {
   TcBuild &t = *out;
   DevBuf fl, lmax;
   cudaError_t e = fl.alloc(4, s);
@@ -1119,8 +1231,9 @@ int tc_build(const float *Xp, const uint32_t *perm, const uint64_t *offsets, con
   if (e == cudaSuccess) e = cudaMalloc(&t.lcnorm, nr * 4);
   if (e == cudaSuccess) e = cudaMalloc(&t.mu, kp * 4);
   if (e == cudaSuccess) e = cudaMalloc(&t.iperm, n * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&t.rep_rows, nr * 4);
   if (e != cudaSuccess) return cuda_fail(e, "rbc_build: tensor-form operands");
-  *bytes += xh_bytes + (n_pad + kBN) * 4 + 3ull * nr * 4 + kp * 4 + n * 4;
+  *bytes += xh_bytes + (n_pad + kBN) * 4 + 4ull * nr * 4 + kp * 4 + n * 4;
   iperm_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(perm, n, t.iperm);
   if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: row map");
   tc_mu_kernel<<<(kp + 127) / 128, 128, 0, s>>>(R, ld, nr, d, kp, t.format, t.mu);
@@ -1131,6 +1244,8 @@ int tc_build(const float *Xp, const uint32_t *perm, const uint64_t *offsets, con
   tc_convert_kernel<<<(unsigned)((n_pad * 32 + 255) / 256), 256, 0, s>>>(
       Xp, ld, offsets, nr, R, t.mu, n, n_pad, d, kp, t.format, t.lscale, static_cast<uint16_t *>(t.Xh), t.w);
   if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: operand rows");
+  rep_mask_kernel<<<(nr + 127) / 128, 128, 0, s>>>(rep_ids, nr, t.iperm, t.w, t.rep_rows);
+  if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: representative rows");
   if (t.format == kTcExact) {
     if ((e = cudaMalloc(&t.Wh, n_pad * 32)) != cudaSuccess) return cuda_fail(e, "rbc_build: w operand rows");
     *bytes += n_pad * 32;
@@ -1150,12 +1265,21 @@ cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t 
   return launched();
 }
 
-cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *iperm, uint64_t m,
-                           uint32_t sl, uint32_t k, float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau,
-                           cudaStream_t s) {
+cudaError_t launch_rep_seed(const float *Dqr, uint64_t m, uint32_t nr, const uint32_t *rep_rows, uint32_t sl,
+                            float *seed_a, uint32_t *seed_row, cudaStream_t s) {
   if (m == 0) return cudaSuccess;
-  sl_seed_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(res_d, res_i, kw, iperm, m, sl, k, sl_a, sl_row, theta,
-                                                            tau);
+  if (sl > 64) return cudaErrorInvalidValue;
+  const uint64_t threads = m * 32;
+  rep_seed_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(Dqr, m, nr, rep_rows, sl, seed_a, seed_row);
+  return launched();
+}
+
+cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *iperm,
+                           const float *seed_a, const uint32_t *seed_row, uint64_t m, uint32_t sl, uint32_t k,
+                           float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  sl_seed_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(res_d, res_i, kw, iperm, seed_a, seed_row, m, sl, k,
+                                                            sl_a, sl_row, theta, tau);
   return launched();
 }
 
