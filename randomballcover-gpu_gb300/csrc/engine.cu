@@ -638,8 +638,10 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     // 1. distances to the representatives, probe table
     CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
     CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
+    // the nearest representatives: the shortlist seed and, first, the probe table
     if (routed) {
-      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, Pn, near.as<uint32_t>(), near_d.as<float>(), s));
+      CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(),
+                         seed_row.as<uint32_t>(), Pn, near.as<uint32_t>(), near_d.as<float>(), s));
       Router &rt = idx->router->r;
       if (rt.tc_ok()) {
         CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
@@ -654,7 +656,8 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       CK(launch_router_probes(logits.as<float>(), mq, nr, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
                               b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     } else {
-      CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+      CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(),
+                         seed_row.as<uint32_t>(), P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     }
     CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(),
                            mq, kw, s));
@@ -723,8 +726,6 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       idx->profile = prof;
       TRY(rc);
     }
-    CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(), seed_row.as<uint32_t>(),
-                       s));
     CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, seed_a.as<float>(),
                       seed_row.as<uint32_t>(), mq, sl, k, sl_a.as<float>(), sl_row.as<uint32_t>(),
                       sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));

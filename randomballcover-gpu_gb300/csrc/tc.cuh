@@ -166,11 +166,14 @@ cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t 
                               cudaStream_t s);
 cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
                            uint32_t *emax, uint64_t m, uint32_t sl, cudaStream_t s);
-// Each query's sl nearest representatives under (Dqr, representative index),
-// as (exact distance, list-major row) pairs sorted by distance: the rows the
-// tensor search leaves out (w = +inf), which start every shortlist.
+// Each query's sl (<= 64) nearest representatives under (Dqr, representative
+// index), as (exact distance, list-major row) pairs sorted by distance: the
+// rows the tensor search leaves out (w = +inf), which start every shortlist.
+// The first P (<= 32) of them, as (representative, distance), go to
+// probe / probed, as the plain form's probe table would hold them.
 cudaError_t launch_rep_seed(const float *Dqr, uint64_t m, uint32_t nr, const uint32_t *rep_rows, uint32_t sl,
-                            float *seed_a, uint32_t *seed_row, cudaStream_t s);
+                            float *seed_a, uint32_t *seed_row, uint32_t P, uint32_t *probe, float *probed,
+                            cudaStream_t s);
 // Seed the shortlists (after launch_sl_init) with each query's exact top-sl
 // over its probed lists (res_d / res_i: kw-wide lists of original ids, from
 // the FP32 search; rows become list-major through iperm) merged with its

@@ -965,10 +965,13 @@ __global__ void rep_mask_kernel(const uint32_t *__restrict__ rep_ids, uint32_t n
 // (sorted, in registers); the lanes' lists then merge into a sorted 64-entry
 // warp list (entry 32 w + lane in register w).  That list is exact unless a
 // lane that dropped entries holds an 8th entry ahead of the list's last; such
-// queries (rare) redo the merge over every 32-wide chunk of Dqr.
+// queries (rare) redo the merge over every 32-wide chunk of Dqr.  The first P
+// entries are the query's probed lists (the same (distance, index) order as
+// the plain form's probe table).
 __global__ void rep_seed_kernel(const float *__restrict__ Dqr, uint64_t m, uint32_t nr,
                                 const uint32_t *__restrict__ rep_rows, uint32_t sl, float *__restrict__ seed_a,
-                                uint32_t *__restrict__ seed_row) {
+                                uint32_t *__restrict__ seed_row, uint32_t P, uint32_t *__restrict__ probe,
+                                float *__restrict__ probed) {
   constexpr int L = 8;
   const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint32_t lane = threadIdx.x & 31;
@@ -999,10 +1002,17 @@ __global__ void rep_seed_kernel(const float *__restrict__ Dqr, uint64_t m, uint3
   }
   float ld[2] = {INFINITY, INFINITY};
   uint32_t li[2] = {RBC_DUMMY, RBC_DUMMY};
+  // each lane's j-th entries in turn, while some lane still has one ahead of
+  // the list's last (the lanes' lists ascend)
+  float wd = INFINITY;
+  uint32_t wi = RBC_DUMMY;
 #pragma unroll
-  for (int j = 0; j < L; j++) warp_merge_into_w<2>(ld, li, pd[j], pi[j]);
-  const float wd = __shfl_sync(0xffffffffu, ld[1], 31);
-  const uint32_t wi = __shfl_sync(0xffffffffu, li[1], 31);
+  for (int j = 0; j < L; j++) {
+    if (!__any_sync(0xffffffffu, pair_less(pd[j], pi[j], wd, wi))) break;
+    warp_merge_into_w<2>(ld, li, pd[j], pi[j]);
+    wd = __shfl_sync(0xffffffffu, ld[1], 31);
+    wi = __shfl_sync(0xffffffffu, li[1], 31);
+  }
   // a lane that saw more than L entries dropped only entries behind its L-th
   const bool unsure = seen > (uint32_t)L && pair_less(pd[L - 1], pi[L - 1], wd, wi);
   if (__any_sync(0xffffffffu, unsure)) {
@@ -1025,6 +1035,10 @@ __global__ void rep_seed_kernel(const float *__restrict__ Dqr, uint64_t m, uint3
       seed_a[q * sl + j] = li[w] != RBC_DUMMY ? ld[w] : INFINITY;
       seed_row[q * sl + j] = li[w] != RBC_DUMMY ? rep_rows[li[w]] : RBC_DUMMY;
     }
+  }
+  if (lane < P) {  // P <= 32
+    probe[q * P + lane] = li[0];
+    probed[q * P + lane] = li[0] != RBC_DUMMY ? ld[0] : FLT_MAX;
   }
 }
 
@@ -1266,11 +1280,13 @@ cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t 
 }
 
 cudaError_t launch_rep_seed(const float *Dqr, uint64_t m, uint32_t nr, const uint32_t *rep_rows, uint32_t sl,
-                            float *seed_a, uint32_t *seed_row, cudaStream_t s) {
+                            float *seed_a, uint32_t *seed_row, uint32_t P, uint32_t *probe, float *probed,
+                            cudaStream_t s) {
   if (m == 0) return cudaSuccess;
-  if (sl > 64) return cudaErrorInvalidValue;
+  if (sl > 64 || P > 32) return cudaErrorInvalidValue;
   const uint64_t threads = m * 32;
-  rep_seed_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(Dqr, m, nr, rep_rows, sl, seed_a, seed_row);
+  rep_seed_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(Dqr, m, nr, rep_rows, sl, seed_a, seed_row, P,
+                                                                    probe, probed);
   return launched();
 }
 
