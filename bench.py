@@ -7,7 +7,9 @@ Workload (default, the configuration the headline metric is quoted on):
             float32), from the engine's counter-based generator, seed 3;
   queries   m = 10,000 rows from the same distribution (independent stream);
   search    exact 10-NN under squared L2, results sorted by (distance, id),
-            4,096 representatives.
+            1,024 representatives (measured on GB300 at 512 / 1,024 / 4,096:
+            239k / 245k / 211k queries/s for the headline form, about 7,100
+            for the plain form at each count).
 One step = one exact query call for all m queries with the index and the
 queries resident in HBM.  The 5.12 GB database is far larger than the 129 MB
 L2, so no flush is needed between steps.
@@ -60,7 +62,7 @@ WORKLOADS = {
                train=0, epochs=0, forms="oneshot,tensor,plain",
                metric="exact 32-NN queries/s, n=1,048,576 d=128 mixture, plain FP32 RBC",
                desc="1,000-component Gaussian mixture, sigma 0.05"),
-    "c3": dict(kind=2, seed=3, n=10_000_000, m=10_000, d=128, k=10, reps=4096, ncomp=1, slo=0.0, shi=0.0,
+    "c3": dict(kind=2, seed=3, n=10_000_000, m=10_000, d=128, k=10, reps=1024, ncomp=1, slo=0.0, shi=0.0,
                train=100_000, epochs=2, forms="plain,tensor,learned", metric=METRIC,
                desc="geometric(mean 20) integer features"),
     "c4": dict(kind=1, seed=4, instances=64, n_lo=10_000, n_hi=2_000_000, dims=(32, 64, 128), ks=(1, 10, 32),
@@ -92,6 +94,8 @@ def parse():
     ap.add_argument("--router-probes", type=int, default=1, help="lists the learned form adds from the router")
     ap.add_argument("--forms", default=None,
                     help="forms to time; the last one listed is the headline (default: per workload)")
+    ap.add_argument("--tc-tuning", default=None, metavar="PROBES,ROWS",
+                    help="fixed tensor-form knobs instead of timing them (profiling runs)")
     a = ap.parse_args()
     w = dict(WORKLOADS[a.workload])
     for key in ("n", "m", "reps", "train"):
@@ -378,7 +382,10 @@ def run_engine(a):
 
     def timed(mode, steps, warmup, sample_clocks=False):
         if mode & pyrbc.QUERY_EXACT_TC and k <= 32:
-            idx.autotune_tc(Qtune, k, mode)
+            if a.tc_tuning:
+                idx.set_tc_tuning(*(int(v) for v in a.tc_tuning.split(",")))
+            else:
+                idx.autotune_tc(Qtune, k, mode)
             tuning[mode] = idx.tc_tuning()
         for _ in range(warmup):
             idx.query(Q, k, mode=mode, out=(ids, dists))
