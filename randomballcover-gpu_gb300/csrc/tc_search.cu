@@ -73,7 +73,8 @@ using namespace sm100;
 
 constexpr int kBM = 128, kBN = 128, kEpiGroups = 2;
 constexpr int kThreads = 128 + 128 * kEpiGroups;
-constexpr int kLocal = 8;  // per-thread candidate buffer, in registers
+constexpr int kLocal = 8;  // per-thread candidate buffer, in registers (16 in the probe round's
+                           // BF16 instance, whose lists meet many more candidates)
 constexpr uint32_t kTile16K = 16384;           // 128 rows x 128 bytes (one 64-wide K block of halves)
 constexpr uint32_t kWTile = 4096;              // 128 rows x 32 bytes: the folded w operand of one B tile
 constexpr uint32_t kLockSpin = 1u << 22;
@@ -175,9 +176,10 @@ __device__ __forceinline__ float warp_publish(const TcArgs &a, uint32_t q, const
 
 // Sorted insertion of (av, row) into a lane's register buffer (ascending,
 // empty slots +inf); the caller guarantees a free slot.
-__device__ __forceinline__ void insert_local(float (&la)[kLocal], uint32_t (&li)[kLocal], float av, uint32_t row) {
+template <int LOC>
+__device__ __forceinline__ void insert_local(float (&la)[LOC], uint32_t (&li)[LOC], float av, uint32_t row) {
 #pragma unroll
-  for (int j = kLocal - 1; j > 0; j--) {
+  for (int j = LOC - 1; j > 0; j--) {
     const bool shift = row_less(av, row, la[j - 1], li[j - 1]);
     const bool here = !shift && row_less(av, row, la[j], li[j]);
     la[j] = shift ? la[j - 1] : (here ? av : la[j]);
@@ -194,8 +196,9 @@ __device__ __forceinline__ void insert_local(float (&la)[kLocal], uint32_t (&li)
 // the lane's shared-memory staging area with 16-byte loads (one round trip),
 // the candidates are inserted there, the result goes to the other buffer and
 // the buffers swap, under the query's lock.  Returns the new threshold.
-__device__ __forceinline__ float lane_merge(const TcArgs &a, uint32_t q, const float (&la)[kLocal],
-                                            const uint32_t (&li)[kLocal], uint32_t nl, float *stage) {
+template <int LOC>
+__device__ __forceinline__ float lane_merge(const TcArgs &a, uint32_t q, const float (&la)[LOC],
+                                            const uint32_t (&li)[LOC], uint32_t nl, float *stage) {
   uint32_t spins = 0;
   while (atomicCAS(a.sl_lock + q, 0u, 1u) != 0u) {
     if (++spins > kLockSpin) {
@@ -217,7 +220,7 @@ __device__ __forceinline__ float lane_merge(const TcArgs &a, uint32_t q, const f
     sr[4 * j] = vr.x; sr[4 * j + 1] = vr.y; sr[4 * j + 2] = vr.z; sr[4 * j + 3] = vr.w;
   }
 #pragma unroll
-  for (uint32_t e = 0; e < (uint32_t)kLocal; e++) {
+  for (uint32_t e = 0; e < (uint32_t)LOC; e++) {
     if (e >= nl) break;
     const float av = la[e];
     const uint32_t ar = li[e];
@@ -287,6 +290,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   // accumulator holds D = q.x' - w / 2 and v = -2 D needs no per-value work
   // in the epilogue.  The split format adds w in the epilogue instead.
   constexpr bool FOLD = !SPLIT;
+  constexpr int LOC = (MT == 1 && !SPLIT) ? 2 * kLocal : kLocal;  // candidate buffer entries per lane
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_a_full[kMaxA], bar_a_empty[kMaxA], bar_b_full[kMaxB], bar_b_empty[kMaxB],
       bar_t_full[4], bar_t_empty[4], bar_x_full[4], bar_r_full[2], bar_r_empty[2];
@@ -514,10 +518,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp >= 4) {
     // ------------------------------------------------ epilogue (two warpgroups)
     const uint32_t grp = (warp - 4) >> 2, ew = warp & 3, et = ew * 32 + lane;
-    float myla[kLocal];  // this lane's candidates, ascending (approx, row)
-    uint32_t myli[kLocal];
+    float myla[LOC];  // this lane's candidates, ascending (approx, row)
+    uint32_t myli[LOC];
 #pragma unroll
-    for (int j = 0; j < kLocal; j++) {
+    for (int j = 0; j < LOC; j++) {
       myla[j] = INFINITY;
       myli[j] = RBC_DUMMY;
     }
@@ -531,10 +535,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     auto flush = [&](uint32_t need, uint32_t q, uint32_t &nl, float &thv, float dq) {
       if (a.stage_words) {
         if ((need >> lane) & 1u) {
-          thv = v_threshold(lane_merge(a, q, myla, myli, nl, mystage), dq);
+          thv = v_threshold(lane_merge<LOC>(a, q, myla, myli, nl, mystage), dq);
           nl = 0;
 #pragma unroll
-          for (int j = 0; j < kLocal; j++) {
+          for (int j = 0; j < LOC; j++) {
             myla[j] = INFINITY;
             myli[j] = RBC_DUMMY;
           }
@@ -545,13 +549,26 @@ __global__ void __launch_bounds__(kThreads, 1)
       while (need) {
         const uint32_t l = __ffs(need) - 1;
         need &= need - 1;
-        const float th = warp_publish(a, __shfl_sync(0xffffffffu, q, l), myla, myli,
-                                      __shfl_sync(0xffffffffu, nl, l), l);
+        const uint32_t ql = __shfl_sync(0xffffffffu, q, l), nll = __shfl_sync(0xffffffffu, nl, l);
+        float th = 0.f;
+        // the warp network takes kLocal candidates at a time
+#pragma unroll
+        for (int h = 0; h < LOC / kLocal; h++) {
+          float ha[kLocal];
+          uint32_t hi[kLocal];
+#pragma unroll
+          for (int j = 0; j < kLocal; j++) {
+            ha[j] = myla[h * kLocal + j];
+            hi[j] = myli[h * kLocal + j];
+          }
+          const uint32_t nh = min(max((int)nll - h * kLocal, 0), kLocal);
+          if (h == 0 || nh > 0) th = warp_publish(a, ql, ha, hi, nh, l);
+        }
         if (lane == l) {
           nl = 0;
           thv = v_threshold(th, dq);
 #pragma unroll
-          for (int j = 0; j < kLocal; j++) {
+          for (int j = 0; j < LOC; j++) {
             myla[j] = INFINITY;
             myli[j] = RBC_DUMMY;
           }
@@ -659,11 +676,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             const uint32_t rbase = p + c * CW + 32 * h;
             while (__any_sync(0xffffffffu, pend != 0)) {
-              while (pend && nl < (uint32_t)kLocal) {
+              while (pend && nl < (uint32_t)LOC) {
                 const int e = __ffs(pend) - 1;
                 pend &= pend - 1;
                 if (vs[e] <= thv) {
-                  insert_local(myla, myli, dq + vs[e], rbase + e);
+                  insert_local<LOC>(myla, myli, dq + vs[e], rbase + e);
                   nl++;
                 }
               }
