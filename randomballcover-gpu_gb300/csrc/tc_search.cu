@@ -196,18 +196,29 @@ __device__ __forceinline__ void insert_local(float (&la)[LOC], uint32_t (&li)[LO
 // the lane's shared-memory staging area with 16-byte loads (one round trip),
 // the candidates are inserted there, the result goes to the other buffer and
 // the buffers swap, under the query's lock.  Returns the new threshold.
+// The lock is a plain mutex held by one thread: taking it with an acquire CAS
+// and releasing it with a release store orders the critical section's loads
+// and stores against every other holder's without separate fences.
+__device__ __forceinline__ uint32_t lock_cas_acquire(uint32_t *p) {
+  uint32_t old;
+  asm volatile("atom.acquire.gpu.global.cas.b32 %0, [%1], 0, 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+__device__ __forceinline__ void unlock_release(uint32_t *p) {
+  asm volatile("st.release.gpu.global.b32 [%0], 0;" ::"l"(p) : "memory");
+}
+
 template <int LOC>
 __device__ __forceinline__ float lane_merge(const TcArgs &a, uint32_t q, const float (&la)[LOC],
                                             const uint32_t (&li)[LOC], uint32_t nl, float *stage) {
   uint32_t spins = 0;
-  while (atomicCAS(a.sl_lock + q, 0u, 1u) != 0u) {
+  while (lock_cas_acquire(a.sl_lock + q) != 0u) {
     if (++spins > kLockSpin) {
       raise_error(a.err, RBC_ERR_ITER_LIMIT);
       return __uint_as_float(__ldcg(a.sl_theta + q));
     }
     __nanosleep(64);
   }
-  __threadfence();
   const uint32_t SL = a.sl, sel = __ldcg(a.sl_sel + q);
   const uint64_t cur = ((uint64_t)sel * a.m + q) * SL, nxt = ((uint64_t)(sel ^ 1u) * a.m + q) * SL;
   float *sa = stage;
@@ -240,11 +251,9 @@ __device__ __forceinline__ float lane_merge(const TcArgs &a, uint32_t q, const f
   }
   // FLT_MAX, not +inf, while the list is short
   const float theta = sr[SL - 1] != RBC_DUMMY ? sa[SL - 1] : FLT_MAX;
-  __threadfence();
   a.sl_theta[q] = __float_as_uint(theta);
   a.sl_sel[q] = sel ^ 1u;
-  __threadfence();
-  atomicExch(a.sl_lock + q, 0u);
+  unlock_release(a.sl_lock + q);  // after every store above
   return theta;
 }
 
