@@ -270,6 +270,22 @@ struct RowStateF {
 
 __device__ const float g_inf = INFINITY;
 
+// r[base + e] for a run-time e in [0, 32), with static register indices only:
+// five levels of selects on the bits of e.
+template <int N>
+__device__ __forceinline__ float select32(const uint32_t (&r)[N], int base, int e) {
+  float s[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) s[i] = __uint_as_float((e & 16) ? r[base + 16 + i] : r[base + i]);
+#pragma unroll
+  for (int i = 0; i < 8; i++) s[i] = (e & 8) ? s[i + 8] : s[i];
+#pragma unroll
+  for (int i = 0; i < 4; i++) s[i] = (e & 4) ? s[i + 4] : s[i];
+#pragma unroll
+  for (int i = 0; i < 2; i++) s[i] = (e & 2) ? s[i + 2] : s[i];
+  return (e & 1) ? s[1] : s[0];
+}
+
 // max(a, b, c) in one instruction (sm_100 and later)
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
   float r;
@@ -676,20 +692,20 @@ __global__ void __launch_bounds__(kThreads, 1)
           // none are left
 #pragma unroll
           for (uint32_t h = 0; h < CW / 32; h++) {
-            float vs[32];
             uint32_t pend = 0;
 #pragma unroll
-            for (int e = 0; e < 32; e++) {
-              vs[e] = __uint_as_float(r[32 * h + e]);
-              pend |= (uint32_t)(vs[e] <= thv) << e;
-            }
+            for (int e = 0; e < 32; e++) pend |= (uint32_t)(__uint_as_float(r[32 * h + e]) <= thv) << e;
             const uint32_t rbase = p + c * CW + 32 * h;
             while (__any_sync(0xffffffffu, pend != 0)) {
               while (pend && nl < (uint32_t)LOC) {
                 const int e = __ffs(pend) - 1;
                 pend &= pend - 1;
-                if (vs[e] <= thv) {
-                  insert_local<LOC>(myla, myli, dq + vs[e], rbase + e);
+                // the column's value by a select tree over the registers (an
+                // indexed array would live in local memory, whose traffic
+                // competes with the MMAs' shared-memory operand reads)
+                const float v = select32(r, 32 * h, e);
+                if (v <= thv) {
+                  insert_local<LOC>(myla, myli, dq + v, rbase + e);
                   nl++;
                 }
               }
