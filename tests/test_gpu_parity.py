@@ -335,3 +335,32 @@ def test_tensor_core_autotune(rbc, oracle):
     with pytest.raises(rbc.RBCError):
         idx.set_tc_tuning(9, 0)
     idx.close()
+
+
+@pytest.mark.parametrize("case", [
+    # n, d, nr, k, value range: the representatives seed every shortlist
+    (8000, 64, 32, 10, 255),    # fewer representatives (32) than shortlist rows (40)
+    (20000, 16, 64, 10, 3),     # values 0-2: many duplicate rows and tied distances
+    (12000, 32, 64, 32, 3),     # k = 32 (56-row shortlists), ties
+    (6000, 128, 500, 1, 255),   # 1-NN, more representatives than shortlist rows
+])
+def test_tensor_core_representative_seed(rbc, oracle, case):
+    """Each shortlist starts with the query's nearest representatives (exact
+    distances) and their rows are left out of the tensor search; results stay
+    the oracle's, ties and duplicate rows included, and equal the plain
+    form's on the same index."""
+    n, d, nr, k, vmax = case
+    rng = np.random.default_rng(n + d + nr)
+    Xn = rng.integers(0, vmax, size=(n, d)).astype(np.float32)
+    Qn = rng.integers(0, vmax, size=(257, d)).astype(np.float32)
+    import torch
+    X = torch.from_numpy(Xn).cuda()
+    Q = torch.from_numpy(Qn).cuda()
+    idx = rbc.Index(X, nr, seed=5, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    assert idx.info()["tc_format"] == rbc.TC_BF16
+    ids, dists = idx.query(Q, k, mode=rbc.QUERY_EXACT_TC)
+    ri, rd = oracle.knn(Xn, Qn, k)
+    assert_same(ids, dists, ri, rd, rbc)
+    ids2, dists2 = idx.query(Q, k)
+    assert (ids2 == ids).all() and (dists2 == dists).all()
+    idx.close()
