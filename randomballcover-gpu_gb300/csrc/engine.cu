@@ -230,10 +230,6 @@ int build_tc(rbc_index *idx, cudaStream_t s) {
   TRY(tc_build(idx->Xp, idx->perm, idx->offsets, idx->R, idx->radius, rid.as<uint32_t>(), idx->n, idx->n_pad,
                idx->nr, idx->d, idx->ld, idx->kp, &idx->tc, &idx->device_bytes, s));
   CK(tc_make_map(&idx->tmB, idx->tc.Xh, idx->n_pad, idx->tc.cols, 128));
-  if (idx->tc.Wh)
-    CK(tc_make_map_w(&idx->tmW, idx->tc.Wh, idx->n_pad));
-  else
-    idx->tmW = idx->tmB;  // the split format reads no w operand
   CK(cudaStreamSynchronize(s));
   return RBC_OK;
 }
@@ -678,6 +674,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     ta.zero_row = (uint32_t)mq;
     ta.d = idx->d;
     ta.w = idx->tc.w;
+    ta.wh = static_cast<const uint4 *>(idx->tc.Wh);
     ta.lscale = idx->tc.lscale;
     ta.lxmax = idx->tc.lxmax;
     ta.lcnorm = idx->tc.lcnorm;
@@ -739,7 +736,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
                           -1, tc_query_tile(kTcSplit), large));
       if (idx->profile) CK(cudaEventRecord(idx->ev_pool[2], s));
-      CK(launch_tc_search(tmA, idx->tmB, idx->tmW, ta, grid, s, true));
+      CK(launch_tc_search(tmA, idx->tmB, ta, grid, s, true));
       if (idx->profile) {
         CK(cudaEventRecord(idx->ev_pool[3], s));
         tc_probe = true;
@@ -754,7 +751,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     TRY(plan_and_search(idx, b, mq, P, k, 1, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
                         -1, qtile));
     if (idx->profile) CK(cudaEventRecord(idx->ev_pool[0], s));
-    CK(launch_tc_search(tmA, idx->tmB, idx->tmW, ta, grid, s));
+    CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
     if (idx->profile) CK(cudaEventRecord(idx->ev_pool[1], s));
     ra.tau = nullptr;
     ra.ids = dIds ? dIds + b0 * ldo : nullptr;

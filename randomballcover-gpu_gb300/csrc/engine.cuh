@@ -108,7 +108,6 @@ struct rbc_index {
   uint64_t n_pad = 0;
   uint32_t kp = 0;
   CUtensorMap tmB;                // TMA map of tc.Xh (128-row boxes, 128-byte swizzle)
-  CUtensorMap tmW;                // BF16 format: TMA map of tc.Wh (128-row boxes, 32-byte swizzle)
   // double-precision variant (rbc_build_f64, flag RBC_BUILD_F64): the double
   // rows in original order (stride ld64) and their largest L2 / L1 norms
   double *X64 = nullptr;

@@ -41,6 +41,7 @@ struct TcArgs {
   uint32_t zero_row;        // an all-zero row of the query operand (gathered for empty slots)
   uint32_t d;
   const float *w;           // per database row: ||x'||^2 + 2 c.x' (x' = x - c, c its representative)
+  const uint4 *wh;          // BF16 format: per row the w pieces, 32 bytes (TcBuild::Wh)
   const float *lscale;      // per list: power-of-two scale of the stored halves
   const float *lxmax;       // per list: bound on ||x'||
   const float *lcnorm;      // per list: ||c - mu||
@@ -139,14 +140,12 @@ uint32_t tc_kp(uint32_t d);
 int tc_grid();
 uint32_t tc_query_tile(uint32_t format);  // queries per work item (128 x tiles per CTA)
 cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32_t cols, uint32_t box_rows);
-// TMA map of the BF16 format's w operand rows (16 halves, 128-row boxes, 32-byte swizzle)
-cudaError_t tc_make_map_w(CUtensorMap *map, const void *ptr, uint64_t rows);
 
 // Build: centered rows of each list (x' = x - c_r), the format check, per-list
 // scales and bounds, the half-precision operand rows and w.
 struct TcBuild {
   void *Xh;          // n_pad x cols halves (cols = kp, or 2 kp for the split format)
-  void *Wh;          // BF16 format: n_pad x 16 halves, the w operand of the folded product
+  void *Wh;          // BF16 format: (n_pad + 128) x 16 halves, the w operand of the folded product
   float *w;          // n_pad + 128
   float *lscale, *lxmax, *lcnorm;  // nr each
   float *mu;         // kp: the query centering vector (zero in the exact format)
@@ -185,9 +184,8 @@ cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t k
                            float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, cudaStream_t s);
 // narrow: one 128-query tile per B tile in the BF16 format as well (items
 // planned with query tiles of 128), for item sets whose tiles run sparse.
-// tmW: the w operand rows (BF16 format; unused by the split format).
-cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUtensorMap &tmW,
-                             const TcArgs &a, int grid, cudaStream_t s, bool narrow = false);
+cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
+                             cudaStream_t s, bool narrow = false);
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s);
 
 }  // namespace rbc

@@ -306,11 +306,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 template <int MT, bool SPLIT>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                     const __grid_constant__ CUtensorMap tmW, const __grid_constant__ TcArgs a) {
+                     const __grid_constant__ TcArgs a) {
   constexpr uint32_t ACC = SPLIT ? 2 : 1;     // accumulators per query tile: hi.hi (+ corrections)
   constexpr uint32_t NSLOT = 4 / (MT * ACC);  // tensor-memory slots of MT x ACC x 128 columns
   // BF16 format: w is folded into the product.  Each B stage carries the
-  // tile's w operand (three BF16 pieces per row, by TMA from tmW) and one
+  // tile's w operand (three BF16 pieces per row: the tile's 128 rows of a.wh
+  // are one contiguous 4 KB block, brought by one bulk copy) and one
   // more MMA per accumulator multiplies it by a constant -1/4 tile, so the
   // accumulator holds D = q.x' - w / 2 and v = -2 D needs no per-value work
   // in the epilogue.  The split format adds w in the epilogue instead.
@@ -382,7 +383,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ------------------------------------------------ TMA producer of the B tiles
     if (lane == 0) {
       prefetch_tensormap(&tmB);
-      if (FOLD) prefetch_tensormap(&tmW);
       uint32_t bi = 0;
       unsigned long long pairs = 0, lists = 0;
       bool ok = true;
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int32_t row = (int32_t)(item.p0 + (uint64_t)t * kBN);
           for (uint32_t k = 0; k < kbh; k++)
             tma_load_2d(sB + sb * b_stage + k * kTile16K, &tmB, (int32_t)(k * 64), row, &bar_b_full[sb]);
-          if (FOLD) tma_load_2d(sB + sb * b_stage + b_bytes, &tmW, 0, row, &bar_b_full[sb]);
+          if (FOLD) bulk_load(sB + sb * b_stage + b_bytes, a.wh + 2 * (uint64_t)row, kWTile, &bar_b_full[sb]);
         }
       }
       // drain: wait (bounded) for the copies still in flight before leaving
@@ -1170,8 +1170,7 @@ size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs, uint32_t stage_words) {
 }
 
 template <int MT, bool SPLIT>
-cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUtensorMap &tmW, TcArgs a, int grid,
-                      cudaStream_t s) {
+cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s) {
   // deepest pipeline that fits: B depth first (it hides the L2 latency of
   // every tile), then a second query stage (it hides the gather at item starts)
   // merge staging (2 SL + 1 words per epilogue thread) first: the lane-parallel
@@ -1206,7 +1205,7 @@ cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUte
   cudaError_t e =
       cudaFuncSetAttribute(tc_search_kernel<MT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  tc_search_kernel<MT, SPLIT><<<grid, kThreads, smem, s>>>(tmA, tmB, tmW, a);
+  tc_search_kernel<MT, SPLIT><<<grid, kThreads, smem, s>>>(tmA, tmB, a);
   return launched();
 }
 
@@ -1241,19 +1240,6 @@ cudaError_t tc_make_map(CUtensorMap *map, const void *ptr, uint64_t rows, uint32
   cuuint32_t es[2] = {1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(ptr), dims, strides, box, es,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
-}
-
-cudaError_t tc_make_map_w(CUtensorMap *map, const void *ptr, uint64_t rows) {
-  cudaError_t e = resolve_encode();
-  if (e != cudaSuccess) return e;
-  cuuint64_t dims[2] = {16, rows};
-  cuuint64_t strides[1] = {32};
-  cuuint32_t box[2] = {16, 128};
-  cuuint32_t es[2] = {1, 1};
-  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(ptr), dims, strides, box, es,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
@@ -1303,9 +1289,10 @@ int tc_build(const float *Xp, const uint32_t *perm, const uint64_t *offsets, con
   rep_mask_kernel<<<(nr + 127) / 128, 128, 0, s>>>(rep_ids, nr, t.iperm, t.w, t.rep_rows);
   if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: representative rows");
   if (t.format == kTcExact) {
-    if ((e = cudaMalloc(&t.Wh, n_pad * 32)) != cudaSuccess) return cuda_fail(e, "rbc_build: w operand rows");
-    *bytes += n_pad * 32;
-    tc_wrows_kernel<<<(unsigned)((n_pad + 255) / 256), 256, 0, s>>>(t.w, n_pad, static_cast<uint4 *>(t.Wh));
+    // a tile's 128 rows are read whole: kBN rows of padding past n_pad
+    if ((e = cudaMalloc(&t.Wh, (n_pad + kBN) * 32)) != cudaSuccess) return cuda_fail(e, "rbc_build: w operand rows");
+    *bytes += (n_pad + kBN) * 32;
+    tc_wrows_kernel<<<(unsigned)((n_pad + kBN + 255) / 256), 256, 0, s>>>(t.w, n_pad + kBN, static_cast<uint4 *>(t.Wh));
     if ((e = launched()) != cudaSuccess) return cuda_fail(e, "rbc_build: w operand rows");
   }
   return RBC_OK;
@@ -1355,11 +1342,12 @@ int tc_grid() {
   return sms > 0 ? sms : 1;
 }
 
-cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUtensorMap &tmW,
-                             const TcArgs &a, int grid, cudaStream_t s, bool narrow) {
+cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
+                             cudaStream_t s, bool narrow) {
   if (a.kb < 1 || a.kb > 2) return cudaErrorInvalidValue;
-  if (a.format == kTcSplit) return launch_tc<1, true>(tmA, tmB, tmW, a, grid, s);
-  return narrow ? launch_tc<1, false>(tmA, tmB, tmW, a, grid, s) : launch_tc<2, false>(tmA, tmB, tmW, a, grid, s);
+  if (a.format == kTcSplit) return launch_tc<1, true>(tmA, tmB, a, grid, s);
+  if (!a.wh) return cudaErrorInvalidValue;
+  return narrow ? launch_tc<1, false>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
 }
 
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s) {
