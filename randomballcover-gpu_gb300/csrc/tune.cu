@@ -164,7 +164,7 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   uint32_t best_p = 0;
   uint64_t best_rows = 0;
   int rc = RBC_OK;
-  for (uint32_t p : {2u, 4u, 8u}) {
+  for (uint32_t p : {1u, 2u, 4u, 8u}) {
     for (uint64_t r : {2048ull, 8192ull, 32768ull}) {
       idx->tc_probes = p;
       idx->tc_probe_rows = r;
