@@ -19,37 +19,46 @@
 //          identity then carries w = ||x'||^2 + 2 (c - mu).x'), three products:
 //          hi.hi into one tensor-memory accumulator, hi.lo + lo.hi into a
 //          second one, so the large accumulation runs over d terms only.
-// Each query keeps the SL = 40 rows of smallest approx (a shortlist of 4k for
-// k = 10).  Every shortlist starts with the query's SL nearest
-// representatives (database rows whose exact distances Dqr the pruning already
-// has), merged with the exact probe results of the FP32 path; the
-// representatives' rows carry w = +inf, so the tensor search never meets them
-// again.  A representative outside the seed is no nearer than the seed's
-// largest distance, which bounds the shortlist's from above, so the
-// certificate below covers it like any other row left out.  The rerank computes their exact distances and sorts by
-// (distance, id).  |approx - exact| <= E(q) over every row searched, with E
+// In the exact format w is folded into the product: three BF16 pieces of w
+// per row ride with each B tile and one more MMA step against a constant
+// -1/4 tile leaves D = q.x' - w/2 in tensor memory, so v = -2 D needs no
+// per-value arithmetic.
+//
+// Each query keeps the SL = 4k rows (40 to 56) of smallest approx.  Every
+// shortlist starts with the query's SL nearest representatives (database rows
+// whose exact distances Dqr the pruning already has), merged with the exact
+// probe results of the FP32 path; the representatives' rows carry w = +inf,
+// so the tensor search never meets them again.  A representative outside the
+// seed is no nearer than the seed's largest distance, which bounds the
+// shortlist's from above, so the certificate below covers it like any other
+// row left out.  The rerank computes the shortlist's exact distances and sorts
+// by (distance, id).  |approx - exact| <= E(q) over every row searched, with E
 // from tc_error_bound; if the shortlist's largest approx minus E is above the
 // k-th exact distance, no other row can be in the top k, so the result equals
 // the FP32 oracle's; otherwise the query is recomputed by the plain FP32 path.
 //
 // Work items are the planner's list-major items: rows [p0, p0 + np) of one
-// list against up to 128 MT queries (MT = 2 in the exact format, 1 in split).
+// list against up to 128 MT queries (MT = 2 in the exact format's pruned
+// round; 1 in its probe round and in the split format).
 // Kernel structure (one persistent CTA per SM, 384 threads):
-//   warp 0      TMA producer: the item's query rows gathered from the half-
-//               precision query matrix with tile::gather4 (128-byte swizzled,
-//               K-major), then 128-row B tiles of the item into a ring;
+//   warp 0      TMA producer: 128-row B tiles of each item into a ring (with
+//               the tile's w pieces, one bulk copy, in the exact format);
 //   warp 1      tcgen05.mma issuer: per B tile MT x ACC accumulators of
 //               128 x 128 in tensor memory (512 columns hold 4 / (MT ACC)
 //               slots), commits free the B stage and hand the slot to the
 //               epilogue;
-//   warp 2      stages each B tile's row constants w into shared memory
-//               (cp.async; +inf past the item's rows, which masks them);
+//   warp 2      split format: stages each B tile's row constants w into
+//               shared memory (cp.async; +inf past the item's rows);
+//   warp 3      per item: gathers the query rows with tile::gather4 (128-byte
+//               swizzled, K-major) and stages each row's query, Dqr and error
+//               bound;
 //   warps 4-11  epilogue, two warpgroups (MT = 2: one per query tile; MT = 1:
-//               alternate B tiles): tcgen05.ld of its query row, one FMA per
-//               value, a running minimum per 32 columns against the query's
-//               threshold, candidates into a small per-thread buffer that is
-//               merged into the query's global shortlist (double-buffered,
-//               bounded per-query lock) when full and at the end of the item.
+//               alternate B tiles): tcgen05.ld of its query row, a 3-input max
+//               per pair of columns against the query's threshold (the split
+//               format forms approx with FMAs), candidates into a small
+//               per-thread buffer that is merged into the query's global
+//               shortlist (double-buffered, bounded per-query lock) when full
+//               and at the end of the item.
 // All mbarrier waits are bounded (sm100.cuh); a timeout sets the error word.
 #include <cuda.h>
 #include <cudaTypedefs.h>
