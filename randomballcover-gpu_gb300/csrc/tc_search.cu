@@ -495,32 +495,50 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
       const SearchItem item = a.items[it];
       const uint32_t slot = ai & 1, sa = ai % AS;
+      // the item's row states are read from global memory before the staging
+      // slot frees (their latency hides behind that wait), then written
+      // lane l owns rows 4l..4l+3 of each query tile (one gather4 per tile and K block)
+      int32_t rr[MT][4];
+      float dqv[MT][4], qnv[MT][4];
+      uint32_t qin[MT][4];
+#pragma unroll
+      for (int g = 0; g < MT; g++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const uint32_t row = g * kBM + 4 * lane + j;
+          rr[g][j] = row < item.nq ? (int32_t)a.qidx[item.q0 + row] : (int32_t)a.zero_row;
+        }
+#pragma unroll
+      for (int g = 0; g < MT; g++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const uint32_t row = g * kBM + 4 * lane + j, q = (uint32_t)rr[g][j];
+          const bool v = row < item.nq;
+          dqv[g][j] = v ? a.Dqr[(uint64_t)q * a.nr + item.list] : 0.f;
+          qnv[g][j] = v ? a.qnorm[q] : 0.f;
+          qin[g][j] = v ? (a.q_inexact ? a.q_inexact[q] : 1u) : 0u;
+        }
+      const float X = a.lxmax[item.list], C = a.lcnorm[item.list];
       if (ai >= 2) ok = mbar_wait(&bar_r_empty[slot], ((ai >> 1) - 1) & 1, a.err);
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
-      // lane l owns rows 4l..4l+3 of each query tile (one gather4 per tile and K block)
-      int32_t rr[MT][4];
       RowState *dst = rs + slot * 2 * kBM;
       RowStateF *dstf = rsf + slot * 2 * kBM;
       const float ls = SPLIT ? a.lscale[item.list] : 1.f;
-      const float X = a.lxmax[item.list], C = a.lcnorm[item.list];
 #pragma unroll
       for (int g = 0; g < MT; g++)
 #pragma unroll
         for (int j = 0; j < 4; j++) {
           const uint32_t row = g * kBM + 4 * lane + j;
           RowState st{0u, 0.f, -FLT_MAX, -2.f};  // rows past the item's queries: no value passes
-          rr[g][j] = (int32_t)a.zero_row;
           if (row < item.nq) {
-            const uint32_t q = a.qidx[item.q0 + row];
-            const float dq = a.Dqr[(uint64_t)q * a.nr + item.list];
-            rr[g][j] = (int32_t)q;
+            const uint32_t q = (uint32_t)rr[g][j];
+            const float dq = dqv[g][j];
             st.q = q;
             st.dq = dq;
             if (!FOLD) st.thv = v_threshold(__uint_as_float(__ldcg(a.sl_theta + q)), dq);
             if (SPLIT) st.alpha = -2.f / (a.qscale[q] * ls);
-            const float E = tc_error_bound(dq, a.qnorm[q], X, C, a.q_inexact ? a.q_inexact[q] : 1u, a.x_inexact,
-                                           a.format, a.d);
+            const float E = tc_error_bound(dq, qnv[g][j], X, C, qin[g][j], a.x_inexact, a.format, a.d);
             atomicMax(a.emax + q, __float_as_uint(E));
           }
           if (FOLD)
