@@ -683,6 +683,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             tmem_ld64(taddr + c * CW, *reinterpret_cast<uint32_t(*)[64]>(r));
           }
           tmem_wait_ld();
+          if (c == kBN / CW - 1) {
+            // the tile's last accumulator read is in registers: the slot goes
+            // back to the MMA warp before this chunk's candidates (and any
+            // shortlist merge) are handled
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_t_empty[slot]);
+          }
           if (FOLD) {
             if (valid < kBN) {
 #pragma unroll
@@ -740,9 +748,6 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&bar_t_empty[slot]);
       }
       flush(__ballot_sync(0xffffffffu, nl > 0), q, nl, thv, dq);
       __syncwarp();
