@@ -46,10 +46,11 @@ namespace {
 
 constexpr uint32_t kDefaultProbes = 1;  // lists searched before planning (the one-shot plan)
 constexpr uint32_t kTcProbes = 4;       // the tensor form: a tighter start for its shortlists
-// The tensor form's probe round searches lists of fewer rows than this on the
-// FP32 path (few queries share a probed list; small tensor items are
-// dominated by fixed costs and shortlist merges) and larger ones on the
-// tensor cores.  RBC_TC_PROBE_ROWS overrides it.
+// The tensor form's probe round searches the first this many rows of every
+// probed list on the FP32 path (whole lists when shorter: few queries share a
+// probed list, and small tensor items are dominated by fixed costs and
+// shortlist merges) and the rest of longer lists on the tensor cores, into
+// shortlists those exact rows already hold.  RBC_TC_PROBE_ROWS overrides it.
 constexpr uint64_t kTcProbeRows = 8192;
 
 void pool_setup() {
@@ -716,8 +717,10 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     {
       const bool prof = idx->profile;
       idx->profile = false;
+      // the first probe_rows rows of every probed list (whole lists when
+      // shorter): exact seeds that give the tensor round a tight threshold
       ListFilter small;
-      small.rows_hi = probe_rows;
+      small.take = probe_rows;
       const int rc = plan_and_search(idx, b, mq, P, sl, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, pgrid,
                                      nullptr, s, 2, ptq, 0, small);
       idx->profile = prof;
@@ -730,9 +733,10 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     // 128-query tile per B tile (measured faster than two-tile items even for
     // the busiest probed lists), then the k-th exact distance of each
     // shortlist tightens the threshold
-    if (idx->max_list >= probe_rows) {
-      ListFilter large;
-      large.rows_lo = probe_rows;
+    if (idx->max_list > probe_rows) {
+      ListFilter large;  // the rest of the longer lists
+      large.rows_lo = probe_rows + 1;
+      large.skip = probe_rows;
       TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
                           -1, tc_query_tile(kTcSplit), large));
       if (idx->profile) CK(cudaEventRecord(idx->ev_pool[2], s));

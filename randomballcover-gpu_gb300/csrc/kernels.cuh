@@ -148,9 +148,12 @@ struct PlanArgs {
 cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s);
 // Which lists of a plan get work items: rows_lo <= rows < rows_hi and
 // cnt_lo <= planned queries < cnt_hi.
+// Of each selected list, only rows [skip, skip + take) (list-relative) get
+// items; a list with no rows there gets none.
 struct ListFilter {
   uint64_t rows_lo = 0, rows_hi = UINT64_MAX;
   uint32_t cnt_lo = 0, cnt_hi = UINT32_MAX;
+  uint64_t skip = 0, take = UINT64_MAX;
 };
 // Items per list: query tiles x chunks of at most max_rows list rows, for
 // the lists the filter selects only.

@@ -186,19 +186,30 @@ __global__ void plan_probe_kernel(PlanArgs a) {
   }
 }
 
-// Work items per list: query tiles x row chunks of at most max_rows rows
-// (long lists are cut so one item cannot hold up the whole launch).
-__device__ __forceinline__ uint32_t row_chunks(const uint64_t *offsets, uint32_t r, uint32_t max_rows) {
+// The rows of list r the filter's window keeps: [lo, lo + n) list-relative.
+__device__ __forceinline__ void row_window(const uint64_t *offsets, uint32_t r, const ListFilter &f, uint64_t &lo,
+                                           uint64_t &n) {
   const uint64_t np = offsets[r + 1] - offsets[r];
-  return np == 0 ? 1u : (uint32_t)((np + max_rows - 1) / max_rows);
+  lo = min(f.skip, np);
+  n = min(np - lo, f.take);
 }
 
-// Lists the filter leaves out get no items.
+// Work items per list: query tiles x row chunks of at most max_rows rows
+// (long lists are cut so one item cannot hold up the whole launch).
+__device__ __forceinline__ uint32_t row_chunks(const uint64_t *offsets, uint32_t r, uint32_t max_rows,
+                                               const ListFilter &f) {
+  uint64_t lo, n;
+  row_window(offsets, r, f, lo, n);
+  return n == 0 ? 1u : (uint32_t)((n + max_rows - 1) / max_rows);
+}
+
+// Lists the filter leaves out get no items (nor do lists whose window is
+// empty when the window skips rows).
 __device__ __forceinline__ bool list_selected(const uint64_t *offsets, const uint32_t *list_cnt, uint32_t r,
                                               const ListFilter &f) {
   const uint64_t np = offsets[r + 1] - offsets[r];
   const uint32_t c = list_cnt[r];
-  return np >= f.rows_lo && np < f.rows_hi && c >= f.cnt_lo && c < f.cnt_hi;
+  return np >= f.rows_lo && np < f.rows_hi && c >= f.cnt_lo && c < f.cnt_hi && (f.skip == 0 || np > f.skip);
 }
 
 __global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, const uint64_t *__restrict__ offsets,
@@ -207,7 +218,7 @@ __global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, con
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < nr)
     tile_cnt[r] = list_selected(offsets, list_cnt, r, f)
-                      ? (list_cnt[r] + qtile - 1) / qtile * row_chunks(offsets, r, max_rows)
+                      ? (list_cnt[r] + qtile - 1) / qtile * row_chunks(offsets, r, max_rows, f)
                       : 0;
   if (r == nr) tile_cnt[nr] = 0;
 }
@@ -229,8 +240,10 @@ __global__ void plan_items_kernel(const uint32_t *__restrict__ list_cnt, const u
   }
   if (total > cap || r >= nr || !list_selected(offsets, list_cnt, r, f)) return;
   const uint32_t cnt = list_cnt[r];
-  const uint32_t nt = (cnt + qtile - 1) / qtile, nc = row_chunks(offsets, r, max_rows);
-  const uint64_t p0 = offsets[r], np = offsets[r + 1] - offsets[r];
+  const uint32_t nt = (cnt + qtile - 1) / qtile, nc = row_chunks(offsets, r, max_rows, f);
+  uint64_t lo, np;
+  row_window(offsets, r, f, lo, np);
+  const uint64_t p0 = offsets[r] + lo;
   uint32_t slot = tile_start[r];
   for (uint32_t c = 0; c < nc; c++) {
     for (uint32_t t = 0; t < nt; t++) {
