@@ -172,8 +172,9 @@ int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, ui
 /* Tuning of the tensor-core form: nearest lists searched in its probe round
  * (1-8; 0 keeps the default, 4) and how many rows of each probed list the
  * FP32 path searches first (whole lists when shorter; the rest of a longer
- * list goes to the tensor cores; 0 keeps the default, 8192).  rbc_autotune_tc times 1, 2, 4, 8 probes x 2048, 8192, 32768 rows on
- * sample queries in the given mode (RBC_QUERY_EXACT_TC, optionally
+ * list goes to the tensor cores; 0 keeps the default, 8192).
+ * rbc_autotune_tc times 1, 2, 4, 8 probes x 2048, 8192, 32768 rows on sample
+ * queries in the given mode (RBC_QUERY_EXACT_TC, optionally
  * | RBC_QUERY_ROUTED) and keeps the fastest.  Results never change. */
 int rbc_set_tc_tuning(rbc_index *index, uint32_t probes, uint64_t probe_rows);
 int rbc_get_tc_tuning(const rbc_index *index, uint32_t *probes, uint64_t *probe_rows);
