@@ -245,7 +245,9 @@ def host_matrix(w, stream, rows, threads):
 def cpu_knn_timed(X, Qs, k, threads):
     """Time the reference's CPU path on Qs: its own bruteCPU (1-NN, compiled from
     the reference sources) when that build is present, else the oracle's
-    restatement of the same distance loop with (dist, id) k-NN selection."""
+    restatement of the same distance loop with (dist, id) k-NN selection.
+    Returns (seconds, kind, description, answer); answer is (ids, dists) of
+    the k-NN, or (1-NN ids as one column, None) from bruteCPU."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     if oracle.ref_available():
@@ -265,10 +267,54 @@ def cpu_knn_timed(X, Qs, k, threads):
             t.start()
         for t in ths:
             t.join()
-        return time.perf_counter() - t0, "reference", "bruteCPU (brute.cu:91-112), 1-NN"
+        return time.perf_counter() - t0, "reference", "bruteCPU (brute.cu:91-112), 1-NN", (out[:, None], None)
     t0 = time.perf_counter()
-    oracle.knn(X, Qs, k, threads=threads)
-    return time.perf_counter() - t0, "port", f"oracle restatement of distVec/bruteCPU, {k}-NN"
+    ans = oracle.knn(X, Qs, k, threads=threads)
+    return time.perf_counter() - t0, "port", f"oracle restatement of distVec/bruteCPU, {k}-NN", ans
+
+
+PARITY_RTOL = 1e-6  # distance tolerance (relative); ids must be equal bit for bit
+
+
+def compare_answers(got_ids, got_d, want):
+    """(ids equal, distances equal bit for bit, distances within PARITY_RTOL)
+    of a GPU answer against the oracle's (k columns, or bruteCPU's 1-NN column)."""
+    want_ids, want_d = want
+    g = np.ascontiguousarray(got_ids).view(np.uint32)
+    if want_d is None:
+        return bool((g[:, 0] == want_ids[:, 0]).all()), None, None
+    gd = np.asarray(got_d, np.float32)
+    ids_eq = bool((g == want_ids).all())
+    bits = bool((gd.view(np.uint32) == want_d.view(np.uint32)).all())
+    tol = bool((np.abs(gd.astype(np.float64) - want_d) <= PARITY_RTOL * np.abs(want_d.astype(np.float64))).all())
+    return ids_eq, bits, tol
+
+
+def parity_report(results, forms, sel, want, extra_rows=None, extra_want=None):
+    """Every listed form's answers on the sampled queries `sel` against the
+    oracle's; extra_rows / extra_want: more queries (the tensor forms'
+    FP32-fallback queries) checked the same way."""
+    out = {"queries": int(len(sel)), "forms": list(forms), "ids_equal": True, "dists_equal": True,
+           "dists_within_rtol": True, "rtol": PARITY_RTOL, "per_form": {}}
+    for f in forms:
+        r = results[f]
+        ids_eq, bits, tol = compare_answers(r["ids"][sel].cpu().numpy(), r["dists"][sel].cpu().numpy(), want)
+        row = {"ids_equal": ids_eq, "dists_equal": bits, "dists_within_rtol": tol}
+        if extra_rows is not None and len(extra_rows):
+            e_ids, e_bits, e_tol = compare_answers(r["ids"][extra_rows].cpu().numpy(),
+                                                   r["dists"][extra_rows].cpu().numpy(), extra_want)
+            row["fallback_queries"] = {"queries": int(len(extra_rows)), "ids_equal": e_ids, "dists_equal": e_bits}
+            ids_eq, bits, tol = ids_eq and e_ids, bits and e_bits, tol and e_tol
+        out["per_form"][f] = row
+        out["ids_equal"] &= ids_eq
+        out["dists_equal"] = None if bits is None else (out["dists_equal"] and bits)
+        out["dists_within_rtol"] = None if tol is None else (out["dists_within_rtol"] and tol)
+    out["fallback_queries_checked"] = int(len(extra_rows)) if extra_rows is not None else 0
+    return out
+
+
+def parity_failed(p):
+    return p is not None and (not p["ids_equal"] or p["dists_within_rtol"] is False)
 
 
 # ------------------------------------------------------------------ reference arm
@@ -300,7 +346,7 @@ def run_reference(a):
     total = 0.0
     kind = desc = None
     for i in range(a.steps):
-        t, kind, desc = step(a.warmup + i)
+        t, kind, desc, _ = step(a.warmup + i)
         total += t
     value = per_step * a.steps / total
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
@@ -416,6 +462,7 @@ def run_engine(a):
         acc["value"] = replica_rate(m, steps, world, acc["ms"])
         acc["ids"] = ids.clone()
         acc["dists"] = dists.clone()
+        acc["fallback_ids"] = idx.fallback_queries() if mode & pyrbc.QUERY_EXACT_TC else np.empty(0, np.uint32)
         acc["fp64"] = fp64_error(X, Q, ids, dists)
         return acc
 
@@ -482,14 +529,30 @@ def run_engine(a):
                                  "note": "difference form costs sub+mul+add per pair-dim, 2 flops counted"}
 
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        # the CPU baseline's answers double as the full-size parity check:
+        # queries spread evenly over the batch, every exact form compared
+        # with them bit for bit, plus every query a tensor form sent to its
+        # FP32 fallback (up to 256), whose oracle answers are computed here
         threads = os.cpu_count() or 1
-        nq = a.cpu_queries_per_thread * threads
+        nq = min(m, a.cpu_queries_per_thread * threads)
+        sel = np.unique(np.linspace(0, m - 1, nq).round().astype(np.int64))
         Xh = X.cpu().numpy()
-        Qs = Q[:nq].cpu().numpy()
-        t, kind, desc = cpu_knn_timed(Xh, Qs, k, threads)
-        cpu = {"value": nq / t, "unit": UNIT, "cores": threads, "kind": kind,
-               "sample": f"{nq} of the {m:,} queries over the full {w['n']:,}-row database; {desc}"}
+        Qs = Q[torch.from_numpy(sel).cuda()].cpu().numpy()
+        t, kind, desc, ans = cpu_knn_timed(Xh, Qs, k, threads)
+        cpu = {"value": len(sel) / t, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"{len(sel)} of the {m:,} queries (evenly spaced) over the full {w['n']:,}-row database; "
+                         f"{desc}"}
+        fb = np.unique(np.concatenate([results[f]["fallback_ids"] for f in exact_forms] or [np.empty(0)]))
+        fb = fb.astype(np.int64)[:256]
+        fb_want = None
+        if len(fb):
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            fb_want = oracle.knn(Xh, Q[torch.from_numpy(fb).cuda()].cpu().numpy(), k, threads=threads)
+        parity = parity_report(results, exact_forms, sel, ans, fb if len(fb) else None, fb_want)
+        parity["oracle"] = kind
 
     if rank == 0:
         names = {"plain": "plain FP32 exact RBC", "tensor": "exact RBC, BF16 tcgen05 list search + FP32 rerank",
@@ -515,11 +578,13 @@ def run_engine(a):
                 "data": "synthetic (counter-based generator on the GPU)",
                 "config": dict(config(a, names[head]), parallelism=f"replicas{world}"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "extra": extra}
+                "clocks": clk, "parity": parity, "extra": extra}
         print(json.dumps(line), flush=True)
     idx.close()
     if dist:
         dist.destroy_process_group()
+    if parity_failed(parity):
+        sys.exit("parity: GPU answers differ from the oracle's")
 
 
 def side_measurements(a, idx, X, Q, results, exact_forms):
@@ -679,13 +744,30 @@ def run_batch(a):
                 "fp32_core": {"achieved_tflops": achieved, "peak_tflops": fp32_peak, "frac": achieved / fp32_peak},
                 "note": "achieved = evaluated (query, row) pairs x 2d over the whole graph step"}
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         threads = os.cpu_count() or 1
         r = max(inst, key=lambda z: z["n"])
         nq = min(r["m"], 2 * threads)
-        t, kind, desc = cpu_knn_timed(r["X"].cpu().numpy(), r["Q"][:nq].cpu().numpy(), r["k"], threads)
+        t, kind, desc, _ = cpu_knn_timed(r["X"].cpu().numpy(), r["Q"][:nq].cpu().numpy(), r["k"], threads)
         cpu = {"value": nq / t, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": f"{nq} queries of the largest instance (n={r['n']:,}, d={r['d']}); {desc}"}
+        # parity: 4 queries of every instance (first, last, two between)
+        # against the oracle, the batched answers compared bit for bit
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        parity = {"queries": 0, "instances": len(inst), "ids_equal": True, "dists_equal": True,
+                  "dists_within_rtol": True, "rtol": PARITY_RTOL}
+        for r, o in zip(inst, outs):
+            sel = np.unique(np.linspace(0, r["m"] - 1, min(4, r["m"])).round().astype(np.int64))
+            tsel = torch.from_numpy(sel).cuda()
+            want = oracle.knn(r["X"].cpu().numpy(), r["Q"][tsel].cpu().numpy(), r["k"], threads=threads)
+            ids_eq, bits, tol = compare_answers(o[0][tsel].cpu().numpy(), o[1][tsel].cpu().numpy(), want)
+            parity["queries"] += len(sel)
+            parity["ids_equal"] &= ids_eq
+            parity["dists_equal"] &= bits
+            parity["dists_within_rtol"] &= tol
+        parity["oracle"] = "port"
     if rank == 0:
         extra = {"build_and_tune_s": build_s, "queries_per_step": total_m, "pairs_per_step": pairs,
                  "one_by_one_ms_per_step": seq_ms, "one_by_one_value": world * total_m / (seq_ms / 1000.0),
@@ -698,13 +780,15 @@ def run_batch(a):
                 "config": dict(config(a, "batched exact RBC, FP32 list search, CUDA graph"),
                                parallelism=f"replicas{world}"),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "extra": extra}
+                "clocks": clk, "parity": parity, "extra": extra}
         print(json.dumps(line), flush=True)
     batch.close()
     for r in inst:
         r["idx"].close()
     if dist:
         dist.destroy_process_group()
+    if parity_failed(parity):
+        sys.exit("parity: GPU answers differ from the oracle's")
 
 
 def main():

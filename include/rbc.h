@@ -2,7 +2,8 @@
  * rbc.h -- legacy Random Ball Cover API (C++ linkage, by-value structs).
  *
  * Same declarations as the reference's rbc.h:11-26 so programs written for it
- * (driver.cu) compile and link unchanged.  buildRBC builds both the
+ * (driver.cu, or code that runs the query plan step by step) compile and link
+ * unchanged.  buildRBC builds both the
  * reference's one-shot lists (exposed in rbcStruct) and the partition used for
  * exact search; queryRBC / kqueryRBC return EXACT 1 / 32 nearest neighbours by
  * default.  rbc_set_legacy_query_mode(RBC_QUERY_ONESHOT) restores the
@@ -25,6 +26,10 @@ void computeCounts(unint *, unint, unint *);
 void buildQMap(matrix, unint *, unint *, unint, unint *);
 void idIntersection(charMatrix);
 void fullIntersection(charMatrix);
+void initCompPlan(compPlan *, charMatrix, unint *, unint *, unint);
+void freeCompPlan(compPlan *);
+void computeNNs(matrix, intMatrix, matrix, unint *, compPlan, unint *, real *, unint);
+void computeKNNs(matrix, intMatrix, matrix, unint *, compPlan, intMatrix, matrix, unint);
 void setupReps(matrix, rbcStruct *, unint);
 
 #ifdef __cplusplus

@@ -146,6 +146,12 @@ int rbc_query(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint3
 int rbc_query_host(rbc_index *index, const float *hQ, uint64_t m, uint32_t ldq, uint32_t k,
                    uint32_t mode, uint32_t *hIds, float *hDists, uint32_t ldo);
 int rbc_get_query_stats(const rbc_index *index, rbc_query_stats *stats);
+/* The queries (indices into that call's batch, increasing) that the last
+ * RBC_QUERY_EXACT_TC call on this index recomputed on the FP32 path because
+ * the tensor form's certificate left them open; *count receives how many
+ * there were and min(count, cap) of them go to h_ids.  No counterpart in the
+ * reference: it lets a caller check those answers on their own. */
+int rbc_get_fallback_queries(const rbc_index *index, uint32_t *h_ids, uint64_t cap, uint64_t *count);
 
 /* ---- batched queries over many indexes (no counterpart in the reference) ----
  * Instances (index, device queries, k, outputs) are added, then rbc_batch_run
@@ -241,12 +247,15 @@ int rbc_brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, ui
  * allocator, latency-bound callers that must not wait on an allocator, and
  * code running inside another allocator's callback.  Results equal
  * rbc_brute_knn's.  Its working memory is one fixed device array of about
- * 2.4 MB held by every GPU that loads the library.  Limits: m <= 8192 queries
- * per call, d a multiple of 4 and at most 512, ldx == ldq a multiple of 4,
- * dX and dQ 16-byte aligned; other shapes return RBC_ERR_UNSUPPORTED.  All
- * calls share the array, so calls that overlap on the GPU race: order them on
- * one stream.  The first call on each device looks the array up and should
- * come before any stream capture. */
+ * 2.4 MB, part of the library's device code: CUDA loads that code lazily, so
+ * a device gives the array its memory at the library's first call there and
+ * keeps it until the process exits.  A call with m = 0 takes the array and
+ * looks its address up, nothing else: make one on every device at start-up,
+ * before any stream capture.  Limits: m <= 8192 queries per call, d a
+ * multiple of 4 and at most 512, ldx == ldq a multiple of 4, dX and dQ
+ * 16-byte aligned; other shapes return RBC_ERR_UNSUPPORTED.  All calls share
+ * the array, so calls that overlap on the GPU race: order them on one
+ * stream. */
 int rbc_brute_knn_noalloc(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m,
                           uint32_t ldq, uint32_t d, uint32_t k, int metric, uint32_t *dIds,
                           float *dDists, uint32_t ldo, void *stream);

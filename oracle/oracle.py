@@ -15,7 +15,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "librbc_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
 REF64_PATH = os.path.join(HERE, "_ref", "libref_f64.so")  # the reference built with real = double
-REF_DIR = "/root/reference"
+# where the reference's sources are: this environment variable, else the tree
+# the last `make ref` compiled (recorded beside its outputs)
+REF_ENV = "RBC_REFERENCE_DIR"
+REF_RECORD = os.path.join(HERE, "_ref", "SOURCE_DIR")
 
 L2, L1 = 0, 1
 DUMMY = 0xFFFFFFFF
@@ -31,13 +34,27 @@ U64P = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
 F64P = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 
 
-def build(with_ref=None):
-    """Compile the oracle (always) and the reference build (when its sources exist)."""
+def ref_dir():
+    """The reference's source tree: $RBC_REFERENCE_DIR, else the one the last
+    reference build recorded; None when neither is present on this machine."""
+    cands = [os.environ.get(REF_ENV)]
+    if os.path.exists(REF_RECORD):
+        cands.append(open(REF_RECORD).read().strip())
+    for c in cands:
+        if c and os.path.isdir(c):
+            return c
+    return None
+
+
+def build(with_ref=None, source=None):
+    """Compile the oracle (always) and the reference build (when its sources
+    are present: `source`, else ref_dir())."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    src = source or ref_dir()
     if with_ref is None:
-        with_ref = os.path.isdir(REF_DIR)
-    if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={REF_DIR}"], check=True)
+        with_ref = src is not None
+    if with_ref and src:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={src}"], check=True)
 
 
 def lib():

@@ -619,6 +619,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(stats.alloc(2 * sizeof(unsigned long long), s));
   CK(cudaMemsetAsync(stats.p, 0, 2 * sizeof(unsigned long long), s));
   uint64_t nfail_total = 0;
+  idx->fallback_ids.clear();
   double tc_ms = 0;
   uint32_t tc_launches = 0;
   while (idx->ev_pool.size() < 4 && idx->profile) {
@@ -780,6 +781,12 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     }
     const uint32_t nfail = hc[1];
     nfail_total += nfail;
+    if (nfail) {
+      std::vector<uint32_t> f(nfail);
+      CK(cudaMemcpy(f.data(), failq.p, nfail * 4ull, cudaMemcpyDeviceToHost));
+      std::sort(f.begin(), f.end());
+      for (uint32_t q : f) idx->fallback_ids.push_back((uint32_t)(b0 + q));
+    }
     if (nfail && (dIds || dDists)) {
       DevBuf Qf, fi, fd;
       CK(Qf.alloc((uint64_t)nfail * ld * 4, s));
@@ -1024,6 +1031,13 @@ int rbc_query_host(rbc_index *idx, const float *hQ, uint64_t m, uint32_t ldq, ui
 int rbc_get_query_stats(const rbc_index *idx, rbc_query_stats *st) {
   if (!idx || !st) return fail(RBC_ERR_INVALID, "rbc_get_query_stats: NULL argument");
   *st = idx->stats;
+  return RBC_OK;
+}
+
+int rbc_get_fallback_queries(const rbc_index *idx, uint32_t *h_ids, uint64_t cap, uint64_t *count) {
+  if (!idx || !count || (cap && !h_ids)) return fail(RBC_ERR_INVALID, "rbc_get_fallback_queries: NULL argument");
+  *count = idx->fallback_ids.size();
+  if (cap && *count) std::memcpy(h_ids, idx->fallback_ids.data(), std::min<uint64_t>(cap, *count) * 4);
   return RBC_OK;
 }
 

@@ -119,6 +119,7 @@ struct rbc_index {
   uint64_t min_list = 0, max_list = 0;
   uint64_t device_bytes = 0;
   rbc_query_stats stats{};
+  std::vector<uint32_t> fallback_ids;  // queries the last tensor-form call recomputed in FP32
   // search tuning (rbc_set_tuning / the autotuner): rows-per-thread of the
   // list-search tile (0 = default) and the longest row run of one work item
   int tune_tq = 0;

@@ -15,6 +15,7 @@
 // same functions over double matrices, answered by the library's double-
 // precision calls.  The one-shot lists are float-only there: rbcS.dxMap stays
 // empty and the one-shot query mode is refused.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -300,6 +301,298 @@ void idIntersection(charMatrix cM) {
 void fullIntersection(charMatrix cM) {
   for (unint i = 0; i < cM.r; i++)
     for (unint j = 0; j < cM.c; j++) cM.mat[IDX(i, j, cM.ld)] = 1;
+}
+
+// ------------------------------------------------------------------ compPlan
+// The reference's query plan (rbc.cu:375-440): query group g (the queries
+// whose nearest representative is g, laid out in 16-slot blocks by
+// buildQMap) is compared with the database groups j where cM[g][j] is set.
+// Row g of qGroupToXGroup lists those j, groupCountX their list lengths;
+// qToQGroup maps every query slot to its group.  Built on the host and moved
+// to the device like the reference's; freeCompPlan releases it.
+namespace {
+
+template <typename T>
+__global__ void gather_pad_kernel(const T *__restrict__ src, uint64_t ld_src, const uint32_t *__restrict__ rows,
+                                  uint64_t n, uint32_t d, T *__restrict__ dst, uint32_t ld_dst) {
+  const uint64_t total = n * ld_dst;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = i / ld_dst;
+    const uint32_t c = (uint32_t)(i - r * ld_dst);
+    dst[i] = c < d ? src[(uint64_t)rows[r] * ld_src + c] : T(0);
+  }
+}
+
+// dst row r = src row rows[r] (columns past d zeroed); rows is on the device.
+template <typename T>
+cudaError_t gather_pad(const T *src, uint64_t ld_src, const uint32_t *rows, uint64_t n, uint32_t d, T *dst,
+                       uint32_t ld_dst) {
+  if (n == 0) return cudaSuccess;
+  const uint64_t total = n * ld_dst;
+  const unsigned grid = (unsigned)std::min<uint64_t>((total + 255) / 256, 152ull * 32);
+  gather_pad_kernel<T><<<grid, 256>>>(src, ld_src, rows, n, d, dst, ld_dst);
+  return rbc::launched();
+}
+
+template <typename T>
+T *dev_alloc(size_t count) {
+  T *p = nullptr;
+  checkErr(cudaMalloc((void **)&p, std::max<size_t>(count, 1) * sizeof(T)));
+  return p;
+}
+
+template <typename T>
+std::vector<T> to_host(const T *d, size_t count) {
+  std::vector<T> h(count);
+  if (count) checkErr(cudaMemcpy(h.data(), d, count * sizeof(T), cudaMemcpyDeviceToHost));
+  return h;
+}
+
+// One run of consecutive query blocks of the same group: its real queries and
+// the database groups (list, length) it is compared with.
+struct PlanRun {
+  unint g;
+  std::vector<unint> queries;
+  std::vector<std::pair<unint, unint>> groups;
+};
+
+// The plan read back from the device and checked against the matrices it
+// indexes (ids, lists and lengths in range), as runs of query blocks.
+std::vector<PlanRun> read_plan(const matrix &dx, const intMatrix &dxMap, const matrix &dq, const unint *dqMap,
+                               const compPlan &dcP, unint compLength, const char *who) {
+  if (compLength % BLOCK_SIZE) die(who, RBC_ERR_INVALID);
+  const std::vector<unint> qmap = to_host(dqMap, compLength);
+  const std::vector<unint> q2g = to_host(dcP.qToQGroup, compLength);
+  unint gmax = 0;
+  for (unint b = 0; b < compLength; b += BLOCK_SIZE) gmax = std::max(gmax, q2g[b]);
+  const std::vector<unint> num = to_host(dcP.numGroups, compLength ? gmax + 1 : 0);
+  const size_t width = (size_t)(compLength ? gmax + 1 : 0) * dcP.ld;
+  const std::vector<unint> xg = to_host(dcP.qGroupToXGroup, width), cnt = to_host(dcP.groupCountX, width);
+  std::vector<PlanRun> runs;
+  for (unint b = 0; b < compLength; b += BLOCK_SIZE) {
+    const unint g = q2g[b];
+    if (runs.empty() || runs.back().g != g) {
+      PlanRun r;
+      r.g = g;
+      if (num[g] > dcP.ld) die(who, RBC_ERR_INVALID);
+      for (unint i = 0; i < num[g]; i++) {
+        const unint j = xg[(size_t)g * dcP.ld + i], c = cnt[(size_t)g * dcP.ld + i];
+        if (j >= dxMap.r || c > dxMap.ld) die(who, RBC_ERR_INVALID);
+        r.groups.push_back({j, c});
+      }
+      runs.push_back(std::move(r));
+    }
+    for (unint t = 0; t < BLOCK_SIZE; t++) {
+      const unint q = qmap[b + t];
+      if (q == DUMMY_IDX) continue;
+      if (q >= dq.r) die(who, RBC_ERR_INVALID);
+      runs.back().queries.push_back(q);
+    }
+  }
+  (void)dx;
+  return runs;
+}
+
+// Database ids of the lists a plan uses, each list once: rows, and the first
+// row of every list in it (UINT64_MAX for unused lists).
+void plan_rows(const std::vector<PlanRun> &runs, const matrix &dx, const intMatrix &dxMap,
+               std::vector<unint> &rows, std::vector<uint64_t> &first, const char *who) {
+  unint jmax = 0;
+  for (const PlanRun &r : runs)
+    for (auto &gc : r.groups) jmax = std::max(jmax, gc.first + 1);
+  const std::vector<unint> lists = to_host(dxMap.mat, (size_t)jmax * dxMap.ld);
+  first.assign(jmax, UINT64_MAX);
+  std::vector<unint> len(jmax, 0);
+  for (const PlanRun &r : runs)
+    for (auto &gc : r.groups) len[gc.first] = std::max(len[gc.first], gc.second);
+  for (unint j = 0; j < jmax; j++) {
+    if (!len[j]) continue;
+    first[j] = rows.size();
+    for (unint t = 0; t < len[j]; t++) {
+      const unint id = lists[(size_t)j * dxMap.ld + t];
+      if (id >= dx.r) die(who, RBC_ERR_INVALID);
+      rows.push_back(id);
+    }
+  }
+}
+
+#ifndef RBC_REAL_DOUBLE
+// The plan's searches in one persistent list-search launch: the lists' rows
+// gathered (zero-padded) into one buffer, work items (query tile of a run,
+// row chunk of one of its lists), per-query sorted (dist, id) lists of the
+// engine's exact FP32 search.
+void plan_search(const matrix &dx, const intMatrix &dxMap, const matrix &dq, const unint *dqMap, const compPlan &dcP,
+                 unint compLength, unint k, unint *hIds, real *hDists, unint ldo, const char *who) {
+  const std::vector<PlanRun> runs = read_plan(dx, dxMap, dq, dqMap, dcP, compLength, who);
+  std::vector<unint> rows;
+  std::vector<uint64_t> first;
+  plan_rows(runs, dx, dxMap, rows, first, who);
+  const uint32_t d = dq.c, ld = rbc::pad16(d), dp = rbc::pad4(d), m = dq.r;
+  if (dx.c != d || d > rbc::kMaxDim) die(who, RBC_ERR_UNSUPPORTED);
+  const uint32_t kw = rbc::list_width_for(k), qtile = (uint32_t)rbc::search_query_tile(dp, 0, kw);
+  constexpr uint32_t kChunk = 16384;
+  std::vector<unint> qidx;
+  std::vector<rbc::SearchItem> items;
+  for (const PlanRun &r : runs) {
+    const uint32_t q0 = (uint32_t)qidx.size(), nq = (uint32_t)r.queries.size();
+    qidx.insert(qidx.end(), r.queries.begin(), r.queries.end());
+    for (auto &gc : r.groups)
+      for (uint32_t c0 = 0; c0 < gc.second; c0 += kChunk)
+        for (uint32_t t0 = 0; t0 < nq; t0 += qtile) {
+          rbc::SearchItem it{};
+          it.p0 = first[gc.first] + c0;
+          it.np = std::min(kChunk, gc.second - c0);
+          it.list = gc.first;
+          it.q0 = q0 + t0;
+          it.nq = std::min(qtile, nq - t0);
+          items.push_back(it);
+        }
+  }
+  float *Xg = dev_alloc<float>(rows.size() * ld), *Qp = dev_alloc<float>((size_t)m * ld);
+  float *res_d = dev_alloc<float>((size_t)m * kw), *out_d = dev_alloc<float>((size_t)m * k);
+  unint *d_rows = dev_alloc<unint>(rows.size()), *d_qidx = dev_alloc<unint>(qidx.size());
+  unint *res_i = dev_alloc<unint>((size_t)m * kw), *out_i = dev_alloc<unint>((size_t)m * k);
+  unint *tau = dev_alloc<unint>(m), *lock = dev_alloc<unint>(m), *ctl = dev_alloc<unint>(16);
+  rbc::SearchItem *d_items = dev_alloc<rbc::SearchItem>(items.size());
+  checkErr(cudaMemcpy(d_rows, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice));
+  checkErr(cudaMemcpy(d_qidx, qidx.data(), qidx.size() * 4, cudaMemcpyHostToDevice));
+  checkErr(cudaMemcpy(d_items, items.data(), items.size() * sizeof(rbc::SearchItem), cudaMemcpyHostToDevice));
+  checkErr(cudaMemset(ctl, 0, 64));
+  const uint32_t nitems = (uint32_t)items.size();
+  checkErr(cudaMemcpy(ctl + 1, &nitems, 4, cudaMemcpyHostToDevice));
+  checkErr(gather_pad<float>(dx.mat, dx.ld, d_rows, rows.size(), d, Xg, ld));
+  checkErr(rbc::launch_pad_rows(dq.mat, dq.ld, Qp, ld, m, d, nullptr));
+  checkErr(rbc::launch_init_results(res_d, res_i, tau, lock, m, kw, nullptr));
+  rbc::SearchArgs sa{};
+  sa.X = Xg;
+  sa.pid = d_rows;
+  sa.Q = Qp;
+  sa.qidx = d_qidx;
+  sa.items = d_items;
+  sa.nitems = ctl + 1;
+  sa.work = ctl;
+  sa.res_d = res_d;
+  sa.res_i = res_i;
+  sa.tau = tau;
+  sa.lock = lock;
+  sa.err = ctl + 2;
+  sa.ld = ld;
+  sa.dp = dp;
+  sa.k = k;
+  if (nitems) checkErr(rbc::launch_search(g_metric, sa, rbc::search_grid(g_metric, dp, 0, kw), nullptr));
+  checkErr(rbc::launch_write_results(res_d, res_i, m, k, kw, out_i, out_d, k, nullptr));
+  unint err_word = 0;
+  checkErr(cudaMemcpy(&err_word, ctl + 2, 4, cudaMemcpyDeviceToHost));
+  if (err_word) die(who, (int)err_word);
+  const std::vector<unint> hi = to_host(out_i, (size_t)m * k);
+  const std::vector<float> hd = to_host(out_d, (size_t)m * k);
+  for (unint q = 0; q < m; q++)
+    for (unint j = 0; j < k; j++) {
+      hIds[(size_t)q * ldo + j] = hi[(size_t)q * k + j];
+      if (hDists) hDists[(size_t)q * ldo + j] = hd[(size_t)q * k + j];
+    }
+  void *ptrs[] = {Xg, Qp, res_d, out_d, d_rows, d_qidx, res_i, out_i, tau, lock, ctl, d_items};
+  for (void *p : ptrs) cudaFree(p);
+}
+#else
+// The double build: each run of query blocks answered by the double brute
+// force over its lists' rows (gathered), ids mapped back through the lists.
+void plan_search(const matrix &dx, const intMatrix &dxMap, const matrix &dq, const unint *dqMap, const compPlan &dcP,
+                 unint compLength, unint k, unint *hIds, real *hDists, unint ldo, const char *who) {
+  const std::vector<PlanRun> runs = read_plan(dx, dxMap, dq, dqMap, dcP, compLength, who);
+  std::vector<unint> all_rows;
+  std::vector<uint64_t> first;
+  plan_rows(runs, dx, dxMap, all_rows, first, who);
+  const uint32_t d = dq.c, ld = rbc::pad16(d);
+  if (dx.c != d) die(who, RBC_ERR_UNSUPPORTED);
+  for (unint q = 0; q < dq.r; q++)
+    for (unint j = 0; j < k; j++) {
+      hIds[(size_t)q * ldo + j] = DUMMY_IDX;
+      if (hDists) hDists[(size_t)q * ldo + j] = MAX_REAL;
+    }
+  for (const PlanRun &r : runs) {
+    if (r.queries.empty()) continue;
+    std::vector<unint> rows;
+    for (auto &gc : r.groups)
+      rows.insert(rows.end(), all_rows.begin() + first[gc.first], all_rows.begin() + first[gc.first] + gc.second);
+    if (rows.empty()) continue;
+    const size_t nq = r.queries.size(), nx = rows.size();
+    unint *d_rows = dev_alloc<unint>(nx), *d_q = dev_alloc<unint>(nq), *ids = dev_alloc<unint>(nq * k);
+    real *Xg = dev_alloc<real>(nx * ld), *Qg = dev_alloc<real>(nq * ld), *dd = dev_alloc<real>(nq * k);
+    checkErr(cudaMemcpy(d_rows, rows.data(), nx * 4, cudaMemcpyHostToDevice));
+    checkErr(cudaMemcpy(d_q, r.queries.data(), nq * 4, cudaMemcpyHostToDevice));
+    checkErr(gather_pad<real>(dx.mat, dx.ld, d_rows, nx, d, Xg, ld));
+    checkErr(gather_pad<real>(dq.mat, dq.ld, d_q, nq, d, Qg, ld));
+    const int rc = rbc_brute_knn_f64(Xg, nx, ld, Qg, nq, ld, d, k, g_metric, ids, dd, k, nullptr, nullptr);
+    if (rc != RBC_OK) die(who, rc);
+    const std::vector<unint> hi = to_host(ids, nq * k);
+    const std::vector<real> hd = to_host(dd, nq * k);
+    for (size_t t = 0; t < nq; t++)
+      for (unint j = 0; j < k; j++) {
+        const unint pos = hi[t * k + j];
+        hIds[(size_t)r.queries[t] * ldo + j] = pos < nx ? rows[pos] : DUMMY_IDX;
+        if (hDists) hDists[(size_t)r.queries[t] * ldo + j] = hd[t * k + j];
+      }
+    void *ptrs[] = {d_rows, d_q, ids, Xg, Qg, dd};
+    for (void *p : ptrs) cudaFree(p);
+  }
+}
+#endif
+
+}  // namespace
+
+void initCompPlan(compPlan *dcP, charMatrix cM, unint *groupCountQ, unint *groupCountX, unint numReps) {
+  if (!dcP || (numReps && (!cM.mat || !groupCountQ || !groupCountX))) die("initCompPlan", RBC_ERR_INVALID);
+  std::vector<unint> num(numReps, 0);
+  unint width = 0;
+  for (unint g = 0; g < numReps; g++) {
+    for (unint j = 0; j < numReps; j++) num[g] += cM.mat[IDX(g, j, cM.ld)] ? 1u : 0u;
+    width = std::max(width, num[g]);
+  }
+  std::vector<unint> q2g;
+  for (unint g = 0; g < numReps; g++) q2g.insert(q2g.end(), PAD(groupCountQ[g]), g);
+  std::vector<unint> xg((size_t)numReps * width, 0), cnt((size_t)numReps * width, 0);
+  for (unint g = 0; g < numReps; g++)
+    for (unint j = 0, t = 0; j < numReps; j++)
+      if (cM.mat[IDX(g, j, cM.ld)]) {
+        xg[IDX(g, t, width)] = j;
+        cnt[IDX(g, t++, width)] = groupCountX[j];
+      }
+  auto up = [](const std::vector<unint> &h) {
+    unint *p = dev_alloc<unint>(h.size());
+    if (!h.empty()) checkErr(cudaMemcpy(p, h.data(), h.size() * 4, cudaMemcpyHostToDevice));
+    return p;
+  };
+  dcP->numGroups = up(num);
+  dcP->groupCountX = up(cnt);
+  dcP->qToQGroup = up(q2g);
+  dcP->qGroupToXGroup = up(xg);
+  dcP->ld = width;
+}
+
+void freeCompPlan(compPlan *dcP) {
+  if (!dcP) return;
+  cudaFree(dcP->numGroups);
+  cudaFree(dcP->groupCountX);
+  cudaFree(dcP->qToQGroup);
+  cudaFree(dcP->qGroupToXGroup);
+  dcP->numGroups = dcP->groupCountX = dcP->qToQGroup = dcP->qGroupToXGroup = nullptr;
+}
+
+// 1-NN of every query over the lists its plan names, into host NNs / NNdists
+// (rbc.cu:317-330).  dx, dxMap, dq and dqMap are device data.
+void computeNNs(matrix dx, intMatrix dxMap, matrix dq, unint *dqMap, compPlan dcP, unint *NNs, real *NNdists,
+                unint compLength) {
+  if (!NNs) die("computeNNs", RBC_ERR_INVALID);
+  plan_search(dx, dxMap, dq, dqMap, dcP, compLength, 1, NNs, NNdists, 1, "computeNNs");
+}
+
+// KMAX nearest neighbours of every query over the lists its plan names,
+// sorted by (dist, id), into the host matrices NNs / NNdists (rbc.cu:333-348).
+void computeKNNs(matrix dx, intMatrix dxMap, matrix dq, unint *dqMap, compPlan dcP, intMatrix NNs, matrix NNdists,
+                 unint compLength) {
+  if (!NNs.mat || (NNdists.mat && NNdists.ld != NNs.ld) || NNs.ld < KMAX) die("computeKNNs", RBC_ERR_INVALID);
+  plan_search(dx, dxMap, dq, dqMap, dcP, compLength, KMAX, NNs.mat, NNdists.mat, NNs.ld, "computeKNNs");
 }
 
 // Random representatives copied to a padded device matrix rbcS->dr (rbc.cu:212-229).

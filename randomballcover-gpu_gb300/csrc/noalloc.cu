@@ -16,13 +16,20 @@
 //     and at most 512, X and Q sharing one row stride (a multiple of 4 floats)
 //     and 16-byte aligned: the kernel reads the caller's rows directly
 //     instead of copying them into padded buffers;
-//   * the array (about 2.4 MB) is held by every GPU that loads this library
-//     until the process exits;
+//   * the array (about 2.4 MB) is part of this library's device code; CUDA
+//     loads that code on each device lazily, so the array takes device
+//     memory at the first call on a device and keeps it until the process
+//     exits.  A call with m = 0 does exactly that and nothing else: make one
+//     at start-up on every device, while memory is still free and before any
+//     stream capture (it also looks the array's device address up with
+//     cudaGetSymbolAddress);
+//   * the address is looked up again when the device's context changes
+//     (after cudaDeviceReset, say);
 //   * all calls share the array: calls that overlap on the GPU (different
 //     streams or threads without ordering between them) race and corrupt each
-//     other's results.  Order them on one stream, or serialise them;
-//   * the first call on each device looks the array's device address up
-//     (cudaGetSymbolAddress); make that first call before any stream capture.
+//     other's results.  Order them on one stream, or serialise them.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "engine.cuh"
@@ -57,22 +64,58 @@ namespace rbc {
 namespace {
 
 std::mutex g_mu;
-void *g_scratch_addr[64] = {};
+// Per device: the array's address and the id of the context it belongs to.
+struct ScratchSlot {
+  void *addr = nullptr;
+  unsigned long long ctx = 0;
+};
+ScratchSlot g_slot[64];
 
-// Device address of the array on the current device, looked up once per device.
+// Unique id of the calling thread's current context (driver entry points
+// found at run time, so the library needs no link to the driver); false when
+// there is none or the driver lacks the calls.
+bool current_context_id(unsigned long long *id) {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", (void **)&get_current, 4000, cudaEnableDefault, &q1) !=
+            cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess)
+      get_current = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", (void **)&get_id, 12000, cudaEnableDefault, &q2) !=
+            cudaSuccess ||
+        q2 != cudaDriverEntryPointSuccess)
+      get_id = nullptr;
+    tried = true;
+  }
+  CUcontext c = nullptr;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c) return false;
+  return get_id(c, id) == CUDA_SUCCESS;
+}
+
+// Device address of the array on the current device: looked up once per
+// device and context, with that device current.
 int scratch_address(unsigned char **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "rbc_brute_knn_noalloc: cudaGetDevice");
   if (dev < 0 || dev >= 64) return fail(RBC_ERR_UNSUPPORTED, "rbc_brute_knn_noalloc: device index above 63");
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
+  ScratchSlot &slot = g_slot[dev];
+  unsigned long long ctx = 0;
+  const bool known = current_context_id(&ctx);
+  if (!slot.addr || !known || ctx != slot.ctx) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) return cuda_fail(e, "rbc_brute_knn_noalloc: cudaGetSymbolAddress");
-    g_scratch_addr[dev] = p;
+    slot.addr = p;
+    slot.ctx = current_context_id(&ctx) ? ctx : 0;
   }
-  *out = static_cast<unsigned char *>(g_scratch_addr[dev]);
+  *out = static_cast<unsigned char *>(slot.addr);
   return RBC_OK;
 }
 
@@ -90,7 +133,8 @@ extern "C" int rbc_brute_knn_noalloc(const float *dX, uint64_t n, uint32_t ldx, 
   if (k < 1 || k > (uint32_t)kListWidth) return fail(RBC_ERR_INVALID, "rbc_brute_knn_noalloc: k must be in [1, 32]");
   if (ldo < k) return fail(RBC_ERR_INVALID, "rbc_brute_knn_noalloc: ldo < k");
   if (metric != RBC_L2 && metric != RBC_L1) return fail(RBC_ERR_INVALID, "rbc_brute_knn_noalloc: unknown metric");
-  if (m == 0) return RBC_OK;
+  unsigned char *scr = nullptr;
+  if (m == 0) return scratch_address(&scr);  // the start-up call: the array is taken and found, nothing else
   if (m > kNoAllocMaxQueries)
     return fail(RBC_ERR_UNSUPPORTED, "rbc_brute_knn_noalloc: more than 8192 queries per call (split the batch)");
   if (!dQ || (!dIds && !dDists) || (n && !dX)) return fail(RBC_ERR_INVALID, "rbc_brute_knn_noalloc: NULL buffer");
@@ -102,7 +146,6 @@ extern "C" int rbc_brute_knn_noalloc(const float *dX, uint64_t n, uint32_t ldx, 
   if (!aligned16(dX) || !aligned16(dQ))
     return fail(RBC_ERR_UNSUPPORTED, "rbc_brute_knn_noalloc: X and Q must be 16-byte aligned");
 
-  unsigned char *scr = nullptr;
   int rc = scratch_address(&scr);
   if (rc != RBC_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;

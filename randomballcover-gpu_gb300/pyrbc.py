@@ -71,6 +71,7 @@ SIGNATURES = {
     "rbc_query": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP, _VP, _U32, _VP], _INT),
     "rbc_query_host": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP, _VP, _U32], _INT),
     "rbc_get_query_stats": ([_VP, C.POINTER(QueryStats)], _INT),
+    "rbc_get_fallback_queries": ([_VP, _VP, _U64, C.POINTER(_U64)], _INT),
     "rbc_batch_create": ([C.POINTER(_VP)], _INT),
     "rbc_batch_add": ([_VP, _VP, _VP, _U64, _U32, _U32, _VP, _VP, _U32], _INT),
     "rbc_batch_run": ([_VP, _VP], _INT),
@@ -270,6 +271,15 @@ class Index:
         st = QueryStats()
         check(lib().rbc_get_query_stats(self.h, C.byref(st)))
         return {f: getattr(st, f) for f, _ in QueryStats._fields_}
+
+    def fallback_queries(self):
+        """Indices of the queries the last tensor-form call recomputed on the FP32 path."""
+        n = C.c_uint64()
+        check(lib().rbc_get_fallback_queries(self.h, None, 0, C.byref(n)))
+        out = np.empty(n.value, np.uint32)
+        if n.value:
+            check(lib().rbc_get_fallback_queries(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out
 
     def set_profiling(self, enable=True):
         check(lib().rbc_set_profiling(self.h, int(enable)))

@@ -54,7 +54,11 @@ def test_legacy_names_have_reference_mangling(engine_lib):
     for sym in ("_Z8buildRBC6matrixP9rbcStructjj", "_Z9kqueryRBC6matrix9rbcStruct9intMatrixS_",
                 "_Z8queryRBC6matrix9rbcStructPjPf", "_Z10destroyRBCP9rbcStruct", "_Z6bruteK6matrixS_9intMatrixS_",
                 "_Z8bruteCPU6matrixS_Pj", "_Z11bruteSearch6matrixS_Pj", "_Z15bruteRangeCount6matrixS_PfPj",
-                "_Z7distVec6matrixS_jj", "_Z7initMatP6matrixjj"):
+                "_Z7distVec6matrixS_jj", "_Z7initMatP6matrixjj",
+                # the query plan of rbc.h:22-25
+                "_Z12initCompPlanP8compPlan10charMatrixPjS2_j", "_Z12freeCompPlanP8compPlan",
+                "_Z10computeNNs6matrix9intMatrixS_Pj8compPlanS1_Pfj",
+                "_Z11computeKNNs6matrix9intMatrixS_Pj8compPlanS0_S_j"):
         assert sym in out, sym
 
 

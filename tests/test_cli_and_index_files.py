@@ -44,6 +44,87 @@ def test_load_rejects_bad_files(engine_lib, tmp_path):
     assert L.rbc_load(str(tmp_path / "missing.idx").encode(), C.byref(h)) == engine_lib.ERR_IO
 
 
+def _index_file(n=64, d=4, nr=4, **hdr):
+    """A small partition-only index file laid out as rbc_save writes one
+    (persist.cu): 128-byte header, representative ids, representatives,
+    list-major rows, partition arrays.  Keyword arguments override header
+    fields; the arrays come back for editing."""
+    import struct
+    ld, dp = (d + 15) // 16 * 16, (d + 3) // 4 * 4
+    per = n // nr
+    h = dict(version=2, d=d, ld=ld, dp=dp, nr=nr, s=0, lds=0, kp=0, flags=1, ld64=0, metric=0, n=n, n_pad=0,
+             xi_rows=0, min_list=per, max_list=per)
+    h.update(hdr)
+    arrays = {
+        "rep_ids": np.arange(nr, dtype=np.uint32) * per,
+        "R": np.zeros(((nr + 15) // 16 * 16, ld), np.float32),
+        "Xp": np.zeros((n, ld), np.float32),
+        "perm": np.arange(n, dtype=np.uint32),
+        "offsets": np.arange(nr + 1, dtype=np.uint64) * per,
+        "radius": np.ones(nr, np.float32),
+        "owner": (np.arange(n) // max(per, 1)).astype(np.uint32),
+    }
+    return h, arrays
+
+
+def _write_index(path, h, arrays, tail=b""):
+    import struct
+    head = b"RBCGB300" + struct.pack("<10Ii4x5Q32x", h["version"], h["d"], h["ld"], h["dp"], h["nr"], h["s"],
+                                     h["lds"], h["kp"], h["flags"], h["ld64"], h["metric"], h["n"], h["n_pad"],
+                                     h["xi_rows"], h["min_list"], h["max_list"])
+    assert len(head) == 128
+    body = b"".join(np.ascontiguousarray(arrays[k]).tobytes()
+                    for k in ("rep_ids", "R", "Xp", "perm", "offsets", "radius", "owner"))
+    path.write_bytes(head + body + tail)
+
+
+def test_load_checks_every_field_before_the_device(engine_lib, tmp_path):
+    """rbc_load refuses a damaged index file with RBC_ERR_IO before its first
+    CUDA call: header fields, the file length, and the arrays that index into
+    others (representative ids, list offsets, the partition's rows and
+    owners, radii).  The intact file passes the checks (here, without a GPU,
+    it then stops at the first CUDA call)."""
+    import ctypes as C
+    L = engine_lib.lib()
+    p = tmp_path / "i.idx"
+
+    def load(h, a, tail=b""):
+        _write_index(p, h, a, tail)
+        out = C.c_void_p()
+        rc = L.rbc_load(str(p).encode(), C.byref(out))
+        if rc == 0:
+            L.rbc_destroy(out)
+        return rc, L.rbc_last_error().decode()
+
+    h, a = _index_file()
+    rc, _ = load(h, a)
+    assert rc in (0, engine_lib.ERR_CUDA), rc
+    header_cases = [dict(d=600), dict(ld=32), dict(dp=8), dict(metric=5), dict(flags=1 | 0x40), dict(flags=0),
+                    dict(flags=4 | 2, s=8, lds=16), dict(nr=65), dict(n=0), dict(min_list=3), dict(max_list=100),
+                    dict(xi_rows=7), dict(flags=1 | 2, s=80, lds=80)]
+    for case in header_cases:
+        h2, a2 = _index_file(**case)
+        rc, msg = load(h2, a2)
+        assert rc == engine_lib.ERR_IO, (case, rc, msg)
+    edits = [("offsets", 2, 10), ("offsets", 4, 63), ("offsets", 0, 1), ("perm", 5, 64), ("perm", 5, 6),
+             ("owner", 3, 2), ("owner", 3, 9), ("radius", 1, np.nan), ("radius", 1, -1.0), ("rep_ids", 1, 0),
+             ("rep_ids", 2, 64)]
+    for name, i, v in edits:
+        h2, a2 = _index_file()
+        a2[name][i] = v
+        rc, msg = load(h2, a2)
+        assert rc == engine_lib.ERR_IO and "corrupt" in msg, (name, i, v, rc, msg)
+    h2, a2 = _index_file()
+    for tail in (b"\0" * 4,):
+        rc, msg = load(h2, a2, tail)
+        assert rc == engine_lib.ERR_IO and "longer" in msg, msg
+    _write_index(p, h2, a2)
+    p.write_bytes(p.read_bytes()[:-4])
+    out = C.c_void_p()
+    assert L.rbc_load(str(p).encode(), C.byref(out)) == engine_lib.ERR_IO
+    assert b"truncated" in L.rbc_last_error()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["exact", "tc", "oneshot"])
 def test_cli_on_sample_input(engine_lib, rbc, oracle, tmp_path, mode):

@@ -160,6 +160,48 @@ def test_rbc_exact_equals_oracle(rbc, oracle, metric, case):
     idx.close()
 
 
+def test_c1_full_size_every_form_equals_oracle(rbc, oracle):
+    """The first benchmark configuration at its full size: n = 65,536 uniform
+    rows in d = 16, all 8,192 queries, 256 representatives, 1-NN (and 32-NN),
+    the plain exact form and the tensor form against the oracle; the
+    one-shot form against the oracle's one-shot restatement."""
+    n, m, d, nr = 65536, 8192, 16, 256
+    X = rbc.synth(0, 1, 0, n, d)
+    Q = rbc.synth(0, 1, 1, m, d)
+    Xh, Qh = X.cpu().numpy(), Q.cpu().numpy()
+    idx = rbc.Index(X, nr, s=nr, seed=1, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16 | rbc.BUILD_ONESHOT)
+    for k in (1, 32):
+        ri, rd = oracle.knn(Xh, Qh, k)
+        for mode in (rbc.QUERY_EXACT, rbc.QUERY_EXACT_TC):
+            ids, dists = idx.query(Q, k, mode=mode)
+            assert_same(ids, dists, ri, rd, rbc)
+    reps = idx.reps()
+    lists, counts = idx.oneshot()
+    rl, rc, _ = oracle.oneshot_build(Xh, reps, nr)
+    np.testing.assert_array_equal(counts, rc)
+    np.testing.assert_array_equal(lists, rl)
+    oi, od = oracle.oneshot_query(Xh, reps, lists, counts, Qh, 1)
+    ids, dists = idx.query(Q, 1, mode=rbc.QUERY_ONESHOT)
+    assert_same(ids, dists, oi, od, rbc)
+    idx.close()
+
+
+def test_fallback_queries_are_reported_and_exact(rbc, oracle):
+    """The queries the tensor form's certificate leaves open are listed by
+    rbc_get_fallback_queries (as many as the stats count) and their answers,
+    recomputed on the FP32 path, equal the oracle's."""
+    X = rbc.synth(1, 31, 0, 30000, 128, ncomp=300, sigma_lo=0.05, sigma_hi=0.05)
+    Q = rbc.synth(1, 31, 1, 2000, 128, ncomp=300, sigma_lo=0.05, sigma_hi=0.05)
+    idx = rbc.Index(X, 200, seed=2, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
+    fb = idx.fallback_queries()
+    assert len(fb) == idx.stats()["fallback_queries"]
+    assert (np.diff(fb.astype(np.int64)) > 0).all() and (fb < 2000).all()
+    ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), 10)
+    assert_same(ids, dists, ri, rd, rbc)
+    idx.close()
+
+
 def test_rbc_exact_edge_cases(rbc, oracle):
     rng = np.random.default_rng(8)
     # n < k, nr == n, single rep, all-duplicate database, queries on top of points

@@ -10,7 +10,8 @@ import pytest
 from conftest import GOLDEN, ROOT, load_golden
 
 INCLUDE = os.path.join(ROOT, "include")
-REF_DRIVER = "/root/reference/driver.cu"
+REF_SRC = __import__("oracle").ref_dir()  # the reference's sources, where this machine has them
+REF_DRIVER = os.path.join(REF_SRC, "driver.cu") if REF_SRC else ""
 
 
 def compile_program(src, out, engine_lib, extra=(), lib="rbcgb"):
@@ -63,6 +64,74 @@ def test_legacy_driver_on_sample_input(engine_lib, rbc, tmp_path):
     for j in range(3):
         np.testing.assert_array_equal(nn[j * 128:(j + 1) * 128], g["ref_bruteCPU_1nn"])
     np.testing.assert_array_equal(nn[384:].view(np.float32), g["dists_l2"][:, 0])
+
+
+def test_legacy_plan_driver_compiles(engine_lib, tmp_path):
+    """The plan functions of the reference's rbc.h (initCompPlan, freeCompPlan,
+    computeNNs, computeKNNs) link, in both builds."""
+    src = os.path.join(ROOT, "tests", "legacy_plan_driver.cu")
+    compile_program(src, str(tmp_path / "plan"), engine_lib)
+    compile_program(src, str(tmp_path / "plan64"), engine_lib, extra=("-DRBC_REAL_DOUBLE",), lib="rbcgb_f64")
+
+
+def _plan_oracle(oracle, X, Q, members_of, k=32):
+    """For every query, the oracle's k-NN over the database rows members_of(i)
+    (increasing ids, repeats kept), as (ids, dists) under (distance, id)."""
+    ids = np.full((Q.shape[0], k), oracle.DUMMY, np.uint32)
+    dists = np.full((Q.shape[0], k), oracle.FLT_MAX, np.float32)
+    for i in range(Q.shape[0]):
+        mem = members_of(i)
+        if len(mem) == 0:
+            continue
+        pos, dd = oracle.knn(np.ascontiguousarray(X[mem]), np.ascontiguousarray(Q[i:i + 1]), k)
+        ok = pos[0] != oracle.DUMMY
+        ids[i, ok] = mem[pos[0][ok]]
+        dists[i, ok] = dd[0][ok]
+    return ids, dists
+
+
+@pytest.mark.gpu
+def test_plan_api_on_sample_input(engine_lib, rbc, oracle, tmp_path):
+    """The reference's kqueryRBC / queryRBC steps run one by one (rbc.cu:19-123)
+    through initCompPlan + computeKNNs / computeNNs: under the identity
+    computation matrix each query gets the oracle's 32-NN over its nearest
+    representative's one-shot list, under the full matrix over every list
+    (rows in several lists count once per list), and computeNNs the first of
+    the identity answer."""
+    exe = compile_program(os.path.join(ROOT, "tests", "legacy_plan_driver.cu"), str(tmp_path / "plan"), engine_lib)
+    out = str(tmp_path / "plan.bin")
+    m, nr = 128, 128
+    r = subprocess.run([exe, os.path.join(GOLDEN, "sample_db.bin"), os.path.join(GOLDEN, "sample_queries.bin"),
+                        "1024", str(m), "16", str(nr), out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = np.fromfile(out, np.uint8)
+    off = 0
+
+    def take(count, dt):
+        nonlocal off
+        a = raw[off:off + 4 * count].view(dt)
+        off += 4 * count
+        return a
+
+    rep = take(m, np.uint32)
+    lists = take(nr * nr, np.uint32).reshape(nr, nr)
+    counts = take(nr, np.uint32)
+    id_ids, id_d = take(m * 32, np.uint32).reshape(m, 32), take(m * 32, np.float32).reshape(m, 32)
+    full_ids, full_d = take(m * 32, np.uint32).reshape(m, 32), take(m * 32, np.float32).reshape(m, 32)
+    nn1, d1 = take(m, np.uint32), take(m, np.float32)
+    assert off == raw.size
+    assert (rep < nr).all() and counts.sum() > 0
+    X, Q = sample_inputs()
+    own = [lists[j, :counts[j]] for j in range(nr)]
+    allm = np.sort(np.concatenate(own))
+    want_ids, want_d = _plan_oracle(oracle, X, Q, lambda i: own[rep[i]])
+    np.testing.assert_array_equal(id_ids, want_ids)
+    np.testing.assert_array_equal(id_d, want_d)
+    want_ids, want_d = _plan_oracle(oracle, X, Q, lambda i: allm)
+    np.testing.assert_array_equal(full_ids, want_ids)
+    np.testing.assert_array_equal(full_d, want_d)
+    np.testing.assert_array_equal(nn1, id_ids[:, 0])
+    np.testing.assert_array_equal(d1, id_d[:, 0])
 
 
 # ------------------------------------------------------------------ the double build
