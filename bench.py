@@ -91,7 +91,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-side", action="store_true",
                     help="skip the c2 side measurements (k = 128 and the double-precision variant)")
-    ap.add_argument("--router-probes", type=int, default=1, help="lists the learned form adds from the router")
+    ap.add_argument("--router-probes", type=int, default=0,
+                    help="lists the learned form probes from the router (0: none, the distance head plans instead)")
     ap.add_argument("--forms", default=None,
                     help="forms to time; the last one listed is the headline (default: per workload)")
     ap.add_argument("--tc-tuning", default=None, metavar="PROBES,ROWS",
@@ -397,22 +398,33 @@ def run_engine(a):
     # the learned router: trained on the GPU on queries the RBC labels
     router_info = None
     if "learned" in forms:
+        # the router's two heads, trained on labels the RBC produces: the list
+        # owning each training query's nearest neighbour, and its k-th
+        # distance over its nearest representative's
         Qtr = pyrbc.synth(w["kind"], w["seed"], 2, w["train"], w["d"], **synth)
         t0 = time.perf_counter()
-        labels = idx.owner_labels(Qtr)
+        labels, tdist, tnear = idx.router_labels(Qtr, k)
         torch.cuda.synchronize()
         label_s = time.perf_counter() - t0
-        router = pyrbc.Router(w["d"], 512, w["reps"], seed=w["seed"])
+        router = pyrbc.Router(w["d"], 512, w["reps"], seed=w["seed"], distance_head=True)
         t0 = time.perf_counter()
-        loss = router.train(Qtr, labels, epochs=w["epochs"], batch=1024, lr=2e-3, seed=w["seed"])
+        loss = router.train_with_distance(Qtr, labels, tdist, tnear, epochs=w["epochs"], batch=1024, lr=2e-3,
+                                          seed=w["seed"])
         torch.cuda.synchronize()
         train_s = time.perf_counter() - t0
-        del Qtr, labels
-        test_labels = idx.owner_labels(Q).long()
+        del Qtr, labels, tdist, tnear
+        test_labels, true_d, near_d = idx.router_labels(Q, k)
         top1 = router.logits(Q).argmax(1)
+        ratio = (router.predict_distance(Q, near_d) / true_d).float()
+        mu, sg, margin = router.distance_params()
         router_info = {"train_queries": w["train"], "epochs": w["epochs"], "label_s": label_s, "train_s": train_s,
-                       "final_loss": loss, "probe_recall_top1": (top1 == test_labels).float().mean().item(),
-                       "architecture": f"MLP {w['d']}->512->512->{w['reps']} GELU, BF16 weights, FP32 accumulate"}
+                       "final_loss": loss, "probe_recall_top1": (top1 == test_labels.long()).float().mean().item(),
+                       "distance_head": {"median_predicted_over_true": ratio.median().item(),
+                                         "share_below_true": (ratio < 1).float().mean().item(),
+                                         "margin_sigma_units": margin, "log_ratio_sigma": sg},
+                       "architecture": f"MLP {w['d']}->512->512->{w['reps']} (+1 distance output) GELU, "
+                                       "BF16 weights, FP32 accumulate"}
+        # probes = 0: no probe round; the predicted k-th distance plans the search
         idx.set_router(router, probes=a.router_probes)
 
     modes = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC, "oneshot": pyrbc.QUERY_ONESHOT,
@@ -432,7 +444,7 @@ def run_engine(a):
                 idx.set_tc_tuning(*(int(v) for v in a.tc_tuning.split(",")))
             else:
                 idx.autotune_tc(Qtune, k, mode)
-            tuning[mode] = idx.tc_tuning()
+            tuning[mode] = list(idx.tc_tuning()) + (["plain FP32 search chosen"] if idx.info()["tc_plain"] else [])
         for _ in range(warmup):
             idx.query(Q, k, mode=mode, out=(ids, dists))
         barrier()
@@ -518,12 +530,13 @@ def run_engine(a):
     avg_launch_s = res["search_ms"] / max(res["search_launches"], 1) / 1000.0
     achieved = flops_per_launch / avg_launch_s / 1e12 if avg_launch_s > 0 else 0.0
     sm_mhz = (clk or {}).get("sm_mhz") or 1920.0
-    kernel = "search_kernel" if head == "plain" else "tc_search_kernel"
+    head_plain = head == "plain" or (modes[head] & pyrbc.QUERY_EXACT_TC and idx.info()["tc_plain"])
+    kernel = "search_kernel" if head_plain else "tc_search_kernel"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
                 "frac": achieved / bf16, "traffic": committed_traffic(kernel), "kernel": kernel,
                 "peak_source": f"{src} bf16 dense burst (MEASURED_PEAKS.json)",
                 "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
-    if head == "plain":
+    if head_plain:
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
         roofline["fp32_core"] = {"achieved_tflops": achieved, "peak_tflops": fp32_peak, "frac": achieved / fp32_peak,
                                  "note": "difference form costs sub+mul+add per pair-dim, 2 flops counted"}
@@ -557,7 +570,8 @@ def run_engine(a):
     if rank == 0:
         names = {"plain": "plain FP32 exact RBC", "tensor": "exact RBC, BF16 tcgen05 list search + FP32 rerank",
                  "oneshot": "the reference's one-shot RBC (approximate)",
-                 "learned": "exact RBC, learned router + BF16 tcgen05 list search + FP32 rerank",
+                 "learned": "exact RBC, learned router (its predicted k-th distance plans the search) + BF16 "
+                            "tcgen05 list search + FP32 rerank",
                  "learned_plain": "exact RBC, learned router + FP32 list search"}
         extra = {"build_s": build_s, "min_list": info["min_list"], "max_list": info["max_list"],
                  "tc_format": ["bf16", "fp16_split"][info["tc_format"]], "same_ids_all_exact_forms": same,

@@ -97,6 +97,9 @@ typedef struct {
   uint64_t min_list, max_list; /* partition list sizes                  */
   uint64_t device_bytes;       /* device memory held by the index        */
   uint32_t tc_format;          /* RBC_TC_* (with RBC_BUILD_BF16)         */
+  uint32_t tc_plain;           /* 1: rbc_autotune_tc found the plain FP32
+                                  search faster, and RBC_QUERY_EXACT_TC
+                                  calls run it                          */
 } rbc_index_info;
 
 typedef struct {               /* work done by the last rbc_query on an index */
@@ -147,10 +150,13 @@ int rbc_query_host(rbc_index *index, const float *hQ, uint64_t m, uint32_t ldq, 
                    uint32_t mode, uint32_t *hIds, float *hDists, uint32_t ldo);
 int rbc_get_query_stats(const rbc_index *index, rbc_query_stats *stats);
 /* The queries (indices into that call's batch, increasing) that the last
- * RBC_QUERY_EXACT_TC call on this index recomputed on the FP32 path because
- * the tensor form's certificate left them open; *count receives how many
- * there were and min(count, cap) of them go to h_ids.  No counterpart in the
- * reference: it lets a caller check those answers on their own. */
+ * RBC_QUERY_EXACT_TC call on this index answered a second time: recomputed
+ * on the FP32 path because the tensor form's certificate left them open,
+ * or, in a routed call without a probe round (rbc_set_router with probes =
+ * 0), searched again with the probe round because their k-th distance
+ * exceeded the prediction.  *count receives how many there were and
+ * min(count, cap) of them go to h_ids.  No counterpart in the reference: it
+ * lets a caller check those answers on their own. */
 int rbc_get_fallback_queries(const rbc_index *index, uint32_t *h_ids, uint64_t cap, uint64_t *count);
 
 /* ---- batched queries over many indexes (no counterpart in the reference) ----
@@ -176,12 +182,19 @@ int rbc_set_tuning(rbc_index *index, int tq, uint32_t item_rows);
 int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
                  const char *cache_path, void *stream);
 /* Tuning of the tensor-core form: nearest lists searched in its probe round
- * (1-8; 0 keeps the default, 4) and how many rows of each probed list the
- * FP32 path searches first (whole lists when shorter; the rest of a longer
- * list goes to the tensor cores; 0 keeps the default, 8192).
- * rbc_autotune_tc times 1, 2, 4, 8 probes x 2048, 8192, 32768 rows on sample
+ * (1-8; 0 keeps the default, 4; RBC_TC_ROUTER_ONLY: none in routed calls,
+ * whose probe round then searches the router's picks alone, and one in
+ * others) and how many rows of each probed list the FP32 path searches
+ * first (whole lists when shorter; the rest of a longer list goes to the
+ * tensor cores; 0 keeps the default, 8192).
+ * rbc_autotune_tc times 1, 2, 4, 8 probes (and RBC_TC_ROUTER_ONLY in routed
+ * mode) x 2048, 8192, 32768 rows on sample
  * queries in the given mode (RBC_QUERY_EXACT_TC, optionally
- * | RBC_QUERY_ROUTED) and keeps the fastest.  Results never change. */
+ * | RBC_QUERY_ROUTED) and keeps the fastest; it also times the plain FP32
+ * search (RBC_QUERY_EXACT with the same routing) and, when that is faster,
+ * makes RBC_QUERY_EXACT_TC calls on this index run it (info.tc_plain).
+ * rbc_set_tc_tuning selects the tensor form again.  Results never change. */
+#define RBC_TC_ROUTER_ONLY 0xFFu
 int rbc_set_tc_tuning(rbc_index *index, uint32_t probes, uint64_t probe_rows);
 int rbc_get_tc_tuning(const rbc_index *index, uint32_t *probes, uint64_t *probe_rows);
 int rbc_autotune_tc(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
@@ -215,8 +228,57 @@ int rbc_router_logits(rbc_router *router, const float *dQ, uint64_t m, uint32_t 
 int rbc_owner_labels(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t *dLabels,
                      void *stream);
 /* Attach (or detach, router = NULL) a router to an index; RBC_QUERY_ROUTED
- * queries then probe its top `probes` (1..7) lists first. */
+ * queries then probe its top `probes` (1..7) lists first.  probes = 0 (a
+ * router with a distance head): the tensor form skips its probe round and
+ * plans with the predicted k-th distance (see below). */
 int rbc_set_router(rbc_index *index, rbc_router *router, uint32_t probes);
+
+/* The router's distance head: one more output of the last layer, a
+ * regression of the normalised log ratio of the query's k-th neighbour
+ * distance to the distance of its nearest representative (which every query
+ * computes exactly), trained beside the list classifier (squared error, same
+ * Adam steps).  A
+ * routed tensor-form query with probes = 0 skips the probe round: it prunes
+ * every list with tau = min(prediction, k-th nearest representative), caps
+ * each shortlist at tau (1 + 2^-10) and searches.  The answer is accepted
+ * only when its exact k-th distance is at most tau (nothing pruned or turned
+ * away can then be in the top k); the other queries are answered again by
+ * the tensor form with its probe round.  Results stay exact; a good
+ * prediction saves the probe round.  No counterpart in the reference.
+ * Parameters: as rbc_router_create, with W3 and b3 one row longer (the
+ * head's weights last). */
+int rbc_router_create_with_distance(uint32_t d, uint32_t hidden, uint32_t num_lists, uint64_t seed,
+                                    rbc_router **out);
+/* Labels for both heads from one exact k-NN query: the list owning each
+ * query's nearest neighbour (dLabels), its k-th distance (dDist, as
+ * rbc_query reports distances) and its nearest representative's distance
+ * (dNear); any output may be NULL.  k <= 32. */
+int rbc_router_labels(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
+                      uint32_t *dLabels, float *dDist, float *dNear, void *stream);
+/* Training of both heads on n labelled queries.  The distance targets
+ * log(dDist / dNear) are normalised (mean and spread); rows where either
+ * distance is zero or not finite train the list head only.  The last 2 % of
+ * the rows (when n >= 1000) are held out: the margin added to every
+ * prediction is the 99.5th percentile of (target - prediction) over them. */
+int rbc_router_train_with_distance(rbc_router *router, const float *dQ, uint64_t n, uint32_t ldq,
+                                   const uint32_t *dLabels, const float *dDist, const float *dNear,
+                                   uint32_t epochs, uint32_t batch, float lr, uint64_t seed, float *final_loss,
+                                   void *stream);
+/* Loss and gradients of one batch with both heads; dTargets are the distance
+ * head's targets in its own (normalised) units, NaN for none. */
+int rbc_router_gradients_with_distance(rbc_router *router, const float *dQ, uint32_t batch, uint32_t ldq,
+                                       const uint32_t *dLabels, const float *dTargets, float *loss,
+                                       float *h_grads, void *stream);
+/* Predicted k-th distances (margin included) of m queries whose nearest
+ * representatives are at dNear. */
+int rbc_router_predict_distance(rbc_router *router, const float *dQ, uint64_t m, uint32_t ldq, const float *dNear,
+                                float *dDist, void *stream);
+/* The head's normalisation (log(distance / nearest representative's) =
+ * mu + sigma (output + margin)) and
+ * margin; the margin can be set (a larger one: fewer queries answered twice,
+ * more lists searched). */
+int rbc_router_distance_params(const rbc_router *router, float *mu, float *sigma, float *margin);
+int rbc_router_set_distance_margin(rbc_router *router, float margin);
 
 /* Benchmark instrumentation (no counterpart in the reference): with profiling
  * on, every list-search kernel launch of a query call is bracketed by CUDA

@@ -129,10 +129,12 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
   a.offsets = offsets;
   a.probe = b.probe.as<uint32_t>();
   a.probed = b.probed.as<float>();
+  a.dq0 = b.dq0;
   a.tau = b.tau.as<uint32_t>();
   a.m = m;
   a.nr = nr;
   a.P = P;
+  a.P_excl = b.plan_all ? 0 : P;
   a.metric = (uint32_t)idx->metric;
   a.qtile = qtile;
   const double g = (double)(idx->dp + 8) * 1.1920928955078125e-07;
@@ -425,9 +427,11 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     offsets = idx->os_offsets;
   } else if (base == RBC_QUERY_EXACT_TC) {
     if (!(idx->flags & RBC_BUILD_BF16)) return fail(RBC_ERR_INVALID, "rbc_query: index has no BF16 lists");
-    if (k <= kTcMaxK) return query_tc(idx, dQ, m, ldq, k, mode, dIds, dDists, ldo, s);
-    // wider k: the shortlists stop at 56 entries; the FP32 exact search over
-    // the same partition lists answers (a BF16 index always has them)
+    if (k <= kTcMaxK && !idx->tc_plain) return query_tc(idx, dQ, m, ldq, k, mode, dIds, dDists, ldo, s);
+    // wider k (the shortlists stop at 56 entries), or the autotuner found the
+    // plain search faster: the FP32 exact search over the same partition
+    // lists answers (a BF16 index always has them); no query falls back
+    idx->fallback_ids.clear();
     return query_index(idx, dQ, m, ldq, k, (mode & ~0xFFu) | RBC_QUERY_EXACT, dIds, dDists, ldo, s);
   } else {
     return fail(RBC_ERR_INVALID, "rbc_query: unknown mode");
@@ -555,10 +559,21 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   // lists searched in the probe round: the nearest representatives' (plus,
   // routed, the router's picks among the others); RBC_TC_PROBES overrides the
   // number of nearest ones
+  // number of nearest ones; RBC_TC_ROUTER_ONLY (routed calls): none, the
+  // router's picks alone
+  // A routed call whose router has a distance head and probes = 0 skips the
+  // probe round: every list is planned with tau = min(predicted k-th
+  // distance, k-th nearest representative), the shortlists are capped at
+  // tau (1 + 2^-10), and a query is accepted only if its exact k-th distance
+  // is at most tau; the others are answered again with the probe round.
+  const bool spec = routed && idx->router->r.T && idx->router_probes == 0;
   uint32_t Pn = idx->tc_probes ? idx->tc_probes : kTcProbes;
+  if (Pn == RBC_TC_ROUTER_ONLY) Pn = routed ? 0 : 1;
   if (const char *env = std::getenv("RBC_TC_PROBES")) Pn = std::max(1, std::min(8, std::atoi(env)));
+  if (spec) Pn = 1;  // the nearest representative only: the bound needs its distance
   Pn = std::min(Pn, nr);
-  const uint32_t P = routed ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
+  const uint32_t Pnear = std::max(Pn, 1u);  // nearest representatives found (the bound needs the first)
+  const uint32_t P = routed && !spec ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
   const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
   // the probe round's FP32 lists hold a whole shortlist; its query tiles
   // follow the probed queries per list (16 wide when few share a list)
@@ -566,6 +581,8 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   uint64_t probe_rows = idx->tc_probe_rows ? idx->tc_probe_rows : kTcProbeRows;
   if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) probe_rows = std::strtoull(env, nullptr, 10);
   const uint32_t qtile = tc_query_tile(fmt);
+  uint32_t lsu_gather = 1;
+  if (const char *env = std::getenv("RBC_TC_GATHER")) lsu_gather = std::strcmp(env, "tma") != 0;
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
   const uint64_t probe_per_list = mb * P / nr;
   const int ptq = search_tq_for(idx->dp, probe_per_list >= 48 ? 4 : (probe_per_list >= 24 ? 2 : 1), kw);
@@ -596,11 +613,17 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(b.ctl.alloc(64, s));
   CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
   DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
-      stats, seed_a, seed_row;
-  if (routed) {
-    CK(near.alloc(mb * Pn * 4, s));
-    CK(near_d.alloc(mb * Pn * 4, s));
+      stats, seed_a, seed_row, sl_cap, tpred;
+  b.plan_all = spec;
+  if (spec) {
+    CK(tpred.alloc(mb * 4, s));
+  } else if (routed) {
+    CK(near.alloc(mb * Pnear * 4, s));
+    CK(near_d.alloc(mb * Pnear * 4, s));
     CK(logits.alloc(mb * nr * 4, s));
+    // without nearest lists in the probe table the pruning bound takes the
+    // nearest representative's distance from here
+    if (Pn == 0) b.dq0 = near_d.as<float>();
   }
   CK(Qh.alloc((mb + 1) * cols * 2, s));
   CK(qscale.alloc((mb + 1) * 4, s));
@@ -613,6 +636,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   CK(sl_sel.alloc(mb * 4, s));
   CK(sl_theta.alloc(mb * 4, s));
   CK(sl_lock.alloc(mb * 4, s));
+  if (spec) CK(sl_cap.alloc(mb * 4, s));
   CK(emax.alloc(mb * 4, s));
   CK(ctl.alloc(64, s));
   CK(failq.alloc(mb * 4, s));
@@ -637,9 +661,9 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
     CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
     // the nearest representatives: the shortlist seed and, first, the probe table
-    if (routed) {
+    if (routed && !spec) {
       CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(),
-                         seed_row.as<uint32_t>(), Pn, near.as<uint32_t>(), near_d.as<float>(), s));
+                         seed_row.as<uint32_t>(), Pnear, near.as<uint32_t>(), near_d.as<float>(), s));
       Router &rt = idx->router->r;
       if (rt.tc_ok()) {
         CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
@@ -656,6 +680,9 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     } else {
       CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(),
                          seed_row.as<uint32_t>(), P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+      if (spec)
+        CK(idx->router->r.predict_tau(b.Qp.as<float>(), ld, (uint32_t)mq, b.probed.as<float>(), tpred.as<float>(),
+                                      b.ctl.as<uint32_t>() + 2, s));
     }
     CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(),
                            mq, kw, s));
@@ -690,9 +717,13 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     ta.sl_row = sl_row.as<uint32_t>();
     ta.sl_sel = sl_sel.as<uint32_t>();
     ta.sl_theta = sl_theta.as<uint32_t>();
+    ta.sl_cap = spec ? sl_cap.as<uint32_t>() : nullptr;
     ta.sl_lock = sl_lock.as<uint32_t>();
     ta.emax = emax.as<uint32_t>();
     ta.m = mq;
+    ta.qh = static_cast<const uint16_t *>(Qh.p);
+    ta.qcols = cols;
+    ta.lsu_gather = lsu_gather;
     ta.offsets = idx->offsets;
     ta.stats = stats.as<unsigned long long>();
     ta.err = ctl.as<uint32_t>();
@@ -709,13 +740,16 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     ra.sl_row = sl_row.as<uint32_t>();
     ra.sl_sel = sl_sel.as<uint32_t>();
     ra.emax = emax.as<uint32_t>();
+    ra.sl_cap = spec ? sl_cap.as<uint32_t>() : nullptr;
+    ra.tplan = nullptr;
     ra.ldo = ldo;
     ra.nfail = ctl.as<uint32_t>() + 1;
     ra.fail = failq.as<uint32_t>();
     // probe round, small lists: searched exactly on the FP32 path; every
     // query's exact top-sl there seeds its shortlist, and its k-th distance
-    // the pruning threshold
-    {
+    // the pruning threshold (none in the speculative plan: the seed is the
+    // nearest representatives, the threshold the prediction)
+    if (!spec) {
       const bool prof = idx->profile;
       idx->profile = false;
       // the first probe_rows rows of every probed list (whole lists when
@@ -730,11 +764,19 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, seed_a.as<float>(),
                       seed_row.as<uint32_t>(), mq, sl, k, sl_a.as<float>(), sl_row.as<uint32_t>(),
                       sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));
+    // the speculative plan: the predicted k-th distance lowers the planning
+    // threshold and caps every shortlist (only rows that can still reach the
+    // top k pass the tensor search's filter); the certificate then also
+    // checks the k-th distance against it
+    if (spec) {
+      CK(launch_cap(b.tau.as<uint32_t>(), tpred.as<float>(), mq, sl_cap.as<uint32_t>(), sl_theta.as<uint32_t>(), s));
+      ra.tplan = b.tau.as<uint32_t>();
+    }
     // probe round, large lists: tensor search into the seeded shortlists, one
     // 128-query tile per B tile (measured faster than two-tile items even for
     // the busiest probed lists), then the k-th exact distance of each
     // shortlist tightens the threshold
-    if (idx->max_list > probe_rows) {
+    if (!spec && idx->max_list > probe_rows) {
       ListFilter large;  // the rest of the longer lists
       large.rows_lo = probe_rows + 1;
       large.skip = probe_rows;
@@ -796,9 +838,21 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       rbc_profile keep = idx->prof;
       rbc_query_stats keep_stats = idx->stats;
       const int keep_tq = idx->tune_tq;
-      idx->tune_tq = 1;  // a handful of queries: 16-query tiles
-      const int rc = query_index(idx, Qf.as<float>(), nfail, ld, k, RBC_QUERY_EXACT, fi.as<uint32_t>(), fd.as<float>(),
-                                 k, s);
+      const bool keep_profile = idx->profile;
+      int rc;
+      if (spec) {
+        // a prediction that fell short (or a certificate left open): the
+        // tensor form again, with its probe round this time
+        std::vector<uint32_t> keep_fb;
+        keep_fb.swap(idx->fallback_ids);
+        idx->profile = false;
+        rc = query_tc(idx, Qf.as<float>(), nfail, ld, k, RBC_QUERY_EXACT_TC, fi.as<uint32_t>(), fd.as<float>(), k, s);
+        idx->fallback_ids.swap(keep_fb);
+      } else {
+        idx->tune_tq = 1;  // a handful of queries: 16-query tiles
+        rc = query_index(idx, Qf.as<float>(), nfail, ld, k, RBC_QUERY_EXACT, fi.as<uint32_t>(), fd.as<float>(), k, s);
+      }
+      idx->profile = keep_profile;
       idx->tune_tq = keep_tq;
       idx->prof = keep;
       idx->stats = keep_stats;
@@ -976,6 +1030,7 @@ int rbc_get_info(const rbc_index *idx, rbc_index_info *info) {
   info->max_list = idx->max_list;
   info->device_bytes = idx->device_bytes;
   info->tc_format = idx->tc.format;
+  info->tc_plain = idx->tc_plain ? 1u : 0u;
   return RBC_OK;
 }
 
@@ -1045,7 +1100,9 @@ int rbc_set_router(rbc_index *idx, rbc_router *router, uint32_t probes) {
   if (!idx) return fail(RBC_ERR_INVALID, "rbc_set_router: NULL index");
   if (router && (router->r.d != idx->d || router->r.L != idx->nr))
     return fail(RBC_ERR_INVALID, "rbc_set_router: router shape does not match the index (d, number of lists)");
-  if (router && (probes < 1 || probes > 7)) return fail(RBC_ERR_INVALID, "rbc_set_router: probes must be in [1, 7]");
+  if (router && probes == 0 && !router->r.T)
+    return fail(RBC_ERR_INVALID, "rbc_set_router: probes = 0 needs a router with a distance head");
+  if (router && probes > 7) return fail(RBC_ERR_INVALID, "rbc_set_router: probes must be in [0, 7]");
   idx->router = router;
   idx->router_probes = router ? probes : 0;
   return RBC_OK;
@@ -1062,6 +1119,34 @@ int rbc_owner_labels(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, 
   const uint32_t mode = (idx->flags & RBC_BUILD_BF16) ? RBC_QUERY_EXACT_TC : RBC_QUERY_EXACT;
   TRY(query_index(idx, dQ, m, ldq, 1, mode, ids.as<uint32_t>(), nullptr, 1, s));
   CK(launch_owner_lookup(ids.as<uint32_t>(), m, 1, idx->owner, dLabels, s));
+  CK(cudaStreamSynchronize(s));
+  return RBC_OK;
+}
+
+int rbc_router_labels(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t *dLabels,
+                      float *dDist, float *dNear, void *stream) {
+  if (!idx || (m && (!dQ || (!dLabels && !dDist && !dNear))))
+    return fail(RBC_ERR_INVALID, "rbc_router_labels: bad argument");
+  if (!(idx->flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_INVALID, "rbc_router_labels: index has no partition");
+  if (k < 1 || k > kTcMaxK) return fail(RBC_ERR_INVALID, "rbc_router_labels: k must be in [1, 32]");
+  if (m == 0) return RBC_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  DevBuf ids, dd;
+  CK(ids.alloc(m * k * 4, s));
+  CK(dd.alloc(m * k * 4, s));
+  const uint32_t mode = (idx->flags & RBC_BUILD_BF16) ? RBC_QUERY_EXACT_TC : RBC_QUERY_EXACT;
+  TRY(query_index(idx, dQ, m, ldq, k, mode, ids.as<uint32_t>(), dd.as<float>(), k, s));
+  if (dLabels) CK(launch_owner_lookup(ids.as<uint32_t>(), m, k, idx->owner, dLabels, s));
+  if (dDist)
+    CK(cudaMemcpy2DAsync(dDist, 4, dd.as<float>() + (k - 1), (size_t)k * 4, 4, m, cudaMemcpyDeviceToDevice, s));
+  if (dNear) {  // the nearest representative's distance, as the queries compute it
+    DevBuf Qp, best;
+    CK(Qp.alloc(m * idx->ld * 4, s));
+    CK(best.alloc(m * 4, s));
+    CK(launch_pad_rows(dQ, ldq, Qp.as<float>(), idx->ld, m, idx->d, s));
+    CK(launch_argmin(idx->metric, Qp.as<float>(), m, idx->R, idx->nr, idx->ld, idx->dp, best.as<uint32_t>(), dNear,
+                     s));
+  }
   CK(cudaStreamSynchronize(s));
   return RBC_OK;
 }

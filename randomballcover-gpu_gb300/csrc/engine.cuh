@@ -49,6 +49,8 @@ struct QueryBufs {
   DevBuf Qp, Dqr, probe, probed, res_d, res_i, tau, lock, cnt, start, cursor, tcnt, tstart, pair_q,
       pair_thr, items, ctl, scan_tmp;
   uint64_t item_cap = 0;
+  const float *dq0 = nullptr;  // nearest-representative distances when the probe table lacks them
+  bool plan_all = false;       // the pruning round plans every list (no probe round ran)
 };
 
 }  // namespace rbc
@@ -129,6 +131,7 @@ struct rbc_index {
   // goes to the tensor cores (0: the defaults)
   uint32_t tc_probes = 0;
   uint64_t tc_probe_rows = 0;
+  bool tc_plain = false;          // the plain FP32 search answers RBC_QUERY_EXACT_TC (it was faster)
   // learned router (rbc_set_router): probes its top router_probes lists
   rbc_router *router = nullptr;
   uint32_t router_probes = 0;

@@ -126,9 +126,12 @@ struct PlanArgs {
   const uint64_t *offsets; // nr+1 list offsets
   const uint32_t *probe;   // m x P probed lists (first column = nearest rep)
   const float *probed;     // m x P their distances
+  const float *dq0;        // per query: distance to its nearest representative (nullptr: probed[q P],
+                           // the probe table then starting with the nearest representative)
   const uint32_t *tau;     // per-query k-th distance bits after the probe phase
   uint64_t m;
   uint32_t nr, P, metric, qtile;
+  uint32_t P_excl;         // mode 1 leaves out the first P_excl probe-table lists (searched already)
   float opg_ru, omg_rd;    // 1 + gamma rounded up, 1 - gamma rounded down (gamma: relative
                            // error bound of a computed distance)
   float c_ru, opc_ru;      // c = 1 + 3 gamma and 1 + c, rounded up

@@ -134,7 +134,7 @@ __global__ void plan_kernel(PlanArgs a) {
   // the per-query terms, once per block
   for (uint32_t j = threadIdx.x; j < q1 - q0; j += blockDim.x) {
     s_tau[j] = __uint_as_float(a.tau[q0 + j]);
-    s_chi0[j] = query_term(a.probed[(q0 + j) * a.P], a);
+    s_chi0[j] = query_term(a.dq0 ? a.dq0[q0 + j] : a.probed[(q0 + j) * a.P], a);
   }
   __syncthreads();
   const bool rv = r < a.nr;
@@ -150,7 +150,7 @@ __global__ void plan_kernel(PlanArgs a) {
     for (uint64_t q = q0; q < q1; q++) {
       if (!nonempty) break;
       bool member = false;
-      for (uint32_t p = 0; p < a.P; p++) member |= a.probe[q * a.P + p] == r;
+      for (uint32_t p = 0; p < a.P_excl; p++) member |= a.probe[q * a.P + p] == r;
       if (member) continue;
       const float thr = prune_threshold(a.Dqr[q * a.nr + r], s_chi0[q - q0], hpsi, a);
       if (thr > s_tau[q - q0]) continue;

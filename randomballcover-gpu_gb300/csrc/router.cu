@@ -17,11 +17,14 @@
 //   bias_gelu        h = x + b, a = GELU(h) (exact erf form), h kept
 //   gelu_backward    dh = da * GELU'(h)
 //   softmax_xent     per row: loss and dz = (softmax(z) - onehot(y)) / B
+//   tau_loss         distance head: loss (z - t)^2 and dz = 2 (z - t) / B
+//                    (rows without a target add nothing)
 //   colsum           bias gradients
 //   adam             m, v, w updates and the BF16 weight copy
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -176,6 +179,26 @@ __global__ void softmax_xent_kernel(float *__restrict__ z, uint32_t L, const uin
   }
 }
 
+// The distance head's squared error on the batch's normalised targets (NaN:
+// no target); zt becomes its gradient.
+__global__ void tau_loss_kernel(float *__restrict__ zt, const float *__restrict__ yt, uint32_t b,
+                                float *__restrict__ loss, float scale) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= b) return;
+  const float t = yt[r];
+  const float e = isfinite(t) ? zt[r] - t : 0.f;
+  if (loss) loss[r] += e * e;
+  zt[r] = 2.f * e * scale;
+}
+
+__global__ void tau_from_head_kernel(const float *__restrict__ z, const float *__restrict__ near, uint64_t m, float mu,
+                                     float sigma, float margin, float *__restrict__ tau) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const float v = near[i] * __expf(fmaf(sigma, z[i] + margin, mu));
+  tau[i] = isfinite(v) ? fminf(v * 1.0001f, FLT_MAX) : FLT_MAX;
+}
+
 // out[n] = sum over rows of g[r][n] (bias gradients).
 __global__ void colsum_kernel(const float *__restrict__ g, uint32_t rows, uint32_t N, float *__restrict__ out) {
   uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -217,16 +240,21 @@ __global__ void init_kernel(float *__restrict__ w, uint64_t total, uint64_t seed
   w[i] = (2.f * u - 1.f) * scale;
 }
 
-// Gather rows of the training set for a batch (order[] holds row indices).
+// Gather rows of the training set for a batch (order[] holds row indices),
+// with their labels and (distance head) targets.
 __global__ void gather_batch_kernel(const float *__restrict__ Q, uint32_t ldq, uint32_t d,
                                     const uint32_t *__restrict__ order, const uint32_t *__restrict__ labels,
-                                    uint32_t batch, float *__restrict__ X, uint32_t *__restrict__ y) {
+                                    const float *__restrict__ tsrc, uint32_t batch, float *__restrict__ X,
+                                    uint32_t *__restrict__ y, float *__restrict__ yt) {
   uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (i >= (uint64_t)batch * d) return;
   uint32_t r = (uint32_t)(i / d), c = (uint32_t)(i - (uint64_t)r * d);
   uint32_t src = order[r];
   X[i] = Q[(uint64_t)src * ldq + c];
-  if (c == 0) y[r] = labels[src];
+  if (c == 0) {
+    y[r] = labels[src];
+    if (yt) yt[r] = tsrc ? tsrc[src] : __int_as_float(0x7fc00000);
+  }
 }
 
 unsigned blocks(uint64_t total, unsigned t = 256) { return (unsigned)((total + t - 1) / t); }
@@ -235,14 +263,15 @@ unsigned blocks(uint64_t total, unsigned t = 256) { return (unsigned)((total + t
 
 // ------------------------------------------------------------------ host
 size_t Router::nparams() const {
-  return (size_t)H * d + H + (size_t)H * H + H + (size_t)L * H + L;
+  return (size_t)H * d + H + (size_t)H * H + H + (size_t)(L + T) * H + (L + T);
 }
 
 cudaError_t Router::alloc_batch(uint32_t b, cudaStream_t s) {
   if (b <= cap) return cudaSuccess;
   for (void *p : {(void *)X, (void *)y, (void *)h1, (void *)a1, (void *)h2, (void *)a2, (void *)z, (void *)ga,
-                  (void *)gb, (void *)loss})
+                  (void *)gb, (void *)loss, (void *)yt, (void *)zt})
     if (p) cudaFreeAsync(p, s);
+  yt = zt = nullptr;
   cudaError_t e = cudaSuccess;
   auto al = [&](auto **p, size_t bytes) {
     if (e == cudaSuccess) e = cudaMallocAsync((void **)p, bytes, s);
@@ -257,14 +286,19 @@ cudaError_t Router::alloc_batch(uint32_t b, cudaStream_t s) {
   al(&ga, (size_t)b * H * 4);
   al(&gb, (size_t)b * H * 4);
   al(&loss, (size_t)b * 4);
+  if (T) {
+    al(&yt, (size_t)b * 4);
+    al(&zt, (size_t)b * 4);
+  }
   cap = e == cudaSuccess ? b : 0;
   return e;
 }
 
-// Forward pass of `b` rows of X (b x d, stride d) into logits z (b x L).
-cudaError_t Router::forward(const float *Xin, uint32_t ldx, uint32_t b, float *zout, cudaStream_t s) {
+// Forward pass of `b` rows of X (b x d, stride d) into logits z (b x L) and,
+// with the distance head, its outputs zt_out (b); either output may be null.
+cudaError_t Router::forward(const float *Xin, uint32_t ldx, uint32_t b, float *zout, cudaStream_t s, float *zt_out) {
   const __nv_bfloat16 *W1 = wb, *W2 = wb + (size_t)H * d + H, *W3 = W2 + (size_t)H * H + H;
-  const float *b1 = w + (size_t)H * d, *b2 = b1 + H + (size_t)H * H, *b3 = b2 + H + (size_t)L * H;
+  const float *b1 = w + (size_t)H * d, *b2 = b1 + H + (size_t)H * H, *b3 = b2 + H + (size_t)(L + T) * H;
   cudaError_t e = gemm<false, true>(Xin, ldx, W1, d, h1, H, b, H, d, b1, false, s);
   if (e == cudaSuccess) {
     gelu_kernel<<<blocks((uint64_t)b * H), 256, 0, s>>>(h1, a1, (uint64_t)b * H);
@@ -275,7 +309,9 @@ cudaError_t Router::forward(const float *Xin, uint32_t ldx, uint32_t b, float *z
     gelu_kernel<<<blocks((uint64_t)b * H), 256, 0, s>>>(h2, a2, (uint64_t)b * H);
     e = launched();
   }
-  if (e == cudaSuccess) e = gemm<false, true>(a2, H, W3, H, zout, L, b, L, H, b3, false, s);
+  if (e == cudaSuccess && zout) e = gemm<false, true>(a2, H, W3, H, zout, L, b, L, H, b3, false, s);
+  if (e == cudaSuccess && T && zt_out)
+    e = gemm<false, true>(a2, H, W3 + (size_t)L * H, H, zt_out, 1, b, 1, H, b3 + L, false, s);
   return e;
 }
 
@@ -283,16 +319,29 @@ cudaError_t Router::forward(const float *Xin, uint32_t ldx, uint32_t b, float *z
 cudaError_t Router::forward_backward(uint32_t b, cudaStream_t s) {
   const __nv_bfloat16 *W2 = wb + (size_t)H * d + H, *W3 = W2 + (size_t)H * H + H;
   float *gW1 = g, *gb1 = g + (size_t)H * d, *gW2 = gb1 + H, *gb2 = gW2 + (size_t)H * H, *gW3 = gb2 + H,
-        *gb3 = gW3 + (size_t)L * H;
-  cudaError_t e = forward(X, d, b, z, s);
+        *gb3 = gW3 + (size_t)(L + T) * H;
+  cudaError_t e = forward(X, d, b, z, s, zt);
   if (e != cudaSuccess) return e;
   softmax_xent_kernel<<<b, 256, 0, s>>>(z, L, y, loss, 1.f / b, 1);
   if ((e = launched()) != cudaSuccess) return e;
-  // layer 3: dW3 = dz^T a2, db3 = colsum dz, da2 = dz W3
+  if (T) {
+    tau_loss_kernel<<<blocks(b), 256, 0, s>>>(zt, yt, b, loss, 1.f / b);
+    if ((e = launched()) != cudaSuccess) return e;
+  }
+  // layer 3: dW3 = dz^T a2, db3 = colsum dz, da2 = dz W3 (each with the
+  // distance head's row when there is one)
   if ((e = gemm<true, false>(z, L, a2, H, gW3, H, L, H, b, nullptr, false, s)) != cudaSuccess) return e;
   colsum_kernel<<<blocks(L), 256, 0, s>>>(z, b, L, gb3);
   if ((e = launched()) != cudaSuccess) return e;
   if ((e = gemm<false, false>(z, L, W3, H, ga, H, b, H, L, nullptr, false, s)) != cudaSuccess) return e;
+  if (T) {
+    if ((e = gemm<true, false>(zt, 1, a2, H, gW3 + (size_t)L * H, H, 1, H, b, nullptr, false, s)) != cudaSuccess)
+      return e;
+    colsum_kernel<<<1, 32, 0, s>>>(zt, b, 1, gb3 + L);
+    if ((e = launched()) != cudaSuccess) return e;
+    if ((e = gemm<false, false>(zt, 1, W3 + (size_t)L * H, H, ga, H, b, H, 1, nullptr, true, s)) != cudaSuccess)
+      return e;
+  }
   gelu_backward_kernel<<<blocks((uint64_t)b * H), 256, 0, s>>>(h2, ga, (uint64_t)b * H);
   if ((e = launched()) != cudaSuccess) return e;
   // layer 2
@@ -326,7 +375,7 @@ cudaError_t Router::refresh_bf16(cudaStream_t s) {
 }
 
 cudaError_t Router::init(uint64_t seed, cudaStream_t s) {
-  const uint64_t sizes[6] = {(uint64_t)H * d, H, (uint64_t)H * H, H, (uint64_t)L * H, L};
+  const uint64_t sizes[6] = {(uint64_t)H * d, H, (uint64_t)H * H, H, (uint64_t)(L + T) * H, L + T};
   const float fan[6] = {(float)d, (float)d, (float)H, (float)H, (float)H, (float)H};
   uint64_t off = 0;
   for (int i = 0; i < 6; i++) {
@@ -343,14 +392,40 @@ cudaError_t Router::init(uint64_t seed, cudaStream_t s) {
 
 cudaError_t Router::gather(const float *Q, uint32_t ldq, const uint32_t *order, const uint32_t *labels, uint32_t b,
                            cudaStream_t s) {
-  gather_batch_kernel<<<blocks((uint64_t)b * d), 256, 0, s>>>(Q, ldq, d, order, labels, b, X, y);
+  gather_batch_kernel<<<blocks((uint64_t)b * d), 256, 0, s>>>(Q, ldq, d, order, labels, tau_src, b, X, y,
+                                                              T ? yt : nullptr);
   return launched();
+}
+
+// The distance head's outputs (normalised units) for b rows, on the queries'
+// inference path: tensor-core layers when hidden allows, else the training
+// forward.
+cudaError_t Router::head_outputs(const float *Xin, uint64_t ldx, uint64_t b, float *zt_out, uint32_t *err,
+                                 cudaStream_t s) {
+  if (!T) return cudaErrorInvalidValue;
+  const uint32_t chunk = tc_ok() ? (1u << 18) : 4096;
+  cudaError_t e = tc_ok() ? cudaSuccess : alloc_batch(chunk, s);
+  for (uint64_t i = 0; i < b && e == cudaSuccess; i += chunk) {
+    const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, b - i);
+    e = tc_ok() ? forward_tc_head(Xin + i * ldx, (uint32_t)ldx, cb, zt_out + i, err, s)
+                : forward(Xin + i * ldx, (uint32_t)ldx, cb, nullptr, s, zt_out + i);
+  }
+  return e;
+}
+
+// Predicted k-th distances: tau = near exp(mu + sigma (z + margin)), near the
+// distance to the query's nearest representative.
+cudaError_t Router::predict_tau(const float *Xin, uint32_t ldx, uint32_t b, const float *near, float *tau,
+                                uint32_t *err, cudaStream_t s) {
+  cudaError_t e = head_outputs(Xin, ldx, b, tau, err, s);
+  if (e == cudaSuccess) e = launch_tau_from_head(tau, near, b, tau_mu, tau_sigma, tau_margin, tau, s);
+  return e;
 }
 
 Router::~Router() {
   for (void *p : {(void *)w, (void *)g, (void *)m1, (void *)m2, (void *)wb, (void *)X, (void *)y, (void *)h1,
                   (void *)a1, (void *)h2, (void *)a2, (void *)z, (void *)ga, (void *)gb, (void *)loss, (void *)xb,
-                  (void *)h1b, (void *)h2b, (void *)w1p})
+                  (void *)h1b, (void *)h2b, (void *)w1p, (void *)yt, (void *)zt})
     if (p) cudaFree(p);
 }
 
@@ -424,6 +499,13 @@ cudaError_t launch_router_probes(const float *logits, uint64_t m, uint32_t L, ui
   return launched();
 }
 
+cudaError_t launch_tau_from_head(const float *z, const float *near, uint64_t m, float mu, float sigma, float margin,
+                                 float *tau, cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  tau_from_head_kernel<<<blocks(m), 256, 0, s>>>(z, near, m, mu, sigma, margin, tau);
+  return launched();
+}
+
 cudaError_t launch_owner_lookup(const uint32_t *ids, uint64_t m, uint32_t ldo, const uint32_t *owner,
                                 uint32_t *labels, cudaStream_t s) {
   if (m == 0) return cudaSuccess;
@@ -444,7 +526,9 @@ using namespace rbc;
 
 extern "C" {
 
-int rbc_router_create(uint32_t d, uint32_t hidden, uint32_t num_lists, uint64_t seed, rbc_router **out) {
+namespace {
+
+int create_router(uint32_t d, uint32_t hidden, uint32_t num_lists, uint32_t heads, uint64_t seed, rbc_router **out) {
   if (!out) return fail(RBC_ERR_INVALID, "rbc_router_create: out is NULL");
   *out = nullptr;
   if (d == 0 || hidden == 0 || num_lists == 0) return fail(RBC_ERR_INVALID, "rbc_router_create: zero size");
@@ -453,6 +537,7 @@ int rbc_router_create(uint32_t d, uint32_t hidden, uint32_t num_lists, uint64_t 
   r.d = d;
   r.H = hidden;
   r.L = num_lists;
+  r.T = heads;
   const size_t P = r.nparams();
   cudaError_t e = cudaMalloc(&r.w, P * 4);
   if (e == cudaSuccess) e = cudaMalloc(&r.g, P * 4);
@@ -467,6 +552,59 @@ int rbc_router_create(uint32_t d, uint32_t hidden, uint32_t num_lists, uint64_t 
   }
   *out = rt;
   return RBC_OK;
+}
+
+// Epochs of Adam over rows [0, n) in shuffled batches; the loss of the last
+// batch (mean over its rows) goes to final_loss.
+int train_loop(Router &r, const float *dQ, uint64_t n, uint32_t ldq, const uint32_t *dLabels, uint32_t epochs,
+               uint32_t batch, float lr, uint64_t seed, float *final_loss, cudaStream_t s) {
+  const uint32_t b = (uint32_t)std::min<uint64_t>(batch, n);
+  RCK(r.alloc_batch(b, s));
+  std::vector<uint32_t> order(n);
+  uint32_t *dorder = nullptr;
+  RCK(cudaMallocAsync(&dorder, n * 4, s));
+  uint64_t state = seed * 0x9E3779B97F4A7C15ull + 1;
+  auto next = [&]() {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  for (uint32_t ep = 0; ep < epochs; ep++) {
+    for (uint64_t i = 0; i < n; i++) order[i] = (uint32_t)i;
+    for (uint64_t i = n - 1; i > 0; i--) std::swap(order[i], order[next() % (i + 1)]);
+    RCK(cudaMemcpyAsync(dorder, order.data(), n * 4, cudaMemcpyHostToDevice, s));
+    RCK(cudaStreamSynchronize(s));  // order[] is reshuffled next epoch
+    const uint64_t steps = n / b;
+    for (uint64_t t = 0; t < steps; t++) {
+      RCK(r.gather(dQ, ldq, dorder + t * b, dLabels, b, s));
+      RCK(r.forward_backward(b, s));
+      RCK(r.adam_step(lr, s));
+    }
+  }
+  if (final_loss) {
+    std::vector<float> l(b);
+    RCK(cudaMemcpyAsync(l.data(), r.loss, b * 4, cudaMemcpyDeviceToHost, s));
+    RCK(cudaStreamSynchronize(s));
+    double last = 0;
+    for (float v : l) last += v;
+    *final_loss = (float)(last / b);
+  }
+  RCK(cudaFreeAsync(dorder, s));
+  RCK(cudaStreamSynchronize(s));
+  return RBC_OK;
+}
+
+}  // namespace
+
+int rbc_router_create(uint32_t d, uint32_t hidden, uint32_t num_lists, uint64_t seed, rbc_router **out) {
+  return create_router(d, hidden, num_lists, 0, seed, out);
+}
+
+int rbc_router_create_with_distance(uint32_t d, uint32_t hidden, uint32_t num_lists, uint64_t seed,
+                                    rbc_router **out) {
+  return create_router(d, hidden, num_lists, 1, seed, out);
 }
 
 int rbc_router_destroy(rbc_router *router) {
@@ -527,42 +665,142 @@ int rbc_router_train(rbc_router *router, const float *dQ, uint64_t n, uint32_t l
   if (ldq < router->r.d) return fail(RBC_ERR_INVALID, "rbc_router_train: ldq < d");
   if (n >= 0xFFFFFFFFull) return fail(RBC_ERR_INVALID, "rbc_router_train: too many samples");
   Router &r = router->r;
+  r.tau_src = nullptr;  // a distance head, if any, gets no targets here
+  return train_loop(r, dQ, n, ldq, dLabels, epochs, batch, lr, seed, final_loss, (cudaStream_t)stream);
+}
+
+int rbc_router_train_with_distance(rbc_router *router, const float *dQ, uint64_t n, uint32_t ldq,
+                                   const uint32_t *dLabels, const float *dDist, const float *dNear, uint32_t epochs,
+                                   uint32_t batch, float lr, uint64_t seed, float *final_loss, void *stream) {
+  if (!router || !dQ || !dLabels || !dDist || !dNear || n == 0 || batch == 0)
+    return fail(RBC_ERR_INVALID, "rbc_router_train_with_distance: bad argument");
+  Router &r = router->r;
+  if (!r.T) return fail(RBC_ERR_INVALID, "rbc_router_train_with_distance: the router has no distance head");
+  if (ldq < r.d) return fail(RBC_ERR_INVALID, "rbc_router_train_with_distance: ldq < d");
+  if (n >= 0xFFFFFFFFull) return fail(RBC_ERR_INVALID, "rbc_router_train_with_distance: too many samples");
   cudaStream_t s = (cudaStream_t)stream;
-  const uint32_t b = (uint32_t)std::min<uint64_t>(batch, n);
-  RCK(r.alloc_batch(b, s));
-  std::vector<uint32_t> order(n);
-  uint32_t *dorder = nullptr;
-  RCK(cudaMallocAsync(&dorder, n * 4, s));
-  uint64_t state = seed * 0x9E3779B97F4A7C15ull + 1;
-  auto next = [&]() {
-    state += 0x9E3779B97F4A7C15ull;
-    uint64_t z = state;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-  };
-  double last = 0;
-  for (uint32_t ep = 0; ep < epochs; ep++) {
-    for (uint64_t i = 0; i < n; i++) order[i] = (uint32_t)i;
-    for (uint64_t i = n - 1; i > 0; i--) std::swap(order[i], order[next() % (i + 1)]);
-    RCK(cudaMemcpyAsync(dorder, order.data(), n * 4, cudaMemcpyHostToDevice, s));
-    RCK(cudaStreamSynchronize(s));  // order[] is reshuffled next epoch
-    const uint64_t steps = n / b;
-    for (uint64_t t = 0; t < steps; t++) {
-      RCK(r.gather(dQ, ldq, dorder + t * b, dLabels, b, s));
-      RCK(r.forward_backward(b, s));
-      RCK(r.adam_step(lr, s));
+  // targets: log of each k-th distance over the nearest representative's,
+  // normalised by the mean and spread of the usable ones (both distances
+  // finite and positive; the others train the lists only)
+  std::vector<float> h(n), hn(n);
+  RCK(cudaMemcpyAsync(h.data(), dDist, n * 4, cudaMemcpyDeviceToHost, s));
+  RCK(cudaMemcpyAsync(hn.data(), dNear, n * 4, cudaMemcpyDeviceToHost, s));
+  RCK(cudaStreamSynchronize(s));
+  auto usable = [](float v) { return std::isfinite(v) && v > 0.f && v < FLT_MAX; };
+  double sum = 0, sum2 = 0;
+  uint64_t cnt = 0;
+  for (uint64_t i = 0; i < n; i++) {
+    if (usable(h[i]) && usable(hn[i])) {
+      const double l = std::log((double)h[i] / (double)hn[i]);
+      h[i] = (float)l;
+      sum += l;
+      sum2 += l * l;
+      cnt++;
+    } else {
+      h[i] = NAN;
     }
   }
-  if (final_loss) {
-    std::vector<float> l(b);
-    RCK(cudaMemcpyAsync(l.data(), r.loss, b * 4, cudaMemcpyDeviceToHost, s));
-    RCK(cudaStreamSynchronize(s));
-    for (float v : l) last += v;
-    *final_loss = (float)(last / b);
+  if (cnt == 0) return fail(RBC_ERR_INVALID, "rbc_router_train_with_distance: no finite positive distance");
+  const double mu = sum / cnt, var = std::max(sum2 / cnt - mu * mu, 1e-12);
+  r.tau_mu = (float)mu;
+  r.tau_sigma = (float)std::sqrt(var);
+  for (uint64_t i = 0; i < n; i++)
+    if (std::isfinite(h[i])) h[i] = (float)((h[i] - mu) / r.tau_sigma);
+  float *dt = nullptr;
+  RCK(cudaMallocAsync(&dt, n * 4, s));
+  RCK(cudaMemcpyAsync(dt, h.data(), n * 4, cudaMemcpyHostToDevice, s));
+  // the last 2 % of the rows are held out to calibrate the margin (all rows
+  // serve both when there are too few)
+  const uint64_t hold = n >= 1000 ? n / 50 : 0, ntrain = n - hold;
+  r.tau_src = dt;
+  int rc = train_loop(r, dQ, ntrain, ldq, dLabels, epochs, batch, lr, seed, final_loss, s);
+  r.tau_src = nullptr;
+  if (rc == RBC_OK) {
+    // margin: the 99.5th percentile of (target - prediction) over the held-out
+    // rows, predicted on the queries' own inference path
+    const uint64_t c0 = hold ? ntrain : 0, nc = hold ? hold : n;
+    float *z = nullptr;
+    uint32_t *err = nullptr, herr = 0;
+    RCK(cudaMallocAsync(&z, nc * 4, s));
+    RCK(cudaMallocAsync(&err, 4, s));
+    RCK(cudaMemsetAsync(err, 0, 4, s));
+    const float keep = r.tau_margin;
+    cudaError_t e = r.head_outputs(dQ + c0 * ldq, ldq, nc, z, err, s);
+    std::vector<float> zh(nc);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(zh.data(), z, nc * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(z, s);
+    cudaFreeAsync(err, s);
+    if (e != cudaSuccess) {
+      r.tau_margin = keep;
+      rc = cuda_fail(e, "rbc_router_train_with_distance: calibration");
+    } else if (herr) {
+      r.tau_margin = keep;
+      rc = fail(RBC_ERR_ITER_LIMIT, "rbc_router_train_with_distance: a bounded device wait ran out");
+    } else {
+      std::vector<float> res;
+      res.reserve(nc);
+      for (uint64_t i = 0; i < nc; i++)
+        if (std::isfinite(h[c0 + i])) res.push_back(h[c0 + i] - zh[i]);
+      if (res.empty()) {
+        r.tau_margin = 3.f;
+      } else {
+        std::sort(res.begin(), res.end());
+        r.tau_margin = res[std::min<size_t>(res.size() - 1, (size_t)(0.995 * res.size()))];
+      }
+    }
   }
-  RCK(cudaFreeAsync(dorder, s));
+  RCK(cudaFreeAsync(dt, s));
   RCK(cudaStreamSynchronize(s));
+  return rc;
+}
+
+int rbc_router_gradients_with_distance(rbc_router *router, const float *dQ, uint32_t batch, uint32_t ldq,
+                                       const uint32_t *dLabels, const float *dTargets, float *loss, float *h_grads,
+                                       void *stream) {
+  if (!router || !dTargets || !router->r.T)
+    return fail(RBC_ERR_INVALID, "rbc_router_gradients_with_distance: bad argument or no distance head");
+  router->r.tau_src = dTargets;
+  const int rc = rbc_router_gradients(router, dQ, batch, ldq, dLabels, loss, h_grads, stream);
+  router->r.tau_src = nullptr;
+  return rc;
+}
+
+int rbc_router_predict_distance(rbc_router *router, const float *dQ, uint64_t m, uint32_t ldq, const float *dNear,
+                                float *dDist, void *stream) {
+  if (!router || (m && (!dQ || !dDist || !dNear)))
+    return fail(RBC_ERR_INVALID, "rbc_router_predict_distance: bad argument");
+  Router &r = router->r;
+  if (!r.T) return fail(RBC_ERR_INVALID, "rbc_router_predict_distance: the router has no distance head");
+  cudaStream_t s = (cudaStream_t)stream;
+  uint32_t *err = nullptr, herr = 0;
+  RCK(cudaMallocAsync(&err, 4, s));
+  RCK(cudaMemsetAsync(err, 0, 4, s));
+  const uint32_t chunk = 1u << 20;
+  for (uint64_t i = 0; i < m; i += chunk) {
+    const uint32_t b = (uint32_t)std::min<uint64_t>(chunk, m - i);
+    RCK(r.predict_tau(dQ + i * ldq, ldq, b, dNear + i, dDist + i, err, s));
+  }
+  RCK(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s));
+  RCK(cudaFreeAsync(err, s));
+  RCK(cudaStreamSynchronize(s));
+  if (herr) return fail(RBC_ERR_ITER_LIMIT, "rbc_router_predict_distance: a bounded device wait ran out");
+  return RBC_OK;
+}
+
+int rbc_router_distance_params(const rbc_router *router, float *mu, float *sigma, float *margin) {
+  if (!router || !router->r.T) return fail(RBC_ERR_INVALID, "rbc_router_distance_params: no distance head");
+  if (mu) *mu = router->r.tau_mu;
+  if (sigma) *sigma = router->r.tau_sigma;
+  if (margin) *margin = router->r.tau_margin;
+  return RBC_OK;
+}
+
+int rbc_router_set_distance_margin(rbc_router *router, float margin) {
+  if (!router || !router->r.T || !std::isfinite(margin))
+    return fail(RBC_ERR_INVALID, "rbc_router_set_distance_margin: no distance head or bad margin");
+  router->r.tau_margin = margin;
   return RBC_OK;
 }
 

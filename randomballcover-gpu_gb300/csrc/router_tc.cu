@@ -208,12 +208,41 @@ cudaError_t Router::forward_tc(const float *Xin, uint32_t ldx, uint32_t b, float
     w1p_version = version;
   }
   const __nv_bfloat16 *W2 = wb + (size_t)H * d + H, *W3 = W2 + (size_t)H * H + H;
-  const float *b1 = w + (size_t)H * d, *b2 = b1 + H + (size_t)H * H, *b3 = b2 + H + (size_t)L * H;
+  const float *b1 = w + (size_t)H * d, *b2 = b1 + H + (size_t)H * H, *b3 = b2 + H + (size_t)(L + T) * H;
   pad_bf16_kernel<<<(unsigned)(((uint64_t)b * kp + 255) / 256), 256, 0, s>>>(Xin, ldx, b, d, kp, xb);
   if ((e = launched()) != cudaSuccess) return e;
   if ((e = gemm_tc<true, true>(xb, b, kp, w1p, H, b1, h1b, H, err, s)) != cudaSuccess) return e;
   if ((e = gemm_tc<true, true>(h1b, b, H, W2, H, b2, h2b, H, err, s)) != cudaSuccess) return e;
+  if (!zout) return cudaSuccess;  // the hidden activations alone (the distance head reads them)
   return gemm_tc<false, false>(h2b, b, H, W3, L, b3, zout, L, err, s);
+}
+
+// The distance head: zt[r] = a2[r] . W3[L] + b3[L], one warp per row over the
+// BF16 activations of the tensor-core layers.
+__global__ void head_kernel(const __nv_bfloat16 *__restrict__ a2, uint32_t b, uint32_t H,
+                            const __nv_bfloat16 *__restrict__ wrow, const float *__restrict__ bias,
+                            float *__restrict__ zt) {
+  const uint64_t r = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (r >= b) return;
+  float acc = 0.f;
+  for (uint32_t h = lane; h < H; h += 32)
+    acc = fmaf(__bfloat162float(a2[r * H + h]), __bfloat162float(wrow[h]), acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) zt[r] = acc + *bias;
+}
+
+cudaError_t Router::forward_tc_head(const float *Xin, uint32_t ldx, uint32_t b, float *zt_out, uint32_t *err,
+                                    cudaStream_t s) {
+  if (!T) return cudaErrorInvalidValue;
+  cudaError_t e = forward_tc(Xin, ldx, b, nullptr, err, s);
+  if (e != cudaSuccess) return e;
+  const __nv_bfloat16 *W3 = wb + (size_t)H * d + H + (size_t)H * H + H;
+  const float *b3 = w + (size_t)H * d + H + (size_t)H * H + H + (size_t)(L + T) * H;
+  head_kernel<<<(unsigned)(((uint64_t)b * 32 + 255) / 256), 256, 0, s>>>(h2b, b, H, W3 + (size_t)L * H, b3 + L,
+                                                                        zt_out);
+  return launched();
 }
 
 }  // namespace rbc

@@ -54,13 +54,18 @@ struct TcArgs {
   float *sl_a;              // [2][m][SL] approx distances, ascending
   uint32_t *sl_row;         // [2][m][SL] database rows (list-major index)
   uint32_t *sl_sel;         // per query: current buffer
-  uint32_t *sl_theta;       // per query: largest approx kept once SL rows are held (float bits)
+  uint32_t *sl_theta;       // per query: largest approx kept once SL rows are held, at most the
+                            // cap (float bits)
+  const uint32_t *sl_cap;   // per query: cap on sl_theta (float bits; nullptr: none)
   uint32_t *sl_lock;
   uint32_t *emax;           // per query: max error bound over the lists searched (float bits)
   uint64_t m;
   const uint64_t *offsets;  // list starts (for the work counters)
   unsigned long long *stats;  // [0] (query, row) pairs, [1] (query, list) pairs; may be null
   uint32_t *err;
+  const uint16_t *qh;           // the query operand rows (half precision), qcols halves each
+  uint32_t qcols;
+  uint32_t lsu_gather;          // 1: query tiles gathered with cp.async instead of tile::gather4
   uint32_t a_stages, b_stages;  // set by launch_tc_search from the shared-memory budget
   uint32_t stage_words;         // set by launch_tc_search: per-thread merge staging (0: none)
 };
@@ -75,6 +80,9 @@ struct RerankArgs {
   const uint32_t *sl_row;
   const uint32_t *sl_sel;
   const uint32_t *emax;
+  const uint32_t *sl_cap; // per query: the cap on the shortlist threshold (nullptr: none)
+  const uint32_t *tplan;  // per query: the threshold the plan pruned with when it was a
+                          // prediction (the k-th exact distance must not exceed it)
   uint32_t *tau;         // if set: the k-th exact distance (float bits) -> pruning threshold
   uint32_t *ids;         // if set (with dists): results and certificate
   float *dists;
@@ -163,6 +171,10 @@ int tc_build(const float *Xp, const uint32_t *perm, const uint64_t *offsets, con
 cudaError_t launch_tc_queries(const float *Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp, uint32_t format,
                               const float *mu, void *Qh, float *qscale, float *qnorm, uint8_t *q_inexact,
                               cudaStream_t s);
+// Per query: tau = min(tau, predicted) when `predicted` is given, the cap
+// tau (1 + 2^-10) on the shortlist threshold, and the threshold lowered to it.
+cudaError_t launch_cap(uint32_t *tau, const float *predicted, uint64_t m, uint32_t *cap, uint32_t *theta,
+                       cudaStream_t s);
 cudaError_t launch_sl_init(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
                            uint32_t *emax, uint64_t m, uint32_t sl, cudaStream_t s);
 // Each query's sl (<= 64) nearest representatives under (Dqr, representative

@@ -101,6 +101,11 @@ __device__ __forceinline__ float v_threshold(float theta, float dq) {
   return fminf(t, FLT_MAX);  // never +inf: masked columns carry v = +inf
 }
 
+// The query's cap on its shortlist threshold (FLT_MAX without one).
+__device__ __forceinline__ float query_cap(const TcArgs &a, uint32_t q) {
+  return a.sl_cap ? __uint_as_float(__ldg(a.sl_cap + q)) : FLT_MAX;
+}
+
 // Merge one lane's sorted candidates (nl <= kLocal entries in the owner
 // lane's registers la/li) into query q's global shortlist, with the whole
 // warp: the current
@@ -170,8 +175,8 @@ __device__ __forceinline__ float warp_publish(const TcArgs &a, uint32_t q, const
   }
   const float alast = __shfl_sync(0xffffffffu, a1, tail - 1);
   const uint32_t ilast = __shfl_sync(0xffffffffu, i1, tail - 1);
-  // FLT_MAX, not +inf, while the list is short
-  const float theta = ilast != RBC_DUMMY ? alast : FLT_MAX;
+  // FLT_MAX, not +inf, while the list is short; never above the query's cap
+  const float theta = fminf(ilast != RBC_DUMMY ? alast : FLT_MAX, query_cap(a, q));
   __threadfence();
   __syncwarp();
   if (lane == owner) {
@@ -258,8 +263,8 @@ __device__ __forceinline__ float lane_merge(const TcArgs &a, uint32_t q, const f
     reinterpret_cast<float4 *>(a.sl_a + nxt)[j] = make_float4(sa[4 * j], sa[4 * j + 1], sa[4 * j + 2], sa[4 * j + 3]);
     reinterpret_cast<uint4 *>(a.sl_row + nxt)[j] = make_uint4(sr[4 * j], sr[4 * j + 1], sr[4 * j + 2], sr[4 * j + 3]);
   }
-  // FLT_MAX, not +inf, while the list is short
-  const float theta = sr[SL - 1] != RBC_DUMMY ? sa[SL - 1] : FLT_MAX;
+  // FLT_MAX, not +inf, while the list is short; never above the query's cap
+  const float theta = fminf(sr[SL - 1] != RBC_DUMMY ? sa[SL - 1] : FLT_MAX, query_cap(a, q));
   a.sl_theta[q] = __float_as_uint(theta);
   a.sl_sel[q] = sel ^ 1u;
   unlock_release(a.sl_lock + q);  // after every store above
@@ -311,6 +316,10 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar) {
 }
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
 
 template <int MT, bool SPLIT>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -551,16 +560,38 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (ai >= AS) ok = mbar_wait(&bar_a_empty[sa], ((ai / AS) - 1) & 1, a.err);
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
-      if (lane == 0) mbar_expect_tx(&bar_a_full[sa], a_stage);
-      __syncwarp();
       unsigned char *dA = sA + sa * a_stage;
+      if (a.lsu_gather) {
+        // 16-byte copies, eight consecutive lanes on one row's 128 bytes of a
+        // K block (coalesced), each chunk written where the 128-byte swizzle
+        // of the MMA descriptor reads it (chunk c of row j at c ^ (j & 7));
+        // the query of each row comes from the row states just staged (rows
+        // past the item's queries read the zero row); the copies land before
+        // the generic -> async proxy fence and the arrival that hands the
+        // stage to the MMA warp
+        const uint32_t total = MT * kBM * kbh * 8;
+        for (uint32_t i = lane; i < total; i += 32) {
+          const uint32_t c = i & 7u, rk = i >> 3, k = rk % kbh, rowg = rk / kbh;
+          const uint32_t g = rowg >> 7, j = rowg & (kBM - 1);
+          const uint32_t q = rowg < item.nq ? (FOLD ? dstf[rowg].q : dst[rowg].q) : a.zero_row;
+          const uint16_t *src = a.qh + (uint64_t)q * a.qcols + k * 64 + c * 8;
+          cp_async16(dA + g * a_tile + k * kTile16K + j * 128 + ((c ^ (j & 7u)) << 4), src);
+        }
+        cp_async_wait_all();
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bar_a_full[sa]);
+      } else {
+        if (lane == 0) mbar_expect_tx(&bar_a_full[sa], a_stage);
+        __syncwarp();
 #pragma unroll
-      for (int g = 0; g < MT; g++)
-        for (uint32_t k = 0; k < kbh; k++)
-          tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
-                      rr[g][2], rr[g][3], &bar_a_full[sa]);
+        for (int g = 0; g < MT; g++)
+          for (uint32_t k = 0; k < kbh; k++)
+            tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
+                        rr[g][2], rr[g][3], &bar_a_full[sa]);
+      }
     }
-    if (lane == 0) {
+    if (lane == 0 && !a.lsu_gather) {
       // drain: wait (bounded) for the gathers still in flight before leaving
       for (uint32_t j = 0; j < AS && j < ai; j++) {
         const uint32_t i = ai - 1 - j;
@@ -683,14 +714,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             tmem_ld64(taddr + c * CW, *reinterpret_cast<uint32_t(*)[64]>(r));
           }
           tmem_wait_ld();
-          if (c == kBN / CW - 1) {
-            // the tile's last accumulator read is in registers: the slot goes
-            // back to the MMA warp before this chunk's candidates (and any
-            // shortlist merge) are handled
+          // the slot goes back (to the MMA warp and, in the split format, to
+          // warp 2, which then restages its row constants) once the tile's
+          // last accumulator read is in registers and -- split format -- its
+          // row constants have been read, before this chunk's candidates (and
+          // any shortlist merge) are handled
+          const bool last = c == kBN / CW - 1;
+          auto release_slot = [&]() {
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&bar_t_empty[slot]);
-          }
+          };
+          if (FOLD && last) release_slot();
           if (FOLD) {
             if (valid < kBN) {
 #pragma unroll
@@ -719,6 +754,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               mn = fminf(mn, fminf(fminf(__uint_as_float(r[4 * j4]), __uint_as_float(r[4 * j4 + 1])),
                                    fminf(__uint_as_float(r[4 * j4 + 2]), __uint_as_float(r[4 * j4 + 3]))));
             }
+            if (last) release_slot();
             if (!__any_sync(0xffffffffu, mn <= thv)) continue;
           }
           // candidates, 32 columns at a time: the values go to a per-thread copy
@@ -1116,6 +1152,27 @@ __global__ void rep_seed_kernel(const float *__restrict__ Dqr, uint64_t m, uint3
   }
 }
 
+// Per query: the planning threshold tau = min(tau, predicted) when a
+// prediction is given (the speculative plan), then the shortlist cap
+// tau (1 + 2^-10) and the shortlist threshold lowered to it.  A row whose
+// approx exceeds the cap cannot reach the top k once the final k-th distance
+// is at most tau and the error bound at most 2^-10 tau; the certificate
+// checks both.
+__global__ void cap_kernel(uint32_t *__restrict__ tau, const float *__restrict__ predicted, uint64_t m,
+                           uint32_t *__restrict__ cap, uint32_t *__restrict__ theta) {
+  const uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (q >= m) return;
+  float t = __uint_as_float(tau[q]);
+  if (predicted) {
+    const float p = predicted[q];
+    if (p >= 0.f && p < t) t = p;  // a NaN or negative prediction is ignored
+    tau[q] = __float_as_uint(t);
+  }
+  const float c = t < FLT_MAX ? fminf(__fmul_ru(t, 1.0009765625f), FLT_MAX) : FLT_MAX;
+  cap[q] = __float_as_uint(c);
+  theta[q] = __float_as_uint(fminf(__uint_as_float(theta[q]), c));
+}
+
 __global__ void iperm_kernel(const uint32_t *__restrict__ perm, uint64_t n, uint32_t *__restrict__ iperm) {
   const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (p < n) iperm[perm[p]] = (uint32_t)p;
@@ -1171,13 +1228,18 @@ __global__ void rerank_kernel(RerankArgs a) {
   if (a.tau && lane == 0) atomicMin(a.tau + q, fbits(kth));
   if (!a.ids && !a.dists) return;
   // certificate: every row searched but not in the shortlist has approx >=
-  // a_last, so its exact distance is >= a_last - E > kth when certified
+  // T = min(cap, a_last) (a_last only when the shortlist is full: otherwise
+  // only the cap turned rows away), so its exact distance is >= T - E > kth
+  // when certified; rows of pruned lists are beyond the plan's threshold,
+  // which must then be at least kth
   bool certified = true;
-  if (valid == a.sl) {
-    const double a_last = (double)sa_q[a.sl - 1];
+  const float cap = a.sl_cap ? __uint_as_float(a.sl_cap[q]) : FLT_MAX;
+  const float T = valid == a.sl ? fminf(sa_q[a.sl - 1], cap) : cap;
+  if (T < FLT_MAX) {
     const double E = (double)__uint_as_float(a.emax[q]);
-    certified = a_last - E > (double)kth;
+    certified = (double)T - E > (double)kth;
   }
+  if (a.tplan && !(kth <= __uint_as_float(a.tplan[q]))) certified = false;
   if (lane < (int)a.k) {
     if (a.ids) a.ids[q * a.ldo + lane] = li;
     if (a.dists) a.dists[q * a.ldo + lane] = ld;
@@ -1357,6 +1419,13 @@ cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t k
   if (m == 0) return cudaSuccess;
   sl_seed_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(res_d, res_i, kw, iperm, seed_a, seed_row, m, sl, k,
                                                             sl_a, sl_row, theta, tau);
+  return launched();
+}
+
+cudaError_t launch_cap(uint32_t *tau, const float *predicted, uint64_t m, uint32_t *cap, uint32_t *theta,
+                       cudaStream_t s) {
+  if (m == 0) return cudaSuccess;
+  cap_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(tau, predicted, m, cap, theta);
   return launched();
 }
 

@@ -131,9 +131,11 @@ int rbc_autotune(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint
 
 int rbc_set_tc_tuning(rbc_index *idx, uint32_t probes, uint64_t probe_rows) {
   if (!idx) return fail(RBC_ERR_INVALID, "rbc_set_tc_tuning: NULL index");
-  if (probes > 8) return fail(RBC_ERR_INVALID, "rbc_set_tc_tuning: probes must be at most 8");
+  if (probes > 8 && probes != RBC_TC_ROUTER_ONLY)
+    return fail(RBC_ERR_INVALID, "rbc_set_tc_tuning: probes must be at most 8 (or RBC_TC_ROUTER_ONLY)");
   idx->tc_probes = probes;
   idx->tc_probe_rows = probe_rows;
+  idx->tc_plain = false;
   return RBC_OK;
 }
 
@@ -164,7 +166,10 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   uint32_t best_p = 0;
   uint64_t best_rows = 0;
   int rc = RBC_OK;
-  for (uint32_t p : {1u, 2u, 4u, 8u}) {
+  idx->tc_plain = false;
+  const bool routed = (mode & RBC_QUERY_ROUTED) && idx->router;
+  for (uint32_t p : {RBC_TC_ROUTER_ONLY, 1u, 2u, 4u, 8u}) {
+    if (p == RBC_TC_ROUTER_ONLY && !routed) continue;  // the router's picks alone: routed calls only
     for (uint64_t r : {2048ull, 8192ull, 32768ull}) {
       idx->tc_probes = p;
       idx->tc_probe_rows = r;
@@ -187,6 +192,19 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
     }
     if (rc != RBC_OK) break;
   }
+  // the plain FP32 search on the same lists, same routing: when it is the
+  // faster of the two, RBC_QUERY_EXACT_TC calls run it
+  double plain = 1e30;
+  for (int rep = 0; rep < 3 && rc == RBC_OK; rep++) {
+    cudaEventRecord(e0, s);
+    rc = query_index(idx, dQ, m, ldq, k, (mode & ~0xFFu) | RBC_QUERY_EXACT, ids.as<uint32_t>(), dists.as<float>(), k,
+                     s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep) plain = std::min(plain, (double)ms);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   idx->profile = keep_profile;
@@ -194,6 +212,7 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   if (rc != RBC_OK) return rc;
   idx->tc_probes = best_p;
   idx->tc_probe_rows = best_rows;
+  idx->tc_plain = plain < best;
   return RBC_OK;
 }
 

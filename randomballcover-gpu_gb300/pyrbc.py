@@ -21,6 +21,7 @@ K_LIMIT = 128  # largest k of query / brute_knn (KMAX for batches and the no-all
 BUILD_PARTITION, BUILD_ONESHOT, BUILD_BF16, BUILD_F64 = 1, 2, 4, 8
 QUERY_EXACT, QUERY_ONESHOT, QUERY_EXACT_TC = 0, 1, 2
 TC_BF16, TC_FP16_SPLIT = 0, 1
+TC_ROUTER_ONLY = 0xFF  # tensor-form probes: the router's picks alone (routed calls)
 QUERY_ROUTED = 0x1000
 SYNTH_UNIFORM, SYNTH_MIXTURE, SYNTH_GEOMETRIC = 0, 1, 2
 DUMMY = 0xFFFFFFFF
@@ -41,7 +42,8 @@ class BuildParams(C.Structure):
 class IndexInfo(C.Structure):
     _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("ld", C.c_uint32), ("num_reps", C.c_uint32),
                 ("s", C.c_uint32), ("metric", C.c_int), ("flags", C.c_uint32), ("min_list", C.c_uint64),
-                ("max_list", C.c_uint64), ("device_bytes", C.c_uint64), ("tc_format", C.c_uint32)]
+                ("max_list", C.c_uint64), ("device_bytes", C.c_uint64), ("tc_format", C.c_uint32),
+                ("tc_plain", C.c_uint32)]
 
 
 class QueryStats(C.Structure):
@@ -90,6 +92,14 @@ SIGNATURES = {
     "rbc_router_train": ([_VP, _VP, _U64, _U32, _VP, _U32, _U32, _F, _U64, C.POINTER(_F), _VP], _INT),
     "rbc_router_logits": ([_VP, _VP, _U64, _U32, _VP, _VP], _INT),
     "rbc_owner_labels": ([_VP, _VP, _U64, _U32, _VP, _VP], _INT),
+    "rbc_router_create_with_distance": ([_U32, _U32, _U32, _U64, C.POINTER(_VP)], _INT),
+    "rbc_router_labels": ([_VP, _VP, _U64, _U32, _U32, _VP, _VP, _VP, _VP], _INT),
+    "rbc_router_train_with_distance": ([_VP, _VP, _U64, _U32, _VP, _VP, _VP, _U32, _U32, _F, _U64, C.POINTER(_F),
+                                        _VP], _INT),
+    "rbc_router_gradients_with_distance": ([_VP, _VP, _U32, _U32, _VP, _VP, C.POINTER(_F), _VP, _VP], _INT),
+    "rbc_router_predict_distance": ([_VP, _VP, _U64, _U32, _VP, _VP, _VP], _INT),
+    "rbc_router_distance_params": ([_VP, C.POINTER(_F), C.POINTER(_F), C.POINTER(_F)], _INT),
+    "rbc_router_set_distance_margin": ([_VP, _F], _INT),
     "rbc_set_router": ([_VP, _VP, _U32], _INT),
     "rbc_set_profiling": ([_VP, _INT], _INT),
     "rbc_get_profile": ([_VP, C.POINTER(Profile)], _INT),
@@ -292,6 +302,19 @@ class Index:
         check(lib().rbc_owner_labels(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), lab.data_ptr(), _stream(stream)))
         return lab
 
+    def router_labels(self, Q, k, stream=None):
+        """Labels for both router heads: the list owning each query's exact
+        nearest neighbour, the query's exact k-th distance and its nearest
+        representative's distance."""
+        import torch
+        Q = _dev(Q, torch.float32)
+        lab = torch.empty(Q.shape[0], dtype=torch.int32, device=Q.device)
+        dist = torch.empty(Q.shape[0], dtype=torch.float32, device=Q.device)
+        near = torch.empty(Q.shape[0], dtype=torch.float32, device=Q.device)
+        check(lib().rbc_router_labels(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), k, lab.data_ptr(),
+                                      dist.data_ptr(), near.data_ptr(), _stream(stream)))
+        return lab, dist, near
+
     def set_tuning(self, tq=0, item_rows=0):
         check(lib().rbc_set_tuning(self.h, tq, item_rows))
 
@@ -364,11 +387,13 @@ class Batch:
 class Router:
     """The learned list router (MLP d -> hidden -> hidden -> lists, GELU)."""
 
-    def __init__(self, d, hidden, num_lists, seed=0):
+    def __init__(self, d, hidden, num_lists, seed=0, distance_head=False):
         h = C.c_void_p()
-        check(lib().rbc_router_create(d, hidden, num_lists, seed, C.byref(h)))
+        create = lib().rbc_router_create_with_distance if distance_head else lib().rbc_router_create
+        check(create(d, hidden, num_lists, seed, C.byref(h)))
         self.h = h
         self.d, self.hidden, self.num_lists = d, hidden, num_lists
+        self.distance_head = distance_head
 
     def close(self):
         if getattr(self, "h", None):
@@ -417,6 +442,49 @@ class Router:
         check(lib().rbc_router_logits(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), out.data_ptr(),
                                       _stream(stream)))
         return out
+
+    def gradients_with_distance(self, Q, labels, targets, stream=None):
+        """Loss and gradients of one batch with both heads (targets in the
+        distance head's normalised units, NaN for none)."""
+        import torch
+        Q = _dev(Q, torch.float32)
+        lab = _dev(np.asarray(labels, np.int32) if isinstance(labels, np.ndarray) else labels, torch.int32)
+        tg = _dev(np.asarray(targets, np.float32) if isinstance(targets, np.ndarray) else targets, torch.float32)
+        g = np.empty(self.num_params(), np.float32)
+        loss = C.c_float()
+        check(lib().rbc_router_gradients_with_distance(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), lab.data_ptr(),
+                                                       tg.data_ptr(), C.byref(loss), g.ctypes.data, _stream(stream)))
+        return loss.value, g
+
+    def train_with_distance(self, Q, labels, dist, near, epochs=1, batch=1024, lr=1e-3, seed=0, stream=None):
+        import torch
+        Q = _dev(Q, torch.float32)
+        lab = _dev(labels, torch.int32)
+        dd = _dev(dist, torch.float32)
+        nn = _dev(near, torch.float32)
+        loss = C.c_float()
+        check(lib().rbc_router_train_with_distance(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), lab.data_ptr(),
+                                                   dd.data_ptr(), nn.data_ptr(), epochs, batch, lr, seed,
+                                                   C.byref(loss), _stream(stream)))
+        return loss.value
+
+    def predict_distance(self, Q, near, stream=None):
+        import torch
+        Q = _dev(Q, torch.float32)
+        nn = _dev(near, torch.float32)
+        out = torch.empty(Q.shape[0], dtype=torch.float32, device=Q.device)
+        check(lib().rbc_router_predict_distance(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), nn.data_ptr(),
+                                                out.data_ptr(), _stream(stream)))
+        return out
+
+    def distance_params(self):
+        """(mu, sigma, margin): log(distance / nearest representative's) = mu + sigma (head output + margin)."""
+        mu, sg, mg = C.c_float(), C.c_float(), C.c_float()
+        check(lib().rbc_router_distance_params(self.h, C.byref(mu), C.byref(sg), C.byref(mg)))
+        return mu.value, sg.value, mg.value
+
+    def set_distance_margin(self, margin):
+        check(lib().rbc_router_set_distance_margin(self.h, float(margin)))
 
 
 def brute_knn_f64(X, Q, k, metric=L2, stream=None):

@@ -186,6 +186,27 @@ def test_c1_full_size_every_form_equals_oracle(rbc, oracle):
     idx.close()
 
 
+def test_tensor_form_repeated_calls_stay_exact(rbc, oracle):
+    """The split operand format at the first configuration's shape, k = 32,
+    30 calls in a row: every answer of every call equals the oracle's.  (A
+    race between the epilogue's last read of a tile's row constants and
+    their restaging for a later tile once dropped about one neighbour in
+    10^5 answers here; one call rarely shows it, thirty usually do.)"""
+    n, m, d, nr = 65536, 8192, 16, 256
+    X = rbc.synth(0, 1, 0, n, d)
+    Q = rbc.synth(0, 1, 1, m, d)
+    idx = rbc.Index(X, nr, seed=1, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    assert idx.info()["tc_format"] == rbc.TC_FP16_SPLIT
+    ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), 32)
+    wrong = 0
+    for _ in range(30):
+        ids, dists = idx.query(Q, 32, mode=rbc.QUERY_EXACT_TC)
+        wrong += int((rbc.u32(ids) != ri).any(1).sum())
+    assert wrong == 0, wrong
+    np.testing.assert_array_equal(dists.cpu().numpy(), rd)
+    idx.close()
+
+
 def test_fallback_queries_are_reported_and_exact(rbc, oracle):
     """The queries the tensor form's certificate leaves open are listed by
     rbc_get_fallback_queries (as many as the stats count) and their answers,
@@ -373,9 +394,34 @@ def test_tensor_core_autotune(rbc, oracle):
     ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
     assert_same(ids, dists, ri, rd, rbc)
     idx.set_tc_tuning()
-    assert idx.tc_tuning() == (0, 0)
+    assert idx.tc_tuning() == (0, 0) and idx.info()["tc_plain"] == 0
     with pytest.raises(rbc.RBCError):
         idx.set_tc_tuning(9, 0)
+    idx.close()
+
+
+def test_autotune_can_choose_the_plain_form(rbc, oracle):
+    """At d = 16 with lists of ~250 rows (the first benchmark configuration's
+    shape, smaller) the tuner also times the plain FP32 search; whichever it
+    keeps, RBC_QUERY_EXACT_TC answers stay the oracle's, the choice shows in
+    info()["tc_plain"], and setting the tensor knobs selects the tensor form
+    again."""
+    X = rbc.synth(0, 1, 0, 65536, 16)
+    Q = rbc.synth(0, 1, 1, 2000, 16)
+    Qt = rbc.synth(0, 1, 3, 2000, 16)
+    idx = rbc.Index(X, 256, seed=1, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    idx.autotune_tc(Qt, 1)
+    chose_plain = idx.info()["tc_plain"]
+    assert chose_plain in (0, 1)
+    ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), 1)
+    ids, dists = idx.query(Q, 1, mode=rbc.QUERY_EXACT_TC)
+    assert_same(ids, dists, ri, rd, rbc)
+    if chose_plain:
+        assert idx.stats()["fallback_queries"] == 0 and len(idx.fallback_queries()) == 0
+    idx.set_tc_tuning(2, 2048)
+    assert idx.info()["tc_plain"] == 0
+    ids, dists = idx.query(Q, 1, mode=rbc.QUERY_EXACT_TC)
+    assert_same(ids, dists, ri, rd, rbc)
     idx.close()
 
 

@@ -7,7 +7,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, ROOT, load_golden
+from conftest import GOLDEN, ROOT, load_golden, sample_inputs
 
 INCLUDE = os.path.join(ROOT, "include")
 REF_SRC = __import__("oracle").ref_dir()  # the reference's sources, where this machine has them
