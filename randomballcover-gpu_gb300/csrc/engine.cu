@@ -581,8 +581,6 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   uint64_t probe_rows = idx->tc_probe_rows ? idx->tc_probe_rows : kTcProbeRows;
   if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) probe_rows = std::strtoull(env, nullptr, 10);
   const uint32_t qtile = tc_query_tile(fmt);
-  uint32_t lsu_gather = 1;
-  if (const char *env = std::getenv("RBC_TC_GATHER")) lsu_gather = std::strcmp(env, "tma") != 0;
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
   const uint64_t probe_per_list = mb * P / nr;
   const int ptq = search_tq_for(idx->dp, probe_per_list >= 48 ? 4 : (probe_per_list >= 24 ? 2 : 1), kw);
@@ -721,9 +719,6 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     ta.sl_lock = sl_lock.as<uint32_t>();
     ta.emax = emax.as<uint32_t>();
     ta.m = mq;
-    ta.qh = static_cast<const uint16_t *>(Qh.p);
-    ta.qcols = cols;
-    ta.lsu_gather = lsu_gather;
     ta.offsets = idx->offsets;
     ta.stats = stats.as<unsigned long long>();
     ta.err = ctl.as<uint32_t>();

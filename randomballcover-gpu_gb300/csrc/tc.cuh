@@ -63,9 +63,6 @@ struct TcArgs {
   const uint64_t *offsets;  // list starts (for the work counters)
   unsigned long long *stats;  // [0] (query, row) pairs, [1] (query, list) pairs; may be null
   uint32_t *err;
-  const uint16_t *qh;           // the query operand rows (half precision), qcols halves each
-  uint32_t qcols;
-  uint32_t lsu_gather;          // 1: query tiles gathered with cp.async instead of tile::gather4
   uint32_t a_stages, b_stages;  // set by launch_tc_search from the shared-memory budget
   uint32_t stage_words;         // set by launch_tc_search: per-thread merge staging (0: none)
 };

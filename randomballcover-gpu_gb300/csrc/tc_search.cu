@@ -317,9 +317,6 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar) {
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
-}
 
 template <int MT, bool SPLIT>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -561,37 +558,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
       unsigned char *dA = sA + sa * a_stage;
-      if (a.lsu_gather) {
-        // 16-byte copies, eight consecutive lanes on one row's 128 bytes of a
-        // K block (coalesced), each chunk written where the 128-byte swizzle
-        // of the MMA descriptor reads it (chunk c of row j at c ^ (j & 7));
-        // the query of each row comes from the row states just staged (rows
-        // past the item's queries read the zero row); the copies land before
-        // the generic -> async proxy fence and the arrival that hands the
-        // stage to the MMA warp
-        const uint32_t total = MT * kBM * kbh * 8;
-        for (uint32_t i = lane; i < total; i += 32) {
-          const uint32_t c = i & 7u, rk = i >> 3, k = rk % kbh, rowg = rk / kbh;
-          const uint32_t g = rowg >> 7, j = rowg & (kBM - 1);
-          const uint32_t q = rowg < item.nq ? (FOLD ? dstf[rowg].q : dst[rowg].q) : a.zero_row;
-          const uint16_t *src = a.qh + (uint64_t)q * a.qcols + k * 64 + c * 8;
-          cp_async16(dA + g * a_tile + k * kTile16K + j * 128 + ((c ^ (j & 7u)) << 4), src);
-        }
-        cp_async_wait_all();
-        fence_proxy_async();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&bar_a_full[sa]);
-      } else {
-        if (lane == 0) mbar_expect_tx(&bar_a_full[sa], a_stage);
-        __syncwarp();
+      if (lane == 0) mbar_expect_tx(&bar_a_full[sa], a_stage);
+      __syncwarp();
 #pragma unroll
-        for (int g = 0; g < MT; g++)
-          for (uint32_t k = 0; k < kbh; k++)
-            tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
-                        rr[g][2], rr[g][3], &bar_a_full[sa]);
-      }
+      for (int g = 0; g < MT; g++)
+        for (uint32_t k = 0; k < kbh; k++)
+          tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
+                      rr[g][2], rr[g][3], &bar_a_full[sa]);
     }
-    if (lane == 0 && !a.lsu_gather) {
+    if (lane == 0) {
       // drain: wait (bounded) for the gathers still in flight before leaving
       for (uint32_t j = 0; j < AS && j < ai; j++) {
         const uint32_t i = ai - 1 - j;
