@@ -91,8 +91,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-side", action="store_true",
                     help="skip the c2 side measurements (k = 128 and the double-precision variant)")
-    ap.add_argument("--router-probes", type=int, default=0,
-                    help="lists the learned form probes from the router (0: none, the distance head plans instead)")
+    ap.add_argument("--router-probes", type=int, default=2,
+                    help="lists the learned form probes from the router (the tuner then tries 1 and 2; "
+                         "0: none, the distance head plans instead)")
     ap.add_argument("--forms", default=None,
                     help="forms to time; the last one listed is the headline (default: per workload)")
     ap.add_argument("--tc-tuning", default=None, metavar="PROBES,ROWS",
@@ -424,7 +425,9 @@ def run_engine(a):
                                          "margin_sigma_units": margin, "log_ratio_sigma": sg},
                        "architecture": f"MLP {w['d']}->512->512->{w['reps']} (+1 distance output) GELU, "
                                        "BF16 weights, FP32 accumulate"}
-        # probes = 0: no probe round; the predicted k-th distance plans the search
+        # the router's picks join the probe round (the tuner chooses one or two
+        # and whether the nearest representatives' lists come too); with
+        # --router-probes 0 the predicted k-th distance plans the search instead
         idx.set_router(router, probes=a.router_probes)
 
     modes = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC, "oneshot": pyrbc.QUERY_ONESHOT,
@@ -444,7 +447,10 @@ def run_engine(a):
                 idx.set_tc_tuning(*(int(v) for v in a.tc_tuning.split(",")))
             else:
                 idx.autotune_tc(Qtune, k, mode)
-            tuning[mode] = list(idx.tc_tuning()) + (["plain FP32 search chosen"] if idx.info()["tc_plain"] else [])
+            inf = idx.info()
+            tuning[mode] = list(idx.tc_tuning()) + (["plain FP32 search chosen"] if inf["tc_plain"] else [])
+            if mode & pyrbc.QUERY_ROUTED:
+                tuning[mode].append(f"router picks {inf['router_picks']}")
         for _ in range(warmup):
             idx.query(Q, k, mode=mode, out=(ids, dists))
         barrier()
@@ -570,8 +576,8 @@ def run_engine(a):
     if rank == 0:
         names = {"plain": "plain FP32 exact RBC", "tensor": "exact RBC, BF16 tcgen05 list search + FP32 rerank",
                  "oneshot": "the reference's one-shot RBC (approximate)",
-                 "learned": "exact RBC, learned router (its predicted k-th distance plans the search) + BF16 "
-                            "tcgen05 list search + FP32 rerank",
+                 "learned": "exact RBC, learned router (its picks in the probe round) + BF16 tcgen05 list search "
+                            "+ FP32 rerank",
                  "learned_plain": "exact RBC, learned router + FP32 list search"}
         extra = {"build_s": build_s, "min_list": info["min_list"], "max_list": info["max_list"],
                  "tc_format": ["bf16", "fp16_split"][info["tc_format"]], "same_ids_all_exact_forms": same,

@@ -100,6 +100,7 @@ typedef struct {
   uint32_t tc_plain;           /* 1: rbc_autotune_tc found the plain FP32
                                   search faster, and RBC_QUERY_EXACT_TC
                                   calls run it                          */
+  uint32_t router_picks;       /* lists routed calls take from the router */
 } rbc_index_info;
 
 typedef struct {               /* work done by the last rbc_query on an index */
@@ -190,7 +191,9 @@ int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, ui
  * rbc_autotune_tc times 1, 2, 4, 8 probes (and RBC_TC_ROUTER_ONLY in routed
  * mode) x 2048, 8192, 32768 rows on sample
  * queries in the given mode (RBC_QUERY_EXACT_TC, optionally
- * | RBC_QUERY_ROUTED) and keeps the fastest; it also times the plain FP32
+ * | RBC_QUERY_ROUTED, where it also tries one and two router picks when
+ * the router was attached with picks) and keeps the fastest; it also times
+ * the plain FP32
  * search (RBC_QUERY_EXACT with the same routing) and, when that is faster,
  * makes RBC_QUERY_EXACT_TC calls on this index run it (info.tc_plain).
  * rbc_set_tc_tuning selects the tensor form again.  Results never change. */
@@ -223,6 +226,13 @@ int rbc_router_train(rbc_router *router, const float *dQ, uint64_t n, uint32_t l
  * multiple of 64, else the training kernels' FP32-activation forward. */
 int rbc_router_logits(rbc_router *router, const float *dQ, uint64_t m, uint32_t ldq, float *dLogits,
                       void *stream);
+/* The router's P (1..16) most likely lists per query, largest logit first,
+ * ties to the lower list: m x P into dLists -- the picks routed queries
+ * probe.  With hidden a multiple of 64 and at most 512 the last layer runs
+ * fused with the selection on the tensor cores (no logits are formed in
+ * memory). */
+int rbc_router_top_lists(rbc_router *router, const float *dQ, uint64_t m, uint32_t ldq, uint32_t P,
+                         uint32_t *dLists, void *stream);
 /* Training labels produced by the RBC: the list owning each query's exact
  * nearest neighbour. */
 int rbc_owner_labels(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t *dLabels,

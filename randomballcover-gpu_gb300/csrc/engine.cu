@@ -474,7 +474,7 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   if (routed) {
     CK(near.alloc(mb * Pn * 4, s));
     CK(near_d.alloc(mb * Pn * 4, s));
-    CK(logits.alloc(mb * nr * 4, s));
+    if (!idx->router->r.top_ok(P)) CK(logits.alloc(mb * nr * 4, s));
   }
   CK(stats.alloc(2 * sizeof(unsigned long long), s));
   CK(cudaMemsetAsync(stats.p, 0, 2 * sizeof(unsigned long long), s));
@@ -487,18 +487,24 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     if (routed) {
       CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, Pn, near.as<uint32_t>(), near_d.as<float>(), s));
       Router &rt = idx->router->r;
-      if (rt.tc_ok()) {
-        CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
+      if (rt.top_ok(P)) {
+        // the last layer fused with the selection: no logits written
+        CK(rt.probes_tc(b.Qp.as<float>(), ld, (uint32_t)mq, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
+                        b.probe.as<uint32_t>(), b.probed.as<float>(), b.ctl.as<uint32_t>() + 2, s));
       } else {
-        const uint32_t chunk = 4096;
-        CK(rt.alloc_batch(chunk, s));
-        for (uint64_t i = 0; i < mq; i += chunk) {
-          const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
-          CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+        if (rt.tc_ok()) {
+          CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
+        } else {
+          const uint32_t chunk = 4096;
+          CK(rt.alloc_batch(chunk, s));
+          for (uint64_t i = 0; i < mq; i += chunk) {
+            const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
+            CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+          }
         }
+        CK(launch_router_probes(logits.as<float>(), mq, nr, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
+                                b.probe.as<uint32_t>(), b.probed.as<float>(), s));
       }
-      CK(launch_router_probes(logits.as<float>(), mq, nr, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
-                              b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     } else {
       CK(launch_row_topp(b.Dqr.as<float>(), mq, nr, P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     }
@@ -618,7 +624,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   } else if (routed) {
     CK(near.alloc(mb * Pnear * 4, s));
     CK(near_d.alloc(mb * Pnear * 4, s));
-    CK(logits.alloc(mb * nr * 4, s));
+    if (!idx->router->r.top_ok(P)) CK(logits.alloc(mb * nr * 4, s));
     // without nearest lists in the probe table the pruning bound takes the
     // nearest representative's distance from here
     if (Pn == 0) b.dq0 = near_d.as<float>();
@@ -663,18 +669,24 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(),
                          seed_row.as<uint32_t>(), Pnear, near.as<uint32_t>(), near_d.as<float>(), s));
       Router &rt = idx->router->r;
-      if (rt.tc_ok()) {
-        CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
+      if (rt.top_ok(P)) {
+        // the last layer fused with the selection: no logits written
+        CK(rt.probes_tc(b.Qp.as<float>(), ld, (uint32_t)mq, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
+                        b.probe.as<uint32_t>(), b.probed.as<float>(), b.ctl.as<uint32_t>() + 2, s));
       } else {
-        const uint32_t chunk = 4096;
-        CK(rt.alloc_batch(chunk, s));
-        for (uint64_t i = 0; i < mq; i += chunk) {
-          const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
-          CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+        if (rt.tc_ok()) {
+          CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
+        } else {
+          const uint32_t chunk = 4096;
+          CK(rt.alloc_batch(chunk, s));
+          for (uint64_t i = 0; i < mq; i += chunk) {
+            const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
+            CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
+          }
         }
+        CK(launch_router_probes(logits.as<float>(), mq, nr, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
+                                b.probe.as<uint32_t>(), b.probed.as<float>(), s));
       }
-      CK(launch_router_probes(logits.as<float>(), mq, nr, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
-                              b.probe.as<uint32_t>(), b.probed.as<float>(), s));
     } else {
       CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(),
                          seed_row.as<uint32_t>(), P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
@@ -1026,6 +1038,7 @@ int rbc_get_info(const rbc_index *idx, rbc_index_info *info) {
   info->device_bytes = idx->device_bytes;
   info->tc_format = idx->tc.format;
   info->tc_plain = idx->tc_plain ? 1u : 0u;
+  info->router_picks = idx->router ? idx->router_probes : 0u;
   return RBC_OK;
 }
 

@@ -789,6 +789,49 @@ int rbc_router_predict_distance(rbc_router *router, const float *dQ, uint64_t m,
   return RBC_OK;
 }
 
+int rbc_router_top_lists(rbc_router *router, const float *dQ, uint64_t m, uint32_t ldq, uint32_t P, uint32_t *dLists,
+                         void *stream) {
+  if (!router || (m && (!dQ || !dLists)) || P < 1 || P > 16)
+    return fail(RBC_ERR_INVALID, "rbc_router_top_lists: bad argument (P in [1, 16])");
+  Router &r = router->r;
+  if (ldq < r.d) return fail(RBC_ERR_INVALID, "rbc_router_top_lists: ldq < d");
+  if (m == 0) return RBC_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  uint32_t *err = nullptr, herr = 0;
+  float *scratch = nullptr;
+  const bool fused = r.top_ok(P);
+  const uint32_t chunk = fused ? (1u << 18) : 8192;
+  const size_t per = fused ? P : (size_t)P + r.L;  // probed distances (+ logits)
+  RCK(cudaMallocAsync(&err, 4, s));
+  RCK(cudaMemsetAsync(err, 0, 4, s));
+  RCK(cudaMallocAsync(&scratch, (size_t)std::min<uint64_t>(chunk, m) * per * 4, s));
+  cudaError_t e = cudaSuccess;
+  for (uint64_t i = 0; i < m && e == cudaSuccess; i += chunk) {
+    const uint32_t b = (uint32_t)std::min<uint64_t>(chunk, m - i);
+    if (fused) {
+      e = r.probes_tc(dQ + i * ldq, ldq, b, P, 0, nullptr, nullptr, dLists + i * P, scratch, err, s);
+    } else {
+      float *logits = scratch + (size_t)std::min<uint64_t>(chunk, m) * P;
+      if (r.tc_ok()) {
+        e = r.forward_tc(dQ + i * ldq, ldq, b, logits, err, s);
+      } else {
+        e = r.alloc_batch(std::min<uint32_t>(b, 4096), s);
+        for (uint32_t j = 0; j < b && e == cudaSuccess; j += 4096)
+          e = r.forward(dQ + (i + j) * ldq, ldq, std::min<uint32_t>(4096, b - j), logits + (size_t)j * r.L, s);
+      }
+      if (e == cudaSuccess)
+        e = launch_router_probes(logits, b, r.L, P, 0, nullptr, nullptr, dLists + i * P, scratch, s);
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(scratch, s);
+  cudaFreeAsync(err, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "rbc_router_top_lists");
+  if (herr) return fail(RBC_ERR_ITER_LIMIT, "rbc_router_top_lists: a bounded device wait ran out");
+  return RBC_OK;
+}
+
 int rbc_router_distance_params(const rbc_router *router, float *mu, float *sigma, float *margin) {
   if (!router || !router->r.T) return fail(RBC_ERR_INVALID, "rbc_router_distance_params: no distance head");
   if (mu) *mu = router->r.tau_mu;

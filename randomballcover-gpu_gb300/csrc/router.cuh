@@ -43,6 +43,11 @@ struct Router {
   __nv_bfloat16 *xb = nullptr, *h1b = nullptr, *h2b = nullptr, *w1p = nullptr;
   uint64_t w1p_version = ~0ull;
   bool tc_ok() const;
+  // the probe table straight from the hidden activations (the last layer
+  // fused with the top-P selection, no logits written): when top_ok(P + Pn)
+  bool top_ok(uint32_t width) const;
+  cudaError_t probes_tc(const float *X, uint32_t ldx, uint32_t b, uint32_t P, uint32_t Pn, const uint32_t *nearest,
+                        const float *nearest_d, uint32_t *probe, float *probed, uint32_t *err, cudaStream_t s);
   cudaError_t forward_tc(const float *X, uint32_t ldx, uint32_t b, float *z, uint32_t *err, cudaStream_t s);
   // the distance head alone: its outputs, and the predicted k-th distances
   // (distance units, margin included)

@@ -144,6 +144,188 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
+// The last layer fused with the probe-table selection.  A CTA holds 128
+// queries' hidden activations (128 x H BF16) in shared memory for the whole
+// launch and streams the weights of 128 lists at a time through a 4-stage
+// TMA ring; the MMA warp accumulates each block of 128 logits into one of
+// two tensor-memory buffers while four epilogue warps (one query row per
+// thread) read the other, add the bias and keep the K largest logits (ties
+// to the lower list) in registers.  No logit is written: each query gets its
+// Pn nearest representatives' lists, then the P best others.
+constexpr uint32_t kTopStages = 4;
+constexpr uint32_t kTopThreads = 192;  // warp 0 loads, warp 1 issues MMAs, warps 2-5 select
+
+template <int K>
+__global__ void __launch_bounds__(kTopThreads, 1)
+    router_top_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
+                      const float *__restrict__ bias, uint32_t M, uint32_t L, uint32_t KB, uint32_t P, uint32_t Pn,
+                      const uint32_t *__restrict__ nearest, const float *__restrict__ nearest_d,
+                      uint32_t *__restrict__ probe, float *__restrict__ probed, uint32_t *err) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t a_full, b_full[kTopStages], b_empty[kTopStages], t_full[2], t_empty[2];
+  __shared__ uint32_t tslot;
+  unsigned char *base =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char *sA = base, *sB = base + KB * kGTile;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t m0 = blockIdx.x * 128, nchunks = (L + 127) / 128;
+  if (warp == 1) {
+    tmem_alloc(&tslot, 256);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&a_full, 1);
+    for (uint32_t s = 0; s < kTopStages; s++) {
+      mbar_init(&b_full[s], 1);
+      mbar_init(&b_empty[s], 1);
+    }
+    for (uint32_t s = 0; s < 2; s++) {
+      mbar_init(&t_full[s], 1);
+      mbar_init(&t_empty[s], 4);
+    }
+    fence_barrier_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tslot;
+  if (warp == 0) {
+    if (lane == 0) {
+      prefetch_tensormap(&tmX);
+      prefetch_tensormap(&tmW);
+      mbar_expect_tx(&a_full, KB * kGTile);
+      for (uint32_t kb = 0; kb < KB; kb++) tma_load_2d(sA + kb * kGTile, &tmX, (int32_t)(kb * 64), (int32_t)m0, &a_full);
+      uint32_t it = 0;
+      bool ok = true;
+      for (uint32_t j = 0; j < nchunks && ok; j++)
+        for (uint32_t kb = 0; kb < KB; kb++, it++) {
+          const uint32_t s = it % kTopStages;
+          if (it >= kTopStages && !(ok = mbar_wait(&b_empty[s], ((it / kTopStages) - 1) & 1, err))) break;
+          mbar_expect_tx(&b_full[s], kGTile);
+          tma_load_2d(sB + s * kGTile, &tmW, (int32_t)(kb * 64), (int32_t)(j * 128), &b_full[s]);
+        }
+      // drain: every load issued has landed before the CTA may leave
+      mbar_wait(&a_full, 0, nullptr);
+      for (uint32_t t = 0; t < kTopStages && t < it; t++) {
+        const uint32_t i = it - 1 - t;
+        mbar_wait(&b_full[i % kTopStages], (i / kTopStages) & 1, nullptr);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(128, 128);
+      bool ok = mbar_wait(&a_full, 0, err);
+      uint32_t it = 0;
+      for (uint32_t j = 0; j < nchunks && ok; j++) {
+        const uint32_t slot = j & 1;
+        if (j >= 2 && !(ok = mbar_wait(&t_empty[slot], ((j >> 1) - 1) & 1, err))) break;
+        tc_fence_after();
+        for (uint32_t kb = 0; kb < KB; kb++, it++) {
+          const uint32_t s = it % kTopStages;
+          if (!(ok = mbar_wait(&b_full[s], (it / kTopStages) & 1, err))) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(sA + kb * kGTile), b0 = smem_u32(sB + s * kGTile);
+#pragma unroll
+          for (uint32_t kk = 0; kk < 4; kk++)
+            mma_bf16(tmem + slot * 128, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc, (kb | kk) != 0);
+          mma_commit(&b_empty[s]);
+        }
+        if (ok) mma_commit(&t_full[slot]);
+      }
+    }
+  } else {
+    const uint32_t ew = warp & 3, row = m0 + ew * 32 + lane;
+    float tv[K];
+    uint32_t ti[K];
+#pragma unroll
+    for (int t = 0; t < K; t++) {
+      tv[t] = -INFINITY;
+      ti[t] = RBC_DUMMY;
+    }
+    bool ok = true;
+    for (uint32_t j = 0; j < nchunks && ok; j++) {
+      const uint32_t slot = j & 1;
+      if (!(ok = mbar_wait(&t_full[slot], (j >> 1) & 1, err))) break;
+      tc_fence_after();
+#pragma unroll 1
+      for (uint32_t c = 0; c < 4; c++) {
+        uint32_t r[32];
+        __syncwarp();
+        tmem_ld32(tmem + ((ew * 32) << 16) + slot * 128 + c * 32, r);
+        tmem_wait_ld();
+        if (c == 3) {  // the buffer's last read is in registers: it goes back to the MMA warp
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&t_empty[slot]);
+        }
+        const uint32_t nb = j * 128 + c * 32;
+#pragma unroll
+        for (int e = 0; e < 32; e++) {
+          const uint32_t n = nb + e;
+          if (n >= L) break;
+          const float v = __uint_as_float(r[e]) + __ldg(bias + n);
+          if (!(v > tv[K - 1])) continue;  // lists come in increasing order: an equal value never displaces
+#pragma unroll
+          for (int t = K - 1; t > 0; t--) {
+            const bool shift = v > tv[t - 1];
+            const bool here = !shift && v > tv[t];
+            tv[t] = shift ? tv[t - 1] : (here ? v : tv[t]);
+            ti[t] = shift ? ti[t - 1] : (here ? n : ti[t]);
+          }
+          if (v > tv[0]) {
+            tv[0] = v;
+            ti[0] = n;
+          }
+        }
+      }
+    }
+    if (ok && row < M) {
+      const uint32_t W = Pn + P;
+      for (uint32_t t = 0; t < Pn; t++) {
+        probe[(uint64_t)row * W + t] = nearest[(uint64_t)row * Pn + t];
+        probed[(uint64_t)row * W + t] = nearest_d[(uint64_t)row * Pn + t];
+      }
+      uint32_t got = 0;
+#pragma unroll
+      for (int t = 0; t < K; t++) {
+        bool taken = ti[t] == RBC_DUMMY;
+        for (uint32_t u = 0; u < Pn; u++) taken |= nearest[(uint64_t)row * Pn + u] == ti[t];
+        if (!taken && got < P) {
+          probe[(uint64_t)row * W + Pn + got] = ti[t];
+          probed[(uint64_t)row * W + Pn + got] = 0.f;
+          got++;
+        }
+      }
+      for (; got < P; got++) {
+        probe[(uint64_t)row * W + Pn + got] = RBC_DUMMY;
+        probed[(uint64_t)row * W + Pn + got] = 0.f;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 256);
+  }
+}
+
+template <int K>
+cudaError_t launch_router_top(const void *X, uint32_t M, uint32_t H, const void *W, uint32_t L, const float *bias,
+                              uint32_t P, uint32_t Pn, const uint32_t *nearest, const float *nearest_d, uint32_t *probe,
+                              float *probed, uint32_t *err, cudaStream_t s) {
+  CUtensorMap tmX, tmW;
+  cudaError_t e = tc_make_map(&tmX, X, M, H, 128);
+  if (e == cudaSuccess) e = tc_make_map(&tmW, W, L, H, 128);
+  const size_t smem = 1024 + (size_t)(H / 64 + kTopStages) * kGTile;
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(router_top_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  router_top_kernel<K><<<(M + 127) / 128, kTopThreads, smem, s>>>(tmX, tmW, bias, M, L, H / 64, P, Pn, nearest,
+                                                                  nearest_d, probe, probed, err);
+  return launched();
+}
+
 // rows x cols FP32 (row stride ld) -> rows x kp BF16, zero beyond cols.
 __global__ void pad_bf16_kernel(const float *__restrict__ src, uint32_t ld, uint64_t rows, uint32_t cols,
                                 uint32_t kp, __nv_bfloat16 *__restrict__ dst) {
@@ -182,6 +364,23 @@ cudaError_t gemm_tc(const void *X, uint32_t M, uint32_t K, const void *W, uint32
 }  // namespace
 
 bool Router::tc_ok() const { return H % 64 == 0 && H >= 64; }
+
+bool Router::top_ok(uint32_t width) const { return tc_ok() && H <= 512 && width >= 1 && width <= 16; }
+
+cudaError_t Router::probes_tc(const float *Xin, uint32_t ldx, uint32_t b, uint32_t P, uint32_t Pn,
+                              const uint32_t *nearest, const float *nearest_d, uint32_t *probe, float *probed,
+                              uint32_t *err, cudaStream_t s) {
+  if (!top_ok(P + Pn)) return cudaErrorInvalidValue;
+  cudaError_t e = forward_tc(Xin, ldx, b, nullptr, err, s);
+  if (e != cudaSuccess) return e;
+  const __nv_bfloat16 *W3 = wb + (size_t)H * d + H + (size_t)H * H + H;
+  const float *b3 = w + (size_t)H * d + H + (size_t)H * H + H + (size_t)(L + T) * H;
+  const uint32_t width = P + Pn;
+  if (width <= 2) return launch_router_top<2>(h2b, b, H, W3, L, b3, P, Pn, nearest, nearest_d, probe, probed, err, s);
+  if (width <= 4) return launch_router_top<4>(h2b, b, H, W3, L, b3, P, Pn, nearest, nearest_d, probe, probed, err, s);
+  if (width <= 8) return launch_router_top<8>(h2b, b, H, W3, L, b3, P, Pn, nearest, nearest_d, probe, probed, err, s);
+  return launch_router_top<16>(h2b, b, H, W3, L, b3, P, Pn, nearest, nearest_d, probe, probed, err, s);
+}
 
 cudaError_t Router::forward_tc(const float *Xin, uint32_t ldx, uint32_t b, float *zout, uint32_t *err,
                                cudaStream_t s) {

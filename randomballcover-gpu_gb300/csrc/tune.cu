@@ -167,31 +167,43 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   uint64_t best_rows = 0;
   int rc = RBC_OK;
   idx->tc_plain = false;
+  // routed calls with router picks also try one and two picks (a call that
+  // plans with the router's distance head, picks = 0, keeps its setting)
   const bool routed = (mode & RBC_QUERY_ROUTED) && idx->router;
-  for (uint32_t p : {RBC_TC_ROUTER_ONLY, 1u, 2u, 4u, 8u}) {
-    if (p == RBC_TC_ROUTER_ONLY && !routed) continue;  // the router's picks alone: routed calls only
-    for (uint64_t r : {2048ull, 8192ull, 32768ull}) {
-      idx->tc_probes = p;
-      idx->tc_probe_rows = r;
-      double ms_min = 1e30;
-      for (int rep = 0; rep < 3 && rc == RBC_OK; rep++) {  // the first run warms up
-        cudaEventRecord(e0, s);
-        rc = query_index(idx, dQ, m, ldq, k, mode, ids.as<uint32_t>(), dists.as<float>(), k, s);
-        cudaEventRecord(e1, s);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (rep) ms_min = std::min(ms_min, (double)ms);
+  const uint32_t user_picks = idx->router_probes;
+  std::vector<uint32_t> picks_set = {user_picks};
+  if (routed && user_picks > 0) picks_set = {1u, 2u};
+  uint32_t best_picks = user_picks;
+  for (uint32_t picks : picks_set) {
+    idx->router_probes = picks;
+    for (uint32_t p : {RBC_TC_ROUTER_ONLY, 1u, 2u, 4u, 8u}) {
+      if (p == RBC_TC_ROUTER_ONLY && !routed) continue;  // the router's picks alone: routed calls only
+      for (uint64_t r : {2048ull, 8192ull, 32768ull}) {
+        idx->tc_probes = p;
+        idx->tc_probe_rows = r;
+        double ms_min = 1e30;
+        for (int rep = 0; rep < 3 && rc == RBC_OK; rep++) {  // the first run warms up
+          cudaEventRecord(e0, s);
+          rc = query_index(idx, dQ, m, ldq, k, mode, ids.as<uint32_t>(), dists.as<float>(), k, s);
+          cudaEventRecord(e1, s);
+          cudaEventSynchronize(e1);
+          float ms = 0;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (rep) ms_min = std::min(ms_min, (double)ms);
+        }
+        if (rc != RBC_OK) break;
+        if (ms_min < best) {
+          best = ms_min;
+          best_p = p;
+          best_rows = r;
+          best_picks = picks;
+        }
       }
       if (rc != RBC_OK) break;
-      if (ms_min < best) {
-        best = ms_min;
-        best_p = p;
-        best_rows = r;
-      }
     }
     if (rc != RBC_OK) break;
   }
+  idx->router_probes = rc == RBC_OK ? best_picks : user_picks;
   // the plain FP32 search on the same lists, same routing: when it is the
   // faster of the two, RBC_QUERY_EXACT_TC calls run it
   double plain = 1e30;

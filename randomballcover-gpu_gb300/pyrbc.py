@@ -43,7 +43,7 @@ class IndexInfo(C.Structure):
     _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("ld", C.c_uint32), ("num_reps", C.c_uint32),
                 ("s", C.c_uint32), ("metric", C.c_int), ("flags", C.c_uint32), ("min_list", C.c_uint64),
                 ("max_list", C.c_uint64), ("device_bytes", C.c_uint64), ("tc_format", C.c_uint32),
-                ("tc_plain", C.c_uint32)]
+                ("tc_plain", C.c_uint32), ("router_picks", C.c_uint32)]
 
 
 class QueryStats(C.Structure):
@@ -98,6 +98,7 @@ SIGNATURES = {
                                         _VP], _INT),
     "rbc_router_gradients_with_distance": ([_VP, _VP, _U32, _U32, _VP, _VP, C.POINTER(_F), _VP, _VP], _INT),
     "rbc_router_predict_distance": ([_VP, _VP, _U64, _U32, _VP, _VP, _VP], _INT),
+    "rbc_router_top_lists": ([_VP, _VP, _U64, _U32, _U32, _VP, _VP], _INT),
     "rbc_router_distance_params": ([_VP, C.POINTER(_F), C.POINTER(_F), C.POINTER(_F)], _INT),
     "rbc_router_set_distance_margin": ([_VP, _F], _INT),
     "rbc_set_router": ([_VP, _VP, _U32], _INT),
@@ -441,6 +442,15 @@ class Router:
         out = torch.empty((Q.shape[0], self.num_lists), dtype=torch.float32, device=Q.device)
         check(lib().rbc_router_logits(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), out.data_ptr(),
                                       _stream(stream)))
+        return out
+
+    def top_lists(self, Q, P, stream=None):
+        """The P most likely lists per query (largest logit first, ties to the lower list)."""
+        import torch
+        Q = _dev(Q, torch.float32)
+        out = torch.empty((Q.shape[0], P), dtype=torch.int32, device=Q.device)
+        check(lib().rbc_router_top_lists(self.h, Q.data_ptr(), Q.shape[0], Q.stride(0), P, out.data_ptr(),
+                                         _stream(stream)))
         return out
 
     def gradients_with_distance(self, Q, labels, targets, stream=None):

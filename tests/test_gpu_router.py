@@ -257,3 +257,23 @@ def test_predicted_distance_plan_is_exact(rbc, oracle):
         idx.set_router(rbc.Router(d, 64, nr, seed=1), probes=0)  # no distance head
     idx.close()
     r.close()
+
+
+@pytest.mark.parametrize("d,H,L,P", [(128, 512, 4096, 2), (64, 256, 1000, 5), (32, 128, 300, 16)])
+def test_fused_top_lists_match_the_logits(rbc, d, H, L, P):
+    """The routed queries' probe picks come from the last layer fused with the
+    selection (no logits in memory); they equal the top P of the logits the
+    unfused tensor-core GEMMs write, ties to the lower list, wherever the
+    gap to the next logit is clear of rounding."""
+    rng = np.random.default_rng(L + P)
+    r = rbc.Router(d, H, L, seed=11)
+    X = rng.standard_normal((3000, d)).astype(np.float32)
+    top = rbc.u32(r.top_lists(X, P)).astype(np.int64)
+    z = r.logits(X).cpu().numpy().astype(np.float64)
+    order = np.argsort(-z, axis=1, kind="stable")[:, :P + 1]
+    zs = np.take_along_axis(z, order, 1)
+    gap = np.abs(np.diff(zs, axis=1)).min(1) > 1e-4 * np.abs(zs).max(1)
+    assert gap.mean() > 0.9
+    np.testing.assert_array_equal(top[gap], order[gap, :P])
+    assert (top >= 0).all() and (top < L).all()
+    r.close()
