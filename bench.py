@@ -66,8 +66,8 @@ WORKLOADS = {
                train=100_000, epochs=2, forms="plain,tensor,learned", metric=METRIC,
                desc="geometric(mean 20) integer features"),
     "c4": dict(kind=1, seed=4, instances=64, n_lo=10_000, n_hi=2_000_000, dims=(32, 64, 128), ks=(1, 10, 32),
-               comp_lo=100, comp_hi=1000, slo=0.05, shi=0.05, forms="batch",
-               metric="exact k-NN queries/s over 64 batched heterogeneous RBC instances (one graph), plain FP32",
+               comp_lo=100, comp_hi=1000, slo=0.05, shi=0.05, forms="fp32,tensor",
+               metric="exact k-NN queries/s over 64 batched heterogeneous RBC instances (one graph)",
                desc="64 instances, n log-uniform in [1e4, 2e6], d in {32, 64, 128}, k in {1, 10, 32}, m = n/100"),
     "c5": dict(kind=1, seed=5, n=4_194_304, m=100_000, d=128, k=10, reps=4096, ncomp=2000, slo=0.02, shi=0.1,
                train=1_000_000, epochs=3, forms="plain,tensor,learned",
@@ -671,7 +671,11 @@ def batch_instances(w):
 
 def run_batch(a):
     """64 independent (database, query set) instances answered by one captured
-    graph per step (rbc_batch); compared with answering them one by one."""
+    graph per step (rbc_batch), in two variants: the FP32 search (one
+    persistent launch per round over every instance) and the tensor form
+    (BF16 / FP16 hi-lo operands on tcgen05, uncertified queries searched
+    again on the device inside the graph).  Each is compared with answering
+    the instances one by one."""
     import torch
     import pyrbc
 
@@ -683,6 +687,9 @@ def run_batch(a):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     stream = torch.cuda.current_stream()
+    forms = [f for f in a.forms.split(",") if f]
+    head = forms[-1]
+    modes = {"fp32": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC}
     specs = batch_instances(w)
     inst = []
     t0 = time.perf_counter()
@@ -690,51 +697,79 @@ def run_batch(a):
         syn = dict(ncomp=ncomp, sigma_lo=w["slo"], sigma_hi=w["shi"])
         X = pyrbc.synth(w["kind"], w["seed"] * 1000 + i, 0, n, d, **syn)
         Q = pyrbc.synth(w["kind"], w["seed"] * 1000 + i, 1, m, d, **syn)
-        idx = pyrbc.Index(X, reps, seed=i)
+        idx = pyrbc.Index(X, reps, seed=i, flags=pyrbc.BUILD_PARTITION | pyrbc.BUILD_BF16)
         idx.autotune(Q, k)
+        if "tensor" in forms:
+            idx.autotune_tc(Q, k)
         inst.append({"X": X, "Q": Q, "idx": idx, "k": k, "m": m, "n": n, "d": d})
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     total_m = sum(r["m"] for r in inst)
-
-    # one by one (the same exact query per instance), for comparison and the pair counts
-    pairs = flops = 0
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    seq = []
-    for r in inst:
-        seq.append(r["idx"].query(r["Q"], r["k"]))
-        st = r["idx"].stats()
-        pairs += st["point_pairs"]
-        flops += st["point_pairs"] * 2 * r["d"]
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    for _ in range(a.steps):
+    hbm, bf16, bf16_sus, src = peaks()
+    res = {}
+    for f in forms:
+        mode = modes[f]
+        # one by one (the same exact query per instance), for comparison and the pair counts
+        pairs = flops = fallbacks = 0
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        seq = []
         for r in inst:
-            r["idx"].query(r["Q"], r["k"], out=None)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    seq_ms = ev0.elapsed_time(ev1) / a.steps
+            seq.append(r["idx"].query(r["Q"], r["k"], mode=mode))
+            st = r["idx"].stats()
+            pairs += st["point_pairs"]
+            flops += st["point_pairs"] * 2 * r["d"]
+            fallbacks += st["fallback_queries"]
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(a.steps):
+            for r in inst:
+                r["idx"].query(r["Q"], r["k"], mode=mode)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        seq_ms = ev0.elapsed_time(ev1) / a.steps
+        batch = pyrbc.Batch()
+        outs = [batch.add(r["idx"], r["Q"], r["k"], mode=mode) for r in inst]
+        for _ in range(a.warmup):
+            batch.run()
+        torch.cuda.synchronize()
+        same = all(bool((o[0] == s_[0]).all().item()) and bool((o[1] == s_[1]).all().item())
+                   for o, s_ in zip(outs, seq))
+        fp64 = max(fp64_error(r["X"], r["Q"], o[0], o[1], sample=64) for r, o in zip(inst, outs))
+        clocks = ClockSampler(local) if f == head else None
+        if clocks:
+            clocks.start()
+        l0 = pyrbc.kernel_launches()
+        ev0.record(stream)
+        for _ in range(a.steps):
+            batch.run()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        clk = clocks.stop() if clocks else None
+        launches = pyrbc.kernel_launches() - l0
+        ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
+        sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+        achieved = flops / (ms / a.steps / 1000.0) / 1e12
+        if f == "fp32":
+            fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+            roof = {"bound": "fp32 pipe", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                    "frac": achieved / fp32_peak, "traffic": committed_traffic("search_kernel_batch"),
+                    "kernel": "search_kernel (whole graph step)",
+                    "peak_source": f"FP32 pipe: 152 SMs x 128 lanes x 2 flops x {sm_mhz:.0f} MHz (no measured "
+                                   "FP32 peak; the difference form issues 3 instructions per 2 flops counted)",
+                    "note": "achieved = evaluated (query, row) pairs x 2d over the whole graph step"}
+        else:
+            roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                    "frac": achieved / bf16, "traffic": committed_traffic("tc_search_kernel_batch"),
+                    "kernel": "tc_search_kernel (whole graph step)",
+                    "peak_source": f"{src} bf16 dense burst (MEASURED_PEAKS.json)",
+                    "note": "achieved = evaluated (query, row) pairs x 2d over the whole graph step; the FP16 "
+                            "hi/lo operands take 3 MMAs per pair"}
+        res[f] = {"batch": batch, "outs": outs, "ms": ms, "value": replica_rate(total_m, a.steps, world, ms),
+                  "launches": launches, "clocks": clk, "roofline": roof, "seq_ms": seq_ms, "pairs": pairs,
+                  "same": same, "fp64": fp64, "fallbacks": fallbacks}
 
-    batch = pyrbc.Batch()
-    outs = [batch.add(r["idx"], r["Q"], r["k"]) for r in inst]
-    for _ in range(a.warmup):
-        batch.run()
-    torch.cuda.synchronize()
-    same = all(bool((o[0] == s[0]).all().item()) and bool((o[1] == s[1]).all().item()) for o, s in zip(outs, seq))
-    fp64 = max(fp64_error(r["X"], r["Q"], o[0], o[1], sample=64) for r, o in zip(inst, outs))
-    clocks = ClockSampler(local)
-    clocks.start()
-    l0 = pyrbc.kernel_launches()
-    ev0.record(stream)
-    for _ in range(a.steps):
-        batch.run()
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    launches = pyrbc.kernel_launches() - l0
-    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
-    value = replica_rate(total_m, a.steps, world, ms)
-
+    h = res[head]
+    batch, outs, ms = h["batch"], h["outs"], h["ms"]
     # end to end: pinned host queries copied in, results copied out, every step
     hq = [r["Q"].cpu().pin_memory() for r in inst]
     hi = [torch.empty_like(o[0], device="cpu").pin_memory() for o in outs]
@@ -754,15 +789,6 @@ def run_batch(a):
     e2e_s = time.perf_counter() - t0
     e2e = {"value": world * total_m * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h)}
-    hbm, bf16, bf16_sus, src = peaks()
-    sm_mhz = clk.get("sm_mhz") or 1920.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    achieved = flops / (ms / a.steps / 1000.0) / 1e12
-    roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
-                "traffic": committed_traffic("search_kernel_batch"), "kernel": "search_kernel (whole graph step)",
-                "peak_source": f"{src} bf16 dense burst (MEASURED_PEAKS.json)",
-                "fp32_core": {"achieved_tflops": achieved, "peak_tflops": fp32_peak, "frac": achieved / fp32_peak},
-                "note": "achieved = evaluated (query, row) pairs x 2d over the whole graph step"}
     cpu = None
     parity = None
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
@@ -773,36 +799,47 @@ def run_batch(a):
         cpu = {"value": nq / t, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": f"{nq} queries of the largest instance (n={r['n']:,}, d={r['d']}); {desc}"}
         # parity: 4 queries of every instance (first, last, two between)
-        # against the oracle, the batched answers compared bit for bit
+        # against the oracle, every variant's batched answers bit for bit
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
-        parity = {"queries": 0, "instances": len(inst), "ids_equal": True, "dists_equal": True,
+        parity = {"queries": 0, "instances": len(inst), "forms": forms, "ids_equal": True, "dists_equal": True,
                   "dists_within_rtol": True, "rtol": PARITY_RTOL}
-        for r, o in zip(inst, outs):
+        for j, r in enumerate(inst):
             sel = np.unique(np.linspace(0, r["m"] - 1, min(4, r["m"])).round().astype(np.int64))
             tsel = torch.from_numpy(sel).cuda()
             want = oracle.knn(r["X"].cpu().numpy(), r["Q"][tsel].cpu().numpy(), r["k"], threads=threads)
-            ids_eq, bits, tol = compare_answers(o[0][tsel].cpu().numpy(), o[1][tsel].cpu().numpy(), want)
             parity["queries"] += len(sel)
-            parity["ids_equal"] &= ids_eq
-            parity["dists_equal"] &= bits
-            parity["dists_within_rtol"] &= tol
+            for f in forms:
+                o = res[f]["outs"][j]
+                ids_eq, bits, tol = compare_answers(o[0][tsel].cpu().numpy(), o[1][tsel].cpu().numpy(), want)
+                parity["ids_equal"] &= ids_eq
+                parity["dists_equal"] &= bits
+                parity["dists_within_rtol"] &= tol
         parity["oracle"] = "port"
     if rank == 0:
-        extra = {"build_and_tune_s": build_s, "queries_per_step": total_m, "pairs_per_step": pairs,
-                 "one_by_one_ms_per_step": seq_ms, "one_by_one_value": world * total_m / (seq_ms / 1000.0),
-                 "batched_speedup": seq_ms / (ms / a.steps), "same_ids_as_one_by_one": same,
-                 "max_rel_dist_error_vs_fp64": fp64,
+        extra = {"build_and_tune_s": build_s, "queries_per_step": total_m, "forms": {},
                  "instances": [{"n": r["n"], "d": r["d"], "k": r["k"], "m": r["m"]} for r in inst]}
-        line = {"metric": w["metric"], "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        for f, r_ in res.items():
+            extra["forms"][f] = {"value": r_["value"], "ms_per_step": r_["ms"] / a.steps,
+                                 "launches_per_step": r_["launches"] / a.steps, "pairs_per_step": r_["pairs"],
+                                 "one_by_one_ms_per_step": r_["seq_ms"],
+                                 "one_by_one_value": world * total_m / (r_["seq_ms"] / 1000.0),
+                                 "batched_speedup": r_["seq_ms"] / (r_["ms"] / a.steps),
+                                 "same_ids_as_one_by_one": r_["same"], "max_rel_dist_error_vs_fp64": r_["fp64"],
+                                 "uncertified_queries_per_step": r_["fallbacks"],
+                                 "roofline": r_["roofline"]}
+        names = {"fp32": "batched exact RBC, FP32 list search, CUDA graph",
+                 "tensor": "batched exact RBC, tcgen05 list search + FP32 rerank, CUDA graph"}
+        line = {"metric": w["metric"], "value": h["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (counter-based generator on the GPU)",
-                "config": dict(config(a, "batched exact RBC, FP32 list search, CUDA graph"),
-                               parallelism=f"replicas{world}"),
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "parity": parity, "extra": extra}
+                "vs_baseline": None, "dtype": "f32" if head == "fp32" else "bf16/fp16+f32",
+                "data": "synthetic (counter-based generator on the GPU)",
+                "config": dict(config(a, names[head]), parallelism=f"replicas{world}"),
+                "roofline": h["roofline"], "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(h["launches"]),
+                "clocks": h["clocks"], "parity": parity, "extra": extra}
         print(json.dumps(line), flush=True)
-    batch.close()
+    for r_ in res.values():
+        r_["batch"].close()
     for r in inst:
         r["idx"].close()
     if dist:

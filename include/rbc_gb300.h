@@ -162,15 +162,20 @@ int rbc_get_fallback_queries(const rbc_index *index, uint32_t *h_ids, uint64_t c
 
 /* ---- batched queries over many indexes (no counterpart in the reference) ----
  * Instances (index, device queries, k, outputs) are added, then rbc_batch_run
- * answers all of them exactly: each round plans every instance, then one
- * persistent search launch serves all instances' work.  The first run
- * captures the whole sequence into a CUDA graph; later runs replay it, so
- * new query values written into the same buffers are answered by one graph
- * launch.  Instances must share the metric; m x num_reps <= 2^28 each. */
+ * answers all of them exactly: each round plans every FP32 instance, then
+ * one persistent search launch serves all their work; tensor-form instances
+ * (rbc_batch_add_mode with RBC_QUERY_EXACT_TC, BF16 indexes, k <= 32) each
+ * run their rounds on the tensor cores, the queries their certificate
+ * leaves open searched again on the device.  The first run captures the
+ * whole sequence into a CUDA graph; later runs replay it, so new query
+ * values written into the same buffers are answered by one graph launch.
+ * Instances must share the metric; m x num_reps <= 2^28 each. */
 typedef struct rbc_batch rbc_batch;
 int rbc_batch_create(rbc_batch **out);
 int rbc_batch_add(rbc_batch *batch, rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
                   uint32_t *dIds, float *dDists, uint32_t ldo);
+int rbc_batch_add_mode(rbc_batch *batch, rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
+                       uint32_t mode, uint32_t *dIds, float *dDists, uint32_t ldo);
 int rbc_batch_run(rbc_batch *batch, void *stream);
 int rbc_batch_destroy(rbc_batch *batch);
 

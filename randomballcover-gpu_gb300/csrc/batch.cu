@@ -61,14 +61,18 @@ struct BatchInstance {
   const float *Q;
   uint64_t m;
   uint32_t ldq, k, ldo;
+  uint32_t mode;  // RBC_QUERY_EXACT (the shared FP32 search) or RBC_QUERY_EXACT_TC
   uint32_t *ids;
   float *dists;
   QueryBufs b;
+  std::unique_ptr<TcQuery> tc;  // the tensor form's buffers (RBC_QUERY_EXACT_TC)
 };
 
 struct rbc_batch {
   std::vector<std::unique_ptr<BatchInstance>> inst;
   std::vector<void *> owned;
+  std::vector<cudaStream_t> branch;  // capture-time side streams (tensor-form instances)
+  std::vector<cudaEvent_t> marks;
   bool ready = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -84,6 +88,8 @@ struct rbc_batch {
       cudaStreamDestroy(cap);
     }
     for (void *p : owned) cudaFree(p);
+    for (cudaStream_t b : branch) cudaStreamDestroy(b);
+    for (cudaEvent_t e : marks) cudaEventDestroy(e);
   }
 };
 
@@ -100,15 +106,19 @@ namespace {
     if (rc_ != RBC_OK) return rc_;  \
   } while (0)
 
-// Allocate every buffer, then record the whole two-round sequence on a
-// capture stream into a graph.
+// Allocate every buffer, then record the whole sequence on a capture stream
+// into a graph: the FP32 instances' two rounds, each one persistent search
+// launch over all of them, then every tensor-form instance's round (its
+// uncertified queries searched again on the device).
 int prepare(rbc_batch *bt) {
-  const uint32_t N = (uint32_t)bt->inst.size();
+  std::vector<BatchInstance *> fp, tcv;
+  for (auto &ip : bt->inst) (ip->mode == RBC_QUERY_EXACT_TC ? tcv : fp).push_back(ip.get());
+  const uint32_t N = (uint32_t)fp.size();
   const int metric = bt->inst[0]->idx->metric;
   // one tile geometry for the shared launch: the smallest query tile any instance needs
   int tq = 4;
   uint32_t dp_max = 0;
-  for (auto &ip : bt->inst) {
+  for (BatchInstance *ip : fp) {
     tq = std::min(tq, search_tq_for(ip->idx->dp, ip->idx->tune_tq));
     dp_max = std::max(dp_max, ip->idx->dp);
   }
@@ -121,7 +131,7 @@ int prepare(rbc_batch *bt) {
   std::vector<SearchItem *> srcs(N);
   std::vector<uint32_t *> counts(N);
   for (uint32_t i = 0; i < N; i++) {
-    BatchInstance &in = *bt->inst[i];
+    BatchInstance &in = *fp[i];
     rbc_index *idx = in.idx;
     const uint32_t nr = idx->nr, ld = idx->ld;
     QueryBufs &b = in.b;
@@ -164,6 +174,24 @@ int prepare(rbc_batch *bt) {
     a.qthr = b.pair_thr.as<float>();
     args1[i] = a;
   }
+  for (BatchInstance *ip : tcv) {
+    ip->tc = std::make_unique<TcQuery>();
+    BTRY(tc_setup(ip->idx, ip->m, ip->k, RBC_QUERY_EXACT_TC, true, *ip->tc, s));
+  }
+  // the tensor-form instances are captured on side streams forked from the
+  // capture stream and joined back, so the graph holds them as parallel
+  // branches (a few at a time share the GPU instead of running in turn)
+  const uint32_t nbranch = (uint32_t)std::min<size_t>(tcv.size(), 8);
+  for (uint32_t i = 0; i < nbranch; i++) {
+    cudaStream_t b;
+    BCK(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking));
+    bt->branch.push_back(b);
+  }
+  for (size_t i = 0; i < 2 * tcv.size() + 1; i++) {
+    cudaEvent_t e;
+    BCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    bt->marks.push_back(e);
+  }
   BCK(cudaStreamSynchronize(s));
   SearchArgs *t0 = dalloc<SearchArgs>(N, bt->owned), *t1 = dalloc<SearchArgs>(N, bt->owned);
   SearchItem **dsrc = dalloc<SearchItem *>(N, bt->owned);
@@ -177,7 +205,7 @@ int prepare(rbc_batch *bt) {
   BCK(cudaMemcpy(t1, args1.data(), N * sizeof(SearchArgs), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(dsrc, srcs.data(), N * sizeof(void *), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(dcnt, counts.data(), N * sizeof(void *), cudaMemcpyHostToDevice));
-  const int grid = search_grid(metric, dp_max, tq);
+  const int grid = N ? search_grid(metric, dp_max, tq) : 1;
   SearchArgs g{};
   g.items = all;
   g.nitems = bt->ctl + 1;
@@ -193,7 +221,7 @@ int prepare(rbc_batch *bt) {
   int rc = RBC_OK;
   auto capture = [&]() -> int {
     BCK(cudaMemsetAsync(bt->ctl, 0, 64, s));
-    for (auto &ip : bt->inst) {
+    for (BatchInstance *ip : fp) {
       BatchInstance &in = *ip;
       rbc_index *idx = in.idx;
       QueryBufs &b = in.b;
@@ -205,8 +233,8 @@ int prepare(rbc_batch *bt) {
       BCK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
                               b.lock.as<uint32_t>(), in.m, kListWidth, s));
     }
-    for (uint32_t round = 0; round < 2; round++) {
-      for (auto &ip : bt->inst)
+    for (uint32_t round = 0; round < 2 && N; round++) {
+      for (BatchInstance *ip : fp)
         BTRY(plan_and_search(ip->idx, ip->b, ip->m, 1, ip->k, round, ip->idx->Xp, ip->idx->perm, ip->idx->offsets,
                              ip->idx->radius, grid, nullptr, s, 1, tq));
       batch_offsets_kernel<<<1, 1, 0, s>>>(dcnt, N, offs, bt->ctl + 1);
@@ -217,10 +245,31 @@ int prepare(rbc_batch *bt) {
       g.insts = round == 0 ? t0 : t1;
       BCK(launch_search(metric, g, grid, s, tq));
     }
-    for (auto &ip : bt->inst)
+    for (BatchInstance *ip : fp)
       BCK(launch_write_results(ip->b.res_d.as<float>(), ip->b.res_i.as<uint32_t>(), ip->m, ip->k, kListWidth, ip->ids,
-                               ip->dists,
-                               ip->ldo, s));
+                               ip->dists, ip->ldo, s));
+    // the tensor-form instances, each a whole round with its device fallback;
+    // the instances of one index share a branch (its router's scratch is the
+    // index's), distinct indexes go round the branches; their error words
+    // fold into the batch's
+    if (!tcv.empty()) {
+      BCK(cudaEventRecord(bt->marks[0], s));
+      for (cudaStream_t b : bt->branch) BCK(cudaStreamWaitEvent(b, bt->marks[0], 0));
+      std::vector<std::pair<rbc_index *, size_t>> lane;
+      for (size_t i = 0; i < tcv.size(); i++) {
+        BatchInstance *ip = tcv[i];
+        auto it = std::find_if(lane.begin(), lane.end(), [&](const auto &e) { return e.first == ip->idx; });
+        if (it == lane.end()) it = lane.insert(lane.end(), {ip->idx, lane.size() % bt->branch.size()});
+        const size_t j = it->second;
+        cudaStream_t b = bt->branch[j];
+        BTRY(tc_enqueue(ip->idx, *ip->tc, ip->Q, ip->m, ip->ldq, ip->ids, ip->dists, ip->ldo, true, bt->ctl + 2,
+                        nullptr, b));
+      }
+      for (size_t j = 0; j < bt->branch.size(); j++) {
+        BCK(cudaEventRecord(bt->marks[1 + j], bt->branch[j]));
+        BCK(cudaStreamWaitEvent(s, bt->marks[1 + j], 0));
+      }
+    }
     return RBC_OK;
   };
   rc = capture();
@@ -251,9 +300,18 @@ int rbc_batch_create(rbc_batch **out) {
 
 int rbc_batch_add(rbc_batch *bt, rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
                   uint32_t *dIds, float *dDists, uint32_t ldo) {
+  return rbc_batch_add_mode(bt, idx, dQ, m, ldq, k, RBC_QUERY_EXACT, dIds, dDists, ldo);
+}
+
+int rbc_batch_add_mode(rbc_batch *bt, rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
+                       uint32_t mode, uint32_t *dIds, float *dDists, uint32_t ldo) {
   if (!bt || !idx) return fail(RBC_ERR_INVALID, "rbc_batch_add: NULL argument");
   if (bt->ready) return fail(RBC_ERR_INVALID, "rbc_batch_add: the batch already ran; create a new one");
   if (!(idx->flags & RBC_BUILD_PARTITION)) return fail(RBC_ERR_INVALID, "rbc_batch_add: index has no partition");
+  if (mode != RBC_QUERY_EXACT && mode != RBC_QUERY_EXACT_TC)
+    return fail(RBC_ERR_INVALID, "rbc_batch_add: mode must be RBC_QUERY_EXACT or RBC_QUERY_EXACT_TC");
+  if (mode == RBC_QUERY_EXACT_TC && !(idx->flags & RBC_BUILD_BF16))
+    return fail(RBC_ERR_INVALID, "rbc_batch_add: RBC_QUERY_EXACT_TC needs an index built with RBC_BUILD_BF16");
   if (idx->flags & RBC_BUILD_F64) return fail(RBC_ERR_INVALID, "rbc_batch_add: index holds doubles: rbc_query_f64");
   if (k < 1 || k > (uint32_t)kListWidth || ldo < k || ldq < idx->d || m == 0 || !dQ || (!dIds && !dDists))
     return fail(RBC_ERR_INVALID, "rbc_batch_add: bad query arguments");
@@ -268,6 +326,7 @@ int rbc_batch_add(rbc_batch *bt, rbc_index *idx, const float *dQ, uint64_t m, ui
   in->ldq = ldq;
   in->k = k;
   in->ldo = ldo;
+  in->mode = mode;
   in->ids = dIds;
   in->dists = dDists;
   bt->inst.push_back(std::move(in));

@@ -556,46 +556,50 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
 //      plain exact path.
 // Rows of pruned lists cannot be in the top k (exact bounds), so the
 // certificate covers everything.  The rounds need no host round trip.
-int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode, uint32_t *dIds,
-             float *dDists, uint32_t ldo, cudaStream_t s) {
-  pool_setup();
-  const uint32_t nr = idx->nr, ld = idx->ld, kp = idx->kp, fmt = idx->tc.format, cols = idx->tc.cols;
-  const bool routed = (mode & RBC_QUERY_ROUTED) != 0;
-  if (routed && !idx->router) return fail(RBC_ERR_INVALID, "rbc_query: RBC_QUERY_ROUTED without a router");
+// The host-side choices and every buffer of a tensor-form round for batches
+// of up to mb queries (see TcQuery).
+int tc_setup(rbc_index *idx, uint64_t mb, uint32_t k, uint32_t mode, bool graph, TcQuery &t, cudaStream_t s) {
+  const uint32_t nr = idx->nr, ld = idx->ld, cols = idx->tc.cols;
+  t.routed = (mode & RBC_QUERY_ROUTED) != 0;
+  if (t.routed && !idx->router) return fail(RBC_ERR_INVALID, "rbc_query: RBC_QUERY_ROUTED without a router");
+  if (graph && t.routed) return fail(RBC_ERR_UNSUPPORTED, "rbc_query: routed tensor-form queries in a graph");
   // lists searched in the probe round: the nearest representatives' (plus,
   // routed, the router's picks among the others); RBC_TC_PROBES overrides the
-  // number of nearest ones
   // number of nearest ones; RBC_TC_ROUTER_ONLY (routed calls): none, the
-  // router's picks alone
+  // router's picks alone.
   // A routed call whose router has a distance head and probes = 0 skips the
   // probe round: every list is planned with tau = min(predicted k-th
   // distance, k-th nearest representative), the shortlists are capped at
   // tau (1 + 2^-10), and a query is accepted only if its exact k-th distance
   // is at most tau; the others are answered again with the probe round.
-  const bool spec = routed && idx->router->r.T && idx->router_probes == 0;
+  t.spec = t.routed && idx->router->r.T && idx->router_probes == 0;
   uint32_t Pn = idx->tc_probes ? idx->tc_probes : kTcProbes;
-  if (Pn == RBC_TC_ROUTER_ONLY) Pn = routed ? 0 : 1;
+  if (Pn == RBC_TC_ROUTER_ONLY) Pn = t.routed ? 0 : 1;
   if (const char *env = std::getenv("RBC_TC_PROBES")) Pn = std::max(1, std::min(8, std::atoi(env)));
-  if (spec) Pn = 1;  // the nearest representative only: the bound needs its distance
-  Pn = std::min(Pn, nr);
-  const uint32_t Pnear = std::max(Pn, 1u);  // nearest representatives found (the bound needs the first)
-  const uint32_t P = routed && !spec ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
-  const int grid = tc_grid(), sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
+  if (t.spec) Pn = 1;  // the nearest representative only: the bound needs its distance
+  t.Pn = Pn = std::min(Pn, nr);
+  t.Pnear = std::max(Pn, 1u);  // nearest representatives found (the bound needs the first)
+  t.P = t.routed && !t.spec ? Pn + std::min(idx->router_probes, nr - Pn) : Pn;
+  t.k = k;
+  t.mb = mb;
+  t.grid = tc_grid();
+  t.sgrid = search_grid(idx->metric, idx->dp, idx->tune_tq);
   // the probe round's FP32 lists hold a whole shortlist; its query tiles
   // follow the probed queries per list (16 wide when few share a list)
-  const uint32_t sl = tc_shortlist(k), kw = list_width_for(sl);
-  uint64_t probe_rows = idx->tc_probe_rows ? idx->tc_probe_rows : kTcProbeRows;
-  if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) probe_rows = std::strtoull(env, nullptr, 10);
-  const uint32_t qtile = tc_query_tile(fmt);
-  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
-  const uint64_t probe_per_list = mb * P / nr;
-  const int ptq = search_tq_for(idx->dp, probe_per_list >= 48 ? 4 : (probe_per_list >= 24 ? 2 : 1), kw);
-  const int pgrid = search_grid(idx->metric, idx->dp, ptq, kw);
-  QueryBufs b;
+  t.sl = tc_shortlist(k);
+  t.kw = list_width_for(t.sl);
+  t.probe_rows = idx->tc_probe_rows ? idx->tc_probe_rows : kTcProbeRows;
+  if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) t.probe_rows = std::strtoull(env, nullptr, 10);
+  t.qtile = tc_query_tile(idx->tc.format);
+  const uint64_t probe_per_list = mb * t.P / nr;
+  t.ptq = search_tq_for(idx->dp, probe_per_list >= 48 ? 4 : (probe_per_list >= 24 ? 2 : 1), t.kw);
+  t.pgrid = search_grid(idx->metric, idx->dp, t.ptq, t.kw);
+  const uint32_t P = t.P, sl = t.sl, kw = t.kw;
+  QueryBufs &b = t.b;
   // work items of the three plans: pruned round (query tiles of qtile), probe
   // round on the FP32 path (16) and on the tensor cores (128)
   const uint64_t pair_cap = mb * nr,
-                 item_cap = std::max({item_capacity(idx, mb, qtile), item_capacity(idx, mb, 16, P),
+                 item_cap = std::max({item_capacity(idx, mb, t.qtile), item_capacity(idx, mb, 16, P),
                                       item_capacity(idx, mb, tc_query_tile(kTcSplit), P)});
   CK(b.Qp.alloc(mb * ld * 4, s));
   CK(b.Dqr.alloc(mb * nr * 4, s));
@@ -616,36 +620,263 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   b.item_cap = item_cap;
   CK(b.ctl.alloc(64, s));
   CK(b.scan_tmp.alloc(scan_temp_bytes(nr + 1), s));
-  DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
-      stats, seed_a, seed_row, sl_cap, tpred;
-  b.plan_all = spec;
-  if (spec) {
-    CK(tpred.alloc(mb * 4, s));
-  } else if (routed) {
-    CK(near.alloc(mb * Pnear * 4, s));
-    CK(near_d.alloc(mb * Pnear * 4, s));
-    if (!idx->router->r.top_ok(P)) CK(logits.alloc(mb * nr * 4, s));
+  b.plan_all = t.spec;
+  if (t.spec) {
+    CK(t.tpred.alloc(mb * 4, s));
+  } else if (t.routed) {
+    CK(t.near.alloc(mb * t.Pnear * 4, s));
+    CK(t.near_d.alloc(mb * t.Pnear * 4, s));
+    if (!idx->router->r.top_ok(P)) CK(t.logits.alloc(mb * nr * 4, s));
     // without nearest lists in the probe table the pruning bound takes the
     // nearest representative's distance from here
-    if (Pn == 0) b.dq0 = near_d.as<float>();
+    if (Pn == 0) b.dq0 = t.near_d.as<float>();
   }
-  CK(Qh.alloc((mb + 1) * cols * 2, s));
-  CK(qscale.alloc((mb + 1) * 4, s));
-  CK(qnorm.alloc((mb + 1) * 4, s));
-  CK(qinex.alloc(mb + 1, s));
-  CK(sl_a.alloc(2 * mb * sl * 4, s));
-  CK(seed_a.alloc(mb * sl * 4, s));
-  CK(seed_row.alloc(mb * sl * 4, s));
-  CK(sl_row.alloc(2 * mb * sl * 4, s));
-  CK(sl_sel.alloc(mb * 4, s));
-  CK(sl_theta.alloc(mb * 4, s));
-  CK(sl_lock.alloc(mb * 4, s));
-  if (spec) CK(sl_cap.alloc(mb * 4, s));
-  CK(emax.alloc(mb * 4, s));
-  CK(ctl.alloc(64, s));
-  CK(failq.alloc(mb * 4, s));
-  CK(stats.alloc(2 * sizeof(unsigned long long), s));
-  CK(cudaMemsetAsync(stats.p, 0, 2 * sizeof(unsigned long long), s));
+  CK(t.Qh.alloc((mb + 1) * cols * 2, s));
+  CK(t.qscale.alloc((mb + 1) * 4, s));
+  CK(t.qnorm.alloc((mb + 1) * 4, s));
+  CK(t.qinex.alloc(mb + 1, s));
+  CK(t.sl_a.alloc(2 * mb * sl * 4, s));
+  CK(t.seed_a.alloc(mb * sl * 4, s));
+  CK(t.seed_row.alloc(mb * sl * 4, s));
+  CK(t.sl_row.alloc(2 * mb * sl * 4, s));
+  CK(t.sl_sel.alloc(mb * 4, s));
+  CK(t.sl_theta.alloc(mb * 4, s));
+  CK(t.sl_lock.alloc(mb * 4, s));
+  if (t.spec) CK(t.sl_cap.alloc(mb * 4, s));
+  CK(t.emax.alloc(mb * 4, s));
+  CK(t.ctl.alloc(64, s));
+  CK(t.failq.alloc(mb * 4, s));
+  CK(t.stats.alloc(2 * sizeof(unsigned long long), s));
+  if (graph) {
+    // the device fallback: every (row chunk, 16 TQ listed queries) pair for
+    // as many queries as the batch holds
+    const uint32_t fkw = list_width_for(k);
+    t.fb_qtile = (uint32_t)search_query_tile(idx->dp, 0, fkw);
+    t.fb_grid = search_grid(idx->metric, idx->dp, 0, fkw);
+    t.fb_chunk = (uint32_t)std::max<uint64_t>(4096, (idx->n + 4ull * t.fb_grid - 1) / (4ull * t.fb_grid));
+    t.fb_chunk = (t.fb_chunk + 31) / 32 * 32;
+    t.fb_cap = ((idx->n + t.fb_chunk - 1) / t.fb_chunk) * ((mb + t.fb_qtile - 1) / t.fb_qtile);
+    CK(t.fb_items.alloc(std::max<uint64_t>(t.fb_cap, 1) * sizeof(SearchItem), s));
+    CK(t.fb_ctl.alloc(64, s));
+  }
+  return RBC_OK;
+}
+
+// The kernels of one batch of mq <= t.mb queries (their rows at dQ, results
+// to dIds / dDists).  Outside graph mode the caller reads the control words
+// and answers the uncertified queries; *tc_probe tells whether a tensor probe
+// round ran (its launch was timed into events 2 and 3 when profiling).
+int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_t ldq, uint32_t *dIds, float *dDists,
+               uint32_t ldo, bool graph, uint32_t *err_sink, bool *tc_probe, cudaStream_t s) {
+  const uint32_t nr = idx->nr, ld = idx->ld, kp = idx->kp, fmt = idx->tc.format, cols = idx->tc.cols;
+  const uint32_t k = t.k, sl = t.sl, kw = t.kw, P = t.P, Pn = t.Pn;
+  const bool spec = t.spec, prof = idx->profile && !graph;
+  QueryBufs &b = t.b;
+  if (tc_probe) *tc_probe = false;
+  CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
+  CK(cudaMemsetAsync(t.ctl.p, 0, 64, s));
+  if (graph) CK(cudaMemsetAsync(t.stats.p, 0, 2 * sizeof(unsigned long long), s));
+  // 1. distances to the representatives, probe table
+  CK(launch_pad_rows(dQ, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
+  CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
+  // the nearest representatives: the shortlist seed and, first, the probe table
+  if (t.routed && !spec) {
+    CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, t.seed_a.as<float>(),
+                       t.seed_row.as<uint32_t>(), t.Pnear, t.near.as<uint32_t>(), t.near_d.as<float>(), s));
+    Router &rt = idx->router->r;
+    if (rt.top_ok(P)) {
+      // the last layer fused with the selection: no logits written
+      CK(rt.probes_tc(b.Qp.as<float>(), ld, (uint32_t)mq, P - Pn, Pn, t.near.as<uint32_t>(), t.near_d.as<float>(),
+                      b.probe.as<uint32_t>(), b.probed.as<float>(), b.ctl.as<uint32_t>() + 2, s));
+    } else {
+      if (rt.tc_ok()) {
+        CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, t.logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
+      } else {
+        const uint32_t chunk = 4096;
+        CK(rt.alloc_batch(chunk, s));
+        for (uint64_t i = 0; i < mq; i += chunk) {
+          const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
+          CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, t.logits.as<float>() + i * nr, s));
+        }
+      }
+      CK(launch_router_probes(t.logits.as<float>(), mq, nr, P - Pn, Pn, t.near.as<uint32_t>(), t.near_d.as<float>(),
+                              b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+    }
+  } else {
+    CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, t.seed_a.as<float>(),
+                       t.seed_row.as<uint32_t>(), P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
+    if (spec)
+      CK(idx->router->r.predict_tau(b.Qp.as<float>(), ld, (uint32_t)mq, b.probed.as<float>(), t.tpred.as<float>(),
+                                    b.ctl.as<uint32_t>() + 2, s));
+  }
+  CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(), mq,
+                         kw, s));
+  // query operands (row mq is the zero row gathered for empty item slots)
+  CK(launch_tc_queries(b.Qp.as<float>(), ld, mq, idx->d, kp, fmt, idx->tc.mu, t.Qh.p, t.qscale.as<float>(),
+                       t.qnorm.as<float>(), t.qinex.as<uint8_t>(), s));
+  CUtensorMap tmA;
+  CK(tc_make_map(&tmA, t.Qh.p, mq + 1, cols, 1));
+  CK(launch_sl_init(t.sl_a.as<float>(), t.sl_row.as<uint32_t>(), t.sl_sel.as<uint32_t>(), t.sl_theta.as<uint32_t>(),
+                    t.sl_lock.as<uint32_t>(), t.emax.as<uint32_t>(), mq, sl, s));
+  TcArgs ta{};
+  ta.items = b.items.as<SearchItem>();
+  ta.nitems = b.ctl.as<uint32_t>() + 1;
+  ta.qidx = b.pair_q.as<uint32_t>();
+  ta.Dqr = b.Dqr.as<float>();
+  ta.nr = nr;
+  ta.kb = kp / 64;
+  ta.zero_row = (uint32_t)mq;
+  ta.d = idx->d;
+  ta.w = idx->tc.w;
+  ta.wh = static_cast<const uint4 *>(idx->tc.Wh);
+  ta.lscale = idx->tc.lscale;
+  ta.lxmax = idx->tc.lxmax;
+  ta.lcnorm = idx->tc.lcnorm;
+  ta.qscale = t.qscale.as<float>();
+  ta.qnorm = t.qnorm.as<float>();
+  ta.q_inexact = t.qinex.as<uint8_t>();
+  ta.x_inexact = idx->tc.x_inexact;
+  ta.format = fmt;
+  ta.sl = sl;
+  ta.sl_a = t.sl_a.as<float>();
+  ta.sl_row = t.sl_row.as<uint32_t>();
+  ta.sl_sel = t.sl_sel.as<uint32_t>();
+  ta.sl_theta = t.sl_theta.as<uint32_t>();
+  ta.sl_cap = spec ? t.sl_cap.as<uint32_t>() : nullptr;
+  ta.sl_lock = t.sl_lock.as<uint32_t>();
+  ta.emax = t.emax.as<uint32_t>();
+  ta.m = mq;
+  ta.offsets = idx->offsets;
+  ta.stats = t.stats.as<unsigned long long>();
+  ta.err = t.ctl.as<uint32_t>();
+  RerankArgs ra{};
+  ra.X = idx->Xp;
+  ra.pid = idx->perm;
+  ra.Q = b.Qp.as<float>();
+  ra.ld = ld;
+  ra.dp = idx->dp;
+  ra.k = k;
+  ra.sl = sl;
+  ra.m = mq;
+  ra.sl_a = t.sl_a.as<float>();
+  ra.sl_row = t.sl_row.as<uint32_t>();
+  ra.sl_sel = t.sl_sel.as<uint32_t>();
+  ra.emax = t.emax.as<uint32_t>();
+  ra.sl_cap = spec ? t.sl_cap.as<uint32_t>() : nullptr;
+  ra.tplan = nullptr;
+  ra.ldo = ldo;
+  ra.nfail = t.ctl.as<uint32_t>() + 1;
+  ra.fail = t.failq.as<uint32_t>();
+  // probe round, small lists: searched exactly on the FP32 path; every
+  // query's exact top-sl there seeds its shortlist, and its k-th distance
+  // the pruning threshold (none in the speculative plan: the seed is the
+  // nearest representatives, the threshold the prediction)
+  if (!spec) {
+    const bool keep = idx->profile;
+    idx->profile = false;
+    // the first probe_rows rows of every probed list (whole lists when
+    // shorter): exact seeds that give the tensor round a tight threshold
+    ListFilter small;
+    small.take = t.probe_rows;
+    const int rc = plan_and_search(idx, b, mq, P, sl, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, t.pgrid,
+                                   nullptr, s, 2, t.ptq, 0, small);
+    idx->profile = keep;
+    TRY(rc);
+  }
+  CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, t.seed_a.as<float>(),
+                    t.seed_row.as<uint32_t>(), mq, sl, k, t.sl_a.as<float>(), t.sl_row.as<uint32_t>(),
+                    t.sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));
+  // the speculative plan: the predicted k-th distance lowers the planning
+  // threshold and caps every shortlist (only rows that can still reach the
+  // top k pass the tensor search's filter); the certificate then also
+  // checks the k-th distance against it
+  if (spec) {
+    CK(launch_cap(b.tau.as<uint32_t>(), t.tpred.as<float>(), mq, t.sl_cap.as<uint32_t>(), t.sl_theta.as<uint32_t>(),
+                  s));
+    ra.tplan = b.tau.as<uint32_t>();
+  }
+  // probe round, large lists: tensor search into the seeded shortlists, one
+  // 128-query tile per B tile (measured faster than two-tile items even for
+  // the busiest probed lists), then the k-th exact distance of each
+  // shortlist tightens the threshold
+  if (!spec && idx->max_list > t.probe_rows) {
+    ListFilter large;  // the rest of the longer lists
+    large.rows_lo = t.probe_rows + 1;
+    large.skip = t.probe_rows;
+    TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, t.sgrid, nullptr, s, 1, -1,
+                        tc_query_tile(kTcSplit), large));
+    if (prof) CK(cudaEventRecord(idx->ev_pool[2], s));
+    CK(launch_tc_search(tmA, idx->tmB, ta, t.grid, s, true));
+    if (prof) CK(cudaEventRecord(idx->ev_pool[3], s));
+    if (tc_probe) *tc_probe = true;
+    ra.tau = b.tau.as<uint32_t>();
+    ra.ids = nullptr;
+    ra.dists = nullptr;
+    CK(launch_rerank(idx->metric, ra, s));
+  }
+  // pruned round: every other list whose bound survives, on the tensor
+  // cores, into the same shortlists; exact rerank and certificate
+  TRY(plan_and_search(idx, b, mq, P, k, 1, idx->Xp, idx->perm, idx->offsets, idx->radius, t.sgrid, nullptr, s, 1, -1,
+                      t.qtile));
+  if (prof) CK(cudaEventRecord(idx->ev_pool[0], s));
+  CK(launch_tc_search(tmA, idx->tmB, ta, t.grid, s));
+  if (prof) CK(cudaEventRecord(idx->ev_pool[1], s));
+  ra.tau = nullptr;
+  ra.ids = dIds;
+  ra.dists = dDists;
+  CK(launch_rerank(idx->metric, ra, s));
+  if (!graph) return RBC_OK;
+  // graph mode: the queries the certificate left open (their count and rows
+  // on the device) searched again over every row on the FP32 path, their
+  // answers written over the tensor form's
+  const uint32_t fkw = list_width_for(k);
+  uint32_t *fctl = t.fb_ctl.as<uint32_t>();  // [0] work, [1] items, [2] error
+  CK(cudaMemsetAsync(fctl, 0, 64, s));
+  CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(), mq,
+                         fkw, s));
+  CK(launch_listed_items(t.fb_items.as<SearchItem>(), fctl + 1, t.ctl.as<uint32_t>() + 1, idx->n, t.fb_chunk,
+                         t.fb_qtile, t.fb_cap, fctl + 2, s));
+  SearchArgs fa{};
+  fa.X = idx->Xp;
+  fa.pid = idx->perm;
+  fa.Q = b.Qp.as<float>();
+  fa.qidx = t.failq.as<uint32_t>();
+  fa.items = t.fb_items.as<SearchItem>();
+  fa.nitems = fctl + 1;
+  fa.work = fctl;
+  fa.res_d = b.res_d.as<float>();
+  fa.res_i = b.res_i.as<uint32_t>();
+  fa.tau = b.tau.as<uint32_t>();
+  fa.lock = b.lock.as<uint32_t>();
+  fa.err = fctl + 2;
+  fa.ld = ld;
+  fa.dp = idx->dp;
+  fa.k = k;
+  CK(launch_search(idx->metric, fa, t.fb_grid, s));
+  CK(launch_listed_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), fkw, t.failq.as<uint32_t>(),
+                           t.ctl.as<uint32_t>() + 1, mq, k, dIds, dDists, ldo, s));
+  if (err_sink) {
+    ErrWords w{};
+    w.w[0] = t.ctl.as<uint32_t>();
+    w.w[1] = b.ctl.as<uint32_t>() + 2;
+    w.w[2] = fctl + 2;
+    CK(launch_fold_errors(w, err_sink, s));
+  }
+  return RBC_OK;
+}
+
+// Tensor-core exact query: tc_setup, then per batch tc_enqueue, the control
+// words read back, and the uncertified queries answered again on the host's
+// command (the FP32 exact search, or for a speculative plan the tensor form
+// with its probe round).
+int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode, uint32_t *dIds,
+             float *dDists, uint32_t ldo, cudaStream_t s) {
+  pool_setup();
+  const uint32_t nr = idx->nr, ld = idx->ld;
+  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(tc_query_tile(idx->tc.format), (1ull << 27) / nr));
+  TcQuery t;
+  TRY(tc_setup(idx, mb, k, mode, false, t, s));
+  CK(cudaMemsetAsync(t.stats.p, 0, 2 * sizeof(unsigned long long), s));
   uint64_t nfail_total = 0;
   idx->fallback_ids.clear();
   double tc_ms = 0;
@@ -659,161 +890,11 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   for (uint64_t b0 = 0; b0 < m; b0 += mb) {
     const uint64_t mq = std::min(mb, m - b0);
     bool tc_probe = false;
-    CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
-    CK(cudaMemsetAsync(ctl.p, 0, 64, s));
-    // 1. distances to the representatives, probe table
-    CK(launch_pad_rows(dQ + b0 * ldq, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
-    CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
-    // the nearest representatives: the shortlist seed and, first, the probe table
-    if (routed && !spec) {
-      CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(),
-                         seed_row.as<uint32_t>(), Pnear, near.as<uint32_t>(), near_d.as<float>(), s));
-      Router &rt = idx->router->r;
-      if (rt.top_ok(P)) {
-        // the last layer fused with the selection: no logits written
-        CK(rt.probes_tc(b.Qp.as<float>(), ld, (uint32_t)mq, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
-                        b.probe.as<uint32_t>(), b.probed.as<float>(), b.ctl.as<uint32_t>() + 2, s));
-      } else {
-        if (rt.tc_ok()) {
-          CK(rt.forward_tc(b.Qp.as<float>(), ld, (uint32_t)mq, logits.as<float>(), b.ctl.as<uint32_t>() + 2, s));
-        } else {
-          const uint32_t chunk = 4096;
-          CK(rt.alloc_batch(chunk, s));
-          for (uint64_t i = 0; i < mq; i += chunk) {
-            const uint32_t cb = (uint32_t)std::min<uint64_t>(chunk, mq - i);
-            CK(rt.forward(b.Qp.as<float>() + i * ld, ld, cb, logits.as<float>() + i * nr, s));
-          }
-        }
-        CK(launch_router_probes(logits.as<float>(), mq, nr, P - Pn, Pn, near.as<uint32_t>(), near_d.as<float>(),
-                                b.probe.as<uint32_t>(), b.probed.as<float>(), s));
-      }
-    } else {
-      CK(launch_rep_seed(b.Dqr.as<float>(), mq, nr, idx->tc.rep_rows, sl, seed_a.as<float>(),
-                         seed_row.as<uint32_t>(), P, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
-      if (spec)
-        CK(idx->router->r.predict_tau(b.Qp.as<float>(), ld, (uint32_t)mq, b.probed.as<float>(), tpred.as<float>(),
-                                      b.ctl.as<uint32_t>() + 2, s));
-    }
-    CK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(), b.lock.as<uint32_t>(),
-                           mq, kw, s));
-    // query operands (row mq is the zero row gathered for empty item slots)
-    CK(launch_tc_queries(b.Qp.as<float>(), ld, mq, idx->d, kp, fmt, idx->tc.mu, Qh.p, qscale.as<float>(),
-                         qnorm.as<float>(), qinex.as<uint8_t>(), s));
-    CUtensorMap tmA;
-    CK(tc_make_map(&tmA, Qh.p, mq + 1, cols, 1));
-    CK(launch_sl_init(sl_a.as<float>(), sl_row.as<uint32_t>(), sl_sel.as<uint32_t>(), sl_theta.as<uint32_t>(),
-                      sl_lock.as<uint32_t>(), emax.as<uint32_t>(), mq, sl, s));
-    TcArgs ta{};
-    ta.items = b.items.as<SearchItem>();
-    ta.nitems = b.ctl.as<uint32_t>() + 1;
-    ta.qidx = b.pair_q.as<uint32_t>();
-    ta.Dqr = b.Dqr.as<float>();
-    ta.nr = nr;
-    ta.kb = kp / 64;
-    ta.zero_row = (uint32_t)mq;
-    ta.d = idx->d;
-    ta.w = idx->tc.w;
-    ta.wh = static_cast<const uint4 *>(idx->tc.Wh);
-    ta.lscale = idx->tc.lscale;
-    ta.lxmax = idx->tc.lxmax;
-    ta.lcnorm = idx->tc.lcnorm;
-    ta.qscale = qscale.as<float>();
-    ta.qnorm = qnorm.as<float>();
-    ta.q_inexact = qinex.as<uint8_t>();
-    ta.x_inexact = idx->tc.x_inexact;
-    ta.format = fmt;
-    ta.sl = sl;
-    ta.sl_a = sl_a.as<float>();
-    ta.sl_row = sl_row.as<uint32_t>();
-    ta.sl_sel = sl_sel.as<uint32_t>();
-    ta.sl_theta = sl_theta.as<uint32_t>();
-    ta.sl_cap = spec ? sl_cap.as<uint32_t>() : nullptr;
-    ta.sl_lock = sl_lock.as<uint32_t>();
-    ta.emax = emax.as<uint32_t>();
-    ta.m = mq;
-    ta.offsets = idx->offsets;
-    ta.stats = stats.as<unsigned long long>();
-    ta.err = ctl.as<uint32_t>();
-    RerankArgs ra{};
-    ra.X = idx->Xp;
-    ra.pid = idx->perm;
-    ra.Q = b.Qp.as<float>();
-    ra.ld = ld;
-    ra.dp = idx->dp;
-    ra.k = k;
-    ra.sl = sl;
-    ra.m = mq;
-    ra.sl_a = sl_a.as<float>();
-    ra.sl_row = sl_row.as<uint32_t>();
-    ra.sl_sel = sl_sel.as<uint32_t>();
-    ra.emax = emax.as<uint32_t>();
-    ra.sl_cap = spec ? sl_cap.as<uint32_t>() : nullptr;
-    ra.tplan = nullptr;
-    ra.ldo = ldo;
-    ra.nfail = ctl.as<uint32_t>() + 1;
-    ra.fail = failq.as<uint32_t>();
-    // probe round, small lists: searched exactly on the FP32 path; every
-    // query's exact top-sl there seeds its shortlist, and its k-th distance
-    // the pruning threshold (none in the speculative plan: the seed is the
-    // nearest representatives, the threshold the prediction)
-    if (!spec) {
-      const bool prof = idx->profile;
-      idx->profile = false;
-      // the first probe_rows rows of every probed list (whole lists when
-      // shorter): exact seeds that give the tensor round a tight threshold
-      ListFilter small;
-      small.take = probe_rows;
-      const int rc = plan_and_search(idx, b, mq, P, sl, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, pgrid,
-                                     nullptr, s, 2, ptq, 0, small);
-      idx->profile = prof;
-      TRY(rc);
-    }
-    CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, seed_a.as<float>(),
-                      seed_row.as<uint32_t>(), mq, sl, k, sl_a.as<float>(), sl_row.as<uint32_t>(),
-                      sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));
-    // the speculative plan: the predicted k-th distance lowers the planning
-    // threshold and caps every shortlist (only rows that can still reach the
-    // top k pass the tensor search's filter); the certificate then also
-    // checks the k-th distance against it
-    if (spec) {
-      CK(launch_cap(b.tau.as<uint32_t>(), tpred.as<float>(), mq, sl_cap.as<uint32_t>(), sl_theta.as<uint32_t>(), s));
-      ra.tplan = b.tau.as<uint32_t>();
-    }
-    // probe round, large lists: tensor search into the seeded shortlists, one
-    // 128-query tile per B tile (measured faster than two-tile items even for
-    // the busiest probed lists), then the k-th exact distance of each
-    // shortlist tightens the threshold
-    if (!spec && idx->max_list > probe_rows) {
-      ListFilter large;  // the rest of the longer lists
-      large.rows_lo = probe_rows + 1;
-      large.skip = probe_rows;
-      TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
-                          -1, tc_query_tile(kTcSplit), large));
-      if (idx->profile) CK(cudaEventRecord(idx->ev_pool[2], s));
-      CK(launch_tc_search(tmA, idx->tmB, ta, grid, s, true));
-      if (idx->profile) {
-        CK(cudaEventRecord(idx->ev_pool[3], s));
-        tc_probe = true;
-      }
-      ra.tau = b.tau.as<uint32_t>();
-      ra.ids = nullptr;
-      ra.dists = nullptr;
-      CK(launch_rerank(idx->metric, ra, s));
-    }
-    // pruned round: every other list whose bound survives, on the tensor
-    // cores, into the same shortlists; exact rerank and certificate
-    TRY(plan_and_search(idx, b, mq, P, k, 1, idx->Xp, idx->perm, idx->offsets, idx->radius, sgrid, nullptr, s, 1,
-                        -1, qtile));
-    if (idx->profile) CK(cudaEventRecord(idx->ev_pool[0], s));
-    CK(launch_tc_search(tmA, idx->tmB, ta, grid, s));
-    if (idx->profile) CK(cudaEventRecord(idx->ev_pool[1], s));
-    ra.tau = nullptr;
-    ra.ids = dIds ? dIds + b0 * ldo : nullptr;
-    ra.dists = dDists ? dDists + b0 * ldo : nullptr;
-    CK(launch_rerank(idx->metric, ra, s));
+    TRY(tc_enqueue(idx, t, dQ + b0 * ldq, mq, ldq, dIds ? dIds + b0 * ldo : nullptr,
+                   dDists ? dDists + b0 * ldo : nullptr, ldo, false, nullptr, &tc_probe, s));
     uint32_t hc[2], bc[3];
-    CK(cudaMemcpyAsync(hc, ctl.p, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(bc, b.ctl.p, 12, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hc, t.ctl.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(bc, t.b.ctl.p, 12, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (hc[0] || bc[2])
       return fail(hc[0] ? (int)hc[0] : (int)bc[2], "rbc_query: a device-side check failed (bounded wait or work-list size)");
@@ -832,7 +913,7 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
     nfail_total += nfail;
     if (nfail) {
       std::vector<uint32_t> f(nfail);
-      CK(cudaMemcpy(f.data(), failq.p, nfail * 4ull, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(f.data(), t.failq.p, nfail * 4ull, cudaMemcpyDeviceToHost));
       std::sort(f.begin(), f.end());
       for (uint32_t q : f) idx->fallback_ids.push_back((uint32_t)(b0 + q));
     }
@@ -841,13 +922,13 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       CK(Qf.alloc((uint64_t)nfail * ld * 4, s));
       CK(fi.alloc((uint64_t)nfail * k * 4, s));
       CK(fd.alloc((uint64_t)nfail * k * 4, s));
-      CK(launch_gather_rows(b.Qp.as<float>(), ld, failq.as<uint32_t>(), nfail, Qf.as<float>(), s));
+      CK(launch_gather_rows(t.b.Qp.as<float>(), ld, t.failq.as<uint32_t>(), nfail, Qf.as<float>(), s));
       rbc_profile keep = idx->prof;
       rbc_query_stats keep_stats = idx->stats;
       const int keep_tq = idx->tune_tq;
       const bool keep_profile = idx->profile;
       int rc;
-      if (spec) {
+      if (t.spec) {
         // a prediction that fell short (or a certificate left open): the
         // tensor form again, with its probe round this time
         std::vector<uint32_t> keep_fb;
@@ -864,13 +945,13 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       idx->prof = keep;
       idx->stats = keep_stats;
       TRY(rc);
-      CK(launch_scatter_results(fi.as<uint32_t>(), fd.as<float>(), failq.as<uint32_t>(), nfail, k,
+      CK(launch_scatter_results(fi.as<uint32_t>(), fd.as<float>(), t.failq.as<uint32_t>(), nfail, k,
                                 dIds ? dIds + b0 * ldo : nullptr, dDists ? dDists + b0 * ldo : nullptr, ldo, s));
       CK(cudaStreamSynchronize(s));
     }
   }
   unsigned long long st[2] = {0, 0};
-  CK(cudaMemcpy(st, stats.p, sizeof(st), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(st, t.stats.p, sizeof(st), cudaMemcpyDeviceToHost));
   idx->stats.queries = m;
   idx->stats.rep_pairs = m * nr;
   idx->stats.point_pairs = st[0];

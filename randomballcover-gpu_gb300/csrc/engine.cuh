@@ -53,6 +53,27 @@ struct QueryBufs {
   bool plan_all = false;       // the pruning round plans every list (no probe round ran)
 };
 
+// One tensor-form query round set up for batches of up to mb queries: the
+// host-side choices and every buffer (tc_setup), then the kernels of one
+// batch (tc_enqueue).  In graph mode tc_enqueue synchronises nothing: the
+// queries the certificate leaves open are searched again on the device (the
+// FP32 search over the whole database, its work list sized by their count on
+// the device) and the error words are folded into err_sink.
+struct TcQuery {
+  bool routed = false, spec = false;
+  uint32_t k = 0, Pn = 0, Pnear = 0, P = 0, sl = 0, kw = 0, qtile = 0;
+  uint64_t probe_rows = 0, mb = 0;
+  int grid = 0, sgrid = 0, ptq = 0, pgrid = 0;
+  QueryBufs b;
+  DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
+      stats, seed_a, seed_row, sl_cap, tpred;
+  // graph mode: the device fallback's work list and control words
+  DevBuf fb_items, fb_ctl;
+  uint32_t fb_chunk = 0, fb_qtile = 0;
+  uint64_t fb_cap = 0;
+  int fb_grid = 0;
+};
+
 }  // namespace rbc
 
 struct rbc_index;
@@ -75,6 +96,9 @@ int build_tc(rbc_index *idx, cudaStream_t s);
 uint64_t item_capacity(const rbc_index *idx, uint64_t mb, uint32_t qtile, uint32_t probes = 0);
 int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
                 uint32_t *dIds, float *dDists, uint32_t ldo, cudaStream_t s);
+int tc_setup(rbc_index *idx, uint64_t mb, uint32_t k, uint32_t mode, bool graph, TcQuery &t, cudaStream_t s);
+int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_t ldq, uint32_t *dIds, float *dDists,
+               uint32_t ldo, bool graph, uint32_t *err_sink, bool *tc_probe, cudaStream_t s);
 int build_index(const float *dX, uint64_t n, uint32_t d, uint32_t ldx, const rbc_build_params *p,
                 cudaStream_t s, rbc_index **out);
 int brute_knn(const float *dX, uint64_t n, uint32_t ldx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t d,

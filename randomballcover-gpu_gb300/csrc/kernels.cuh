@@ -69,6 +69,19 @@ cudaError_t launch_scatter_results(const uint32_t *src_i, const float *src_d, co
                                    cudaStream_t s);
 cudaError_t launch_brute_items(SearchItem *items, uint32_t *nitems, uint32_t *qidx, uint64_t n,
                                uint32_t chunk, uint64_t m, uint32_t qtile, cudaStream_t s);
+// The same over every row for the queries listed first in a slot array, their
+// number *count read on the device; at most cap items (RBC_ERR_NOMEM otherwise).
+cudaError_t launch_listed_items(SearchItem *items, uint32_t *nitems, const uint32_t *count, uint64_t n, uint32_t chunk,
+                                uint32_t qtile, uint64_t cap, uint32_t *err, cudaStream_t s);
+// ids[rows[r] * ldo + j] = res_i[rows[r] * kw + j] (and the distances) for r < *count (<= cap).
+cudaError_t launch_listed_results(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *rows,
+                                  const uint32_t *count, uint64_t cap, uint32_t k, uint32_t *ids, float *dists,
+                                  uint32_t ldo, cudaStream_t s);
+// *dst = max(*dst, *src.w[i]) over the non-null src.w[i] (error words folded into one).
+struct ErrWords {
+  const uint32_t *w[4];
+};
+cudaError_t launch_fold_errors(ErrWords src, uint32_t *dst, cudaStream_t s);
 
 // Row-matrix utilities.
 cudaError_t launch_pad_rows(const float *src, uint64_t ld_src, float *dst, uint32_t ld_dst,

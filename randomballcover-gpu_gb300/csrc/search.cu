@@ -331,7 +331,76 @@ __global__ void brute_items_kernel(SearchItem *items, uint32_t *nitems, uint32_t
   if (i == 0) *nitems = (uint32_t)(nchunks * ntile);
 }
 
+// Work items of the search over every row for the queries listed first in a
+// slot array, their number (*count) known only on the device: every (row
+// chunk, tile of listed queries) pair, chunk-major.  A count whose items
+// would not fit cap gives no items and records RBC_ERR_NOMEM (the caller
+// sizes cap for every query of the batch, so this cannot happen).
+__global__ void listed_items_kernel(SearchItem *items, uint32_t *nitems, const uint32_t *count, uint64_t n,
+                                    uint32_t chunk, uint32_t qtile, uint64_t cap, uint32_t *err) {
+  const uint32_t c = *count;
+  const uint64_t nchunks = (n + chunk - 1) / chunk, ntile = (c + (uint64_t)qtile - 1) / qtile;
+  const uint64_t total = nchunks * ntile;
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i == 0) {
+    *nitems = total <= cap ? (uint32_t)total : 0u;
+    if (total > cap) atomicMax(err, (uint32_t)RBC_ERR_NOMEM);
+  }
+  if (total > cap || i >= total) return;
+  const uint64_t ch = i / ntile, t = i - ch * ntile;
+  SearchItem it;
+  it.p0 = ch * chunk;
+  it.np = (uint32_t)min((uint64_t)chunk, n - ch * chunk);
+  it.list = RBC_DUMMY;
+  it.q0 = (uint32_t)(t * qtile);
+  it.nq = (uint32_t)min((uint64_t)qtile, (uint64_t)c - t * qtile);
+  it.inst = 0;
+  it.pad = 0;
+  items[i] = it;
+}
+
+// ids / dists rows of the *count queries listed in rows[] from the per-query lists.
+__global__ void listed_results_kernel(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *rows,
+                                      const uint32_t *count, uint64_t cap, uint32_t k, uint32_t *ids, float *dists,
+                                      uint32_t ldo) {
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t r = i / k;
+  if (r >= cap || r >= *count) return;
+  const uint32_t j = (uint32_t)(i - r * k), q = rows[r];
+  if (ids) ids[(uint64_t)q * ldo + j] = res_i[(uint64_t)q * kw + j];
+  if (dists) dists[(uint64_t)q * ldo + j] = res_d[(uint64_t)q * kw + j];
+}
+
+__global__ void fold_errors_kernel(ErrWords src, uint32_t *dst) {
+  uint32_t v = 0;
+  for (int i = 0; i < 4; i++)
+    if (src.w[i]) v = max(v, *src.w[i]);
+  if (v) atomicMax(dst, v);
+}
+
 }  // namespace
+
+cudaError_t launch_fold_errors(ErrWords src, uint32_t *dst, cudaStream_t s) {
+  fold_errors_kernel<<<1, 1, 0, s>>>(src, dst);
+  return launched();
+}
+
+cudaError_t launch_listed_items(SearchItem *items, uint32_t *nitems, const uint32_t *count, uint64_t n, uint32_t chunk,
+                                uint32_t qtile, uint64_t cap, uint32_t *err, cudaStream_t s) {
+  const uint64_t threads = std::max<uint64_t>(cap, 1);
+  listed_items_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(items, nitems, count, n, chunk, qtile, cap,
+                                                                        err);
+  return launched();
+}
+
+cudaError_t launch_listed_results(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *rows,
+                                  const uint32_t *count, uint64_t cap, uint32_t k, uint32_t *ids, float *dists,
+                                  uint32_t ldo, cudaStream_t s) {
+  const uint64_t total = std::max<uint64_t>(cap * k, 1);
+  listed_results_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(res_d, res_i, kw, rows, count, cap, k, ids,
+                                                                        dists, ldo);
+  return launched();
+}
 
 // Rows per thread in the query dimension (query tile = 16 TQ).  The default
 // keeps the shared-memory tile under ~100 KB; `tq` (1, 2 or 4) overrides it

@@ -76,6 +76,7 @@ SIGNATURES = {
     "rbc_get_fallback_queries": ([_VP, _VP, _U64, C.POINTER(_U64)], _INT),
     "rbc_batch_create": ([C.POINTER(_VP)], _INT),
     "rbc_batch_add": ([_VP, _VP, _VP, _U64, _U32, _U32, _VP, _VP, _U32], _INT),
+    "rbc_batch_add_mode": ([_VP, _VP, _VP, _U64, _U32, _U32, _U32, _VP, _VP, _U32], _INT),
     "rbc_batch_run": ([_VP, _VP], _INT),
     "rbc_batch_destroy": ([_VP], _INT),
     "rbc_set_tuning": ([_VP, _INT, _U32], _INT),
@@ -363,14 +364,16 @@ class Batch:
         self.h = h
         self.keep = []
 
-    def add(self, index, Q, k):
-        """Queries Q (CUDA tensor, kept alive by the batch); returns (ids, dists) filled by run()."""
+    def add(self, index, Q, k, mode=QUERY_EXACT):
+        """Queries Q (CUDA tensor, kept alive by the batch); returns (ids, dists)
+        filled by run().  mode QUERY_EXACT_TC answers the instance with the
+        tensor form (BF16 index, k <= 32)."""
         import torch
         m = Q.shape[0]
         ids = torch.empty((m, k), dtype=torch.int32, device=Q.device)
         dists = torch.empty((m, k), dtype=torch.float32, device=Q.device)
-        check(lib().rbc_batch_add(self.h, index.h, Q.data_ptr(), m, Q.stride(0), k, ids.data_ptr(),
-                                  dists.data_ptr(), k))
+        check(lib().rbc_batch_add_mode(self.h, index.h, Q.data_ptr(), m, Q.stride(0), k, mode, ids.data_ptr(),
+                                       dists.data_ptr(), k))
         self.keep.append((index, Q, ids, dists))
         return ids, dists
 

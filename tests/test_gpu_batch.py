@@ -57,6 +57,53 @@ def test_batch_heterogeneous_instances(rbc, oracle, metric):
         c[0].close()
 
 
+def test_batch_tensor_form_instances(rbc, oracle):
+    """Tensor-form instances (RBC_QUERY_EXACT_TC) in one captured graph beside
+    an FP32 one: the split operand format (float mixture), the BF16 format
+    (integer features, k = 32), and rows repeated 60 times, where tied
+    distances leave nearly every certificate open so the device-side
+    re-search answers those queries.  Exact on the first run and on replays
+    with new query values."""
+    rng = np.random.default_rng(77)
+    batch = rbc.Batch()
+    cases = []
+
+    def add(X, Qn, nr, k, mode, seed):
+        flags = rbc.BUILD_PARTITION | (rbc.BUILD_BF16 if mode == rbc.QUERY_EXACT_TC else 0)
+        idx = rbc.Index(X, nr, seed=seed, flags=flags)
+        Qd = torch.from_numpy(Qn).cuda()
+        ids, dists = batch.add(idx, Qd, k, mode=mode)
+        cases.append((idx, X, Qd, k, ids, dists))
+
+    add(clustered(rng, 30000, 64, centers=300, spread=0.3), clustered(rng, 300, 64, centers=300, spread=0.3), 200, 10,
+        rbc.QUERY_EXACT_TC, 1)
+    add(rng.integers(0, 40, (20000, 128)).astype(np.float32), rng.integers(0, 40, (257, 128)).astype(np.float32), 100,
+        32, rbc.QUERY_EXACT_TC, 2)
+    base = rng.standard_normal((300, 32)).astype(np.float32)
+    add(np.repeat(base, 60, axis=0), rng.standard_normal((150, 32)).astype(np.float32), 64, 10, rbc.QUERY_EXACT_TC, 3)
+    add(clustered(rng, 5000, 37), clustered(rng, 200, 37), 100, 5, rbc.QUERY_EXACT, 4)
+    assert cases[0][0].info()["tc_format"] == rbc.TC_FP16_SPLIT and cases[1][0].info()["tc_format"] == rbc.TC_BF16
+    for rep in range(3):
+        if rep:
+            for idx, X, Qd, k, ids, dists in cases:
+                if rep == 2 and X.shape[1] == 128:
+                    Qd.copy_(torch.from_numpy(rng.integers(0, 40, tuple(Qd.shape)).astype(np.float32)))
+                elif rep == 2:
+                    Qd.copy_(Qd[torch.randperm(Qd.shape[0], device=Qd.device)] + 0.01)
+        batch.run()
+        torch.cuda.synchronize()
+        for idx, X, Qd, k, ids, dists in cases:
+            check_exact(ids, dists, X, Qd.cpu().numpy(), k, 0, rbc, oracle)
+    # the duplicate-heavy instance: the tensor form alone leaves most of its
+    # certificates open (the batch answered them on the device)
+    idx, X, Qd = cases[2][0], cases[2][1], cases[2][2]
+    idx.query(Qd, 10, mode=rbc.QUERY_EXACT_TC)
+    assert idx.stats()["fallback_queries"] > Qd.shape[0] // 2
+    batch.close()
+    for c in cases:
+        c[0].close()
+
+
 def test_batch_64_instances_config_shape(rbc, oracle):
     """The batched configuration's shape scaled down: 64 instances, n log-uniform,
     d in {32, 64, 128}, k in {1, 10, 32}, m = n / 100, Gaussian mixtures with
