@@ -458,7 +458,8 @@ def run_engine(a):
         if clocks:
             clocks.start()
         l0 = pyrbc.kernel_launches()
-        acc = {"search_ms": 0.0, "search_launches": 0, "point_pairs": 0, "lists": 0, "fallback": 0}
+        acc = {"search_ms": 0.0, "search_launches": 0, "point_pairs": 0, "lists": 0, "fallback": 0,
+               "pruned_ms": 0.0, "pruned_launches": 0, "pruned_pairs": 0}
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
@@ -468,6 +469,8 @@ def run_engine(a):
             st = idx.stats()
             acc["search_ms"] += p["search_ms"]
             acc["search_launches"] += p["search_launches"]
+            for key in ("pruned_ms", "pruned_launches", "pruned_pairs"):
+                acc[key] += p[key]
             acc["point_pairs"] += st["point_pairs"]
             acc["lists"] += st["lists_probed"]
             acc["fallback"] += st["fallback_queries"]
@@ -542,6 +545,26 @@ def run_engine(a):
                 "frac": achieved / bf16, "traffic": committed_traffic(kernel), "kernel": kernel,
                 "peak_source": f"{src} bf16 dense burst (MEASURED_PEAKS.json)",
                 "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
+    if not head_plain and res["pruned_launches"] and res["pruned_launches"] < res["search_launches"]:
+        # the tensor form launches two instances of its list search per
+        # call: the pruned round (two query tiles per B tile, the dominant
+        # launch) and the probe round's large lists (one query tile); the
+        # roofline is the pruned round's, both together are listed beside it
+        pl = res["pruned_launches"]
+        p_flops = res["pruned_pairs"] * 2 * w["d"] / pl
+        p_s = res["pruned_ms"] / pl / 1000.0
+        o_l = res["search_launches"] - pl
+        o_s = (res["search_ms"] - res["pruned_ms"]) / max(o_l, 1) / 1000.0
+        o_flops = (res["point_pairs"] - res["pruned_pairs"]) * 2 * w["d"] / max(o_l, 1)
+        all_launches = {k_: roofline.pop(k_) for k_ in ("achieved", "frac", "flops_per_launch", "avg_launch_ms")}
+        roofline.update({"achieved": p_flops / p_s / 1e12, "frac": p_flops / p_s / 1e12 / bf16,
+                         "kernel": f"tc_search_kernel<MT={1 if idx.info()['tc_format'] else 2}> (pruned round)",
+                         "flops_per_launch": p_flops,
+                         "avg_launch_ms": p_s * 1e3,
+                         "probe_round_launch": {"kernel": "tc_search_kernel<MT=1> (probe round, large lists)",
+                                                "avg_launch_ms": o_s * 1e3, "flops_per_launch": o_flops,
+                                                "achieved": o_flops / o_s / 1e12 if o_s > 0 else 0.0},
+                         "all_tensor_launches": all_launches})
     if head_plain:
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
         roofline["fp32_core"] = {"achieved_tflops": achieved, "peak_tflops": fp32_peak, "frac": achieved / fp32_peak,

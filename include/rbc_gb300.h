@@ -301,6 +301,12 @@ int rbc_router_set_distance_margin(rbc_router *router, float margin);
 typedef struct {
   uint64_t search_launches; /* list-search kernel launches in the last query call */
   double search_ms;         /* their summed duration in milliseconds            */
+  /* tensor form: the pruned round's launches alone (the probe round's large
+   * lists are the rest of the launches above) and the (query, row) pairs
+   * they evaluated; zero for the other forms */
+  uint64_t pruned_launches;
+  double pruned_ms;
+  uint64_t pruned_pairs;
 } rbc_profile;
 int rbc_set_profiling(rbc_index *index, int enable);
 int rbc_get_profile(const rbc_index *index, rbc_profile *profile);

@@ -109,7 +109,8 @@ namespace {
 // Allocate every buffer, then record the whole sequence on a capture stream
 // into a graph: the FP32 instances' two rounds, each one persistent search
 // launch over all of them, then every tensor-form instance's round (its
-// uncertified queries searched again on the device).
+// uncertified queries searched again on the device), the per-instance work
+// on parallel branches.
 int prepare(rbc_batch *bt) {
   std::vector<BatchInstance *> fp, tcv;
   for (auto &ip : bt->inst) (ip->mode == RBC_QUERY_EXACT_TC ? tcv : fp).push_back(ip.get());
@@ -178,20 +179,29 @@ int prepare(rbc_batch *bt) {
     ip->tc = std::make_unique<TcQuery>();
     BTRY(tc_setup(ip->idx, ip->m, ip->k, RBC_QUERY_EXACT_TC, true, *ip->tc, s));
   }
-  // the tensor-form instances are captured on side streams forked from the
-  // capture stream and joined back, so the graph holds them as parallel
-  // branches (a few at a time share the GPU instead of running in turn)
-  const uint32_t nbranch = (uint32_t)std::min<size_t>(tcv.size(), 8);
+  // Each instance's own launches (set-up, planning, results, the tensor-form
+  // rounds) are captured on side streams forked from the capture stream and
+  // joined back before each shared search launch, so the graph holds them as
+  // parallel branches instead of running them in turn.  The instances of one
+  // index share a branch (its router's scratch is the index's); distinct
+  // indexes go round the branches.
+  const uint32_t nbranch = (uint32_t)std::min<size_t>(bt->inst.size(), 8);
   for (uint32_t i = 0; i < nbranch; i++) {
     cudaStream_t b;
     BCK(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking));
     bt->branch.push_back(b);
   }
-  for (size_t i = 0; i < 2 * tcv.size() + 1; i++) {
+  for (size_t i = 0; i < 3 * (nbranch + 1); i++) {
     cudaEvent_t e;
     BCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     bt->marks.push_back(e);
   }
+  std::vector<std::pair<rbc_index *, cudaStream_t>> lanes;
+  auto lane_of = [&](rbc_index *idx) {
+    auto it = std::find_if(lanes.begin(), lanes.end(), [&](const auto &e) { return e.first == idx; });
+    if (it == lanes.end()) it = lanes.insert(lanes.end(), {idx, bt->branch[lanes.size() % nbranch]});
+    return it->second;
+  };
   BCK(cudaStreamSynchronize(s));
   SearchArgs *t0 = dalloc<SearchArgs>(N, bt->owned), *t1 = dalloc<SearchArgs>(N, bt->owned);
   SearchItem **dsrc = dalloc<SearchItem *>(N, bt->owned);
@@ -219,24 +229,44 @@ int prepare(rbc_batch *bt) {
   const unsigned long long l0 = g_kernel_launches.load();
   BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int rc = RBC_OK;
+  cudaEvent_t *mark = bt->marks.data();
+  auto fork = [&]() -> int {
+    BCK(cudaEventRecord(*mark, s));
+    for (cudaStream_t b : bt->branch) BCK(cudaStreamWaitEvent(b, *mark, 0));
+    mark++;
+    return RBC_OK;
+  };
+  auto join = [&]() -> int {
+    for (cudaStream_t b : bt->branch) {
+      BCK(cudaEventRecord(*mark, b));
+      BCK(cudaStreamWaitEvent(s, *mark, 0));
+      mark++;
+    }
+    return RBC_OK;
+  };
   auto capture = [&]() -> int {
     BCK(cudaMemsetAsync(bt->ctl, 0, 64, s));
-    for (BatchInstance *ip : fp) {
-      BatchInstance &in = *ip;
-      rbc_index *idx = in.idx;
-      QueryBufs &b = in.b;
-      BCK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
-      BCK(launch_pad_rows(in.Q, in.ldq, b.Qp.as<float>(), idx->ld, in.m, idx->d, s));
-      BCK(launch_dense_dist(idx->metric, b.Qp.as<float>(), in.m, idx->R, idx->nr, idx->ld, idx->dp,
-                            b.Dqr.as<float>(), idx->nr, s));
-      BCK(launch_row_topp(b.Dqr.as<float>(), in.m, idx->nr, 1, b.probe.as<uint32_t>(), b.probed.as<float>(), s));
-      BCK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
-                              b.lock.as<uint32_t>(), in.m, kListWidth, s));
-    }
     for (uint32_t round = 0; round < 2 && N; round++) {
-      for (BatchInstance *ip : fp)
-        BTRY(plan_and_search(ip->idx, ip->b, ip->m, 1, ip->k, round, ip->idx->Xp, ip->idx->perm, ip->idx->offsets,
-                             ip->idx->radius, grid, nullptr, s, 1, tq));
+      BTRY(fork());
+      for (BatchInstance *ip : fp) {
+        BatchInstance &in = *ip;
+        rbc_index *idx = in.idx;
+        QueryBufs &b = in.b;
+        cudaStream_t ls = lane_of(idx);
+        if (round == 0) {
+          BCK(cudaMemsetAsync(b.ctl.p, 0, 64, ls));
+          BCK(launch_pad_rows(in.Q, in.ldq, b.Qp.as<float>(), idx->ld, in.m, idx->d, ls));
+          BCK(launch_dense_dist(idx->metric, b.Qp.as<float>(), in.m, idx->R, idx->nr, idx->ld, idx->dp,
+                                b.Dqr.as<float>(), idx->nr, ls));
+          BCK(launch_row_topp(b.Dqr.as<float>(), in.m, idx->nr, 1, b.probe.as<uint32_t>(), b.probed.as<float>(),
+                              ls));
+          BCK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
+                                  b.lock.as<uint32_t>(), in.m, kListWidth, ls));
+        }
+        BTRY(plan_and_search(idx, b, in.m, 1, in.k, round, idx->Xp, idx->perm, idx->offsets, idx->radius, grid,
+                             nullptr, ls, 1, tq));
+      }
+      BTRY(join());
       batch_offsets_kernel<<<1, 1, 0, s>>>(dcnt, N, offs, bt->ctl + 1);
       BCK(launched());
       batch_concat_kernel<<<dim3(64, N), 256, 0, s>>>(dsrc, dcnt, offs, all);
@@ -245,32 +275,16 @@ int prepare(rbc_batch *bt) {
       g.insts = round == 0 ? t0 : t1;
       BCK(launch_search(metric, g, grid, s, tq));
     }
+    // the FP32 instances' results and the tensor-form instances, each a whole
+    // round with its device fallback; their error words fold into the batch's
+    BTRY(fork());
     for (BatchInstance *ip : fp)
       BCK(launch_write_results(ip->b.res_d.as<float>(), ip->b.res_i.as<uint32_t>(), ip->m, ip->k, kListWidth, ip->ids,
-                               ip->dists, ip->ldo, s));
-    // the tensor-form instances, each a whole round with its device fallback;
-    // the instances of one index share a branch (its router's scratch is the
-    // index's), distinct indexes go round the branches; their error words
-    // fold into the batch's
-    if (!tcv.empty()) {
-      BCK(cudaEventRecord(bt->marks[0], s));
-      for (cudaStream_t b : bt->branch) BCK(cudaStreamWaitEvent(b, bt->marks[0], 0));
-      std::vector<std::pair<rbc_index *, size_t>> lane;
-      for (size_t i = 0; i < tcv.size(); i++) {
-        BatchInstance *ip = tcv[i];
-        auto it = std::find_if(lane.begin(), lane.end(), [&](const auto &e) { return e.first == ip->idx; });
-        if (it == lane.end()) it = lane.insert(lane.end(), {ip->idx, lane.size() % bt->branch.size()});
-        const size_t j = it->second;
-        cudaStream_t b = bt->branch[j];
-        BTRY(tc_enqueue(ip->idx, *ip->tc, ip->Q, ip->m, ip->ldq, ip->ids, ip->dists, ip->ldo, true, bt->ctl + 2,
-                        nullptr, b));
-      }
-      for (size_t j = 0; j < bt->branch.size(); j++) {
-        BCK(cudaEventRecord(bt->marks[1 + j], bt->branch[j]));
-        BCK(cudaStreamWaitEvent(s, bt->marks[1 + j], 0));
-      }
-    }
-    return RBC_OK;
+                               ip->dists, ip->ldo, lane_of(ip->idx)));
+    for (BatchInstance *ip : tcv)
+      BTRY(tc_enqueue(ip->idx, *ip->tc, ip->Q, ip->m, ip->ldq, ip->ids, ip->dists, ip->ldo, true, bt->ctl + 2,
+                      nullptr, lane_of(ip->idx)));
+    return join();
   };
   rc = capture();
   cudaGraph_t graph = nullptr;

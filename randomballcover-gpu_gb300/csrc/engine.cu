@@ -531,6 +531,9 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     if (idx->profile) {
       idx->prof.search_launches = idx->ev_used / 2;
       idx->prof.search_ms = 0;
+      idx->prof.pruned_launches = 0;
+      idx->prof.pruned_ms = 0;
+      idx->prof.pruned_pairs = 0;
       for (size_t i = 0; i + 1 < idx->ev_used; i += 2) {
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, idx->ev_pool[i], idx->ev_pool[i + 1]));
@@ -646,7 +649,7 @@ int tc_setup(rbc_index *idx, uint64_t mb, uint32_t k, uint32_t mode, bool graph,
   CK(t.emax.alloc(mb * 4, s));
   CK(t.ctl.alloc(64, s));
   CK(t.failq.alloc(mb * 4, s));
-  CK(t.stats.alloc(2 * sizeof(unsigned long long), s));
+  CK(t.stats.alloc(4 * sizeof(unsigned long long), s));  // pruned round [0, 1], probe round [2, 3]
   if (graph) {
     // the device fallback: every (row chunk, 16 TQ listed queries) pair for
     // as many queries as the batch holds
@@ -675,7 +678,7 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
   if (tc_probe) *tc_probe = false;
   CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
   CK(cudaMemsetAsync(t.ctl.p, 0, 64, s));
-  if (graph) CK(cudaMemsetAsync(t.stats.p, 0, 2 * sizeof(unsigned long long), s));
+  if (graph) CK(cudaMemsetAsync(t.stats.p, 0, 4 * sizeof(unsigned long long), s));
   // 1. distances to the representatives, probe table
   CK(launch_pad_rows(dQ, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
   CK(launch_dense_dist(idx->metric, b.Qp.as<float>(), mq, idx->R, nr, ld, idx->dp, b.Dqr.as<float>(), nr, s));
@@ -805,8 +808,10 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
     large.skip = t.probe_rows;
     TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, t.sgrid, nullptr, s, 1, -1,
                         tc_query_tile(kTcSplit), large));
+    TcArgs tp = ta;
+    tp.stats = ta.stats + 2;
     if (prof) CK(cudaEventRecord(idx->ev_pool[2], s));
-    CK(launch_tc_search(tmA, idx->tmB, ta, t.grid, s, true));
+    CK(launch_tc_search(tmA, idx->tmB, tp, t.grid, s, true));
     if (prof) CK(cudaEventRecord(idx->ev_pool[3], s));
     if (tc_probe) *tc_probe = true;
     ra.tau = b.tau.as<uint32_t>();
@@ -876,11 +881,11 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
   const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(tc_query_tile(idx->tc.format), (1ull << 27) / nr));
   TcQuery t;
   TRY(tc_setup(idx, mb, k, mode, false, t, s));
-  CK(cudaMemsetAsync(t.stats.p, 0, 2 * sizeof(unsigned long long), s));
+  CK(cudaMemsetAsync(t.stats.p, 0, 4 * sizeof(unsigned long long), s));
   uint64_t nfail_total = 0;
   idx->fallback_ids.clear();
-  double tc_ms = 0;
-  uint32_t tc_launches = 0;
+  double tc_ms = 0, pruned_ms = 0;
+  uint32_t tc_launches = 0, pruned_launches = 0;
   while (idx->ev_pool.size() < 4 && idx->profile) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
@@ -903,6 +908,8 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       CK(cudaEventElapsedTime(&ms, idx->ev_pool[0], idx->ev_pool[1]));
       tc_ms += ms;
       tc_launches += 1;
+      pruned_ms += ms;
+      pruned_launches += 1;
       if (tc_probe) {
         CK(cudaEventElapsedTime(&ms, idx->ev_pool[2], idx->ev_pool[3]));
         tc_ms += ms;
@@ -950,16 +957,19 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
       CK(cudaStreamSynchronize(s));
     }
   }
-  unsigned long long st[2] = {0, 0};
+  unsigned long long st[4] = {0, 0, 0, 0};
   CK(cudaMemcpy(st, t.stats.p, sizeof(st), cudaMemcpyDeviceToHost));
   idx->stats.queries = m;
   idx->stats.rep_pairs = m * nr;
-  idx->stats.point_pairs = st[0];
-  idx->stats.lists_probed = st[1];
+  idx->stats.point_pairs = st[0] + st[2];
+  idx->stats.lists_probed = st[1] + st[3];
   idx->stats.fallback_queries = nfail_total;
   if (idx->profile) {
     idx->prof.search_launches = tc_launches;
     idx->prof.search_ms = tc_ms;
+    idx->prof.pruned_launches = pruned_launches;
+    idx->prof.pruned_ms = pruned_ms;
+    idx->prof.pruned_pairs = st[0];
   }
   return RBC_OK;
 }

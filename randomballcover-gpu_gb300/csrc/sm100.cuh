@@ -42,11 +42,28 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                : "memory");
 }
 
+// One poll; a thread whose phase is not complete may be suspended (up to
+// kSuspendNs, woken early when the phase completes), so waiting warps leave
+// their scheduler's issue slots to the warps that have work.
+constexpr uint32_t kSuspendNs = 100000;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "n"(kSuspendNs)
+      : "memory");
+  return ok != 0;
+}
+
+// Non-blocking test of the phase with the given parity.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
       : "r"(smem_u32(bar)), "r"(parity)
@@ -61,10 +78,11 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 }
 
 // Bounded wait for the phase with the given parity to complete: gives up
-// after kWaitLimitNs of wall time (or kSpinLimit polls, whichever is first).
+// after kWaitLimitNs of wall time (checked every 256 polls, each at most
+// kSuspendNs long) or kSpinLimit polls, whichever is first.
 constexpr uint64_t kWaitLimitNs = 4000000000ull;
 __device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, uint32_t parity, uint32_t *err, uint64_t limit_ns) {
-  if (mbar_try_wait(bar, parity)) return true;
+  if (mbar_test_wait(bar, parity)) return true;  // the common case: already complete, no blocking poll
   const uint64_t t0 = globaltimer_ns();
   for (uint32_t i = 1; i < kSpinLimit; i++) {
     if (mbar_try_wait(bar, parity)) return true;
@@ -146,6 +164,69 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
       "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Warp-collective issue: every lane of the warp executes these with the same
+// (warp-uniform) operands and one elected lane issues the instructions, so
+// the operands stay in the uniform datapath instead of being moved there from
+// one lane's registers each time.  tcgen05 operations issued by one thread
+// run in issue order where the PTX rules pipeline them (a copy before the
+// MMAs that read its columns); a commit tracks the issuing lane's operations.
+//
+// The four K = 16 steps of one 64-wide K block: D[tmem] (+)= A[tmem] *
+// B[smem]^T, A's rows in the tensor-memory lanes with its K values packed two
+// per 32-bit column (columns a_tmem + 8 j for step j), B K-major BF16 in
+// shared memory (the descriptor's start address advanced by 32 bytes, 2
+// units, per step); the first step accumulates when acc0 is non-zero.
+__device__ __forceinline__ void mma_bf16_ts_kblock_warp(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc,
+                                                        uint32_t idesc, uint32_t acc0) {
+  asm volatile(
+      "{\n\t.reg .pred e, p0, pt;\n\t.reg .b64 b1, b2, b3;\n\t.reg .b32 a1, a2, a3;\n\t"
+      "elect.sync _|e, 0xffffffff;\n\t"
+      "setp.ne.b32 p0, %4, 0;\n\t"
+      "setp.eq.b32 pt, %3, %3;\n\t"
+      "add.s64 b1, %2, 2;\n\t"
+      "add.s64 b2, %2, 4;\n\t"
+      "add.s64 b3, %2, 6;\n\t"
+      "add.u32 a1, %1, 8;\n\t"
+      "add.u32 a2, %1, 16;\n\t"
+      "add.u32 a3, %1, 24;\n\t"
+      "@e tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p0;\n\t"
+      "@e tcgen05.mma.cta_group::1.kind::f16 [%0], [a1], b1, %3, pt;\n\t"
+      "@e tcgen05.mma.cta_group::1.kind::f16 [%0], [a2], b2, %3, pt;\n\t"
+      "@e tcgen05.mma.cta_group::1.kind::f16 [%0], [a3], b3, %3, pt;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(acc0)
+      : "memory");
+}
+// D[tmem] (+)= A[smem] * B[smem]^T, both operands K-major BF16.
+__device__ __forceinline__ void mma_bf16_warp(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                              uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred e, p;\n\t"
+      "elect.sync _|e, 0xffffffff;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// Copy a 128-row x 256-bit matrix (one K = 16 step of a K-major half-precision
+// tile, as the shared-memory descriptor lays it out) into 128 lanes x 8
+// columns of tensor memory, the layout an MMA reads its A operand in.
+__device__ __forceinline__ void tmem_cp_128x256b_warp(uint32_t taddr, uint64_t s_desc) {
+  asm volatile(
+      "{\n\t.reg .pred e;\n\t"
+      "elect.sync _|e, 0xffffffff;\n\t"
+      "@e tcgen05.cp.cta_group::1.128x256b [%0], %1;\n\t}" ::"r"(taddr),
+      "l"(s_desc)
+      : "memory");
+}
+// Arrive on an mbarrier once the elected lane's issued operations are done.
+__device__ __forceinline__ void mma_commit_warp(uint64_t *bar) {
+  asm volatile(
+      "{\n\t.reg .pred e;\n\t"
+      "elect.sync _|e, 0xffffffff;\n\t"
+      "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(smem_u32(bar))
       : "memory");
 }
 

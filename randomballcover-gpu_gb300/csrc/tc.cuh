@@ -64,8 +64,20 @@ struct TcArgs {
   unsigned long long *stats;  // [0] (query, row) pairs, [1] (query, list) pairs; may be null
   uint32_t *err;
   uint32_t a_stages, b_stages;  // set by launch_tc_search from the shared-memory budget
-  uint32_t stage_words;         // set by launch_tc_search: per-thread merge staging (0: none)
+  uint32_t stage_words;         // set by launch_tc_search: words of one merge staging area (0: none)
+  uint32_t stage_lanes;         // set by launch_tc_search: lanes of an epilogue warp with a staging
+                                // area (32, or 16: the warp merges in two rounds)
+  // profiling (RBC_TC_TRACE set): per CTA kTcTraceWords clock64 counters of
+  // where each role's cycles went; null otherwise
+  unsigned long long *trace;
 };
+constexpr uint32_t kTcTraceWords = 16;
+// CTA 0 also logs a window of kTcTraceEvents accumulator blocks from block
+// kTcTraceFirst on: per block the clocks of [0] its MMAs' issue start, [1]
+// their commit, [2] the epilogue seeing it full, [3] its release, and per B
+// tile [4] the start and [5] the end of the MMA warp's wait for it (after
+// the grid's counters)
+constexpr uint32_t kTcTraceEvents = 128, kTcTraceFirst = 2000;
 
 struct RerankArgs {
   const float *X;        // FP32 database rows (list-major), stride ld

@@ -43,10 +43,20 @@
 // Kernel structure (one persistent CTA per SM, 384 threads):
 //   warp 0      TMA producer: 128-row B tiles of each item into a ring (with
 //               the tile's w pieces, one bulk copy, in the exact format);
-//   warp 1      tcgen05.mma issuer: per B tile MT x ACC accumulators of
-//               128 x 128 in tensor memory (512 columns hold 4 / (MT ACC)
-//               slots), commits free the B stage and hand the slot to the
-//               epilogue;
+//   warps 1-2   tcgen05.mma issuers.  BF16 format: per item, tcgen05.cp moves
+//               the gathered query tiles from their shared-memory stage into
+//               tensor memory (the stage then takes the next item's gather,
+//               and the MMAs read A from tensor memory, so shared memory
+//               serves only the B operand); the accumulator of each (B tile,
+//               query tile) pair is one of three 128 x 128 blocks taken in
+//               turn, the query tiles fill the other 128 columns.  With two
+//               query tiles warp 1 issues tile 0's MMAs and warp 2 tile 1's
+//               (each a whole warp with one elected lane issuing, so one
+//               warp's waits and commits do not hold up the other's).
+//               Split format: warp 1, per B tile MT x 2 accumulators of
+//               128 x 128 (512 columns hold 4 / (2 MT) slots), A from shared
+//               memory.  Commits free the B stage and hand the accumulator to
+//               the epilogue;
 //   warp 2      split format: stages each B tile's row constants w into
 //               shared memory (cp.async; +inf past the item's rows);
 //   warp 3      per item: gathers the query rows with tile::gather4 (128-byte
@@ -69,6 +79,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <vector>
 
 #include "engine.cuh"
 #include "sm100.cuh"
@@ -85,6 +96,11 @@ constexpr int kThreads = 128 + 128 * kEpiGroups;
 constexpr int kLocal = 8;  // per-thread candidate buffer, in registers (16 in the probe round's
                            // BF16 instance, whose lists meet many more candidates)
 constexpr uint32_t kTile16K = 16384;           // 128 rows x 128 bytes (one 64-wide K block of halves)
+// BF16 format: the accumulator of one (B tile, query tile) pair is one of
+// kBlocks blocks of 128 columns in tensor memory columns [0, 384), taken in
+// turn; the item's query tiles sit at [kTmemA, kTmemA + MT x 64).  The
+// epilogue reads a block kChunk columns at a time.
+constexpr uint32_t kBlocks = 3, kTmemA = 384, kChunk = 64;
 constexpr uint32_t kWTile = 4096;              // 128 rows x 32 bytes: the folded w operand of one B tile
 constexpr uint32_t kLockSpin = 1u << 22;
 constexpr uint32_t kMaxA = 2, kMaxB = 4;
@@ -323,7 +339,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const __grid_constant__ TcArgs a) {
   constexpr uint32_t ACC = SPLIT ? 2 : 1;     // accumulators per query tile: hi.hi (+ corrections)
-  constexpr uint32_t NSLOT = 4 / (MT * ACC);  // tensor-memory slots of MT x ACC x 128 columns
+  constexpr uint32_t NSLOT = 4 / (MT * ACC);  // split format: tensor-memory slots of MT x ACC x 128 columns
   // BF16 format: w is folded into the product.  Each B stage carries the
   // tile's w operand (three BF16 pieces per row: the tile's 128 rows of a.wh
   // are one contiguous 4 KB block, brought by one bulk copy) and one
@@ -331,10 +347,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   // accumulator holds D = q.x' - w / 2 and v = -2 D needs no per-value work
   // in the epilogue.  The split format adds w in the epilogue instead.
   constexpr bool FOLD = !SPLIT;
+  constexpr uint32_t kIssuers = (FOLD && MT == 2) ? 2 : 1;  // warps issuing MMAs
   constexpr int LOC = (MT == 1 && !SPLIT) ? 2 * kLocal : kLocal;  // candidate buffer entries per lane
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_a_full[kMaxA], bar_a_empty[kMaxA], bar_b_full[kMaxB], bar_b_empty[kMaxB],
-      bar_t_full[4], bar_t_empty[4], bar_x_full[4], bar_r_full[2], bar_r_empty[2];
+      bar_t_full[4], bar_t_empty[4], bar_x_full[4], bar_r_full[2], bar_r_empty[2], bar_q_free[2];
+  // BF16 format: per accumulator block and issuer, "full" (the issuer's
+  // commit, waited by the epilogue group of the same query tile) and "empty"
+  // (arrivals of the other group, waited by this issuer); with two issuers a
+  // block's uses alternate between them, and one barrier per block would let
+  // a waiter run two phases ahead, where the parity test aliases
+  __shared__ __align__(8) uint64_t bar_bf[kBlocks][2], bar_be[kBlocks][2];
   __shared__ uint32_t tmem_slot;
 
   unsigned char *base =
@@ -363,21 +386,28 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (tid == 0) {
     for (uint32_t s = 0; s < kMaxA; s++) {
       mbar_init(&bar_a_full[s], 1);
-      mbar_init(&bar_a_empty[s], 1);
+      mbar_init(&bar_a_empty[s], kIssuers);
     }
     for (uint32_t s = 0; s < kMaxB; s++) {
       mbar_init(&bar_b_full[s], 1);
-      mbar_init(&bar_b_empty[s], 1);
+      mbar_init(&bar_b_empty[s], kIssuers);
     }
     for (uint32_t b = 0; b < 4; b++) {
       mbar_init(&bar_t_full[b], 1);
-      mbar_init(&bar_t_empty[b], MT == 2 ? 8 : 4);
+      mbar_init(&bar_t_empty[b], 4);  // one epilogue warpgroup reads each accumulator
       mbar_init(&bar_x_full[b], 32);
     }
     for (uint32_t b = 0; b < 2; b++) {
       mbar_init(&bar_r_full[b], 1);
       mbar_init(&bar_r_empty[b], 8);
     }
+    mbar_init(&bar_q_free[0], 1);
+    mbar_init(&bar_q_free[1], 1);
+    for (uint32_t b = 0; b < kBlocks; b++)
+      for (uint32_t i = 0; i < 2; i++) {
+        mbar_init(&bar_bf[b][i], 1);
+        mbar_init(&bar_be[b][i], 4);  // one epilogue warpgroup
+      }
     fence_barrier_init();
   }
   if (FOLD && tid < (int)(kWTile / 16)) {
@@ -393,13 +423,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
   const uint32_t nitems = *a.nitems;
+  // profiling clock (RBC_TC_TRACE): read only when tracing
+  auto tclk = [&]() -> long long { return a.trace ? clock64() : 0ll; };
 
   if (warp == 0) {
     // ------------------------------------------------ TMA producer of the B tiles
     if (lane == 0) {
       prefetch_tensormap(&tmB);
       uint32_t bi = 0;
-      unsigned long long pairs = 0, lists = 0;
+      unsigned long long pairs = 0, lists = 0, t_wait = 0;
+      const long long t_all = tclk();
       bool ok = true;
       for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
         const SearchItem item = a.items[it];
@@ -408,7 +441,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (a.offsets && item.p0 == a.offsets[item.list]) lists += item.nq;
         for (uint32_t t = 0; t < ntiles; t++, bi++) {
           const uint32_t sb = bi % BS, use = bi / BS;
+          const long long t0 = tclk();
           if (use > 0 && !(ok = mbar_wait(&bar_b_empty[sb], (use - 1) & 1, a.err))) break;
+          t_wait += tclk() - t0;
           mbar_expect_tx(&bar_b_full[sb], b_stage);
           const int32_t row = (int32_t)(item.p0 + (uint64_t)t * kBN);
           for (uint32_t k = 0; k < kbh; k++)
@@ -425,11 +460,128 @@ __global__ void __launch_bounds__(kThreads, 1)
         atomicAdd(a.stats, pairs);
         atomicAdd(a.stats + 1, lists);
       }
+      if (a.trace) {
+        a.trace[blockIdx.x * kTcTraceWords + 6] = t_wait;
+        a.trace[blockIdx.x * kTcTraceWords + 7] = tclk() - t_all;
+        a.trace[blockIdx.x * kTcTraceWords + 15] = bi;
+      }
     }
-  } else if (warp == 1) {
-    // ------------------------------------------------ MMA issuer
-    if (lane == 0) {
-      const uint32_t idesc = SPLIT ? idesc_f16_f32(kBM, kBN) : idesc_bf16_f32(kBM, kBN);
+  } else if (warp == 1 || (FOLD && MT == 2 && warp == 2)) {
+    // ------------------------------------------------ MMA issuers
+    if constexpr (FOLD) {
+      // BF16 format: the item's query tiles are copied from their shared-
+      // memory stage into tensor memory (the stage then takes the next item's
+      // gather while this item runs) and read from there; the accumulator of
+      // each (B tile, query tile) pair u = MT t + g takes block u mod kBlocks.
+      // MT = 2: warp 1 issues query tile 0's MMAs and warp 2 query tile 1's,
+      // each copying its own tile into tensor memory behind its own
+      // query-free barrier, both committing to a B stage's empty barrier
+      // (count two) and to the query stage's (count two): the per-tile waits,
+      // fences and commits of an issuing warp are halved.  MT = 1: warp 1.
+      // The whole warp runs the loop (every lane polls, a vote makes the
+      // outcome uniform), so the operands are warp-uniform and one elected
+      // lane issues each instruction; the descriptors of a B stage are built
+      // once and offset by constants (the start address field is in 16-byte
+      // units and no offset carries out of it).
+      const uint32_t g = MT == 2 ? (uint32_t)warp - 1 : 0u;
+      const uint32_t idesc = idesc_bf16_f32(kBM, kBN);
+      const uint32_t tAg = tmem + kTmemA + g * kb * 4 * 8;
+      const uint64_t kd = sw32_desc(smem_u32(sK));
+      const uint32_t n_items = __shfl_sync(0xffffffffu, nitems, 0);
+      uint32_t ai = 0, bi = 0;
+      uint32_t site = 0;  // diagnostics: the wait that gave up
+      auto wait = [&](uint64_t *bar, uint32_t parity) {
+        const bool r = __all_sync(0xffffffffu, mbar_wait(bar, parity, a.err)) != 0;
+        if (!r && a.trace && lane == 0)
+          a.trace[(size_t)gridDim.x * kTcTraceWords + 6 * kTcTraceEvents + blockIdx.x * 4 + g] =
+              (1ull << 63) | ((unsigned long long)site << 56) | ((unsigned long long)ai << 32) | (bi << 1) | parity;
+        return r;
+      };
+      // ring positions and phase parities kept as counters (no runtime divisions in the loop)
+      uint32_t sa = 0, aph = 0, sb = 0, bph = 0;
+      bool ok = true;
+      long long *ev = (a.trace && blockIdx.x == 0)
+                          ? reinterpret_cast<long long *>(a.trace + (size_t)gridDim.x * kTcTraceWords)
+                          : nullptr;
+      // cycles (warp 1): [0] all, [1] waiting for the query tile, [2] for the
+      // previous item's MMAs, [3] for B tiles, [4] for accumulator blocks; [5] MMAs
+      unsigned long long tr[6] = {0, 0, 0, 0, 0, 0};
+      const bool tracing = a.trace != nullptr;  // clock reads only when tracing
+      auto clk = [&]() -> long long { return tracing ? clock64() : 0ll; };
+      const long long t_all = clk();
+      long long t0;
+      for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ai++) {
+        const uint32_t ntiles = __shfl_sync(0xffffffffu, (a.items[it].np + kBN - 1) / kBN, 0);
+        t0 = clk();
+        site = 1;
+        if (!(ok = wait(&bar_a_full[sa], aph))) break;
+        tr[1] += clk() - t0;
+        // this issuer's previous MMAs read its query tile in tensor memory until they complete
+        t0 = clk();
+        site = 2;
+        if (ai > 0 && !(ok = wait(&bar_q_free[g], (ai - 1) & 1))) break;
+        tr[2] += clk() - t0;
+        tc_fence_after();
+        const uint64_t ad0 = sw128_desc(smem_u32(sA + sa * a_stage + g * a_tile));
+#pragma unroll
+        for (uint32_t k = 0; k < 2; k++)
+          if (k < kb) {
+#pragma unroll
+            for (uint32_t kk = 0; kk < 4; kk++)
+              tmem_cp_128x256b_warp(tAg + (k * 4 + kk) * 8, ad0 + ((k * kTile16K + kk * 32) >> 4));
+          }
+        mma_commit_warp(&bar_a_empty[sa]);  // the stage is free once the copies are done
+        if (++sa == AS) {
+          sa = 0;
+          aph ^= 1u;
+        }
+        for (uint32_t t = 0; t < ntiles && ok; t++, bi++) {
+          t0 = clk();
+          site = 3;
+          if (!(ok = wait(&bar_b_full[sb], bph))) break;
+          const long long t1 = clk();
+          tr[3] += t1 - t0;
+          if (ev && g == 0 && lane == 0 && MT * bi >= kTcTraceFirst && MT * bi < kTcTraceFirst + kTcTraceEvents) {
+            ev[4 * kTcTraceEvents + MT * bi - kTcTraceFirst] = t0;
+            ev[5 * kTcTraceEvents + MT * bi - kTcTraceFirst] = t1;
+          }
+          const uint32_t b0 = smem_u32(sB + sb * b_stage);
+          const uint64_t bd0 = sw128_desc(b0), wd0 = sw32_desc(b0 + b_bytes);
+          // use j = u / kBlocks of block blk: with two issuers this issuer's
+          // uses of the block are every other one, so its barriers count
+          // phases j / 2; with one, j
+          const uint32_t u = MT * bi + g, blk = u % kBlocks, j = u / kBlocks;
+          t0 = clk();
+          site = 4;
+          if (j > 0 && !(ok = wait(&bar_be[blk][g], (kIssuers == 2 ? (j - 1) >> 1 : j - 1) & 1))) break;
+          const long long t2 = clk();
+          tr[4] += t2 - t0;
+          tc_fence_after();
+          const uint32_t d = tmem + blk * kBN;
+#pragma unroll
+          for (uint32_t k = 0; k < 2; k++)
+            if (k < kb) mma_bf16_ts_kblock_warp(d, tAg + k * 4 * 8, bd0 + ((k * kTile16K) >> 4), idesc, k);
+          // -w / 2 last: the products' partial sums stay at the scale of |q| |x'|
+          mma_bf16_warp(d, kd, wd0, idesc, 1);
+          tr[5] += kb * 4 + 1;
+          mma_commit_warp(&bar_bf[blk][g]);
+          mma_commit_warp(&bar_b_empty[sb]);
+          if (ev && lane == 0 && u >= kTcTraceFirst && u < kTcTraceFirst + kTcTraceEvents) {
+            ev[u - kTcTraceFirst] = t2;
+            ev[kTcTraceEvents + u - kTcTraceFirst] = clk();
+          }
+          if (++sb == BS) {
+            sb = 0;
+            bph ^= 1u;
+          }
+        }
+        if (ok) mma_commit_warp(&bar_q_free[g]);
+      }
+      tr[0] = clk() - t_all;
+      if (a.trace && g == 0 && lane == 0)
+        for (int j = 0; j < 6; j++) a.trace[blockIdx.x * kTcTraceWords + j] = tr[j];
+    } else if (lane == 0) {
+      const uint32_t idesc = idesc_f16_f32(kBM, kBN);
       uint32_t ai = 0, bi = 0;
       bool ok = true;
       for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
@@ -452,16 +604,12 @@ __global__ void __launch_bounds__(kThreads, 1)
               for (uint32_t kk = 0; kk < 4; kk++) {
                 const uint32_t off = k * kTile16K + kk * 32;
                 const uint32_t acc = (k | kk) != 0;
+                const uint32_t lo = kb * kTile16K;
                 mma_bf16(d, sw128_desc(a0 + off), sw128_desc(b0 + off), idesc, acc);
-                if (SPLIT) {
-                  const uint32_t lo = kb * kTile16K;
-                  mma_bf16(d + kBN, sw128_desc(a0 + off), sw128_desc(b0 + lo + off), idesc, acc);
-                  mma_bf16(d + kBN, sw128_desc(a0 + lo + off), sw128_desc(b0 + off), idesc, 1);
-                }
+                mma_bf16(d + kBN, sw128_desc(a0 + off), sw128_desc(b0 + lo + off), idesc, acc);
+                mma_bf16(d + kBN, sw128_desc(a0 + lo + off), sw128_desc(b0 + off), idesc, 1);
               }
             }
-            // -w / 2 last: the products' partial sums stay at the scale of |q| |x'|
-            if (FOLD) mma_bf16(d, sw32_desc(smem_u32(sK)), sw32_desc(b0 + b_bytes), idesc, 1);
           }
           mma_commit(&bar_b_empty[sb]);
           mma_commit(&bar_t_full[slot]);
@@ -498,6 +646,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) prefetch_tensormap(&tmA);
     uint32_t ai = 0;
     bool ok = true;
+    unsigned long long w3[2] = {0, 0};  // cycles waiting for a row-state slot, for the query stage
+    const long long t_all = tclk();
     for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
       const SearchItem item = a.items[it];
       const uint32_t slot = ai & 1, sa = ai % AS;
@@ -525,7 +675,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           qin[g][j] = v ? (a.q_inexact ? a.q_inexact[q] : 1u) : 0u;
         }
       const float X = a.lxmax[item.list], C = a.lcnorm[item.list];
+      long long t0 = tclk();
       if (ai >= 2) ok = mbar_wait(&bar_r_empty[slot], ((ai >> 1) - 1) & 1, a.err);
+      w3[0] += tclk() - t0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
       RowState *dst = rs + slot * 2 * kBM;
@@ -554,7 +706,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       __syncwarp();
       if (lane == 0) mbar_arrive(&bar_r_full[slot]);
+      t0 = tclk();
       if (ai >= AS) ok = mbar_wait(&bar_a_empty[sa], ((ai / AS) - 1) & 1, a.err);
+      w3[1] += tclk() - t0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
       unsigned char *dA = sA + sa * a_stage;
@@ -565,6 +719,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (uint32_t k = 0; k < kbh; k++)
           tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
                       rr[g][2], rr[g][3], &bar_a_full[sa]);
+    }
+    if (lane == 0 && a.trace) {
+      a.trace[blockIdx.x * kTcTraceWords + 8] = w3[0];
+      a.trace[blockIdx.x * kTcTraceWords + 9] = w3[1];
+      a.trace[blockIdx.x * kTcTraceWords + 10] = tclk() - t_all;
     }
     if (lane == 0) {
       // drain: wait (bounded) for the gathers still in flight before leaving
@@ -586,22 +745,32 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t arow = (MT == 2 ? grp * kBM : 0) + et;  // this thread's row of the item's query tiles
     uint32_t ai = 0, bi = 0;
     bool ok = true;
-    float *mystage = mstage + (grp * kBM + et) * a.stage_words;
+    const uint32_t sl_lanes = a.stage_lanes ? a.stage_lanes : 32u;
+    float *mystage = mstage + ((warp - 4) * sl_lanes + lane % sl_lanes) * a.stage_words;
     // merge the buffers of the lanes in `need` into their queries' shortlists:
-    // every lane at once on its own query (BF16 format), or one lane at a
-    // time with the whole warp (when shared memory holds no staging areas)
+    // every lane with a staging area at once, each on its own query (a warp
+    // with 16 areas takes its lanes in two rounds), or one lane at a time with
+    // the whole warp (when shared memory holds no staging areas)
+    // cycles (reported by one thread): waiting for row states, for
+    // accumulators, merging shortlists
+    unsigned long long ep[3] = {0, 0, 0};
+    const long long t_all = tclk();
     auto flush = [&](uint32_t need, uint32_t q, uint32_t &nl, float &thv, float dq) {
+      const long long tf = tclk();
       if (a.stage_words) {
-        if ((need >> lane) & 1u) {
-          thv = v_threshold(lane_merge<LOC>(a, q, myla, myli, nl, mystage), dq);
-          nl = 0;
+        for (uint32_t r0 = 0; r0 < 32; r0 += sl_lanes) {
+          if (((need >> lane) & 1u) && lane - r0 < sl_lanes) {
+            thv = v_threshold(lane_merge<LOC>(a, q, myla, myli, nl, mystage), dq);
+            nl = 0;
 #pragma unroll
-          for (int j = 0; j < LOC; j++) {
-            myla[j] = INFINITY;
-            myli[j] = RBC_DUMMY;
+            for (int j = 0; j < LOC; j++) {
+              myla[j] = INFINITY;
+              myli[j] = RBC_DUMMY;
+            }
           }
+          __syncwarp();
         }
-        __syncwarp();
+        ep[2] += tclk() - tf;
         return;
       }
       while (need) {
@@ -632,12 +801,15 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       }
+      ep[2] += tclk() - tf;
     };
     for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
       const SearchItem item = a.items[it];
       const uint32_t ntiles = (item.np + kBN - 1) / kBN;
       const uint32_t rslot = ai & 1;
+      long long tw = tclk();
       if (!(ok = mbar_wait(&bar_r_full[rslot], (ai >> 1) & 1, a.err))) break;
+      ep[0] += tclk() - tw;
       uint32_t q;
       float dq, alpha = -2.f, thv;
       if (FOLD) {
@@ -658,62 +830,114 @@ __global__ void __launch_bounds__(kThreads, 1)
       // larger, older value only lets more candidates through), so the read's
       // latency hides behind a tile of work
       float th_next = arow < item.nq ? __uint_as_float(__ldcg(a.sl_theta + q)) : FLT_MAX;
+      // candidates among CW values v (32 columns at a time, the row of
+      // column e being rbase + e): the values go to a per-thread copy
+      // (indexed by the candidate bits), then into the lane's buffer; full
+      // buffers are merged by the warp, which tightens the filter, until none
+      // are left
+      auto candidates = [&](auto &r, uint32_t rbase0) {
+        constexpr uint32_t CWN = sizeof(r) / sizeof(r[0]);
+#pragma unroll
+        for (uint32_t h = 0; h < CWN / 32; h++) {
+          uint32_t pend = 0;
+#pragma unroll
+          for (int e = 0; e < 32; e++) pend |= (uint32_t)(__uint_as_float(r[32 * h + e]) <= thv) << e;
+          const uint32_t rbase = rbase0 + 32 * h;
+          while (__any_sync(0xffffffffu, pend != 0)) {
+            while (pend && nl < (uint32_t)LOC) {
+              const int e = __ffs(pend) - 1;
+              pend &= pend - 1;
+              // the column's value by a select tree over the registers (an
+              // indexed array would live in local memory, whose traffic
+              // competes with the MMAs' shared-memory operand reads)
+              const float v = select32(r, 32 * h, e);
+              if (v <= thv) {
+                insert_local<LOC>(myla, myli, dq + v, rbase + e);
+                nl++;
+              }
+            }
+            flush(__ballot_sync(0xffffffffu, pend != 0), q, nl, thv, dq);
+          }
+        }
+      };
       for (uint32_t t = 0; t < ntiles && ok; t++, bi++) {
         if (MT == 1 && (bi & 1u) != grp) continue;
-        const uint32_t slot = bi % NSLOT;
         const float th_now = th_next;
         th_next = arow < item.nq ? __uint_as_float(__ldcg(a.sl_theta + q)) : FLT_MAX;
-        if (!(ok = mbar_wait(&bar_t_full[slot], (bi / NSLOT) & 1, a.err))) break;
-        if (!FOLD && !(ok = mbar_wait(&bar_x_full[slot], (bi / NSLOT) & 1, a.err))) break;
-        if (arow < item.nq) thv = fminf(thv, v_threshold(th_now, dq));
-        tc_fence_after();
-        const float *xr = xs + slot * kBN;
-        const uint32_t taddr = tmem + ((32u * ew) << 16) + (slot * MT + (MT == 2 ? grp : 0)) * ACC * kBN;
         const uint32_t p = (uint32_t)(item.p0 + (uint64_t)t * kBN);
-        // BF16 format: columns past the item's rows hold other rows' values
         const uint32_t valid = min((uint32_t)kBN, item.np - t * kBN);
-        // v = -2 D <= thv  <=>  D >= -thv / 2 (rounded down: never misses a value)
-        const float tD = __fmul_rd(-0.5f, thv);
-        // CW columns of the accumulator(s) per tensor-memory read (64 in the BF16
-        // format, 32 with the split format's two accumulators): approx, filter,
-        // candidates
-        constexpr uint32_t CW = SPLIT ? 32 : 64;
-#pragma unroll 1
-        for (uint32_t c = 0; c < kBN / CW; c++) {
-          uint32_t r[CW], r2[SPLIT ? 32 : 1];
-          __syncwarp();
-          if (SPLIT) {
-            tmem_ld32(taddr + c * CW, *reinterpret_cast<uint32_t(*)[32]>(r));
-            tmem_ld32(taddr + kBN + c * CW, *reinterpret_cast<uint32_t(*)[32]>(r2));
-          } else {
-            tmem_ld64(taddr + c * CW, *reinterpret_cast<uint32_t(*)[64]>(r));
+        if constexpr (FOLD) {
+          if (arow < item.nq) thv = fminf(thv, v_threshold(th_now, dq));
+          // v = -2 D <= thv  <=>  D >= -thv / 2 (rounded down: never misses a value)
+          const float tD = __fmul_rd(-0.5f, thv);
+          // this group's accumulator block of the tile (MT = 2: its query
+          // tile; MT = 1: every other tile), kChunk columns at a time
+          const uint32_t gq = MT == 2 ? grp : 0u;  // the issuer of this group's blocks
+          const uint32_t u = MT * bi + gq, blk = u % kBlocks, j = u / kBlocks;
+          tw = tclk();
+          if (!(ok = mbar_wait(&bar_bf[blk][gq], (kIssuers == 2 ? j >> 1 : j) & 1, a.err))) {
+            if (a.trace && lane == 0)
+              a.trace[(size_t)gridDim.x * kTcTraceWords + 6 * kTcTraceEvents + blockIdx.x * 4 + 2 + grp] =
+                  (1ull << 63) | (5ull << 56) | ((unsigned long long)ai << 32) | (bi << 1) | (j & 1);
+            break;
           }
-          tmem_wait_ld();
-          // the slot goes back (to the MMA warp and, in the split format, to
-          // warp 2, which then restages its row constants) once the tile's
-          // last accumulator read is in registers and -- split format -- its
-          // row constants have been read, before this chunk's candidates (and
-          // any shortlist merge) are handled
-          const bool last = c == kBN / CW - 1;
-          auto release_slot = [&]() {
-            tc_fence_before();
+          const long long tfull = tclk();
+          ep[1] += tfull - tw;
+          const bool logu = a.trace && blockIdx.x == 0 && ew == 0 && lane == 0 && u >= kTcTraceFirst &&
+                            u < kTcTraceFirst + kTcTraceEvents;
+          long long *evu = logu ? reinterpret_cast<long long *>(a.trace + (size_t)gridDim.x * kTcTraceWords) +
+                                      (u - kTcTraceFirst)
+                                : nullptr;
+          if (evu) evu[2 * kTcTraceEvents] = tfull;
+          tc_fence_after();
+#pragma unroll 1
+          for (uint32_t c = 0; c < kBN / kChunk; c++) {
+            uint32_t r[kChunk];
             __syncwarp();
-            if (lane == 0) mbar_arrive(&bar_t_empty[slot]);
-          };
-          if (FOLD && last) release_slot();
-          if (FOLD) {
-            if (valid < kBN) {
+            tmem_ld64(tmem + ((32u * ew) << 16) + blk * kBN + c * kChunk, r);
+            tmem_wait_ld();
+            // the block goes back to the MMA warp once its last values are in
+            // registers, before this chunk's candidates are handled
+            if (c == kBN / kChunk - 1) {
+              tc_fence_before();
+              __syncwarp();
+              // the next use of the block is the other issuer's (two issuers)
+              if (lane == 0) mbar_arrive(&bar_be[blk][kIssuers == 2 ? 1u - gq : 0u]);
+              if (evu) evu[3 * kTcTraceEvents] = clock64();
+            }
+            // columns past the item's rows hold other rows' values
+            const uint32_t c0 = c * kChunk;
+            if (valid < c0 + kChunk) {
 #pragma unroll
-              for (uint32_t j = 0; j < CW; j++)
-                if (c * CW + j >= valid) r[j] = 0xff800000u;  // -inf: v = +inf, never a candidate
+              for (uint32_t j = 0; j < kChunk; j++)
+                if (c0 + j >= valid) r[j] = 0xff800000u;  // -inf: v = +inf, never a candidate
             }
             float mx = -INFINITY;
 #pragma unroll
-            for (uint32_t j = 0; j < CW; j += 2) mx = fmax3(mx, __uint_as_float(r[j]), __uint_as_float(r[j + 1]));
+            for (uint32_t j = 0; j < kChunk; j += 2) mx = fmax3(mx, __uint_as_float(r[j]), __uint_as_float(r[j + 1]));
             if (!__any_sync(0xffffffffu, mx >= tD)) continue;
 #pragma unroll
-            for (uint32_t j = 0; j < CW; j++) r[j] = __float_as_uint(-2.f * __uint_as_float(r[j]));
-          } else {
+            for (uint32_t j = 0; j < kChunk; j++) r[j] = __float_as_uint(-2.f * __uint_as_float(r[j]));
+            candidates(r, p + c0);
+          }
+        } else {
+          const uint32_t slot = bi % NSLOT;
+          if (!(ok = mbar_wait(&bar_t_full[slot], (bi / NSLOT) & 1, a.err))) break;
+          if (!(ok = mbar_wait(&bar_x_full[slot], (bi / NSLOT) & 1, a.err))) break;
+          if (arow < item.nq) thv = fminf(thv, v_threshold(th_now, dq));
+          tc_fence_after();
+          const float *xr = xs + slot * kBN;
+          const uint32_t taddr = tmem + ((32u * ew) << 16) + (slot * MT + (MT == 2 ? grp : 0)) * ACC * kBN;
+          // 32 columns of both accumulators per tensor-memory read: approx,
+          // filter, candidates
+          constexpr uint32_t CW = 32;
+#pragma unroll 1
+          for (uint32_t c = 0; c < kBN / CW; c++) {
+            uint32_t r[CW], r2[CW];
+            __syncwarp();
+            tmem_ld32(taddr + c * CW, r);
+            tmem_ld32(taddr + kBN + c * CW, r2);
+            tmem_wait_ld();
             // v in place of the accumulator values
             float mn = INFINITY;
 #pragma unroll
@@ -723,46 +947,34 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
               for (int e = 0; e < 4; e++) {
                 float tv = fmaf(alpha, __uint_as_float(r[4 * j4 + e]), xw[e]);
-                if (SPLIT) tv = fmaf(alpha, __uint_as_float(r2[(4 * j4 + e) % (SPLIT ? 32 : 1)]), tv);
+                tv = fmaf(alpha, __uint_as_float(r2[4 * j4 + e]), tv);
                 r[4 * j4 + e] = __float_as_uint(tv);
               }
               mn = fminf(mn, fminf(fminf(__uint_as_float(r[4 * j4]), __uint_as_float(r[4 * j4 + 1])),
                                    fminf(__uint_as_float(r[4 * j4 + 2]), __uint_as_float(r[4 * j4 + 3]))));
             }
-            if (last) release_slot();
-            if (!__any_sync(0xffffffffu, mn <= thv)) continue;
-          }
-          // candidates, 32 columns at a time: the values go to a per-thread copy
-          // (indexed by the candidate bits), then into the lane's buffer; full
-          // buffers are merged by the warp, which tightens the filter, until
-          // none are left
-#pragma unroll
-          for (uint32_t h = 0; h < CW / 32; h++) {
-            uint32_t pend = 0;
-#pragma unroll
-            for (int e = 0; e < 32; e++) pend |= (uint32_t)(__uint_as_float(r[32 * h + e]) <= thv) << e;
-            const uint32_t rbase = p + c * CW + 32 * h;
-            while (__any_sync(0xffffffffu, pend != 0)) {
-              while (pend && nl < (uint32_t)LOC) {
-                const int e = __ffs(pend) - 1;
-                pend &= pend - 1;
-                // the column's value by a select tree over the registers (an
-                // indexed array would live in local memory, whose traffic
-                // competes with the MMAs' shared-memory operand reads)
-                const float v = select32(r, 32 * h, e);
-                if (v <= thv) {
-                  insert_local<LOC>(myla, myli, dq + v, rbase + e);
-                  nl++;
-                }
-              }
-              flush(__ballot_sync(0xffffffffu, pend != 0), q, nl, thv, dq);
+            // the slot goes back (to the MMA warp and to warp 2, which then
+            // restages its row constants) once the tile's last accumulator
+            // read is in registers and its row constants have been read,
+            // before this chunk's candidates (and any shortlist merge) are
+            // handled
+            if (c == kBN / CW - 1) {
+              tc_fence_before();
+              __syncwarp();
+              if (lane == 0) mbar_arrive(&bar_t_empty[slot]);
             }
+            if (!__any_sync(0xffffffffu, mn <= thv)) continue;
+            candidates(r, p + c * CW);
           }
         }
       }
       flush(__ballot_sync(0xffffffffu, nl > 0), q, nl, thv, dq);
       __syncwarp();
       if (lane == 0) mbar_arrive(&bar_r_empty[rslot]);
+    }
+    if (a.trace && warp == 4 && lane == 0) {
+      for (int j = 0; j < 3; j++) a.trace[blockIdx.x * kTcTraceWords + 11 + j] = ep[j];
+      a.trace[blockIdx.x * kTcTraceWords + 14] = tclk() - t_all;
     }
   }
   tc_fence_before();
@@ -1228,49 +1440,66 @@ __global__ void rerank_kernel(RerankArgs a) {
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
 template <int MT, bool SPLIT>
-size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs, uint32_t stage_words) {
+size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs, uint32_t stage_words, uint32_t stage_lanes = 32) {
   const size_t kbh = SPLIT ? 2 * kb : kb;
   const size_t nslot = 4 / (MT * (SPLIT ? 2 : 1));
   const size_t b_stage = kbh * kTile16K + (SPLIT ? 0 : kWTile);
   const size_t consts = SPLIT ? nslot * kBN * 4 : kWTile;  // row constants, or the w product's constant tile
   const size_t states = 2 * 2 * kBM * (SPLIT ? sizeof(RowState) : sizeof(RowStateF));
   return 1024 + (size_t)as * MT * kbh * kTile16K + (size_t)bs * b_stage + consts + states +
-         (size_t)kEpiGroups * kBM * stage_words * 4;
+         (size_t)kEpiGroups * 4 * stage_lanes * stage_words * 4;
 }
 
 template <int MT, bool SPLIT>
 cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s) {
-  // deepest pipeline that fits: B depth first (it hides the L2 latency of
-  // every tile), then a second query stage (it hides the gather at item starts)
-  // merge staging (2 SL + 1 words per epilogue thread) first: the lane-parallel
-  // shortlist merges matter more than pipeline depth
+  // Shared-memory plan.  BF16 format with two query tiles (the pruned round):
+  // its query tiles live in tensor memory, so one query stage suffices, and
+  // three B stages with staging areas for half of each warp's lanes measured
+  // faster than two B stages with staging for all (c3: 22.1 against 23.5 ms
+  // per launch; the two MMA warps wait on B tiles otherwise).  Otherwise the
+  // deepest pipeline that fits with merge staging (2 SL + 1 words) for every
+  // epilogue thread -- the lane-parallel shortlist merges matter more than
+  // pipeline depth: B depth first (it hides the L2 latency of every tile),
+  // then a second query stage (it hides the gather at item starts).
   static const uint32_t pref[][2] = {{2, 4}, {2, 3}, {1, 4}, {1, 3}, {2, 2}, {1, 2}};
   uint32_t as = 0, bs = 0;
+  a.stage_lanes = 32;
+  if (!SPLIT && MT == 2 && smem_bytes<MT, SPLIT>(a.kb, 1, 3, 2 * a.sl + 1, 16) <= kSmemLimit) {
+    as = 1;
+    bs = 3;
+    a.stage_words = 2 * a.sl + 1;
+    a.stage_lanes = 16;
+  }
   for (uint32_t sw : {2 * a.sl + 1, 0u}) {
+    if (as) break;
     for (const auto &c : pref)
       if (smem_bytes<MT, SPLIT>(a.kb, c[0], c[1], sw) <= kSmemLimit) {
         as = c[0];
         bs = c[1];
         break;
       }
-    if (as) {
-      a.stage_words = sw;
-      break;
-    }
+    if (as) a.stage_words = sw;
   }
-  // RBC_TC_STAGES="a,b" overrides the choice (tuning experiments) when it fits
+  // RBC_TC_STAGES="a,b[,s]" overrides the choice (tuning experiments) when it
+  // fits: a query stages, b B stages, s staging areas per epilogue warp (32,
+  // 16, or 0: without the merge staging, warp merges one lane at a time)
   if (const char *env = std::getenv("RBC_TC_STAGES")) {
-    unsigned ea = 0, eb = 0;
-    if (std::sscanf(env, "%u,%u", &ea, &eb) == 2 && ea >= 1 && ea <= kMaxA && eb >= 2 && eb <= kMaxB &&
-        smem_bytes<MT, SPLIT>(a.kb, ea, eb, a.stage_words) <= kSmemLimit) {
+    unsigned ea = 0, eb = 0, es = 32;
+    const int got = std::sscanf(env, "%u,%u,%u", &ea, &eb, &es);
+    const uint32_t lanes = got == 3 ? (es >= 32 || es == 1 ? 32u : es >= 16 ? 16u : 0u) : 32u;
+    const uint32_t sw = lanes ? 2 * a.sl + 1 : 0u;
+    if (got >= 2 && ea >= 1 && ea <= kMaxA && eb >= 2 && eb <= kMaxB &&
+        smem_bytes<MT, SPLIT>(a.kb, ea, eb, sw, lanes) <= kSmemLimit) {
       as = ea;
       bs = eb;
+      a.stage_words = sw;
+      a.stage_lanes = lanes;
     }
   }
   if (!as) return cudaErrorInvalidConfiguration;
   a.a_stages = as;
   a.b_stages = bs;
-  const size_t smem = smem_bytes<MT, SPLIT>(a.kb, as, bs, a.stage_words);
+  const size_t smem = smem_bytes<MT, SPLIT>(a.kb, as, bs, a.stage_words, a.stage_lanes);
   cudaError_t e =
       cudaFuncSetAttribute(tc_search_kernel<MT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -1418,11 +1647,77 @@ int tc_grid() {
   return sms > 0 ? sms : 1;
 }
 
+namespace {
+// RBC_TC_TRACE set: each launch records where every role's cycles went
+// (per-CTA clock64 counters) and prints the CTAs' averages to stderr.  The
+// launch then synchronises its stream: profiling runs only, not inside a
+// graph capture.
+cudaError_t launch_tc_traced(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s,
+                             bool narrow) {
+  const size_t words = (size_t)grid * kTcTraceWords + 6 * kTcTraceEvents + (size_t)grid * 4;
+  unsigned long long *buf = nullptr;
+  cudaError_t e = cudaMallocAsync(&buf, words * 8, s);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(buf, 0, words * 8, s)) != cudaSuccess) return e;
+  a.trace = buf;
+  const int mt = (a.format == kTcSplit || narrow) ? 1 : 2;
+  if (a.format == kTcSplit)
+    e = launch_tc<1, true>(tmA, tmB, a, grid, s);
+  else
+    e = narrow ? launch_tc<1, false>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
+  if (e != cudaSuccess) return e;
+  std::vector<unsigned long long> h(words);
+  if ((e = cudaMemcpyAsync(h.data(), buf, words * 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  cudaFreeAsync(buf, s);
+  {
+    // CTA 0's window of blocks: clocks relative to the first issue
+    const long long *ev = reinterpret_cast<const long long *>(h.data() + (size_t)grid * kTcTraceWords);
+    const long long base = ev[0];
+    if (base) {
+      std::fprintf(stderr, "tc_events MT=%d (u: issue-start commit full release | B-wait start end)\n",
+                   (a.format == kTcSplit || narrow) ? 1 : 2);
+      for (uint32_t i = 0; i < kTcTraceEvents; i++) {
+        auto rel = [&](int j) { return ev[j * kTcTraceEvents + i] ? ev[j * kTcTraceEvents + i] - base : -1ll; };
+        std::fprintf(stderr, "ev %u %lld %lld %lld %lld | %lld %lld\n", kTcTraceFirst + i, rel(0), rel(1), rel(2),
+                     rel(3), rel(4), rel(5));
+      }
+    }
+  }
+  {
+    const unsigned long long *f = h.data() + (size_t)grid * kTcTraceWords + 6 * kTcTraceEvents;
+    int shown = 0;
+    for (int c = 0; c < grid && shown < 12; c++)
+      for (int j = 0; j < 4; j++)
+        if (f[c * 4 + j] >> 63) {
+          const unsigned long long v = f[c * 4 + j];
+          std::fprintf(stderr, "tc_wait_failed cta=%d role=%d site=%llu item=%llu tile=%llu parity=%llu\n", c, j,
+                       (v >> 56) & 0x7f, (v >> 32) & 0xffffff, (v & 0xffffffffull) >> 1, v & 1);
+          shown++;
+        }
+  }
+  double m[kTcTraceWords] = {0};
+  for (int c = 0; c < grid; c++)
+    for (uint32_t j = 0; j < kTcTraceWords; j++) m[j] += (double)h[(size_t)c * kTcTraceWords + j] / grid;
+  auto pct = [&](int j, int of) { return m[of] > 0 ? 100.0 * m[j] / m[of] : 0.0; };
+  std::fprintf(stderr,
+               "tc_trace MT=%d format=%u grid=%d | mma: %.0f cyc, wait query %.1f%% prev-item %.1f%% B %.1f%% "
+               "slot %.1f%%, %.0f MMAs (%.1f cyc each) | producer: wait stage %.1f%%, %.0f tiles | gather warp: "
+               "wait rows %.1f%% stage %.1f%% | epilogue: wait rows %.1f%% acc %.1f%% merge %.1f%% of %.0f cyc\n",
+               mt, a.format, grid, m[0], pct(1, 0), pct(2, 0), pct(3, 0), pct(4, 0), m[5],
+               m[5] > 0 ? m[0] / m[5] : 0.0, pct(6, 7), m[15], pct(8, 10), pct(9, 10), pct(11, 14), pct(12, 14),
+               pct(13, 14), m[14]);
+  return cudaSuccess;
+}
+}  // namespace
+
 cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
                              cudaStream_t s, bool narrow) {
   if (a.kb < 1 || a.kb > 2) return cudaErrorInvalidValue;
+  if (a.format != kTcSplit && !a.wh) return cudaErrorInvalidValue;
+  static const bool trace = std::getenv("RBC_TC_TRACE") != nullptr;
+  if (trace) return launch_tc_traced(tmA, tmB, a, grid, s, narrow);
   if (a.format == kTcSplit) return launch_tc<1, true>(tmA, tmB, a, grid, s);
-  if (!a.wh) return cudaErrorInvalidValue;
   return narrow ? launch_tc<1, false>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
 }
 

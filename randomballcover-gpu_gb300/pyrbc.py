@@ -52,7 +52,8 @@ class QueryStats(C.Structure):
 
 
 class Profile(C.Structure):
-    _fields_ = [("search_launches", C.c_uint64), ("search_ms", C.c_double)]
+    _fields_ = [("search_launches", C.c_uint64), ("search_ms", C.c_double), ("pruned_launches", C.c_uint64),
+                ("pruned_ms", C.c_double), ("pruned_pairs", C.c_uint64)]
 
 
 # Every symbol of include/rbc_gb300.h with its ctypes signature.
@@ -348,7 +349,8 @@ class Index:
     def profile(self):
         p = Profile()
         check(lib().rbc_get_profile(self.h, C.byref(p)))
-        return {"search_launches": p.search_launches, "search_ms": p.search_ms}
+        return {"search_launches": p.search_launches, "search_ms": p.search_ms, "pruned_launches": p.pruned_launches,
+                "pruned_ms": p.pruned_ms, "pruned_pairs": p.pruned_pairs}
 
 
 def kernel_launches():
