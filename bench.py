@@ -96,6 +96,8 @@ def parse():
                          "0: none, the distance head plans instead)")
     ap.add_argument("--forms", default=None,
                     help="forms to time; the last one listed is the headline (default: per workload)")
+    ap.add_argument("--item-rows", type=int, default=0,
+                    help="longest row run of one work item (rbc_set_tuning; 0: the index's default)")
     ap.add_argument("--tc-tuning", default=None, metavar="PROBES,ROWS",
                     help="fixed tensor-form knobs instead of timing them (profiling runs)")
     a = ap.parse_args()
@@ -432,6 +434,8 @@ def run_engine(a):
 
     modes = {"plain": pyrbc.QUERY_EXACT, "tensor": pyrbc.QUERY_EXACT_TC, "oneshot": pyrbc.QUERY_ONESHOT,
              "learned": pyrbc.QUERY_EXACT_TC | pyrbc.QUERY_ROUTED, "learned_plain": pyrbc.QUERY_EXACT | pyrbc.QUERY_ROUTED}
+    if a.item_rows:
+        idx.set_tuning(0, a.item_rows)
     idx.set_profiling(True)
     ids = torch.empty((m, k), dtype=torch.int32, device="cuda")
     dists = torch.empty((m, k), dtype=torch.float32, device="cuda")
