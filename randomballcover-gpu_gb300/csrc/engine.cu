@@ -646,6 +646,7 @@ int tc_setup(rbc_index *idx, uint64_t mb, uint32_t k, uint32_t mode, bool graph,
   CK(t.sl_theta.alloc(mb * 4, s));
   CK(t.sl_lock.alloc(mb * 4, s));
   if (t.spec) CK(t.sl_cap.alloc(mb * 4, s));
+  CK(t.drop.alloc(mb * 4, s));
   CK(t.emax.alloc(mb * 4, s));
   CK(t.ctl.alloc(64, s));
   CK(t.failq.alloc(mb * 4, s));
@@ -678,6 +679,7 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
   if (tc_probe) *tc_probe = false;
   CK(cudaMemsetAsync(b.ctl.p, 0, 64, s));
   CK(cudaMemsetAsync(t.ctl.p, 0, 64, s));
+  CK(cudaMemsetAsync(t.drop.p, 0x7F, mq * 4, s));  // 0x7F7F7F7F: a finite float above every distance
   if (graph) CK(cudaMemsetAsync(t.stats.p, 0, 4 * sizeof(unsigned long long), s));
   // 1. distances to the representatives, probe table
   CK(launch_pad_rows(dQ, ldq, b.Qp.as<float>(), ld, mq, idx->d, s));
@@ -746,6 +748,8 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
   ta.sl_sel = t.sl_sel.as<uint32_t>();
   ta.sl_theta = t.sl_theta.as<uint32_t>();
   ta.sl_cap = spec ? t.sl_cap.as<uint32_t>() : nullptr;
+  ta.drop = t.drop.as<uint32_t>();
+  ta.keep_k = 0;
   ta.sl_lock = t.sl_lock.as<uint32_t>();
   ta.emax = t.emax.as<uint32_t>();
   ta.m = mq;
@@ -766,6 +770,7 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
   ra.sl_sel = t.sl_sel.as<uint32_t>();
   ra.emax = t.emax.as<uint32_t>();
   ra.sl_cap = spec ? t.sl_cap.as<uint32_t>() : nullptr;
+  ra.drop = t.drop.as<uint32_t>();
   ra.tplan = nullptr;
   ra.ldo = ldo;
   ra.nfail = t.ctl.as<uint32_t>() + 1;
@@ -808,8 +813,12 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
     large.skip = t.probe_rows;
     TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, t.sgrid, nullptr, s, 1, -1,
                         tc_query_tile(kTcSplit), large));
+    // the probe round's candidate buffers keep each query's best and merge
+    // once per item (its lists hold few queries, many of them busy hubs,
+    // where merges per buffer-full would queue on the queries' locks)
     TcArgs tp = ta;
     tp.stats = ta.stats + 2;
+    tp.keep_k = k;
     if (prof) CK(cudaEventRecord(idx->ev_pool[2], s));
     CK(launch_tc_search(tmA, idx->tmB, tp, t.grid, s, true));
     if (prof) CK(cudaEventRecord(idx->ev_pool[3], s));

@@ -66,7 +66,7 @@ struct TcQuery {
   int grid = 0, sgrid = 0, ptq = 0, pgrid = 0;
   QueryBufs b;
   DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
-      stats, seed_a, seed_row, sl_cap, tpred;
+      stats, seed_a, seed_row, sl_cap, tpred, drop;
   // graph mode: the device fallback's work list and control words
   DevBuf fb_items, fb_ctl;
   uint32_t fb_chunk = 0, fb_qtile = 0;

@@ -67,6 +67,13 @@ struct TcArgs {
   uint32_t stage_words;         // set by launch_tc_search: words of one merge staging area (0: none)
   uint32_t stage_lanes;         // set by launch_tc_search: lanes of an epilogue warp with a staging
                                 // area (32, or 16: the warp merges in two rounds)
+  // keep_k != 0 (launches with one query tile, k <= the per-thread buffer):
+  // each thread keeps its query's best buffer-full of candidates of an item
+  // and merges them once at the item's end; every row it leaves out has
+  // approx at least the buffer's last value then, recorded in drop[q]
+  // (float bits, atomic min; 0x7F7F7F7F when nothing was left out)
+  uint32_t keep_k;
+  uint32_t *drop;
   // profiling (RBC_TC_TRACE set): per CTA kTcTraceWords clock64 counters of
   // where each role's cycles went; null otherwise
   unsigned long long *trace;
@@ -90,6 +97,8 @@ struct RerankArgs {
   const uint32_t *sl_sel;
   const uint32_t *emax;
   const uint32_t *sl_cap; // per query: the cap on the shortlist threshold (nullptr: none)
+  const uint32_t *drop;   // per query: bound on the approx of rows the search left out of
+                          // candidate buffers (float bits; nullptr: none)
   const uint32_t *tplan;  // per query: the threshold the plan pruned with when it was a
                           // prediction (the k-th exact distance must not exceed it)
   uint32_t *tau;         // if set: the k-th exact distance (float bits) -> pruning threshold

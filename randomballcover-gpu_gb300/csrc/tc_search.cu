@@ -205,7 +205,8 @@ __device__ __forceinline__ float warp_publish(const TcArgs &a, uint32_t q, const
 }
 
 // Sorted insertion of (av, row) into a lane's register buffer (ascending,
-// empty slots +inf); the caller guarantees a free slot.
+// empty slots +inf); with the buffer full the last entry falls off (and an
+// entry not below it is not inserted).
 template <int LOC>
 __device__ __forceinline__ void insert_local(float (&la)[LOC], uint32_t (&li)[LOC], float av, uint32_t row) {
 #pragma unroll
@@ -743,6 +744,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       myli[j] = RBC_DUMMY;
     }
     const uint32_t arow = (MT == 2 ? grp * kBM : 0) + et;  // this thread's row of the item's query tiles
+    const bool keep = MT == 1 && a.keep_k != 0 && a.keep_k <= (uint32_t)LOC && a.drop != nullptr;
     uint32_t ai = 0, bi = 0;
     bool ok = true;
     const uint32_t sl_lanes = a.stage_lanes ? a.stage_lanes : 32u;
@@ -825,6 +827,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         thv = st.thv;
       }
       uint32_t nl = 0;
+      bool dropped = false;  // keep-best mode: some row of the item was left out
       // other CTAs tighten the query's shortlist all the time: each tile
       // refreshes the filter with the threshold read one tile earlier (a
       // larger, older value only lets more candidates through), so the read's
@@ -835,6 +838,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       // (indexed by the candidate bits), then into the lane's buffer; full
       // buffers are merged by the warp, which tightens the filter, until none
       // are left
+      // Keep-best mode: a full buffer keeps the best LOC candidates, its last
+      // value tightens the filter, and the merge waits for the item's end.
       auto candidates = [&](auto &r, uint32_t rbase0) {
         constexpr uint32_t CWN = sizeof(r) / sizeof(r[0]);
 #pragma unroll
@@ -844,7 +849,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int e = 0; e < 32; e++) pend |= (uint32_t)(__uint_as_float(r[32 * h + e]) <= thv) << e;
           const uint32_t rbase = rbase0 + 32 * h;
           while (__any_sync(0xffffffffu, pend != 0)) {
-            while (pend && nl < (uint32_t)LOC) {
+            while (pend && (keep || nl < (uint32_t)LOC)) {
               const int e = __ffs(pend) - 1;
               pend &= pend - 1;
               // the column's value by a select tree over the registers (an
@@ -853,10 +858,14 @@ __global__ void __launch_bounds__(kThreads, 1)
               const float v = select32(r, 32 * h, e);
               if (v <= thv) {
                 insert_local<LOC>(myla, myli, dq + v, rbase + e);
-                nl++;
+                if (nl < (uint32_t)LOC) nl++;
+                if (keep && nl == (uint32_t)LOC) {
+                  dropped = true;
+                  thv = fminf(thv, v_threshold(myla[LOC - 1], dq));
+                }
               }
             }
-            flush(__ballot_sync(0xffffffffu, pend != 0), q, nl, thv, dq);
+            if (!keep) flush(__ballot_sync(0xffffffffu, pend != 0), q, nl, thv, dq);
           }
         }
       };
@@ -968,6 +977,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       }
+      if (keep && dropped && arow < item.nq)
+        atomicMin(a.drop + q, __float_as_uint(fmaxf(myla[LOC - 1], 0.f)));  // non-negative: bits order
       flush(__ballot_sync(0xffffffffu, nl > 0), q, nl, thv, dq);
       __syncwarp();
       if (lane == 0) mbar_arrive(&bar_r_empty[rslot]);
@@ -1415,12 +1426,14 @@ __global__ void rerank_kernel(RerankArgs a) {
   if (a.tau && lane == 0) atomicMin(a.tau + q, fbits(kth));
   if (!a.ids && !a.dists) return;
   // certificate: every row searched but not in the shortlist has approx >=
-  // T = min(cap, a_last) (a_last only when the shortlist is full: otherwise
-  // only the cap turned rows away), so its exact distance is >= T - E > kth
+  // T = min(cap, drop, a_last) (a_last only when the shortlist is full:
+  // otherwise only the cap and the candidate buffers turned rows away), so
+  // its exact distance is >= T - E > kth
   // when certified; rows of pruned lists are beyond the plan's threshold,
   // which must then be at least kth
   bool certified = true;
-  const float cap = a.sl_cap ? __uint_as_float(a.sl_cap[q]) : FLT_MAX;
+  const float cap = fminf(a.sl_cap ? __uint_as_float(a.sl_cap[q]) : FLT_MAX,
+                          a.drop ? __uint_as_float(a.drop[q]) : FLT_MAX);  // rows left out of buffers too
   const float T = valid == a.sl ? fminf(sa_q[a.sl - 1], cap) : cap;
   if (T < FLT_MAX) {
     const double E = (double)__uint_as_float(a.emax[q]);
