@@ -815,7 +815,8 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
                         tc_query_tile(kTcSplit), large));
     // the probe round's candidate buffers keep each query's best and merge
     // once per item (its lists hold few queries, many of them busy hubs,
-    // where merges per buffer-full would queue on the queries' locks)
+    // where merges per buffer-full queued on the queries' locks: c3 probe
+    // launch 7.7 -> 5.0 ms; the same in the pruned round measured no gain)
     TcArgs tp = ta;
     tp.stats = ta.stats + 2;
     tp.keep_k = k;

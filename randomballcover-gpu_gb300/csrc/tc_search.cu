@@ -349,7 +349,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   // in the epilogue.  The split format adds w in the epilogue instead.
   constexpr bool FOLD = !SPLIT;
   constexpr uint32_t kIssuers = (FOLD && MT == 2) ? 2 : 1;  // warps issuing MMAs
-  constexpr int LOC = (MT == 1 && !SPLIT) ? 2 * kLocal : kLocal;  // candidate buffer entries per lane
+  // candidate buffer entries per lane: 16 in the BF16 format's probe round
+  // (its lists meet many more candidates), kLocal otherwise
+  constexpr int LOC = (MT == 1 && !SPLIT) ? 2 * kLocal : kLocal;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_a_full[kMaxA], bar_a_empty[kMaxA], bar_b_full[kMaxB], bar_b_empty[kMaxB],
       bar_t_full[4], bar_t_empty[4], bar_x_full[4], bar_r_full[2], bar_r_empty[2], bar_q_free[2];
@@ -744,7 +746,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       myli[j] = RBC_DUMMY;
     }
     const uint32_t arow = (MT == 2 ? grp * kBM : 0) + et;  // this thread's row of the item's query tiles
-    const bool keep = MT == 1 && a.keep_k != 0 && a.keep_k <= (uint32_t)LOC && a.drop != nullptr;
+    // keep-best mode when the buffer holds k and four more (the margin keeps
+    // the rows left out clear of the k-th distance for the certificate)
+    const bool keep = a.keep_k != 0 && a.keep_k + 4 <= (uint32_t)LOC && a.drop != nullptr;
     uint32_t ai = 0, bi = 0;
     bool ok = true;
     const uint32_t sl_lanes = a.stage_lanes ? a.stage_lanes : 32u;
@@ -782,13 +786,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         float th = 0.f;
         // the warp network takes kLocal candidates at a time
 #pragma unroll
-        for (int h = 0; h < LOC / kLocal; h++) {
+        for (int h = 0; h < (LOC + kLocal - 1) / kLocal; h++) {
           float ha[kLocal];
           uint32_t hi[kLocal];
 #pragma unroll
           for (int j = 0; j < kLocal; j++) {
-            ha[j] = myla[h * kLocal + j];
-            hi[j] = myli[h * kLocal + j];
+            ha[j] = h * kLocal + j < LOC ? myla[h * kLocal + j < LOC ? h * kLocal + j : 0] : INFINITY;
+            hi[j] = h * kLocal + j < LOC ? myli[h * kLocal + j < LOC ? h * kLocal + j : 0] : RBC_DUMMY;
           }
           const uint32_t nh = min(max((int)nll - h * kLocal, 0), kLocal);
           if (h == 0 || nh > 0) th = warp_publish(a, ql, ha, hi, nh, l);
