@@ -195,12 +195,14 @@ def peaks():
     return 6800.0, 1900.0, 1700.0, "fallback"
 
 
-def committed_traffic(kernel):
-    """Per-launch DRAM bytes of a kernel from the committed ncu summary, if any."""
+def committed_traffic(kernel, workload=None):
+    """Per-launch DRAM bytes of a kernel at a workload's default size, from the
+    committed ncu summary (a line `traffic_bytes_per_launch_<workload>: B`),
+    if any."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_traffic.md")
-    if not os.path.exists(path):
+    if not workload or not os.path.exists(path):
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([\d.eE+]+)", open(path).read())
+    m = re.search(rf"traffic_bytes_per_launch_{workload}:\s*([\d.eE+]+)", open(path).read())
     return float(m.group(1)) if m else None
 
 
@@ -546,7 +548,7 @@ def run_engine(a):
     head_plain = head == "plain" or (modes[head] & pyrbc.QUERY_EXACT_TC and idx.info()["tc_plain"])
     kernel = "search_kernel" if head_plain else "tc_search_kernel"
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                "frac": achieved / bf16, "traffic": committed_traffic(kernel), "kernel": kernel,
+                "frac": achieved / bf16, "traffic": committed_traffic(kernel, a.workload if a.n is None and a.m is None else None), "kernel": kernel,
                 "peak_source": f"{src} bf16 dense burst (MEASURED_PEAKS.json)",
                 "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
     if not head_plain and res["pruned_launches"] and res["pruned_launches"] < res["search_launches"]:
