@@ -456,7 +456,8 @@ def run_engine(a):
             inf = idx.info()
             tuning[mode] = list(idx.tc_tuning()) + (["plain FP32 search chosen"] if inf["tc_plain"] else [])
             if mode & pyrbc.QUERY_ROUTED:
-                tuning[mode].append(f"router picks {inf['router_picks']}")
+                tuning[mode].append("router not consulted (the tuner measured the nearest lists alone faster)"
+                                    if inf["tc_unrouted"] else f"router picks {inf['router_picks']}")
         for _ in range(warmup):
             idx.query(Q, k, mode=mode, out=(ids, dists))
         barrier()

@@ -101,6 +101,10 @@ typedef struct {
                                   search faster, and RBC_QUERY_EXACT_TC
                                   calls run it                          */
   uint32_t router_picks;       /* lists routed calls take from the router */
+  uint32_t tc_unrouted;        /* 1: rbc_autotune_tc found routed tensor-form
+                                  calls faster without the router's picks
+                                  (the nearest lists alone), and they skip
+                                  the router                             */
 } rbc_index_info;
 
 typedef struct {               /* work done by the last rbc_query on an index */
@@ -196,12 +200,14 @@ int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, ui
  * rbc_autotune_tc times 1, 2, 4, 8 probes (and RBC_TC_ROUTER_ONLY in routed
  * mode) x 2048, 8192, 32768 rows on sample
  * queries in the given mode (RBC_QUERY_EXACT_TC, optionally
- * | RBC_QUERY_ROUTED, where it also tries one and two router picks when
- * the router was attached with picks) and keeps the fastest; it also times
- * the plain FP32
+ * | RBC_QUERY_ROUTED, where it also tries one and two router picks, and the
+ * nearest lists without the router, when the router was attached with picks;
+ * the last makes routed tensor-form calls skip the router, info.tc_unrouted)
+ * and keeps the fastest; it also times the plain FP32
  * search (RBC_QUERY_EXACT with the same routing) and, when that is faster,
  * makes RBC_QUERY_EXACT_TC calls on this index run it (info.tc_plain).
- * rbc_set_tc_tuning selects the tensor form again.  Results never change. */
+ * rbc_set_tc_tuning selects the tensor form, routed as asked, again; so does
+ * attaching a router.  Results never change. */
 #define RBC_TC_ROUTER_ONLY 0xFFu
 int rbc_set_tc_tuning(rbc_index *index, uint32_t probes, uint64_t probe_rows);
 int rbc_get_tc_tuning(const rbc_index *index, uint32_t *probes, uint64_t *probe_rows);

@@ -427,6 +427,8 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
     offsets = idx->os_offsets;
   } else if (base == RBC_QUERY_EXACT_TC) {
     if (!(idx->flags & RBC_BUILD_BF16)) return fail(RBC_ERR_INVALID, "rbc_query: index has no BF16 lists");
+    // the autotuner may have found the router's picks not worth their cost
+    if (idx->tc_unrouted) mode &= ~(uint32_t)RBC_QUERY_ROUTED;
     if (k <= kTcMaxK && !idx->tc_plain) return query_tc(idx, dQ, m, ldq, k, mode, dIds, dDists, ldo, s);
     // wider k (the shortlists stop at 56 entries), or the autotuner found the
     // plain search faster: the FP32 exact search over the same partition
@@ -1140,6 +1142,7 @@ int rbc_get_info(const rbc_index *idx, rbc_index_info *info) {
   info->tc_format = idx->tc.format;
   info->tc_plain = idx->tc_plain ? 1u : 0u;
   info->router_picks = idx->router ? idx->router_probes : 0u;
+  info->tc_unrouted = idx->tc_unrouted ? 1u : 0u;
   return RBC_OK;
 }
 
@@ -1214,6 +1217,7 @@ int rbc_set_router(rbc_index *idx, rbc_router *router, uint32_t probes) {
   if (router && probes > 7) return fail(RBC_ERR_INVALID, "rbc_set_router: probes must be in [0, 7]");
   idx->router = router;
   idx->router_probes = router ? probes : 0;
+  idx->tc_unrouted = false;  // a tuning decision about another router does not carry over
   return RBC_OK;
 }
 

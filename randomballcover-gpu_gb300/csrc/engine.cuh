@@ -159,6 +159,7 @@ struct rbc_index {
   // learned router (rbc_set_router): probes its top router_probes lists
   rbc_router *router = nullptr;
   uint32_t router_probes = 0;
+  bool tc_unrouted = false;  // rbc_autotune_tc: routed tensor-form calls skip the router
   // benchmark instrumentation (rbc_set_profiling)
   bool profile = false;
   std::vector<cudaEvent_t> ev_pool;  // pairs of events around search launches

@@ -136,6 +136,7 @@ int rbc_set_tc_tuning(rbc_index *idx, uint32_t probes, uint64_t probe_rows) {
   idx->tc_probes = probes;
   idx->tc_probe_rows = probe_rows;
   idx->tc_plain = false;
+  idx->tc_unrouted = false;
   return RBC_OK;
 }
 
@@ -167,17 +168,23 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   uint64_t best_rows = 0;
   int rc = RBC_OK;
   idx->tc_plain = false;
-  // routed calls with router picks also try one and two picks (a call that
-  // plans with the router's distance head, picks = 0, keeps its setting)
+  // routed calls with router picks also try one and two picks, and the
+  // nearest lists without the router (picks = kNoRouter below: the call then
+  // skips it); a call that plans with the router's distance head (picks = 0)
+  // keeps its setting
   const bool routed = (mode & RBC_QUERY_ROUTED) && idx->router;
   const uint32_t user_picks = idx->router_probes;
+  constexpr uint32_t kNoRouter = 0xFFFFFFFFu;
   std::vector<uint32_t> picks_set = {user_picks};
-  if (routed && user_picks > 0) picks_set = {1u, 2u};
+  if (routed && user_picks > 0) picks_set = {1u, 2u, kNoRouter};
   uint32_t best_picks = user_picks;
+  idx->tc_unrouted = false;
   for (uint32_t picks : picks_set) {
-    idx->router_probes = picks;
+    const bool unrouted = picks == kNoRouter;
+    idx->router_probes = unrouted ? user_picks : picks;
+    idx->tc_unrouted = unrouted;
     for (uint32_t p : {RBC_TC_ROUTER_ONLY, 1u, 2u, 4u, 8u}) {
-      if (p == RBC_TC_ROUTER_ONLY && !routed) continue;  // the router's picks alone: routed calls only
+      if (p == RBC_TC_ROUTER_ONLY && (!routed || unrouted)) continue;  // the router's picks alone: routed calls only
       for (uint64_t r : {2048ull, 8192ull, 32768ull}) {
         idx->tc_probes = p;
         idx->tc_probe_rows = r;
@@ -203,7 +210,8 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
     }
     if (rc != RBC_OK) break;
   }
-  idx->router_probes = rc == RBC_OK ? best_picks : user_picks;
+  idx->tc_unrouted = rc == RBC_OK && best_picks == kNoRouter;
+  idx->router_probes = rc == RBC_OK && best_picks != kNoRouter ? best_picks : user_picks;
   // the plain FP32 search on the same lists, same routing: when it is the
   // faster of the two, RBC_QUERY_EXACT_TC calls run it
   double plain = 1e30;

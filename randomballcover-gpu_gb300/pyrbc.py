@@ -43,7 +43,8 @@ class IndexInfo(C.Structure):
     _fields_ = [("n", C.c_uint64), ("d", C.c_uint32), ("ld", C.c_uint32), ("num_reps", C.c_uint32),
                 ("s", C.c_uint32), ("metric", C.c_int), ("flags", C.c_uint32), ("min_list", C.c_uint64),
                 ("max_list", C.c_uint64), ("device_bytes", C.c_uint64), ("tc_format", C.c_uint32),
-                ("tc_plain", C.c_uint32), ("router_picks", C.c_uint32)]
+                ("tc_plain", C.c_uint32), ("router_picks", C.c_uint32),
+                ("tc_unrouted", C.c_uint32)]
 
 
 class QueryStats(C.Structure):

@@ -277,3 +277,42 @@ def test_fused_top_lists_match_the_logits(rbc, d, H, L, P):
     np.testing.assert_array_equal(top[gap], order[gap, :P])
     assert (top >= 0).all() and (top < L).all()
     r.close()
+
+
+def test_autotune_may_skip_an_unhelpful_router(rbc, oracle):
+    """An untrained router (random weights) on i.i.d. integer features: its
+    picks are noise.  rbc_autotune_tc in routed mode also times the nearest
+    lists without the router; whichever it keeps, routed tensor-form answers
+    stay the oracle's, and when it skips the router (info()["tc_unrouted"])
+    a routed call does exactly the unrouted call's work.  Setting the knobs
+    by hand or attaching the router again consults the router again."""
+    n, d, nr = 60000, 64, 128
+    X = rbc.synth(2, 17, 0, n, d)
+    Q = rbc.synth(2, 17, 1, 400, d)
+    Qt = rbc.synth(2, 17, 3, 2000, d)
+    idx = rbc.Index(X, nr, seed=3, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    r = rbc.Router(d, 64, nr, seed=9)
+    idx.set_router(r, probes=2)
+    routed = rbc.QUERY_EXACT_TC | rbc.QUERY_ROUTED
+    idx.autotune_tc(Qt, 10, routed)
+    skip = idx.info()["tc_unrouted"]
+    assert skip in (0, 1)
+    ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), 10)
+    ids, dists = idx.query(Q, 10, mode=routed)
+    np.testing.assert_array_equal(rbc.u32(ids), ri)
+    np.testing.assert_array_equal(dists.cpu().numpy(), rd)
+    st_routed = idx.stats()
+    if skip:
+        idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
+        st_plain = idx.stats()
+        assert st_routed["lists_probed"] == st_plain["lists_probed"]
+        assert st_routed["point_pairs"] == st_plain["point_pairs"]
+    p, rows = idx.tc_tuning()
+    idx.set_tc_tuning(p if p else 2, rows)
+    assert idx.info()["tc_unrouted"] == 0
+    idx.set_router(r, probes=2)
+    assert idx.info()["tc_unrouted"] == 0
+    ids, dists = idx.query(Q, 10, mode=routed)
+    np.testing.assert_array_equal(rbc.u32(ids), ri)
+    idx.close()
+    r.close()
