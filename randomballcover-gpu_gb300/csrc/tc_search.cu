@@ -925,9 +925,15 @@ __global__ void __launch_bounds__(kThreads, 1)
               for (uint32_t j = 0; j < kChunk; j++)
                 if (c0 + j >= valid) r[j] = 0xff800000u;  // -inf: v = +inf, never a candidate
             }
-            float mx = -INFINITY;
+            // four independent 3-input max chains, then their max: a short
+            // dependency chain between the two reads of the block
+            float m4[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
 #pragma unroll
-            for (uint32_t j = 0; j < kChunk; j += 2) mx = fmax3(mx, __uint_as_float(r[j]), __uint_as_float(r[j + 1]));
+            for (uint32_t j = 0; j < kChunk; j += 8)
+#pragma unroll
+              for (uint32_t i = 0; i < 4; i++)
+                m4[i] = fmax3(m4[i], __uint_as_float(r[j + 2 * i]), __uint_as_float(r[j + 2 * i + 1]));
+            const float mx = fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3]));
             if (!__any_sync(0xffffffffu, mx >= tD)) continue;
 #pragma unroll
             for (uint32_t j = 0; j < kChunk; j++) r[j] = __float_as_uint(-2.f * __uint_as_float(r[j]));

@@ -193,6 +193,9 @@ def test_router_only_probes_gain_over_the_nearest_list(rbc, oracle):
     print(f"one probed list: nearest {nearest['point_pairs'] / 2000:.0f} pairs, {nearest['lists_probed'] / 2000:.1f}"
           f" lists per query; router {routed['point_pairs'] / 2000:.0f} pairs, "
           f"{routed['lists_probed'] / 2000:.1f} lists per query")
+    # the gain: the router's probe leaves the pruning fewer pairs and lists
+    assert routed["point_pairs"] < nearest["point_pairs"], (routed, nearest)
+    assert routed["lists_probed"] <= nearest["lists_probed"], (routed, nearest)
     idx.close()
     r.close()
 
