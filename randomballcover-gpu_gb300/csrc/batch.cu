@@ -107,10 +107,12 @@ namespace {
   } while (0)
 
 // Allocate every buffer, then record the whole sequence on a capture stream
-// into a graph: the FP32 instances' two rounds, each one persistent search
-// launch over all of them, then every tensor-form instance's round (its
-// uncertified queries searched again on the device), the per-instance work
-// on parallel branches.
+// into a graph: the FP32 instances' set-up (one launch each for the padded
+// queries, the nearest representatives and empty results, one distance launch
+// per padded dimension), their two rounds (each one batched plan round and
+// one persistent search launch over all of them) and their write-back; then
+// every tensor-form instance's round (its uncertified queries searched again
+// on the device), those on parallel branches.
 int prepare(rbc_batch *bt) {
   std::vector<BatchInstance *> fp, tcv;
   for (auto &ip : bt->inst) (ip->mode == RBC_QUERY_EXACT_TC ? tcv : fp).push_back(ip.get());
@@ -175,17 +177,78 @@ int prepare(rbc_batch *bt) {
     a.qthr = b.pair_thr.as<float>();
     args1[i] = a;
   }
+  // the FP32 instances' set-up, plan rounds and write-back run as batched
+  // launches over device tables of per-instance arguments (the distance
+  // blocks once per padded dimension)
+  std::vector<BatchQuery> qtab(N);
+  std::vector<BatchPlan> ptab(N);
+  std::vector<std::vector<DenseInst>> dgroups;
+  std::vector<std::pair<uint32_t, uint32_t>> dkeys;  // (ld, dp) of each group
+  uint64_t m_max = 0, elems_max = 0, mk_max = 0;
+  uint32_t nr_max = 0;
+  for (uint32_t i = 0; i < N; i++) {
+    BatchInstance &in = *fp[i];
+    rbc_index *idx = in.idx;
+    QueryBufs &b = in.b;
+    BatchQuery q{};
+    q.Q = in.Q;
+    q.ldq = in.ldq;
+    q.m = in.m;
+    q.Qp = b.Qp.as<float>();
+    q.ld = idx->ld;
+    q.d = idx->d;
+    q.Dqr = b.Dqr.as<float>();
+    q.nr = idx->nr;
+    q.probe = b.probe.as<uint32_t>();
+    q.probed = b.probed.as<float>();
+    q.res_d = b.res_d.as<float>();
+    q.res_i = b.res_i.as<uint32_t>();
+    q.tau = b.tau.as<uint32_t>();
+    q.lock = b.lock.as<uint32_t>();
+    q.kw = kListWidth;
+    q.ctl = b.ctl.as<uint32_t>();
+    q.k = in.k;
+    q.ldo = in.ldo;
+    q.ids = in.ids;
+    q.dists = in.dists;
+    qtab[i] = q;
+    BatchPlan bp{};
+    // the query tile the single-index planner would take for this instance
+    bp.qtile = (uint32_t)search_query_tile(idx->dp, tq, list_width_for(in.k));
+    fill_plan_args(idx, b, in.m, 1, bp.qtile, idx->offsets, idx->radius, bp.a);
+    bp.cnt = b.cnt.as<uint32_t>();
+    bp.start = b.start.as<uint32_t>();
+    bp.cursor = b.cursor.as<uint32_t>();
+    bp.tcnt = b.tcnt.as<uint32_t>();
+    bp.tstart = b.tstart.as<uint32_t>();
+    bp.max_rows = idx->item_rows;
+    bp.items = b.items.as<SearchItem>();
+    bp.cap = b.item_cap;
+    bp.nitems = b.ctl.as<uint32_t>() + 1;
+    bp.err = b.ctl.as<uint32_t>() + 2;
+    ptab[i] = bp;
+    const std::pair<uint32_t, uint32_t> key(idx->ld, idx->dp);
+    size_t g = std::find(dkeys.begin(), dkeys.end(), key) - dkeys.begin();
+    if (g == dkeys.size()) {
+      dkeys.push_back(key);
+      dgroups.emplace_back();
+    }
+    dgroups[g].push_back(DenseInst{b.Qp.as<float>(), in.m, idx->R, idx->nr, b.Dqr.as<float>(), idx->nr});
+    m_max = std::max<uint64_t>(m_max, in.m);
+    nr_max = std::max(nr_max, idx->nr);
+    elems_max = std::max<uint64_t>(elems_max, in.m * idx->ld);
+    mk_max = std::max<uint64_t>(mk_max, in.m * in.k);
+  }
   for (BatchInstance *ip : tcv) {
     ip->tc = std::make_unique<TcQuery>();
     BTRY(tc_setup(ip->idx, ip->m, ip->k, RBC_QUERY_EXACT_TC, true, *ip->tc, s));
   }
-  // Each instance's own launches (set-up, planning, results, the tensor-form
-  // rounds) are captured on side streams forked from the capture stream and
-  // joined back before each shared search launch, so the graph holds them as
-  // parallel branches instead of running them in turn.  The instances of one
-  // index share a branch (its router's scratch is the index's); distinct
-  // indexes go round the branches.
-  const uint32_t nbranch = (uint32_t)std::min<size_t>(bt->inst.size(), 8);
+  // The tensor-form instances are captured on side streams forked from the
+  // capture stream and joined back, so the graph holds them as parallel
+  // branches instead of running them in turn.  The instances of one index
+  // share a branch (its router's scratch is the index's); distinct indexes go
+  // round the branches.
+  const uint32_t nbranch = (uint32_t)std::min<size_t>(tcv.size(), 8);
   for (uint32_t i = 0; i < nbranch; i++) {
     cudaStream_t b;
     BCK(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking));
@@ -215,6 +278,17 @@ int prepare(rbc_batch *bt) {
   BCK(cudaMemcpy(t1, args1.data(), N * sizeof(SearchArgs), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(dsrc, srcs.data(), N * sizeof(void *), cudaMemcpyHostToDevice));
   BCK(cudaMemcpy(dcnt, counts.data(), N * sizeof(void *), cudaMemcpyHostToDevice));
+  BatchQuery *dq = dalloc<BatchQuery>(N, bt->owned);
+  BatchPlan *dp_tab = dalloc<BatchPlan>(N, bt->owned);
+  if (N && (!dq || !dp_tab)) return fail(RBC_ERR_NOMEM, "rbc_batch_run: device allocation failed");
+  BCK(cudaMemcpy(dq, qtab.data(), N * sizeof(BatchQuery), cudaMemcpyHostToDevice));
+  BCK(cudaMemcpy(dp_tab, ptab.data(), N * sizeof(BatchPlan), cudaMemcpyHostToDevice));
+  std::vector<DenseInst *> ddev(dgroups.size());
+  for (size_t g = 0; g < dgroups.size(); g++) {
+    ddev[g] = dalloc<DenseInst>(dgroups[g].size(), bt->owned);
+    if (!ddev[g]) return fail(RBC_ERR_NOMEM, "rbc_batch_run: device allocation failed");
+    BCK(cudaMemcpy(ddev[g], dgroups[g].data(), dgroups[g].size() * sizeof(DenseInst), cudaMemcpyHostToDevice));
+  }
   const int grid = N ? search_grid(metric, dp_max, tq) : 1;
   SearchArgs g{};
   g.items = all;
@@ -246,27 +320,21 @@ int prepare(rbc_batch *bt) {
   };
   auto capture = [&]() -> int {
     BCK(cudaMemsetAsync(bt->ctl, 0, 64, s));
-    for (uint32_t round = 0; round < 2 && N; round++) {
-      BTRY(fork());
-      for (BatchInstance *ip : fp) {
-        BatchInstance &in = *ip;
-        rbc_index *idx = in.idx;
-        QueryBufs &b = in.b;
-        cudaStream_t ls = lane_of(idx);
-        if (round == 0) {
-          BCK(cudaMemsetAsync(b.ctl.p, 0, 64, ls));
-          BCK(launch_pad_rows(in.Q, in.ldq, b.Qp.as<float>(), idx->ld, in.m, idx->d, ls));
-          BCK(launch_dense_dist(idx->metric, b.Qp.as<float>(), in.m, idx->R, idx->nr, idx->ld, idx->dp,
-                                b.Dqr.as<float>(), idx->nr, ls));
-          BCK(launch_row_topp(b.Dqr.as<float>(), in.m, idx->nr, 1, b.probe.as<uint32_t>(), b.probed.as<float>(),
-                              ls));
-          BCK(launch_init_results(b.res_d.as<float>(), b.res_i.as<uint32_t>(), b.tau.as<uint32_t>(),
-                                  b.lock.as<uint32_t>(), in.m, kListWidth, ls));
+    if (N) {
+      BCK(launch_batch_pad(dq, N, elems_max, s));
+      for (size_t gi = 0; gi < dgroups.size(); gi++) {
+        uint64_t na = 0, nb = 0;
+        for (const DenseInst &di : dgroups[gi]) {
+          na = std::max(na, di.na);
+          nb = std::max(nb, di.nb);
         }
-        BTRY(plan_and_search(idx, b, in.m, 1, in.k, round, idx->Xp, idx->perm, idx->offsets, idx->radius, grid,
-                             nullptr, ls, 1, tq));
+        BCK(launch_dense_dist_batch(metric, ddev[gi], (uint32_t)dgroups[gi].size(), na, nb, dkeys[gi].first,
+                                    dkeys[gi].second, s));
       }
-      BTRY(join());
+      BCK(launch_batch_nearest(dq, N, m_max, s));
+    }
+    for (uint32_t round = 0; round < 2 && N; round++) {
+      BCK(launch_plan_batch(dp_tab, N, round, nr_max, m_max, 1, s));
       batch_offsets_kernel<<<1, 1, 0, s>>>(dcnt, N, offs, bt->ctl + 1);
       BCK(launched());
       batch_concat_kernel<<<dim3(64, N), 256, 0, s>>>(dsrc, dcnt, offs, all);
@@ -275,12 +343,11 @@ int prepare(rbc_batch *bt) {
       g.insts = round == 0 ? t0 : t1;
       BCK(launch_search(metric, g, grid, s, tq));
     }
-    // the FP32 instances' results and the tensor-form instances, each a whole
-    // round with its device fallback; their error words fold into the batch's
+    if (N) BCK(launch_batch_write(dq, N, mk_max, s));
+    // the tensor-form instances, each a whole round with its device fallback
+    // on a branch; their error words fold into the batch's
+    if (tcv.empty()) return RBC_OK;
     BTRY(fork());
-    for (BatchInstance *ip : fp)
-      BCK(launch_write_results(ip->b.res_d.as<float>(), ip->b.res_i.as<uint32_t>(), ip->m, ip->k, kListWidth, ip->ids,
-                               ip->dists, ip->ldo, lane_of(ip->idx)));
     for (BatchInstance *ip : tcv)
       BTRY(tc_enqueue(ip->idx, *ip->tc, ip->Q, ip->m, ip->ldq, ip->ids, ip->dists, ip->ldo, true, bt->ctl + 2,
                       nullptr, lane_of(ip->idx)));

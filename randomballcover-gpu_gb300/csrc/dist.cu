@@ -38,18 +38,31 @@ __device__ __forceinline__ void stage_row_block(float *Rs, uint32_t S, const flo
   }
 }
 
-// D[i][j] for rows of block blockIdx.x and columns [c0, c1).
-template <int METRIC, int TQ>
+// D[i][j] for rows of block blockIdx.x and columns [c0, c1).  A batched
+// launch takes instance blockIdx.z's operands from the table; its blocks past
+// the instance's rows or columns return.
+template <int METRIC, int TQ, bool BATCH = false>
 __global__ void __launch_bounds__(kTileThreads, 2)
     dense_kernel(const float *__restrict__ A, uint64_t na, const float *__restrict__ B, uint64_t nb,
-                 uint32_t ld, uint32_t dp, float *__restrict__ D, uint64_t ldD, uint32_t cols_per_cta) {
+                 uint32_t ld, uint32_t dp, float *__restrict__ D, uint64_t ldD, uint32_t cols_per_cta,
+                 const DenseInst *__restrict__ tab = nullptr) {
   constexpr uint32_t BQ = 16 * TQ;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (BATCH) {
+    const DenseInst &di = tab[blockIdx.z];
+    A = di.A;
+    na = di.na;
+    B = di.B;
+    nb = di.nb;
+    D = di.D;
+    ldD = di.ldD;
+  }
   const uint32_t S = dp + 4;
   float *Rs = reinterpret_cast<float *>(smem_raw);
   float *Cs0 = Rs + BQ * S, *Cs1 = Cs0 + kTileCols * S;
   const int tq = threadIdx.x >> 4, tx = threadIdx.x & 15;
   const uint64_t r0 = (uint64_t)blockIdx.x * BQ;
+  if (r0 >= na) return;
   const uint32_t rvalid = (uint32_t)min((uint64_t)BQ, na - r0);
   const uint64_t c0 = (uint64_t)blockIdx.y * cols_per_cta;
   if (c0 >= nb) return;
@@ -233,6 +246,19 @@ cudaError_t dense_tq(const float *A, uint64_t na, const float *B, uint64_t nb, u
 }
 
 template <int METRIC, int TQ>
+cudaError_t dense_batch_tq(const DenseInst *tab, uint32_t ninst, uint64_t na_max, uint64_t nb_max, uint32_t ld,
+                           uint32_t dp, cudaStream_t s) {
+  size_t smem = rows_smem_bytes<TQ>(dp);
+  cudaError_t e = prep(dense_kernel<METRIC, TQ, true>, smem);
+  if (e != cudaSuccess) return e;
+  const uint32_t cpc = 512;
+  dim3 grid((unsigned)((na_max + 16 * TQ - 1) / (16 * TQ)), (unsigned)((nb_max + cpc - 1) / cpc), ninst);
+  dense_kernel<METRIC, TQ, true><<<grid, kTileThreads, smem, s>>>(nullptr, 0, nullptr, 0, ld, dp, nullptr, 0, cpc,
+                                                                   tab);
+  return launched();
+}
+
+template <int METRIC, int TQ>
 cudaError_t argmin_tq(const float *A, uint64_t na, const float *B, uint32_t nb, uint32_t ld, uint32_t dp,
                       uint32_t *best, float *bestd, cudaStream_t s) {
   size_t smem = rows_smem_bytes<TQ>(dp);
@@ -284,6 +310,12 @@ cudaError_t launch_dense_dist(int metric, const float *A, uint64_t na, const flo
                               uint32_t ld, uint32_t dp, float *D, uint64_t ldD, cudaStream_t s) {
   if (na == 0 || nb == 0) return cudaSuccess;
   RBC_DISPATCH(metric, dp, dense_tq, A, na, B, nb, ld, dp, D, ldD, s);
+}
+
+cudaError_t launch_dense_dist_batch(int metric, const DenseInst *tab, uint32_t ninst, uint64_t na_max,
+                                    uint64_t nb_max, uint32_t ld, uint32_t dp, cudaStream_t s) {
+  if (ninst == 0 || na_max == 0 || nb_max == 0) return cudaSuccess;
+  RBC_DISPATCH(metric, dp, dense_batch_tq, tab, ninst, na_max, nb_max, ld, dp, s);
 }
 
 cudaError_t launch_argmin(int metric, const float *A, uint64_t na, const float *B, uint32_t nb,

@@ -116,14 +116,10 @@ static float round_down_f(double v) {
   return (double)f > v ? std::nextafter(f, 0.f) : f;
 }
 
-int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
-                    const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
-                    int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq, uint32_t qtile_over,
-                    ListFilter filter) {
-  const int tqv = tq < 0 ? idx->tune_tq : tq;
-  const uint32_t nr = idx->nr, qtile = qtile_over ? qtile_over : (uint32_t)search_query_tile(idx->dp, tqv, list_width_for(k));
-  uint32_t *ctl = b.ctl.as<uint32_t>();  // [0] work, [1] nitems, [2] err
-  PlanArgs a{};
+void fill_plan_args(const rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t qtile,
+                    const uint64_t *offsets, const float *radius, PlanArgs &a) {
+  const uint32_t nr = idx->nr;
+  a = PlanArgs{};
   a.Dqr = b.Dqr.as<float>();
   a.radius = radius;
   a.offsets = offsets;
@@ -150,6 +146,17 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
   a.list_cursor = b.cursor.as<uint32_t>();
   a.pair_q = b.pair_q.as<uint32_t>();
   a.pair_thr = b.pair_thr.as<float>();
+}
+
+int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t k, uint32_t mode,
+                    const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
+                    int grid, unsigned long long *stats, cudaStream_t s, int stage, int tq, uint32_t qtile_over,
+                    ListFilter filter) {
+  const int tqv = tq < 0 ? idx->tune_tq : tq;
+  const uint32_t nr = idx->nr, qtile = qtile_over ? qtile_over : (uint32_t)search_query_tile(idx->dp, tqv, list_width_for(k));
+  uint32_t *ctl = b.ctl.as<uint32_t>();  // [0] work, [1] nitems, [2] err
+  PlanArgs a;
+  fill_plan_args(idx, b, m, P, qtile, offsets, radius, a);
   uint32_t *cnt = b.cnt.as<uint32_t>(), *start = b.start.as<uint32_t>();
   uint32_t *tcnt = b.tcnt.as<uint32_t>(), *tstart = b.tstart.as<uint32_t>();
 

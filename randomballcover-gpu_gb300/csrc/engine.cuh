@@ -88,6 +88,11 @@ int plan_and_search(rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32
                     const float *X, const uint32_t *pid, const uint64_t *offsets, const float *radius,
                     int grid, unsigned long long *stats, cudaStream_t s, int stage = 2, int tq = -1,
                     uint32_t qtile = 0, ListFilter filter = ListFilter());
+// The plan arguments of one query round (the per-index directed-rounding
+// constants of the pruning bound, the round's buffers); list_cnt and phase
+// are left to the caller.
+void fill_plan_args(const rbc_index *idx, QueryBufs &b, uint64_t m, uint32_t P, uint32_t qtile,
+                    const uint64_t *offsets, const float *radius, PlanArgs &a);
 // Build the tensor-core operands of an index that has its partition.
 int build_tc(rbc_index *idx, cudaStream_t s);
 // Work items a plan of mb queries can produce with query tiles of qtile

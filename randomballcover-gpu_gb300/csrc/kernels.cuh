@@ -162,6 +162,60 @@ struct PlanArgs {
 // pruning bound survives.  a.phase 0 counts per list into a.list_cnt; phase 1
 // fills pair_q / pair_thr with a.list_cnt pointing at the scanned starts.
 cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s);
+// One instance of a batched query set-up and result write-back (rbc_batch).
+struct BatchQuery {
+  const float *Q;        // m rows of d floats, stride ldq
+  uint64_t ldq, m;
+  float *Qp;             // padded copy, stride ld
+  uint32_t ld, d;
+  const float *Dqr;      // m x nr query-representative distances
+  uint32_t nr;
+  uint32_t *probe;       // per query: the nearest representative, and its distance
+  float *probed;
+  float *res_d;          // per query kw result entries, threshold, lock
+  uint32_t *res_i, *tau, *lock;
+  uint32_t kw;
+  uint32_t *ctl;         // 16 control words, zeroed by the set-up
+  uint32_t k, ldo;       // write-back: the first k entries of each list
+  uint32_t *ids;
+  float *dists;
+};
+// Padded query copies of every instance in one launch.
+cudaError_t launch_batch_pad(const BatchQuery *tab, uint32_t ninst, uint64_t elems_max, cudaStream_t s);
+// Every instance's nearest representatives (ties to the lower index, as
+// launch_row_topp with P = 1), empty result lists and zeroed control words.
+cudaError_t launch_batch_nearest(const BatchQuery *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s);
+// Every instance's results written out (as launch_write_results).
+cudaError_t launch_batch_write(const BatchQuery *tab, uint32_t ninst, uint64_t mk_max, cudaStream_t s);
+// One instance of a batched dense distance block: D (na x nb, row stride ldD)
+// = distances of A's rows to B's rows.
+struct DenseInst {
+  const float *A;
+  uint64_t na;
+  const float *B;
+  uint64_t nb;
+  float *D;
+  uint64_t ldD;
+};
+// Every instance of the table in one launch; all share the row stride ld and
+// the padded dimension dp (the maxima size the grid).
+cudaError_t launch_dense_dist_batch(int metric, const DenseInst *tab, uint32_t ninst, uint64_t na_max,
+                                    uint64_t nb_max, uint32_t ld, uint32_t dp, cudaStream_t s);
+// One instance of a batched plan round (rbc_batch): its plan arguments
+// (list_cnt and phase are set per step) and its plan buffers.
+struct BatchPlan {
+  PlanArgs a;
+  uint32_t *cnt, *start, *cursor, *tcnt, *tstart;  // nr + 1 each
+  uint32_t qtile, max_rows;
+  SearchItem *items;
+  uint64_t cap;
+  uint32_t *nitems, *err;
+};
+// A whole plan round (count, scan, fill, tiles per list, scan, items) of
+// every instance in the device table, each step one launch over all of them;
+// the maxima size the grids (blocks past an instance's sizes return).
+cudaError_t launch_plan_batch(const BatchPlan *tab, uint32_t ninst, uint32_t mode, uint32_t nr_max, uint64_t m_max,
+                              uint32_t P_max, cudaStream_t s);
 // Which lists of a plan get work items: rows_lo <= rows < rows_hi and
 // cnt_lo <= planned queries < cnt_hi.
 // Of each selected list, only rows [skip, skip + take) (list-relative) get

@@ -124,12 +124,28 @@ __device__ __forceinline__ float psi_bound(float psi, const PlanArgs &a) {
   return a.metric == RBC_L1 ? t : __fsqrt_ru(t);
 }
 
+// A batched launch takes instance blockIdx.z's arguments from the table, its
+// list counters by phase.
+template <bool BATCH>
+__device__ __forceinline__ PlanArgs plan_args_of(const PlanArgs &a0, const BatchPlan *tab, uint32_t phase) {
+  if (!BATCH) return a0;
+  const BatchPlan &bp = tab[blockIdx.z];
+  PlanArgs a = bp.a;
+  a.phase = phase;
+  a.list_cnt = phase == 0 ? bp.cnt : bp.start;
+  a.list_cursor = bp.cursor;
+  return a;
+}
+
 // mode 1: every (query, list) pair except the probed ones whose bound
 // survives; pass 0 counts per list, pass 1 writes the list-major entries.
-__global__ void plan_kernel(PlanArgs a) {
+template <bool BATCH>
+__global__ void plan_kernel(PlanArgs a0, const BatchPlan *tab, uint32_t phase) {
   __shared__ float s_tau[kPlanQueries], s_chi0[kPlanQueries];
+  const PlanArgs a = plan_args_of<BATCH>(a0, tab, phase);
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t q0 = (uint64_t)blockIdx.y * kPlanQueries;
+  if (q0 >= a.m) return;  // a batched grid's blocks past this instance's queries
   const uint64_t q1 = min(a.m, q0 + kPlanQueries);
   // the per-query terms, once per block
   for (uint32_t j = threadIdx.x; j < q1 - q0; j += blockDim.x) {
@@ -168,7 +184,9 @@ __global__ void plan_kernel(PlanArgs a) {
 
 // mode 0: the probe pairs (q, probe[q][p]) of non-empty lists, each list once
 // per query; one thread per probe entry.
-__global__ void plan_probe_kernel(PlanArgs a) {
+template <bool BATCH>
+__global__ void plan_probe_kernel(PlanArgs a0, const BatchPlan *tab, uint32_t phase) {
+  const PlanArgs a = plan_args_of<BATCH>(a0, tab, phase);
   const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (i >= a.m * a.P) return;
   const uint64_t q = i / a.P;
@@ -212,10 +230,10 @@ __device__ __forceinline__ bool list_selected(const uint64_t *offsets, const uin
   return np >= f.rows_lo && np < f.rows_hi && c >= f.cnt_lo && c < f.cnt_hi && (f.skip == 0 || np > f.skip);
 }
 
-__global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, const uint64_t *__restrict__ offsets,
-                                      uint32_t nr, uint32_t qtile, uint32_t max_rows, ListFilter f,
-                                      uint32_t *__restrict__ tile_cnt) {
-  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void tiles_per_list(const uint32_t *__restrict__ list_cnt,
+                                               const uint64_t *__restrict__ offsets, uint32_t nr, uint32_t qtile,
+                                               uint32_t max_rows, const ListFilter &f,
+                                               uint32_t *__restrict__ tile_cnt, uint32_t r) {
   if (r < nr)
     tile_cnt[r] = list_selected(offsets, list_cnt, r, f)
                       ? (list_cnt[r] + qtile - 1) / qtile * row_chunks(offsets, r, max_rows, f)
@@ -223,16 +241,23 @@ __global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, con
   if (r == nr) tile_cnt[nr] = 0;
 }
 
+__global__ void tiles_per_list_kernel(const uint32_t *__restrict__ list_cnt, const uint64_t *__restrict__ offsets,
+                                      uint32_t nr, uint32_t qtile, uint32_t max_rows, ListFilter f,
+                                      uint32_t *__restrict__ tile_cnt) {
+  tiles_per_list(list_cnt, offsets, nr, qtile, max_rows, f, tile_cnt, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // items for list r: its query tiles x row chunks, in list order.  A plan
 // with more items than the buffer holds writes none, records RBC_ERR_NOMEM
 // and leaves an empty work list (the caller sizes the buffer so this cannot
 // happen; the check keeps every write in bounds regardless).
-__global__ void plan_items_kernel(const uint32_t *__restrict__ list_cnt, const uint32_t *__restrict__ list_start,
-                                  const uint32_t *__restrict__ tile_start, const uint64_t *__restrict__ offsets,
-                                  uint32_t nr, uint32_t qtile, uint32_t max_rows, ListFilter f,
-                                  SearchItem *__restrict__ items, uint64_t cap, uint32_t *__restrict__ nitems,
-                                  uint32_t *__restrict__ err) {
-  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void plan_items(const uint32_t *__restrict__ list_cnt,
+                                           const uint32_t *__restrict__ list_start,
+                                           const uint32_t *__restrict__ tile_start,
+                                           const uint64_t *__restrict__ offsets, uint32_t nr, uint32_t qtile,
+                                           uint32_t max_rows, const ListFilter &f, SearchItem *__restrict__ items,
+                                           uint64_t cap, uint32_t *__restrict__ nitems, uint32_t *__restrict__ err,
+                                           uint32_t r) {
   const uint32_t total = tile_start[nr];
   if (r == nr) {
     *nitems = total <= cap ? total : 0u;
@@ -260,6 +285,77 @@ __global__ void plan_items_kernel(const uint32_t *__restrict__ list_cnt, const u
   }
 }
 
+__global__ void plan_items_kernel(const uint32_t *__restrict__ list_cnt, const uint32_t *__restrict__ list_start,
+                                  const uint32_t *__restrict__ tile_start, const uint64_t *__restrict__ offsets,
+                                  uint32_t nr, uint32_t qtile, uint32_t max_rows, ListFilter f,
+                                  SearchItem *__restrict__ items, uint64_t cap, uint32_t *__restrict__ nitems,
+                                  uint32_t *__restrict__ err) {
+  plan_items(list_cnt, list_start, tile_start, offsets, nr, qtile, max_rows, f, items, cap, nitems, err,
+             blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// ---------------------------------------------------------------- batched plan rounds (rbc_batch)
+// Instance blockIdx.z (blockIdx.y for the one-block scans) of the table.
+__global__ void batch_zero_kernel(const BatchPlan *tab) {
+  const BatchPlan &bp = tab[blockIdx.z];
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r <= bp.a.nr) {
+    bp.cnt[r] = 0;
+    bp.cursor[r] = 0;
+  }
+}
+
+// Exclusive scan of nr + 1 counters, one block per instance, in 256-entry
+// steps with a running carry (the lists of one instance number thousands at
+// most).
+__global__ void batch_scan_kernel(const BatchPlan *tab, uint32_t which) {
+  __shared__ uint32_t wsum[8];
+  const BatchPlan &bp = tab[blockIdx.y];
+  const uint32_t *in = which ? bp.tcnt : bp.cnt;
+  uint32_t *out = which ? bp.tstart : bp.start;
+  const uint32_t n = bp.a.nr + 1, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < n; base += 256) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < n ? in[i] : 0u;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((int)lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      uint32_t t = lane < 8 ? wsum[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+        if ((int)lane >= o) t += y;
+      }
+      if (lane < 8) wsum[lane] = t;
+    }
+    __syncthreads();
+    if (i < n) out[i] = carry + (w ? wsum[w - 1] : 0u) + x - v;
+    carry += wsum[7];
+    __syncthreads();
+  }
+}
+
+__global__ void batch_tiles_kernel(const BatchPlan *tab) {
+  const BatchPlan &bp = tab[blockIdx.z];
+  tiles_per_list(bp.cnt, bp.a.offsets, bp.a.nr, bp.qtile, bp.max_rows, ListFilter(), bp.tcnt,
+                 blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void batch_items_kernel(const BatchPlan *tab) {
+  const BatchPlan &bp = tab[blockIdx.z];
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r > bp.a.nr) return;
+  plan_items(bp.cnt, bp.start, bp.tstart, bp.a.offsets, bp.a.nr, bp.qtile, bp.max_rows, ListFilter(), bp.items,
+             bp.cap, bp.nitems, bp.err, r);
+}
+
 }  // namespace
 
 cudaError_t launch_row_topp(const float *D, uint64_t m, uint32_t nr, uint32_t P, uint32_t *probe, float *probed,
@@ -276,11 +372,40 @@ cudaError_t launch_plan_pass(const PlanArgs &a, uint32_t mode, cudaStream_t s) {
   if (a.m == 0) return cudaSuccess;
   if (mode == 0) {
     const uint64_t total = a.m * a.P;
-    plan_probe_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(a);
+    plan_probe_kernel<false><<<(unsigned)((total + 255) / 256), 256, 0, s>>>(a, nullptr, a.phase);
   } else {
     dim3 grid((a.nr + 255) / 256, (unsigned)((a.m + kPlanQueries - 1) / kPlanQueries));
-    plan_kernel<<<grid, 256, 0, s>>>(a);
+    plan_kernel<false><<<grid, 256, 0, s>>>(a, nullptr, a.phase);
   }
+  return launched();
+}
+
+cudaError_t launch_plan_batch(const BatchPlan *tab, uint32_t ninst, uint32_t mode, uint32_t nr_max, uint64_t m_max,
+                              uint32_t P_max, cudaStream_t s) {
+  if (ninst == 0 || m_max == 0) return cudaSuccess;
+  const unsigned lists = (nr_max + 1 + 255) / 256;
+  batch_zero_kernel<<<dim3(lists, 1, ninst), 256, 0, s>>>(tab);
+  cudaError_t e = launched();
+  for (uint32_t phase = 0; phase < 2 && e == cudaSuccess; phase++) {
+    if (mode == 0) {
+      plan_probe_kernel<true><<<dim3((unsigned)((m_max * P_max + 255) / 256), 1, ninst), 256, 0, s>>>(
+          PlanArgs{}, tab, phase);
+    } else {
+      plan_kernel<true><<<dim3((nr_max + 255) / 256, (unsigned)((m_max + kPlanQueries - 1) / kPlanQueries), ninst),
+                          256, 0, s>>>(PlanArgs{}, tab, phase);
+    }
+    if ((e = launched()) != cudaSuccess) break;
+    if (phase == 0) {
+      batch_scan_kernel<<<dim3(1, ninst), 256, 0, s>>>(tab, 0);
+      e = launched();
+    }
+  }
+  if (e != cudaSuccess) return e;
+  batch_tiles_kernel<<<dim3(lists, 1, ninst), 256, 0, s>>>(tab);
+  if ((e = launched()) != cudaSuccess) return e;
+  batch_scan_kernel<<<dim3(1, ninst), 256, 0, s>>>(tab, 1);
+  if ((e = launched()) != cudaSuccess) return e;
+  batch_items_kernel<<<dim3(lists, 1, ninst), 256, 0, s>>>(tab);
   return launched();
 }
 

@@ -301,6 +301,68 @@ __global__ void write_results_kernel(const float *res_d, const uint32_t *res_i, 
   if (dists) dists[q * ldo + j] = res_d[q * kw + j];
 }
 
+// ---------------------------------------------------------------- batched query set-up (rbc_batch)
+// instance blockIdx.z of the table
+__global__ void batch_pad_kernel(const BatchQuery *tab) {
+  const BatchQuery &bq = tab[blockIdx.z];
+  const uint64_t total = bq.m * bq.ld;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = i / bq.ld;
+    const uint32_t c = (uint32_t)(i - r * bq.ld);
+    bq.Qp[i] = c < bq.d ? bq.Q[r * bq.ldq + c] : 0.f;
+  }
+}
+
+// one warp per query: the nearest representative under (distance, index),
+// then the query's empty result list
+__global__ void batch_nearest_kernel(const BatchQuery *tab) {
+  const BatchQuery &bq = tab[blockIdx.z];
+  if (blockIdx.x == 0 && threadIdx.x < 16) bq.ctl[threadIdx.x] = 0;
+  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (q >= bq.m) return;
+  const float *row = bq.Dqr + q * bq.nr;
+  float bd = FLT_MAX;
+  uint32_t bi = RBC_DUMMY;
+  for (uint32_t r = lane; r < bq.nr; r += 32) {
+    const float v = row[r];
+    if (pair_less(v, r, bd, bi)) {
+      bd = v;
+      bi = r;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+    const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (pair_less(od, oi, bd, bi)) {
+      bd = od;
+      bi = oi;
+    }
+  }
+  if (lane == 0) {
+    bq.probe[q] = bi;
+    bq.probed[q] = bd;
+    bq.tau[q] = fbits(FLT_MAX);
+    bq.lock[q] = 0;
+  }
+  for (uint32_t j = lane; j < bq.kw; j += 32) {
+    bq.res_d[q * bq.kw + j] = FLT_MAX;
+    bq.res_i[q * bq.kw + j] = RBC_DUMMY;
+  }
+}
+
+__global__ void batch_write_kernel(const BatchQuery *tab) {
+  const BatchQuery &bq = tab[blockIdx.z];
+  const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (i >= bq.m * bq.k) return;
+  const uint64_t q = i / bq.k;
+  const uint32_t j = (uint32_t)(i - q * bq.k);
+  if (bq.ids) bq.ids[q * bq.ldo + j] = bq.res_i[q * bq.kw + j];
+  if (bq.dists) bq.dists[q * bq.ldo + j] = bq.res_d[q * bq.kw + j];
+}
+
 __global__ void scatter_results_kernel(const uint32_t *src_i, const float *src_d, const uint32_t *rows, uint32_t nrows,
                                        uint32_t k, uint32_t *ids, float *dists, uint32_t ldo) {
   uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -449,6 +511,26 @@ cudaError_t launch_search(int metric, const SearchArgs &a, int grid, cudaStream_
   const uint32_t w = list_width_for(a.k) / 32;
   const int tqv = search_tq_for(a.dp, tq, 32 * w);
   RBC_SEARCH_DISPATCH(metric, tqv, w, launch_tq, a, grid, s);
+}
+
+cudaError_t launch_batch_pad(const BatchQuery *tab, uint32_t ninst, uint64_t elems_max, cudaStream_t s) {
+  if (ninst == 0 || elems_max == 0) return cudaSuccess;
+  const unsigned grid = (unsigned)std::min<uint64_t>((elems_max + 255) / 256, 1024);
+  batch_pad_kernel<<<dim3(grid, 1, ninst), 256, 0, s>>>(tab);
+  return launched();
+}
+
+cudaError_t launch_batch_nearest(const BatchQuery *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s) {
+  if (ninst == 0) return cudaSuccess;
+  const unsigned grid = (unsigned)std::max<uint64_t>((m_max * 32 + 255) / 256, 1);
+  batch_nearest_kernel<<<dim3(grid, 1, ninst), 256, 0, s>>>(tab);
+  return launched();
+}
+
+cudaError_t launch_batch_write(const BatchQuery *tab, uint32_t ninst, uint64_t mk_max, cudaStream_t s) {
+  if (ninst == 0 || mk_max == 0) return cudaSuccess;
+  batch_write_kernel<<<dim3((unsigned)((mk_max + 255) / 256), 1, ninst), 256, 0, s>>>(tab);
+  return launched();
 }
 
 cudaError_t launch_init_results(float *res_d, uint32_t *res_i, uint32_t *tau, uint32_t *lock,
