@@ -583,41 +583,58 @@ __global__ void __launch_bounds__(kThreads, 1)
       tr[0] = clk() - t_all;
       if (a.trace && g == 0 && lane == 0)
         for (int j = 0; j < 6; j++) a.trace[blockIdx.x * kTcTraceWords + j] = tr[j];
-    } else if (lane == 0) {
+    } else {
+      // split format: one query tile, A from shared memory; per B tile three
+      // MMAs per K step (hi.hi into the first accumulator, hi.lo + lo.hi
+      // into the second).  Issued like the BF16 path: the whole warp runs the
+      // loop, one elected lane issues, descriptors offset by constants.
+      static_assert(MT == 1, "the split format runs one query tile per B tile");
       const uint32_t idesc = idesc_f16_f32(kBM, kBN);
-      uint32_t ai = 0, bi = 0;
+      const uint32_t n_items = __shfl_sync(0xffffffffu, nitems, 0);
+      auto wait = [&](uint64_t *bar, uint32_t parity) {
+        return __all_sync(0xffffffffu, mbar_wait(bar, parity, a.err)) != 0;
+      };
+      uint32_t bi = 0, sa = 0, aph = 0, sb = 0, bph = 0, slot = 0, sph = 0;
+      const uint32_t lo = (kb * kTile16K) >> 4;  // the lo halves, in descriptor units
       bool ok = true;
-      for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
-        const SearchItem item = a.items[it];
-        const uint32_t sa = ai % AS;
-        if (!(ok = mbar_wait(&bar_a_full[sa], (ai / AS) & 1, a.err))) break;
-        const uint32_t ntiles = (item.np + kBN - 1) / kBN;
+      for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+        const uint32_t ntiles = __shfl_sync(0xffffffffu, (a.items[it].np + kBN - 1) / kBN, 0);
+        if (!(ok = wait(&bar_a_full[sa], aph))) break;
+        const uint64_t ad0 = sw128_desc(smem_u32(sA + sa * a_stage));
         for (uint32_t t = 0; t < ntiles; t++, bi++) {
-          const uint32_t sb = bi % BS, slot = bi % NSLOT;
-          if (!(ok = mbar_wait(&bar_b_full[sb], (bi / BS) & 1, a.err))) break;
-          if (bi >= NSLOT && !(ok = mbar_wait(&bar_t_empty[slot], ((bi / NSLOT) - 1) & 1, a.err))) break;
+          if (!(ok = wait(&bar_b_full[sb], bph))) break;
+          if (bi >= NSLOT && !(ok = wait(&bar_t_empty[slot], sph ^ 1u))) break;
           tc_fence_after();
-          const uint32_t b0 = smem_u32(sB + sb * b_stage);
+          const uint64_t bd0 = sw128_desc(smem_u32(sB + sb * b_stage));
+          const uint32_t d = tmem + slot * ACC * kBN;
 #pragma unroll
-          for (int g = 0; g < MT; g++) {
-            const uint32_t d = tmem + (slot * MT + g) * ACC * kBN;
-            const uint32_t a0 = smem_u32(sA + sa * a_stage + g * a_tile);
-            for (uint32_t k = 0; k < kb; k++) {
+          for (uint32_t k = 0; k < 2; k++)
+            if (k < kb) {
 #pragma unroll
               for (uint32_t kk = 0; kk < 4; kk++) {
-                const uint32_t off = k * kTile16K + kk * 32;
+                const uint32_t off = (k * kTile16K + kk * 32) >> 4;
                 const uint32_t acc = (k | kk) != 0;
-                const uint32_t lo = kb * kTile16K;
-                mma_bf16(d, sw128_desc(a0 + off), sw128_desc(b0 + off), idesc, acc);
-                mma_bf16(d + kBN, sw128_desc(a0 + off), sw128_desc(b0 + lo + off), idesc, acc);
-                mma_bf16(d + kBN, sw128_desc(a0 + lo + off), sw128_desc(b0 + off), idesc, 1);
+                mma_bf16_warp(d, ad0 + off, bd0 + off, idesc, acc);
+                mma_bf16_warp(d + kBN, ad0 + off, bd0 + lo + off, idesc, acc);
+                mma_bf16_warp(d + kBN, ad0 + lo + off, bd0 + off, idesc, 1);
               }
             }
+          mma_commit_warp(&bar_b_empty[sb]);
+          mma_commit_warp(&bar_t_full[slot]);
+          if (++sb == BS) {
+            sb = 0;
+            bph ^= 1u;
           }
-          mma_commit(&bar_b_empty[sb]);
-          mma_commit(&bar_t_full[slot]);
+          if (++slot == NSLOT) {
+            slot = 0;
+            sph ^= 1u;
+          }
         }
-        if (ok) mma_commit(&bar_a_empty[sa]);
+        if (ok) mma_commit_warp(&bar_a_empty[sa]);
+        if (++sa == AS) {
+          sa = 0;
+          aph ^= 1u;
+        }
       }
     }
   } else if (warp == 2 && !FOLD) {
