@@ -897,7 +897,11 @@ int query_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint32_t
              float *dDists, uint32_t ldo, cudaStream_t s) {
   pool_setup();
   const uint32_t nr = idx->nr, ld = idx->ld;
-  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(tc_query_tile(idx->tc.format), (1ull << 27) / nr));
+  // query batches of up to 2^29 (query, representative) pairs: the distances
+  // and the plan take ~10 bytes a pair (5 GB at most), and a larger batch puts
+  // more queries on each probed list (wider FP32 probe tiles, fuller tensor
+  // tiles, fewer launches)
+  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(tc_query_tile(idx->tc.format), (1ull << 29) / nr));
   TcQuery t;
   TRY(tc_setup(idx, mb, k, mode, false, t, s));
   CK(cudaMemsetAsync(t.stats.p, 0, 4 * sizeof(unsigned long long), s));
