@@ -455,8 +455,8 @@ int query_index(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint3
   const uint32_t kw = list_width_for(k);
   const uint32_t qtile = (uint32_t)search_query_tile(idx->dp, idx->tune_tq, kw);
   const int grid = search_grid(idx->metric, idx->dp, idx->tune_tq, kw);
-  // batch so the m x nr plan arrays stay near 2^27 entries
-  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 27) / nr));
+  // batch so the m x nr plan arrays stay near 2^29 entries (~10 bytes each)
+  const uint64_t mb = std::min<uint64_t>(m, std::max<uint64_t>(qtile, (1ull << 29) / nr));
   QueryBufs b;
   const uint64_t pair_cap = mb * nr;
   const uint64_t item_cap = item_capacity(idx, mb, qtile);

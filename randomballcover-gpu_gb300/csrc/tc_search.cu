@@ -671,8 +671,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
       const SearchItem item = a.items[it];
       const uint32_t slot = ai & 1, sa = ai % AS;
-      // the item's row states are read from global memory before the staging
-      // slot frees (their latency hides behind that wait), then written
+      // The query tiles' gather goes out first: it needs only the query rows
+      // and a free query stage, not the row-state slot, which frees only when
+      // the epilogue finishes the item before last.  Then the item's row
+      // states are read from global memory (their latency hides behind the
+      // slot's wait) and written.
       // lane l owns rows 4l..4l+3 of each query tile (one gather4 per tile and K block)
       int32_t rr[MT][4];
       float dqv[MT][4], qnv[MT][4];
@@ -684,6 +687,21 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t row = g * kBM + 4 * lane + j;
           rr[g][j] = row < item.nq ? (int32_t)a.qidx[item.q0 + row] : (int32_t)a.zero_row;
         }
+      long long t0 = tclk();
+      if (ai >= AS) ok = mbar_wait(&bar_a_empty[sa], ((ai / AS) - 1) & 1, a.err);
+      w3[1] += tclk() - t0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      {
+        unsigned char *dA = sA + sa * a_stage;
+        if (lane == 0) mbar_expect_tx(&bar_a_full[sa], a_stage);
+        __syncwarp();
+#pragma unroll
+        for (int g = 0; g < MT; g++)
+          for (uint32_t k = 0; k < kbh; k++)
+            tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
+                        rr[g][2], rr[g][3], &bar_a_full[sa]);
+      }
 #pragma unroll
       for (int g = 0; g < MT; g++)
 #pragma unroll
@@ -695,7 +713,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           qin[g][j] = v ? (a.q_inexact ? a.q_inexact[q] : 1u) : 0u;
         }
       const float X = a.lxmax[item.list], C = a.lcnorm[item.list];
-      long long t0 = tclk();
+      t0 = tclk();
       if (ai >= 2) ok = mbar_wait(&bar_r_empty[slot], ((ai >> 1) - 1) & 1, a.err);
       w3[0] += tclk() - t0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -726,19 +744,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       __syncwarp();
       if (lane == 0) mbar_arrive(&bar_r_full[slot]);
-      t0 = tclk();
-      if (ai >= AS) ok = mbar_wait(&bar_a_empty[sa], ((ai / AS) - 1) & 1, a.err);
-      w3[1] += tclk() - t0;
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      if (!ok) break;
-      unsigned char *dA = sA + sa * a_stage;
-      if (lane == 0) mbar_expect_tx(&bar_a_full[sa], a_stage);
-      __syncwarp();
-#pragma unroll
-      for (int g = 0; g < MT; g++)
-        for (uint32_t k = 0; k < kbh; k++)
-          tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
-                      rr[g][2], rr[g][3], &bar_a_full[sa]);
     }
     if (lane == 0 && a.trace) {
       a.trace[blockIdx.x * kTcTraceWords + 8] = w3[0];
