@@ -452,3 +452,35 @@ def test_tensor_core_representative_seed(rbc, oracle, case):
     ids2, dists2 = idx.query(Q, k)
     assert (ids2 == ids).all() and (dists2 == dists).all()
     idx.close()
+
+
+def test_probe_buffers_that_leave_out_tied_rows_fall_back_exactly(rbc, oracle, monkeypatch):
+    """The probe round's candidate buffers keep each query's best 16 rows of a
+    work item and bound the rows they leave out for the certificate.  Each of
+    the first 32 queries has 200 identical rows at squared distance 1 in its
+    probed list (the tensor cores take whole probed lists here), so its
+    buffer leaves out rows tied with the k-th distance: the certificate must
+    turn those queries to the FP32 path, which returns the lowest ids of the
+    tie, as the oracle does."""
+    import torch
+    rng = np.random.default_rng(11)
+    n, d, nr, m, k = 30000, 64, 64, 64, 10
+    Xn = rng.integers(0, 200, size=(n, d)).astype(np.float32)
+    Qn = rng.integers(0, 200, size=(m, d)).astype(np.float32)
+    planted = 32
+    for i in range(planted):
+        p = Qn[i].copy()
+        p[0] += 1.0
+        Xn[i * 200:(i + 1) * 200] = p
+    monkeypatch.setenv("RBC_TC_PROBE_ROWS", "0")
+    X = torch.from_numpy(Xn).cuda()
+    Q = torch.from_numpy(Qn).cuda()
+    idx = rbc.Index(X, nr, seed=3, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+    assert idx.info()["tc_format"] == rbc.TC_BF16
+    ids, dists = idx.query(Q, k, mode=rbc.QUERY_EXACT_TC)
+    ri, rd = oracle.knn(Xn, Qn, k)
+    assert_same(ids, dists, ri, rd, rbc)
+    fb = set(int(q) for q in idx.fallback_queries())
+    assert fb, "no query reached the FP32 path"
+    assert fb <= set(range(planted)), fb  # only the planted ties are left open
+    idx.close()
