@@ -454,7 +454,10 @@ def run_engine(a):
             else:
                 idx.autotune_tc(Qtune, k, mode)
             inf = idx.info()
-            tuning[mode] = list(idx.tc_tuning()) + (["plain FP32 search chosen"] if inf["tc_plain"] else [])
+            p_, r_ = idx.tc_tuning()
+            tuning[mode] = ["router picks only" if p_ == pyrbc.TC_ROUTER_ONLY else p_,
+                            "no FP32 prefix" if r_ == pyrbc.TC_PREFIX_NONE else r_]
+            tuning[mode] += ["plain FP32 search chosen"] if inf["tc_plain"] else []
             if mode & pyrbc.QUERY_ROUTED:
                 tuning[mode].append("router not consulted (the tuner measured the nearest lists alone faster)"
                                     if inf["tc_unrouted"] else f"router picks {inf['router_picks']}")

@@ -196,9 +196,10 @@ int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, ui
  * whose probe round then searches the router's picks alone, and one in
  * others) and how many rows of each probed list the FP32 path searches
  * first (whole lists when shorter; the rest of a longer list goes to the
- * tensor cores; 0 keeps the default, 8192).
+ * tensor cores; 0 keeps the default, 8192; RBC_TC_PREFIX_NONE: none, the
+ * tensor cores search whole probed lists).
  * rbc_autotune_tc times 1, 2, 4, 8 probes (and RBC_TC_ROUTER_ONLY in routed
- * mode) x 2048, 8192, 32768 rows on sample
+ * mode) x RBC_TC_PREFIX_NONE, 512, 2048, 8192, 32768 rows on sample
  * queries in the given mode (RBC_QUERY_EXACT_TC, optionally
  * | RBC_QUERY_ROUTED, where it also tries one and two router picks, and the
  * nearest lists without the router, when the router was attached with picks;
@@ -209,6 +210,7 @@ int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, ui
  * rbc_set_tc_tuning selects the tensor form, routed as asked, again; so does
  * attaching a router.  Results never change. */
 #define RBC_TC_ROUTER_ONLY 0xFFu
+#define RBC_TC_PREFIX_NONE 0xFFFFFFFFFFFFFFFFull
 int rbc_set_tc_tuning(rbc_index *index, uint32_t probes, uint64_t probe_rows);
 int rbc_get_tc_tuning(const rbc_index *index, uint32_t *probes, uint64_t *probe_rows);
 int rbc_autotune_tc(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,

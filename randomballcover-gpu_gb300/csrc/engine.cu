@@ -600,7 +600,7 @@ int tc_setup(rbc_index *idx, uint64_t mb, uint32_t k, uint32_t mode, bool graph,
   // follow the probed queries per list (16 wide when few share a list)
   t.sl = tc_shortlist(k);
   t.kw = list_width_for(t.sl);
-  t.probe_rows = idx->tc_probe_rows ? idx->tc_probe_rows : kTcProbeRows;
+  t.probe_rows = idx->tc_probe_rows == RBC_TC_PREFIX_NONE ? 0 : idx->tc_probe_rows ? idx->tc_probe_rows : kTcProbeRows;
   if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) t.probe_rows = std::strtoull(env, nullptr, 10);
   t.qtile = tc_query_tile(idx->tc.format);
   const uint64_t probe_per_list = mb * t.P / nr;

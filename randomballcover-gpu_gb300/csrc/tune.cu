@@ -185,7 +185,7 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
     idx->tc_unrouted = unrouted;
     for (uint32_t p : {RBC_TC_ROUTER_ONLY, 1u, 2u, 4u, 8u}) {
       if (p == RBC_TC_ROUTER_ONLY && (!routed || unrouted)) continue;  // the router's picks alone: routed calls only
-      for (uint64_t r : {2048ull, 8192ull, 32768ull}) {
+      for (uint64_t r : {RBC_TC_PREFIX_NONE, 512ull, 2048ull, 8192ull, 32768ull}) {
         idx->tc_probes = p;
         idx->tc_probe_rows = r;
         double ms_min = 1e30;

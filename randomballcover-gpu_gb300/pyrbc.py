@@ -22,6 +22,7 @@ BUILD_PARTITION, BUILD_ONESHOT, BUILD_BF16, BUILD_F64 = 1, 2, 4, 8
 QUERY_EXACT, QUERY_ONESHOT, QUERY_EXACT_TC = 0, 1, 2
 TC_BF16, TC_FP16_SPLIT = 0, 1
 TC_ROUTER_ONLY = 0xFF  # tensor-form probes: the router's picks alone (routed calls)
+TC_PREFIX_NONE = 0xFFFFFFFFFFFFFFFF  # tensor-form probe rows: no FP32 prefix, the tensor cores take whole lists
 QUERY_ROUTED = 0x1000
 SYNTH_UNIFORM, SYNTH_MIXTURE, SYNTH_GEOMETRIC = 0, 1, 2
 DUMMY = 0xFFFFFFFF

@@ -386,11 +386,14 @@ def test_tensor_core_autotune(rbc, oracle):
     assert idx.tc_tuning() == (0, 0)
     idx.autotune_tc(Qt, 10)
     p, r = idx.tc_tuning()
-    assert p in (1, 2, 4, 8) and r in (2048, 8192, 32768)
+    assert p in (1, 2, 4, 8) and r in (rbc.TC_PREFIX_NONE, 512, 2048, 8192, 32768)
     ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
     ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), 10)
     assert_same(ids, dists, ri, rd, rbc)
-    idx.set_tc_tuning(1, 100)  # manual setting, then back to the defaults
+    idx.set_tc_tuning(1, 100)  # manual settings, then back to the defaults
+    ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
+    assert_same(ids, dists, ri, rd, rbc)
+    idx.set_tc_tuning(2, rbc.TC_PREFIX_NONE)  # no FP32 prefix: whole probed lists on the tensor cores
     ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
     assert_same(ids, dists, ri, rd, rbc)
     idx.set_tc_tuning()
