@@ -820,8 +820,16 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
     ListFilter large;  // the rest of the longer lists
     large.rows_lo = t.probe_rows + 1;
     large.skip = t.probe_rows;
-    TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, t.sgrid, nullptr, s, 1, -1,
-                        tc_query_tile(kTcSplit), large));
+    // items twice the index's row run: each query's buffers merge once per
+    // item, and the probed lists' few queries leave the launch short of work
+    // items anyway (c3: 16,384 / 32,768 / 65,536 / 131,072 rows gave a 5.16 /
+    // 4.48 / 4.91 / 5.09 ms probe launch; whole lists 10.2 ms)
+    const uint32_t keep_rows = idx->item_rows;
+    idx->item_rows = (uint32_t)std::min<uint64_t>(2ull * keep_rows, 1u << 30);
+    const int prc = plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, t.sgrid,
+                                    nullptr, s, 1, -1, tc_query_tile(kTcSplit), large);
+    idx->item_rows = keep_rows;
+    TRY(prc);
     // the probe round's candidate buffers keep each query's best and merge
     // once per item (its lists hold few queries, many of them busy hubs,
     // where merges per buffer-full queued on the queries' locks: c3 probe
