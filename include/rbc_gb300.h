@@ -168,9 +168,12 @@ int rbc_get_fallback_queries(const rbc_index *index, uint32_t *h_ids, uint64_t c
  * Instances (index, device queries, k, outputs) are added, then rbc_batch_run
  * answers all of them exactly: each round plans every FP32 instance, then
  * one persistent search launch serves all their work; tensor-form instances
- * (rbc_batch_add_mode with RBC_QUERY_EXACT_TC, BF16 indexes, k <= 32) each
- * run their rounds on the tensor cores, the queries their certificate
- * leaves open searched again on the device.  The first run captures the
+ * (rbc_batch_add_mode with RBC_QUERY_EXACT_TC, BF16 indexes, k <= 32) run
+ * their rounds on the tensor cores the same way, one tensor-search launch
+ * per round in which each instance owns a range of CTAs, the queries their
+ * certificates leave open searched again on the device (an instance whose
+ * index the autotuner set to the plain search, info.tc_plain, runs with the
+ * FP32 instances).  The first run captures the
  * whole sequence into a CUDA graph; later runs replay it, so new query
  * values written into the same buffers are answered by one graph launch.
  * Instances must share the metric; m x num_reps <= 2^28 each. */

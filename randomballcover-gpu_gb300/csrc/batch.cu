@@ -6,9 +6,11 @@
 // (probe, then pruned) plans every instance (small kernels), concatenates all
 // instances' work items into one queue tagged with the instance, and runs a
 // single persistent list-search launch over the queue: the kernel reads the
-// instance's database, queries, lists and results from a device table.  The
-// captured graph replays the rounds for new query values in the same
-// buffers.  The reference runs one (database, query set) per call with a
+// instance's database, queries, lists and results from a device table.
+// Tensor-form instances run their three rounds the same way, their tensor
+// searches one grid per round in which each instance owns a range of CTAs
+// and its tensor maps come from the table.  The captured graph replays the
+// rounds for new query values in the same buffers.  The reference runs one (database, query set) per call with a
 // host round trip between every kernel (rbc.cu:72-123).
 #include <algorithm>
 #include <memory>
@@ -21,7 +23,10 @@ namespace rbc {
 
 namespace {
 
-__global__ void batch_offsets_kernel(uint32_t *const *counts, uint32_t ninst, uint32_t *offsets, uint32_t *total) {
+// The instances' item offsets in the concatenated queue, its length, and the
+// search's work counter zeroed.
+__global__ void batch_offsets_kernel(uint32_t *const *counts, uint32_t ninst, uint32_t *offsets, uint32_t *total,
+                                     uint32_t *work) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   uint32_t s = 0;
   for (uint32_t i = 0; i < ninst; i++) {
@@ -29,6 +34,7 @@ __global__ void batch_offsets_kernel(uint32_t *const *counts, uint32_t ninst, ui
     s += *counts[i];
   }
   *total = s;
+  *work = 0;
 }
 
 __global__ void batch_concat_kernel(const SearchItem *const *src, uint32_t *const *counts, const uint32_t *offsets,
@@ -66,13 +72,12 @@ struct BatchInstance {
   float *dists;
   QueryBufs b;
   std::unique_ptr<TcQuery> tc;  // the tensor form's buffers (RBC_QUERY_EXACT_TC)
+  DevBuf fb_items, fb_ctl;      // tensor form: the batched device fallback's items and control words
 };
 
 struct rbc_batch {
   std::vector<std::unique_ptr<BatchInstance>> inst;
   std::vector<void *> owned;
-  std::vector<cudaStream_t> branch;  // capture-time side streams (tensor-form instances)
-  std::vector<cudaEvent_t> marks;
   bool ready = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -88,8 +93,6 @@ struct rbc_batch {
       cudaStreamDestroy(cap);
     }
     for (void *p : owned) cudaFree(p);
-    for (cudaStream_t b : branch) cudaStreamDestroy(b);
-    for (cudaEvent_t e : marks) cudaEventDestroy(e);
   }
 };
 
@@ -106,16 +109,446 @@ namespace {
     if (rc_ != RBC_OK) return rc_;  \
   } while (0)
 
+template <typename T>
+T *to_dev(const std::vector<T> &v, std::vector<void *> &owned) {
+  T *d = dalloc<T>(v.size(), owned);
+  if (d && !v.empty() && cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    return nullptr;
+  return d;
+}
+
+// The tensor-form instances of a batch.  Each step of their query -- set-up,
+// the probe round on the FP32 path (the first rows of the probed lists) and
+// on the tensor cores (the rest), the pruned round, both reranks and the
+// device fallback for uncertified queries -- is one launch over a device
+// table of per-instance arguments; the FP32 searches run over the
+// instances' concatenated work items, the tensor searches over per-instance
+// CTA ranges of one grid per operand format.
+struct TcTables {
+  uint32_t T = 0;
+  uint64_t m_max = 0, elems_max = 0, mkw_max = 0;
+  uint32_t nr_max = 0, P_max = 0, dp_max = 0;
+  BatchQuery *pad = nullptr;
+  std::vector<std::pair<uint32_t, uint32_t>> dkeys;  // (ld, dp) of each distance group
+  std::vector<std::vector<DenseInst>> dgroups;
+  std::vector<DenseInst *> ddev;
+  TcPrepArgs *prep = nullptr;
+  BatchPlan *plan[3] = {};  // FP32 probe round, tensor probe round, pruned round
+  bool fp_probe = false, tc_probe = false;
+  SearchArgs *sp = nullptr, *sf = nullptr;  // the FP32 searches: probe round, fallback
+  SearchItem **src_p = nullptr, **src_f = nullptr;
+  uint32_t **cnt_p = nullptr, **cnt_f = nullptr;
+  uint32_t *offs = nullptr;
+  SearchItem *all = nullptr;
+  int tq_p = 1, grid_p = 1, tq_f = 1, grid_f = 1;
+  SlSeedArgs *seed = nullptr;
+  struct Launch {
+    TcBatchEntry *tab;
+    uint32_t n, ctas, format;
+    size_t smem;
+  };
+  std::vector<Launch> tc[2];  // probe round (one query tile per B tile), pruned round
+  RerankArgs *rr[2] = {};
+  ListedArgs *listed = nullptr;
+  ErrWords *errs = nullptr;
+};
+
+int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStream_t s, TcTables &x) {
+  const uint32_t T = x.T = (uint32_t)tcv.size();
+  if (!T) return RBC_OK;
+  const int metric = tcv[0]->idx->metric;
+  constexpr uint32_t kwp = 64, kwf = 32;  // list widths: shortlists (40-56 rows), results (k <= 32)
+  int tq_p = 4, tq_f = 4;
+  for (BatchInstance *ip : tcv) {
+    ip->tc = std::make_unique<TcQuery>();
+    BTRY(tc_setup(ip->idx, ip->m, ip->k, RBC_QUERY_EXACT_TC, false, *ip->tc, s));
+    if (ip->tc->kw != kwp) return fail(RBC_ERR_UNSUPPORTED, "rbc_batch_run: tensor shortlist wider than 64");
+    x.dp_max = std::max(x.dp_max, ip->idx->dp);
+    tq_p = std::min(tq_p, search_tq_for(ip->idx->dp, ip->tc->ptq, kwp));
+    tq_f = std::min(tq_f, search_tq_for(ip->idx->dp, 0, kwf));
+  }
+  // the shared FP32 launches: one tile geometry, the one the widest rows allow
+  x.tq_p = search_tq_for(x.dp_max, tq_p, kwp);
+  x.tq_f = search_tq_for(x.dp_max, tq_f, kwf);
+  x.grid_p = search_grid(metric, x.dp_max, x.tq_p, kwp);
+  x.grid_f = search_grid(metric, x.dp_max, x.tq_f, kwf);
+  const uint32_t qtile_p = 16 * x.tq_p, qtile_f = 16 * x.tq_f;
+
+  std::vector<BatchQuery> pad(T);
+  std::vector<TcPrepArgs> prep(T);
+  std::vector<BatchPlan> plan[3] = {std::vector<BatchPlan>(T), std::vector<BatchPlan>(T), std::vector<BatchPlan>(T)};
+  std::vector<SearchArgs> sp(T), sf(T);
+  std::vector<SearchItem *> src_p(T), src_f(T);
+  std::vector<uint32_t *> cnt_p(T), cnt_f(T);
+  std::vector<SlSeedArgs> seed(T);
+  std::vector<RerankArgs> rr[2] = {std::vector<RerankArgs>(T), std::vector<RerankArgs>(T)};
+  std::vector<ListedArgs> listed(T);
+  std::vector<ErrWords> errs(T);
+  std::vector<TcBatchEntry> ent[2] = {std::vector<TcBatchEntry>(T), std::vector<TcBatchEntry>(T)};
+  std::vector<size_t> smem[2] = {std::vector<size_t>(T), std::vector<size_t>(T)};
+  std::vector<double> weight(T);
+  std::vector<bool> probes(T);
+  uint64_t all_p = 0, all_f = 0;
+  for (uint32_t i = 0; i < T; i++) {
+    BatchInstance &in = *tcv[i];
+    rbc_index *idx = in.idx;
+    TcQuery &t = *in.tc;
+    QueryBufs &b = t.b;
+    const uint64_t mq = in.m;
+    const uint32_t ld = idx->ld, fmt = idx->tc.format;
+    x.m_max = std::max(x.m_max, mq);
+    x.nr_max = std::max(x.nr_max, idx->nr);
+    x.P_max = std::max(x.P_max, t.P);
+    x.elems_max = std::max<uint64_t>(x.elems_max, mq * ld);
+    x.mkw_max = std::max<uint64_t>(x.mkw_max, mq * kwf);
+    BatchQuery q{};
+    q.Q = in.Q;
+    q.ldq = in.ldq;
+    q.m = mq;
+    q.Qp = b.Qp.as<float>();
+    q.ld = ld;
+    q.d = idx->d;
+    pad[i] = q;
+    const std::pair<uint32_t, uint32_t> key(ld, idx->dp);
+    size_t g = std::find(x.dkeys.begin(), x.dkeys.end(), key) - x.dkeys.begin();
+    if (g == x.dkeys.size()) {
+      x.dkeys.push_back(key);
+      x.dgroups.emplace_back();
+    }
+    x.dgroups[g].push_back(DenseInst{b.Qp.as<float>(), mq, idx->R, idx->nr, b.Dqr.as<float>(), idx->nr});
+    // the device fallback: every (row chunk, listed query tile) pair for as
+    // many queries as the instance holds
+    uint32_t chunk = (uint32_t)std::max<uint64_t>(4096, (idx->n + 4ull * x.grid_f - 1) / (4ull * x.grid_f));
+    chunk = (chunk + 31) / 32 * 32;
+    const uint64_t fcap = ((idx->n + chunk - 1) / chunk) * ((mq + qtile_f - 1) / qtile_f);
+    BCK(in.fb_items.alloc(std::max<uint64_t>(fcap, 1) * sizeof(SearchItem), s));
+    BCK(in.fb_ctl.alloc(64, s));
+    uint32_t *fctl = in.fb_ctl.as<uint32_t>();
+    all_f += fcap;
+
+    TcPrepArgs pa{};
+    pa.Dqr = b.Dqr.as<float>();
+    pa.m = mq;
+    pa.nr = idx->nr;
+    pa.sl = t.sl;
+    pa.P = t.P;
+    pa.rep_rows = idx->tc.rep_rows;
+    pa.seed_a = t.seed_a.as<float>();
+    pa.seed_row = t.seed_row.as<uint32_t>();
+    pa.probe = b.probe.as<uint32_t>();
+    pa.probed = b.probed.as<float>();
+    pa.Qp = b.Qp.as<float>();
+    pa.ld = ld;
+    pa.d = idx->d;
+    pa.kp = idx->kp;
+    pa.format = fmt;
+    pa.mu = idx->tc.mu;
+    pa.Qh = t.Qh.as<uint16_t>();
+    pa.qscale = t.qscale.as<float>();
+    pa.qnorm = t.qnorm.as<float>();
+    pa.qinex = t.qinex.as<uint8_t>();
+    pa.sl_a = t.sl_a.as<float>();
+    pa.sl_row = t.sl_row.as<uint32_t>();
+    pa.sl_sel = t.sl_sel.as<uint32_t>();
+    pa.sl_theta = t.sl_theta.as<uint32_t>();
+    pa.sl_lock = t.sl_lock.as<uint32_t>();
+    pa.emax = t.emax.as<uint32_t>();
+    pa.drop = t.drop.as<uint32_t>();
+    pa.res_d = b.res_d.as<float>();
+    pa.res_i = b.res_i.as<uint32_t>();
+    pa.tau = b.tau.as<uint32_t>();
+    pa.lock = b.lock.as<uint32_t>();
+    pa.kw = t.kw;
+    pa.ctl[0] = b.ctl.as<uint32_t>();
+    pa.ctl[1] = t.ctl.as<uint32_t>();
+    pa.ctl[2] = fctl;
+    pa.stats = t.stats.as<unsigned long long>();
+    prep[i] = pa;
+
+    // the three plan rounds, as tc_enqueue plans them
+    probes[i] = idx->max_list > t.probe_rows;
+    x.fp_probe |= t.probe_rows > 0;
+    x.tc_probe |= probes[i];
+    for (int r = 0; r < 3; r++) {
+      BatchPlan bp{};
+      bp.qtile = r == 0 ? qtile_p : (r == 1 ? tc_query_tile(kTcSplit) : t.qtile);
+      fill_plan_args(idx, b, mq, t.P, bp.qtile, idx->offsets, idx->radius, bp.a);
+      bp.cnt = b.cnt.as<uint32_t>();
+      bp.start = b.start.as<uint32_t>();
+      bp.cursor = b.cursor.as<uint32_t>();
+      bp.tcnt = b.tcnt.as<uint32_t>();
+      bp.tstart = b.tstart.as<uint32_t>();
+      bp.max_rows = r == 1 ? (uint32_t)std::min<uint64_t>(2ull * idx->item_rows, 1u << 30) : idx->item_rows;
+      bp.items = b.items.as<SearchItem>();
+      bp.cap = b.item_cap;
+      bp.nitems = b.ctl.as<uint32_t>() + 1;
+      bp.err = b.ctl.as<uint32_t>() + 2;
+      if (r == 0) bp.f.take = t.probe_rows;
+      if (r == 1) {
+        bp.f.rows_lo = t.probe_rows + 1;
+        bp.f.skip = t.probe_rows;
+      }
+      plan[r][i] = bp;
+    }
+    all_p += item_capacity(idx, mq, qtile_p, t.P);
+
+    SearchArgs a{};
+    a.X = idx->Xp;
+    a.pid = idx->perm;
+    a.Q = b.Qp.as<float>();
+    a.qidx = b.pair_q.as<uint32_t>();
+    a.res_d = b.res_d.as<float>();
+    a.res_i = b.res_i.as<uint32_t>();
+    a.tau = b.tau.as<uint32_t>();
+    a.lock = b.lock.as<uint32_t>();
+    a.ld = ld;
+    a.dp = idx->dp;
+    a.k = t.sl;
+    sp[i] = a;
+    a.qidx = t.failq.as<uint32_t>();
+    a.k = in.k;
+    sf[i] = a;
+    src_p[i] = b.items.as<SearchItem>();
+    cnt_p[i] = b.ctl.as<uint32_t>() + 1;
+    src_f[i] = in.fb_items.as<SearchItem>();
+    cnt_f[i] = fctl + 1;
+    SlSeedArgs sa{};
+    sa.res_d = b.res_d.as<float>();
+    sa.res_i = b.res_i.as<uint32_t>();
+    sa.kw = t.kw;
+    sa.iperm = idx->tc.iperm;
+    sa.seed_a = t.seed_a.as<float>();
+    sa.seed_row = t.seed_row.as<uint32_t>();
+    sa.m = mq;
+    sa.sl = t.sl;
+    sa.k = in.k;
+    sa.sl_a = t.sl_a.as<float>();
+    sa.sl_row = t.sl_row.as<uint32_t>();
+    sa.theta = t.sl_theta.as<uint32_t>();
+    sa.tau = b.tau.as<uint32_t>();
+    seed[i] = sa;
+
+    TcArgs ta{};
+    ta.items = b.items.as<SearchItem>();
+    ta.nitems = b.ctl.as<uint32_t>() + 1;
+    ta.qidx = b.pair_q.as<uint32_t>();
+    ta.Dqr = b.Dqr.as<float>();
+    ta.nr = idx->nr;
+    ta.kb = idx->kp / 64;
+    ta.zero_row = (uint32_t)mq;
+    ta.d = idx->d;
+    ta.w = idx->tc.w;
+    ta.wh = static_cast<const uint4 *>(idx->tc.Wh);
+    ta.lscale = idx->tc.lscale;
+    ta.lxmax = idx->tc.lxmax;
+    ta.lcnorm = idx->tc.lcnorm;
+    ta.qscale = t.qscale.as<float>();
+    ta.qnorm = t.qnorm.as<float>();
+    ta.q_inexact = t.qinex.as<uint8_t>();
+    ta.x_inexact = idx->tc.x_inexact;
+    ta.format = fmt;
+    ta.sl = t.sl;
+    ta.sl_a = t.sl_a.as<float>();
+    ta.sl_row = t.sl_row.as<uint32_t>();
+    ta.sl_sel = t.sl_sel.as<uint32_t>();
+    ta.sl_theta = t.sl_theta.as<uint32_t>();
+    ta.drop = t.drop.as<uint32_t>();
+    ta.sl_lock = t.sl_lock.as<uint32_t>();
+    ta.emax = t.emax.as<uint32_t>();
+    ta.m = mq;
+    ta.offsets = idx->offsets;
+    ta.stats = t.stats.as<unsigned long long>();
+    ta.err = t.ctl.as<uint32_t>();
+    TcArgs tp = ta;
+    tp.stats = ta.stats + 2;
+    tp.keep_k = in.k;
+    TcBatchEntry e{};
+    BCK(tc_make_map(&e.tmA, t.Qh.p, mq + 1, idx->tc.cols, 1));
+    e.tmB = idx->tmB;
+    e.a = tp;
+    smem[0][i] = tc_stage_plan(e.a, true);
+    ent[0][i] = e;
+    e.a = ta;
+    smem[1][i] = tc_stage_plan(e.a, false);
+    ent[1][i] = e;
+    if (!smem[0][i] || !smem[1][i]) return fail(RBC_ERR_UNSUPPORTED, "rbc_batch_run: no shared-memory plan fits");
+    weight[i] = (double)mq * (double)idx->n * (double)ta.kb * (fmt == kTcSplit ? 2.0 : 1.0);
+
+    RerankArgs ra{};
+    ra.X = idx->Xp;
+    ra.pid = idx->perm;
+    ra.Q = b.Qp.as<float>();
+    ra.ld = ld;
+    ra.dp = idx->dp;
+    ra.k = in.k;
+    ra.sl = t.sl;
+    ra.m = mq;
+    ra.sl_a = t.sl_a.as<float>();
+    ra.sl_row = t.sl_row.as<uint32_t>();
+    ra.sl_sel = t.sl_sel.as<uint32_t>();
+    ra.emax = t.emax.as<uint32_t>();
+    ra.drop = t.drop.as<uint32_t>();
+    ra.ldo = in.ldo;
+    ra.nfail = t.ctl.as<uint32_t>() + 1;
+    ra.fail = t.failq.as<uint32_t>();
+    RerankArgs r0 = ra;
+    r0.tau = b.tau.as<uint32_t>();
+    if (!probes[i]) r0.m = 0;  // no tensor probe round: its threshold update does not run either
+    rr[0][i] = r0;
+    ra.ids = in.ids;
+    ra.dists = in.dists;
+    rr[1][i] = ra;
+
+    ListedArgs la{};
+    la.res_d = b.res_d.as<float>();
+    la.res_i = b.res_i.as<uint32_t>();
+    la.tau = b.tau.as<uint32_t>();
+    la.lock = b.lock.as<uint32_t>();
+    la.m = mq;
+    la.kw = kwf;
+    la.ctl = fctl;
+    la.items = in.fb_items.as<SearchItem>();
+    la.n = idx->n;
+    la.cap = fcap;
+    la.chunk = chunk;
+    la.qtile = qtile_f;
+    la.rows = t.failq.as<uint32_t>();
+    la.count = t.ctl.as<uint32_t>() + 1;
+    la.k = in.k;
+    la.ldo = in.ldo;
+    la.ids = in.ids;
+    la.dists = in.dists;
+    listed[i] = la;
+    errs[i] = ErrWords{{t.ctl.as<uint32_t>(), b.ctl.as<uint32_t>() + 2, fctl + 2, nullptr}};
+  }
+  BCK(cudaStreamSynchronize(s));
+  std::vector<void *> &o = bt->owned;
+  x.pad = to_dev(pad, o);
+  x.prep = to_dev(prep, o);
+  for (int r = 0; r < 3; r++) x.plan[r] = to_dev(plan[r], o);
+  x.sp = to_dev(sp, o);
+  x.sf = to_dev(sf, o);
+  x.src_p = to_dev(src_p, o);
+  x.src_f = to_dev(src_f, o);
+  x.cnt_p = to_dev(cnt_p, o);
+  x.cnt_f = to_dev(cnt_f, o);
+  x.offs = dalloc<uint32_t>(T, o);
+  x.all = dalloc<SearchItem>(std::max(x.fp_probe ? all_p : 0, all_f), o);
+  x.seed = to_dev(seed, o);
+  x.rr[0] = to_dev(rr[0], o);
+  x.rr[1] = to_dev(rr[1], o);
+  x.listed = to_dev(listed, o);
+  x.errs = to_dev(errs, o);
+  if (!x.pad || !x.prep || !x.plan[0] || !x.plan[1] || !x.plan[2] || !x.sp || !x.sf || !x.src_p || !x.src_f ||
+      !x.cnt_p || !x.cnt_f || !x.offs || !x.all || !x.seed || !x.rr[0] || !x.rr[1] || !x.listed || !x.errs)
+    return fail(RBC_ERR_NOMEM, "rbc_batch_run: device allocation failed");
+  for (const auto &gr : x.dgroups) {
+    x.ddev.push_back(to_dev(gr, o));
+    if (!x.ddev.back()) return fail(RBC_ERR_NOMEM, "rbc_batch_run: device allocation failed");
+  }
+  // the tensor searches: per round and operand format one grid, each
+  // instance a CTA range sized by its share of the work (about two waves in
+  // all), the largest first
+  const uint32_t sms = (uint32_t)tc_grid();
+  for (int r = 0; r < 2; r++)
+    for (uint32_t fmt : {(uint32_t)kTcExact, (uint32_t)kTcSplit}) {
+      std::vector<uint32_t> mem;
+      double wsum = 0;
+      for (uint32_t i = 0; i < T; i++)
+        if (tcv[i]->idx->tc.format == fmt && (r == 1 || probes[i])) {
+          mem.push_back(i);
+          wsum += weight[i];
+        }
+      if (mem.empty()) continue;
+      std::stable_sort(mem.begin(), mem.end(), [&](uint32_t a, uint32_t b) { return weight[a] > weight[b]; });
+      std::vector<TcBatchEntry> tab;
+      uint32_t cta = 0;
+      size_t sm = 0;
+      for (uint32_t i : mem) {
+        TcBatchEntry e = ent[r][i];
+        const double share = wsum > 0 ? weight[i] / wsum : 1.0;
+        e.ctas = (uint32_t)std::min<double>(sms, std::max(1.0, std::ceil(2.0 * sms * share)));
+        e.cta0 = cta;
+        cta += e.ctas;
+        sm = std::max(sm, smem[r][i]);
+        tab.push_back(e);
+      }
+      TcBatchEntry *d = to_dev(tab, o);
+      if (!d) return fail(RBC_ERR_NOMEM, "rbc_batch_run: device allocation failed");
+      x.tc[r].push_back(TcTables::Launch{d, (uint32_t)tab.size(), cta, fmt, sm});
+    }
+  return RBC_OK;
+}
+
+// Record the tensor-form instances' query (see TcTables) on stream s.
+int capture_tc(const TcTables &x, int metric, uint32_t *ctl, cudaStream_t s) {
+  const uint32_t T = x.T;
+  if (!T) return RBC_OK;
+  BCK(launch_batch_pad(x.pad, T, x.elems_max, s));
+  for (size_t gi = 0; gi < x.dgroups.size(); gi++) {
+    uint64_t na = 0, nb = 0;
+    for (const DenseInst &di : x.dgroups[gi]) {
+      na = std::max(na, di.na);
+      nb = std::max(nb, di.nb);
+    }
+    BCK(launch_dense_dist_batch(metric, x.ddev[gi], (uint32_t)x.dgroups[gi].size(), na, nb, x.dkeys[gi].first,
+                                x.dkeys[gi].second, s));
+  }
+  BCK(launch_tc_prep_batch(x.prep, T, x.m_max, s));
+  SearchArgs g{};
+  g.items = x.all;
+  g.nitems = ctl + 1;
+  g.work = ctl;
+  g.err = ctl + 2;
+  g.dp = x.dp_max;  // sizes the shared-memory tile of the shared launches
+  if (x.fp_probe) {
+    BCK(launch_plan_batch(x.plan[0], T, 0, x.nr_max, x.m_max, x.P_max, s));
+    batch_offsets_kernel<<<1, 1, 0, s>>>(x.cnt_p, T, x.offs, ctl + 1, ctl);
+    BCK(launched());
+    batch_concat_kernel<<<dim3(64, T), 256, 0, s>>>(x.src_p, x.cnt_p, x.offs, x.all);
+    BCK(launched());
+    g.insts = x.sp;
+    g.k = 64;  // shortlist-wide lists
+    BCK(launch_search(metric, g, x.grid_p, s, x.tq_p));
+  }
+  BCK(launch_sl_seed_batch(x.seed, T, x.m_max, s));
+  if (x.tc_probe) {
+    BCK(launch_plan_batch(x.plan[1], T, 0, x.nr_max, x.m_max, x.P_max, s));
+    for (const auto &L : x.tc[0]) BCK(launch_tc_search_batch(L.tab, L.n, L.ctas, L.format, true, L.smem, s));
+    BCK(launch_rerank_batch(metric, x.rr[0], T, x.m_max, s));
+  }
+  BCK(launch_plan_batch(x.plan[2], T, 1, x.nr_max, x.m_max, x.P_max, s));
+  for (const auto &L : x.tc[1]) BCK(launch_tc_search_batch(L.tab, L.n, L.ctas, L.format, false, L.smem, s));
+  BCK(launch_rerank_batch(metric, x.rr[1], T, x.m_max, s));
+  // the uncertified queries (their count on the device) searched again over
+  // every row on the FP32 path, their answers written over the tensor form's
+  BCK(launch_listed_init_batch(x.listed, T, x.mkw_max, s));
+  BCK(launch_listed_items_batch(x.listed, T, s));
+  batch_offsets_kernel<<<1, 1, 0, s>>>(x.cnt_f, T, x.offs, ctl + 1, ctl);
+  BCK(launched());
+  batch_concat_kernel<<<dim3(64, T), 256, 0, s>>>(x.src_f, x.cnt_f, x.offs, x.all);
+  BCK(launched());
+  g.insts = x.sf;
+  g.k = 32;
+  BCK(launch_search(metric, g, x.grid_f, s, x.tq_f));
+  BCK(launch_listed_results_batch(x.listed, T, s));
+  BCK(launch_fold_errors_batch(x.errs, T, ctl + 2, s));
+  return RBC_OK;
+}
+
 // Allocate every buffer, then record the whole sequence on a capture stream
 // into a graph: the FP32 instances' set-up (one launch each for the padded
 // queries, the nearest representatives and empty results, one distance launch
 // per padded dimension), their two rounds (each one batched plan round and
 // one persistent search launch over all of them) and their write-back; then
-// every tensor-form instance's round (its uncertified queries searched again
-// on the device), those on parallel branches.
+// the tensor-form instances' rounds, each step one launch over all of them
+// (TcTables).
 int prepare(rbc_batch *bt) {
+  // a tensor-form instance whose index the autotuner set to the plain search
+  // (rbc_index_info.tc_plain) joins the FP32 instances, as its single query
+  // call would run the FP32 search
   std::vector<BatchInstance *> fp, tcv;
-  for (auto &ip : bt->inst) (ip->mode == RBC_QUERY_EXACT_TC ? tcv : fp).push_back(ip.get());
+  for (auto &ip : bt->inst) (ip->mode == RBC_QUERY_EXACT_TC && !ip->idx->tc_plain ? tcv : fp).push_back(ip.get());
   const uint32_t N = (uint32_t)fp.size();
   const int metric = bt->inst[0]->idx->metric;
   // one tile geometry for the shared launch: the smallest query tile any instance needs
@@ -239,32 +672,8 @@ int prepare(rbc_batch *bt) {
     elems_max = std::max<uint64_t>(elems_max, in.m * idx->ld);
     mk_max = std::max<uint64_t>(mk_max, in.m * in.k);
   }
-  for (BatchInstance *ip : tcv) {
-    ip->tc = std::make_unique<TcQuery>();
-    BTRY(tc_setup(ip->idx, ip->m, ip->k, RBC_QUERY_EXACT_TC, true, *ip->tc, s));
-  }
-  // The tensor-form instances are captured on side streams forked from the
-  // capture stream and joined back, so the graph holds them as parallel
-  // branches instead of running them in turn.  The instances of one index
-  // share a branch (its router's scratch is the index's); distinct indexes go
-  // round the branches.
-  const uint32_t nbranch = (uint32_t)std::min<size_t>(tcv.size(), 8);
-  for (uint32_t i = 0; i < nbranch; i++) {
-    cudaStream_t b;
-    BCK(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking));
-    bt->branch.push_back(b);
-  }
-  for (size_t i = 0; i < 3 * (nbranch + 1); i++) {
-    cudaEvent_t e;
-    BCK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    bt->marks.push_back(e);
-  }
-  std::vector<std::pair<rbc_index *, cudaStream_t>> lanes;
-  auto lane_of = [&](rbc_index *idx) {
-    auto it = std::find_if(lanes.begin(), lanes.end(), [&](const auto &e) { return e.first == idx; });
-    if (it == lanes.end()) it = lanes.insert(lanes.end(), {idx, bt->branch[lanes.size() % nbranch]});
-    return it->second;
-  };
+  TcTables tx;
+  BTRY(prepare_tc(bt, tcv, s, tx));
   BCK(cudaStreamSynchronize(s));
   SearchArgs *t0 = dalloc<SearchArgs>(N, bt->owned), *t1 = dalloc<SearchArgs>(N, bt->owned);
   SearchItem **dsrc = dalloc<SearchItem *>(N, bt->owned);
@@ -303,21 +712,6 @@ int prepare(rbc_batch *bt) {
   const unsigned long long l0 = g_kernel_launches.load();
   BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int rc = RBC_OK;
-  cudaEvent_t *mark = bt->marks.data();
-  auto fork = [&]() -> int {
-    BCK(cudaEventRecord(*mark, s));
-    for (cudaStream_t b : bt->branch) BCK(cudaStreamWaitEvent(b, *mark, 0));
-    mark++;
-    return RBC_OK;
-  };
-  auto join = [&]() -> int {
-    for (cudaStream_t b : bt->branch) {
-      BCK(cudaEventRecord(*mark, b));
-      BCK(cudaStreamWaitEvent(s, *mark, 0));
-      mark++;
-    }
-    return RBC_OK;
-  };
   auto capture = [&]() -> int {
     BCK(cudaMemsetAsync(bt->ctl, 0, 64, s));
     if (N) {
@@ -335,23 +729,16 @@ int prepare(rbc_batch *bt) {
     }
     for (uint32_t round = 0; round < 2 && N; round++) {
       BCK(launch_plan_batch(dp_tab, N, round, nr_max, m_max, 1, s));
-      batch_offsets_kernel<<<1, 1, 0, s>>>(dcnt, N, offs, bt->ctl + 1);
+      batch_offsets_kernel<<<1, 1, 0, s>>>(dcnt, N, offs, bt->ctl + 1, bt->ctl);
       BCK(launched());
       batch_concat_kernel<<<dim3(64, N), 256, 0, s>>>(dsrc, dcnt, offs, all);
       BCK(launched());
-      BCK(cudaMemsetAsync(bt->ctl, 0, 4, s));
       g.insts = round == 0 ? t0 : t1;
       BCK(launch_search(metric, g, grid, s, tq));
     }
     if (N) BCK(launch_batch_write(dq, N, mk_max, s));
-    // the tensor-form instances, each a whole round with its device fallback
-    // on a branch; their error words fold into the batch's
-    if (tcv.empty()) return RBC_OK;
-    BTRY(fork());
-    for (BatchInstance *ip : tcv)
-      BTRY(tc_enqueue(ip->idx, *ip->tc, ip->Q, ip->m, ip->ldq, ip->ids, ip->dists, ip->ldo, true, bt->ctl + 2,
-                      nullptr, lane_of(ip->idx)));
-    return join();
+    // the tensor-form instances; their error words fold into the batch's
+    return capture_tc(tx, metric, bt->ctl, s);
   };
   rc = capture();
   cudaGraph_t graph = nullptr;

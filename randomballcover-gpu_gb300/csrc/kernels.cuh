@@ -82,6 +82,31 @@ struct ErrWords {
   const uint32_t *w[4];
 };
 cudaError_t launch_fold_errors(ErrWords src, uint32_t *dst, cudaStream_t s);
+// Each entry's words folded into *dst (one launch for n entries).
+cudaError_t launch_fold_errors_batch(const ErrWords *tab, uint32_t n, uint32_t *dst, cudaStream_t s);
+// One instance of a batched device fallback (rbc_batch): the *count queries
+// listed first in rows[] searched again over all n database rows.
+struct ListedArgs {
+  float *res_d;         // m x kw per-query lists, thresholds and locks (reset first)
+  uint32_t *res_i, *tau, *lock;
+  uint64_t m;
+  uint32_t kw;
+  uint32_t *ctl;        // 16 control words, zeroed by the reset: [1] items, [2] error
+  SearchItem *items;    // (row chunk, tile of listed queries) items, at most cap
+  uint64_t n, cap;
+  uint32_t chunk, qtile;
+  const uint32_t *rows;
+  const uint32_t *count;
+  uint32_t k, ldo;      // results of the listed queries written to ids / dists
+  uint32_t *ids;
+  float *dists;
+};
+// Per instance: the reset (launch_init_results over m x kw entries, control
+// words zeroed), the work items (launch_listed_items) and the results
+// (launch_listed_results), each one launch over the whole table.
+cudaError_t launch_listed_init_batch(const ListedArgs *tab, uint32_t ninst, uint64_t mkw_max, cudaStream_t s);
+cudaError_t launch_listed_items_batch(const ListedArgs *tab, uint32_t ninst, cudaStream_t s);
+cudaError_t launch_listed_results_batch(const ListedArgs *tab, uint32_t ninst, cudaStream_t s);
 
 // Row-matrix utilities.
 cudaError_t launch_pad_rows(const float *src, uint64_t ld_src, float *dst, uint32_t ld_dst,
@@ -201,21 +226,6 @@ struct DenseInst {
 // the padded dimension dp (the maxima size the grid).
 cudaError_t launch_dense_dist_batch(int metric, const DenseInst *tab, uint32_t ninst, uint64_t na_max,
                                     uint64_t nb_max, uint32_t ld, uint32_t dp, cudaStream_t s);
-// One instance of a batched plan round (rbc_batch): its plan arguments
-// (list_cnt and phase are set per step) and its plan buffers.
-struct BatchPlan {
-  PlanArgs a;
-  uint32_t *cnt, *start, *cursor, *tcnt, *tstart;  // nr + 1 each
-  uint32_t qtile, max_rows;
-  SearchItem *items;
-  uint64_t cap;
-  uint32_t *nitems, *err;
-};
-// A whole plan round (count, scan, fill, tiles per list, scan, items) of
-// every instance in the device table, each step one launch over all of them;
-// the maxima size the grids (blocks past an instance's sizes return).
-cudaError_t launch_plan_batch(const BatchPlan *tab, uint32_t ninst, uint32_t mode, uint32_t nr_max, uint64_t m_max,
-                              uint32_t P_max, cudaStream_t s);
 // Which lists of a plan get work items: rows_lo <= rows < rows_hi and
 // cnt_lo <= planned queries < cnt_hi.
 // Of each selected list, only rows [skip, skip + take) (list-relative) get
@@ -225,6 +235,22 @@ struct ListFilter {
   uint32_t cnt_lo = 0, cnt_hi = UINT32_MAX;
   uint64_t skip = 0, take = UINT64_MAX;
 };
+// One instance of a batched plan round (rbc_batch): its plan arguments
+// (list_cnt and phase are set per step) and its plan buffers.
+struct BatchPlan {
+  PlanArgs a;
+  uint32_t *cnt, *start, *cursor, *tcnt, *tstart;  // nr + 1 each
+  uint32_t qtile, max_rows;
+  ListFilter f;  // the lists (and rows of them) that get work items
+  SearchItem *items;
+  uint64_t cap;
+  uint32_t *nitems, *err;
+};
+// A whole plan round (count, scan, fill, tiles per list, scan, items) of
+// every instance in the device table, each step one launch over all of them;
+// the maxima size the grids (blocks past an instance's sizes return).
+cudaError_t launch_plan_batch(const BatchPlan *tab, uint32_t ninst, uint32_t mode, uint32_t nr_max, uint64_t m_max,
+                              uint32_t P_max, cudaStream_t s);
 // Items per list: query tiles x chunks of at most max_rows list rows, for
 // the lists the filter selects only.
 cudaError_t launch_tiles_per_list(const uint32_t *list_cnt, const uint64_t *offsets, uint32_t nr,

@@ -344,7 +344,7 @@ __global__ void batch_scan_kernel(const BatchPlan *tab, uint32_t which) {
 
 __global__ void batch_tiles_kernel(const BatchPlan *tab) {
   const BatchPlan &bp = tab[blockIdx.z];
-  tiles_per_list(bp.cnt, bp.a.offsets, bp.a.nr, bp.qtile, bp.max_rows, ListFilter(), bp.tcnt,
+  tiles_per_list(bp.cnt, bp.a.offsets, bp.a.nr, bp.qtile, bp.max_rows, bp.f, bp.tcnt,
                  blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -352,7 +352,7 @@ __global__ void batch_items_kernel(const BatchPlan *tab) {
   const BatchPlan &bp = tab[blockIdx.z];
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r > bp.a.nr) return;
-  plan_items(bp.cnt, bp.start, bp.tstart, bp.a.offsets, bp.a.nr, bp.qtile, bp.max_rows, ListFilter(), bp.items,
+  plan_items(bp.cnt, bp.start, bp.tstart, bp.a.offsets, bp.a.nr, bp.qtile, bp.max_rows, bp.f, bp.items,
              bp.cap, bp.nitems, bp.err, r);
 }
 

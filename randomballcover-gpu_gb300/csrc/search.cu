@@ -440,10 +440,103 @@ __global__ void fold_errors_kernel(ErrWords src, uint32_t *dst) {
   if (v) atomicMax(dst, v);
 }
 
+// ---------------------------------------------------------------- batched device fallback (rbc_batch)
+// Instance blockIdx.y of the table.  Empty kw-wide lists and open thresholds
+// for every query, control words zeroed.
+__global__ void listed_init_batch_kernel(const ListedArgs *__restrict__ tab) {
+  const ListedArgs &a = tab[blockIdx.y];
+  if (blockIdx.x == 0 && threadIdx.x < 16) a.ctl[threadIdx.x] = 0;
+  const uint64_t total = a.m * a.kw;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    a.res_d[i] = FLT_MAX;
+    a.res_i[i] = RBC_DUMMY;
+    if (i % a.kw == 0) {
+      a.tau[i / a.kw] = fbits(FLT_MAX);
+      a.lock[i / a.kw] = 0;
+    }
+  }
+}
+
+// The work items of the search over every row for the instance's listed
+// queries (as listed_items_kernel), grid-stride: the count is usually small.
+__global__ void listed_items_batch_kernel(const ListedArgs *__restrict__ tab) {
+  const ListedArgs &a = tab[blockIdx.y];
+  const uint32_t c = *a.count;
+  const uint64_t nchunks = (a.n + a.chunk - 1) / a.chunk, ntile = (c + (uint64_t)a.qtile - 1) / a.qtile;
+  const uint64_t total = nchunks * ntile;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.ctl[1] = total <= a.cap ? (uint32_t)total : 0u;
+    if (total > a.cap) atomicMax(a.ctl + 2, (uint32_t)RBC_ERR_NOMEM);
+  }
+  if (total > a.cap) return;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t ch = i / ntile, t = i - ch * ntile;
+    SearchItem it;
+    it.p0 = ch * a.chunk;
+    it.np = (uint32_t)min((uint64_t)a.chunk, a.n - ch * a.chunk);
+    it.list = RBC_DUMMY;
+    it.q0 = (uint32_t)(t * a.qtile);
+    it.nq = (uint32_t)min((uint64_t)a.qtile, (uint64_t)c - t * a.qtile);
+    it.inst = 0;
+    it.pad = 0;
+    a.items[i] = it;
+  }
+}
+
+// The listed queries' results written over the instance's outputs.
+__global__ void listed_results_batch_kernel(const ListedArgs *__restrict__ tab) {
+  const ListedArgs &a = tab[blockIdx.y];
+  const uint64_t total = min((uint64_t)*a.count, a.m) * a.k;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = i / a.k;
+    const uint32_t j = (uint32_t)(i - r * a.k), q = a.rows[r];
+    if (a.ids) a.ids[(uint64_t)q * a.ldo + j] = a.res_i[(uint64_t)q * a.kw + j];
+    if (a.dists) a.dists[(uint64_t)q * a.ldo + j] = a.res_d[(uint64_t)q * a.kw + j];
+  }
+}
+
+// One thread per table entry: its error words folded into *dst.
+__global__ void fold_errors_batch_kernel(const ErrWords *__restrict__ tab, uint32_t n, uint32_t *dst) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  uint32_t v = 0;
+  for (int i = 0; i < 4; i++)
+    if (tab[e].w[i]) v = max(v, *tab[e].w[i]);
+  if (v) atomicMax(dst, v);
+}
+
 }  // namespace
 
 cudaError_t launch_fold_errors(ErrWords src, uint32_t *dst, cudaStream_t s) {
   fold_errors_kernel<<<1, 1, 0, s>>>(src, dst);
+  return launched();
+}
+
+cudaError_t launch_fold_errors_batch(const ErrWords *tab, uint32_t n, uint32_t *dst, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  fold_errors_batch_kernel<<<(n + 127) / 128, 128, 0, s>>>(tab, n, dst);
+  return launched();
+}
+
+cudaError_t launch_listed_init_batch(const ListedArgs *tab, uint32_t ninst, uint64_t mkw_max, cudaStream_t s) {
+  if (ninst == 0 || mkw_max == 0) return cudaSuccess;
+  const unsigned grid = (unsigned)std::min<uint64_t>((mkw_max + 255) / 256, 512);
+  listed_init_batch_kernel<<<dim3(grid, ninst), 256, 0, s>>>(tab);
+  return launched();
+}
+
+cudaError_t launch_listed_items_batch(const ListedArgs *tab, uint32_t ninst, cudaStream_t s) {
+  if (ninst == 0) return cudaSuccess;
+  listed_items_batch_kernel<<<dim3(8, ninst), 256, 0, s>>>(tab);
+  return launched();
+}
+
+cudaError_t launch_listed_results_batch(const ListedArgs *tab, uint32_t ninst, cudaStream_t s) {
+  if (ninst == 0) return cudaSuccess;
+  listed_results_batch_kernel<<<dim3(8, ninst), 256, 0, s>>>(tab);
   return launched();
 }
 

@@ -132,6 +132,14 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
+// A tensor map in global memory written by the host (a copy before the
+// launch): acquire its 128 bytes for the tensor-map proxy before a TMA
+// instruction reads it.
+__device__ __forceinline__ void fence_tensormap_acquire(const CUtensorMap *map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
+               : "memory");
+}
+
 // ---------------------------------------------------------------- tcgen05
 // Allocation is done by one full warp; the column address lands in smem.
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {

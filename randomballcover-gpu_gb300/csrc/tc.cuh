@@ -218,4 +218,68 @@ cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, con
                              cudaStream_t s, bool narrow = false);
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s);
 
+// ---------------------------------------------------------------- batched tensor queries (rbc_batch)
+// One instance of a batched tensor search: its tensor maps, its arguments
+// (stage fields from tc_stage_plan) and its CTA range in the batched grid.
+// (CUtensorMap's own alignment keeps every map of a table on the boundary
+// TMA needs.)
+struct TcBatchEntry {
+  CUtensorMap tmA, tmB;
+  TcArgs a;
+  uint32_t cta0, ctas;
+};
+// The shared-memory stage plan launch_tc_search takes for a's kb, sl and
+// format (narrow: one query tile per B tile): fills a's stage fields and
+// returns the dynamic shared-memory bytes (0 when nothing fits).
+size_t tc_stage_plan(TcArgs &a, bool narrow);
+// Every instance of the table (ascending cta0, one format and width) in one
+// launch of total_ctas CTAs, each with smem bytes of dynamic shared memory
+// (the largest of the instances' plans).
+cudaError_t launch_tc_search_batch(const TcBatchEntry *tab, uint32_t ninst, uint32_t total_ctas, uint32_t format,
+                                   bool narrow, size_t smem, cudaStream_t s);
+// Everything a tensor query sets up before its probe round, per instance:
+// the nearest representatives and the probe table (as launch_rep_seed), the
+// operand rows (launch_tc_queries), empty shortlists (launch_sl_init), empty
+// kw-wide FP32 lists with open thresholds (launch_init_results), candidate
+// drop bounds at 0x7F7F7F7F, and zeroed control words and counters.
+struct TcPrepArgs {
+  const float *Dqr;
+  uint64_t m;
+  uint32_t nr, sl, P;
+  const uint32_t *rep_rows;
+  float *seed_a;
+  uint32_t *seed_row, *probe;
+  float *probed;
+  const float *Qp;
+  uint32_t ld, d, kp, format;
+  const float *mu;
+  uint16_t *Qh;
+  float *qscale, *qnorm;
+  uint8_t *qinex;
+  float *sl_a;
+  uint32_t *sl_row, *sl_sel, *sl_theta, *sl_lock, *emax, *drop;
+  float *res_d;
+  uint32_t *res_i, *tau, *lock;
+  uint32_t kw;
+  uint32_t *ctl[4];  // 16 words each (nullptr: none)
+  unsigned long long *stats;  // 4 counters
+};
+cudaError_t launch_tc_prep_batch(const TcPrepArgs *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s);
+// The arguments of launch_sl_seed, one instance.
+struct SlSeedArgs {
+  const float *res_d;
+  const uint32_t *res_i;
+  uint32_t kw;
+  const uint32_t *iperm;
+  const float *seed_a;
+  const uint32_t *seed_row;
+  uint64_t m;
+  uint32_t sl, k;
+  float *sl_a;
+  uint32_t *sl_row, *theta, *tau;
+};
+cudaError_t launch_sl_seed_batch(const SlSeedArgs *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s);
+// launch_rerank over every instance of the table (instances with m = 0 do nothing).
+cudaError_t launch_rerank_batch(int metric, const RerankArgs *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s);
+
 }  // namespace rbc

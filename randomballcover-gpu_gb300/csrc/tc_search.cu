@@ -336,9 +336,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 
 template <int MT, bool SPLIT>
-__global__ void __launch_bounds__(kThreads, 1)
-    tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                     const __grid_constant__ TcArgs a) {
+__device__ __forceinline__ void tc_search_body(const CUtensorMap *pA, const CUtensorMap *pB, const TcArgs &a,
+                                               const uint32_t cta, const uint32_t ncta) {
   constexpr uint32_t ACC = SPLIT ? 2 : 1;     // accumulators per query tile: hi.hi (+ corrections)
   constexpr uint32_t NSLOT = 4 / (MT * ACC);  // split format: tensor-memory slots of MT x ACC x 128 columns
   // BF16 format: w is folded into the product.  Each B stage carries the
@@ -432,12 +431,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     // ------------------------------------------------ TMA producer of the B tiles
     if (lane == 0) {
-      prefetch_tensormap(&tmB);
+      prefetch_tensormap(pB);
       uint32_t bi = 0;
       unsigned long long pairs = 0, lists = 0, t_wait = 0;
       const long long t_all = tclk();
       bool ok = true;
-      for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+      for (uint32_t it = cta; it < nitems && ok; it += ncta) {
         const SearchItem item = a.items[it];
         const uint32_t ntiles = (item.np + kBN - 1) / kBN;
         pairs += (unsigned long long)item.nq * item.np;
@@ -450,7 +449,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           mbar_expect_tx(&bar_b_full[sb], b_stage);
           const int32_t row = (int32_t)(item.p0 + (uint64_t)t * kBN);
           for (uint32_t k = 0; k < kbh; k++)
-            tma_load_2d(sB + sb * b_stage + k * kTile16K, &tmB, (int32_t)(k * 64), row, &bar_b_full[sb]);
+            tma_load_2d(sB + sb * b_stage + k * kTile16K, pB, (int32_t)(k * 64), row, &bar_b_full[sb]);
           if (FOLD) bulk_load(sB + sb * b_stage + b_bytes, a.wh + 2 * (uint64_t)row, kWTile, &bar_b_full[sb]);
         }
       }
@@ -464,9 +463,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         atomicAdd(a.stats + 1, lists);
       }
       if (a.trace) {
-        a.trace[blockIdx.x * kTcTraceWords + 6] = t_wait;
-        a.trace[blockIdx.x * kTcTraceWords + 7] = tclk() - t_all;
-        a.trace[blockIdx.x * kTcTraceWords + 15] = bi;
+        a.trace[cta * kTcTraceWords + 6] = t_wait;
+        a.trace[cta * kTcTraceWords + 7] = tclk() - t_all;
+        a.trace[cta * kTcTraceWords + 15] = bi;
       }
     }
   } else if (warp == 1 || (FOLD && MT == 2 && warp == 2)) {
@@ -496,15 +495,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       auto wait = [&](uint64_t *bar, uint32_t parity) {
         const bool r = __all_sync(0xffffffffu, mbar_wait(bar, parity, a.err)) != 0;
         if (!r && a.trace && lane == 0)
-          a.trace[(size_t)gridDim.x * kTcTraceWords + 6 * kTcTraceEvents + blockIdx.x * 4 + g] =
+          a.trace[(size_t)ncta * kTcTraceWords + 6 * kTcTraceEvents + cta * 4 + g] =
               (1ull << 63) | ((unsigned long long)site << 56) | ((unsigned long long)ai << 32) | (bi << 1) | parity;
         return r;
       };
       // ring positions and phase parities kept as counters (no runtime divisions in the loop)
       uint32_t sa = 0, aph = 0, sb = 0, bph = 0;
       bool ok = true;
-      long long *ev = (a.trace && blockIdx.x == 0)
-                          ? reinterpret_cast<long long *>(a.trace + (size_t)gridDim.x * kTcTraceWords)
+      long long *ev = (a.trace && cta == 0)
+                          ? reinterpret_cast<long long *>(a.trace + (size_t)ncta * kTcTraceWords)
                           : nullptr;
       // cycles (warp 1): [0] all, [1] waiting for the query tile, [2] for the
       // previous item's MMAs, [3] for B tiles, [4] for accumulator blocks; [5] MMAs
@@ -513,7 +512,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       auto clk = [&]() -> long long { return tracing ? clock64() : 0ll; };
       const long long t_all = clk();
       long long t0;
-      for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x, ai++) {
+      for (uint32_t it = cta; it < n_items && ok; it += ncta, ai++) {
         const uint32_t ntiles = __shfl_sync(0xffffffffu, (a.items[it].np + kBN - 1) / kBN, 0);
         t0 = clk();
         site = 1;
@@ -582,7 +581,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       tr[0] = clk() - t_all;
       if (a.trace && g == 0 && lane == 0)
-        for (int j = 0; j < 6; j++) a.trace[blockIdx.x * kTcTraceWords + j] = tr[j];
+        for (int j = 0; j < 6; j++) a.trace[cta * kTcTraceWords + j] = tr[j];
     } else {
       // split format: one query tile, A from shared memory; per B tile three
       // MMAs per K step (hi.hi into the first accumulator, hi.lo + lo.hi
@@ -597,7 +596,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t bi = 0, sa = 0, aph = 0, sb = 0, bph = 0, slot = 0, sph = 0;
       const uint32_t lo = (kb * kTile16K) >> 4;  // the lo halves, in descriptor units
       bool ok = true;
-      for (uint32_t it = blockIdx.x; it < n_items && ok; it += gridDim.x) {
+      for (uint32_t it = cta; it < n_items && ok; it += ncta) {
         const uint32_t ntiles = __shfl_sync(0xffffffffu, (a.items[it].np + kBN - 1) / kBN, 0);
         if (!(ok = wait(&bar_a_full[sa], aph))) break;
         const uint64_t ad0 = sw128_desc(smem_u32(sA + sa * a_stage));
@@ -641,7 +640,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ------------------------------------------------ row constants of each B tile (split format)
     uint32_t bi = 0;
     bool ok = true;
-    for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+    for (uint32_t it = cta; it < nitems && ok; it += ncta) {
       const SearchItem item = a.items[it];
       const uint32_t ntiles = (item.np + kBN - 1) / kBN;
       for (uint32_t t = 0; t < ntiles; t++, bi++) {
@@ -663,12 +662,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     cp_async_wait_all();
   } else if (warp == 3) {
     // ------------------------------------------------ per item: row states and the query tile gather
-    if (lane == 0) prefetch_tensormap(&tmA);
+    if (lane == 0) prefetch_tensormap(pA);
     uint32_t ai = 0;
     bool ok = true;
     unsigned long long w3[2] = {0, 0};  // cycles waiting for a row-state slot, for the query stage
     const long long t_all = tclk();
-    for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
+    for (uint32_t it = cta; it < nitems && ok; it += ncta, ai++) {
       const SearchItem item = a.items[it];
       const uint32_t slot = ai & 1, sa = ai % AS;
       // The query tiles' gather goes out first: it needs only the query rows
@@ -699,7 +698,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int g = 0; g < MT; g++)
           for (uint32_t k = 0; k < kbh; k++)
-            tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, &tmA, (int32_t)(k * 64), rr[g][0], rr[g][1],
+            tma_gather4(dA + g * a_tile + k * kTile16K + lane * 512, pA, (int32_t)(k * 64), rr[g][0], rr[g][1],
                         rr[g][2], rr[g][3], &bar_a_full[sa]);
       }
 #pragma unroll
@@ -746,9 +745,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (lane == 0) mbar_arrive(&bar_r_full[slot]);
     }
     if (lane == 0 && a.trace) {
-      a.trace[blockIdx.x * kTcTraceWords + 8] = w3[0];
-      a.trace[blockIdx.x * kTcTraceWords + 9] = w3[1];
-      a.trace[blockIdx.x * kTcTraceWords + 10] = tclk() - t_all;
+      a.trace[cta * kTcTraceWords + 8] = w3[0];
+      a.trace[cta * kTcTraceWords + 9] = w3[1];
+      a.trace[cta * kTcTraceWords + 10] = tclk() - t_all;
     }
     if (lane == 0) {
       // drain: wait (bounded) for the gathers still in flight before leaving
@@ -831,7 +830,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       ep[2] += tclk() - tf;
     };
-    for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x, ai++) {
+    for (uint32_t it = cta; it < nitems && ok; it += ncta, ai++) {
       const SearchItem item = a.items[it];
       const uint32_t ntiles = (item.np + kBN - 1) / kBN;
       const uint32_t rslot = ai & 1;
@@ -912,15 +911,15 @@ __global__ void __launch_bounds__(kThreads, 1)
           tw = tclk();
           if (!(ok = mbar_wait(&bar_bf[blk][gq], (kIssuers == 2 ? j >> 1 : j) & 1, a.err))) {
             if (a.trace && lane == 0)
-              a.trace[(size_t)gridDim.x * kTcTraceWords + 6 * kTcTraceEvents + blockIdx.x * 4 + 2 + grp] =
+              a.trace[(size_t)ncta * kTcTraceWords + 6 * kTcTraceEvents + cta * 4 + 2 + grp] =
                   (1ull << 63) | (5ull << 56) | ((unsigned long long)ai << 32) | (bi << 1) | (j & 1);
             break;
           }
           const long long tfull = tclk();
           ep[1] += tfull - tw;
-          const bool logu = a.trace && blockIdx.x == 0 && ew == 0 && lane == 0 && u >= kTcTraceFirst &&
+          const bool logu = a.trace && cta == 0 && ew == 0 && lane == 0 && u >= kTcTraceFirst &&
                             u < kTcTraceFirst + kTcTraceEvents;
-          long long *evu = logu ? reinterpret_cast<long long *>(a.trace + (size_t)gridDim.x * kTcTraceWords) +
+          long long *evu = logu ? reinterpret_cast<long long *>(a.trace + (size_t)ncta * kTcTraceWords) +
                                       (u - kTcTraceFirst)
                                 : nullptr;
           if (evu) evu[2 * kTcTraceEvents] = tfull;
@@ -1016,8 +1015,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (lane == 0) mbar_arrive(&bar_r_empty[rslot]);
     }
     if (a.trace && warp == 4 && lane == 0) {
-      for (int j = 0; j < 3; j++) a.trace[blockIdx.x * kTcTraceWords + 11 + j] = ep[j];
-      a.trace[blockIdx.x * kTcTraceWords + 14] = tclk() - t_all;
+      for (int j = 0; j < 3; j++) a.trace[cta * kTcTraceWords + 11 + j] = ep[j];
+      a.trace[cta * kTcTraceWords + 14] = tclk() - t_all;
     }
   }
   tc_fence_before();
@@ -1026,6 +1025,36 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fence_after();
     tmem_dealloc(tmem, 512);
   }
+}
+
+// One instance: tensor maps and arguments from the launch's parameters.
+template <int MT, bool SPLIT>
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     const __grid_constant__ TcArgs a) {
+  tc_search_body<MT, SPLIT>(&tmA, &tmB, a, blockIdx.x, gridDim.x);
+}
+
+// Many instances in one launch: CTA blockIdx.x works for the instance whose
+// range [cta0, cta0 + ctas) holds it (the table ascends by cta0), on that
+// instance's items with that instance's tensor maps and arguments, which a
+// host copy wrote to global memory before the launch.
+template <int MT, bool SPLIT>
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_search_batch_kernel(const TcBatchEntry *__restrict__ tab, uint32_t ninst) {
+  uint32_t lo = 0, hi = ninst;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (tab[mid].cta0 <= blockIdx.x)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const TcBatchEntry &e = tab[lo];
+  if (blockIdx.x < e.cta0 || blockIdx.x - e.cta0 >= e.ctas) return;
+  fence_tensormap_acquire(&e.tmA);
+  fence_tensormap_acquire(&e.tmB);
+  tc_search_body<MT, SPLIT>(&e.tmA, &e.tmB, e.a, blockIdx.x - e.cta0, e.ctas);
 }
 
 // ------------------------------------------------------------------ build kernels
@@ -1177,12 +1206,11 @@ __global__ void tc_wrows_kernel(const float *__restrict__ w, uint64_t n_pad, uin
 
 // One warp per query row (row m is the zero row): the operand row of q - mu,
 // its scale, ||q - mu|| and whether some value is not exact in BF16.
-__global__ void tc_query_kernel(const float *__restrict__ Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp,
-                                uint32_t format, const float *__restrict__ mu, uint16_t *__restrict__ Qh,
-                                float *__restrict__ qscale, float *__restrict__ qnorm, uint8_t *__restrict__ qinex) {
-  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint32_t lane = threadIdx.x & 31;
-  if (q > m) return;
+__device__ __forceinline__ void tc_query_warp(const float *__restrict__ Q, uint32_t ld, uint64_t m, uint32_t d,
+                                              uint32_t kp, uint32_t format, const float *__restrict__ mu,
+                                              uint16_t *__restrict__ Qh, float *__restrict__ qscale,
+                                              float *__restrict__ qnorm, uint8_t *__restrict__ qinex, uint64_t q,
+                                              uint32_t lane) {
   const uint32_t cols = format == kTcSplit ? 2 * kp : kp;
   uint16_t *dst = Qh + q * cols;
   if (q == m) {
@@ -1224,6 +1252,14 @@ __global__ void tc_query_kernel(const float *__restrict__ Q, uint32_t ld, uint64
   }
 }
 
+__global__ void tc_query_kernel(const float *__restrict__ Q, uint32_t ld, uint64_t m, uint32_t d, uint32_t kp,
+                                uint32_t format, const float *__restrict__ mu, uint16_t *__restrict__ Qh,
+                                float *__restrict__ qscale, float *__restrict__ qnorm, uint8_t *__restrict__ qinex) {
+  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  if (q > m) return;
+  tc_query_warp(Q, ld, m, d, kp, format, mu, Qh, qscale, qnorm, qinex, q, threadIdx.x & 31);
+}
+
 // Both shortlist buffers empty, buffer 0 current, thresholds open, locks free,
 // error bounds zero.
 __global__ void sl_init_kernel(float *sl_a, uint32_t *sl_row, uint32_t *sel, uint32_t *theta, uint32_t *lock,
@@ -1246,13 +1282,16 @@ __global__ void sl_init_kernel(float *sl_a, uint32_t *sl_row, uint32_t *sel, uin
 // Those rows are exact, so they add nothing to the error bound; a probed row
 // left out ranks after the sl-th under (distance, id), hence after every
 // shortlist entry's value, which the certificate already covers.
-__global__ void sl_seed_kernel(const float *__restrict__ res_d, const uint32_t *__restrict__ res_i, uint32_t kw,
-                               const uint32_t *__restrict__ iperm, const float *__restrict__ seed_a,
-                               const uint32_t *__restrict__ seed_row, uint64_t m, uint32_t sl, uint32_t k,
-                               float *__restrict__ sl_a, uint32_t *__restrict__ sl_row, uint32_t *__restrict__ theta,
-                               uint32_t *__restrict__ tau) {
+template <bool BATCH>
+__global__ void sl_seed_kernel(const __grid_constant__ SlSeedArgs a0, const SlSeedArgs *__restrict__ tab) {
+  const SlSeedArgs &a = BATCH ? tab[blockIdx.y] : a0;
   const uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (q >= m) return;
+  if (q >= a.m) return;
+  const float *__restrict__ res_d = a.res_d, *__restrict__ seed_a = a.seed_a;
+  const uint32_t *__restrict__ res_i = a.res_i, *__restrict__ iperm = a.iperm, *__restrict__ seed_row = a.seed_row;
+  const uint32_t kw = a.kw, sl = a.sl, k = a.k;
+  float *__restrict__ sl_a = a.sl_a;
+  uint32_t *__restrict__ sl_row = a.sl_row, *__restrict__ theta = a.theta, *__restrict__ tau = a.tau;
   const float *rd = res_d + q * kw;
   const uint32_t *ri = res_i + q * kw;
   const float *sa = seed_a + q * sl;
@@ -1308,14 +1347,12 @@ __global__ void rep_mask_kernel(const uint32_t *__restrict__ rep_ids, uint32_t n
 // queries (rare) redo the merge over every 32-wide chunk of Dqr.  The first P
 // entries are the query's probed lists (the same (distance, index) order as
 // the plain form's probe table).
-__global__ void rep_seed_kernel(const float *__restrict__ Dqr, uint64_t m, uint32_t nr,
-                                const uint32_t *__restrict__ rep_rows, uint32_t sl, float *__restrict__ seed_a,
-                                uint32_t *__restrict__ seed_row, uint32_t P, uint32_t *__restrict__ probe,
-                                float *__restrict__ probed) {
+__device__ __forceinline__ void rep_seed_warp(const float *__restrict__ Dqr, uint32_t nr,
+                                              const uint32_t *__restrict__ rep_rows, uint32_t sl,
+                                              float *__restrict__ seed_a, uint32_t *__restrict__ seed_row, uint32_t P,
+                                              uint32_t *__restrict__ probe, float *__restrict__ probed, uint64_t q,
+                                              uint32_t lane) {
   constexpr int L = 8;
-  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint32_t lane = threadIdx.x & 31;
-  if (q >= m) return;
   const float *row = Dqr + q * nr;
   float pd[L];
   uint32_t pi[L];
@@ -1382,6 +1419,52 @@ __global__ void rep_seed_kernel(const float *__restrict__ Dqr, uint64_t m, uint3
   }
 }
 
+__global__ void rep_seed_kernel(const float *__restrict__ Dqr, uint64_t m, uint32_t nr,
+                                const uint32_t *__restrict__ rep_rows, uint32_t sl, float *__restrict__ seed_a,
+                                uint32_t *__restrict__ seed_row, uint32_t P, uint32_t *__restrict__ probe,
+                                float *__restrict__ probed) {
+  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  if (q >= m) return;
+  rep_seed_warp(Dqr, nr, rep_rows, sl, seed_a, seed_row, P, probe, probed, q, threadIdx.x & 31);
+}
+
+// Batched set-up of the tensor query (rbc_batch), instance blockIdx.y, one
+// warp per query row (row m: the zero operand row): the nearest
+// representatives and the probe table, the query's operand row, empty
+// shortlists, FP32 probe-round lists and candidate-drop bound; block 0 also
+// zeroes the instance's control words and counters.
+__global__ void tc_prep_batch_kernel(const TcPrepArgs *__restrict__ tab) {
+  const TcPrepArgs &a = tab[blockIdx.y];
+  if (blockIdx.x == 0 && threadIdx.x < 16)
+    for (int c = 0; c < 4; c++)
+      if (a.ctl[c]) a.ctl[c][threadIdx.x] = 0;
+  if (blockIdx.x == 0 && threadIdx.x < 4) a.stats[threadIdx.x] = 0;
+  const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  if (q > a.m) return;
+  tc_query_warp(a.Qp, a.ld, a.m, a.d, a.kp, a.format, a.mu, a.Qh, a.qscale, a.qnorm, a.qinex, q, lane);
+  if (q == a.m) return;
+  rep_seed_warp(a.Dqr, a.nr, a.rep_rows, a.sl, a.seed_a, a.seed_row, a.P, a.probe, a.probed, q, lane);
+  for (uint32_t j = lane; j < a.sl; j += 32)
+    for (uint64_t b = 0; b < 2; b++) {
+      a.sl_a[(b * a.m + q) * a.sl + j] = INFINITY;
+      a.sl_row[(b * a.m + q) * a.sl + j] = RBC_DUMMY;
+    }
+  for (uint32_t j = lane; j < a.kw; j += 32) {
+    a.res_d[q * a.kw + j] = FLT_MAX;
+    a.res_i[q * a.kw + j] = RBC_DUMMY;
+  }
+  if (lane == 0) {
+    a.sl_sel[q] = 0;
+    a.sl_theta[q] = __float_as_uint(FLT_MAX);
+    a.sl_lock[q] = 0;
+    a.emax[q] = 0;
+    a.drop[q] = 0x7F7F7F7Fu;  // a finite float above every distance
+    a.tau[q] = __float_as_uint(FLT_MAX);
+    a.lock[q] = 0;
+  }
+}
+
 // Per query: the planning threshold tau = min(tau, predicted) when a
 // prediction is given (the speculative plan), then the shortlist cap
 // tau (1 + 2^-10) and the shortlist threshold lowered to it.  A row whose
@@ -1410,8 +1493,9 @@ __global__ void iperm_kernel(const uint32_t *__restrict__ perm, uint64_t n, uint
 
 // Exact rerank of each query's shortlist (one warp per query): the k-th exact
 // distance as a pruning threshold, or the results and the certificate.
-template <int METRIC>
-__global__ void rerank_kernel(RerankArgs a) {
+template <int METRIC, bool BATCH>
+__global__ void rerank_kernel(const __grid_constant__ RerankArgs a0, const RerankArgs *__restrict__ tab) {
+  const RerankArgs &a = BATCH ? tab[blockIdx.y] : a0;
   const uint64_t q = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (q >= a.m) return;
@@ -1496,7 +1580,7 @@ size_t smem_bytes(uint32_t kb, uint32_t as, uint32_t bs, uint32_t stage_words, u
 }
 
 template <int MT, bool SPLIT>
-cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s) {
+size_t plan_stages(TcArgs &a) {
   // Shared-memory plan.  BF16 format with two query tiles (the pruned round):
   // its query tiles live in tensor memory, so one query stage suffices, and
   // three B stages with staging areas for half of each warp's lanes measured
@@ -1541,14 +1625,29 @@ cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, 
       a.stage_lanes = lanes;
     }
   }
-  if (!as) return cudaErrorInvalidConfiguration;
+  if (!as) return 0;
   a.a_stages = as;
   a.b_stages = bs;
-  const size_t smem = smem_bytes<MT, SPLIT>(a.kb, as, bs, a.stage_words, a.stage_lanes);
+  return smem_bytes<MT, SPLIT>(a.kb, as, bs, a.stage_words, a.stage_lanes);
+}
+
+template <int MT, bool SPLIT>
+cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s) {
+  const size_t smem = plan_stages<MT, SPLIT>(a);
+  if (!smem) return cudaErrorInvalidConfiguration;
   cudaError_t e =
       cudaFuncSetAttribute(tc_search_kernel<MT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   tc_search_kernel<MT, SPLIT><<<grid, kThreads, smem, s>>>(tmA, tmB, a);
+  return launched();
+}
+
+template <int MT, bool SPLIT>
+cudaError_t launch_tc_batch(const TcBatchEntry *tab, uint32_t ninst, uint32_t ctas, size_t smem, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(tc_search_batch_kernel<MT, SPLIT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  tc_search_batch_kernel<MT, SPLIT><<<ctas, kThreads, smem, s>>>(tab, ninst);
   return launched();
 }
 
@@ -1666,8 +1765,21 @@ cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t k
                            const float *seed_a, const uint32_t *seed_row, uint64_t m, uint32_t sl, uint32_t k,
                            float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, cudaStream_t s) {
   if (m == 0) return cudaSuccess;
-  sl_seed_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(res_d, res_i, kw, iperm, seed_a, seed_row, m, sl, k,
-                                                            sl_a, sl_row, theta, tau);
+  const SlSeedArgs a{res_d, res_i, kw, iperm, seed_a, seed_row, m, sl, k, sl_a, sl_row, theta, tau};
+  sl_seed_kernel<false><<<(unsigned)((m + 127) / 128), 128, 0, s>>>(a, nullptr);
+  return launched();
+}
+
+cudaError_t launch_sl_seed_batch(const SlSeedArgs *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s) {
+  if (ninst == 0 || m_max == 0) return cudaSuccess;
+  sl_seed_kernel<true><<<dim3((unsigned)((m_max + 127) / 128), ninst), 128, 0, s>>>(SlSeedArgs{}, tab);
+  return launched();
+}
+
+cudaError_t launch_tc_prep_batch(const TcPrepArgs *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s) {
+  if (ninst == 0) return cudaSuccess;
+  const uint64_t threads = (m_max + 1) * 32;
+  tc_prep_batch_kernel<<<dim3((unsigned)((threads + 255) / 256), ninst), 256, 0, s>>>(tab);
   return launched();
 }
 
@@ -1766,14 +1878,38 @@ cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, con
   return narrow ? launch_tc<1, false>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
 }
 
+size_t tc_stage_plan(TcArgs &a, bool narrow) {
+  if (a.format == kTcSplit) return plan_stages<1, true>(a);
+  return narrow ? plan_stages<1, false>(a) : plan_stages<2, false>(a);
+}
+
+cudaError_t launch_tc_search_batch(const TcBatchEntry *tab, uint32_t ninst, uint32_t total_ctas, uint32_t format,
+                                   bool narrow, size_t smem, cudaStream_t s) {
+  if (ninst == 0 || total_ctas == 0) return cudaSuccess;
+  if (smem == 0 || smem > kSmemLimit) return cudaErrorInvalidConfiguration;
+  if (format == kTcSplit) return launch_tc_batch<1, true>(tab, ninst, total_ctas, smem, s);
+  return narrow ? launch_tc_batch<1, false>(tab, ninst, total_ctas, smem, s)
+                : launch_tc_batch<2, false>(tab, ninst, total_ctas, smem, s);
+}
+
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s) {
   if (a.m == 0) return cudaSuccess;
   const uint64_t threads = a.m * 32;
   const unsigned grid = (unsigned)((threads + 255) / 256);
   if (metric == RBC_L1)
-    rerank_kernel<RBC_L1><<<grid, 256, 0, s>>>(a);
+    rerank_kernel<RBC_L1, false><<<grid, 256, 0, s>>>(a, nullptr);
   else
-    rerank_kernel<RBC_L2><<<grid, 256, 0, s>>>(a);
+    rerank_kernel<RBC_L2, false><<<grid, 256, 0, s>>>(a, nullptr);
+  return launched();
+}
+
+cudaError_t launch_rerank_batch(int metric, const RerankArgs *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s) {
+  if (ninst == 0 || m_max == 0) return cudaSuccess;
+  const dim3 grid((unsigned)((m_max * 32 + 255) / 256), ninst);
+  if (metric == RBC_L1)
+    rerank_kernel<RBC_L1, true><<<grid, 256, 0, s>>>(RerankArgs{}, tab);
+  else
+    rerank_kernel<RBC_L2, true><<<grid, 256, 0, s>>>(RerankArgs{}, tab);
   return launched();
 }
 

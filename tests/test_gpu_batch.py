@@ -104,6 +104,54 @@ def test_batch_tensor_form_instances(rbc, oracle):
         c[0].close()
 
 
+def test_batch_tensor_rounds_in_few_launches(rbc, oracle):
+    """64 tensor-form instances -- both operand formats, d in {32, 64, 128},
+    k in {1, 10, 32}, probe rounds with FP32 prefixes, without them (the
+    tensor cores take the probed lists whole) and with lists shorter than
+    the prefix -- answered by one graph whose replay launches a few dozen
+    kernels (each step of the query one launch over every instance), not a
+    pipeline per instance.  Exact on the first run and on a replay with new
+    query values."""
+    rng = np.random.default_rng(11)
+    batch = rbc.Batch()
+    cases = []
+    for i in range(64):
+        n = int(np.exp(rng.uniform(np.log(2000), np.log(30000))))
+        d = int(rng.choice([32, 64, 128]))
+        k = int(rng.choice([1, 10, 32]))
+        m = max(2, n // 100)
+        if i % 2:  # integer features: the BF16 format
+            X = rng.integers(0, 30, (n, d)).astype(np.float32)
+            Q = rng.integers(0, 30, (m, d)).astype(np.float32)
+        else:
+            X = clustered(rng, n, d, centers=50)
+            Q = clustered(rng, m, d, centers=50)
+        idx = rbc.Index(X, int(max(32, np.sqrt(n))), seed=i, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+        if i % 3 == 0:
+            idx.set_tc_tuning(2, rbc.TC_PREFIX_NONE)
+        elif i % 3 == 1:
+            idx.set_tc_tuning(4, 64)
+        Qd = torch.from_numpy(Q).cuda()
+        cases.append((idx, X, Qd, k) + batch.add(idx, Qd, k, mode=rbc.QUERY_EXACT_TC))
+    assert {c[0].info()["tc_format"] for c in cases} == {rbc.TC_BF16, rbc.TC_FP16_SPLIT}
+    batch.run()
+    torch.cuda.synchronize()
+    for idx, X, Qd, k, ids, dists in cases:
+        check_exact(ids, dists, X, Qd.cpu().numpy(), k, 0, rbc, oracle)
+    for idx, X, Qd, k, ids, dists in cases:
+        Qd.copy_(Qd[torch.randperm(Qd.shape[0], device=Qd.device)] + 1.0)
+    l0 = rbc.kernel_launches()
+    batch.run()
+    per_replay = rbc.kernel_launches() - l0
+    torch.cuda.synchronize()
+    assert 0 < per_replay <= 64, per_replay
+    for idx, X, Qd, k, ids, dists in cases:
+        check_exact(ids, dists, X, Qd.cpu().numpy(), k, 0, rbc, oracle)
+    batch.close()
+    for c in cases:
+        c[0].close()
+
+
 def test_batch_64_instances_config_shape(rbc, oracle):
     """The batched configuration's shape scaled down: 64 instances, n log-uniform,
     d in {32, 64, 128}, k in {1, 10, 32}, m = n / 100, Gaussian mixtures with
