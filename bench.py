@@ -772,11 +772,14 @@ def run_batch(a):
         if clocks:
             clocks.start()
         l0 = pyrbc.kernel_launches()
+        # an NVTX range around the timed steps (a profiler can keep to it)
+        torch.cuda.nvtx.range_push(f"batch_{f}")
         ev0.record(stream)
         for _ in range(a.steps):
             batch.run()
         ev1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         clk = clocks.stop() if clocks else None
         launches = pyrbc.kernel_launches() - l0
         ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
