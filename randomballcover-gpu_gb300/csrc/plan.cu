@@ -118,6 +118,27 @@ __device__ __forceinline__ float prune_threshold(float dqr, float chi0, float hp
   return a.metric == RBC_L1 ? __fmul_rd(lb, a.omg_rd) : __fmul_rd(__fmul_rd(lb, lb), a.omg_rd);
 }
 
+// A cheaper test that prunes only pairs prune_threshold prunes too, for the
+// bulk of them.  With s = sqrt(tau / (1-g)) (L2; tau / (1-g) for L1) and a
+// margin m = 1 + 2^-16 on every step: lb > s m gives thr > tau, and lb > s m
+// follows from lo > L = min(s m + hpsi, s m (1 + c) + chi0) m, which in turn
+// follows from D(q,r) > L^2 (1+g) m (L2; L (1+g) m for L1).  The margins
+// exceed every rounding of these float evaluations (a few units in 2^-24
+// relative), s is kept at least 1e-18 (L2; 1e-30 for L1) so that lb > s m
+// cannot underflow thr to zero, and tau = FLT_MAX (or NaN, which the full
+// test never prunes against) gives s = +inf: no pair.
+constexpr float kFastMargin = 1.0000152587890625f;  // 1 + 2^-16
+__device__ __forceinline__ float fast_s(float tau, const PlanArgs &a) {
+  if (!(tau < FLT_MAX)) return INFINITY;
+  const float t = __fdiv_ru(tau, a.omg_rd);
+  return fmaxf(a.metric == RBC_L1 ? t : __fsqrt_ru(t), a.metric == RBC_L1 ? 1e-30f : 1e-18f) * kFastMargin;
+}
+// D(q,r) above this value: the pair is pruned (sm = fast_s, lb2 = sm (1 + c) + chi0).
+__device__ __forceinline__ float fast_reject(float sm, float lb2, float hpsi, const PlanArgs &a) {
+  const float L = fminf(sm + hpsi, lb2) * kFastMargin;
+  return (a.metric == RBC_L1 ? L : L * L) * a.opg_ru * kFastMargin;
+}
+
 // Bound on the radius term of list r (see prune_threshold), rounded up.
 __device__ __forceinline__ float psi_bound(float psi, const PlanArgs &a) {
   const float t = __fdiv_ru(psi, a.omg_rd);
@@ -141,7 +162,7 @@ __device__ __forceinline__ PlanArgs plan_args_of(const PlanArgs &a0, const Batch
 // survives; pass 0 counts per list, pass 1 writes the list-major entries.
 template <bool BATCH>
 __global__ void plan_kernel(PlanArgs a0, const BatchPlan *tab, uint32_t phase) {
-  __shared__ float s_tau[kPlanQueries], s_chi0[kPlanQueries];
+  __shared__ float s_tau[kPlanQueries], s_chi0[kPlanQueries], s_sm[kPlanQueries], s_lb2[kPlanQueries];
   const PlanArgs a = plan_args_of<BATCH>(a0, tab, phase);
   const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t q0 = (uint64_t)blockIdx.y * kPlanQueries;
@@ -149,8 +170,13 @@ __global__ void plan_kernel(PlanArgs a0, const BatchPlan *tab, uint32_t phase) {
   const uint64_t q1 = min(a.m, q0 + kPlanQueries);
   // the per-query terms, once per block
   for (uint32_t j = threadIdx.x; j < q1 - q0; j += blockDim.x) {
-    s_tau[j] = __uint_as_float(a.tau[q0 + j]);
-    s_chi0[j] = query_term(a.dq0 ? a.dq0[q0 + j] : a.probed[(q0 + j) * a.P], a);
+    const float tau = __uint_as_float(a.tau[q0 + j]);
+    const float chi0 = query_term(a.dq0 ? a.dq0[q0 + j] : a.probed[(q0 + j) * a.P], a);
+    const float sm = fast_s(tau, a);
+    s_tau[j] = tau;
+    s_chi0[j] = chi0;
+    s_sm[j] = sm;
+    s_lb2[j] = sm * a.opc_ru * kFastMargin + chi0;
   }
   __syncthreads();
   const bool rv = r < a.nr;
@@ -168,7 +194,9 @@ __global__ void plan_kernel(PlanArgs a0, const BatchPlan *tab, uint32_t phase) {
       bool member = false;
       for (uint32_t p = 0; p < a.P_excl; p++) member |= a.probe[q * a.P + p] == r;
       if (member) continue;
-      const float thr = prune_threshold(a.Dqr[q * a.nr + r], s_chi0[q - q0], hpsi, a);
+      const float dqr = a.Dqr[q * a.nr + r];
+      if (dqr > fast_reject(s_sm[q - q0], s_lb2[q - q0], hpsi, a)) continue;  // pruned (by the full bound too)
+      const float thr = prune_threshold(dqr, s_chi0[q - q0], hpsi, a);
       if (thr > s_tau[q - q0]) continue;
       if (sweep == 0) {
         cnt++;

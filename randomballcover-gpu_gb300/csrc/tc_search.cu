@@ -1361,21 +1361,35 @@ __device__ __forceinline__ void rep_seed_warp(const float *__restrict__ Dqr, uin
     pd[j] = INFINITY;
     pi[j] = RBC_DUMMY;
   }
+  // entries lane, lane + 32, ... in turn, read kU at a time so that each
+  // lane keeps several loads in flight (the row is read once, from DRAM)
+  constexpr int kU = 8;
   uint32_t seen = 0;
-  for (uint32_t r = lane; r < nr; r += 32, seen++) {
-    float cv = row[r];
-    uint32_t ci = r;
-    if (!pair_less(cv, ci, pd[L - 1], pi[L - 1])) continue;
+  for (uint32_t r0 = 0; r0 < nr; r0 += 32 * kU) {
+    float v[kU];
 #pragma unroll
-    for (int j = 0; j < L; j++)
-      if (pair_less(cv, ci, pd[j], pi[j])) {
-        const float td = pd[j];
-        const uint32_t ti = pi[j];
-        pd[j] = cv;
-        pi[j] = ci;
-        cv = td;
-        ci = ti;
-      }
+    for (int u = 0; u < kU; u++) {
+      const uint32_t r = r0 + 32 * u + lane;
+      v[u] = r < nr ? __ldg(row + r) : INFINITY;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      float cv = v[u];
+      uint32_t ci = r0 + 32 * u + lane;
+      if (ci >= nr) break;
+      seen++;
+      if (!pair_less(cv, ci, pd[L - 1], pi[L - 1])) continue;
+#pragma unroll
+      for (int j = 0; j < L; j++)
+        if (pair_less(cv, ci, pd[j], pi[j])) {
+          const float td = pd[j];
+          const uint32_t ti = pi[j];
+          pd[j] = cv;
+          pi[j] = ci;
+          cv = td;
+          ci = ti;
+        }
+    }
   }
   float ld[2] = {INFINITY, INFINITY};
   uint32_t li[2] = {RBC_DUMMY, RBC_DUMMY};
