@@ -98,8 +98,9 @@ def parse():
                     help="forms to time; the last one listed is the headline (default: per workload)")
     ap.add_argument("--item-rows", type=int, default=0,
                     help="longest row run of one work item (rbc_set_tuning; 0: the index's default)")
-    ap.add_argument("--tc-tuning", default=None, metavar="PROBES,ROWS",
-                    help="fixed tensor-form knobs instead of timing them (profiling runs)")
+    ap.add_argument("--tc-tuning", default=None, metavar="PROBES,ROWS[,CAP]",
+                    help="fixed tensor-form knobs instead of timing them (profiling runs): probed lists, FP32 "
+                         "prefix rows, and the probe cap (rows; 0 or absent: none)")
     a = ap.parse_args()
     w = dict(WORKLOADS[a.workload])
     for key in ("n", "m", "reps", "train"):
@@ -450,13 +451,16 @@ def run_engine(a):
     def timed(mode, steps, warmup, sample_clocks=False):
         if mode & pyrbc.QUERY_EXACT_TC and k <= 32:
             if a.tc_tuning:
-                idx.set_tc_tuning(*(int(v) for v in a.tc_tuning.split(",")))
+                knobs = [int(v) for v in a.tc_tuning.split(",")]
+                idx.set_tc_tuning(*knobs[:2])
+                idx.set_tc_probe_cap(knobs[2] if len(knobs) > 2 else 0)
             else:
                 idx.autotune_tc(Qtune, k, mode)
             inf = idx.info()
             p_, r_ = idx.tc_tuning()
             tuning[mode] = ["router picks only" if p_ == pyrbc.TC_ROUTER_ONLY else p_,
                             "no FP32 prefix" if r_ == pyrbc.TC_PREFIX_NONE else r_]
+            tuning[mode] += [f"probe cap {inf['tc_probe_cap']} rows"] if inf["tc_probe_cap"] else []
             tuning[mode] += ["plain FP32 search chosen"] if inf["tc_plain"] else []
             if mode & pyrbc.QUERY_ROUTED:
                 tuning[mode].append("router not consulted (the tuner measured the nearest lists alone faster)"

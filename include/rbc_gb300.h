@@ -105,6 +105,7 @@ typedef struct {
                                   calls faster without the router's picks
                                   (the nearest lists alone), and they skip
                                   the router                             */
+  uint64_t tc_probe_cap;       /* rbc_set_tc_probe_cap (0: none)          */
 } rbc_index_info;
 
 typedef struct {               /* work done by the last rbc_query on an index */
@@ -211,11 +212,18 @@ int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, ui
  * search (RBC_QUERY_EXACT with the same routing) and, when that is faster,
  * makes RBC_QUERY_EXACT_TC calls on this index run it (info.tc_plain).
  * rbc_set_tc_tuning selects the tensor form, routed as asked, again; so does
- * attaching a router.  Results never change. */
+ * attaching a router.  Results never change.
+ * rbc_set_tc_probe_cap: the probe round's tensor search takes at most `rows`
+ * rows of each probed list past the FP32 prefix (0: all of them); the rest
+ * of a longer list is searched after the probe round's threshold update, by
+ * the tensor search with two query tiles per B tile.  rbc_autotune_tc tries
+ * 32768, 65536 and 131072 rows with its best probe count and with 8 probes
+ * once the other knobs are chosen, and keeps one when it is faster. */
 #define RBC_TC_ROUTER_ONLY 0xFFu
 #define RBC_TC_PREFIX_NONE 0xFFFFFFFFFFFFFFFFull
 int rbc_set_tc_tuning(rbc_index *index, uint32_t probes, uint64_t probe_rows);
 int rbc_get_tc_tuning(const rbc_index *index, uint32_t *probes, uint64_t *probe_rows);
+int rbc_set_tc_probe_cap(rbc_index *index, uint64_t rows);
 int rbc_autotune_tc(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k, uint32_t mode,
                     void *stream);
 

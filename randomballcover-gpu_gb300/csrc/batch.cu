@@ -133,8 +133,10 @@ struct TcTables {
   std::vector<std::vector<DenseInst>> dgroups;
   std::vector<DenseInst *> ddev;
   TcPrepArgs *prep = nullptr;
-  BatchPlan *plan[3] = {};  // FP32 probe round, tensor probe round, pruned round
-  bool fp_probe = false, tc_probe = false;
+  // FP32 probe round, tensor probe round, pruned round, the rest of capped
+  // probed lists (rbc_set_tc_probe_cap)
+  BatchPlan *plan[4] = {};
+  bool fp_probe = false, tc_probe = false, rest = false;
   SearchArgs *sp = nullptr, *sf = nullptr;  // the FP32 searches: probe round, fallback
   SearchItem **src_p = nullptr, **src_f = nullptr;
   uint32_t **cnt_p = nullptr, **cnt_f = nullptr;
@@ -147,7 +149,7 @@ struct TcTables {
     uint32_t n, ctas, format;
     size_t smem;
   };
-  std::vector<Launch> tc[2];  // probe round (one query tile per B tile), pruned round
+  std::vector<Launch> tc[3];  // probe round (one query tile per B tile), pruned round, capped lists' rest
   RerankArgs *rr[2] = {};
   ListedArgs *listed = nullptr;
   ErrWords *errs = nullptr;
@@ -176,7 +178,8 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
 
   std::vector<BatchQuery> pad(T);
   std::vector<TcPrepArgs> prep(T);
-  std::vector<BatchPlan> plan[3] = {std::vector<BatchPlan>(T), std::vector<BatchPlan>(T), std::vector<BatchPlan>(T)};
+  std::vector<BatchPlan> plan[4] = {std::vector<BatchPlan>(T), std::vector<BatchPlan>(T), std::vector<BatchPlan>(T),
+                                    std::vector<BatchPlan>(T)};
   std::vector<SearchArgs> sp(T), sf(T);
   std::vector<SearchItem *> src_p(T), src_f(T);
   std::vector<uint32_t *> cnt_p(T), cnt_f(T);
@@ -184,10 +187,11 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
   std::vector<RerankArgs> rr[2] = {std::vector<RerankArgs>(T), std::vector<RerankArgs>(T)};
   std::vector<ListedArgs> listed(T);
   std::vector<ErrWords> errs(T);
-  std::vector<TcBatchEntry> ent[2] = {std::vector<TcBatchEntry>(T), std::vector<TcBatchEntry>(T)};
-  std::vector<size_t> smem[2] = {std::vector<size_t>(T), std::vector<size_t>(T)};
+  std::vector<TcBatchEntry> ent[3] = {std::vector<TcBatchEntry>(T), std::vector<TcBatchEntry>(T),
+                                     std::vector<TcBatchEntry>(T)};
+  std::vector<size_t> smem[3] = {std::vector<size_t>(T), std::vector<size_t>(T), std::vector<size_t>(T)};
   std::vector<double> weight(T);
-  std::vector<bool> probes(T);
+  std::vector<bool> probes(T), rests(T);
   uint64_t all_p = 0, all_f = 0;
   for (uint32_t i = 0; i < T; i++) {
     BatchInstance &in = *tcv[i];
@@ -265,11 +269,15 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
     pa.stats = t.stats.as<unsigned long long>();
     prep[i] = pa;
 
-    // the three plan rounds, as tc_enqueue plans them
+    // the plan rounds, as tc_enqueue plans them
     probes[i] = idx->max_list > t.probe_rows;
+    rests[i] = probes[i] && t.probe_cap && idx->max_list > t.probe_rows + t.probe_cap;
     x.fp_probe |= t.probe_rows > 0;
     x.tc_probe |= probes[i];
-    for (int r = 0; r < 3; r++) {
+    x.rest |= rests[i];
+    // plan[0] FP32 probe round, [1] tensor probe round, [2] pruned round,
+    // [3] the rest of capped probed lists (nothing selected without a cap)
+    for (int r = 0; r < 4; r++) {
       BatchPlan bp{};
       bp.qtile = r == 0 ? qtile_p : (r == 1 ? tc_query_tile(kTcSplit) : t.qtile);
       fill_plan_args(idx, b, mq, t.P, bp.qtile, idx->offsets, idx->radius, bp.a);
@@ -287,6 +295,11 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
       if (r == 1) {
         bp.f.rows_lo = t.probe_rows + 1;
         bp.f.skip = t.probe_rows;
+        if (t.probe_cap) bp.f.take = t.probe_cap;
+      }
+      if (r == 3) {
+        bp.f.rows_lo = rests[i] ? t.probe_rows + t.probe_cap + 1 : UINT64_MAX;
+        bp.f.skip = rests[i] ? t.probe_rows + t.probe_cap : 0;
       }
       plan[r][i] = bp;
     }
@@ -371,6 +384,9 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
     e.a = ta;
     smem[1][i] = tc_stage_plan(e.a, false);
     ent[1][i] = e;
+    e.a.stats = ta.stats + 2;  // the capped lists' rest counts with the probe round
+    smem[2][i] = smem[1][i];
+    ent[2][i] = e;
     if (!smem[0][i] || !smem[1][i]) return fail(RBC_ERR_UNSUPPORTED, "rbc_batch_run: no shared-memory plan fits");
     weight[i] = (double)mq * (double)idx->n * (double)ta.kb * (fmt == kTcSplit ? 2.0 : 1.0);
 
@@ -425,7 +441,7 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
   std::vector<void *> &o = bt->owned;
   x.pad = to_dev(pad, o);
   x.prep = to_dev(prep, o);
-  for (int r = 0; r < 3; r++) x.plan[r] = to_dev(plan[r], o);
+  for (int r = 0; r < 4; r++) x.plan[r] = to_dev(plan[r], o);
   x.sp = to_dev(sp, o);
   x.sf = to_dev(sf, o);
   x.src_p = to_dev(src_p, o);
@@ -439,8 +455,8 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
   x.rr[1] = to_dev(rr[1], o);
   x.listed = to_dev(listed, o);
   x.errs = to_dev(errs, o);
-  if (!x.pad || !x.prep || !x.plan[0] || !x.plan[1] || !x.plan[2] || !x.sp || !x.sf || !x.src_p || !x.src_f ||
-      !x.cnt_p || !x.cnt_f || !x.offs || !x.all || !x.seed || !x.rr[0] || !x.rr[1] || !x.listed || !x.errs)
+  if (!x.pad || !x.prep || !x.plan[0] || !x.plan[1] || !x.plan[2] || !x.plan[3] || !x.sp || !x.sf || !x.src_p ||
+      !x.src_f || !x.cnt_p || !x.cnt_f || !x.offs || !x.all || !x.seed || !x.rr[0] || !x.rr[1] || !x.listed || !x.errs)
     return fail(RBC_ERR_NOMEM, "rbc_batch_run: device allocation failed");
   for (const auto &gr : x.dgroups) {
     x.ddev.push_back(to_dev(gr, o));
@@ -450,12 +466,12 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
   // instance a CTA range sized by its share of the work (about two waves in
   // all), the largest first
   const uint32_t sms = (uint32_t)tc_grid();
-  for (int r = 0; r < 2; r++)
+  for (int r = 0; r < 3; r++)
     for (uint32_t fmt : {(uint32_t)kTcExact, (uint32_t)kTcSplit}) {
       std::vector<uint32_t> mem;
       double wsum = 0;
       for (uint32_t i = 0; i < T; i++)
-        if (tcv[i]->idx->tc.format == fmt && (r == 1 || probes[i])) {
+        if (tcv[i]->idx->tc.format == fmt && (r == 0 ? probes[i] : (r == 1 || rests[i]))) {
           mem.push_back(i);
           wsum += weight[i];
         }
@@ -515,6 +531,11 @@ int capture_tc(const TcTables &x, int metric, uint32_t *ctl, cudaStream_t s) {
   if (x.tc_probe) {
     BCK(launch_plan_batch(x.plan[1], T, 0, x.nr_max, x.m_max, x.P_max, s));
     for (const auto &L : x.tc[0]) BCK(launch_tc_search_batch(L.tab, L.n, L.ctas, L.format, true, L.smem, s));
+    BCK(launch_rerank_batch(metric, x.rr[0], T, x.m_max, s));
+  }
+  if (x.rest) {
+    BCK(launch_plan_batch(x.plan[3], T, 0, x.nr_max, x.m_max, x.P_max, s));
+    for (const auto &L : x.tc[2]) BCK(launch_tc_search_batch(L.tab, L.n, L.ctas, L.format, false, L.smem, s));
     BCK(launch_rerank_batch(metric, x.rr[0], T, x.m_max, s));
   }
   BCK(launch_plan_batch(x.plan[2], T, 1, x.nr_max, x.m_max, x.P_max, s));

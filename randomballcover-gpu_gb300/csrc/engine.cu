@@ -46,12 +46,6 @@ namespace {
 
 constexpr uint32_t kDefaultProbes = 1;  // lists searched before planning (the one-shot plan)
 constexpr uint32_t kTcProbes = 4;       // the tensor form: a tighter start for its shortlists
-// The tensor form's probe round searches the first this many rows of every
-// probed list on the FP32 path (whole lists when shorter: few queries share a
-// probed list, and small tensor items are dominated by fixed costs and
-// shortlist merges) and the rest of longer lists on the tensor cores, into
-// shortlists those exact rows already hold.  RBC_TC_PROBE_ROWS overrides it.
-constexpr uint64_t kTcProbeRows = 8192;
 
 void pool_setup() {
   static bool done[64] = {};
@@ -602,6 +596,7 @@ int tc_setup(rbc_index *idx, uint64_t mb, uint32_t k, uint32_t mode, bool graph,
   t.kw = list_width_for(t.sl);
   t.probe_rows = idx->tc_probe_rows == RBC_TC_PREFIX_NONE ? 0 : idx->tc_probe_rows ? idx->tc_probe_rows : kTcProbeRows;
   if (const char *env = std::getenv("RBC_TC_PROBE_ROWS")) t.probe_rows = std::strtoull(env, nullptr, 10);
+  t.probe_cap = idx->tc_probe_cap;
   t.qtile = tc_query_tile(idx->tc.format);
   const uint64_t probe_per_list = mb * t.P / nr;
   t.ptq = search_tq_for(idx->dp, probe_per_list >= 48 ? 4 : (probe_per_list >= 24 ? 2 : 1), t.kw);
@@ -816,10 +811,18 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
   // 128-query tile per B tile (measured faster than two-tile items even for
   // the busiest probed lists), then the k-th exact distance of each
   // shortlist tightens the threshold
+  // a probe cap c (rbc_set_tc_probe_cap): the tensor probe round takes rows
+  // [probe_rows, probe_rows + c) of each probed list; the rest of the longer
+  // lists follows, once the threshold is tight, in a launch of the kernel
+  // with two query tiles per B tile (hub lists hold most probed rows and
+  // hundreds of probing queries: c3, 8 probed lists, 65,536 rows: 370k ->
+  // 376k queries/s)
+  const uint64_t cap = t.probe_cap;
   if (!spec && idx->max_list > t.probe_rows) {
     ListFilter large;  // the rest of the longer lists
     large.rows_lo = t.probe_rows + 1;
     large.skip = t.probe_rows;
+    if (cap) large.take = cap;
     // items twice the index's row run: each query's buffers merge once per
     // item, and the probed lists' few queries leave the launch short of work
     // items anyway (c3: 16,384 / 32,768 / 65,536 / 131,072 rows gave a 5.16 /
@@ -845,6 +848,17 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
     ra.ids = nullptr;
     ra.dists = nullptr;
     CK(launch_rerank(idx->metric, ra, s));
+    if (cap && idx->max_list > t.probe_rows + cap) {
+      ListFilter rest;
+      rest.rows_lo = t.probe_rows + cap + 1;
+      rest.skip = t.probe_rows + cap;
+      TRY(plan_and_search(idx, b, mq, P, k, 0, idx->Xp, idx->perm, idx->offsets, idx->radius, t.sgrid, nullptr, s, 1,
+                          -1, t.qtile, rest));
+      TcArgs tr = ta;
+      tr.stats = ta.stats + 2;
+      CK(launch_tc_search(tmA, idx->tmB, tr, t.grid, s));
+      CK(launch_rerank(idx->metric, ra, s));
+    }
   }
   // pruned round: every other list whose bound survives, on the tensor
   // cores, into the same shortlists; exact rerank and certificate
@@ -1162,6 +1176,7 @@ int rbc_get_info(const rbc_index *idx, rbc_index_info *info) {
   info->tc_plain = idx->tc_plain ? 1u : 0u;
   info->router_picks = idx->router ? idx->router_probes : 0u;
   info->tc_unrouted = idx->tc_unrouted ? 1u : 0u;
+  info->tc_probe_cap = idx->tc_probe_cap;
   return RBC_OK;
 }
 

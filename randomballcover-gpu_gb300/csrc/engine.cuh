@@ -59,10 +59,17 @@ struct QueryBufs {
 // queries the certificate leaves open are searched again on the device (the
 // FP32 search over the whole database, its work list sized by their count on
 // the device) and the error words are folded into err_sink.
+// The tensor form's probe round searches the first this many rows of every
+// probed list on the FP32 path (whole lists when shorter: few queries share a
+// probed list, and small tensor items are dominated by fixed costs and
+// shortlist merges) and the rest of longer lists on the tensor cores, into
+// shortlists those exact rows already hold.  RBC_TC_PROBE_ROWS overrides it.
+constexpr uint64_t kTcProbeRows = 8192;
+
 struct TcQuery {
   bool routed = false, spec = false;
   uint32_t k = 0, Pn = 0, Pnear = 0, P = 0, sl = 0, kw = 0, qtile = 0;
-  uint64_t probe_rows = 0, mb = 0;
+  uint64_t probe_rows = 0, probe_cap = 0, mb = 0;
   int grid = 0, sgrid = 0, ptq = 0, pgrid = 0;
   QueryBufs b;
   DevBuf near, near_d, logits, Qh, qscale, qnorm, qinex, sl_a, sl_row, sl_sel, sl_theta, sl_lock, emax, ctl, failq,
@@ -160,6 +167,7 @@ struct rbc_index {
   // goes to the tensor cores (0: the defaults)
   uint32_t tc_probes = 0;
   uint64_t tc_probe_rows = 0;
+  uint64_t tc_probe_cap = 0;      // rows past the FP32 prefix the tensor probe round takes (0: all)
   bool tc_plain = false;          // the plain FP32 search answers RBC_QUERY_EXACT_TC (it was faster)
   // learned router (rbc_set_router): probes its top router_probes lists
   rbc_router *router = nullptr;

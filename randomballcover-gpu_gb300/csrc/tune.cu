@@ -140,6 +140,12 @@ int rbc_set_tc_tuning(rbc_index *idx, uint32_t probes, uint64_t probe_rows) {
   return RBC_OK;
 }
 
+int rbc_set_tc_probe_cap(rbc_index *idx, uint64_t rows) {
+  if (!idx) return fail(RBC_ERR_INVALID, "rbc_set_tc_probe_cap: NULL index");
+  idx->tc_probe_cap = rows;
+  return RBC_OK;
+}
+
 int rbc_get_tc_tuning(const rbc_index *idx, uint32_t *probes, uint64_t *probe_rows) {
   if (!idx || !probes || !probe_rows) return fail(RBC_ERR_INVALID, "rbc_get_tc_tuning: NULL argument");
   *probes = idx->tc_probes;
@@ -168,6 +174,23 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   uint64_t best_rows = 0;
   int rc = RBC_OK;
   idx->tc_plain = false;
+  idx->tc_probe_cap = 0;
+  // the fastest of three calls after a warm-up one
+  auto time_calls = [&](uint32_t qmode, double &out) -> int {
+    double ms_min = 1e30;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, s);
+      const int r = query_index(idx, dQ, m, ldq, k, qmode, ids.as<uint32_t>(), dists.as<float>(), k, s);
+      if (r != RBC_OK) return r;
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep) ms_min = std::min(ms_min, (double)ms);
+    }
+    out = ms_min;
+    return RBC_OK;
+  };
   // routed calls with router picks also try one and two picks, and the
   // nearest lists without the router (picks = kNoRouter below: the call then
   // skips it); a call that plans with the router's distance head (picks = 0)
@@ -188,19 +211,10 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
       for (uint64_t r : {RBC_TC_PREFIX_NONE, 512ull, 2048ull, 8192ull, 32768ull}) {
         idx->tc_probes = p;
         idx->tc_probe_rows = r;
-        double ms_min = 1e30;
-        for (int rep = 0; rep < 3 && rc == RBC_OK; rep++) {  // the first run warms up
-          cudaEventRecord(e0, s);
-          rc = query_index(idx, dQ, m, ldq, k, mode, ids.as<uint32_t>(), dists.as<float>(), k, s);
-          cudaEventRecord(e1, s);
-          cudaEventSynchronize(e1);
-          float ms = 0;
-          cudaEventElapsedTime(&ms, e0, e1);
-          if (rep) ms_min = std::min(ms_min, (double)ms);
-        }
-        if (rc != RBC_OK) break;
-        if (ms_min < best) {
-          best = ms_min;
+        double ms = 1e30;
+        if ((rc = time_calls(mode, ms)) != RBC_OK) break;
+        if (ms < best) {
+          best = ms;
           best_p = p;
           best_rows = r;
           best_picks = picks;
@@ -212,19 +226,31 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   }
   idx->tc_unrouted = rc == RBC_OK && best_picks == kNoRouter;
   idx->router_probes = rc == RBC_OK && best_picks != kNoRouter ? best_picks : user_picks;
+  // the probe cap, on the chosen knobs and with 8 probes (it pays where hub
+  // lists hold most of the probed rows)
+  uint64_t best_cap = 0;
+  const uint64_t prefix = best_rows == RBC_TC_PREFIX_NONE ? 0 : (best_rows ? best_rows : kTcProbeRows);
+  for (uint32_t p : {best_p, 8u}) {
+    if (rc != RBC_OK || (p == 8u && best_p == 8u)) break;
+    for (uint64_t c : {32768ull, 65536ull, 131072ull}) {
+      if (idx->max_list <= prefix + c) continue;  // the cap would leave every list whole
+      idx->tc_probes = p;
+      idx->tc_probe_rows = best_rows;
+      idx->tc_probe_cap = c;
+      double ms = 1e30;
+      if ((rc = time_calls(mode, ms)) != RBC_OK) break;
+      if (ms < best) {
+        best = ms;
+        best_p = p;
+        best_cap = c;
+      }
+    }
+  }
+  idx->tc_probe_cap = 0;
   // the plain FP32 search on the same lists, same routing: when it is the
   // faster of the two, RBC_QUERY_EXACT_TC calls run it
   double plain = 1e30;
-  for (int rep = 0; rep < 3 && rc == RBC_OK; rep++) {
-    cudaEventRecord(e0, s);
-    rc = query_index(idx, dQ, m, ldq, k, (mode & ~0xFFu) | RBC_QUERY_EXACT, ids.as<uint32_t>(), dists.as<float>(), k,
-                     s);
-    cudaEventRecord(e1, s);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (rep) plain = std::min(plain, (double)ms);
-  }
+  if (rc == RBC_OK) rc = time_calls((mode & ~0xFFu) | RBC_QUERY_EXACT, plain);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   idx->profile = keep_profile;
@@ -232,6 +258,7 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   if (rc != RBC_OK) return rc;
   idx->tc_probes = best_p;
   idx->tc_probe_rows = best_rows;
+  idx->tc_probe_cap = best_cap;
   idx->tc_plain = plain < best;
   return RBC_OK;
 }

@@ -45,7 +45,7 @@ class IndexInfo(C.Structure):
                 ("s", C.c_uint32), ("metric", C.c_int), ("flags", C.c_uint32), ("min_list", C.c_uint64),
                 ("max_list", C.c_uint64), ("device_bytes", C.c_uint64), ("tc_format", C.c_uint32),
                 ("tc_plain", C.c_uint32), ("router_picks", C.c_uint32),
-                ("tc_unrouted", C.c_uint32)]
+                ("tc_unrouted", C.c_uint32), ("tc_probe_cap", C.c_uint64)]
 
 
 class QueryStats(C.Structure):
@@ -87,6 +87,7 @@ SIGNATURES = {
     "rbc_set_tc_tuning": ([_VP, _U32, _U64], _INT),
     "rbc_autotune_tc": ([_VP, _VP, _U64, _U32, _U32, _U32, _VP], _INT),
     "rbc_get_tc_tuning": ([_VP, C.POINTER(_U32), C.POINTER(_U64)], _INT),
+    "rbc_set_tc_probe_cap": ([_VP, _U64], _INT),
     "rbc_router_create": ([_U32, _U32, _U32, _U64, C.POINTER(_VP)], _INT),
     "rbc_router_destroy": ([_VP], _INT),
     "rbc_router_num_params": ([_VP, C.POINTER(_U64)], _INT),
@@ -331,6 +332,10 @@ class Index:
 
     def set_tc_tuning(self, probes=0, probe_rows=0):
         check(lib().rbc_set_tc_tuning(self.h, probes, probe_rows))
+
+    def set_tc_probe_cap(self, rows):
+        """Rows of each probed list the tensor probe round takes (0: all)."""
+        check(lib().rbc_set_tc_probe_cap(self.h, rows))
 
     def tc_tuning(self):
         """(probes, probe_rows) of the tensor form; 0 means the default."""

@@ -107,8 +107,9 @@ def test_batch_tensor_form_instances(rbc, oracle):
 def test_batch_tensor_rounds_in_few_launches(rbc, oracle):
     """64 tensor-form instances -- both operand formats, d in {32, 64, 128},
     k in {1, 10, 32}, probe rounds with FP32 prefixes, without them (the
-    tensor cores take the probed lists whole) and with lists shorter than
-    the prefix -- answered by one graph whose replay launches a few dozen
+    tensor cores take the probed lists whole, some capped: the rest of their
+    longer lists searched after the threshold update) and with lists shorter
+    than the prefix -- answered by one graph whose replay launches a few dozen
     kernels (each step of the query one launch over every instance), not a
     pipeline per instance.  Exact on the first run and on a replay with new
     query values."""
@@ -129,6 +130,8 @@ def test_batch_tensor_rounds_in_few_launches(rbc, oracle):
         idx = rbc.Index(X, int(max(32, np.sqrt(n))), seed=i, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
         if i % 3 == 0:
             idx.set_tc_tuning(2, rbc.TC_PREFIX_NONE)
+            if i % 2 == 0:
+                idx.set_tc_probe_cap(128)  # the rest of longer probed lists in a round of its own
         elif i % 3 == 1:
             idx.set_tc_tuning(4, 64)
         Qd = torch.from_numpy(Q).cuda()

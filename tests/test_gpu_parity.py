@@ -376,6 +376,29 @@ def test_tensor_core_probe_round_busy_lists(rbc, oracle, monkeypatch):
     idx.close()
 
 
+@pytest.mark.parametrize("probe_rows", [0, 300])
+def test_tensor_core_probe_cap(rbc, oracle, probe_rows):
+    """A probe cap: the probe round's tensor search takes the first rows of
+    each longer probed list (past the FP32 prefix), and the rest is searched
+    after the threshold update with two query tiles per B tile; both operand
+    formats, 8 probed lists, caps below and above the list sizes, every answer
+    the oracle's.  A tuning without a cap answers the same."""
+    for kind, k in ((2, 10), (1, 32)):
+        X = rbc.synth(kind, 41, 0, 60000, 64, ncomp=120, sigma_lo=0.05, sigma_hi=0.05)
+        Q = rbc.synth(kind, 41, 1, 1500, 64, ncomp=120, sigma_lo=0.05, sigma_hi=0.05)
+        idx = rbc.Index(X, 100, seed=6, flags=rbc.BUILD_PARTITION | rbc.BUILD_BF16)
+        inf = idx.info()
+        assert inf["max_list"] > probe_rows + 200
+        idx.set_tc_tuning(8, probe_rows if probe_rows else rbc.TC_PREFIX_NONE)
+        ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), k)
+        for cap in (64, 200, inf["max_list"] + 1, 0):
+            idx.set_tc_probe_cap(cap)
+            assert idx.info()["tc_probe_cap"] == cap
+            ids, dists = idx.query(Q, k, mode=rbc.QUERY_EXACT_TC)
+            assert_same(ids, dists, ri, rd, rbc)
+        idx.close()
+
+
 def test_tensor_core_autotune(rbc, oracle):
     """rbc_autotune_tc picks the probe count and the FP32 / tensor split on
     sample queries; answers stay the oracle's whatever it picks."""
@@ -387,6 +410,7 @@ def test_tensor_core_autotune(rbc, oracle):
     idx.autotune_tc(Qt, 10)
     p, r = idx.tc_tuning()
     assert p in (1, 2, 4, 8) and r in (rbc.TC_PREFIX_NONE, 512, 2048, 8192, 32768)
+    assert idx.info()["tc_probe_cap"] in (0, 32768, 65536, 131072)
     ids, dists = idx.query(Q, 10, mode=rbc.QUERY_EXACT_TC)
     ri, rd = oracle.knn(X.cpu().numpy(), Q.cpu().numpy(), 10)
     assert_same(ids, dists, ri, rd, rbc)
