@@ -196,7 +196,7 @@ int rbc_set_tuning(rbc_index *index, int tq, uint32_t item_rows);
 int rbc_autotune(rbc_index *index, const float *dQ, uint64_t m, uint32_t ldq, uint32_t k,
                  const char *cache_path, void *stream);
 /* Tuning of the tensor-core form: nearest lists searched in its probe round
- * (1-8; 0 keeps the default, 4; RBC_TC_ROUTER_ONLY: none in routed calls,
+ * (1-16; 0 keeps the default, 4; RBC_TC_ROUTER_ONLY: none in routed calls,
  * whose probe round then searches the router's picks alone, and one in
  * others) and how many rows of each probed list the FP32 path searches
  * first (whole lists when shorter; the rest of a longer list goes to the

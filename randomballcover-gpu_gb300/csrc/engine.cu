@@ -581,7 +581,7 @@ int tc_setup(rbc_index *idx, uint64_t mb, uint32_t k, uint32_t mode, bool graph,
   t.spec = t.routed && idx->router->r.T && idx->router_probes == 0;
   uint32_t Pn = idx->tc_probes ? idx->tc_probes : kTcProbes;
   if (Pn == RBC_TC_ROUTER_ONLY) Pn = t.routed ? 0 : 1;
-  if (const char *env = std::getenv("RBC_TC_PROBES")) Pn = std::max(1, std::min(8, std::atoi(env)));
+  if (const char *env = std::getenv("RBC_TC_PROBES")) Pn = std::max(1, std::min(16, std::atoi(env)));
   if (t.spec) Pn = 1;  // the nearest representative only: the bound needs its distance
   t.Pn = Pn = std::min(Pn, nr);
   t.Pnear = std::max(Pn, 1u);  // nearest representatives found (the bound needs the first)

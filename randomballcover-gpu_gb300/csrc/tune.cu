@@ -131,8 +131,8 @@ int rbc_autotune(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, uint
 
 int rbc_set_tc_tuning(rbc_index *idx, uint32_t probes, uint64_t probe_rows) {
   if (!idx) return fail(RBC_ERR_INVALID, "rbc_set_tc_tuning: NULL index");
-  if (probes > 8 && probes != RBC_TC_ROUTER_ONLY)
-    return fail(RBC_ERR_INVALID, "rbc_set_tc_tuning: probes must be at most 8 (or RBC_TC_ROUTER_ONLY)");
+  if (probes > 16 && probes != RBC_TC_ROUTER_ONLY)
+    return fail(RBC_ERR_INVALID, "rbc_set_tc_tuning: probes must be at most 16 (or RBC_TC_ROUTER_ONLY)");
   idx->tc_probes = probes;
   idx->tc_probe_rows = probe_rows;
   idx->tc_plain = false;

@@ -423,7 +423,7 @@ def test_tensor_core_autotune(rbc, oracle):
     idx.set_tc_tuning()
     assert idx.tc_tuning() == (0, 0) and idx.info()["tc_plain"] == 0
     with pytest.raises(rbc.RBCError):
-        idx.set_tc_tuning(9, 0)
+        idx.set_tc_tuning(17, 0)
     idx.close()
 
 
