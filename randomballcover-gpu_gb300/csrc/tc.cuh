@@ -213,7 +213,9 @@ cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t k
                            const float *seed_a, const uint32_t *seed_row, uint64_t m, uint32_t sl, uint32_t k,
                            float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, cudaStream_t s);
 // narrow: one 128-query tile per B tile in the BF16 format as well (items
-// planned with query tiles of 128), for item sets whose tiles run sparse.
+// planned with query tiles of 128), for item sets whose tiles run sparse --
+// the probe rounds; in the split format it selects the probe round's variant
+// (16 candidate-buffer entries per lane, which its keep-best mode needs).
 cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcArgs &a, int grid,
                              cudaStream_t s, bool narrow = false);
 cudaError_t launch_rerank(int metric, const RerankArgs &a, cudaStream_t s);

@@ -335,7 +335,7 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t *bar) {
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 
-template <int MT, bool SPLIT>
+template <int MT, bool SPLIT, bool PROBE>
 __device__ __forceinline__ void tc_search_body(const CUtensorMap *pA, const CUtensorMap *pB, const TcArgs &a,
                                                const uint32_t cta, const uint32_t ncta) {
   constexpr uint32_t ACC = SPLIT ? 2 : 1;     // accumulators per query tile: hi.hi (+ corrections)
@@ -348,9 +348,10 @@ __device__ __forceinline__ void tc_search_body(const CUtensorMap *pA, const CUte
   // in the epilogue.  The split format adds w in the epilogue instead.
   constexpr bool FOLD = !SPLIT;
   constexpr uint32_t kIssuers = (FOLD && MT == 2) ? 2 : 1;  // warps issuing MMAs
-  // candidate buffer entries per lane: 16 in the BF16 format's probe round
-  // (its lists meet many more candidates), kLocal otherwise
-  constexpr int LOC = (MT == 1 && !SPLIT) ? 2 * kLocal : kLocal;
+  // candidate buffer entries per lane: 16 in the probe round (its lists meet
+  // many more candidates; in the BF16 format MT = 1 is the probe round's),
+  // kLocal otherwise
+  constexpr int LOC = (MT == 1 && (!SPLIT || PROBE)) ? 2 * kLocal : kLocal;
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar_a_full[kMaxA], bar_a_empty[kMaxA], bar_b_full[kMaxB], bar_b_empty[kMaxB],
       bar_t_full[4], bar_t_empty[4], bar_x_full[4], bar_r_full[2], bar_r_empty[2], bar_q_free[2];
@@ -1028,18 +1029,19 @@ __device__ __forceinline__ void tc_search_body(const CUtensorMap *pA, const CUte
 }
 
 // One instance: tensor maps and arguments from the launch's parameters.
-template <int MT, bool SPLIT>
+// PROBE: the split format's probe-round variant (wider candidate buffers).
+template <int MT, bool SPLIT, bool PROBE>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const __grid_constant__ TcArgs a) {
-  tc_search_body<MT, SPLIT>(&tmA, &tmB, a, blockIdx.x, gridDim.x);
+  tc_search_body<MT, SPLIT, PROBE>(&tmA, &tmB, a, blockIdx.x, gridDim.x);
 }
 
 // Many instances in one launch: CTA blockIdx.x works for the instance whose
 // range [cta0, cta0 + ctas) holds it (the table ascends by cta0), on that
 // instance's items with that instance's tensor maps and arguments, which a
 // host copy wrote to global memory before the launch.
-template <int MT, bool SPLIT>
+template <int MT, bool SPLIT, bool PROBE>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_search_batch_kernel(const TcBatchEntry *__restrict__ tab, uint32_t ninst) {
   uint32_t lo = 0, hi = ninst;
@@ -1054,7 +1056,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (blockIdx.x < e.cta0 || blockIdx.x - e.cta0 >= e.ctas) return;
   fence_tensormap_acquire(&e.tmA);
   fence_tensormap_acquire(&e.tmB);
-  tc_search_body<MT, SPLIT>(&e.tmA, &e.tmB, e.a, blockIdx.x - e.cta0, e.ctas);
+  tc_search_body<MT, SPLIT, PROBE>(&e.tmA, &e.tmB, e.a, blockIdx.x - e.cta0, e.ctas);
 }
 
 // ------------------------------------------------------------------ build kernels
@@ -1645,23 +1647,23 @@ size_t plan_stages(TcArgs &a) {
   return smem_bytes<MT, SPLIT>(a.kb, as, bs, a.stage_words, a.stage_lanes);
 }
 
-template <int MT, bool SPLIT>
+template <int MT, bool SPLIT, bool PROBE = false>
 cudaError_t launch_tc(const CUtensorMap &tmA, const CUtensorMap &tmB, TcArgs a, int grid, cudaStream_t s) {
   const size_t smem = plan_stages<MT, SPLIT>(a);
   if (!smem) return cudaErrorInvalidConfiguration;
-  cudaError_t e =
-      cudaFuncSetAttribute(tc_search_kernel<MT, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(tc_search_kernel<MT, SPLIT, PROBE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  tc_search_kernel<MT, SPLIT><<<grid, kThreads, smem, s>>>(tmA, tmB, a);
+  tc_search_kernel<MT, SPLIT, PROBE><<<grid, kThreads, smem, s>>>(tmA, tmB, a);
   return launched();
 }
 
-template <int MT, bool SPLIT>
+template <int MT, bool SPLIT, bool PROBE = false>
 cudaError_t launch_tc_batch(const TcBatchEntry *tab, uint32_t ninst, uint32_t ctas, size_t smem, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(tc_search_batch_kernel<MT, SPLIT>,
+  cudaError_t e = cudaFuncSetAttribute(tc_search_batch_kernel<MT, SPLIT, PROBE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  tc_search_batch_kernel<MT, SPLIT><<<ctas, kThreads, smem, s>>>(tab, ninst);
+  tc_search_batch_kernel<MT, SPLIT, PROBE><<<ctas, kThreads, smem, s>>>(tab, ninst);
   return launched();
 }
 
@@ -1833,7 +1835,7 @@ cudaError_t launch_tc_traced(const CUtensorMap &tmA, const CUtensorMap &tmB, TcA
   a.trace = buf;
   const int mt = (a.format == kTcSplit || narrow) ? 1 : 2;
   if (a.format == kTcSplit)
-    e = launch_tc<1, true>(tmA, tmB, a, grid, s);
+    e = narrow ? launch_tc<1, true, true>(tmA, tmB, a, grid, s) : launch_tc<1, true>(tmA, tmB, a, grid, s);
   else
     e = narrow ? launch_tc<1, false>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
   if (e != cudaSuccess) return e;
@@ -1888,7 +1890,8 @@ cudaError_t launch_tc_search(const CUtensorMap &tmA, const CUtensorMap &tmB, con
   if (a.format != kTcSplit && !a.wh) return cudaErrorInvalidValue;
   static const bool trace = std::getenv("RBC_TC_TRACE") != nullptr;
   if (trace) return launch_tc_traced(tmA, tmB, a, grid, s, narrow);
-  if (a.format == kTcSplit) return launch_tc<1, true>(tmA, tmB, a, grid, s);
+  if (a.format == kTcSplit)
+    return narrow ? launch_tc<1, true, true>(tmA, tmB, a, grid, s) : launch_tc<1, true>(tmA, tmB, a, grid, s);
   return narrow ? launch_tc<1, false>(tmA, tmB, a, grid, s) : launch_tc<2, false>(tmA, tmB, a, grid, s);
 }
 
@@ -1901,7 +1904,9 @@ cudaError_t launch_tc_search_batch(const TcBatchEntry *tab, uint32_t ninst, uint
                                    bool narrow, size_t smem, cudaStream_t s) {
   if (ninst == 0 || total_ctas == 0) return cudaSuccess;
   if (smem == 0 || smem > kSmemLimit) return cudaErrorInvalidConfiguration;
-  if (format == kTcSplit) return launch_tc_batch<1, true>(tab, ninst, total_ctas, smem, s);
+  if (format == kTcSplit)
+    return narrow ? launch_tc_batch<1, true, true>(tab, ninst, total_ctas, smem, s)
+                  : launch_tc_batch<1, true>(tab, ninst, total_ctas, smem, s);
   return narrow ? launch_tc_batch<1, false>(tab, ninst, total_ctas, smem, s)
                 : launch_tc_batch<2, false>(tab, ninst, total_ctas, smem, s);
 }
