@@ -562,7 +562,7 @@ cudaError_t launch_listed_results(const float *res_d, const uint32_t *res_i, uin
 // when that tile still fits (the autotuner's knob).  Wider lists (kw 64, 128)
 // take TQ <= 2, halved further while the tile would keep two CTAs off an SM.
 int search_tq_for(uint32_t dp, int tq, uint32_t kw) {
-  int t = (tq == 1 || tq == 2 || tq == 4) && (tq == 1 || dp <= 256 / (tq / 2))
+  int t = (tq == 1 || tq == 2 || tq == 4) && (tq == 1 || dp <= 256u / (uint32_t)(tq / 2))
               ? tq
               : (dp <= 128 ? 4 : (dp <= 256 ? 2 : 1));
   if (kw > 32) {
