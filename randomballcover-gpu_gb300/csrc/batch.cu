@@ -339,6 +339,7 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
     sa.sl_row = t.sl_row.as<uint32_t>();
     sa.theta = t.sl_theta.as<uint32_t>();
     sa.tau = b.tau.as<uint32_t>();
+    sa.cap = t.cap ? t.sl_cap.as<uint32_t>() : nullptr;
     seed[i] = sa;
 
     TcArgs ta{};
@@ -365,6 +366,7 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
     ta.sl_row = t.sl_row.as<uint32_t>();
     ta.sl_sel = t.sl_sel.as<uint32_t>();
     ta.sl_theta = t.sl_theta.as<uint32_t>();
+    ta.sl_cap = sa.cap;
     ta.drop = t.drop.as<uint32_t>();
     ta.sl_lock = t.sl_lock.as<uint32_t>();
     ta.emax = t.emax.as<uint32_t>();
@@ -404,6 +406,9 @@ int prepare_tc(rbc_batch *bt, const std::vector<BatchInstance *> &tcv, cudaStrea
     ra.sl_sel = t.sl_sel.as<uint32_t>();
     ra.emax = t.emax.as<uint32_t>();
     ra.drop = t.drop.as<uint32_t>();
+    ra.sl_cap = sa.cap;
+    ra.cap_out = sa.cap;
+    ra.theta = t.sl_theta.as<uint32_t>();
     ra.ldo = in.ldo;
     ra.nfail = t.ctl.as<uint32_t>() + 1;
     ra.fail = t.failq.as<uint32_t>();

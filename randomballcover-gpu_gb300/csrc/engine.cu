@@ -649,7 +649,12 @@ int tc_setup(rbc_index *idx, uint64_t mb, uint32_t k, uint32_t mode, bool graph,
   CK(t.sl_sel.alloc(mb * 4, s));
   CK(t.sl_theta.alloc(mb * 4, s));
   CK(t.sl_lock.alloc(mb * 4, s));
-  if (t.spec) CK(t.sl_cap.alloc(mb * 4, s));
+  // the BF16 format's error bound is small next to 2^-7 tau, so its
+  // certificate passes under the cap; the FP16 hi/lo format's bound can be
+  // larger (RBC_TC_TAU_CAP=0 or 1 overrides)
+  t.cap = idx->tc.format == kTcExact;
+  if (const char *env = std::getenv("RBC_TC_TAU_CAP")) t.cap = std::atoi(env) != 0;
+  CK(t.sl_cap.alloc(mb * 4, s));
   CK(t.drop.alloc(mb * 4, s));
   CK(t.emax.alloc(mb * 4, s));
   CK(t.ctl.alloc(64, s));
@@ -751,7 +756,12 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
   ta.sl_row = t.sl_row.as<uint32_t>();
   ta.sl_sel = t.sl_sel.as<uint32_t>();
   ta.sl_theta = t.sl_theta.as<uint32_t>();
-  ta.sl_cap = spec ? t.sl_cap.as<uint32_t>() : nullptr;
+  // the shortlist cap: from the prediction (speculative plan) or, once the
+  // seed or a rerank knows an exact bound tau on the k-th distance, tau
+  // (1 + 2^-7) -- rows above it cannot reach the top k, and fewer rows then
+  // queue on the shortlists' merges
+  uint32_t *sl_cap = spec || t.cap ? t.sl_cap.as<uint32_t>() : nullptr;
+  ta.sl_cap = sl_cap;
   ta.drop = t.drop.as<uint32_t>();
   ta.keep_k = 0;
   ta.sl_lock = t.sl_lock.as<uint32_t>();
@@ -773,7 +783,9 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
   ra.sl_row = t.sl_row.as<uint32_t>();
   ra.sl_sel = t.sl_sel.as<uint32_t>();
   ra.emax = t.emax.as<uint32_t>();
-  ra.sl_cap = spec ? t.sl_cap.as<uint32_t>() : nullptr;
+  ra.sl_cap = sl_cap;
+  ra.cap_out = t.cap ? sl_cap : nullptr;
+  ra.theta = t.sl_theta.as<uint32_t>();
   ra.drop = t.drop.as<uint32_t>();
   ra.tplan = nullptr;
   ra.ldo = ldo;
@@ -797,7 +809,7 @@ int tc_enqueue(rbc_index *idx, TcQuery &t, const float *dQ, uint64_t mq, uint32_
   }
   CK(launch_sl_seed(b.res_d.as<float>(), b.res_i.as<uint32_t>(), kw, idx->tc.iperm, t.seed_a.as<float>(),
                     t.seed_row.as<uint32_t>(), mq, sl, k, t.sl_a.as<float>(), t.sl_row.as<uint32_t>(),
-                    t.sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), s));
+                    t.sl_theta.as<uint32_t>(), b.tau.as<uint32_t>(), sl_cap, s));
   // the speculative plan: the predicted k-th distance lowers the planning
   // threshold and caps every shortlist (only rows that can still reach the
   // top k pass the tensor search's filter); the certificate then also

@@ -68,6 +68,7 @@ constexpr uint64_t kTcProbeRows = 8192;
 
 struct TcQuery {
   bool routed = false, spec = false;
+  bool cap = false;  // shortlists capped at tau (1 + 2^-7) once the seed or a rerank knows tau
   uint32_t k = 0, Pn = 0, Pnear = 0, P = 0, sl = 0, kw = 0, qtile = 0;
   uint64_t probe_rows = 0, probe_cap = 0, mb = 0;
   int grid = 0, sgrid = 0, ptq = 0, pgrid = 0;

@@ -102,6 +102,8 @@ struct RerankArgs {
   const uint32_t *tplan;  // per query: the threshold the plan pruned with when it was a
                           // prediction (the k-th exact distance must not exceed it)
   uint32_t *tau;         // if set: the k-th exact distance (float bits) -> pruning threshold
+  uint32_t *cap_out;     // with tau (or nullptr): the shortlist cap tau (1 + 2^-7) written here
+  uint32_t *theta;       //   and the shortlist threshold lowered to it
   uint32_t *ids;         // if set (with dists): results and certificate
   float *dists;
   uint32_t ldo;
@@ -209,9 +211,12 @@ cudaError_t launch_rep_seed(const float *Dqr, uint64_t m, uint32_t nr, const uin
 // nearest representatives (seed_a / seed_row, sl per query), each row once;
 // the shortlist threshold becomes the sl-th distance and tau the k-th (float
 // bits).
+// With cap non-null, also the shortlist cap tau (1 + 2^-7) (float bits) and
+// the threshold lowered to it.
 cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *iperm,
                            const float *seed_a, const uint32_t *seed_row, uint64_t m, uint32_t sl, uint32_t k,
-                           float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, cudaStream_t s);
+                           float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, uint32_t *cap,
+                           cudaStream_t s);
 // narrow: one 128-query tile per B tile in the BF16 format as well (items
 // planned with query tiles of 128), for item sets whose tiles run sparse --
 // the probe rounds; in the split format it selects the probe round's variant
@@ -278,7 +283,7 @@ struct SlSeedArgs {
   uint64_t m;
   uint32_t sl, k;
   float *sl_a;
-  uint32_t *sl_row, *theta, *tau;
+  uint32_t *sl_row, *theta, *tau, *cap;
 };
 cudaError_t launch_sl_seed_batch(const SlSeedArgs *tab, uint32_t ninst, uint64_t m_max, cudaStream_t s);
 // launch_rerank over every instance of the table (instances with m = 0 do nothing).

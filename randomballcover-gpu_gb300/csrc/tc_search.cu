@@ -122,6 +122,15 @@ __device__ __forceinline__ float query_cap(const TcArgs &a, uint32_t q) {
   return a.sl_cap ? __uint_as_float(__ldg(a.sl_cap + q)) : FLT_MAX;
 }
 
+// The cap an exact bound t on the final k-th distance puts on a shortlist
+// threshold: t (1 + 2^-7), rounded up (FLT_MAX while t is open).  A row whose
+// approx exceeds it cannot reach the top k while the error bound stays below
+// 2^-7 t; the certificate checks that bound, and the margin keeps it far
+// from failing (at 2^-10, a few c3 queries a call failed it).
+__device__ __forceinline__ float tau_cap(float t) {
+  return t < FLT_MAX ? fminf(__fmul_ru(t, 1.0078125f), FLT_MAX) : FLT_MAX;
+}
+
 // Merge one lane's sorted candidates (nl <= kLocal entries in the owner
 // lane's registers la/li) into query q's global shortlist, with the whole
 // warp: the current
@@ -1293,7 +1302,8 @@ __global__ void sl_seed_kernel(const __grid_constant__ SlSeedArgs a0, const SlSe
   const uint32_t *__restrict__ res_i = a.res_i, *__restrict__ iperm = a.iperm, *__restrict__ seed_row = a.seed_row;
   const uint32_t kw = a.kw, sl = a.sl, k = a.k;
   float *__restrict__ sl_a = a.sl_a;
-  uint32_t *__restrict__ sl_row = a.sl_row, *__restrict__ theta = a.theta, *__restrict__ tau = a.tau;
+  uint32_t *__restrict__ sl_row = a.sl_row, *__restrict__ theta = a.theta, *__restrict__ tau = a.tau,
+                        *__restrict__ cap = a.cap;
   const float *rd = res_d + q * kw;
   const uint32_t *ri = res_i + q * kw;
   const float *sa = seed_a + q * sl;
@@ -1326,8 +1336,15 @@ __global__ void sl_seed_kernel(const __grid_constant__ SlSeedArgs a0, const SlSe
     oa[t] = INFINITY;
     orow[t] = RBC_DUMMY;
   }
-  theta[q] = __float_as_uint(n == sl ? oa[sl - 1] : FLT_MAX);
-  tau[q] = fbits(n >= k ? oa[k - 1] : FLT_MAX);
+  const float kth = n >= k ? oa[k - 1] : FLT_MAX;
+  float th = n == sl ? oa[sl - 1] : FLT_MAX;
+  tau[q] = fbits(kth);
+  if (cap) {
+    const float c = tau_cap(kth);
+    cap[q] = __float_as_uint(c);
+    th = fminf(th, c);
+  }
+  theta[q] = __float_as_uint(th);
 }
 
 // The representatives' list-major rows, and w = +inf there (the tensor
@@ -1555,7 +1572,14 @@ __global__ void rerank_kernel(const __grid_constant__ RerankArgs a0, const Reran
     }
   }
   const float kth = __shfl_sync(0xffffffffu, ld, a.k - 1);
-  if (a.tau && lane == 0) atomicMin(a.tau + q, fbits(kth));
+  if (a.tau && lane == 0) {
+    const float t = fminf(__uint_as_float(atomicMin(a.tau + q, fbits(kth))), kth);
+    if (a.cap_out) {  // the final k-th distance is at most t
+      const float c = tau_cap(t);
+      a.cap_out[q] = __float_as_uint(c);
+      atomicMin(a.theta + q, __float_as_uint(c));
+    }
+  }
   if (!a.ids && !a.dists) return;
   // certificate: every row searched but not in the shortlist has approx >=
   // T = min(cap, drop, a_last) (a_last only when the shortlist is full:
@@ -1779,9 +1803,10 @@ cudaError_t launch_rep_seed(const float *Dqr, uint64_t m, uint32_t nr, const uin
 
 cudaError_t launch_sl_seed(const float *res_d, const uint32_t *res_i, uint32_t kw, const uint32_t *iperm,
                            const float *seed_a, const uint32_t *seed_row, uint64_t m, uint32_t sl, uint32_t k,
-                           float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, cudaStream_t s) {
+                           float *sl_a, uint32_t *sl_row, uint32_t *theta, uint32_t *tau, uint32_t *cap,
+                           cudaStream_t s) {
   if (m == 0) return cudaSuccess;
-  const SlSeedArgs a{res_d, res_i, kw, iperm, seed_a, seed_row, m, sl, k, sl_a, sl_row, theta, tau};
+  const SlSeedArgs a{res_d, res_i, kw, iperm, seed_a, seed_row, m, sl, k, sl_a, sl_row, theta, tau, cap};
   sl_seed_kernel<false><<<(unsigned)((m + 127) / 128), 128, 0, s>>>(a, nullptr);
   return launched();
 }

@@ -230,8 +230,10 @@ int rbc_autotune_tc(rbc_index *idx, const float *dQ, uint64_t m, uint32_t ldq, u
   // lists hold most of the probed rows)
   uint64_t best_cap = 0;
   const uint64_t prefix = best_rows == RBC_TC_PREFIX_NONE ? 0 : (best_rows ? best_rows : kTcProbeRows);
-  for (uint32_t p : {best_p, 8u}) {
-    if (rc != RBC_OK || (p == 8u && best_p == 8u)) break;
+  std::vector<uint32_t> cap_probes = {best_p};
+  if (best_p != 8u) cap_probes.push_back(8u);
+  for (uint32_t p : cap_probes) {
+    if (rc != RBC_OK) break;
     for (uint64_t c : {32768ull, 65536ull, 131072ull}) {
       if (idx->max_list <= prefix + c) continue;  // the cap would leave every list whole
       idx->tc_probes = p;
