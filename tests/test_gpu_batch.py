@@ -155,6 +155,46 @@ def test_batch_tensor_rounds_in_few_launches(rbc, oracle):
         c[0].close()
 
 
+def test_batch_tensor_edge_instances(rbc, oracle):
+    """Tensor-form batch instances at the edges: one query, one index shared by
+    two instances with different k (and probe caps on it), and an index
+    whose tuner chose the plain FP32 search (it joins the FP32 instances);
+    exact on the first run and on a replay."""
+    rng = np.random.default_rng(21)
+    batch = rbc.Batch()
+    cases = []
+
+    def add(idx, X, Q, k):
+        Qd = torch.from_numpy(Q).cuda()
+        cases.append((idx, X, Qd, k) + batch.add(idx, Qd, k, mode=rbc.QUERY_EXACT_TC))
+
+    flags = rbc.BUILD_PARTITION | rbc.BUILD_BF16
+    Xa = rng.integers(0, 20, (12000, 64)).astype(np.float32)
+    a = rbc.Index(Xa, 60, seed=1, flags=flags)
+    a.set_tc_tuning(4, rbc.TC_PREFIX_NONE)
+    a.set_tc_probe_cap(100)
+    add(a, Xa, rng.integers(0, 20, (1, 64)).astype(np.float32), 10)    # one query
+    add(a, Xa, rng.integers(0, 20, (150, 64)).astype(np.float32), 32)  # the same index, k = 32
+    Xb = clustered(rng, 9000, 32, centers=40)
+    b = rbc.Index(Xb, 64, seed=2, flags=flags)
+    add(b, Xb, clustered(rng, 1, 32, centers=40), 1)                   # one query, 1-NN
+    Xc = rbc.synth(0, 3, 0, 20000, 16).cpu().numpy()
+    c = rbc.Index(Xc, 128, seed=3, flags=flags)
+    c.autotune_tc(rbc.synth(0, 3, 3, 2000, 16), 1)
+    add(c, Xc, rbc.synth(0, 3, 1, 300, 16).cpu().numpy(), 1)
+    for rep in range(2):
+        if rep:
+            for idx, X, Qd, k, ids, dists in cases:
+                Qd.copy_(Qd + 1.0)
+        batch.run()
+        torch.cuda.synchronize()
+        for idx, X, Qd, k, ids, dists in cases:
+            check_exact(ids, dists, X, Qd.cpu().numpy(), k, 0, rbc, oracle)
+    batch.close()
+    for idx in (a, b, c):
+        idx.close()
+
+
 def test_batch_64_instances_config_shape(rbc, oracle):
     """The batched configuration's shape scaled down: 64 instances, n log-uniform,
     d in {32, 64, 128}, k in {1, 10, 32}, m = n / 100, Gaussian mixtures with
